@@ -1,0 +1,363 @@
+#!/usr/bin/env python
+"""Benchmark: equilibrium LDM spectra/s on the 5M-line CO2-like workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one spectrum (scatter -> FFT/Voigt reduce -> IFFT) of the 5M-line
+CO2-like list over 2000-2400 cm-1 at 0.001 cm-1 (400 001 points), 8 x 16 LDM
+nodes, T = 1500 K, p = 1 bar, x = 0.1.  ``value``: spectra/s with the line list
+resident in HBM, timed with CUDA events on the launching stream.  ``e2e``: the
+same through the host API (rg_synthesize_host: conditions in, float32
+spectrum copied back to pinned host memory, synchronous), plus the cold path
+(upload from host arrays + plan + spectrum) reported beside it.  N > 1 runs
+independent replicas, one per GPU (the path needs no exchange between GPUs).
+
+``--impl reference`` times the CPU oracle (an FP64 numpy restatement of the
+reference's CPU LDM path; the reference itself needs pandas/astropy/numba and
+its GPU path needs Vulkan, neither of which exists here) on rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "spectra/s and p50/p99 latency at <=1e-4 rel err: served vs plain GPU LDM"
+WORKLOAD = "co2_5M"
+KERNELS_PER_STEP = 5
+STAGES = ["k_scatter", "k_col_fft_fwd", "k_row_fft_voigt", "k_row_ifft", "k_col_ifft"]
+
+
+def workload_desc(n_lines, n_v, grid):
+    return {
+        "workload": (f"CO2-like synthetic list, {n_lines} lines, 2000-2400 cm-1 at 0.001 cm-1 "
+                     f"({n_v} points), {grid[0]}x{grid[1]} LDM nodes, T=1500 K, p=1 bar, x=0.1"),
+        "n_lines": n_lines, "n_v": n_v, "n_ft": grid[2], "ldm_nodes": [grid[0], grid[1]],
+        "l2": "inputs larger than L2 (line list 160 MB, LDM 205 MB, FFT workspace 420 MB)",
+        "parallelism": "replicas",
+    }
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.proc or not self.path:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(n_lines_read, n_nodes, n_v, n_ft, n_pairs):
+    """Bytes each kernel must move once (per launch): the line records, the LDM
+    written once (n_v columns, no zero padding), the packed complex FFT rows,
+    the accumulator and the output."""
+    return {
+        "k_scatter": n_lines_read * 32 + n_nodes * n_v * 4,
+        "k_col_fft_fwd": n_nodes * n_v * 4 + n_pairs * n_ft * 8,
+        "k_row_fft_voigt": n_pairs * n_ft * 8 + n_ft * 8,
+        "k_row_ifft": 2 * n_ft * 8,
+        "k_col_ifft": n_ft * 8 + n_v * 4,
+    }
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    """Per-launch DRAM traffic of the dominant kernel from the committed ncu
+    summary (profiles/*.json), if present."""
+    p = os.path.join(ROOT, "profiles", "traffic_co2_5M.json")
+    if os.path.exists(p):
+        return json.load(open(p))
+    return {}
+
+
+def cpu_baseline_sample(lines, grid, workers, frac=20):
+    """Oracle timing on a bounded sample: the per-line stages (scaling +
+    scatter) on 1/frac of the lines (contiguous block), scaled by frac, plus
+    the full FFT/convolution stage (independent of the line count)."""
+    import numpy as np
+
+    from oracle import ldm_oracle as O
+    n = len(lines["v0"])
+    m = n // frac
+    lo = (n - m) // 2
+    sub = {k: np.asarray(v)[lo:lo + m] for k, v in lines.items()}
+    t0 = time.perf_counter()
+    kpos, lgG, lgL, S = O.line_quantities(sub, 1500.0, 1.0, 0.1, 2000.0, 0.001, molar_mass=44.0)
+    LDM = O.ldm_scatter(kpos, lgG, lgL, S, 400001, grid)
+    t1 = time.perf_counter()
+    O.ldm_convolve(LDM, 400001, 0.001, grid, int(grid_nft(grid)), fft_workers=workers)
+    t2 = time.perf_counter()
+    return (t1 - t0) * (n / m) + (t2 - t1), (t1 - t0), (t2 - t1), m
+
+
+_NFT = {}
+
+
+def grid_nft(grid):
+    return _NFT["n_ft"]
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    from radis_gb300 import _build, _lib as L, synthetic as S
+    _build.build()
+    lines = S.co2_like()
+    n_v = S.grid_points(2000.0, 2400.0, 0.001)
+    g = L.grid_estimate(lines, 44.0, 2000.0, 0.001, n_v, 1500.0, 1.0, 0.1, n_G=8, n_L=16)
+    _NFT["n_ft"] = g.n_ft
+    workers = os.cpu_count() or 1
+    times = []
+    parts = []
+    for i in range(args.warmup + args.steps):
+        t, tl, tc, m = cpu_baseline_sample(lines, g.axes(), workers)
+        if i >= args.warmup:
+            times.append(t)
+            parts.append((tl, tc))
+    step = statistics.mean(times)
+    value = 1.0 / step
+    sample = (f"per step: scaling+scatter of {m} of {len(lines['v0'])} lines (x{len(lines['v0']) / m:.0f}) "
+              f"+ full FFT/Voigt stage ({g.n_G * g.n_L} node rows of {g.n_ft}); numpy/scipy FP64")
+    out = {
+        "metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": workload_desc(len(lines["v0"]), n_v, (g.n_G, g.n_L, g.n_ft)),
+        "cpu_baseline": {"value": value, "unit": "spectra/s", "cores": workers, "kind": "port",
+                         "sample": sample + f"; FFT threads {workers}, add.at single-threaded"},
+        "e2e": {"value": value, "unit": "spectra/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "stage_s": {"lines_scaled": statistics.mean(p[0] for p in parts) * len(lines["v0"]) / m,
+                    "fft_voigt": statistics.mean(p[1] for p in parts)},
+    }
+    print(json.dumps(out))
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from radis_gb300 import _build
+    if rank == 0:
+        _build.build()
+    if ws > 1:
+        dist.barrier()
+    from radis_gb300 import _lib as L, synthetic as S
+
+    T, p, x = 1500.0, 1.0, 0.1
+    vmin, vmax, dv = 2000.0, 2400.0, 0.001
+    n_v = S.grid_points(vmin, vmax, dv)
+    lines = S.co2_like()
+    n_lines = len(lines["v0"])
+    ctx = L.Context(local)
+    t0 = time.perf_counter()
+    ln = L.Lines(ctx, lines, 44.0)
+    plan = L.Plan(ln, vmin, dv, n_v, n_G=8, n_L=16)
+    setup_s = time.perf_counter() - t0
+    g = plan.grid(T, p, x)
+    n_nodes = g.n_G * g.n_L + (g.n_G * g.n_L) % 2
+    stream = torch.cuda.Stream()
+    out = torch.empty(n_v, dtype=torch.float32, device="cuda")
+    sptr = stream.cuda_stream
+
+    for _ in range(max(args.warmup, 3)):
+        plan.synthesize_device(T, p, x, out.data_ptr(), sptr)
+    torch.cuda.synchronize()
+    # lines actually read by the scatter (window + shift margins): all of them here
+    info = plan.synthesize_device(T, p, x, out.data_ptr(), sptr, timing=1)
+    lines_in_window = info.lines_in_window
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+
+    K = args.steps
+    ring_steps = min(K, 200)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        if ws > 1:
+            dist.barrier()
+        e0.record(stream)
+        for i in range(K):
+            plan.synthesize_device(T, p, x, out.data_ptr(), sptr, timing=2 if i < ring_steps else 0)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if ws > 1:
+            dist.barrier()
+    ms = e0.elapsed_time(e1) / K
+    stage_sum, stage_n = plan.stage_times()
+    stage_avg = [s / max(stage_n, 1) for s in stage_sum]
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * 1000.0 / ms
+
+    # e2e through the host API: conditions in, spectrum out to pinned memory
+    host = torch.empty(n_v, dtype=torch.float32, pin_memory=True).numpy()
+    lat = []
+    for i in range(max(args.warmup, 3) + K):
+        t0 = time.perf_counter()
+        plan.synthesize_host(T, p, x, out=host)
+        if i >= max(args.warmup, 3):
+            lat.append(time.perf_counter() - t0)
+    e2e_ms = statistics.mean(lat) * 1e3
+    lat_ms = sorted(v * 1e3 for v in lat)
+    p50 = lat_ms[len(lat_ms) // 2]
+    p99 = lat_ms[min(len(lat_ms) - 1, int(math.ceil(0.99 * len(lat_ms))) - 1)]
+    if ws > 1:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    # cold path: upload from host arrays + plan + one spectrum (eq_spectrum_gpu with exit_gpu)
+    cold = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        ln2 = L.Lines(ctx, lines, 44.0)
+        pl2 = L.Plan(ln2, vmin, dv, n_v, n_G=8, n_L=16)
+        pl2.synthesize_host(T, p, x, out=host)
+        cold.append(time.perf_counter() - t0)
+        pl2.close()
+        ln2.close()
+
+    peak, peak_kind = load_peaks()
+    ab = algorithmic_bytes(lines_in_window, n_nodes, n_v, g.n_ft, n_nodes // 2)
+    dom = max(range(5), key=lambda i: stage_avg[i])
+    name = STAGES[dom]
+    achieved = ab[name] / (stage_avg[dom] * 1e-3) / 1e9
+    traffic = load_traffic().get(name)
+    stages = {STAGES[i]: {"ms": stage_avg[i], "algorithmic_bytes": ab[STAGES[i]],
+                          "GB/s": ab[STAGES[i]] / (stage_avg[i] * 1e-3) / 1e9 if stage_avg[i] else None}
+              for i in range(5)}
+
+    res = None
+    if rank == 0:
+        res = {
+            "metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": ws, "steps": K,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload_desc(n_lines, n_v, (g.n_G, g.n_L, g.n_ft)),
+            "clocks": clk.summary(),
+            "gpu_launches": KERNELS_PER_STEP * K,
+            "e2e": {"value": ws * 1000.0 / e2e_ms, "unit": "spectra/s",
+                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": n_v * 4,
+                    "note": ("resident line list; per step the conditions travel as kernel "
+                             "parameters and the float32 spectrum is copied to pinned host memory")},
+            "e2e_cold": {"value": 1.0 / statistics.mean(cold), "unit": "spectra/s",
+                         "h2d_bytes_per_step": n_lines * (8 + 8 + 4 * 4), "d2h_bytes_per_step": n_v * 4,
+                         "note": "line upload from host arrays + envelopes + plan + one spectrum"},
+            "latency_ms": {"p50": p50, "p99": p99, "of": "host API call, plain per-request"},
+            "roofline": {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                         "traffic": traffic, "algorithmic_bytes_per_launch": ab[name],
+                         "avg_launch_ms": stage_avg[dom]},
+            "stages": stages,
+            "setup_s": setup_s,
+        }
+        if ws == 1 and not args.no_cpu_baseline:
+            _NFT["n_ft"] = g.n_ft
+            workers = os.cpu_count() or 1
+            t, tl, tc, m = cpu_baseline_sample(lines, g.axes(), workers)
+            res["cpu_baseline"] = {
+                "value": 1.0 / t, "unit": "spectra/s", "cores": workers, "kind": "port",
+                "sample": (f"oracle (FP64 numpy restatement of the reference CPU LDM path): scaling+scatter "
+                           f"of {m} of {n_lines} lines scaled x{n_lines / m:.0f} ({tl:.2f} s) + full FFT/Voigt "
+                           f"stage ({tc:.2f} s, scipy.fft workers={workers}); add.at single-threaded")}
+        print(json.dumps(res))
+    plan.close()
+    ln.close()
+    ctx.close()
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,171 @@
+/*
+ * radis_gb300 — C ABI of the GB300 (sm_103a) equilibrium LDM/DIT spectrum
+ * synthesis.  Plain pointers and sizes only; no torch or CUDA-runtime types
+ * in the signatures (streams are passed as `void*` = cudaStream_t).
+ *
+ * The entry points replace the reference's GPU application object
+ * (radis 0.17.1, paths relative to the radis project root):
+ *
+ *   rg_ctx_create / rg_ctx_destroy  <- GPUApplication.__init__ / free
+ *        (radis/gpu/vulkan/vulkan_compute_lib.py:26-73, gpu.py:376-380)
+ *   rg_lines_upload / rg_lines_free <- gpuApp.__init__ line-database upload
+ *        (radis/gpu/gpu.py:127-203; init_G_params/init_L_params params.py:8-81)
+ *   rg_plan_create / rg_plan_free   <- gpuApp.__init__ grid, buffers and
+ *        pre-recorded command list (gpu.py:133-141, 205-284)
+ *   rg_plan_grid                    <- set_pTQ/set_G_params/set_L_params +
+ *        get_griddims (params.py:89-155, gpu.py:372-374)
+ *   rg_synthesize / rg_synthesize_host <- gpuApp.iterate (gpu.py:302-370):
+ *        clear -> FillLDM (cmdFillLDM.comp) -> R2C FFT -> ApplyLineshapes
+ *        (cmdApplyLineshapes.comp) -> C2R IFFT -> D2H
+ *   rg_grid_estimate                <- the same rules on host arrays, no device
+ *   rg_debug_ldm                    <- no reference entry point: reads back the
+ *        LDM tensor so the scatter can be checked on its own
+ *
+ * Every function returns an int status (RG_OK = 0); none aborts.  The text of
+ * the last error on the calling thread is returned by rg_last_error().
+ * A plan is not re-entrant: calls on one plan are serialised by an internal
+ * mutex.  Distinct plans may be used concurrently from different threads.
+ */
+#ifndef RADIS_GB300_H
+#define RADIS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RG_ABI_VERSION 1
+
+enum rg_status {
+    RG_OK = 0,
+    RG_ERR_ARG = 1,        /* invalid argument / size                         */
+    RG_ERR_CUDA = 2,       /* a CUDA runtime call failed                      */
+    RG_ERR_OOM = 3,        /* device or host allocation failed                */
+    RG_ERR_UNSORTED = 4,   /* line positions v0 are not ascending             */
+    RG_ERR_RANGE = 5,      /* grid too large for the kernels' limits          */
+    RG_ERR_TIMEOUT = 6,    /* a bounded device wait gave up                   */
+    RG_ERR_STATE = 7       /* object used after free / wrong context          */
+};
+
+typedef struct rg_ctx rg_ctx;
+typedef struct rg_lines rg_lines;
+typedef struct rg_plan rg_plan;
+
+/* Line list, host arrays of length n (structure of arrays).
+ * Mirrors the columns the reference uploads (gpu.py:190-203): v0 = wav,
+ * da = Pshft, na = Tdpair, gamma_arr = (selbrd, airbrd), El, iso; the
+ * intensity is given as S_ref = HITRAN line intensity at T_ref (the CPU path's
+ * `int` column, base.py:2664) — convert an Einstein-A based S0 with
+ * S_ref = S0 exp(-c2 El/Tref) (1 - exp(-c2 v0/Tref)) / Q(Tref). */
+typedef struct {
+    int64_t n;
+    const double* v0;      /* line centre (cm-1), ascending, required        */
+    const double* s_ref;   /* intensity at T_ref (cm-1/(molecule cm-2))      */
+    const float* e_low;    /* lower-state energy (cm-1)                       */
+    const float* g_air;    /* air-broadened HWHM at T_ref (cm-1/atm)          */
+    const float* g_self;   /* self-broadened HWHM at T_ref (cm-1/atm)         */
+    const float* n_air;    /* temperature exponent of the widths              */
+    const float* delta;    /* pressure shift (cm-1/atm); NULL = no shift      */
+    const uint8_t* iso;    /* isotope slot in [0, n_iso); NULL = all slot 0   */
+} rg_line_arrays;
+
+typedef struct {
+    int n_iso;                 /* 1..16                                       */
+    double molar_mass[16];     /* g/mol per isotope slot                      */
+    double t_ref;              /* reference temperature (K), usually 296      */
+} rg_isotopes;
+
+/* Spectral grid v_k = vmin + k dv, k < n_v, and the LDM node policy:
+ * dxG/dxL > 0  -> node spacing given, node count from the width envelope
+ *                 (the reference's set_G_params/set_L_params, params.py:89-117);
+ * n_G/n_L  > 1 -> node count given, spacing = envelope span / (n - 1).     */
+typedef struct {
+    double vmin;
+    double dv;
+    int64_t n_v;
+    double dxG, dxL;
+    int n_G, n_L;
+    double folding_thresh;     /* <= 0 -> 1e-6 (factory.py:437)              */
+    int64_t n_ft;              /* 0 -> smallest supported length >= 2 n_v     */
+} rg_plan_desc;
+
+/* Gas conditions of one spectrum.  Pressure in bar (as the reference API);
+ * widths and shift use atm = bar / 1.01325 like the CPU path. */
+typedef struct {
+    double T;                  /* K                                           */
+    double p_bar;              /* bar                                         */
+    double x;                  /* mole fraction of the absorber               */
+    const double* q_ratio;     /* [n_iso] Q(T_ref)/Q(T); NULL -> all 1        */
+} rg_conditions;
+
+/* LDM axes chosen for one condition set (log of FWHM in cm-1). */
+typedef struct {
+    double log_wG_min, dxG;
+    double log_wL_min, dxL;
+    int n_G, n_L;
+    int64_t n_ft;              /* FFT length                                   */
+    int64_t n1, n2;            /* FFT factorisation n_ft = n1 * n2             */
+} rg_grid;
+
+typedef struct {
+    rg_grid grid;
+    double log_scale;          /* abscoeff = out * exp(log_scale)              */
+    float stage_ms[6];         /* scatter, fft-col, fft-row+voigt, ifft-row,
+                                  ifft-col, total (filled when timing != 0)    */
+    int64_t lines_in_window;   /* lines whose k0 >= 0 and k0+1 < n_v          */
+} rg_spectrum_info;
+
+int rg_abi_version(void);
+const char* rg_last_error(void);
+
+int rg_ctx_create(int device, rg_ctx** out);
+int rg_ctx_destroy(rg_ctx* ctx);
+
+int rg_lines_upload(rg_ctx* ctx, const rg_line_arrays* lines, const rg_isotopes* iso,
+                    rg_lines** out);
+int rg_lines_free(rg_lines* lines);
+int rg_lines_count(const rg_lines* lines, int64_t* n);
+
+int rg_plan_create(rg_lines* lines, const rg_plan_desc* desc, rg_plan** out);
+int rg_plan_free(rg_plan* plan);
+
+/* Host-only: the node axes and FFT factorisation the plan uses at `cond`. */
+int rg_plan_grid(rg_plan* plan, const rg_conditions* cond, rg_grid* out);
+
+/* Host-only, no device needed: the grid a plan over these host lines would
+ * use at `cond` (the reference's init_*_params + set_*_params + get_griddims,
+ * params.py:8-155, gpu.py:372-374).  Lets a scheduler size the LDM of a
+ * request before any device memory is touched. */
+int rg_grid_estimate(const rg_line_arrays* lines, const rg_isotopes* iso, const rg_plan_desc* desc,
+                     const rg_conditions* cond, rg_grid* out);
+
+/* Enqueue one spectrum on `stream` (NULL = the context's stream).
+ * `out_dev`: device array of n_v floats (abscoeff in cm-1 times
+ * exp(-info.log_scale)).  timing = 0: asynchronous; 1: synchronises the stream
+ * and fills info->stage_ms; 2: asynchronous, records per-stage CUDA events on
+ * `stream` into a ring of 256 spectra read back by rg_plan_stage_times. */
+int rg_synthesize(rg_plan* plan, const rg_conditions* cond, float* out_dev, void* stream,
+                  int timing, rg_spectrum_info* info);
+
+/* Sums (ms) of the stage times recorded with timing = 2 since the last call:
+ * scatter, fft-col, fft-row+voigt, ifft-row, ifft-col, total; *count =
+ * spectra recorded.  Synchronises the recording stream and empties the ring.
+ * (The reference's per-command Vulkan timestamps, gpu.py:260-280, 360.) */
+int rg_plan_stage_times(rg_plan* plan, double* sum_ms, int64_t* count);
+
+/* As rg_synthesize, then copies the n_v floats to `out_host` (pinned or
+ * pageable) and waits for the copy: the drop-in `iterate()` form. */
+int rg_synthesize_host(rg_plan* plan, const rg_conditions* cond, float* out_host,
+                       void* stream, rg_spectrum_info* info);
+
+/* Test hook: runs only the fused scale+scatter and copies the LDM tensor to
+ * host as [n_nodes][n_v] floats (node = l*n_L + m), in units of
+ * exp(info.log_scale) cm-1 . cm (times dv: no 1/dv yet).  capacity in floats. */
+int rg_debug_ldm(rg_plan* plan, const rg_conditions* cond, float* ldm_host, int64_t capacity,
+                 rg_spectrum_info* info);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RADIS_GB300_H */

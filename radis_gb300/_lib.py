@@ -1,0 +1,336 @@
+"""ctypes binding of ``libradisgb.so`` (the C ABI in include/radis_gb300.h).
+
+The product path has no CPU fallback: if the library is missing or the CUDA
+runtime cannot be loaded, every entry point raises ``NativeLibraryError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libradisgb.so")
+
+RG_OK = 0
+STATUS = {1: "RG_ERR_ARG", 2: "RG_ERR_CUDA", 3: "RG_ERR_OOM", 4: "RG_ERR_UNSORTED",
+          5: "RG_ERR_RANGE", 6: "RG_ERR_TIMEOUT", 7: "RG_ERR_STATE"}
+
+# every symbol the header declares (checked by the CPU test suite)
+EXPORTS = [
+    "rg_abi_version", "rg_last_error", "rg_ctx_create", "rg_ctx_destroy", "rg_lines_upload",
+    "rg_lines_free", "rg_lines_count", "rg_plan_create", "rg_plan_free", "rg_plan_grid", "rg_grid_estimate",
+    "rg_synthesize", "rg_synthesize_host", "rg_debug_ldm", "rg_plan_stage_times",
+]
+
+
+class NativeLibraryError(RuntimeError):
+    pass
+
+
+class RgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class LineArrays(C.Structure):
+    _fields_ = [("n", C.c_int64), ("v0", C.c_void_p), ("s_ref", C.c_void_p),
+                ("e_low", C.c_void_p), ("g_air", C.c_void_p), ("g_self", C.c_void_p),
+                ("n_air", C.c_void_p), ("delta", C.c_void_p), ("iso", C.c_void_p)]
+
+
+class Isotopes(C.Structure):
+    _fields_ = [("n_iso", C.c_int), ("molar_mass", C.c_double * 16), ("t_ref", C.c_double)]
+
+
+class PlanDesc(C.Structure):
+    _fields_ = [("vmin", C.c_double), ("dv", C.c_double), ("n_v", C.c_int64),
+                ("dxG", C.c_double), ("dxL", C.c_double), ("n_G", C.c_int), ("n_L", C.c_int),
+                ("folding_thresh", C.c_double), ("n_ft", C.c_int64)]
+
+
+class Conditions(C.Structure):
+    _fields_ = [("T", C.c_double), ("p_bar", C.c_double), ("x", C.c_double),
+                ("q_ratio", C.c_void_p)]
+
+
+class Grid(C.Structure):
+    _fields_ = [("log_wG_min", C.c_double), ("dxG", C.c_double), ("log_wL_min", C.c_double),
+                ("dxL", C.c_double), ("n_G", C.c_int), ("n_L", C.c_int), ("n_ft", C.c_int64),
+                ("n1", C.c_int64), ("n2", C.c_int64)]
+
+    def axes(self):
+        """(log_wG_min, dxG, N_G, log_wL_min, dxL, N_L) as the oracle takes them."""
+        return (self.log_wG_min, self.dxG, self.n_G, self.log_wL_min, self.dxL, self.n_L)
+
+
+class SpectrumInfo(C.Structure):
+    _fields_ = [("grid", Grid), ("log_scale", C.c_double), ("stage_ms", C.c_float * 6),
+                ("lines_in_window", C.c_int64)]
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load (once) and return the native library; raise loudly if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise NativeLibraryError(
+            f"{p} is missing: build it with `python -m radis_gb300._build` "
+            "(there is no CPU fallback for the synthesis path)")
+    try:
+        lib = C.CDLL(p)
+    except OSError as e:   # e.g. libcudart.so.13 not found
+        raise NativeLibraryError(f"cannot load {p}: {e}") from e
+    vp, i64 = C.c_void_p, C.c_int64
+    sig = {
+        "rg_abi_version": ([], C.c_int),
+        "rg_last_error": ([], C.c_char_p),
+        "rg_ctx_create": ([C.c_int, C.POINTER(vp)], C.c_int),
+        "rg_ctx_destroy": ([vp], C.c_int),
+        "rg_lines_upload": ([vp, C.POINTER(LineArrays), C.POINTER(Isotopes), C.POINTER(vp)], C.c_int),
+        "rg_lines_free": ([vp], C.c_int),
+        "rg_lines_count": ([vp, C.POINTER(i64)], C.c_int),
+        "rg_plan_create": ([vp, C.POINTER(PlanDesc), C.POINTER(vp)], C.c_int),
+        "rg_plan_free": ([vp], C.c_int),
+        "rg_plan_grid": ([vp, C.POINTER(Conditions), C.POINTER(Grid)], C.c_int),
+        "rg_grid_estimate": ([C.POINTER(LineArrays), C.POINTER(Isotopes), C.POINTER(PlanDesc),
+                              C.POINTER(Conditions), C.POINTER(Grid)], C.c_int),
+        "rg_synthesize": ([vp, C.POINTER(Conditions), vp, vp, C.c_int, C.POINTER(SpectrumInfo)], C.c_int),
+        "rg_synthesize_host": ([vp, C.POINTER(Conditions), vp, vp, C.POINTER(SpectrumInfo)], C.c_int),
+        "rg_plan_stage_times": ([vp, C.POINTER(C.c_double), C.POINTER(i64)], C.c_int),
+        "rg_debug_ldm": ([vp, C.POINTER(Conditions), vp, i64, C.POINTER(SpectrumInfo)], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def check(code: int):
+    if code != RG_OK:
+        msg = load().rg_last_error()
+        raise RgError(code, msg.decode() if msg else "")
+
+
+def ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """One device and its stream (rg_ctx)."""
+
+    def __init__(self, device: int = 0):
+        lib = load()
+        h = C.c_void_p()
+        check(lib.rg_ctx_create(int(device), C.byref(h)))
+        self._h = h
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            check(load().rg_ctx_destroy(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Lines:
+    """Device-resident line list (rg_lines).  Arrays are copied at construction;
+    v0 must be ascending (sort with ``sort_lines`` first)."""
+
+    COLS = ("v0", "S_ref", "El", "g_air", "g_self", "n_air", "delta", "iso")
+
+    def __init__(self, ctx: Context, lines: dict, molar_mass, t_ref: float = 296.0):
+        lib = load()
+        self.ctx = ctx
+        self._keep = dict(
+            v0=np.ascontiguousarray(lines["v0"], dtype=np.float64),
+            s=np.ascontiguousarray(lines["S_ref"], dtype=np.float64),
+            el=np.ascontiguousarray(lines["El"], dtype=np.float32),
+            ga=np.ascontiguousarray(lines["g_air"], dtype=np.float32),
+            gs=np.ascontiguousarray(lines["g_self"], dtype=np.float32),
+            na=np.ascontiguousarray(lines["n_air"], dtype=np.float32),
+        )
+        k = self._keep
+        d = lines.get("delta")
+        k["dl"] = None if d is None else np.ascontiguousarray(d, dtype=np.float32)
+        iso = lines.get("iso")
+        k["iso"] = None if iso is None else np.ascontiguousarray(iso, dtype=np.uint8)
+        mm = np.atleast_1d(np.asarray(molar_mass, dtype=np.float64))
+        self.n_iso = len(mm)
+        la = LineArrays(len(k["v0"]), ptr(k["v0"]), ptr(k["s"]), ptr(k["el"]), ptr(k["ga"]),
+                        ptr(k["gs"]), ptr(k["na"]), ptr(k["dl"]), ptr(k["iso"]))
+        iso_s = Isotopes()
+        iso_s.n_iso = self.n_iso
+        for i, m in enumerate(mm):
+            iso_s.molar_mass[i] = float(m)
+        iso_s.t_ref = float(t_ref)
+        h = C.c_void_p()
+        check(lib.rg_lines_upload(ctx.handle, C.byref(la), C.byref(iso_s), C.byref(h)))
+        self._h = h
+        self.n = len(k["v0"])
+        self.molar_mass = mm
+        self.t_ref = t_ref
+        self._keep = None   # host copies no longer needed
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            check(load().rg_lines_free(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Plan:
+    """Spectral grid + workspace over one line list (rg_plan)."""
+
+    def __init__(self, lines: Lines, vmin: float, dv: float, n_v: int, dxG=None, dxL=None,
+                 n_G=None, n_L=None, folding_thresh: float = 1e-6, n_ft: int = 0):
+        lib = load()
+        self.lines = lines
+        d = PlanDesc(float(vmin), float(dv), int(n_v), float(dxG or 0.0), float(dxL or 0.0),
+                     int(n_G or 0), int(n_L or 0), float(folding_thresh), int(n_ft))
+        h = C.c_void_p()
+        check(lib.rg_plan_create(lines.handle, C.byref(d), C.byref(h)))
+        self._h = h
+        self.vmin, self.dv, self.n_v = float(vmin), float(dv), int(n_v)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _cond(self, T, p_bar, x, q_ratio):
+        q = None
+        if q_ratio is not None:
+            q = np.ascontiguousarray(np.broadcast_to(np.asarray(q_ratio, np.float64),
+                                                     (self.lines.n_iso,)))
+        return Conditions(float(T), float(p_bar), float(x), ptr(q)), q
+
+    def grid(self, T, p_bar, x, q_ratio=None) -> Grid:
+        c, _q = self._cond(T, p_bar, x, q_ratio)
+        g = Grid()
+        check(load().rg_plan_grid(self._h, C.byref(c), C.byref(g)))
+        return g
+
+    def synthesize_host(self, T, p_bar, x, q_ratio=None, out=None):
+        """Blocking: returns (float32 array n_v, SpectrumInfo); abscoeff in cm-1
+        is ``out * exp(info.log_scale)``."""
+        c, _q = self._cond(T, p_bar, x, q_ratio)
+        if out is None:
+            out = np.empty(self.n_v, dtype=np.float32)
+        info = SpectrumInfo()
+        check(load().rg_synthesize_host(self._h, C.byref(c), ptr(out), None, C.byref(info)))
+        return out, info
+
+    def synthesize_device(self, T, p_bar, x, out_dev_ptr: int, stream_ptr: int | None = None,
+                          q_ratio=None, timing: int = 0):
+        """Enqueue on a caller stream into a caller device buffer (n_v floats).
+        timing: 0 none, 1 synchronous per-stage times in the returned info,
+        2 per-stage events into the plan's ring (read with ``stage_times``)."""
+        c, _q = self._cond(T, p_bar, x, q_ratio)
+        info = SpectrumInfo()
+        check(load().rg_synthesize(self._h, C.byref(c), C.c_void_p(out_dev_ptr),
+                                   C.c_void_p(stream_ptr) if stream_ptr else None,
+                                   int(timing), C.byref(info)))
+        return info
+
+    def stage_times(self):
+        """(sum of ms per stage [scatter, fft-col, fft-row+voigt, ifft-row,
+        ifft-col, total], count) of spectra enqueued with timing=2."""
+        s = (C.c_double * 6)()
+        n = C.c_int64()
+        check(load().rg_plan_stage_times(self._h, s, C.byref(n)))
+        return list(s), n.value
+
+    def debug_ldm(self, T, p_bar, x, q_ratio=None):
+        """Scatter only; returns (LDM [N_G, N_L, n_v] float32, info)."""
+        c, _q = self._cond(T, p_bar, x, q_ratio)
+        g = self.grid(T, p_bar, x, q_ratio)
+        buf = np.empty(g.n_G * g.n_L * self.n_v, dtype=np.float32)
+        info = SpectrumInfo()
+        check(load().rg_debug_ldm(self._h, C.byref(c), ptr(buf), buf.size, C.byref(info)))
+        return buf.reshape(g.n_G, g.n_L, self.n_v), info
+
+    def close(self):
+        if getattr(self, "_h", None):
+            check(load().rg_plan_free(self._h))
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def sort_lines(lines: dict) -> dict:
+    """Stable sort of a column dict by v0 (the CPU path sorts by shiftwav with
+    mergesort, radis/lbl/base.py:2370; the GPU kernels need v0 order)."""
+    v0 = np.asarray(lines["v0"])
+    if np.all(v0[1:] >= v0[:-1]):
+        return lines
+    order = np.argsort(v0, kind="stable")
+    return {k: (np.asarray(v)[order] if v is not None and np.ndim(v) == 1 and len(v) == len(v0) else v)
+            for k, v in lines.items()}
+
+
+def _line_arrays(lines: dict):
+    keep = dict(
+        v0=np.ascontiguousarray(lines["v0"], dtype=np.float64),
+        s=np.ascontiguousarray(lines["S_ref"], dtype=np.float64),
+        el=np.ascontiguousarray(lines["El"], dtype=np.float32),
+        ga=np.ascontiguousarray(lines["g_air"], dtype=np.float32),
+        gs=np.ascontiguousarray(lines["g_self"], dtype=np.float32),
+        na=np.ascontiguousarray(lines["n_air"], dtype=np.float32))
+    d, iso = lines.get("delta"), lines.get("iso")
+    keep["dl"] = None if d is None else np.ascontiguousarray(d, dtype=np.float32)
+    keep["iso"] = None if iso is None else np.ascontiguousarray(iso, dtype=np.uint8)
+    la = LineArrays(len(keep["v0"]), ptr(keep["v0"]), ptr(keep["s"]), ptr(keep["el"]),
+                    ptr(keep["ga"]), ptr(keep["gs"]), ptr(keep["na"]), ptr(keep["dl"]),
+                    ptr(keep["iso"]))
+    return la, keep
+
+
+def grid_estimate(lines: dict, molar_mass, vmin, dv, n_v, T, p_bar, x, dxG=None, dxL=None,
+                  n_G=None, n_L=None, t_ref=296.0, q_ratio=None, n_ft=0) -> Grid:
+    """Host-only (no GPU): the LDM grid a plan would use (rg_grid_estimate)."""
+    la, keep = _line_arrays(lines)
+    mm = np.atleast_1d(np.asarray(molar_mass, dtype=np.float64))
+    iso_s = Isotopes()
+    iso_s.n_iso = len(mm)
+    for i, m in enumerate(mm):
+        iso_s.molar_mass[i] = float(m)
+    iso_s.t_ref = float(t_ref)
+    d = PlanDesc(float(vmin), float(dv), int(n_v), float(dxG or 0.0), float(dxL or 0.0),
+                 int(n_G or 0), int(n_L or 0), 1e-6, int(n_ft))
+    q = None if q_ratio is None else np.ascontiguousarray(
+        np.broadcast_to(np.asarray(q_ratio, np.float64), (len(mm),)))
+    c = Conditions(float(T), float(p_bar), float(x), ptr(q))
+    g = Grid()
+    check(load().rg_grid_estimate(C.byref(la), C.byref(iso_s), C.byref(d), C.byref(c), C.byref(g)))
+    return g

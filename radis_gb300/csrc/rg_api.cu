@@ -1,0 +1,940 @@
+// Host side of the C ABI declared in include/radis_gb300.h.
+//
+// Object model (reference: radis/gpu/gpu.py gpuApp):
+//   rg_ctx    one device + one non-blocking stream  (GPUApplication)
+//   rg_lines  device-resident line list, structure of arrays, sorted by v0,
+//             plus host-side envelopes of widths and intensities
+//             (gpuApp.__init__ upload gpu.py:190-203; init_*_params params.py)
+//   rg_plan   spectral grid, FFT factorisation + twiddle tables, line index per
+//             grid column and the grow-only LDM / FFT workspace
+//             (gpu.py:133-141, 205-239; the x1.5 grow rule of
+//             vulkan_compute_lib.py:1308-1323 becomes x1.25 here)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdarg>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <new>
+
+#include "rg_internal.h"
+
+using namespace rg;
+
+// ---------------------------------------------------------------------------
+// error reporting
+// ---------------------------------------------------------------------------
+static thread_local std::string g_err;
+
+static int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CU(call)                                                                            \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return fail(e_ == cudaErrorMemoryAllocation ? RG_ERR_OOM : RG_ERR_CUDA,         \
+                        "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                        __LINE__);                                                          \
+    } while (0)
+
+#define RG(call)                                                   \
+    do {                                                           \
+        int r_ = (call);                                           \
+        if (r_ != RG_OK) {                                         \
+            if (g_err.empty()) fail(r_, "%s failed", #call);       \
+            return r_;                                             \
+        }                                                          \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// objects
+// ---------------------------------------------------------------------------
+struct rg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t magic = 0x52474358;
+};
+
+// Host-side summary of a line list: everything the per-spectrum grid and
+// scale computation needs (the reference keeps the same data as module
+// globals in radis/gpu/params.py:66-86).
+struct Envelope {
+    int64_t n = 0;
+    int n_iso = 1;
+    double t_ref = 296.0;
+    double log_c2Mm[kMaxIso] = {0};            // log(FWHM_G / (v0 sqrt(T)))
+    double lv_min[kMaxIso], lv_max[kMaxIso];   // per-iso min/max log v0
+    double max_abs_delta = 0.0;
+    Hull wl_lo, wl_hi;   // (n_air, log min/max(g_self, g_air))
+    Hull s_hi;           // (E_low, ln S')  S' = S_ref / (1 - exp(-c2 v0 / Tref))
+};
+
+struct rg_lines {
+    rg_ctx* ctx = nullptr;
+    int64_t n = 0;
+    float2* v0 = nullptr;
+    float* ls2 = nullptr;
+    float* el = nullptr;
+    float* ga = nullptr;
+    float* gs = nullptr;
+    float* na = nullptr;
+    float* dl = nullptr;
+    uint8_t* iso = nullptr;
+    int n_iso = 1;
+    double t_ref = 296.0;
+    Envelope env;
+    int plans = 0;
+    uint32_t magic = 0x52474C4E;
+};
+
+struct rg_plan {
+    rg_lines* lines = nullptr;
+    rg_plan_desc desc{};
+    std::mutex mu;
+    // FFT factorisation
+    int64_t n = 0;
+    int n1 = 0, n2 = 0, B = 0;
+    FftLen f1, f2;
+    float2* tw_hi = nullptr;
+    float2* tw_lo = nullptr;
+    // column index
+    int64_t* col_start = nullptr;
+    int col_off = 0, col_count = 0;
+    double p_atm_max = 0.0;
+    // workspace (grow-only)
+    int nodes_cap = 0;
+    int64_t row_stride = 0;
+    float* ldm = nullptr;
+    float2* y = nullptr;
+    float2* g = nullptr;
+    float* out_d = nullptr;
+    unsigned long long* counter = nullptr;
+    cudaEvent_t ev[6] = {nullptr};
+    // ring of per-stage events recorded without synchronisation (timing == 2)
+    static constexpr int kRing = 256;
+    std::vector<cudaEvent_t> ring;      // kRing * 6 events, created lazily
+    int ring_used = 0;
+    bool ring_ldm_only[kRing] = {false};
+    cudaStream_t ring_stream = nullptr;
+    uint32_t magic = 0x52475041;
+};
+
+namespace {
+
+// smallest 5-smooth m >= x
+int64_t next_smooth(int64_t x) {
+    for (int64_t m = std::max<int64_t>(x, 1);; ++m) {
+        int64_t r = m;
+        for (int p : {2, 3, 5})
+            while (r % p == 0) r /= p;
+        if (r == 1) return m;
+    }
+}
+
+bool radices(int L, int* rad, int* np) {
+    int r = L, k = 0;
+    int a = 0;
+    while (r % 2 == 0) {
+        r /= 2;
+        ++a;
+    }
+    while (a >= 3) {
+        rad[k++] = 8;
+        a -= 3;
+    }
+    if (a == 2) rad[k++] = 4;
+    if (a == 1) rad[k++] = 2;
+    while (r % 3 == 0) {
+        r /= 3;
+        rad[k++] = 3;
+    }
+    while (r % 5 == 0) {
+        r /= 5;
+        rad[k++] = 5;
+    }
+    *np = k;
+    return r == 1 && k <= kMaxPasses;
+}
+
+constexpr int kN2Max = 512 * 24;   // row FFT limit (threads x accumulators)
+
+// choose n = n1 * n2 >= n_min, n1 a power of two <= 512, n2 = 32 * (5-smooth)
+bool choose_fft(int64_t n_min, int64_t forced, int* n1o, int* n2o) {
+    int64_t best = std::numeric_limits<int64_t>::max();
+    int b1 = 0, b2 = 0;
+    for (int n1 = 512; n1 >= 8; n1 /= 2) {
+        int64_t n2;
+        if (forced) {
+            if (forced % n1) continue;
+            n2 = forced / n1;
+            if (n2 % 32) continue;
+            int64_t m = n2 / 32, r = m;
+            for (int p : {2, 3, 5})
+                while (r % p == 0) r /= p;
+            if (r != 1) continue;
+        } else {
+            int64_t need = (n_min + n1 - 1) / n1;
+            n2 = 32 * next_smooth((need + 31) / 32);
+        }
+        if (n2 > kN2Max) continue;
+        int64_t n = (int64_t)n1 * n2;
+        if (n < n_min) continue;
+        // prefer the shorter transform, then the larger n1 (fewer row FFT launches)
+        if (n < best) {
+            best = n;
+            b1 = n1;
+            b2 = (int)n2;
+        }
+    }
+    if (!b1) return false;
+    *n1o = b1;
+    *n2o = b2;
+    return true;
+}
+
+int upload_twiddles(int L, float2** out) {
+    std::vector<float2> h(L);
+    for (int t = 0; t < L; ++t) {
+        double ang = -2.0 * kPi * (double)t / (double)L;
+        h[t].x = (float)std::cos(ang);
+        h[t].y = (float)std::sin(ang);
+    }
+    CU(cudaMalloc(out, sizeof(float2) * L));
+    CU(cudaMemcpy(*out, h.data(), sizeof(float2) * L, cudaMemcpyHostToDevice));
+    return RG_OK;
+}
+
+int make_fftlen(int L, FftLen* f) {
+    f->L = L;
+    if (!radices(L, f->radix, &f->npass)) return fail(RG_ERR_RANGE, "FFT length %d not factorable", L);
+    return upload_twiddles(L, &f->tw);
+}
+
+void split(double v, float* hi, float* lo) {
+    *hi = (float)v;
+    *lo = (float)(v - (double)*hi);
+}
+
+template <typename T>
+void dfree(T*& p) {
+    if (p) cudaFree((void*)p);
+    p = nullptr;
+}
+
+// Per-spectrum host parameters (the reference's set_pTQ / set_G_params /
+// set_L_params, radis/gpu/params.py:89-155).
+struct SpecHost {
+    rg_grid grid;
+    double p_atm, log_scale_int, log_scale_out;
+    int n_nodes;       // padded to even
+};
+
+int compute_grid_env(const Envelope& E, const rg_plan_desc& d, int64_t n_ft, int n1, int n2,
+                     const rg_conditions* c, SpecHost* s) {
+    const Envelope* L = &E;
+    if (!(c->T > 0) || !(c->p_bar > 0) || !(c->x >= 0 && c->x <= 1))
+        return fail(RG_ERR_ARG, "conditions out of range: T=%g p=%g x=%g", c->T, c->p_bar, c->x);
+    const double eps = 1e-4;   // params.py:89,107
+    const double T = c->T;
+    s->p_atm = c->p_bar / kAtm;
+    // Gaussian axis: min/max of log v0 + log_c2Mm + 0.5 log T  (params.py:70-81,107-117)
+    double lg_lo = std::numeric_limits<double>::infinity(), lg_hi = -lg_lo;
+    for (int i = 0; i < L->n_iso; ++i) {
+        if (!(L->lv_min[i] <= L->lv_max[i])) continue;
+        lg_lo = std::min(lg_lo, L->lv_min[i] + L->log_c2Mm[i]);
+        lg_hi = std::max(lg_hi, L->lv_max[i] + L->log_c2Mm[i]);
+    }
+    lg_lo += 0.5 * std::log(T);
+    lg_hi += 0.5 * std::log(T) + eps;
+    // Lorentzian axis: envelopes over log(T_ref/T)  (params.py:8-67,89-104)
+    const double t = std::log(L->t_ref / T);
+    const double l2p = std::log(2.0 * s->p_atm);
+    double ll_lo = L->wl_lo.min_at(t) + l2p;
+    double ll_hi = L->wl_hi.max_at(t) + l2p + eps;
+    if (!std::isfinite(lg_lo) || !std::isfinite(lg_hi) || !std::isfinite(ll_lo) || !std::isfinite(ll_hi))
+        return fail(RG_ERR_ARG, "line widths are not finite (zero or negative broadening?)");
+    rg_grid& g = s->grid;
+    g.log_wG_min = lg_lo;
+    g.log_wL_min = ll_lo;
+    if (d.n_G > 1) {
+        g.n_G = d.n_G;
+        g.dxG = (lg_hi - lg_lo) / (d.n_G - 1);
+    } else {
+        g.dxG = d.dxG;
+        g.n_G = (int)std::ceil((lg_hi - lg_lo) / d.dxG) + 1;
+    }
+    if (d.n_L > 1) {
+        g.n_L = d.n_L;
+        g.dxL = (ll_hi - ll_lo) / (d.n_L - 1);
+    } else {
+        g.dxL = d.dxL;
+        g.n_L = (int)std::ceil((ll_hi - ll_lo) / d.dxL) + 1;
+    }
+    // a degenerate span (all widths equal) still needs a positive spacing
+    if (!(g.dxG > 0)) g.dxG = 1e-3;
+    if (!(g.dxL > 0)) g.dxL = 1e-3;
+    g.n_G = std::max(g.n_G, 2);
+    g.n_L = std::max(g.n_L, 2);
+    if (g.n_G > kMaxAxis || g.n_L > kMaxAxis || g.n_G * g.n_L > kMaxNodes - 1)
+        return fail(RG_ERR_RANGE, "LDM grid %d x %d exceeds the kernel limits (%d per axis, %d nodes)",
+                    g.n_G, g.n_L, kMaxAxis, kMaxNodes - 1);
+    g.n_ft = n_ft;
+    g.n1 = n1;
+    g.n2 = n2;
+    s->n_nodes = (g.n_G * g.n_L + 1) & ~1;
+    // intensity scale: the largest line intensity is at most exp(log_scale_int)
+    const double aT = -kC2 * (1.0 / T - 1.0 / L->t_ref);
+    const double dens = (c->p_bar * 1e5) / (kKb * T) * 1e-6 * c->x;   // factory.py:908-912
+    double lq = -std::numeric_limits<double>::infinity();
+    for (int i = 0; i < L->n_iso; ++i) {
+        double q = c->q_ratio ? c->q_ratio[i] : 1.0;
+        if (q > 0) lq = std::max(lq, std::log(q));
+    }
+    double smax = L->s_hi.max_at(aT);
+    double ls = (std::isfinite(smax) && dens > 0 && std::isfinite(lq)) ? smax + std::log(dens) + lq : 0.0;
+    s->log_scale_int = ls;
+    const double head = ls + std::log((double)std::max<int64_t>(L->n, 1) / d.dv);
+    s->log_scale_out = (head < 85.0 && ls > -60.0) ? 0.0 : ls;
+    return RG_OK;
+}
+
+int compute_grid(rg_plan* P, const rg_conditions* c, SpecHost* s) {
+    return compute_grid_env(P->lines->env, P->desc, P->n, P->n1, P->n2, c, s);
+}
+
+// Envelope of a host line list (per-iso v0 range, width and intensity hulls).
+int build_envelope(const rg_line_arrays* in, const rg_isotopes* iso, Envelope* E) {
+    if (!in || !iso) return fail(RG_ERR_ARG, "NULL argument");
+    if (in->n <= 0) return fail(RG_ERR_ARG, "empty line list");
+    if (!in->v0 || !in->s_ref || !in->e_low || !in->g_air || !in->g_self || !in->n_air)
+        return fail(RG_ERR_ARG, "a required line column is NULL");
+    if (iso->n_iso < 1 || iso->n_iso > kMaxIso) return fail(RG_ERR_ARG, "n_iso %d not in [1,16]", iso->n_iso);
+    if (!(iso->t_ref > 0)) return fail(RG_ERR_ARG, "t_ref must be positive");
+    const int64_t n = in->n;
+    E->n = n;
+    E->n_iso = iso->n_iso;
+    E->t_ref = iso->t_ref;
+    for (int i = 0; i < E->n_iso; ++i) {
+        if (!(iso->molar_mass[i] > 0)) return fail(RG_ERR_ARG, "molar_mass[%d] must be positive", i);
+        // log FWHM_G - log v0 - 0.5 log T = log(2 sqrt(2 NA k ln2 / M) / c)  (broadening.py:170-172)
+        E->log_c2Mm[i] = std::log(2.0 / kCcgs * std::sqrt(2.0 * kNA * kKbCgs * kLn2 / iso->molar_mass[i]));
+        E->lv_min[i] = std::numeric_limits<double>::infinity();
+        E->lv_max[i] = -std::numeric_limits<double>::infinity();
+    }
+    E->max_abs_delta = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        int k = in->iso ? in->iso[i] : 0;
+        if (k >= E->n_iso) return fail(RG_ERR_ARG, "iso[%lld] = %d >= n_iso", (long long)i, k);
+        if (!(in->v0[i] > 0)) return fail(RG_ERR_ARG, "v0[%lld] must be positive", (long long)i);
+        double lv = std::log(in->v0[i]);
+        E->lv_min[k] = std::min(E->lv_min[k], lv);
+        E->lv_max[k] = std::max(E->lv_max[k], lv);
+        if (in->delta) E->max_abs_delta = std::max(E->max_abs_delta, (double)std::fabs(in->delta[i]));
+    }
+    struct WidthSrc : PointSource {
+        const rg_line_arrays* in;
+        bool lo;
+        int64_t size() const override { return in->n; }
+        void get(int64_t i, double* a, double* b) const override {
+            *a = in->n_air[i];
+            float g = lo ? std::min(in->g_self[i], in->g_air[i]) : std::max(in->g_self[i], in->g_air[i]);
+            *b = g > 0 ? std::log((double)g) : -std::numeric_limits<double>::infinity();
+        }
+    };
+    WidthSrc wlo, whi;
+    wlo.in = whi.in = in;
+    wlo.lo = true;
+    whi.lo = false;
+    E->wl_lo = lower_hull_src(wlo);
+    E->wl_hi = upper_hull_src(whi);
+    if (E->wl_lo.a.empty() || E->wl_hi.a.empty())
+        return fail(RG_ERR_ARG, "no line has a positive broadening coefficient");
+    struct SSrc : PointSource {
+        const rg_line_arrays* in;
+        double c2_tref;
+        int64_t size() const override { return in->n; }
+        void get(int64_t i, double* a, double* b) const override {
+            *a = in->e_low[i];
+            double s = in->s_ref[i];
+            *b = s > 0 ? std::log(s) - std::log(-std::expm1(-c2_tref * in->v0[i]))
+                       : -std::numeric_limits<double>::infinity();
+        }
+    };
+    SSrc ss;
+    ss.in = in;
+    ss.c2_tref = kC2 / E->t_ref;
+    E->s_hi = upper_hull_src(ss);
+    return RG_OK;
+}
+
+int ensure_workspace(rg_plan* P, int n_nodes) {
+    if (n_nodes <= P->nodes_cap) return RG_OK;
+    int cap = std::min(kMaxNodes, std::max(n_nodes, (int)(P->nodes_cap * 1.25) + 2));
+    cap = (cap + 1) & ~1;
+    CU(cudaStreamSynchronize(P->lines->ctx->stream));
+    dfree(P->ldm);
+    dfree(P->y);
+    P->nodes_cap = 0;
+    CU(cudaMalloc(&P->ldm, sizeof(float) * (size_t)cap * P->row_stride));
+    CU(cudaMalloc(&P->y, sizeof(float2) * (size_t)(cap / 2) * P->n));
+    P->nodes_cap = cap;
+    return RG_OK;
+}
+
+int scatter_tile(int n_nodes) {
+    const int budget = 200 * 1024;
+    int tk = budget / (4 * n_nodes);
+    tk = (tk / 8) * 8;
+    return std::min(tk, 2048);
+}
+
+int build_scatter_args(rg_plan* P, const rg_conditions* c, const SpecHost& s, ScatterArgs* a) {
+    const rg_lines* L = P->lines;
+    const rg_grid& g = s.grid;
+    std::memset(a, 0, sizeof *a);
+    a->v0 = L->v0;
+    a->ls2 = L->ls2;
+    a->el = L->el;
+    a->ga = L->ga;
+    a->gs = L->gs;
+    a->na = L->na;
+    a->dl = L->dl;
+    a->iso = L->n_iso > 1 ? L->iso : nullptr;
+    a->col_start = P->col_start;
+    a->col_off = P->col_off;
+    a->col_count = P->col_count;
+    a->n_v = (int)P->desc.n_v;
+    a->n_nodes = s.n_nodes;
+    a->NG = g.n_G;
+    a->NL = g.n_L;
+    a->row_stride = P->row_stride;
+    a->ldm = P->ldm;
+    a->TK = scatter_tile(s.n_nodes);
+    if (a->TK < 8) return fail(RG_ERR_RANGE, "LDM grid of %d nodes does not fit a shared-memory tile", s.n_nodes);
+    if (s.p_atm > P->p_atm_max)
+        return fail(RG_ERR_RANGE, "pressure %g atm above the plan's shift-index limit %g atm", s.p_atm,
+                    P->p_atm_max);
+    a->margin_cols = (int)std::ceil(L->env.max_abs_delta * s.p_atm / P->desc.dv) + 1;
+    split(P->desc.vmin, &a->vmin_hi, &a->vmin_lo);
+    split(1.0 / P->desc.dv, &a->inv_dv_hi, &a->inv_dv_lo);
+    a->p_atm = (float)s.p_atm;
+    a->x_self = (float)c->x;
+    const double T = c->T;
+    a->lgG_scale = (float)(kLn2 / g.dxG);
+    for (int i = 0; i < L->n_iso; ++i)
+        a->cG[i] = (float)((L->env.log_c2Mm[i] + 0.5 * std::log(T) - g.log_wG_min) / g.dxG);
+    a->lgL_scale = (float)(kLn2 / g.dxL);
+    a->tL = (float)(std::log(L->t_ref / T) / g.dxL);
+    a->cL = (float)((std::log(2.0 * s.p_atm) - g.log_wL_min) / g.dxL);
+    split(-kC2 * (1.0 / T - 1.0 / L->t_ref) * kLog2e, &a->aT_hi, &a->aT_lo);
+    const double dens = (c->p_bar * 1e5) / (kKb * T) * 1e-6 * c->x;
+    for (int i = 0; i < L->n_iso; ++i) {
+        double q = c->q_ratio ? c->q_ratio[i] : 1.0;
+        double b = (q > 0 && dens > 0) ? (std::log(q * dens) - s.log_scale_int) * kLog2e : -1e30;
+        if (b < -1e30) b = -1e30;
+        split(b, &a->bI_hi[i], &a->bI_lo[i]);
+    }
+    a->stim_c = (float)(kC2 / T * kLog2e);
+    a->in_window = P->counter;
+    return RG_OK;
+}
+
+// folded Voigt FT of one node (broadening.py:1900-1926), FP64 on the host
+void node_fold(double dv, double wG, double wL, double thresh, int* nfold, double* norm) {
+    auto V = [&](double f) {
+        double g = std::exp(-std::pow(kPi * f * wG, 2) / (4.0 * kLn2));
+        return g * std::exp(-kPi * f * wL);
+    };
+    const double h = 1.0 / (2.0 * dv);
+    int n = 1;
+    double v0 = V(0.0);
+    while (V(n * h) >= thresh && n < 255) {
+        // bin 0: w_fold[0][0] = 0, w_fold[1][0] = 1/(2 dv)
+        v0 += V(n * h + ((n & 1) ? h : 0.0));
+        ++n;
+    }
+    *nfold = n - 1;
+    *norm = 1.0 / v0;
+}
+
+int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st, int timing, bool ldm_only,
+                 rg_spectrum_info* info) {
+    SpecHost s;
+    RG(compute_grid(P, c, &s));
+    RG(ensure_workspace(P, s.n_nodes));
+    ScatterArgs sa;
+    RG(build_scatter_args(P, c, s, &sa));
+    const int n_v = (int)P->desc.n_v;
+    const int n_tiles = (n_v + sa.TK - 1) / sa.TK;
+    const size_t smem = (size_t)s.n_nodes * sa.TK * sizeof(float);
+    cudaEvent_t* ev = P->ev;
+    if (timing == 2) {
+        if (P->ring.empty()) {
+            P->ring.assign(rg_plan::kRing * 6, nullptr);
+            for (auto& e : P->ring) CU(cudaEventCreate(&e));
+        }
+        if (P->ring_used >= rg_plan::kRing) return fail(RG_ERR_RANGE, "stage-timing ring full: read it first");
+        ev = &P->ring[6 * P->ring_used];
+        P->ring_ldm_only[P->ring_used] = ldm_only;
+        P->ring_used++;
+        P->ring_stream = st;
+    } else if (timing) {
+        for (auto& e : P->ev)
+            if (!e) CU(cudaEventCreate(&e));
+    }
+    if (timing) CU(cudaEventRecord(ev[0], st));
+    CU(cudaMemsetAsync(P->counter, 0, sizeof(unsigned long long), st));
+    RG(launch_scatter(sa, n_tiles, smem, st));
+    if (timing) CU(cudaEventRecord(ev[1], st));
+    if (!ldm_only) {
+        const rg_grid& g = s.grid;
+        // K2
+        ColFftArgs ca;
+        std::memset(&ca, 0, sizeof ca);
+        ca.f1 = P->f1;
+        ca.n1 = P->n1;
+        ca.n2 = P->n2;
+        ca.B = P->B;
+        ca.n_v = n_v;
+        ca.n = P->n;
+        ca.row_stride = P->row_stride;
+        ca.n_pairs = s.n_nodes / 2;
+        ca.ldm = P->ldm;
+        ca.y = P->y;
+        ca.tw_hi = P->tw_hi;
+        ca.tw_lo = P->tw_lo;
+        RG(launch_col_fft_fwd(ca, st));
+        if (timing) CU(cudaEventRecord(ev[2], st));
+        // K3
+        VoigtArgs* va = new (std::nothrow) VoigtArgs();
+        if (!va) return fail(RG_ERR_OOM, "host allocation failed");
+        std::unique_ptr<VoigtArgs> vguard(va);
+        va->f2 = P->f2;
+        va->n1 = P->n1;
+        va->n2 = P->n2;
+        va->n = P->n;
+        va->n_pairs = s.n_nodes / 2;
+        va->n_nodes = s.n_nodes;
+        va->NL = g.n_L;
+        va->y = P->y;
+        va->g = P->g;
+        va->inv_ndv = (float)(1.0 / ((double)P->n * P->desc.dv));
+        va->half_fs = (float)(0.5 / P->desc.dv);
+        const double thresh = P->desc.folding_thresh > 0 ? P->desc.folding_thresh : 1e-6;
+        for (int l = 0; l < g.n_G; ++l) {
+            double wG = std::exp(g.log_wG_min + l * g.dxG);
+            va->alpha[l] = (float)(std::pow(kPi * wG, 2) / (4.0 * kLn2) * kLog2e);
+        }
+        for (int m = 0; m < g.n_L; ++m) {
+            double wL = std::exp(g.log_wL_min + m * g.dxL);
+            va->beta[m] = (float)(kPi * wL * kLog2e);
+        }
+        va->any_fold = 0;
+        for (int node = 0; node < s.n_nodes; ++node) {
+            if (node >= g.n_G * g.n_L) {
+                va->norm[node] = 0.f;
+                va->nfold[node] = 0;
+                continue;
+            }
+            int l = node / g.n_L, m = node % g.n_L;
+            int nf;
+            double nrm;
+            node_fold(P->desc.dv, std::exp(g.log_wG_min + l * g.dxG), std::exp(g.log_wL_min + m * g.dxL), thresh,
+                      &nf, &nrm);
+            va->norm[node] = (float)nrm;
+            va->nfold[node] = (unsigned char)nf;
+            if (nf) va->any_fold = 1;
+        }
+        CU(cudaMemsetAsync(P->g, 0, sizeof(float2) * (size_t)P->n, st));
+        RG(launch_row_fft_voigt(*va, st));
+        if (timing) CU(cudaEventRecord(ev[3], st));
+        // K3b
+        RowIfftArgs ra;
+        ra.f2 = P->f2;
+        ra.n1 = P->n1;
+        ra.n2 = P->n2;
+        ra.n = P->n;
+        ra.g = P->g;
+        ra.tw_hi = P->tw_hi;
+        ra.tw_lo = P->tw_lo;
+        RG(launch_row_ifft(ra, st));
+        if (timing) CU(cudaEventRecord(ev[4], st));
+        // K4
+        ca.h = P->g;
+        ca.out = out;
+        ca.out_scale = (float)(std::exp(s.log_scale_int - s.log_scale_out) / ((double)P->n * P->desc.dv));
+        RG(launch_col_ifft(ca, st));
+        if (timing) CU(cudaEventRecord(ev[5], st));
+    }
+    if (info) {
+        std::memset(info, 0, sizeof *info);
+        info->grid = s.grid;
+        info->log_scale = ldm_only ? s.log_scale_int : s.log_scale_out;
+    }
+    if (timing == 1 && info) {
+        CU(cudaStreamSynchronize(st));
+        int last = ldm_only ? 1 : 5;
+        for (int i = 0; i < last; ++i) CU(cudaEventElapsedTime(&info->stage_ms[i], P->ev[i], P->ev[i + 1]));
+        CU(cudaEventElapsedTime(&info->stage_ms[5], P->ev[0], P->ev[last]));
+    }
+    if (info) {
+        unsigned long long cnt = 0;
+        if (timing == 1) {
+            CU(cudaMemcpy(&cnt, P->counter, sizeof cnt, cudaMemcpyDeviceToHost));
+            info->lines_in_window = (int64_t)cnt;
+        } else {
+            info->lines_in_window = -1;
+        }
+    }
+    return RG_OK;
+}
+
+bool valid(const rg_ctx* c) { return c && c->magic == 0x52474358; }
+bool valid(const rg_lines* l) { return l && l->magic == 0x52474C4E; }
+bool valid(const rg_plan* p) { return p && p->magic == 0x52475041; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int rg_abi_version(void) { return RG_ABI_VERSION; }
+
+const char* rg_last_error(void) { return g_err.c_str(); }
+
+int rg_ctx_create(int device, rg_ctx** out) {
+    g_err.clear();
+    if (!out) return fail(RG_ERR_ARG, "out is NULL");
+    int n = 0;
+    CU(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return fail(RG_ERR_ARG, "device %d not in [0, %d)", device, n);
+    CU(cudaSetDevice(device));
+    auto* c = new (std::nothrow) rg_ctx();
+    if (!c) return fail(RG_ERR_OOM, "host allocation failed");
+    c->device = device;
+    cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete c;
+        return fail(RG_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    }
+    *out = c;
+    return RG_OK;
+}
+
+int rg_ctx_destroy(rg_ctx* c) {
+    g_err.clear();
+    if (!c) return RG_OK;
+    if (!valid(c)) return fail(RG_ERR_STATE, "invalid context");
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    cudaStreamDestroy(c->stream);
+    c->magic = 0;
+    delete c;
+    return RG_OK;
+}
+
+int rg_lines_upload(rg_ctx* ctx, const rg_line_arrays* in, const rg_isotopes* iso, rg_lines** out) {
+    g_err.clear();
+    if (!valid(ctx)) return fail(RG_ERR_STATE, "invalid context");
+    if (!in || !iso || !out) return fail(RG_ERR_ARG, "NULL argument");
+    CU(cudaSetDevice(ctx->device));
+    auto* L = new (std::nothrow) rg_lines();
+    if (!L) return fail(RG_ERR_OOM, "host allocation failed");
+    std::unique_ptr<rg_lines> guard(L);
+    RG(build_envelope(in, iso, &L->env));
+    const int64_t n = in->n;
+    L->ctx = ctx;
+    L->n = n;
+    L->n_iso = iso->n_iso;
+    L->t_ref = iso->t_ref;
+
+    cudaStream_t st = ctx->stream;
+    double* v0_tmp = nullptr;
+    double* s_tmp = nullptr;
+    int* flag = nullptr;
+    auto cleanup_tmp = [&]() {
+        if (v0_tmp) cudaFree(v0_tmp);
+        if (s_tmp) cudaFree(s_tmp);
+        if (flag) cudaFree(flag);
+    };
+    auto bail = [&](int code) {
+        cleanup_tmp();
+        dfree(L->v0);
+        dfree(L->ls2);
+        dfree(L->el);
+        dfree(L->ga);
+        dfree(L->gs);
+        dfree(L->na);
+        dfree(L->dl);
+        dfree(L->iso);
+        return code;
+    };
+#define CUB(call)                                                                                    \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess)                                                                       \
+            return bail(fail(e_ == cudaErrorMemoryAllocation ? RG_ERR_OOM : RG_ERR_CUDA, "%s: %s", #call, \
+                             cudaGetErrorString(e_)));                                               \
+    } while (0)
+    const size_t f4 = sizeof(float) * (size_t)n;
+    CUB(cudaMalloc(&v0_tmp, sizeof(double) * n));
+    CUB(cudaMalloc(&s_tmp, sizeof(double) * n));
+    CUB(cudaMalloc(&flag, sizeof(int)));
+    CUB(cudaMalloc(&L->v0, sizeof(float2) * n));
+    CUB(cudaMalloc(&L->ls2, f4));
+    CUB(cudaMalloc(&L->el, f4));
+    CUB(cudaMalloc(&L->ga, f4));
+    CUB(cudaMalloc(&L->gs, f4));
+    CUB(cudaMalloc(&L->na, f4));
+    if (in->delta) CUB(cudaMalloc(&L->dl, f4));
+    if (in->iso && L->n_iso > 1) CUB(cudaMalloc(&L->iso, (size_t)n));
+    CUB(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    CUB(cudaMemcpyAsync(v0_tmp, in->v0, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    CUB(cudaMemcpyAsync(s_tmp, in->s_ref, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    CUB(cudaMemcpyAsync(L->el, in->e_low, f4, cudaMemcpyHostToDevice, st));
+    CUB(cudaMemcpyAsync(L->ga, in->g_air, f4, cudaMemcpyHostToDevice, st));
+    CUB(cudaMemcpyAsync(L->gs, in->g_self, f4, cudaMemcpyHostToDevice, st));
+    CUB(cudaMemcpyAsync(L->na, in->n_air, f4, cudaMemcpyHostToDevice, st));
+    if (in->delta) CUB(cudaMemcpyAsync(L->dl, in->delta, f4, cudaMemcpyHostToDevice, st));
+    if (L->iso) CUB(cudaMemcpyAsync(L->iso, in->iso, (size_t)n, cudaMemcpyHostToDevice, st));
+    if (launch_prepare_lines(v0_tmp, s_tmp, n, kC2 / L->t_ref, L->v0, L->ls2, flag, st) != RG_OK)
+        return bail(fail(RG_ERR_CUDA, "prepare_lines launch: %s", cudaGetErrorString(cudaGetLastError())));
+    int unsorted = 0;
+    CUB(cudaMemcpyAsync(&unsorted, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CUB(cudaStreamSynchronize(st));
+    cleanup_tmp();
+    v0_tmp = nullptr;
+    s_tmp = nullptr;
+    flag = nullptr;
+    if (unsorted) return bail(fail(RG_ERR_UNSORTED, "line positions v0 must be ascending"));
+#undef CUB
+    *out = guard.release();
+    return RG_OK;
+}
+
+int rg_lines_free(rg_lines* L) {
+    g_err.clear();
+    if (!L) return RG_OK;
+    if (!valid(L)) return fail(RG_ERR_STATE, "invalid line list");
+    if (L->plans) return fail(RG_ERR_STATE, "line list still has %d plan(s)", L->plans);
+    cudaSetDevice(L->ctx->device);
+    cudaStreamSynchronize(L->ctx->stream);
+    dfree(L->v0);
+    dfree(L->ls2);
+    dfree(L->el);
+    dfree(L->ga);
+    dfree(L->gs);
+    dfree(L->na);
+    dfree(L->dl);
+    dfree(L->iso);
+    L->magic = 0;
+    delete L;
+    return RG_OK;
+}
+
+int rg_lines_count(const rg_lines* L, int64_t* n) {
+    g_err.clear();
+    if (!valid(L) || !n) return fail(RG_ERR_ARG, "invalid argument");
+    *n = L->n;
+    return RG_OK;
+}
+
+int rg_plan_create(rg_lines* L, const rg_plan_desc* d, rg_plan** out) {
+    g_err.clear();
+    if (!valid(L)) return fail(RG_ERR_STATE, "invalid line list");
+    if (!d || !out) return fail(RG_ERR_ARG, "NULL argument");
+    if (!(d->dv > 0) || d->n_v < 2) return fail(RG_ERR_ARG, "dv must be > 0 and n_v >= 2");
+    if (d->n_v > (int64_t)1 << 30) return fail(RG_ERR_RANGE, "n_v too large");
+    if (!((d->n_G > 1) || d->dxG > 0) || !((d->n_L > 1) || d->dxL > 0))
+        return fail(RG_ERR_ARG, "give dxG/dxL > 0 or node counts n_G/n_L > 1");
+    CU(cudaSetDevice(L->ctx->device));
+    auto* P = new (std::nothrow) rg_plan();
+    if (!P) return fail(RG_ERR_OOM, "host allocation failed");
+    std::unique_ptr<rg_plan> guard(P);
+    P->lines = L;
+    P->desc = *d;
+    int n1, n2;
+    if (!choose_fft(2 * d->n_v, d->n_ft, &n1, &n2))
+        return fail(RG_ERR_RANGE, "no supported FFT length >= %lld (n_ft=%lld)", (long long)(2 * d->n_v),
+                    (long long)d->n_ft);
+    P->n1 = n1;
+    P->n2 = n2;
+    P->n = (int64_t)n1 * n2;
+    P->B = std::min(32, 8192 / n1);
+    RG(make_fftlen(n1, &P->f1));
+    RG(make_fftlen(n2, &P->f2));
+    {
+        const int nh = (int)(P->n / 1024) + 2;
+        std::vector<float2> hi(nh), lo(1024);
+        for (int t = 0; t < nh; ++t) {
+            double ang = -2.0 * kPi * (double)((int64_t)t * 1024 % P->n) / (double)P->n;
+            hi[t].x = (float)std::cos(ang);
+            hi[t].y = (float)std::sin(ang);
+        }
+        for (int t = 0; t < 1024; ++t) {
+            double ang = -2.0 * kPi * (double)t / (double)P->n;
+            lo[t].x = (float)std::cos(ang);
+            lo[t].y = (float)std::sin(ang);
+        }
+        CU(cudaMalloc(&P->tw_hi, sizeof(float2) * nh));
+        CU(cudaMalloc(&P->tw_lo, sizeof(float2) * 1024));
+        CU(cudaMemcpy(P->tw_hi, hi.data(), sizeof(float2) * nh, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(P->tw_lo, lo.data(), sizeof(float2) * 1024, cudaMemcpyHostToDevice));
+    }
+    // line index per grid column, with a margin for pressure shifts up to p_atm_max
+    P->p_atm_max = 200.0;
+    int E = (int)std::ceil(L->env.max_abs_delta * P->p_atm_max / d->dv) + 2;
+    if (E > (1 << 22)) {
+        P->p_atm_max = ((double)(1 << 22) - 2) * d->dv / L->env.max_abs_delta;
+        E = 1 << 22;
+    }
+    P->col_off = E;
+    P->col_count = (int)d->n_v + 1 + 2 * E;
+    CU(cudaMalloc(&P->col_start, sizeof(int64_t) * P->col_count));
+    RG(launch_col_index(L->v0, L->n, d->vmin, d->dv, -E, P->col_count, P->col_start, L->ctx->stream));
+    P->row_stride = (d->n_v + 31) / 32 * 32;
+    CU(cudaMalloc(&P->g, sizeof(float2) * (size_t)P->n));
+    CU(cudaMalloc(&P->out_d, sizeof(float) * (size_t)d->n_v));
+    CU(cudaMalloc(&P->counter, sizeof(unsigned long long)));
+    CU(cudaStreamSynchronize(L->ctx->stream));
+    L->plans++;
+    *out = guard.release();
+    return RG_OK;
+}
+
+int rg_plan_free(rg_plan* P) {
+    g_err.clear();
+    if (!P) return RG_OK;
+    if (!valid(P)) return fail(RG_ERR_STATE, "invalid plan");
+    {
+        std::lock_guard<std::mutex> lk(P->mu);
+        cudaSetDevice(P->lines->ctx->device);
+        cudaStreamSynchronize(P->lines->ctx->stream);
+        cudaDeviceSynchronize();
+        dfree(P->f1.tw);
+        dfree(P->f2.tw);
+        dfree(P->tw_hi);
+        dfree(P->tw_lo);
+        dfree(P->col_start);
+        dfree(P->ldm);
+        dfree(P->y);
+        dfree(P->g);
+        dfree(P->out_d);
+        dfree(P->counter);
+        for (auto& e : P->ev)
+            if (e) cudaEventDestroy(e);
+        for (auto& e : P->ring)
+            if (e) cudaEventDestroy(e);
+        P->lines->plans--;
+        P->magic = 0;
+    }
+    delete P;
+    return RG_OK;
+}
+
+int rg_plan_grid(rg_plan* P, const rg_conditions* c, rg_grid* out) {
+    g_err.clear();
+    if (!valid(P) || !c || !out) return fail(RG_ERR_ARG, "invalid argument");
+    SpecHost s;
+    RG(compute_grid(P, c, &s));
+    *out = s.grid;
+    return RG_OK;
+}
+
+int rg_grid_estimate(const rg_line_arrays* lines, const rg_isotopes* iso, const rg_plan_desc* d,
+                     const rg_conditions* c, rg_grid* out) {
+    g_err.clear();
+    if (!lines || !iso || !d || !c || !out) return fail(RG_ERR_ARG, "NULL argument");
+    if (!(d->dv > 0) || d->n_v < 2) return fail(RG_ERR_ARG, "dv must be > 0 and n_v >= 2");
+    if (!((d->n_G > 1) || d->dxG > 0) || !((d->n_L > 1) || d->dxL > 0))
+        return fail(RG_ERR_ARG, "give dxG/dxL > 0 or node counts n_G/n_L > 1");
+    int n1, n2;
+    if (!choose_fft(2 * d->n_v, d->n_ft, &n1, &n2))
+        return fail(RG_ERR_RANGE, "no supported FFT length >= %lld", (long long)(2 * d->n_v));
+    auto env = std::make_unique<Envelope>();
+    RG(build_envelope(lines, iso, env.get()));
+    SpecHost s;
+    RG(compute_grid_env(*env, *d, (int64_t)n1 * n2, n1, n2, c, &s));
+    *out = s.grid;
+    return RG_OK;
+}
+
+int rg_synthesize(rg_plan* P, const rg_conditions* c, float* out_dev, void* stream, int timing,
+                  rg_spectrum_info* info) {
+    g_err.clear();
+    if (!valid(P) || !c || !out_dev) return fail(RG_ERR_ARG, "invalid argument");
+    std::lock_guard<std::mutex> lk(P->mu);
+    CU(cudaSetDevice(P->lines->ctx->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
+    return run_spectrum(P, c, out_dev, st, timing, false, info);
+}
+
+int rg_plan_stage_times(rg_plan* P, double* sum_ms, int64_t* count) {
+    g_err.clear();
+    if (!valid(P) || !sum_ms || !count) return fail(RG_ERR_ARG, "invalid argument");
+    std::lock_guard<std::mutex> lk(P->mu);
+    for (int k = 0; k < 6; ++k) sum_ms[k] = 0.0;
+    *count = P->ring_used;
+    if (!P->ring_used) return RG_OK;
+    CU(cudaStreamSynchronize(P->ring_stream));
+    for (int r = 0; r < P->ring_used; ++r) {
+        cudaEvent_t* ev = &P->ring[6 * r];
+        int last = P->ring_ldm_only[r] ? 1 : 5;
+        float ms;
+        for (int i = 0; i < last; ++i) {
+            CU(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+            sum_ms[i] += ms;
+        }
+        CU(cudaEventElapsedTime(&ms, ev[0], ev[last]));
+        sum_ms[5] += ms;
+    }
+    P->ring_used = 0;
+    return RG_OK;
+}
+
+int rg_synthesize_host(rg_plan* P, const rg_conditions* c, float* out_host, void* stream,
+                       rg_spectrum_info* info) {
+    g_err.clear();
+    if (!valid(P) || !c || !out_host) return fail(RG_ERR_ARG, "invalid argument");
+    std::lock_guard<std::mutex> lk(P->mu);
+    CU(cudaSetDevice(P->lines->ctx->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
+    RG(run_spectrum(P, c, P->out_d, st, 0, false, info));
+    CU(cudaMemcpyAsync(out_host, P->out_d, sizeof(float) * (size_t)P->desc.n_v, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return RG_OK;
+}
+
+int rg_debug_ldm(rg_plan* P, const rg_conditions* c, float* ldm_host, int64_t capacity,
+                 rg_spectrum_info* info) {
+    g_err.clear();
+    if (!valid(P) || !c || !ldm_host) return fail(RG_ERR_ARG, "invalid argument");
+    std::lock_guard<std::mutex> lk(P->mu);
+    CU(cudaSetDevice(P->lines->ctx->device));
+    cudaStream_t st = P->lines->ctx->stream;
+    rg_spectrum_info tmp;
+    rg_spectrum_info* inf = info ? info : &tmp;
+    RG(run_spectrum(P, c, nullptr, st, 1, true, inf));
+    const int nodes = inf->grid.n_G * inf->grid.n_L;
+    if (capacity < (int64_t)nodes * P->desc.n_v)
+        return fail(RG_ERR_ARG, "capacity %lld < %lld", (long long)capacity, (long long)nodes * P->desc.n_v);
+    CU(cudaMemcpy2DAsync(ldm_host, sizeof(float) * P->desc.n_v, P->ldm, sizeof(float) * P->row_stride,
+                         sizeof(float) * P->desc.n_v, nodes, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return RG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,161 @@
+// Internal types shared by the host side (rg_api.cu, rg_hull.cpp) and the
+// kernels (rg_kernels.cu).  Not part of the public ABI.
+#pragma once
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/radis_gb300.h"
+
+#ifdef __CUDACC__
+#include <cuda_runtime.h>
+#else
+struct float2 { float x, y; };
+typedef struct CUstream_st* cudaStream_t;
+#endif
+
+namespace rg {
+
+// --- physical constants (radis/phys/constants.py:22,33,38,60,69,75,78) -------
+constexpr double kH = 6.62607015e-34;
+constexpr double kC = 2.99792458e8;
+constexpr double kKb = 1.3806490e-23;
+constexpr double kNA = 6.02214076e23;
+constexpr double kC2 = kH * kC / kKb * 100.0;      // hc/k, cm K
+constexpr double kCcgs = 2.99792458e10;
+constexpr double kKbCgs = 1.380648813e-16;         // the CPU Doppler width's k (erg/K)
+constexpr double kPi = 3.14159265358979323846;
+constexpr double kLn2 = 0.69314718055994530942;
+constexpr double kLog2e = 1.44269504088896340736;
+constexpr double kAtm = 1.01325;                    // bar per atm (broadening.py:1063)
+
+constexpr int kMaxIso = 16;
+constexpr int kMaxAxis = 64;        // max nodes along one LDM axis
+constexpr int kMaxNodes = 1024;     // max N_G * N_L (padded to even)
+constexpr int kPairGroup = 8;       // node pairs per Voigt-reduce work item
+constexpr int kMaxPasses = 16;
+
+// --- host-side convex envelopes (rg_hull.cpp) ---------------------------------
+// Lower convex hull of points (a_i, b_i): min_i (b_i + a_i t) for every t is
+// attained at one of its vertices.
+struct Hull {
+    std::vector<double> a, b;
+    double min_at(double t) const;
+    double max_at(double t) const;   // for an upper hull stored as-is
+};
+// exact lower hull / upper hull of n points (non-finite b values are skipped)
+Hull lower_hull(const double* a, const double* b, int64_t n);
+Hull upper_hull(const double* a, const double* b, int64_t n);
+// Same, with the point coordinates produced on the fly by a functor-like
+// callback to avoid materialising n-length temporaries.
+struct PointSource {
+    virtual ~PointSource() {}
+    virtual int64_t size() const = 0;
+    virtual void get(int64_t i, double* a, double* b) const = 0;
+};
+Hull lower_hull_src(const PointSource& s);
+Hull upper_hull_src(const PointSource& s);
+
+// --- FFT plan of one sub-length -------------------------------------------------
+struct FftLen {
+    int L = 0;
+    int npass = 0;
+    int radix[kMaxPasses] = {0};
+    float2* tw = nullptr;       // device: exp(-2 pi i t / L), t < L
+};
+
+// --- kernel argument blocks (passed by value) ----------------------------------
+struct ScatterArgs {
+    const float2* v0;     // (hi, lo) split of the FP64 line centre
+    const float* ls2;     // log2 S_ref - log2(1 - exp(-c2 v0 / Tref))
+    const float* el;
+    const float* ga;
+    const float* gs;
+    const float* na;
+    const float* dl;      // nullable
+    const uint8_t* iso;   // nullable
+    const int64_t* col_start;   // first line with v0 >= vmin + c dv, c = idx - col_off
+    int col_off;
+    int col_count;
+    int n_v;
+    int TK;               // columns per tile (multiple of 8)
+    int n_nodes;          // padded to even
+    int NG, NL;
+    int64_t row_stride;
+    float* ldm;
+    int margin_cols;
+    float vmin_hi, vmin_lo;
+    float inv_dv_hi, inv_dv_lo;
+    float p_atm;
+    float x_self;
+    float lgG_scale;          // ln2 / dxG
+    float cG[kMaxIso];        // (log_c2Mm[iso] + 0.5 log T - log_wG_min) / dxG
+    float lgL_scale;          // ln2 / dxL
+    float tL;                 // log(Tref/T) / dxL
+    float cL;                 // (log(2 p_atm) - log_wL_min) / dxL
+    float aT_hi, aT_lo;       // -c2 (1/T - 1/Tref) log2e (double-float)
+    float bI_hi[kMaxIso], bI_lo[kMaxIso];   // (log(Qr N x) - log_scale) log2e
+    float stim_c;             // c2/T log2e
+    unsigned long long* in_window;   // nullable counter of lines in the window
+};
+
+struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
+    FftLen f1;
+    int n1, n2;
+    int B;                // columns per CTA
+    int n_v;
+    int64_t n;            // n_ft
+    int64_t row_stride;
+    int n_pairs;
+    const float* ldm;     // K2 input
+    float2* y;            // K2 output [pair][n1][n2]
+    const float2* tw_hi;  // exp(-2 pi i 1024 t / N)
+    const float2* tw_lo;  // exp(-2 pi i t / N), t < 1024
+    const float2* h;      // K4 input [n1][n2]
+    float* out;           // K4 output (n_v)
+    float out_scale;
+};
+
+struct VoigtArgs {        // K3 (row FFT + Voigt weights + pair reduction)
+    FftLen f2;
+    int n1, n2;
+    int64_t n;
+    int n_pairs;
+    int n_nodes;
+    int NL;
+    const float2* y;
+    float2* g;            // accumulator [n1][n2]
+    float inv_ndv;        // 1 / (N dv)
+    float half_fs;        // 1 / (2 dv)
+    float alpha[kMaxAxis];    // (pi wG_l)^2 / (4 ln 2) * log2e
+    float beta[kMaxAxis];     // pi wL_m * log2e
+    float norm[kMaxNodes];    // 1 / folded profile at f = 0 (0 for padding node)
+    unsigned char nfold[kMaxNodes];
+    int any_fold;
+};
+
+struct RowIfftArgs {      // K3b (inverse row FFT + twiddle, in place)
+    FftLen f2;
+    int n1, n2;
+    int64_t n;
+    float2* g;
+    const float2* tw_hi;
+    const float2* tw_lo;
+};
+
+// --- launchers (rg_kernels.cu) ---------------------------------------------------
+int launch_prepare_lines(const double* v0_d, const double* s_d, int64_t n, double c2_tref,
+                         float2* v0_out, float* ls2_out, int* unsorted_flag, cudaStream_t st);
+int launch_col_index(const float2* v0, int64_t n, double vmin, double dv, int c_min, int count,
+                     int64_t* col_start, cudaStream_t st);
+int launch_scatter(const ScatterArgs& a, int n_tiles, size_t smem, cudaStream_t st);
+int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st);
+int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st);
+int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st);
+int launch_col_ifft(const ColFftArgs& a, cudaStream_t st);
+size_t col_fft_smem(int n1, int B);
+size_t row_fft_smem(int n2);
+
+}  // namespace rg

@@ -1,0 +1,547 @@
+// Device kernels of the LDM/DIT synthesis for sm_103a.
+//
+// Pipeline of one spectrum (radis/gpu/gpu.py:255-282 is the reference order):
+//   k_scatter       fused per-line scaling + 2x2x2 scatter into a shared-memory
+//                   LDM tile, flushed once to HBM with plain stores
+//                   (replaces cmdFillLDM.comp:75-145 and the buffer clear)
+//   k_col_fft_fwd   first half of a four-step FFT: length-n1 DFTs down the
+//                   columns of two packed node rows + twiddle
+//   k_row_fft_voigt second half: length-n2 DFT of each row, times the analytic
+//                   Voigt FT of the node pair, summed over pairs
+//                   (replaces the R2C FFT + cmdApplyLineshapes.comp:51-90)
+//   k_row_ifft      inverse row DFTs + twiddle, in place
+//   k_col_ifft      inverse column DFTs, real part, scaled, first n_v samples
+//                   (replaces the C2R IFFT)
+// Two real node rows a, b are transformed as one complex row z = a + i b.
+// With W = V_a - i V_b, sum_j Z_j W_j = G and abscoeff = Re(IFFT(G)) / (N dv):
+// the Hermitian pairing of bins k and N-k is absorbed by taking the real part.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+
+#include "rg_internal.h"
+
+namespace rg {
+
+// ---------------------------------------------------------------------------
+// small helpers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float ex2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float lg2(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+// Knuth's TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+// multiply by -i (forward-direction quarter turn)
+__device__ __forceinline__ float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }
+
+// ---------------------------------------------------------------------------
+// forward DFTs of radix 2, 3, 4, 5, 8 in registers (exp(-2 pi i n k / R))
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void dft2(float2* v) {
+    float2 a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+}
+__device__ __forceinline__ void dft4(float2* v) {
+    float2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+    float2 s13 = cadd(v[1], v[3]), d13 = mul_mi(csub(v[1], v[3]));
+    v[0] = cadd(s02, s13);
+    v[2] = csub(s02, s13);
+    v[1] = cadd(d02, d13);
+    v[3] = csub(d02, d13);
+}
+__device__ __forceinline__ void dft3(float2* v) {
+    const float c1 = -0.5f, s1 = 0.86602540378443864676f;   // cos/sin(2 pi / 3)
+    float2 t = cadd(v[1], v[2]);
+    float2 d = csub(v[1], v[2]);
+    float2 a0 = v[0];
+    v[0] = cadd(a0, t);
+    float2 m = make_float2(a0.x + c1 * t.x, a0.y + c1 * t.y);
+    // -i * s1 * d
+    float2 r = make_float2(s1 * d.y, -s1 * d.x);
+    v[1] = cadd(m, r);
+    v[2] = csub(m, r);
+}
+__device__ __forceinline__ void dft5(float2* v) {
+    const float c1 = 0.30901699437494742410f, s1 = 0.95105651629515357212f;  // 2 pi / 5
+    const float c2 = -0.80901699437494742410f, s2 = 0.58778525229247312917f; // 4 pi / 5
+    float2 a0 = v[0];
+    float2 t1 = cadd(v[1], v[4]), d1 = csub(v[1], v[4]);
+    float2 t2 = cadd(v[2], v[3]), d2 = csub(v[2], v[3]);
+    v[0] = make_float2(a0.x + t1.x + t2.x, a0.y + t1.y + t2.y);
+    float2 m1 = make_float2(a0.x + c1 * t1.x + c2 * t2.x, a0.y + c1 * t1.y + c2 * t2.y);
+    float2 m2 = make_float2(a0.x + c2 * t1.x + c1 * t2.x, a0.y + c2 * t1.y + c1 * t2.y);
+    // forward: X1 = m1 - i (s1 d1 + s2 d2), X4 = m1 + i (...)
+    float2 q1 = make_float2(s1 * d1.x + s2 * d2.x, s1 * d1.y + s2 * d2.y);
+    float2 q2 = make_float2(s2 * d1.x - s1 * d2.x, s2 * d1.y - s1 * d2.y);
+    v[1] = cadd(m1, mul_mi(q1));
+    v[4] = csub(m1, mul_mi(q1));
+    v[2] = cadd(m2, mul_mi(q2));
+    v[3] = csub(m2, mul_mi(q2));
+}
+__device__ __forceinline__ void dft8(float2* v) {
+    const float r = 0.70710678118654752440f;
+    // radix-2 split: even / odd halves
+    float2 e[4] = {v[0], v[2], v[4], v[6]};
+    float2 o[4] = {v[1], v[3], v[5], v[7]};
+    dft4(e);
+    dft4(o);
+    // twiddles w8^k = exp(-i pi k / 4), k = 0..3
+    float2 o1 = make_float2(r * (o[1].x + o[1].y), r * (o[1].y - o[1].x));
+    float2 o2 = mul_mi(o[2]);
+    float2 o3 = make_float2(r * (o[3].y - o[3].x), -r * (o[3].x + o[3].y));
+    v[0] = cadd(e[0], o[0]);
+    v[4] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], o1);
+    v[5] = csub(e[1], o1);
+    v[2] = cadd(e[2], o2);
+    v[6] = csub(e[2], o2);
+    v[3] = cadd(e[3], o3);
+    v[7] = csub(e[3], o3);
+}
+
+template <int R>
+__device__ __forceinline__ void dftR(float2* v) {
+    if (R == 2) dft2(v);
+    if (R == 3) dft3(v);
+    if (R == 4) dft4(v);
+    if (R == 5) dft5(v);
+    if (R == 8) dft8(v);
+}
+
+// One Stockham autosort pass over B interleaved transforms of length L
+// (element i of transform b at [i * B + b]).  Pass with radix R after
+// sub-transforms of length Ns: butterfly j reads in[j + r L/R], twiddles by
+// w_{Ns R}^{r (j mod Ns)}, and writes out[(j / Ns) Ns R + (j mod Ns) + r Ns].
+template <int R>
+__device__ __forceinline__ void stockham_pass(const float2* __restrict__ in, float2* __restrict__ out,
+                                              int L, int B, int Ns, const float2* __restrict__ tw) {
+    const int M = L / R;
+    const int total = M * B;
+    const int twstep = L / (Ns * R);
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int j = t / B;
+        const int b = t - j * B;
+        const int k = j % Ns;
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = in[(j + r * M) * B + b];
+        if (Ns > 1) {
+            const int s = k * twstep;
+#pragma unroll
+            for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[r * s]));
+        }
+        dftR<R>(v);
+        const int base = (j - k) * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) out[(base + r * Ns) * B + b] = v[r];
+    }
+}
+
+// Forward DFT of B interleaved transforms; buf0 holds the input.  Returns the
+// buffer that holds the result.  Ends with __syncthreads().
+__device__ float2* fft_batched(float2* buf0, float2* buf1, const FftLen& P, int B) {
+    float2* in = buf0;
+    float2* out = buf1;
+    int Ns = 1;
+    for (int p = 0; p < P.npass; ++p) {
+        const int R = P.radix[p];
+        switch (R) {
+            case 2: stockham_pass<2>(in, out, P.L, B, Ns, P.tw); break;
+            case 3: stockham_pass<3>(in, out, P.L, B, Ns, P.tw); break;
+            case 4: stockham_pass<4>(in, out, P.L, B, Ns, P.tw); break;
+            case 5: stockham_pass<5>(in, out, P.L, B, Ns, P.tw); break;
+            default: stockham_pass<8>(in, out, P.L, B, Ns, P.tw); break;
+        }
+        __syncthreads();
+        float2* t = in;
+        in = out;
+        out = t;
+        Ns *= R;
+    }
+    return in;
+}
+
+// exp(-2 pi i t / N) from a two-level table (t = hi * 1024 + lo)
+__device__ __forceinline__ float2 twiddle_n(const float2* __restrict__ hi, const float2* __restrict__ lo,
+                                            int t) {
+    return cmul(__ldg(&hi[t >> 10]), __ldg(&lo[t & 1023]));
+}
+
+// ---------------------------------------------------------------------------
+// line preparation at upload: (hi, lo) split of v0 and log2 of the intensity
+// ---------------------------------------------------------------------------
+__global__ void k_prepare_lines(const double* __restrict__ v0, const double* __restrict__ s, int64_t n,
+                                double c2_tref, float2* __restrict__ v0_out, float* __restrict__ ls2,
+                                int* unsorted) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = v0[i];
+    float hi = (float)v;
+    float lo = (float)(v - (double)hi);
+    v0_out[i] = make_float2(hi, lo);
+    double si = s[i];
+    // log2 S_ref - log2(1 - exp(-c2 v0 / Tref)) : the stimulated-emission
+    // denominator of base.py:2676 is constant per line
+    double l = si > 0.0 ? log2(si) - log2(-expm1(-c2_tref * v)) : -INFINITY;
+    ls2[i] = (float)l;
+    if (i + 1 < n && v0[i + 1] < v) atomicExch(unsorted, 1);
+}
+
+// first line index with v0 >= vmin + c dv, for c = c_min + idx
+__global__ void k_col_index(const float2* __restrict__ v0, int64_t n, double vmin, double dv, int c_min,
+                            int count, int64_t* __restrict__ col_start) {
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= count) return;
+    const double target = vmin + (double)(c_min + idx) * dv;
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t mid = lo + ((hi - lo) >> 1);
+        float2 w = v0[mid];
+        double v = (double)w.x + (double)w.y;
+        if (v < target)
+            lo = mid + 1;
+        else
+            hi = mid;
+    }
+    col_start[idx] = lo;
+}
+
+// ---------------------------------------------------------------------------
+// K1: fused line scaling + LDM scatter into a shared-memory tile
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_scatter(const ScatterArgs a) {
+    extern __shared__ float4 tile4[];
+    float* tile = reinterpret_cast<float*>(tile4);
+    const int k_start = blockIdx.x * a.TK;
+    const int tk = min(a.TK, a.n_v - k_start);
+    const int n4 = a.n_nodes * a.TK / 4;
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) tile4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncthreads();
+
+    int c_lo = k_start - 1 - a.margin_cols + a.col_off;
+    int c_hi = k_start + tk + a.margin_cols + a.col_off;
+    c_lo = max(0, min(c_lo, a.col_count - 1));
+    c_hi = max(0, min(c_hi, a.col_count - 1));
+    const int64_t i0 = a.col_start[c_lo];
+    const int64_t i1 = a.col_start[c_hi];
+    const int dL = a.TK;
+    const int dG = a.NL * a.TK;
+    unsigned int counted = 0;
+
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        const float2 v = a.v0[i];
+        const float shift = a.dl ? a.dl[i] * a.p_atm : 0.f;
+        // k position in double-float: ((hi - vmin_hi) + (lo - vmin_lo + shift)) / dv
+        float s, e;
+        two_sum(v.x, -a.vmin_hi, s, e);
+        e += (v.y - a.vmin_lo) + shift;
+        const float p = s * a.inv_dv_hi;
+        const float pe = fmaf(s, a.inv_dv_hi, -p) + fmaf(s, a.inv_dv_lo, e * a.inv_dv_hi);
+        float fk = floorf(p);
+        float tv = (p - fk) + pe;
+        const float fl = floorf(tv);
+        fk += fl;
+        tv -= fl;
+        if (!(fk >= 0.f) || fk + 1.f >= (float)a.n_v) continue;   // drop (cmdFillLDM.comp:102)
+        const int k0 = (int)fk;
+        const int c0 = k0 - k_start;
+        const bool own0 = (unsigned)c0 < (unsigned)tk;
+        const bool own1 = (unsigned)(c0 + 1) < (unsigned)tk;
+        if (!(own0 || own1)) continue;
+        if (own0) ++counted;
+        const int is = a.iso ? (int)a.iso[i] : 0;
+        // Gaussian / Lorentzian node coordinates (FWHM, log space)
+        const float pl = fmaf(lg2(v.x), a.lgG_scale, a.cG[is]);
+        const float ga = a.ga[i];
+        const float gam = fmaf(a.x_self, a.gs[i] - ga, ga);
+        const float pm = fmaf(lg2(gam), a.lgL_scale, fmaf(a.na[i], a.tL, a.cL));
+        const int l0 = min(max((int)floorf(pl), 0), a.NG - 2);
+        const int m0 = min(max((int)floorf(pm), 0), a.NL - 2);
+        const float tG = pl - (float)l0;
+        const float tL = pm - (float)m0;
+        // intensity: exponent log2(S_ref) + a_T El + b_iso in double-float
+        const float el = a.el[i];
+        const float ph = el * a.aT_hi;
+        const float pe2 = fmaf(el, a.aT_hi, -ph) + el * a.aT_lo;
+        float s1, e1, s2, e2;
+        two_sum(ph, a.bI_hi[is], s1, e1);
+        two_sum(s1, a.ls2[i], s2, e2);
+        const float arg = s2 + (e1 + e2 + pe2 + a.bI_lo[is]);
+        const float I = ex2(arg) * (1.f - ex2(-a.stim_c * v.x));
+        const float I1 = tv * I;
+        const float I0 = I - I1;
+        const float w11 = tG * tL;
+        const float w10 = tG - w11;          // tG (1 - tL)
+        const float w01 = tL - w11;          // (1 - tG) tL
+        const float w00 = 1.f - tG - w01;    // (1 - tG)(1 - tL)
+        const int base = (l0 * a.NL + m0) * a.TK + c0;
+        if (own0) {
+            atomicAdd(&tile[base], I0 * w00);
+            atomicAdd(&tile[base + dL], I0 * w01);
+            atomicAdd(&tile[base + dG], I0 * w10);
+            atomicAdd(&tile[base + dG + dL], I0 * w11);
+        }
+        if (own1) {
+            atomicAdd(&tile[base + 1], I1 * w00);
+            atomicAdd(&tile[base + 1 + dL], I1 * w01);
+            atomicAdd(&tile[base + 1 + dG], I1 * w10);
+            atomicAdd(&tile[base + 1 + dG + dL], I1 * w11);
+        }
+    }
+    if (a.in_window && counted) atomicAdd(a.in_window, (unsigned long long)counted);
+    __syncthreads();
+    // flush: every column of the tile is owned by this CTA -> plain stores
+    const int tk4 = (tk + 3) >> 2;
+    const int per_row = a.TK >> 2;
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) {
+        const int node = i / per_row;
+        const int c4 = i - node * per_row;
+        if (c4 < tk4)
+            *reinterpret_cast<float4*>(&a.ldm[node * a.row_stride + k_start + 4 * c4]) = tile4[i];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// K2: forward column FFT (length n1) of packed node pairs, times w_N^{n2 k1}
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(512) k_col_fft_fwd(const ColFftArgs a) {
+    extern __shared__ float2 sm[];
+    const int B = a.B;
+    const int n1 = a.n1;
+    float2* buf0 = sm;
+    float2* buf1 = sm + n1 * B;
+    const int c0 = blockIdx.x * B;
+    const int pair = blockIdx.y;
+    const float* ra = a.ldm + (int64_t)(2 * pair) * a.row_stride;
+    const float* rb = ra + a.row_stride;
+    const int total = n1 * B;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int r = t / B;
+        const int b = t - r * B;
+        const int64_t nidx = (int64_t)r * a.n2 + c0 + b;
+        float2 z = make_float2(0.f, 0.f);
+        if (nidx < a.n_v) z = make_float2(__ldg(&ra[nidx]), __ldg(&rb[nidx]));
+        buf0[t] = z;
+    }
+    __syncthreads();
+    float2* res = fft_batched(buf0, buf1, a.f1, B);
+    float2* y = a.y + (int64_t)pair * a.n1 * a.n2;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int k1 = t / B;
+        const int b = t - k1 * B;
+        const int n2i = c0 + b;
+        float2 z = res[t];
+        if (k1 && n2i) z = cmul(z, twiddle_n(a.tw_hi, a.tw_lo, n2i * k1));
+        y[(int64_t)k1 * a.n2 + n2i] = z;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// K3: row FFT (length n2) of each pair, Voigt-FT weights, sum over pairs
+// ---------------------------------------------------------------------------
+constexpr int kRowThreads = 512;
+constexpr int kMaxAccum = 24;     // n2 <= kRowThreads * kMaxAccum
+
+__device__ __forceinline__ float voigt_node(const VoigtArgs& a, int node, float f) {
+    const int l = node / a.NL;
+    const int m = node - l * a.NL;
+    const float al = a.alpha[l];
+    const float bm = a.beta[m];
+    float v = ex2(-fmaf(al * f, f, bm * f));
+    if (a.any_fold) {
+        const int nf = a.nfold[node];
+        for (int q = 1; q <= nf; ++q) {
+            // alias frequency (broadening.py:1914-1926): q/(2 dv) + (f or 1/(2 dv) - f)
+            const float fq = q * a.half_fs + ((q & 1) ? a.half_fs - f : f);
+            v += ex2(-fmaf(al * fq, fq, bm * fq));
+        }
+    }
+    return v * a.norm[node];
+}
+
+__global__ void __launch_bounds__(kRowThreads) k_row_fft_voigt(const VoigtArgs a) {
+    extern __shared__ float2 sm[];
+    const int n2 = a.n2;
+    float2* buf0 = sm;
+    float2* buf1 = sm + n2;
+    const int k1 = blockIdx.x;
+    const int j0 = blockIdx.y * kPairGroup;
+    const int j1 = min(j0 + kPairGroup, a.n_pairs);
+    float2 acc[kMaxAccum];
+#pragma unroll
+    for (int q = 0; q < kMaxAccum; ++q) acc[q] = make_float2(0.f, 0.f);
+
+    for (int j = j0; j < j1; ++j) {
+        const float4* src = reinterpret_cast<const float4*>(a.y + ((int64_t)j * a.n1 + k1) * n2);
+        float4* dst = reinterpret_cast<float4*>(buf0);
+        for (int t = threadIdx.x; t < n2 / 2; t += blockDim.x) dst[t] = __ldg(&src[t]);
+        __syncthreads();
+        float2* res = fft_batched(buf0, buf1, a.f2, 1);
+#pragma unroll
+        for (int q = 0; q < kMaxAccum; ++q) {
+            const int k2 = threadIdx.x + q * kRowThreads;
+            if (k2 < n2) {
+                const int64_t kk = (int64_t)k1 + (int64_t)a.n1 * k2;
+                const int64_t kf = kk <= a.n - kk ? kk : a.n - kk;
+                const float f = (float)kf * a.inv_ndv;
+                const float va = voigt_node(a, 2 * j, f);
+                const float vb = voigt_node(a, 2 * j + 1, f);
+                const float2 z = res[k2];
+                acc[q].x += z.x * va + z.y * vb;
+                acc[q].y += z.y * va - z.x * vb;
+            }
+        }
+        __syncthreads();
+    }
+    float2* g = a.g + (int64_t)k1 * n2;
+#pragma unroll
+    for (int q = 0; q < kMaxAccum; ++q) {
+        const int k2 = threadIdx.x + q * kRowThreads;
+        if (k2 < n2) atomicAdd(&g[k2], acc[q]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// K3b: inverse row FFT (length n2) and inverse twiddle w_N^{-n2 k1}, in place
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kRowThreads) k_row_ifft(const RowIfftArgs a) {
+    extern __shared__ float2 sm[];
+    const int n2 = a.n2;
+    float2* buf0 = sm;
+    float2* buf1 = sm + n2;
+    const int k1 = blockIdx.x;
+    float2* g = a.g + (int64_t)k1 * n2;
+    for (int t = threadIdx.x; t < n2; t += blockDim.x) buf0[t] = conjf2(g[t]);
+    __syncthreads();
+    // inverse DFT = conj(forward DFT(conj(x)))
+    float2* res = fft_batched(buf0, buf1, a.f2, 1);
+    for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+        float2 z = conjf2(res[t]);
+        if (k1 && t) z = cmul(z, conjf2(twiddle_n(a.tw_hi, a.tw_lo, t * k1)));
+        g[t] = z;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// K4: inverse column FFT (length n1), real part, scaled, first n_v samples
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(512) k_col_ifft(const ColFftArgs a) {
+    extern __shared__ float2 sm[];
+    const int B = a.B;
+    const int n1 = a.n1;
+    float2* buf0 = sm;
+    float2* buf1 = sm + n1 * B;
+    const int c0 = blockIdx.x * B;
+    const int total = n1 * B;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int k1 = t / B;
+        const int b = t - k1 * B;
+        buf0[t] = conjf2(a.h[(int64_t)k1 * a.n2 + c0 + b]);
+    }
+    __syncthreads();
+    float2* res = fft_batched(buf0, buf1, a.f1, B);
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int r = t / B;
+        const int b = t - r * B;
+        const int64_t nidx = (int64_t)r * a.n2 + c0 + b;
+        if (nidx < a.n_v) a.out[nidx] = res[t].x * a.out_scale;   // Re(conj(z)) = Re(z)
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+static int check_launch() {
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? RG_OK : RG_ERR_CUDA;
+}
+
+size_t col_fft_smem(int n1, int B) { return (size_t)2 * n1 * B * sizeof(float2); }
+size_t row_fft_smem(int n2) { return (size_t)2 * n2 * sizeof(float2); }
+
+int launch_prepare_lines(const double* v0_d, const double* s_d, int64_t n, double c2_tref, float2* v0_out,
+                         float* ls2_out, int* unsorted_flag, cudaStream_t st) {
+    if (n <= 0) return RG_OK;
+    int64_t blocks = (n + 255) / 256;
+    k_prepare_lines<<<(unsigned)blocks, 256, 0, st>>>(v0_d, s_d, n, c2_tref, v0_out, ls2_out, unsorted_flag);
+    return check_launch();
+}
+
+int launch_col_index(const float2* v0, int64_t n, double vmin, double dv, int c_min, int count,
+                     int64_t* col_start, cudaStream_t st) {
+    k_col_index<<<(count + 255) / 256, 256, 0, st>>>(v0, n, vmin, dv, c_min, count, col_start);
+    return check_launch();
+}
+
+int launch_scatter(const ScatterArgs& a, int n_tiles, size_t smem, cudaStream_t st) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr_set = true;
+    }
+    k_scatter<<<n_tiles, 1024, smem, st>>>(a);
+    return check_launch();
+}
+
+int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_col_fft_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr_set = true;
+    }
+    dim3 grid(a.n2 / a.B, a.n_pairs);
+    k_col_fft_fwd<<<grid, 512, col_fft_smem(a.n1, a.B), st>>>(a);
+    return check_launch();
+}
+
+int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_row_fft_voigt, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr_set = true;
+    }
+    if (a.n2 > kRowThreads * kMaxAccum) return RG_ERR_RANGE;
+    dim3 grid(a.n1, (a.n_pairs + kPairGroup - 1) / kPairGroup);
+    k_row_fft_voigt<<<grid, kRowThreads, row_fft_smem(a.n2), st>>>(a);
+    return check_launch();
+}
+
+int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_row_ifft, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr_set = true;
+    }
+    k_row_ifft<<<a.n1, kRowThreads, row_fft_smem(a.n2), st>>>(a);
+    return check_launch();
+}
+
+int launch_col_ifft(const ColFftArgs& a, cudaStream_t st) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_col_ifft, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr_set = true;
+    }
+    k_col_ifft<<<a.n2 / a.B, 512, col_fft_smem(a.n1, a.B), st>>>(a);
+    return check_launch();
+}
+
+}  // namespace rg
