@@ -432,8 +432,16 @@ int build_scatter_args(rg_plan* P, const rg_conditions* c, const SpecHost& s, Sc
     a->x_self = (float)c->x;
     const double T = c->T;
     a->lgG_scale = (float)(kLn2 / g.dxG);
+    double lv_lo = std::numeric_limits<double>::infinity(), lv_hi = -lv_lo;
     for (int i = 0; i < L->n_iso; ++i)
-        a->cG[i] = (float)((L->env.log_c2Mm[i] + 0.5 * std::log(T) - g.log_wG_min) / g.dxG);
+        if (L->env.lv_min[i] <= L->env.lv_max[i]) {
+            lv_lo = std::min(lv_lo, L->env.lv_min[i]);
+            lv_hi = std::max(lv_hi, L->env.lv_max[i]);
+        }
+    const double lv_ref = 0.5 * (lv_lo + lv_hi);
+    a->inv_vref = (float)std::exp(-lv_ref);
+    for (int i = 0; i < L->n_iso; ++i)
+        a->cG[i] = (float)((lv_ref + L->env.log_c2Mm[i] + 0.5 * std::log(T) - g.log_wG_min) / g.dxG);
     a->lgL_scale = (float)(kLn2 / g.dxL);
     a->tL = (float)(std::log(L->t_ref / T) / g.dxL);
     a->cL = (float)((std::log(2.0 * s.p_atm) - g.log_wL_min) / g.dxL);

@@ -91,7 +91,8 @@ struct ScatterArgs {
     float p_atm;
     float x_self;
     float lgG_scale;          // ln2 / dxG
-    float cG[kMaxIso];        // (log_c2Mm[iso] + 0.5 log T - log_wG_min) / dxG
+    float inv_vref;           // 1 / v_ref (v_ref: geometric middle of the list's v0 range)
+    float cG[kMaxIso];        // (log v_ref + log_c2Mm[iso] + 0.5 log T - log_wG_min) / dxG
     float lgL_scale;          // ln2 / dxL
     float tL;                 // log(Tref/T) / dxL
     float cL;                 // (log(2 p_atm) - log_wL_min) / dxL

@@ -269,7 +269,8 @@ __global__ void __launch_bounds__(1024) k_scatter(const ScatterArgs a) {
         if (own0) ++counted;
         const int is = a.iso ? (int)a.iso[i] : 0;
         // Gaussian / Lorentzian node coordinates (FWHM, log space)
-        const float pl = fmaf(lg2(v.x), a.lgG_scale, a.cG[is]);
+        // log v0 relative to v_ref keeps the FP32 log and the offset free of cancellation
+        const float pl = fmaf(lg2(v.x * a.inv_vref), a.lgG_scale, a.cG[is]);
         const float ga = a.ga[i];
         const float gam = fmaf(a.x_self, a.gs[i] - ga, ga);
         const float pm = fmaf(lg2(gam), a.lgL_scale, fmaf(a.na[i], a.tL, a.cL));
