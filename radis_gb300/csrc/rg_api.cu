@@ -173,7 +173,7 @@ constexpr int kN2Max = 512 * 24;   // row FFT limit (threads x accumulators)
 bool choose_fft(int64_t n_min, int64_t forced, int* n1o, int* n2o) {
     int64_t best = std::numeric_limits<int64_t>::max();
     int b1 = 0, b2 = 0;
-    for (int n1 = 512; n1 >= 8; n1 /= 2) {
+    for (int n1 : {512, 64, 8}) {   // radix-8 register column FFTs
         int64_t n2;
         if (forced) {
             if (forced % n1) continue;
@@ -218,6 +218,12 @@ int upload_twiddles(int L, float2** out) {
 int make_fftlen(int L, FftLen* f) {
     f->L = L;
     if (!radices(L, f->radix, &f->npass)) return fail(RG_ERR_RANGE, "FFT length %d not factorable", L);
+    int ns = 1;
+    for (int p = 0; p < f->npass; ++p) {
+        f->ns[p] = ns;
+        f->mag[p] = ns == 1 ? 0u : (unsigned)(((1ull << 32) + ns - 1) / (unsigned long long)ns);
+        ns *= f->radix[p];
+    }
     return upload_twiddles(L, &f->tw);
 }
 
@@ -392,11 +398,13 @@ int ensure_workspace(rg_plan* P, int n_nodes) {
     return RG_OK;
 }
 
+// Columns per scatter tile: a multiple of 32 (the bank swizzle works inside
+// 32-column groups), sized for two CTAs per SM when the node count allows.
 int scatter_tile(int n_nodes) {
-    const int budget = 200 * 1024;
-    int tk = budget / (4 * n_nodes);
-    tk = (tk / 8) * 8;
-    return std::min(tk, 2048);
+    const int budget2 = 110 * 1024, budget1 = 220 * 1024;
+    int tk = budget2 / (4 * n_nodes) / 32 * 32;
+    if (tk < 32) tk = budget1 / (4 * n_nodes) / 32 * 32;
+    return std::min(tk, 1024);
 }
 
 int build_scatter_args(rg_plan* P, const rg_conditions* c, const SpecHost& s, ScatterArgs* a) {
@@ -421,7 +429,7 @@ int build_scatter_args(rg_plan* P, const rg_conditions* c, const SpecHost& s, Sc
     a->row_stride = P->row_stride;
     a->ldm = P->ldm;
     a->TK = scatter_tile(s.n_nodes);
-    if (a->TK < 8) return fail(RG_ERR_RANGE, "LDM grid of %d nodes does not fit a shared-memory tile", s.n_nodes);
+    if (a->TK < 32) return fail(RG_ERR_RANGE, "LDM grid of %d nodes does not fit a shared-memory tile", s.n_nodes);
     if (s.p_atm > P->p_atm_max)
         return fail(RG_ERR_RANGE, "pressure %g atm above the plan's shift-index limit %g atm", s.p_atm,
                     P->p_atm_max);
@@ -485,7 +493,7 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
     RG(build_scatter_args(P, c, s, &sa));
     const int n_v = (int)P->desc.n_v;
     const int n_tiles = (n_v + sa.TK - 1) / sa.TK;
-    const size_t smem = (size_t)s.n_nodes * sa.TK * sizeof(float);
+    const size_t smem = scatter_smem_floats(s.n_nodes, sa.TK) * sizeof(float);
     cudaEvent_t* ev = P->ev;
     if (timing == 2) {
         if (P->ring.empty()) {
@@ -781,7 +789,7 @@ int rg_plan_create(rg_lines* L, const rg_plan_desc* d, rg_plan** out) {
     P->n1 = n1;
     P->n2 = n2;
     P->n = (int64_t)n1 * n2;
-    P->B = std::min(32, 8192 / n1);
+    P->B = col_block(n1);
     RG(make_fftlen(n1, &P->f1));
     RG(make_fftlen(n2, &P->f2));
     {

@@ -34,7 +34,7 @@ constexpr double kAtm = 1.01325;                    // bar per atm (broadening.p
 constexpr int kMaxIso = 16;
 constexpr int kMaxAxis = 64;        // max nodes along one LDM axis
 constexpr int kMaxNodes = 1024;     // max N_G * N_L (padded to even)
-constexpr int kPairGroup = 8;       // node pairs per Voigt-reduce work item
+constexpr int kPairGroup = 16;      // node pairs per Voigt-reduce work item
 constexpr int kMaxPasses = 16;
 
 // --- host-side convex envelopes (rg_hull.cpp) ---------------------------------
@@ -63,6 +63,8 @@ struct FftLen {
     int L = 0;
     int npass = 0;
     int radix[kMaxPasses] = {0};
+    int ns[kMaxPasses] = {0};          // sub-transform length before each pass
+    unsigned mag[kMaxPasses] = {0};    // ceil(2^32 / ns): j / ns == umulhi(j, mag) for j, ns < 2^16
     float2* tw = nullptr;       // device: exp(-2 pi i t / L), t < L
 };
 
@@ -156,7 +158,7 @@ int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st);
 int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st);
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st);
 int launch_col_ifft(const ColFftArgs& a, cudaStream_t st);
-size_t col_fft_smem(int n1, int B);
-size_t row_fft_smem(int n2);
+int col_block(int n1);               // columns per CTA of the column FFTs
+size_t scatter_smem_floats(int n_nodes, int TK);
 
 }  // namespace rg

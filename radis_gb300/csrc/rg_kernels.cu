@@ -126,57 +126,128 @@ __device__ __forceinline__ void dftR(float2* v) {
     if (R == 8) dft8(v);
 }
 
-// One Stockham autosort pass over B interleaved transforms of length L
-// (element i of transform b at [i * B + b]).  Pass with radix R after
-// sub-transforms of length Ns: butterfly j reads in[j + r L/R], twiddles by
-// w_{Ns R}^{r (j mod Ns)}, and writes out[(j / Ns) Ns R + (j mod Ns) + r Ns].
+// Multiply v[1..R-1] by w^r, w = tw[s] (tw[t] = exp(-2 pi i t / L)); three
+// table reads at most, the other powers by complex products.
 template <int R>
-__device__ __forceinline__ void stockham_pass(const float2* __restrict__ in, float2* __restrict__ out,
-                                              int L, int B, int Ns, const float2* __restrict__ tw) {
-    const int M = L / R;
-    const int total = M * B;
-    const int twstep = L / (Ns * R);
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int j = t / B;
-        const int b = t - j * B;
-        const int k = j % Ns;
-        float2 v[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = in[(j + r * M) * B + b];
-        if (Ns > 1) {
-            const int s = k * twstep;
-#pragma unroll
-            for (int r = 1; r < R; ++r) v[r] = cmul(v[r], __ldg(&tw[r * s]));
-        }
-        dftR<R>(v);
-        const int base = (j - k) * R + k;
-#pragma unroll
-        for (int r = 0; r < R; ++r) out[(base + r * Ns) * B + b] = v[r];
+__device__ __forceinline__ void twiddle(float2* v, const float2* __restrict__ tw, int s) {
+    const float2 w1 = __ldg(&tw[s]);
+    if (R == 2) {
+        v[1] = cmul(v[1], w1);
+    } else if (R == 3) {
+        v[1] = cmul(v[1], w1);
+        v[2] = cmul(v[2], __ldg(&tw[2 * s]));
+    } else if (R == 4) {
+        const float2 w2 = __ldg(&tw[2 * s]);
+        v[1] = cmul(v[1], w1);
+        v[2] = cmul(v[2], w2);
+        v[3] = cmul(v[3], cmul(w1, w2));
+    } else if (R == 5) {
+        const float2 w2 = __ldg(&tw[2 * s]);
+        v[1] = cmul(v[1], w1);
+        v[2] = cmul(v[2], w2);
+        v[3] = cmul(v[3], cmul(w1, w2));
+        v[4] = cmul(v[4], cmul(w2, w2));
+    } else {
+        const float2 w2 = __ldg(&tw[2 * s]);
+        const float2 w4 = __ldg(&tw[4 * s]);
+        const float2 w3 = cmul(w1, w2);
+        v[1] = cmul(v[1], w1);
+        v[2] = cmul(v[2], w2);
+        v[3] = cmul(v[3], w3);
+        v[4] = cmul(v[4], w4);
+        v[5] = cmul(v[5], cmul(w1, w4));
+        v[6] = cmul(v[6], cmul(w2, w4));
+        v[7] = cmul(v[7], cmul(w3, w4));
     }
 }
 
-// Forward DFT of B interleaved transforms; buf0 holds the input.  Returns the
-// buffer that holds the result.  Ends with __syncthreads().
-__device__ float2* fft_batched(float2* buf0, float2* buf1, const FftLen& P, int B) {
+// One Stockham autosort pass over a single transform of length L held in
+// shared memory (sub-transforms of length Ns before the pass): butterfly j
+// reads in[j + r L/R], twiddles by w_{Ns R}^{r (j mod Ns)} and writes
+// out[(j / Ns) Ns R + (j mod Ns) + r Ns].
+template <int R>
+__device__ __forceinline__ void row_pass(const float2* __restrict__ in, float2* __restrict__ out, int L,
+                                         int Ns, unsigned mag, const float2* __restrict__ tw) {
+    const int M = L / R;
+    const int twstep = L / (Ns * R);
+    for (int j = threadIdx.x; j < M; j += blockDim.x) {
+        const int q = Ns == 1 ? j : (int)__umulhi((unsigned)j, mag);
+        const int k = j - q * Ns;
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = in[j + r * M];
+        if (Ns > 1) twiddle<R>(v, tw, k * twstep);
+        dftR<R>(v);
+        const int base = q * Ns * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) out[base + r * Ns] = v[r];
+    }
+}
+
+// Forward DFT of one row in shared memory; buf0 holds the input.  Returns the
+// buffer holding the result.  Ends with __syncthreads().
+__device__ float2* fft_row(float2* buf0, float2* buf1, const FftLen& P) {
     float2* in = buf0;
     float2* out = buf1;
-    int Ns = 1;
     for (int p = 0; p < P.npass; ++p) {
         const int R = P.radix[p];
+        const int Ns = P.ns[p];
+        const unsigned mag = P.mag[p];
         switch (R) {
-            case 2: stockham_pass<2>(in, out, P.L, B, Ns, P.tw); break;
-            case 3: stockham_pass<3>(in, out, P.L, B, Ns, P.tw); break;
-            case 4: stockham_pass<4>(in, out, P.L, B, Ns, P.tw); break;
-            case 5: stockham_pass<5>(in, out, P.L, B, Ns, P.tw); break;
-            default: stockham_pass<8>(in, out, P.L, B, Ns, P.tw); break;
+            case 2: row_pass<2>(in, out, P.L, Ns, mag, P.tw); break;
+            case 3: row_pass<3>(in, out, P.L, Ns, mag, P.tw); break;
+            case 4: row_pass<4>(in, out, P.L, Ns, mag, P.tw); break;
+            case 5: row_pass<5>(in, out, P.L, Ns, mag, P.tw); break;
+            default: row_pass<8>(in, out, P.L, Ns, mag, P.tw); break;
         }
         __syncthreads();
         float2* t = in;
         in = out;
         out = t;
-        Ns *= R;
     }
     return in;
+}
+
+// Column FFT of length N1 in {8, 64, 512} = 8^d, B columns per CTA, N1/8
+// threads per column, one radix-8 butterfly per thread and pass with the
+// eight values in registers; passes exchange through one shared buffer
+// [N1][B].  On entry v[q] = x[j + q N1/8] of column b; on return
+// v[r] = X[j + r N1/8].
+template <int N1>
+struct ColShape {
+    static constexpr int TPC = N1 / 8;
+    static constexpr int B = N1 == 512 ? 16 : 32;
+    static constexpr int THREADS = TPC * B;
+};
+
+template <int N1>
+__device__ __forceinline__ void col_fft8(float2 (&v)[8], float2* sm, int j, int b,
+                                         const float2* __restrict__ tw1) {
+    constexpr int TPC = ColShape<N1>::TPC;
+    constexpr int B = ColShape<N1>::B;
+    dft8(v);
+    if constexpr (N1 > 8) {
+        // pass 1 (Ns = 1) writes out[8 j + r]
+#pragma unroll
+        for (int r = 0; r < 8; ++r) sm[(8 * j + r) * B + b] = v[r];
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < 8; ++r) v[r] = sm[(j + r * TPC) * B + b];
+        const int k = j & 7;
+        twiddle<8>(v, tw1, (N1 / 64) * k);      // w_64^{r k}
+        dft8(v);
+        if constexpr (N1 > 64) {
+            __syncthreads();
+            // pass 2 (Ns = 8) writes out[(j - k) 8 + k + 8 r]
+#pragma unroll
+            for (int r = 0; r < 8; ++r) sm[((j - k) * 8 + k + 8 * r) * B + b] = v[r];
+            __syncthreads();
+#pragma unroll
+            for (int r = 0; r < 8; ++r) v[r] = sm[(j + r * TPC) * B + b];
+            twiddle<8>(v, tw1, j);              // w_512^{r j}
+            dft8(v);
+        }
+    }
 }
 
 // exp(-2 pi i t / N) from a two-level table (t = hi * 1024 + lo)
@@ -227,7 +298,13 @@ __global__ void k_col_index(const float2* __restrict__ v0, int64_t n, double vmi
 // ---------------------------------------------------------------------------
 // K1: fused line scaling + LDM scatter into a shared-memory tile
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(1024) k_scatter(const ScatterArgs a) {
+// Tile layout [node][TK] with the column XOR-swizzled by (node & 7) << 2: lanes
+// of a warp hold neighbouring (sorted) lines, i.e. the same few columns, so
+// without the swizzle their atomics would pile onto the same banks.  The XOR
+// keeps aligned groups of four columns together for the float4 flush.
+__device__ __forceinline__ int tile_addr(int node, int c, int TK) { return node * TK + (c ^ ((node & 7) << 2)); }
+
+__global__ void __launch_bounds__(512, 2) k_scatter(const ScatterArgs a) {
     extern __shared__ float4 tile4[];
     float* tile = reinterpret_cast<float*>(tile4);
     const int k_start = blockIdx.x * a.TK;
@@ -242,10 +319,9 @@ __global__ void __launch_bounds__(1024) k_scatter(const ScatterArgs a) {
     c_hi = max(0, min(c_hi, a.col_count - 1));
     const int64_t i0 = a.col_start[c_lo];
     const int64_t i1 = a.col_start[c_hi];
-    const int dL = a.TK;
-    const int dG = a.NL * a.TK;
     unsigned int counted = 0;
 
+#pragma unroll 2
     for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
         const float2 v = a.v0[i];
         const float shift = a.dl ? a.dl[i] * a.p_atm : 0.f;
@@ -268,8 +344,8 @@ __global__ void __launch_bounds__(1024) k_scatter(const ScatterArgs a) {
         if (!(own0 || own1)) continue;
         if (own0) ++counted;
         const int is = a.iso ? (int)a.iso[i] : 0;
-        // Gaussian / Lorentzian node coordinates (FWHM, log space)
-        // log v0 relative to v_ref keeps the FP32 log and the offset free of cancellation
+        // Gaussian / Lorentzian node coordinates (FWHM, log space); log v0 is
+        // taken relative to v_ref so the FP32 log and offset do not cancel
         const float pl = fmaf(lg2(v.x * a.inv_vref), a.lgG_scale, a.cG[is]);
         const float ga = a.ga[i];
         const float gam = fmaf(a.x_self, a.gs[i] - ga, ga);
@@ -278,7 +354,7 @@ __global__ void __launch_bounds__(1024) k_scatter(const ScatterArgs a) {
         const int m0 = min(max((int)floorf(pm), 0), a.NL - 2);
         const float tG = pl - (float)l0;
         const float tL = pm - (float)m0;
-        // intensity: exponent log2(S_ref) + a_T El + b_iso in double-float
+        // intensity: exponent log2(S') + a_T El + b_iso in double-float
         const float el = a.el[i];
         const float ph = el * a.aT_hi;
         const float pe2 = fmaf(el, a.aT_hi, -ph) + el * a.aT_lo;
@@ -293,18 +369,19 @@ __global__ void __launch_bounds__(1024) k_scatter(const ScatterArgs a) {
         const float w10 = tG - w11;          // tG (1 - tL)
         const float w01 = tL - w11;          // (1 - tG) tL
         const float w00 = 1.f - tG - w01;    // (1 - tG)(1 - tL)
-        const int base = (l0 * a.NL + m0) * a.TK + c0;
+        const int n00 = l0 * a.NL + m0;
+        const int n10 = n00 + a.NL;
         if (own0) {
-            atomicAdd(&tile[base], I0 * w00);
-            atomicAdd(&tile[base + dL], I0 * w01);
-            atomicAdd(&tile[base + dG], I0 * w10);
-            atomicAdd(&tile[base + dG + dL], I0 * w11);
+            atomicAdd(&tile[tile_addr(n00, c0, a.TK)], I0 * w00);
+            atomicAdd(&tile[tile_addr(n00 + 1, c0, a.TK)], I0 * w01);
+            atomicAdd(&tile[tile_addr(n10, c0, a.TK)], I0 * w10);
+            atomicAdd(&tile[tile_addr(n10 + 1, c0, a.TK)], I0 * w11);
         }
         if (own1) {
-            atomicAdd(&tile[base + 1], I1 * w00);
-            atomicAdd(&tile[base + 1 + dL], I1 * w01);
-            atomicAdd(&tile[base + 1 + dG], I1 * w10);
-            atomicAdd(&tile[base + 1 + dG + dL], I1 * w11);
+            atomicAdd(&tile[tile_addr(n00, c0 + 1, a.TK)], I1 * w00);
+            atomicAdd(&tile[tile_addr(n00 + 1, c0 + 1, a.TK)], I1 * w01);
+            atomicAdd(&tile[tile_addr(n10, c0 + 1, a.TK)], I1 * w10);
+            atomicAdd(&tile[tile_addr(n10 + 1, c0 + 1, a.TK)], I1 * w11);
         }
     }
     if (a.in_window && counted) atomicAdd(a.in_window, (unsigned long long)counted);
@@ -316,40 +393,38 @@ __global__ void __launch_bounds__(1024) k_scatter(const ScatterArgs a) {
         const int node = i / per_row;
         const int c4 = i - node * per_row;
         if (c4 < tk4)
-            *reinterpret_cast<float4*>(&a.ldm[node * a.row_stride + k_start + 4 * c4]) = tile4[i];
+            *reinterpret_cast<float4*>(&a.ldm[node * a.row_stride + k_start + 4 * c4]) =
+                tile4[node * per_row + (c4 ^ (node & 7))];
     }
 }
 
 // ---------------------------------------------------------------------------
 // K2: forward column FFT (length n1) of packed node pairs, times w_N^{n2 k1}
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(512) k_col_fft_fwd(const ColFftArgs a) {
+template <int N1>
+__global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_fft_fwd(const ColFftArgs a) {
+    constexpr int TPC = ColShape<N1>::TPC;
+    constexpr int B = ColShape<N1>::B;
     extern __shared__ float2 sm[];
-    const int B = a.B;
-    const int n1 = a.n1;
-    float2* buf0 = sm;
-    float2* buf1 = sm + n1 * B;
+    const int b = threadIdx.x % B;
+    const int j = threadIdx.x / B;
     const int c0 = blockIdx.x * B;
     const int pair = blockIdx.y;
     const float* ra = a.ldm + (int64_t)(2 * pair) * a.row_stride;
     const float* rb = ra + a.row_stride;
-    const int total = n1 * B;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int r = t / B;
-        const int b = t - r * B;
-        const int64_t nidx = (int64_t)r * a.n2 + c0 + b;
-        float2 z = make_float2(0.f, 0.f);
-        if (nidx < a.n_v) z = make_float2(__ldg(&ra[nidx]), __ldg(&rb[nidx]));
-        buf0[t] = z;
+    const int n2i = c0 + b;
+    float2 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int64_t nidx = (int64_t)(j + q * TPC) * a.n2 + n2i;
+        v[q] = nidx < a.n_v ? make_float2(__ldg(&ra[nidx]), __ldg(&rb[nidx])) : make_float2(0.f, 0.f);
     }
-    __syncthreads();
-    float2* res = fft_batched(buf0, buf1, a.f1, B);
-    float2* y = a.y + (int64_t)pair * a.n1 * a.n2;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int k1 = t / B;
-        const int b = t - k1 * B;
-        const int n2i = c0 + b;
-        float2 z = res[t];
+    col_fft8<N1>(v, sm, j, b, a.f1.tw);
+    float2* y = a.y + (int64_t)pair * N1 * a.n2;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int k1 = j + r * TPC;
+        float2 z = v[r];
         if (k1 && n2i) z = cmul(z, twiddle_n(a.tw_hi, a.tw_lo, n2i * k1));
         y[(int64_t)k1 * a.n2 + n2i] = z;
     }
@@ -358,24 +433,32 @@ __global__ void __launch_bounds__(512) k_col_fft_fwd(const ColFftArgs a) {
 // ---------------------------------------------------------------------------
 // K3: row FFT (length n2) of each pair, Voigt-FT weights, sum over pairs
 // ---------------------------------------------------------------------------
-constexpr int kRowThreads = 512;
-constexpr int kMaxAccum = 24;     // n2 <= kRowThreads * kMaxAccum
+constexpr int kRowThreads = 256;
 
-__device__ __forceinline__ float voigt_node(const VoigtArgs& a, int node, float f) {
+struct NodeV {
+    float al, bm, nrm;
+    int nf;
+};
+
+__device__ __forceinline__ NodeV node_params(const VoigtArgs& a, int node) {
     const int l = node / a.NL;
     const int m = node - l * a.NL;
-    const float al = a.alpha[l];
-    const float bm = a.beta[m];
-    float v = ex2(-fmaf(al * f, f, bm * f));
-    if (a.any_fold) {
-        const int nf = a.nfold[node];
-        for (int q = 1; q <= nf; ++q) {
-            // alias frequency (broadening.py:1914-1926): q/(2 dv) + (f or 1/(2 dv) - f)
-            const float fq = q * a.half_fs + ((q & 1) ? a.half_fs - f : f);
-            v += ex2(-fmaf(al * fq, fq, bm * fq));
-        }
+    NodeV n;
+    n.al = a.alpha[l];
+    n.bm = a.beta[m];
+    n.nrm = a.norm[node];
+    n.nf = a.any_fold ? (int)a.nfold[node] : 0;
+    return n;
+}
+
+__device__ __forceinline__ float voigt_eval(const NodeV& n, float f, float half_fs) {
+    float v = ex2(-fmaf(n.al * f, f, n.bm * f));
+    for (int q = 1; q <= n.nf; ++q) {
+        // alias frequency (broadening.py:1914-1926): q/(2 dv) + (f or 1/(2 dv) - f)
+        const float fq = q * half_fs + ((q & 1) ? half_fs - f : f);
+        v += ex2(-fmaf(n.al * fq, fq, n.bm * fq));
     }
-    return v * a.norm[node];
+    return v * n.nrm;
 }
 
 __global__ void __launch_bounds__(kRowThreads) k_row_fft_voigt(const VoigtArgs a) {
@@ -383,41 +466,37 @@ __global__ void __launch_bounds__(kRowThreads) k_row_fft_voigt(const VoigtArgs a
     const int n2 = a.n2;
     float2* buf0 = sm;
     float2* buf1 = sm + n2;
+    float2* acc = sm + 2 * n2;
     const int k1 = blockIdx.x;
     const int j0 = blockIdx.y * kPairGroup;
     const int j1 = min(j0 + kPairGroup, a.n_pairs);
-    float2 acc[kMaxAccum];
-#pragma unroll
-    for (int q = 0; q < kMaxAccum; ++q) acc[q] = make_float2(0.f, 0.f);
+    // each thread owns bins t = threadIdx.x + i blockDim.x of acc: no sync needed
+    for (int t = threadIdx.x; t < n2; t += blockDim.x) acc[t] = make_float2(0.f, 0.f);
 
     for (int j = j0; j < j1; ++j) {
         const float4* src = reinterpret_cast<const float4*>(a.y + ((int64_t)j * a.n1 + k1) * n2);
         float4* dst = reinterpret_cast<float4*>(buf0);
         for (int t = threadIdx.x; t < n2 / 2; t += blockDim.x) dst[t] = __ldg(&src[t]);
         __syncthreads();
-        float2* res = fft_batched(buf0, buf1, a.f2, 1);
-#pragma unroll
-        for (int q = 0; q < kMaxAccum; ++q) {
-            const int k2 = threadIdx.x + q * kRowThreads;
-            if (k2 < n2) {
-                const int64_t kk = (int64_t)k1 + (int64_t)a.n1 * k2;
-                const int64_t kf = kk <= a.n - kk ? kk : a.n - kk;
-                const float f = (float)kf * a.inv_ndv;
-                const float va = voigt_node(a, 2 * j, f);
-                const float vb = voigt_node(a, 2 * j + 1, f);
-                const float2 z = res[k2];
-                acc[q].x += z.x * va + z.y * vb;
-                acc[q].y += z.y * va - z.x * vb;
-            }
+        const float2* res = fft_row(buf0, buf1, a.f2);
+        const NodeV na = node_params(a, 2 * j);
+        const NodeV nb = node_params(a, 2 * j + 1);
+        for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+            const int64_t kk = (int64_t)k1 + (int64_t)a.n1 * t;
+            const int64_t kf = kk <= a.n - kk ? kk : a.n - kk;
+            const float f = (float)kf * a.inv_ndv;
+            const float va = voigt_eval(na, f, a.half_fs);
+            const float vb = voigt_eval(nb, f, a.half_fs);
+            const float2 z = res[t];
+            float2 c = acc[t];
+            c.x += z.x * va + z.y * vb;
+            c.y += z.y * va - z.x * vb;
+            acc[t] = c;
         }
         __syncthreads();
     }
     float2* g = a.g + (int64_t)k1 * n2;
-#pragma unroll
-    for (int q = 0; q < kMaxAccum; ++q) {
-        const int k2 = threadIdx.x + q * kRowThreads;
-        if (k2 < n2) atomicAdd(&g[k2], acc[q]);
-    }
+    for (int t = threadIdx.x; t < n2; t += blockDim.x) atomicAdd(&g[t], acc[t]);
 }
 
 // ---------------------------------------------------------------------------
@@ -433,7 +512,7 @@ __global__ void __launch_bounds__(kRowThreads) k_row_ifft(const RowIfftArgs a) {
     for (int t = threadIdx.x; t < n2; t += blockDim.x) buf0[t] = conjf2(g[t]);
     __syncthreads();
     // inverse DFT = conj(forward DFT(conj(x)))
-    float2* res = fft_batched(buf0, buf1, a.f2, 1);
+    const float2* res = fft_row(buf0, buf1, a.f2);
     for (int t = threadIdx.x; t < n2; t += blockDim.x) {
         float2 z = conjf2(res[t]);
         if (k1 && t) z = cmul(z, conjf2(twiddle_n(a.tw_hi, a.tw_lo, t * k1)));
@@ -444,26 +523,22 @@ __global__ void __launch_bounds__(kRowThreads) k_row_ifft(const RowIfftArgs a) {
 // ---------------------------------------------------------------------------
 // K4: inverse column FFT (length n1), real part, scaled, first n_v samples
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(512) k_col_ifft(const ColFftArgs a) {
+template <int N1>
+__global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_ifft(const ColFftArgs a) {
+    constexpr int TPC = ColShape<N1>::TPC;
+    constexpr int B = ColShape<N1>::B;
     extern __shared__ float2 sm[];
-    const int B = a.B;
-    const int n1 = a.n1;
-    float2* buf0 = sm;
-    float2* buf1 = sm + n1 * B;
-    const int c0 = blockIdx.x * B;
-    const int total = n1 * B;
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int k1 = t / B;
-        const int b = t - k1 * B;
-        buf0[t] = conjf2(a.h[(int64_t)k1 * a.n2 + c0 + b]);
-    }
-    __syncthreads();
-    float2* res = fft_batched(buf0, buf1, a.f1, B);
-    for (int t = threadIdx.x; t < total; t += blockDim.x) {
-        const int r = t / B;
-        const int b = t - r * B;
-        const int64_t nidx = (int64_t)r * a.n2 + c0 + b;
-        if (nidx < a.n_v) a.out[nidx] = res[t].x * a.out_scale;   // Re(conj(z)) = Re(z)
+    const int b = threadIdx.x % B;
+    const int j = threadIdx.x / B;
+    const int n2i = blockIdx.x * B + b;
+    float2 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = conjf2(a.h[(int64_t)(j + q * TPC) * a.n2 + n2i]);
+    col_fft8<N1>(v, sm, j, b, a.f1.tw);
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int64_t nidx = (int64_t)(j + r * TPC) * a.n2 + n2i;
+        if (nidx < a.n_v) a.out[nidx] = v[r].x * a.out_scale;   // Re(conj(z)) = Re(z)
     }
 }
 
@@ -475,8 +550,23 @@ static int check_launch() {
     return e == cudaSuccess ? RG_OK : RG_ERR_CUDA;
 }
 
-size_t col_fft_smem(int n1, int B) { return (size_t)2 * n1 * B * sizeof(float2); }
-size_t row_fft_smem(int n2) { return (size_t)2 * n2 * sizeof(float2); }
+int col_block(int n1) {
+    switch (n1) {
+        case 8: return ColShape<8>::B;
+        case 64: return ColShape<64>::B;
+        default: return ColShape<512>::B;
+    }
+}
+
+size_t scatter_smem_floats(int n_nodes, int TK) { return (size_t)n_nodes * TK; }
+
+template <typename K>
+static void allow_smem(K kernel, bool& done) {
+    if (!done) {
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        done = true;
+    }
+}
 
 int launch_prepare_lines(const double* v0_d, const double* s_d, int64_t n, double c2_tref, float2* v0_out,
                          float* ls2_out, int* unsorted_flag, cudaStream_t st) {
@@ -493,56 +583,60 @@ int launch_col_index(const float2* v0, int64_t n, double vmin, double dv, int c_
 }
 
 int launch_scatter(const ScatterArgs& a, int n_tiles, size_t smem, cudaStream_t st) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr_set = true;
-    }
-    k_scatter<<<n_tiles, 1024, smem, st>>>(a);
+    static bool done = false;
+    allow_smem(k_scatter, done);
+    k_scatter<<<n_tiles, 512, smem, st>>>(a);
+    return check_launch();
+}
+
+template <int N1>
+static int col_fwd(const ColFftArgs& a, cudaStream_t st) {
+    static bool done = false;
+    allow_smem(k_col_fft_fwd<N1>, done);
+    dim3 grid(a.n2 / ColShape<N1>::B, a.n_pairs);
+    k_col_fft_fwd<N1><<<grid, ColShape<N1>::THREADS, N1 * ColShape<N1>::B * sizeof(float2), st>>>(a);
     return check_launch();
 }
 
 int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_col_fft_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr_set = true;
+    switch (a.n1) {
+        case 8: return col_fwd<8>(a, st);
+        case 64: return col_fwd<64>(a, st);
+        case 512: return col_fwd<512>(a, st);
+        default: return RG_ERR_RANGE;
     }
-    dim3 grid(a.n2 / a.B, a.n_pairs);
-    k_col_fft_fwd<<<grid, 512, col_fft_smem(a.n1, a.B), st>>>(a);
-    return check_launch();
 }
 
 int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_row_fft_voigt, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr_set = true;
-    }
-    if (a.n2 > kRowThreads * kMaxAccum) return RG_ERR_RANGE;
+    static bool done = false;
+    allow_smem(k_row_fft_voigt, done);
     dim3 grid(a.n1, (a.n_pairs + kPairGroup - 1) / kPairGroup);
-    k_row_fft_voigt<<<grid, kRowThreads, row_fft_smem(a.n2), st>>>(a);
+    k_row_fft_voigt<<<grid, kRowThreads, 3 * (size_t)a.n2 * sizeof(float2), st>>>(a);
     return check_launch();
 }
 
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_row_ifft, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr_set = true;
-    }
-    k_row_ifft<<<a.n1, kRowThreads, row_fft_smem(a.n2), st>>>(a);
+    static bool done = false;
+    allow_smem(k_row_ifft, done);
+    k_row_ifft<<<a.n1, kRowThreads, 2 * (size_t)a.n2 * sizeof(float2), st>>>(a);
+    return check_launch();
+}
+
+template <int N1>
+static int col_inv(const ColFftArgs& a, cudaStream_t st) {
+    static bool done = false;
+    allow_smem(k_col_ifft<N1>, done);
+    k_col_ifft<N1><<<a.n2 / ColShape<N1>::B, ColShape<N1>::THREADS, N1 * ColShape<N1>::B * sizeof(float2), st>>>(a);
     return check_launch();
 }
 
 int launch_col_ifft(const ColFftArgs& a, cudaStream_t st) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_col_ifft, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr_set = true;
+    switch (a.n1) {
+        case 8: return col_inv<8>(a, st);
+        case 64: return col_inv<64>(a, st);
+        case 512: return col_inv<512>(a, st);
+        default: return RG_ERR_RANGE;
     }
-    k_col_ifft<<<a.n2 / a.B, 512, col_fft_smem(a.n1, a.B), st>>>(a);
-    return check_launch();
 }
 
 }  // namespace rg
