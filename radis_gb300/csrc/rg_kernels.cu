@@ -165,6 +165,12 @@ __device__ __forceinline__ void twiddle(float2* v, const float2* __restrict__ tw
 // shared memory (sub-transforms of length Ns before the pass): butterfly j
 // reads in[j + r L/R], twiddles by w_{Ns R}^{r (j mod Ns)} and writes
 // out[(j / Ns) Ns R + (j mod Ns) + r Ns].
+// Row buffers are padded by one element every 16 (index i lives at
+// rp(i) = i + i/16) so that the stride-R writes of the first pass spread over
+// the banks.
+__device__ __forceinline__ int rp(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int row_buf_len(int n) { return n + (n >> 4) + 1; }
+
 template <int R>
 __device__ __forceinline__ void row_pass(const float2* __restrict__ in, float2* __restrict__ out, int L,
                                          int Ns, unsigned mag, const float2* __restrict__ tw) {
@@ -175,12 +181,12 @@ __device__ __forceinline__ void row_pass(const float2* __restrict__ in, float2* 
         const int k = j - q * Ns;
         float2 v[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = in[j + r * M];
+        for (int r = 0; r < R; ++r) v[r] = in[rp(j + r * M)];
         if (Ns > 1) twiddle<R>(v, tw, k * twstep);
         dftR<R>(v);
         const int base = q * Ns * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) out[base + r * Ns] = v[r];
+        for (int r = 0; r < R; ++r) out[rp(base + r * Ns)] = v[r];
     }
 }
 
@@ -216,7 +222,7 @@ __device__ float2* fft_row(float2* buf0, float2* buf1, const FftLen& P) {
 template <int N1>
 struct ColShape {
     static constexpr int TPC = N1 / 8;
-    static constexpr int B = N1 == 512 ? 16 : 32;
+    static constexpr int B = N1 == 512 ? 8 : 32;
     static constexpr int THREADS = TPC * B;
 };
 
@@ -305,32 +311,60 @@ __global__ void k_col_index(const float2* __restrict__ v0, int64_t n, double vmi
 __device__ __forceinline__ int tile_addr(int node, int c, int TK) { return node * TK + (c ^ ((node & 7) << 2)); }
 
 __global__ void __launch_bounds__(512, 2) k_scatter(const ScatterArgs a) {
-    extern __shared__ float4 tile4[];
-    float* tile = reinterpret_cast<float*>(tile4);
+    // The tile accumulates in 32-bit fixed point with native integer shared
+    // atomics: deterministic, and no compare-and-swap retry loops under
+    // contention.  A line adds at most its (scaled, <= 1) intensity to any one
+    // cell, so a cell's sum is bounded by the number of lines that can touch
+    // its column; the tile's scale 2^e keeps that bound below 2^31.
+    extern __shared__ uint4 tile4[];
+    unsigned* tile = reinterpret_cast<unsigned*>(tile4);
+    __shared__ int red_max[32];
     const int k_start = blockIdx.x * a.TK;
     const int tk = min(a.TK, a.n_v - k_start);
     const int n4 = a.n_nodes * a.TK / 4;
-    for (int i = threadIdx.x; i < n4; i += blockDim.x) tile4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-    __syncthreads();
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) tile4[i] = make_uint4(0u, 0u, 0u, 0u);
 
-    int c_lo = k_start - 1 - a.margin_cols + a.col_off;
-    int c_hi = k_start + tk + a.margin_cols + a.col_off;
-    c_lo = max(0, min(c_lo, a.col_count - 1));
-    c_hi = max(0, min(c_hi, a.col_count - 1));
-    const int64_t i0 = a.col_start[c_lo];
-    const int64_t i1 = a.col_start[c_hi];
+    auto col_idx = [&](int c) { return max(0, min(c + a.col_off, a.col_count - 1)); };
+    int cmax = 0;
+    for (int c = threadIdx.x; c < tk; c += blockDim.x) {
+        const int64_t cnt = a.col_start[col_idx(k_start + c + 1 + a.margin_cols)] -
+                            a.col_start[col_idx(k_start + c - 1 - a.margin_cols)];
+        cmax = max(cmax, (int)min(cnt, (int64_t)0x3fffffff));
+    }
+    for (int o = 16; o; o >>= 1) cmax = max(cmax, __shfl_xor_sync(0xffffffffu, cmax, o));
+    if ((threadIdx.x & 31) == 0) red_max[threadIdx.x >> 5] = cmax;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int m = threadIdx.x < (blockDim.x >> 5) ? red_max[threadIdx.x] : 0;
+        for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) red_max[0] = m;
+    }
+    __syncthreads();
+    // scale = 2^e with (cmax + 1) 2^e <= 2^31
+    const int e = 31 - (32 - __clz(red_max[0] + 1));
+    const float scale = ldexpf(1.f, max(e, 0));
+
+    const int64_t i0 = a.col_start[col_idx(k_start - 1 - a.margin_cols)];
+    const int64_t i1 = a.col_start[col_idx(k_start + tk + a.margin_cols)];
     unsigned int counted = 0;
 
 #pragma unroll 2
     for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+        // issue every load of the line record up front
         const float2 v = a.v0[i];
-        const float shift = a.dl ? a.dl[i] * a.p_atm : 0.f;
+        const float dl = a.dl ? a.dl[i] : 0.f;
+        const float gs = a.gs[i];
+        const float ga = a.ga[i];
+        const float na = a.na[i];
+        const float el = a.el[i];
+        const float ls2 = a.ls2[i];
+        const int is = a.iso ? (int)a.iso[i] : 0;
         // k position in double-float: ((hi - vmin_hi) + (lo - vmin_lo + shift)) / dv
-        float s, e;
-        two_sum(v.x, -a.vmin_hi, s, e);
-        e += (v.y - a.vmin_lo) + shift;
+        float s, e1;
+        two_sum(v.x, -a.vmin_hi, s, e1);
+        e1 += (v.y - a.vmin_lo) + dl * a.p_atm;
         const float p = s * a.inv_dv_hi;
-        const float pe = fmaf(s, a.inv_dv_hi, -p) + fmaf(s, a.inv_dv_lo, e * a.inv_dv_hi);
+        const float pe = fmaf(s, a.inv_dv_hi, -p) + fmaf(s, a.inv_dv_lo, e1 * a.inv_dv_hi);
         float fk = floorf(p);
         float tv = (p - fk) + pe;
         const float fl = floorf(tv);
@@ -343,26 +377,23 @@ __global__ void __launch_bounds__(512, 2) k_scatter(const ScatterArgs a) {
         const bool own1 = (unsigned)(c0 + 1) < (unsigned)tk;
         if (!(own0 || own1)) continue;
         if (own0) ++counted;
-        const int is = a.iso ? (int)a.iso[i] : 0;
         // Gaussian / Lorentzian node coordinates (FWHM, log space); log v0 is
         // taken relative to v_ref so the FP32 log and offset do not cancel
         const float pl = fmaf(lg2(v.x * a.inv_vref), a.lgG_scale, a.cG[is]);
-        const float ga = a.ga[i];
-        const float gam = fmaf(a.x_self, a.gs[i] - ga, ga);
-        const float pm = fmaf(lg2(gam), a.lgL_scale, fmaf(a.na[i], a.tL, a.cL));
+        const float gam = fmaf(a.x_self, gs - ga, ga);
+        const float pm = fmaf(lg2(gam), a.lgL_scale, fmaf(na, a.tL, a.cL));
         const int l0 = min(max((int)floorf(pl), 0), a.NG - 2);
         const int m0 = min(max((int)floorf(pm), 0), a.NL - 2);
         const float tG = pl - (float)l0;
         const float tL = pm - (float)m0;
         // intensity: exponent log2(S') + a_T El + b_iso in double-float
-        const float el = a.el[i];
         const float ph = el * a.aT_hi;
         const float pe2 = fmaf(el, a.aT_hi, -ph) + el * a.aT_lo;
-        float s1, e1, s2, e2;
-        two_sum(ph, a.bI_hi[is], s1, e1);
-        two_sum(s1, a.ls2[i], s2, e2);
-        const float arg = s2 + (e1 + e2 + pe2 + a.bI_lo[is]);
-        const float I = ex2(arg) * (1.f - ex2(-a.stim_c * v.x));
+        float s1, f1, s2, f2;
+        two_sum(ph, a.bI_hi[is], s1, f1);
+        two_sum(s1, ls2, s2, f2);
+        const float arg = s2 + (f1 + f2 + pe2 + a.bI_lo[is]);
+        const float I = ex2(arg) * (1.f - ex2(-a.stim_c * v.x)) * scale;
         const float I1 = tv * I;
         const float I0 = I - I1;
         const float w11 = tG * tL;
@@ -372,29 +403,32 @@ __global__ void __launch_bounds__(512, 2) k_scatter(const ScatterArgs a) {
         const int n00 = l0 * a.NL + m0;
         const int n10 = n00 + a.NL;
         if (own0) {
-            atomicAdd(&tile[tile_addr(n00, c0, a.TK)], I0 * w00);
-            atomicAdd(&tile[tile_addr(n00 + 1, c0, a.TK)], I0 * w01);
-            atomicAdd(&tile[tile_addr(n10, c0, a.TK)], I0 * w10);
-            atomicAdd(&tile[tile_addr(n10 + 1, c0, a.TK)], I0 * w11);
+            atomicAdd(&tile[tile_addr(n00, c0, a.TK)], __float2uint_rn(I0 * w00));
+            atomicAdd(&tile[tile_addr(n00 + 1, c0, a.TK)], __float2uint_rn(I0 * w01));
+            atomicAdd(&tile[tile_addr(n10, c0, a.TK)], __float2uint_rn(I0 * w10));
+            atomicAdd(&tile[tile_addr(n10 + 1, c0, a.TK)], __float2uint_rn(I0 * w11));
         }
         if (own1) {
-            atomicAdd(&tile[tile_addr(n00, c0 + 1, a.TK)], I1 * w00);
-            atomicAdd(&tile[tile_addr(n00 + 1, c0 + 1, a.TK)], I1 * w01);
-            atomicAdd(&tile[tile_addr(n10, c0 + 1, a.TK)], I1 * w10);
-            atomicAdd(&tile[tile_addr(n10 + 1, c0 + 1, a.TK)], I1 * w11);
+            atomicAdd(&tile[tile_addr(n00, c0 + 1, a.TK)], __float2uint_rn(I1 * w00));
+            atomicAdd(&tile[tile_addr(n00 + 1, c0 + 1, a.TK)], __float2uint_rn(I1 * w01));
+            atomicAdd(&tile[tile_addr(n10, c0 + 1, a.TK)], __float2uint_rn(I1 * w10));
+            atomicAdd(&tile[tile_addr(n10 + 1, c0 + 1, a.TK)], __float2uint_rn(I1 * w11));
         }
     }
     if (a.in_window && counted) atomicAdd(a.in_window, (unsigned long long)counted);
     __syncthreads();
     // flush: every column of the tile is owned by this CTA -> plain stores
+    const float inv = 1.f / scale;
     const int tk4 = (tk + 3) >> 2;
     const int per_row = a.TK >> 2;
     for (int i = threadIdx.x; i < n4; i += blockDim.x) {
         const int node = i / per_row;
         const int c4 = i - node * per_row;
-        if (c4 < tk4)
+        if (c4 < tk4) {
+            const uint4 u = tile4[node * per_row + (c4 ^ (node & 7))];
             *reinterpret_cast<float4*>(&a.ldm[node * a.row_stride + k_start + 4 * c4]) =
-                tile4[node * per_row + (c4 ^ (node & 7))];
+                make_float4((float)u.x * inv, (float)u.y * inv, (float)u.z * inv, (float)u.w * inv);
+        }
     }
 }
 
@@ -465,8 +499,8 @@ __global__ void __launch_bounds__(kRowThreads) k_row_fft_voigt(const VoigtArgs a
     extern __shared__ float2 sm[];
     const int n2 = a.n2;
     float2* buf0 = sm;
-    float2* buf1 = sm + n2;
-    float2* acc = sm + 2 * n2;
+    float2* buf1 = sm + row_buf_len(n2);
+    float2* acc = sm + 2 * row_buf_len(n2);
     const int k1 = blockIdx.x;
     const int j0 = blockIdx.y * kPairGroup;
     const int j1 = min(j0 + kPairGroup, a.n_pairs);
@@ -475,8 +509,11 @@ __global__ void __launch_bounds__(kRowThreads) k_row_fft_voigt(const VoigtArgs a
 
     for (int j = j0; j < j1; ++j) {
         const float4* src = reinterpret_cast<const float4*>(a.y + ((int64_t)j * a.n1 + k1) * n2);
-        float4* dst = reinterpret_cast<float4*>(buf0);
-        for (int t = threadIdx.x; t < n2 / 2; t += blockDim.x) dst[t] = __ldg(&src[t]);
+        for (int t = threadIdx.x; t < n2 / 2; t += blockDim.x) {
+            const float4 q = __ldg(&src[t]);
+            buf0[rp(2 * t)] = make_float2(q.x, q.y);        // 2t and 2t+1 share one pad
+            buf0[rp(2 * t) + 1] = make_float2(q.z, q.w);
+        }
         __syncthreads();
         const float2* res = fft_row(buf0, buf1, a.f2);
         const NodeV na = node_params(a, 2 * j);
@@ -487,7 +524,7 @@ __global__ void __launch_bounds__(kRowThreads) k_row_fft_voigt(const VoigtArgs a
             const float f = (float)kf * a.inv_ndv;
             const float va = voigt_eval(na, f, a.half_fs);
             const float vb = voigt_eval(nb, f, a.half_fs);
-            const float2 z = res[t];
+            const float2 z = res[rp(t)];
             float2 c = acc[t];
             c.x += z.x * va + z.y * vb;
             c.y += z.y * va - z.x * vb;
@@ -506,15 +543,15 @@ __global__ void __launch_bounds__(kRowThreads) k_row_ifft(const RowIfftArgs a) {
     extern __shared__ float2 sm[];
     const int n2 = a.n2;
     float2* buf0 = sm;
-    float2* buf1 = sm + n2;
+    float2* buf1 = sm + row_buf_len(n2);
     const int k1 = blockIdx.x;
     float2* g = a.g + (int64_t)k1 * n2;
-    for (int t = threadIdx.x; t < n2; t += blockDim.x) buf0[t] = conjf2(g[t]);
+    for (int t = threadIdx.x; t < n2; t += blockDim.x) buf0[rp(t)] = conjf2(g[t]);
     __syncthreads();
     // inverse DFT = conj(forward DFT(conj(x)))
     const float2* res = fft_row(buf0, buf1, a.f2);
     for (int t = threadIdx.x; t < n2; t += blockDim.x) {
-        float2 z = conjf2(res[t]);
+        float2 z = conjf2(res[rp(t)]);
         if (k1 && t) z = cmul(z, conjf2(twiddle_n(a.tw_hi, a.tw_lo, t * k1)));
         g[t] = z;
     }
@@ -611,14 +648,14 @@ int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st) {
     static bool done = false;
     allow_smem(k_row_fft_voigt, done);
     dim3 grid(a.n1, (a.n_pairs + kPairGroup - 1) / kPairGroup);
-    k_row_fft_voigt<<<grid, kRowThreads, 3 * (size_t)a.n2 * sizeof(float2), st>>>(a);
+    k_row_fft_voigt<<<grid, kRowThreads, (2 * (size_t)row_buf_len(a.n2) + a.n2) * sizeof(float2), st>>>(a);
     return check_launch();
 }
 
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st) {
     static bool done = false;
     allow_smem(k_row_ifft, done);
-    k_row_ifft<<<a.n1, kRowThreads, 2 * (size_t)a.n2 * sizeof(float2), st>>>(a);
+    k_row_ifft<<<a.n1, kRowThreads, 2 * (size_t)row_buf_len(a.n2) * sizeof(float2), st>>>(a);
     return check_launch();
 }
 
