@@ -155,9 +155,10 @@ int rg_synthesize(rg_plan* plan, const rg_conditions* cond, float* out_dev, void
 int rg_plan_stage_times(rg_plan* plan, double* sum_ms, int64_t* count);
 
 /* As rg_synthesize, then copies the n_v floats to `out_host` (pinned or
- * pageable) and waits for the copy: the drop-in `iterate()` form. */
+ * pageable) and waits for the copy: the drop-in `iterate()` form.  timing = 1
+ * fills info->stage_ms (0 or 2 leave it empty). */
 int rg_synthesize_host(rg_plan* plan, const rg_conditions* cond, float* out_host,
-                       void* stream, rg_spectrum_info* info);
+                       void* stream, int timing, rg_spectrum_info* info);
 
 /* Test hook: runs only the fused scale+scatter and copies the LDM tensor to
  * host as [n_nodes][n_v] floats (node = l*n_L + m), in units of

@@ -7,6 +7,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 
 import numpy as np
 
@@ -103,7 +104,8 @@ def load(path: str | None = None):
         "rg_grid_estimate": ([C.POINTER(LineArrays), C.POINTER(Isotopes), C.POINTER(PlanDesc),
                               C.POINTER(Conditions), C.POINTER(Grid)], C.c_int),
         "rg_synthesize": ([vp, C.POINTER(Conditions), vp, vp, C.c_int, C.POINTER(SpectrumInfo)], C.c_int),
-        "rg_synthesize_host": ([vp, C.POINTER(Conditions), vp, vp, C.POINTER(SpectrumInfo)], C.c_int),
+        "rg_synthesize_host": ([vp, C.POINTER(Conditions), vp, vp, C.c_int, C.POINTER(SpectrumInfo)],
+                               C.c_int),
         "rg_plan_stage_times": ([vp, C.POINTER(C.c_double), C.POINTER(i64)], C.c_int),
         "rg_debug_ldm": ([vp, C.POINTER(Conditions), vp, i64, C.POINTER(SpectrumInfo)], C.c_int),
     }
@@ -134,13 +136,19 @@ class Context:
         check(lib.rg_ctx_create(int(device), C.byref(h)))
         self._h = h
         self.device = device
+        self._children = weakref.WeakSet()
 
     @property
     def handle(self):
+        if not self._h:
+            raise RgError(7, "context is closed")
         return self._h
 
     def close(self):
+        """Close the line lists (and their plans) still open, then the context."""
         if getattr(self, "_h", None):
+            for child in list(self._children):
+                child.close()
             check(load().rg_ctx_destroy(self._h))
             self._h = None
 
@@ -185,6 +193,8 @@ class Lines:
         h = C.c_void_p()
         check(lib.rg_lines_upload(ctx.handle, C.byref(la), C.byref(iso_s), C.byref(h)))
         self._h = h
+        self._children = weakref.WeakSet()
+        ctx._children.add(self)
         self.n = len(k["v0"])
         self.molar_mass = mm
         self.t_ref = t_ref
@@ -192,10 +202,15 @@ class Lines:
 
     @property
     def handle(self):
+        if not self._h:
+            raise RgError(7, "line list is closed")
         return self._h
 
     def close(self):
+        """Close the plans still open on this list, then the list."""
         if getattr(self, "_h", None):
+            for child in list(self._children):
+                child.close()
             check(load().rg_lines_free(self._h))
             self._h = None
 
@@ -218,10 +233,13 @@ class Plan:
         h = C.c_void_p()
         check(lib.rg_plan_create(lines.handle, C.byref(d), C.byref(h)))
         self._h = h
+        lines._children.add(self)
         self.vmin, self.dv, self.n_v = float(vmin), float(dv), int(n_v)
 
     @property
     def handle(self):
+        if not self._h:
+            raise RgError(7, "plan is closed")
         return self._h
 
     def _cond(self, T, p_bar, x, q_ratio):
@@ -234,17 +252,18 @@ class Plan:
     def grid(self, T, p_bar, x, q_ratio=None) -> Grid:
         c, _q = self._cond(T, p_bar, x, q_ratio)
         g = Grid()
-        check(load().rg_plan_grid(self._h, C.byref(c), C.byref(g)))
+        check(load().rg_plan_grid(self.handle, C.byref(c), C.byref(g)))
         return g
 
-    def synthesize_host(self, T, p_bar, x, q_ratio=None, out=None):
+    def synthesize_host(self, T, p_bar, x, q_ratio=None, out=None, timing=False):
         """Blocking: returns (float32 array n_v, SpectrumInfo); abscoeff in cm-1
-        is ``out * exp(info.log_scale)``."""
+        is ``out * exp(info.log_scale)``; ``timing`` fills info.stage_ms."""
         c, _q = self._cond(T, p_bar, x, q_ratio)
         if out is None:
             out = np.empty(self.n_v, dtype=np.float32)
         info = SpectrumInfo()
-        check(load().rg_synthesize_host(self._h, C.byref(c), ptr(out), None, C.byref(info)))
+        check(load().rg_synthesize_host(self.handle, C.byref(c), ptr(out), None, 1 if timing else 0,
+                                        C.byref(info)))
         return out, info
 
     def synthesize_device(self, T, p_bar, x, out_dev_ptr: int, stream_ptr: int | None = None,
@@ -254,7 +273,7 @@ class Plan:
         2 per-stage events into the plan's ring (read with ``stage_times``)."""
         c, _q = self._cond(T, p_bar, x, q_ratio)
         info = SpectrumInfo()
-        check(load().rg_synthesize(self._h, C.byref(c), C.c_void_p(out_dev_ptr),
+        check(load().rg_synthesize(self.handle, C.byref(c), C.c_void_p(out_dev_ptr),
                                    C.c_void_p(stream_ptr) if stream_ptr else None,
                                    int(timing), C.byref(info)))
         return info
@@ -264,7 +283,7 @@ class Plan:
         ifft-col, total], count) of spectra enqueued with timing=2."""
         s = (C.c_double * 6)()
         n = C.c_int64()
-        check(load().rg_plan_stage_times(self._h, s, C.byref(n)))
+        check(load().rg_plan_stage_times(self.handle, s, C.byref(n)))
         return list(s), n.value
 
     def debug_ldm(self, T, p_bar, x, q_ratio=None):
@@ -273,7 +292,7 @@ class Plan:
         g = self.grid(T, p_bar, x, q_ratio)
         buf = np.empty(g.n_G * g.n_L * self.n_v, dtype=np.float32)
         info = SpectrumInfo()
-        check(load().rg_debug_ldm(self._h, C.byref(c), ptr(buf), buf.size, C.byref(info)))
+        check(load().rg_debug_ldm(self.handle, C.byref(c), ptr(buf), buf.size, C.byref(info)))
         return buf.reshape(g.n_G, g.n_L, self.n_v), info
 
     def close(self):

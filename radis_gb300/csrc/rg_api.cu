@@ -63,6 +63,7 @@ static int fail(int code, const char* fmt, ...) {
 struct rg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    int lines = 0;            // live line lists on this context
     uint32_t magic = 0x52474358;
 };
 
@@ -654,6 +655,7 @@ int rg_ctx_destroy(rg_ctx* c) {
     g_err.clear();
     if (!c) return RG_OK;
     if (!valid(c)) return fail(RG_ERR_STATE, "invalid context");
+    if (c->lines) return fail(RG_ERR_STATE, "context still has %d line list(s)", c->lines);
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     cudaStreamDestroy(c->stream);
@@ -737,6 +739,7 @@ int rg_lines_upload(rg_ctx* ctx, const rg_line_arrays* in, const rg_isotopes* is
     flag = nullptr;
     if (unsorted) return bail(fail(RG_ERR_UNSORTED, "line positions v0 must be ascending"));
 #undef CUB
+    ctx->lines++;
     *out = guard.release();
     return RG_OK;
 }
@@ -756,6 +759,7 @@ int rg_lines_free(rg_lines* L) {
     dfree(L->na);
     dfree(L->dl);
     dfree(L->iso);
+    L->ctx->lines--;
     L->magic = 0;
     delete L;
     return RG_OK;
@@ -921,14 +925,14 @@ int rg_plan_stage_times(rg_plan* P, double* sum_ms, int64_t* count) {
     return RG_OK;
 }
 
-int rg_synthesize_host(rg_plan* P, const rg_conditions* c, float* out_host, void* stream,
+int rg_synthesize_host(rg_plan* P, const rg_conditions* c, float* out_host, void* stream, int timing,
                        rg_spectrum_info* info) {
     g_err.clear();
     if (!valid(P) || !c || !out_host) return fail(RG_ERR_ARG, "invalid argument");
     std::lock_guard<std::mutex> lk(P->mu);
     CU(cudaSetDevice(P->lines->ctx->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
-    RG(run_spectrum(P, c, P->out_d, st, 0, false, info));
+    RG(run_spectrum(P, c, P->out_d, st, (timing && info) ? 1 : 0, false, info));
     CU(cudaMemcpyAsync(out_host, P->out_d, sizeof(float) * (size_t)P->desc.n_v, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
     return RG_OK;

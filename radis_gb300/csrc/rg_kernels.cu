@@ -597,13 +597,35 @@ int col_block(int n1) {
 
 size_t scatter_smem_floats(int n_nodes, int TK) { return (size_t)n_nodes * TK; }
 
+// Opt the kernel in to the largest dynamic shared memory the device allows
+// next to the kernel's own static shared memory; checks that `need` fits.
 template <typename K>
-static void allow_smem(K kernel, bool& done) {
+static int allow_smem(K kernel, bool& done, size_t need) {
+    static int optin = 0;
+    if (!optin) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) return RG_ERR_CUDA;
+        if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+            return RG_ERR_CUDA;
+    }
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return RG_ERR_CUDA;
+    const size_t avail = (size_t)optin - fa.sharedSizeBytes;
+    if (need > avail) return RG_ERR_RANGE;
     if (!done) {
-        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)avail) != cudaSuccess)
+            return RG_ERR_CUDA;
         done = true;
     }
+    return RG_OK;
 }
+
+#define ALLOW_SMEM(kernel, need)                        \
+    do {                                                 \
+        static bool done_ = false;                       \
+        int r_ = allow_smem(kernel, done_, (need));      \
+        if (r_ != RG_OK) return r_;                      \
+    } while (0)
 
 int launch_prepare_lines(const double* v0_d, const double* s_d, int64_t n, double c2_tref, float2* v0_out,
                          float* ls2_out, int* unsorted_flag, cudaStream_t st) {
@@ -620,16 +642,14 @@ int launch_col_index(const float2* v0, int64_t n, double vmin, double dv, int c_
 }
 
 int launch_scatter(const ScatterArgs& a, int n_tiles, size_t smem, cudaStream_t st) {
-    static bool done = false;
-    allow_smem(k_scatter, done);
+    ALLOW_SMEM(k_scatter, smem);
     k_scatter<<<n_tiles, 512, smem, st>>>(a);
     return check_launch();
 }
 
 template <int N1>
 static int col_fwd(const ColFftArgs& a, cudaStream_t st) {
-    static bool done = false;
-    allow_smem(k_col_fft_fwd<N1>, done);
+    ALLOW_SMEM(k_col_fft_fwd<N1>, N1 * ColShape<N1>::B * sizeof(float2));
     dim3 grid(a.n2 / ColShape<N1>::B, a.n_pairs);
     k_col_fft_fwd<N1><<<grid, ColShape<N1>::THREADS, N1 * ColShape<N1>::B * sizeof(float2), st>>>(a);
     return check_launch();
@@ -645,24 +665,23 @@ int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st) {
 }
 
 int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st) {
-    static bool done = false;
-    allow_smem(k_row_fft_voigt, done);
+    const size_t smem = (2 * (size_t)row_buf_len(a.n2) + a.n2) * sizeof(float2);
+    ALLOW_SMEM(k_row_fft_voigt, smem);
     dim3 grid(a.n1, (a.n_pairs + kPairGroup - 1) / kPairGroup);
-    k_row_fft_voigt<<<grid, kRowThreads, (2 * (size_t)row_buf_len(a.n2) + a.n2) * sizeof(float2), st>>>(a);
+    k_row_fft_voigt<<<grid, kRowThreads, smem, st>>>(a);
     return check_launch();
 }
 
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st) {
-    static bool done = false;
-    allow_smem(k_row_ifft, done);
-    k_row_ifft<<<a.n1, kRowThreads, 2 * (size_t)row_buf_len(a.n2) * sizeof(float2), st>>>(a);
+    const size_t smem = 2 * (size_t)row_buf_len(a.n2) * sizeof(float2);
+    ALLOW_SMEM(k_row_ifft, smem);
+    k_row_ifft<<<a.n1, kRowThreads, smem, st>>>(a);
     return check_launch();
 }
 
 template <int N1>
 static int col_inv(const ColFftArgs& a, cudaStream_t st) {
-    static bool done = false;
-    allow_smem(k_col_ifft<N1>, done);
+    ALLOW_SMEM(k_col_ifft<N1>, N1 * ColShape<N1>::B * sizeof(float2));
     k_col_ifft<N1><<<a.n2 / ColShape<N1>::B, ColShape<N1>::THREADS, N1 * ColShape<N1>::B * sizeof(float2), st>>>(a);
     return check_launch();
 }

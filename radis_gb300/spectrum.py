@@ -1,0 +1,138 @@
+"""Spectrum container returned by the GPU synthesis.
+
+Keeps the reference's output contract for this path
+(radis/lbl/factory.py:1284-1376): quantities wavenumber, abscoeff,
+absorbance, emissivity_noslit, transmittance_noslit, radiance_noslit; the
+conditions keys the GPU path sets; ``recalc_gpu`` (radis/spectrum/spectrum.py:
+6438-6572) to re-run the resident GPU application at new conditions; and
+``exit_gpu`` (spectrum.py:6574-6577).  Derived quantities are computed on the
+host from abscoeff exactly as the reference does.
+"""
+from __future__ import annotations
+
+import warnings
+
+import numpy as np
+
+# radis/phys/constants.py:22,33,38
+_H = 6.62607015e-34
+_C = 2.99792458e8
+_KB = 1.3806490e-23
+
+DEFAULT_UNITS = {
+    "wavenumber": "cm-1",
+    "abscoeff": "cm-1",
+    "absorbance": "",
+    "emissivity_noslit": "",
+    "transmittance_noslit": "",
+    "radiance_noslit": "mW/cm2/sr/nm",
+}
+
+
+class GPUInitWarning(UserWarning):
+    """No GPU application attached (radis/misc/warning.py:68)."""
+
+
+def planck_nm(lambda_nm, T):
+    """Black-body radiance in mW/cm2/sr/nm (radis/phys/blackbody.py:35-74)."""
+    lbd = np.asarray(lambda_nm, dtype=np.float64) * 1e-9
+    return 2 * _H * _C ** 2 / lbd ** 5 / np.expm1(_H * _C / (lbd * _KB * T)) * 1e-10
+
+
+def derived_quantities(wavenumber, abscoeff, path_length, Tgas):
+    """absorbance, emissivity, transmittance, radiance (factory.py:1284-1297,
+    radis/spectrum/equations.py:21-44 with unit mW/sr/cm2/nm)."""
+    absorbance = abscoeff * path_length
+    emissivity = -np.expm1(-absorbance)
+    transmittance = 1 - emissivity
+    radiance = emissivity * planck_nm(1e7 / np.asarray(wavenumber, np.float64), Tgas)
+    return absorbance, emissivity, transmittance, radiance
+
+
+class Spectrum:
+    """Minimal Spectrum: ``get(var)`` -> (wavenumber, values)."""
+
+    def __init__(self, quantities, units=None, conditions=None, cond_units=None, gpu_app=None,
+                 name=None, lines=None, **_):
+        self._q = {k: np.asarray(v) for k, v in quantities.items()}
+        self.units = dict(DEFAULT_UNITS if units is None else units)
+        self.conditions = dict(conditions or {})
+        self.cond_units = dict(cond_units or {})
+        self.gpu_app = gpu_app
+        self.name = name
+        self.lines = lines
+        self._woutrange = None
+
+    @property
+    def c(self):
+        return self.conditions
+
+    def get_vars(self):
+        return [k for k in self._q if k != "wavenumber"]
+
+    def get(self, var, wunit="cm-1", Iunit="default", copy=True):
+        if var not in self._q:
+            self._update(var)
+        w = self._q["wavenumber"]
+        v = self._q[var]
+        if wunit in ("nm", "nm_vac"):
+            w = 1e7 / w
+        return (w.copy(), v.copy()) if copy else (w, v)
+
+    def _update(self, var):
+        if "abscoeff" not in self._q:
+            raise KeyError(var)
+        a, e, t, r = derived_quantities(self._q["wavenumber"], self._q["abscoeff"],
+                                        self.conditions["path_length"], self.conditions["Tgas"])
+        self._q.update(absorbance=a, emissivity_noslit=e, transmittance_noslit=t, radiance_noslit=r)
+        if var not in self._q:
+            raise KeyError(var)
+
+    def crop(self, wmin=None, wmax=None, wunit="cm-1"):
+        w = self._q["wavenumber"]
+        sel = np.ones(len(w), dtype=bool)
+        if wmin is not None:
+            sel &= w >= wmin
+        if wmax is not None:
+            sel &= w <= wmax
+        for k in self._q:
+            self._q[k] = self._q[k][sel]
+        return self
+
+    def recalc_gpu(self, var="transmittance", wunit=None, Iunit=None, pressure=None, Tgas=None,
+                   mole_fraction=None, path_length=None, slit_function=None, verbose=False):
+        """Re-run the resident GPU application at new conditions and return
+        ``var`` (spectrum.py:6438-6572).  Only abscoeff comes from the GPU; the
+        other quantities are re-derived on request."""
+        if self.gpu_app is None:
+            warnings.warn("no GPU application attached to this Spectrum (exit_gpu was "
+                          "called or exit_gpu=True was used)", GPUInitWarning)
+            return None
+        c = self.conditions
+        if pressure is not None:
+            c["pressure"] = pressure
+        if Tgas is not None:
+            c["Tgas"] = Tgas
+        if mole_fraction is not None:
+            c["mole_fraction"] = mole_fraction
+        if path_length is not None:
+            c["path_length"] = path_length
+        abscoeff, times = self.gpu_app.iterate(c["pressure"], c["Tgas"], c["mole_fraction"],
+                                               verbose=verbose)
+        w0, w1 = self._woutrange or (0, len(abscoeff))
+        abscoeff = abscoeff[w0:w1]
+        for k in list(self._q):
+            if k != "wavenumber":
+                del self._q[k]
+        self._q["abscoeff"] = abscoeff
+        n_L, n_G = self.gpu_app.get_griddims()
+        c.update(NwL=n_L, NwG=n_G, gpu_times=times)
+        key = {"transmittance": "transmittance_noslit", "radiance": "radiance_noslit",
+               "emissivity": "emissivity_noslit"}.get(var, var)
+        return self.get(key)[1]
+
+    def exit_gpu(self):
+        """Release the GPU application (spectrum.py:6574-6577)."""
+        if self.gpu_app is not None:
+            self.gpu_app.free()
+            self.gpu_app = None

@@ -1,0 +1,74 @@
+"""CPU checks of the drop-in front end: HITRAN-160 I/O, the factory grid and
+the host-side derived quantities (no GPU)."""
+import os
+
+import numpy as np
+import pytest
+
+from radis_gb300 import SpectrumFactory, hitran
+from radis_gb300 import synthetic as S
+from radis_gb300.spectrum import Spectrum, derived_quantities, planck_nm
+
+REF_FIXTURE = "/root/reference/radis/test/files/hitran_co_3iso_2000_2300cm.par"
+
+
+def test_hitran_roundtrip_idempotent(tmp_path):
+    lines = S.co_like(500)
+    lines["delta"] = np.random.default_rng(3).uniform(-0.005, 0, 500)
+    p1, p2 = tmp_path / "a.par", tmp_path / "b.par"
+    hitran.write_hitran160(p1, lines)
+    r1 = hitran.read_hitran160(p1)
+    hitran.write_hitran160(p2, r1)
+    assert open(p1).read() == open(p2).read()
+    assert all(len(x.rstrip("\n")) == 160 for x in open(p1))
+    np.testing.assert_allclose(r1["v0"], lines["v0"], atol=1e-6)
+    np.testing.assert_allclose(r1["S_ref"], lines["S_ref"], rtol=6e-4)
+    np.testing.assert_allclose(r1["n_air"], lines["n_air"], atol=5e-3)
+
+
+@pytest.mark.skipif(not os.path.exists(REF_FIXTURE), reason="reference tree not mounted")
+def test_hitran_reads_reference_fixture():
+    d = hitran.read_hitran160(REF_FIXTURE)
+    assert len(d["v0"]) == 573
+    assert set(np.unique(d["iso"])) == {1, 2, 3}
+    assert np.all(d["id"] == 5)
+    assert d["v0"].min() >= 2000 and d["v0"].max() <= 2300
+
+
+def test_factory_grid_and_margins():
+    sf = SpectrumFactory(2000.0, 2010.0, wstep=0.01, molecule="CO", neighbour_lines=1.0)
+    assert len(sf.wavenumber) == 1001
+    assert sf.woutrange == (100, 1101)
+    np.testing.assert_allclose(sf.wavenumber_calc[sf.woutrange[0]], 2000.0)
+    np.testing.assert_allclose(sf.wavenumber[-1], 2010.0)
+    with pytest.raises(ValueError):
+        sf.eq_spectrum_gpu(300.0)            # no database loaded
+    with pytest.raises(NotImplementedError):
+        SpectrumFactory(2000, 2010, broadening_method="voigt")
+
+
+def test_derived_quantities():
+    w = np.linspace(2000, 2100, 11)
+    k = np.linspace(0, 2, 11)
+    a, e, t, r = derived_quantities(w, k, 3.0, 1000.0)
+    np.testing.assert_allclose(a, 3 * k)
+    np.testing.assert_allclose(t, np.exp(-3 * k), rtol=1e-12)
+    np.testing.assert_allclose(e, 1 - np.exp(-3 * k), rtol=1e-12, atol=1e-15)
+    # Planck in mW/cm2/sr/nm: 2hc^2/l^5/(exp(hc/lkT)-1) * 1e-10 (blackbody.py:64-69)
+    lam = 1e7 / w * 1e-9
+    h, c, kb = 6.62607015e-34, 2.99792458e8, 1.380649e-23
+    ref = 2 * h * c ** 2 / lam ** 5 / (np.exp(h * c / (lam * kb * 1000.0)) - 1) * 1e-10
+    np.testing.assert_allclose(planck_nm(1e7 / w, 1000.0), ref, rtol=1e-12)
+    np.testing.assert_allclose(r, e * ref, rtol=1e-12)
+
+
+def test_spectrum_get_and_crop():
+    w = np.linspace(2000, 2001, 101)
+    s = Spectrum(dict(wavenumber=w, abscoeff=np.full(101, 0.5)),
+                 conditions=dict(path_length=2.0, Tgas=500.0))
+    ww, T = s.get("transmittance_noslit")
+    np.testing.assert_allclose(T, np.exp(-1.0))
+    s.crop(2000.2, 2000.4)
+    assert s.get("abscoeff")[0][0] == pytest.approx(2000.2)
+    with pytest.warns(UserWarning):
+        assert s.recalc_gpu("abscoeff", Tgas=600) is None
