@@ -62,6 +62,7 @@ static int fail(int code, const char* fmt, ...) {
 // ---------------------------------------------------------------------------
 struct rg_ctx {
     int device = 0;
+    int sms = 1;              // streaming multiprocessors of the device
     cudaStream_t stream = nullptr;
     int lines = 0;            // live line lists on this context
     uint32_t magic = 0x52474358;
@@ -121,6 +122,9 @@ struct rg_plan {
     float2* g = nullptr;
     float* out_d = nullptr;
     unsigned long long* counter = nullptr;
+    unsigned* err = nullptr;          // device flag set by a bounded wait that gave up
+    unsigned* err_host = nullptr;     // pinned copy of err, refreshed after every spectrum
+    int64_t cmax = 0;                 // max lines that can touch one grid column
     cudaEvent_t ev[6] = {nullptr};
     // ring of per-stage events recorded without synchronisation (timing == 2)
     static constexpr int kRing = 256;
@@ -399,13 +403,27 @@ int ensure_workspace(rg_plan* P, int n_nodes) {
     return RG_OK;
 }
 
-// Columns per scatter tile: a multiple of 32 (the bank swizzle works inside
-// 32-column groups), sized for two CTAs per SM when the node count allows.
-int scatter_tile(int n_nodes) {
-    const int budget2 = 110 * 1024, budget1 = 220 * 1024;
-    int tk = budget2 / (4 * n_nodes) / 32 * 32;
-    if (tk < 32) tk = budget1 / (4 * n_nodes) / 32 * 32;
-    return std::min(tk, 1024);
+// Stage chunk (lines) and tile width (columns, a multiple of 32 for the bank
+// swizzle) of the persistent scatter: the largest chunk that still leaves a
+// tile of >= 64 columns (>= 32 for very large node counts) next to the two
+// stage buffers in one CTA's shared memory.
+int scatter_shape(int n_nodes, int* chunk, int* TK, size_t* smem) {
+    size_t avail = 0;
+    RG(scatter_smem_optin(&avail));
+    for (int min_tk : {64, 32})
+        for (int ch : {2048, 1024, 512, 256}) {
+            const size_t fixed = scatter_fixed_smem(ch);
+            if (fixed >= avail) continue;
+            int tk = (int)((avail - fixed) / (4 * (size_t)n_nodes)) / 32 * 32;
+            tk = std::min(tk, 1024);
+            if (tk >= min_tk) {
+                *chunk = ch;
+                *TK = tk;
+                *smem = fixed + (size_t)4 * n_nodes * tk;
+                return RG_OK;
+            }
+        }
+    return fail(RG_ERR_RANGE, "LDM grid of %d nodes does not fit a shared-memory tile", n_nodes);
 }
 
 int build_scatter_args(rg_plan* P, const rg_conditions* c, const SpecHost& s, ScatterArgs* a) {
@@ -429,8 +447,17 @@ int build_scatter_args(rg_plan* P, const rg_conditions* c, const SpecHost& s, Sc
     a->NL = g.n_L;
     a->row_stride = P->row_stride;
     a->ldm = P->ldm;
-    a->TK = scatter_tile(s.n_nodes);
-    if (a->TK < 32) return fail(RG_ERR_RANGE, "LDM grid of %d nodes does not fit a shared-memory tile", s.n_nodes);
+    size_t smem_unused;
+    RG(scatter_shape(s.n_nodes, &a->chunk, &a->TK, &smem_unused));
+    a->n_tiles = (int)((P->desc.n_v + a->TK - 1) / a->TK);
+    // fixed point: cmax lines of (scaled) intensity <= 1 must stay below 2^31
+    {
+        const int64_t m = P->cmax + 1;
+        int bits = 0;
+        while (bits < 62 && ((int64_t)1 << bits) <= m) ++bits;
+        a->fx_scale = std::ldexp(1.f, std::max(0, 31 - bits));
+    }
+    a->err = P->err;
     if (s.p_atm > P->p_atm_max)
         return fail(RG_ERR_RANGE, "pressure %g atm above the plan's shift-index limit %g atm", s.p_atm,
                     P->p_atm_max);
@@ -485,6 +512,15 @@ void node_fold(double dv, double wG, double wL, double thresh, int* nfold, doubl
     *norm = 1.0 / v0;
 }
 
+// After a synchronisation: report (once) a bounded device wait that gave up.
+int take_err(rg_plan* P) {
+    if (*P->err_host) {
+        *P->err_host = 0;
+        return fail(RG_ERR_TIMEOUT, "a bounded device wait in the scatter gave up; the spectrum is invalid");
+    }
+    return RG_OK;
+}
+
 int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st, int timing, bool ldm_only,
                  rg_spectrum_info* info) {
     SpecHost s;
@@ -493,8 +529,12 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
     ScatterArgs sa;
     RG(build_scatter_args(P, c, s, &sa));
     const int n_v = (int)P->desc.n_v;
-    const int n_tiles = (n_v + sa.TK - 1) / sa.TK;
-    const size_t smem = scatter_smem_floats(s.n_nodes, sa.TK) * sizeof(float);
+    int ch_unused, tk_unused;
+    size_t smem;
+    RG(scatter_shape(s.n_nodes, &ch_unused, &tk_unused, &smem));
+    const int sms = P->lines->ctx->sms;
+    const int grid = std::max(std::min(sa.n_tiles, sms),
+                              (sa.n_tiles + kScatMaxTilesPerCta - 1) / kScatMaxTilesPerCta);
     cudaEvent_t* ev = P->ev;
     if (timing == 2) {
         if (P->ring.empty()) {
@@ -512,7 +552,7 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
     }
     if (timing) CU(cudaEventRecord(ev[0], st));
     CU(cudaMemsetAsync(P->counter, 0, sizeof(unsigned long long), st));
-    RG(launch_scatter(sa, n_tiles, smem, st));
+    RG(launch_scatter(sa, grid, smem, st));
     if (timing) CU(cudaEventRecord(ev[1], st));
     if (!ldm_only) {
         const rg_grid& g = s.grid;
@@ -594,6 +634,9 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
         RG(launch_col_ifft(ca, st));
         if (timing) CU(cudaEventRecord(ev[5], st));
     }
+    // publish the device error flag to pinned host memory and clear it
+    CU(cudaMemcpyAsync(P->err_host, P->err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemsetAsync(P->err, 0, sizeof(unsigned), st));
     if (info) {
         std::memset(info, 0, sizeof *info);
         info->grid = s.grid;
@@ -601,6 +644,7 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
     }
     if (timing == 1 && info) {
         CU(cudaStreamSynchronize(st));
+        RG(take_err(P));
         int last = ldm_only ? 1 : 5;
         for (int i = 0; i < last; ++i) CU(cudaEventElapsedTime(&info->stage_ms[i], P->ev[i], P->ev[i + 1]));
         CU(cudaEventElapsedTime(&info->stage_ms[5], P->ev[0], P->ev[last]));
@@ -642,6 +686,8 @@ int rg_ctx_create(int device, rg_ctx** out) {
     auto* c = new (std::nothrow) rg_ctx();
     if (!c) return fail(RG_ERR_OOM, "host allocation failed");
     c->device = device;
+    if (cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess || c->sms < 1)
+        c->sms = 1;
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete c;
@@ -707,18 +753,28 @@ int rg_lines_upload(rg_ctx* ctx, const rg_line_arrays* in, const rg_isotopes* is
             return bail(fail(e_ == cudaErrorMemoryAllocation ? RG_ERR_OOM : RG_ERR_CUDA, "%s: %s", #call, \
                              cudaGetErrorString(e_)));                                               \
     } while (0)
-    const size_t f4 = sizeof(float) * (size_t)n;
+    if (n > (int64_t)0x7fff0000) return bail(fail(RG_ERR_RANGE, "more than 2^31 lines"));
+    // arrays hold a multiple of 16 lines (zero padding) for the 16-line TMA copies
+    const int64_t npad = (n + kLinePad - 1) / kLinePad * kLinePad;
+    const size_t f4 = sizeof(float) * (size_t)n, f4p = sizeof(float) * (size_t)npad;
     CUB(cudaMalloc(&v0_tmp, sizeof(double) * n));
     CUB(cudaMalloc(&s_tmp, sizeof(double) * n));
     CUB(cudaMalloc(&flag, sizeof(int)));
-    CUB(cudaMalloc(&L->v0, sizeof(float2) * n));
-    CUB(cudaMalloc(&L->ls2, f4));
-    CUB(cudaMalloc(&L->el, f4));
-    CUB(cudaMalloc(&L->ga, f4));
-    CUB(cudaMalloc(&L->gs, f4));
-    CUB(cudaMalloc(&L->na, f4));
-    if (in->delta) CUB(cudaMalloc(&L->dl, f4));
-    if (in->iso && L->n_iso > 1) CUB(cudaMalloc(&L->iso, (size_t)n));
+    CUB(cudaMalloc(&L->v0, sizeof(float2) * npad));
+    CUB(cudaMalloc(&L->ls2, f4p));
+    CUB(cudaMalloc(&L->el, f4p));
+    CUB(cudaMalloc(&L->ga, f4p));
+    CUB(cudaMalloc(&L->gs, f4p));
+    CUB(cudaMalloc(&L->na, f4p));
+    if (in->delta) CUB(cudaMalloc(&L->dl, f4p));
+    if (in->iso && L->n_iso > 1) CUB(cudaMalloc(&L->iso, (size_t)npad));
+    if (npad > n) {   // padding lines: v0 = 0 lies outside every window and is dropped
+        const int64_t t = npad - n;
+        CUB(cudaMemsetAsync(L->v0 + n, 0, sizeof(float2) * t, st));
+        for (float* arr : {L->ls2, L->el, L->ga, L->gs, L->na, L->dl})
+            if (arr) CUB(cudaMemsetAsync(arr + n, 0, sizeof(float) * t, st));
+        if (L->iso) CUB(cudaMemsetAsync(L->iso + n, 0, (size_t)t, st));
+    }
     CUB(cudaMemsetAsync(flag, 0, sizeof(int), st));
     CUB(cudaMemcpyAsync(v0_tmp, in->v0, sizeof(double) * n, cudaMemcpyHostToDevice, st));
     CUB(cudaMemcpyAsync(s_tmp, in->s_ref, sizeof(double) * n, cudaMemcpyHostToDevice, st));
@@ -829,6 +885,23 @@ int rg_plan_create(rg_lines* L, const rg_plan_desc* d, rg_plan** out) {
     CU(cudaMalloc(&P->g, sizeof(float2) * (size_t)P->n));
     CU(cudaMalloc(&P->out_d, sizeof(float) * (size_t)d->n_v));
     CU(cudaMalloc(&P->counter, sizeof(unsigned long long)));
+    CU(cudaMalloc(&P->err, sizeof(unsigned)));
+    CU(cudaHostAlloc(&P->err_host, sizeof(unsigned), cudaHostAllocDefault));
+    *P->err_host = 0;
+    CU(cudaMemsetAsync(P->err, 0, sizeof(unsigned), L->ctx->stream));
+    {   // most lines that can touch one column (k0 in {c-1, c}, shifts up to E columns)
+        std::vector<int64_t> cs(P->col_count);
+        CU(cudaMemcpyAsync(cs.data(), P->col_start, sizeof(int64_t) * P->col_count, cudaMemcpyDeviceToHost,
+                           L->ctx->stream));
+        CU(cudaStreamSynchronize(L->ctx->stream));
+        int64_t m = 0;
+        for (int c = 0; c < (int)d->n_v; ++c) {
+            const int lo = std::max(0, c - 1 - E + P->col_off);
+            const int hi = std::min(P->col_count - 1, c + 1 + E + P->col_off);
+            m = std::max(m, cs[hi] - cs[lo]);
+        }
+        P->cmax = m;
+    }
     CU(cudaStreamSynchronize(L->ctx->stream));
     L->plans++;
     *out = guard.release();
@@ -854,6 +927,8 @@ int rg_plan_free(rg_plan* P) {
         dfree(P->g);
         dfree(P->out_d);
         dfree(P->counter);
+        dfree(P->err);
+        if (P->err_host) cudaFreeHost(P->err_host);
         for (auto& e : P->ev)
             if (e) cudaEventDestroy(e);
         for (auto& e : P->ring)
@@ -922,7 +997,7 @@ int rg_plan_stage_times(rg_plan* P, double* sum_ms, int64_t* count) {
         sum_ms[5] += ms;
     }
     P->ring_used = 0;
-    return RG_OK;
+    return take_err(P);
 }
 
 int rg_synthesize_host(rg_plan* P, const rg_conditions* c, float* out_host, void* stream, int timing,
@@ -935,7 +1010,7 @@ int rg_synthesize_host(rg_plan* P, const rg_conditions* c, float* out_host, void
     RG(run_spectrum(P, c, P->out_d, st, (timing && info) ? 1 : 0, false, info));
     CU(cudaMemcpyAsync(out_host, P->out_d, sizeof(float) * (size_t)P->desc.n_v, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
-    return RG_OK;
+    return take_err(P);
 }
 
 int rg_debug_ldm(rg_plan* P, const rg_conditions* c, float* ldm_host, int64_t capacity,
@@ -954,7 +1029,7 @@ int rg_debug_ldm(rg_plan* P, const rg_conditions* c, float* ldm_host, int64_t ca
     CU(cudaMemcpy2DAsync(ldm_host, sizeof(float) * P->desc.n_v, P->ldm, sizeof(float) * P->row_stride,
                          sizeof(float) * P->desc.n_v, nodes, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
-    return RG_OK;
+    return take_err(P);
 }
 
 }  // extern "C"

@@ -102,7 +102,27 @@ struct ScatterArgs {
     float bI_hi[kMaxIso], bI_lo[kMaxIso];   // (log(Qr N x) - log_scale) log2e
     float stim_c;             // c2/T log2e
     unsigned long long* in_window;   // nullable counter of lines in the window
+    // persistent TMA-fed scatter
+    float fx_scale;           // fixed-point scale 2^e of the tile accumulator
+    int n_tiles;
+    int chunk;                // lines per staged chunk (multiple of 16)
+    unsigned* err;            // set to 1 when a bounded wait gives up
 };
+
+// Lines are staged per chunk as [v0 8B][ls2][el][ga][gs][na][dl 4B each][iso 1B]
+// x chunk; line arrays are allocated with room for a multiple of 16 lines.
+constexpr int kLinePad = 16;
+constexpr int kScatThreads = 1024;
+constexpr int kScatMaxTilesPerCta = 512;
+#ifdef __CUDACC__
+#define RG_HD __host__ __device__
+#else
+#define RG_HD
+#endif
+RG_HD inline size_t scatter_stage_bytes(int chunk) { return (size_t)33 * chunk; }
+RG_HD inline size_t scatter_fixed_smem(int chunk) {
+    return 2 * scatter_stage_bytes(chunk) + 16 + 8 * kScatMaxTilesPerCta;
+}
 
 struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
     FftLen f1;
@@ -153,7 +173,8 @@ int launch_prepare_lines(const double* v0_d, const double* s_d, int64_t n, doubl
                          float2* v0_out, float* ls2_out, int* unsorted_flag, cudaStream_t st);
 int launch_col_index(const float2* v0, int64_t n, double vmin, double dv, int c_min, int count,
                      int64_t* col_start, cudaStream_t st);
-int launch_scatter(const ScatterArgs& a, int n_tiles, size_t smem, cudaStream_t st);
+int launch_scatter(const ScatterArgs& a, int grid, size_t smem, cudaStream_t st);
+int scatter_smem_optin(size_t* avail);
 int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st);
 int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st);
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st);

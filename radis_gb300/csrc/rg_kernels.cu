@@ -310,55 +310,93 @@ __global__ void k_col_index(const float2* __restrict__ v0, int64_t n, double vmi
 // keeps aligned groups of four columns together for the float4 flush.
 __device__ __forceinline__ int tile_addr(int node, int c, int TK) { return node * TK + (c ^ ((node & 7) << 2)); }
 
-__global__ void __launch_bounds__(512, 2) k_scatter(const ScatterArgs a) {
-    // The tile accumulates in 32-bit fixed point with native integer shared
-    // atomics: deterministic, and no compare-and-swap retry loops under
-    // contention.  A line adds at most its (scaled, <= 1) intensity to any one
-    // cell, so a cell's sum is bounded by the number of lines that can touch
-    // its column; the tile's scale 2^e keeps that bound below 2^31.
-    extern __shared__ uint4 tile4[];
-    unsigned* tile = reinterpret_cast<unsigned*>(tile4);
-    __shared__ int red_max[32];
-    const int k_start = blockIdx.x * a.TK;
-    const int tk = min(a.TK, a.n_v - k_start);
-    const int n4 = a.n_nodes * a.TK / 4;
-    for (int i = threadIdx.x; i < n4; i += blockDim.x) tile4[i] = make_uint4(0u, 0u, 0u, 0u);
+// --- TMA (cp.async.bulk) + mbarrier helpers ---------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-    auto col_idx = [&](int c) { return max(0, min(c + a.col_off, a.col_count - 1)); };
-    int cmax = 0;
-    for (int c = threadIdx.x; c < tk; c += blockDim.x) {
-        const int64_t cnt = a.col_start[col_idx(k_start + c + 1 + a.margin_cols)] -
-                            a.col_start[col_idx(k_start + c - 1 - a.margin_cols)];
-        cmax = max(cmax, (int)min(cnt, (int64_t)0x3fffffff));
-    }
-    for (int o = 16; o; o >>= 1) cmax = max(cmax, __shfl_xor_sync(0xffffffffu, cmax, o));
-    if ((threadIdx.x & 31) == 0) red_max[threadIdx.x >> 5] = cmax;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        int m = threadIdx.x < (blockDim.x >> 5) ? red_max[threadIdx.x] : 0;
-        for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (threadIdx.x == 0) red_max[0] = m;
-    }
-    __syncthreads();
-    // scale = 2^e with (cmax + 1) 2^e <= 2^31
-    const int e = 31 - (32 - __clz(red_max[0] + 1));
-    const float scale = ldexpf(1.f, max(e, 0));
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait (about one second of SM clocks); false when it gives up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > (1LL << 31)) return false;
+    return true;
+}
 
-    const int64_t i0 = a.col_start[col_idx(k_start - 1 - a.margin_cols)];
-    const int64_t i1 = a.col_start[col_idx(k_start + tk + a.margin_cols)];
-    unsigned int counted = 0;
+struct Stage {
+    const float2* v0;
+    const float* ls2;
+    const float* el;
+    const float* ga;
+    const float* gs;
+    const float* na;
+    const float* dl;
+    const uint8_t* iso;
+};
 
-#pragma unroll 2
-    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-        // issue every load of the line record up front
-        const float2 v = a.v0[i];
-        const float dl = a.dl ? a.dl[i] : 0.f;
-        const float gs = a.gs[i];
-        const float ga = a.ga[i];
-        const float na = a.na[i];
-        const float el = a.el[i];
-        const float ls2 = a.ls2[i];
-        const int is = a.iso ? (int)a.iso[i] : 0;
+__device__ __forceinline__ Stage stage_view(unsigned char* base, int chunk, bool has_dl, bool has_iso) {
+    Stage s;
+    s.v0 = reinterpret_cast<const float2*>(base);
+    s.ls2 = reinterpret_cast<const float*>(base + 8 * chunk);
+    s.el = reinterpret_cast<const float*>(base + 12 * chunk);
+    s.ga = reinterpret_cast<const float*>(base + 16 * chunk);
+    s.gs = reinterpret_cast<const float*>(base + 20 * chunk);
+    s.na = reinterpret_cast<const float*>(base + 24 * chunk);
+    s.dl = has_dl ? reinterpret_cast<const float*>(base + 28 * chunk) : nullptr;
+    s.iso = has_iso ? reinterpret_cast<const uint8_t*>(base + 32 * chunk) : nullptr;
+    return s;
+}
+
+// One thread: copy lines [start, start + count) of every column into a stage
+// buffer (16-line granularity: the arrays are padded to a multiple of 16).
+__device__ __forceinline__ void issue_chunk(const ScatterArgs& a, unsigned char* base, uint64_t* bar, int start,
+                                            int count) {
+    const uint32_t cp = (uint32_t)((count + kLinePad - 1) / kLinePad * kLinePad);
+    const int ch = a.chunk;
+    uint32_t bytes = cp * 8 + cp * 4 * 5;
+    if (a.dl) bytes += cp * 4;
+    if (a.iso) bytes += cp;
+    // the buffer was last read through the generic proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    mbar_expect_tx(bar, bytes);
+    tma_load_1d(base, a.v0 + start, cp * 8, bar);
+    tma_load_1d(base + 8 * ch, a.ls2 + start, cp * 4, bar);
+    tma_load_1d(base + 12 * ch, a.el + start, cp * 4, bar);
+    tma_load_1d(base + 16 * ch, a.ga + start, cp * 4, bar);
+    tma_load_1d(base + 20 * ch, a.gs + start, cp * 4, bar);
+    tma_load_1d(base + 24 * ch, a.na + start, cp * 4, bar);
+    if (a.dl) tma_load_1d(base + 28 * ch, a.dl + start, cp * 4, bar);
+    if (a.iso) tma_load_1d(base + 32 * ch, a.iso + start, cp, bar);
+}
+
+// Scale + scatter of the lines of one staged chunk into the tile accumulator.
+__device__ __forceinline__ unsigned scatter_chunk(const ScatterArgs& a, const Stage& st, int count, int k_start,
+                                                  int tk, unsigned* tile) {
+    unsigned counted = 0;
+    for (int j = threadIdx.x; j < count; j += blockDim.x) {
+        const float2 v = st.v0[j];
+        const float dl = st.dl ? st.dl[j] : 0.f;
         // k position in double-float: ((hi - vmin_hi) + (lo - vmin_lo + shift)) / dv
         float s, e1;
         two_sum(v.x, -a.vmin_hi, s, e1);
@@ -377,23 +415,26 @@ __global__ void __launch_bounds__(512, 2) k_scatter(const ScatterArgs a) {
         const bool own1 = (unsigned)(c0 + 1) < (unsigned)tk;
         if (!(own0 || own1)) continue;
         if (own0) ++counted;
+        const int is = st.iso ? (int)st.iso[j] : 0;
         // Gaussian / Lorentzian node coordinates (FWHM, log space); log v0 is
         // taken relative to v_ref so the FP32 log and offset do not cancel
         const float pl = fmaf(lg2(v.x * a.inv_vref), a.lgG_scale, a.cG[is]);
-        const float gam = fmaf(a.x_self, gs - ga, ga);
-        const float pm = fmaf(lg2(gam), a.lgL_scale, fmaf(na, a.tL, a.cL));
+        const float ga = st.ga[j];
+        const float gam = fmaf(a.x_self, st.gs[j] - ga, ga);
+        const float pm = fmaf(lg2(gam), a.lgL_scale, fmaf(st.na[j], a.tL, a.cL));
         const int l0 = min(max((int)floorf(pl), 0), a.NG - 2);
         const int m0 = min(max((int)floorf(pm), 0), a.NL - 2);
         const float tG = pl - (float)l0;
         const float tL = pm - (float)m0;
         // intensity: exponent log2(S') + a_T El + b_iso in double-float
+        const float el = st.el[j];
         const float ph = el * a.aT_hi;
         const float pe2 = fmaf(el, a.aT_hi, -ph) + el * a.aT_lo;
         float s1, f1, s2, f2;
         two_sum(ph, a.bI_hi[is], s1, f1);
-        two_sum(s1, ls2, s2, f2);
+        two_sum(s1, st.ls2[j], s2, f2);
         const float arg = s2 + (f1 + f2 + pe2 + a.bI_lo[is]);
-        const float I = ex2(arg) * (1.f - ex2(-a.stim_c * v.x)) * scale;
+        const float I = ex2(arg) * (1.f - ex2(-a.stim_c * v.x)) * a.fx_scale;
         const float I1 = tv * I;
         const float I0 = I - I1;
         const float w11 = tG * tL;
@@ -415,21 +456,110 @@ __global__ void __launch_bounds__(512, 2) k_scatter(const ScatterArgs a) {
             atomicAdd(&tile[tile_addr(n10 + 1, c0 + 1, a.TK)], __float2uint_rn(I1 * w11));
         }
     }
-    if (a.in_window && counted) atomicAdd(a.in_window, (unsigned long long)counted);
-    __syncthreads();
-    // flush: every column of the tile is owned by this CTA -> plain stores
-    const float inv = 1.f / scale;
-    const int tk4 = (tk + 3) >> 2;
-    const int per_row = a.TK >> 2;
-    for (int i = threadIdx.x; i < n4; i += blockDim.x) {
-        const int node = i / per_row;
-        const int c4 = i - node * per_row;
-        if (c4 < tk4) {
-            const uint4 u = tile4[node * per_row + (c4 ^ (node & 7))];
-            *reinterpret_cast<float4*>(&a.ldm[node * a.row_stride + k_start + 4 * c4]) =
-                make_float4((float)u.x * inv, (float)u.y * inv, (float)u.z * inv, (float)u.w * inv);
-        }
+    return counted;
+}
+
+// Persistent scatter: CTA b owns tiles b, b + G, b + 2G, ...  Thread 0 streams
+// the tiles' line records chunk by chunk into two stage buffers with TMA bulk
+// copies (mbarrier completion), one chunk ahead of the consumers, across tile
+// boundaries; all threads scatter the current chunk into the tile
+// accumulator (32-bit fixed point, native integer shared atomics,
+// deterministic) and flush each finished tile to HBM with plain stores.
+__global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int ch = a.chunk;
+    unsigned char* stage[2] = {smem, smem + scatter_stage_bytes(ch)};
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * scatter_stage_bytes(ch));
+    int2* rng = reinterpret_cast<int2*>(smem + 2 * scatter_stage_bytes(ch) + 16);
+    uint4* tile4 = reinterpret_cast<uint4*>(smem + scatter_fixed_smem(ch));
+    unsigned* tile = reinterpret_cast<unsigned*>(tile4);
+    const int G = gridDim.x;
+    const int nq = (a.n_tiles - (int)blockIdx.x + G - 1) / G;   // tiles of this CTA (<= kScatMaxTilesPerCta)
+    const int n4 = a.n_nodes * a.TK / 4;
+    const bool has_dl = a.dl != nullptr, has_iso = a.iso != nullptr;
+
+    auto col_idx = [&](int c) { return max(0, min(c + a.col_off, a.col_count - 1)); };
+    for (int q = threadIdx.x; q < nq; q += blockDim.x) {
+        const int k_start = ((int)blockIdx.x + q * G) * a.TK;
+        const int tk = min(a.TK, a.n_v - k_start);
+        const int lo = (int)a.col_start[col_idx(k_start - 1 - a.margin_cols)];
+        const int hi = (int)a.col_start[col_idx(k_start + tk + a.margin_cols)];
+        rng[q] = make_int2(lo / kLinePad * kLinePad, hi);   // 16-line aligned start
     }
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) tile4[i] = make_uint4(0u, 0u, 0u, 0u);
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    // successor of chunk (q, cs) in this CTA's chunk order, skipping empty tiles
+    auto next_chunk = [&](int q, int cs, int& nq2, int& ncs) -> bool {
+        if (q >= 0 && cs + ch < rng[q].y) {
+            nq2 = q;
+            ncs = cs + ch;
+            return true;
+        }
+        for (int r = q + 1; r < nq; ++r)
+            if (rng[r].x < rng[r].y) {
+                nq2 = r;
+                ncs = rng[r].x;
+                return true;
+            }
+        return false;
+    };
+    if (threadIdx.x == 0) {
+        int fq, fcs;
+        if (next_chunk(-1, 0, fq, fcs)) issue_chunk(a, stage[0], &bar[0], fcs, min(ch, rng[fq].y - fcs));
+    }
+
+    uint32_t g = 0;         // chunks consumed so far
+    bool bad = false;
+    unsigned counted = 0;
+    for (int q = 0; q < nq; ++q) {
+        const int k_start = ((int)blockIdx.x + q * G) * a.TK;
+        const int tk = min(a.TK, a.n_v - k_start);
+        const int b = rng[q].y;
+        for (int cs = rng[q].x; cs < b; cs += ch) {
+            if (threadIdx.x == 0) {
+                int nq2, ncs;   // refill the other buffer, released at the end of the last chunk
+                if (next_chunk(q, cs, nq2, ncs))
+                    issue_chunk(a, stage[(g + 1) & 1], &bar[(g + 1) & 1], ncs, min(ch, rng[nq2].y - ncs));
+            }
+            if (!mbar_wait(&bar[g & 1], (g >> 1) & 1)) bad = true;
+            if (__syncthreads_or(bad)) {
+                // give up: report, let the copies in flight land (bounded), leave
+                if (threadIdx.x == 0) {
+                    atomicExch(a.err, 1u);
+                    mbar_wait(&bar[(g + 1) & 1], ((g + 1) >> 1) & 1);
+                }
+                __syncthreads();
+                return;
+            }
+            counted += scatter_chunk(a, stage_view(stage[g & 1], ch, has_dl, has_iso), min(ch, b - cs), k_start, tk,
+                                     tile);
+            __syncthreads();   // stage[g & 1] free again
+            ++g;
+        }
+        // flush the finished tile (plain stores: this CTA owns its columns) and re-zero it
+        const float inv = 1.f / a.fx_scale;
+        const int tk4 = (tk + 3) >> 2;
+        const int per_row = a.TK >> 2;
+        for (int i = threadIdx.x; i < n4; i += blockDim.x) {
+            const int node = i / per_row;
+            const int c4 = i - node * per_row;
+            if (c4 < tk4) {
+                const int si = node * per_row + (c4 ^ (node & 7));
+                const uint4 u = tile4[si];
+                tile4[si] = make_uint4(0u, 0u, 0u, 0u);
+                *reinterpret_cast<float4*>(&a.ldm[node * a.row_stride + k_start + 4 * c4]) =
+                    make_float4((float)u.x * inv, (float)u.y * inv, (float)u.z * inv, (float)u.w * inv);
+            }
+        }
+        __syncthreads();
+    }
+    if (a.in_window && counted) atomicAdd(a.in_window, (unsigned long long)counted);
 }
 
 // ---------------------------------------------------------------------------
@@ -595,7 +725,6 @@ int col_block(int n1) {
     }
 }
 
-size_t scatter_smem_floats(int n_nodes, int TK) { return (size_t)n_nodes * TK; }
 
 // Opt the kernel in to the largest dynamic shared memory the device allows
 // next to the kernel's own static shared memory; checks that `need` fits.
@@ -641,10 +770,21 @@ int launch_col_index(const float2* v0, int64_t n, double vmin, double dv, int c_
     return check_launch();
 }
 
-int launch_scatter(const ScatterArgs& a, int n_tiles, size_t smem, cudaStream_t st) {
+int launch_scatter(const ScatterArgs& a, int grid, size_t smem, cudaStream_t st) {
     ALLOW_SMEM(k_scatter, smem);
-    k_scatter<<<n_tiles, 512, smem, st>>>(a);
+    k_scatter<<<grid, kScatThreads, smem, st>>>(a);
     return check_launch();
+}
+
+int scatter_smem_optin(size_t* avail) {
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return RG_ERR_CUDA;
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+        return RG_ERR_CUDA;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, k_scatter) != cudaSuccess) return RG_ERR_CUDA;
+    *avail = (size_t)optin - fa.sharedSizeBytes;
+    return RG_OK;
 }
 
 template <int N1>
