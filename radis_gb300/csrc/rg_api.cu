@@ -172,7 +172,7 @@ bool radices(int L, int* rad, int* np) {
     return r == 1 && k <= kMaxPasses;
 }
 
-constexpr int kN2Max = 512 * 24;   // row FFT limit (threads x accumulators)
+constexpr int kN2Max = 256 * 32;   // row FFT limit (threads x register accumulators)
 
 // choose n = n1 * n2 >= n_min, n1 a power of two <= 512, n2 = 32 * (5-smooth)
 bool choose_fft(int64_t n_min, int64_t forced, int* n1o, int* n2o) {
@@ -586,6 +586,8 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
         va->NL = g.n_L;
         va->y = P->y;
         va->g = P->g;
+        va->tw_hi = P->tw_hi;
+        va->tw_lo = P->tw_lo;
         va->inv_ndv = (float)(1.0 / ((double)P->n * P->desc.dv));
         va->half_fs = (float)(0.5 / P->desc.dv);
         const double thresh = P->desc.folding_thresh > 0 ? P->desc.folding_thresh : 1e-6;

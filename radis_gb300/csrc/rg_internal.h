@@ -150,6 +150,8 @@ struct VoigtArgs {        // K3 (row FFT + Voigt weights + pair reduction)
     int NL;
     const float2* y;
     float2* g;            // accumulator [n1][n2]
+    const float2* tw_hi;  // exp(-2 pi i 1024 t / N)
+    const float2* tw_lo;  // exp(-2 pi i t / N), t < 1024
     float inv_ndv;        // 1 / (N dv)
     float half_fs;        // 1 / (2 dv)
     float alpha[kMaxAxis];    // (pi wG_l)^2 / (4 ln 2) * log2e

@@ -171,7 +171,7 @@ __device__ __forceinline__ void twiddle(float2* v, const float2* __restrict__ tw
 __device__ __forceinline__ int rp(int i) { return i + (i >> 4); }
 __host__ __device__ constexpr int row_buf_len(int n) { return n + (n >> 4) + 1; }
 
-template <int R>
+template <int R, bool PIN, bool POUT>
 __device__ __forceinline__ void row_pass(const float2* __restrict__ in, float2* __restrict__ out, int L,
                                          int Ns, unsigned mag, const float2* __restrict__ tw) {
     const int M = L / R;
@@ -181,36 +181,51 @@ __device__ __forceinline__ void row_pass(const float2* __restrict__ in, float2* 
         const int k = j - q * Ns;
         float2 v[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = in[rp(j + r * M)];
+        for (int r = 0; r < R; ++r) v[r] = in[PIN ? rp(j + r * M) : j + r * M];
         if (Ns > 1) twiddle<R>(v, tw, k * twstep);
         dftR<R>(v);
         const int base = q * Ns * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) out[rp(base + r * Ns)] = v[r];
+        for (int r = 0; r < R; ++r) out[POUT ? rp(base + r * Ns) : base + r * Ns] = v[r];
     }
 }
 
-// Forward DFT of one row in shared memory; buf0 holds the input.  Returns the
-// buffer holding the result.  Ends with __syncthreads().
-__device__ float2* fft_row(float2* buf0, float2* buf1, const FftLen& P) {
+template <bool PIN, bool POUT>
+__device__ __forceinline__ void row_pass_r(int R, const float2* in, float2* out, int L, int Ns, unsigned mag,
+                                           const float2* tw) {
+    switch (R) {
+        case 2: row_pass<2, PIN, POUT>(in, out, L, Ns, mag, tw); break;
+        case 3: row_pass<3, PIN, POUT>(in, out, L, Ns, mag, tw); break;
+        case 4: row_pass<4, PIN, POUT>(in, out, L, Ns, mag, tw); break;
+        case 5: row_pass<5, PIN, POUT>(in, out, L, Ns, mag, tw); break;
+        default: row_pass<8, PIN, POUT>(in, out, L, Ns, mag, tw); break;
+    }
+}
+
+// Forward DFT of one row in shared memory; buf0 holds the input (plain
+// layout).  Only the first pass's strided writes (and the second pass's reads
+// of them) use the padded layout rp(); later passes access in plain layout.
+// Returns the buffer holding the result; *padded tells its layout.  Ends with
+// __syncthreads().
+__device__ float2* fft_row(float2* buf0, float2* buf1, const FftLen& P, bool* padded) {
     float2* in = buf0;
     float2* out = buf1;
     for (int p = 0; p < P.npass; ++p) {
         const int R = P.radix[p];
         const int Ns = P.ns[p];
         const unsigned mag = P.mag[p];
-        switch (R) {
-            case 2: row_pass<2>(in, out, P.L, Ns, mag, P.tw); break;
-            case 3: row_pass<3>(in, out, P.L, Ns, mag, P.tw); break;
-            case 4: row_pass<4>(in, out, P.L, Ns, mag, P.tw); break;
-            case 5: row_pass<5>(in, out, P.L, Ns, mag, P.tw); break;
-            default: row_pass<8>(in, out, P.L, Ns, mag, P.tw); break;
-        }
+        if (p == 0)
+            row_pass_r<false, true>(R, in, out, P.L, Ns, mag, P.tw);
+        else if (p == 1)
+            row_pass_r<true, false>(R, in, out, P.L, Ns, mag, P.tw);
+        else
+            row_pass_r<false, false>(R, in, out, P.L, Ns, mag, P.tw);
         __syncthreads();
         float2* t = in;
         in = out;
         out = t;
     }
+    *padded = P.npass == 1;
     return in;
 }
 
@@ -563,7 +578,7 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
 }
 
 // ---------------------------------------------------------------------------
-// K2: forward column FFT (length n1) of packed node pairs, times w_N^{n2 k1}
+// K2: forward column FFT (length n1) of packed node pairs
 // ---------------------------------------------------------------------------
 template <int N1>
 __global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_fft_fwd(const ColFftArgs a) {
@@ -584,14 +599,10 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_fft_fwd(const Col
         v[q] = nidx < a.n_v ? make_float2(__ldg(&ra[nidx]), __ldg(&rb[nidx])) : make_float2(0.f, 0.f);
     }
     col_fft8<N1>(v, sm, j, b, a.f1.tw);
+    // the four-step twiddle w_N^{n2 k1} is applied by the row kernel
     float2* y = a.y + (int64_t)pair * N1 * a.n2;
 #pragma unroll
-    for (int r = 0; r < 8; ++r) {
-        const int k1 = j + r * TPC;
-        float2 z = v[r];
-        if (k1 && n2i) z = cmul(z, twiddle_n(a.tw_hi, a.tw_lo, n2i * k1));
-        y[(int64_t)k1 * a.n2 + n2i] = z;
-    }
+    for (int r = 0; r < 8; ++r) y[(j + r * TPC) * a.n2 + n2i] = v[r];
 }
 
 // ---------------------------------------------------------------------------
@@ -625,45 +636,66 @@ __device__ __forceinline__ float voigt_eval(const NodeV& n, float f, float half_
     return v * n.nrm;
 }
 
+// smem: two padded row buffers, the bin frequencies f[t] and the four-step
+// twiddles w_N^{k1 t} of this row (computed once, used by every pair)
+__host__ __device__ inline size_t row_voigt_smem(int n2) {
+    return 2 * (size_t)row_buf_len(n2) * sizeof(float2) + (size_t)n2 * (sizeof(float) + sizeof(float2));
+}
+
+template <int ACC>   // bins per thread held in registers: ACC * kRowThreads >= n2
 __global__ void __launch_bounds__(kRowThreads) k_row_fft_voigt(const VoigtArgs a) {
     extern __shared__ float2 sm[];
     const int n2 = a.n2;
     float2* buf0 = sm;
     float2* buf1 = sm + row_buf_len(n2);
-    float2* acc = sm + 2 * row_buf_len(n2);
+    float2* twr = sm + 2 * row_buf_len(n2);
+    float* fq = reinterpret_cast<float*>(twr + n2);
     const int k1 = blockIdx.x;
+    const int n = (int)a.n;
     const int j0 = blockIdx.y * kPairGroup;
     const int j1 = min(j0 + kPairGroup, a.n_pairs);
-    // each thread owns bins t = threadIdx.x + i blockDim.x of acc: no sync needed
-    for (int t = threadIdx.x; t < n2; t += blockDim.x) acc[t] = make_float2(0.f, 0.f);
+    for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+        const int kk = k1 + a.n1 * t;
+        fq[t] = (float)min(kk, n - kk) * a.inv_ndv;
+        twr[t] = (k1 && t) ? twiddle_n(a.tw_hi, a.tw_lo, k1 * t) : make_float2(1.f, 0.f);
+    }
+    float2 acc[ACC];
+#pragma unroll
+    for (int q = 0; q < ACC; ++q) acc[q] = make_float2(0.f, 0.f);
+    __syncthreads();
 
     for (int j = j0; j < j1; ++j) {
         const float4* src = reinterpret_cast<const float4*>(a.y + ((int64_t)j * a.n1 + k1) * n2);
         for (int t = threadIdx.x; t < n2 / 2; t += blockDim.x) {
             const float4 q = __ldg(&src[t]);
-            buf0[rp(2 * t)] = make_float2(q.x, q.y);        // 2t and 2t+1 share one pad
-            buf0[rp(2 * t) + 1] = make_float2(q.z, q.w);
+            buf0[2 * t] = cmul(make_float2(q.x, q.y), twr[2 * t]);
+            buf0[2 * t + 1] = cmul(make_float2(q.z, q.w), twr[2 * t + 1]);
         }
         __syncthreads();
-        const float2* res = fft_row(buf0, buf1, a.f2);
+        bool padded;
+        const float2* res = fft_row(buf0, buf1, a.f2, &padded);
         const NodeV na = node_params(a, 2 * j);
         const NodeV nb = node_params(a, 2 * j + 1);
-        for (int t = threadIdx.x; t < n2; t += blockDim.x) {
-            const int64_t kk = (int64_t)k1 + (int64_t)a.n1 * t;
-            const int64_t kf = kk <= a.n - kk ? kk : a.n - kk;
-            const float f = (float)kf * a.inv_ndv;
-            const float va = voigt_eval(na, f, a.half_fs);
-            const float vb = voigt_eval(nb, f, a.half_fs);
-            const float2 z = res[rp(t)];
-            float2 c = acc[t];
-            c.x += z.x * va + z.y * vb;
-            c.y += z.y * va - z.x * vb;
-            acc[t] = c;
+#pragma unroll
+        for (int q = 0; q < ACC; ++q) {
+            const int t = threadIdx.x + q * kRowThreads;
+            if (t < n2) {
+                const float f = fq[t];
+                const float va = voigt_eval(na, f, a.half_fs);
+                const float vb = voigt_eval(nb, f, a.half_fs);
+                const float2 z = res[padded ? rp(t) : t];
+                acc[q].x += z.x * va + z.y * vb;
+                acc[q].y += z.y * va - z.x * vb;
+            }
         }
         __syncthreads();
     }
     float2* g = a.g + (int64_t)k1 * n2;
-    for (int t = threadIdx.x; t < n2; t += blockDim.x) atomicAdd(&g[t], acc[t]);
+#pragma unroll
+    for (int q = 0; q < ACC; ++q) {
+        const int t = threadIdx.x + q * kRowThreads;
+        if (t < n2) atomicAdd(&g[t], acc[q]);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -676,12 +708,13 @@ __global__ void __launch_bounds__(kRowThreads) k_row_ifft(const RowIfftArgs a) {
     float2* buf1 = sm + row_buf_len(n2);
     const int k1 = blockIdx.x;
     float2* g = a.g + (int64_t)k1 * n2;
-    for (int t = threadIdx.x; t < n2; t += blockDim.x) buf0[rp(t)] = conjf2(g[t]);
+    for (int t = threadIdx.x; t < n2; t += blockDim.x) buf0[t] = conjf2(g[t]);
     __syncthreads();
     // inverse DFT = conj(forward DFT(conj(x)))
-    const float2* res = fft_row(buf0, buf1, a.f2);
+    bool padded;
+    const float2* res = fft_row(buf0, buf1, a.f2, &padded);
     for (int t = threadIdx.x; t < n2; t += blockDim.x) {
-        float2 z = conjf2(res[rp(t)]);
+        float2 z = conjf2(res[padded ? rp(t) : t]);
         if (k1 && t) z = cmul(z, conjf2(twiddle_n(a.tw_hi, a.tw_lo, t * k1)));
         g[t] = z;
     }
@@ -804,12 +837,22 @@ int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st) {
     }
 }
 
-int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st) {
-    const size_t smem = (2 * (size_t)row_buf_len(a.n2) + a.n2) * sizeof(float2);
-    ALLOW_SMEM(k_row_fft_voigt, smem);
+template <int ACC>
+static int row_voigt(const VoigtArgs& a, cudaStream_t st) {
+    const size_t smem = row_voigt_smem(a.n2);
+    ALLOW_SMEM(k_row_fft_voigt<ACC>, smem);
     dim3 grid(a.n1, (a.n_pairs + kPairGroup - 1) / kPairGroup);
-    k_row_fft_voigt<<<grid, kRowThreads, smem, st>>>(a);
+    k_row_fft_voigt<ACC><<<grid, kRowThreads, smem, st>>>(a);
     return check_launch();
+}
+
+int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st) {
+    const int per = (a.n2 + kRowThreads - 1) / kRowThreads;
+    if (per <= 8) return row_voigt<8>(a, st);
+    if (per <= 16) return row_voigt<16>(a, st);
+    if (per <= 24) return row_voigt<24>(a, st);
+    if (per <= 32) return row_voigt<32>(a, st);
+    return RG_ERR_RANGE;
 }
 
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st) {
