@@ -147,27 +147,29 @@ int64_t next_smooth(int64_t x) {
     }
 }
 
+// Radix plan of a length L = 2^a 3^b 5^c: the leftover 2 or 4 first, then the
+// 3s and 5s, then radix 8 -- the last pass is radix 8 whenever 8 divides L,
+// which the row kernel relies on (n2 is a multiple of 32).
 bool radices(int L, int* rad, int* np) {
     int r = L, k = 0;
-    int a = 0;
+    int a = 0, b = 0, c = 0;
     while (r % 2 == 0) {
         r /= 2;
         ++a;
     }
-    while (a >= 3) {
-        rad[k++] = 8;
-        a -= 3;
-    }
-    if (a == 2) rad[k++] = 4;
-    if (a == 1) rad[k++] = 2;
     while (r % 3 == 0) {
         r /= 3;
-        rad[k++] = 3;
+        ++b;
     }
     while (r % 5 == 0) {
         r /= 5;
-        rad[k++] = 5;
+        ++c;
     }
+    if (a % 3 == 2) rad[k++] = 4;
+    if (a % 3 == 1) rad[k++] = 2;
+    for (int i = 0; i < b; ++i) rad[k++] = 3;
+    for (int i = 0; i < c; ++i) rad[k++] = 5;
+    for (int i = 0; i < a / 3; ++i) rad[k++] = 8;
     *np = k;
     return r == 1 && k <= kMaxPasses;
 }

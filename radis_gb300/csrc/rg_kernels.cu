@@ -636,65 +636,194 @@ __device__ __forceinline__ float voigt_eval(const NodeV& n, float f, float half_
     return v * n.nrm;
 }
 
-// smem: two padded row buffers, the bin frequencies f[t] and the four-step
-// twiddles w_N^{k1 t} of this row (computed once, used by every pair)
-__host__ __device__ inline size_t row_voigt_smem(int n2) {
-    return 2 * (size_t)row_buf_len(n2) * sizeof(float2) + (size_t)n2 * (sizeof(float) + sizeof(float2));
+// Two pairs travel together through the row transform as float4 elements
+// (row A in .xy, row B in .zw): they share the index arithmetic, the twiddle
+// loads and the shared-memory instructions.  Buffers use rp8(i) = i + i/8,
+// which keeps every 16-byte access pattern of the passes conflict-free.
+__device__ __forceinline__ int rp8(int i) { return i + (i >> 3); }
+__host__ __device__ constexpr int row4_len(int n) { return n + (n >> 3) + 1; }
+
+template <int R>
+__device__ __forceinline__ void twiddle2(float2* A, float2* B, const float2* __restrict__ tw, int s) {
+    float2 w[R];
+    w[0] = make_float2(1.f, 0.f);
+    w[1] = __ldg(&tw[s]);
+    if (R >= 3) w[2] = __ldg(&tw[2 * s]);
+    if (R >= 4) w[3] = cmul(w[1], w[2]);
+    if (R == 5) w[4] = cmul(w[2], w[2]);
+    if (R == 8) {
+        w[4] = __ldg(&tw[4 * s]);
+        w[5] = cmul(w[1], w[4]);
+        w[6] = cmul(w[2], w[4]);
+        w[7] = cmul(w[3], w[4]);
+    }
+#pragma unroll
+    for (int r = 1; r < R; ++r) {
+        A[r] = cmul(A[r], w[r]);
+        B[r] = cmul(B[r], w[r]);
+    }
 }
 
-template <int ACC>   // bins per thread held in registers: ACC * kRowThreads >= n2
-__global__ void __launch_bounds__(kRowThreads) k_row_fft_voigt(const VoigtArgs a) {
-    extern __shared__ float2 sm[];
+// first pass (sub-transform length 1): global rows -> registers -> smem
+template <int R>
+__device__ __forceinline__ void row2_first(const float2* __restrict__ ya, const float2* __restrict__ yb,
+                                           const float2* twr, float4* out, int L) {
+    const int M = L / R;
+    for (int j = threadIdx.x; j < M; j += blockDim.x) {
+        float2 A[R], B[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int i = j + r * M;
+            const float2 w = twr[i];
+            A[r] = cmul(__ldg(&ya[i]), w);
+            B[r] = yb ? cmul(__ldg(&yb[i]), w) : make_float2(0.f, 0.f);
+        }
+        dftR<R>(A);
+        dftR<R>(B);
+#pragma unroll
+        for (int r = 0; r < R; ++r) out[rp8(j * R + r)] = make_float4(A[r].x, A[r].y, B[r].x, B[r].y);
+    }
+}
+
+template <int R>
+__device__ __forceinline__ void row2_pass(const float4* __restrict__ in, float4* __restrict__ out, int L, int Ns,
+                                          unsigned mag, const float2* __restrict__ tw) {
+    const int M = L / R;
+    const int twstep = L / (Ns * R);
+    for (int j = threadIdx.x; j < M; j += blockDim.x) {
+        const int q = Ns == 1 ? j : (int)__umulhi((unsigned)j, mag);
+        const int k = j - q * Ns;
+        float2 A[R], B[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const float4 t = in[rp8(j + r * M)];
+            A[r] = make_float2(t.x, t.y);
+            B[r] = make_float2(t.z, t.w);
+        }
+        if (Ns > 1) twiddle2<R>(A, B, tw, k * twstep);
+        dftR<R>(A);
+        dftR<R>(B);
+        const int base = q * Ns * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) out[rp8(base + r * Ns)] = make_float4(A[r].x, A[r].y, B[r].x, B[r].y);
+    }
+}
+
+__host__ __device__ inline size_t row_voigt_smem(int n2) {
+    return 2 * (size_t)row4_len(n2) * sizeof(float4) + (size_t)n2 * sizeof(float2);
+}
+
+// IT = iterations of the last (radix-8) pass per thread: IT * kRowThreads * 8 >= n2
+template <int IT>
+__global__ void __launch_bounds__(kRowThreads, IT == 1 ? 3 : 1) k_row_fft_voigt(const VoigtArgs a) {
+    extern __shared__ float4 sm4[];
     const int n2 = a.n2;
-    float2* buf0 = sm;
-    float2* buf1 = sm + row_buf_len(n2);
-    float2* twr = sm + 2 * row_buf_len(n2);
-    float* fq = reinterpret_cast<float*>(twr + n2);
+    const int len = row4_len(n2);
+    float4* buf0 = sm4;
+    float4* buf1 = sm4 + len;
+    float2* twr = reinterpret_cast<float2*>(sm4 + 2 * len);
     const int k1 = blockIdx.x;
     const int n = (int)a.n;
     const int j0 = blockIdx.y * kPairGroup;
     const int j1 = min(j0 + kPairGroup, a.n_pairs);
-    for (int t = threadIdx.x; t < n2; t += blockDim.x) {
-        const int kk = k1 + a.n1 * t;
-        fq[t] = (float)min(kk, n - kk) * a.inv_ndv;
+    const FftLen& P = a.f2;
+    const int ML = n2 / 8;    // butterflies of the last pass (radix 8, sub-length ML)
+    for (int t = threadIdx.x; t < n2; t += blockDim.x)
         twr[t] = (k1 && t) ? twiddle_n(a.tw_hi, a.tw_lo, k1 * t) : make_float2(1.f, 0.f);
-    }
-    float2 acc[ACC];
+    // frequencies of the bins this thread owns in the last pass: t = jl + r ML
+    float fb[IT * 8];
+    float2 acc[IT * 8];
 #pragma unroll
-    for (int q = 0; q < ACC; ++q) acc[q] = make_float2(0.f, 0.f);
+    for (int it = 0; it < IT; ++it) {
+        const int jl = threadIdx.x + it * kRowThreads;
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            const int kk = k1 + a.n1 * (jl + r * ML);
+            fb[it * 8 + r] = jl < ML ? (float)min(kk, n - kk) * a.inv_ndv : 0.f;
+            acc[it * 8 + r] = make_float2(0.f, 0.f);
+        }
+    }
     __syncthreads();
 
-    for (int j = j0; j < j1; ++j) {
-        const float4* src = reinterpret_cast<const float4*>(a.y + ((int64_t)j * a.n1 + k1) * n2);
-        for (int t = threadIdx.x; t < n2 / 2; t += blockDim.x) {
-            const float4 q = __ldg(&src[t]);
-            buf0[2 * t] = cmul(make_float2(q.x, q.y), twr[2 * t]);
-            buf0[2 * t + 1] = cmul(make_float2(q.z, q.w), twr[2 * t + 1]);
+    for (int j = j0; j < j1; j += 2) {
+        const bool two = j + 1 < j1;
+        const float2* ya = a.y + ((int64_t)j * a.n1 + k1) * n2;
+        const float2* yb = two ? a.y + ((int64_t)(j + 1) * a.n1 + k1) * n2 : nullptr;
+        switch (P.radix[0]) {
+            case 2: row2_first<2>(ya, yb, twr, buf0, n2); break;
+            case 3: row2_first<3>(ya, yb, twr, buf0, n2); break;
+            case 4: row2_first<4>(ya, yb, twr, buf0, n2); break;
+            case 5: row2_first<5>(ya, yb, twr, buf0, n2); break;
+            default: row2_first<8>(ya, yb, twr, buf0, n2); break;
         }
         __syncthreads();
-        bool padded;
-        const float2* res = fft_row(buf0, buf1, a.f2, &padded);
-        const NodeV na = node_params(a, 2 * j);
-        const NodeV nb = node_params(a, 2 * j + 1);
+        float4* in = buf0;
+        float4* out = buf1;
+        for (int p = 1; p < P.npass - 1; ++p) {
+            const int Ns = P.ns[p];
+            const unsigned mag = P.mag[p];
+            switch (P.radix[p]) {
+                case 2: row2_pass<2>(in, out, n2, Ns, mag, P.tw); break;
+                case 3: row2_pass<3>(in, out, n2, Ns, mag, P.tw); break;
+                case 4: row2_pass<4>(in, out, n2, Ns, mag, P.tw); break;
+                case 5: row2_pass<5>(in, out, n2, Ns, mag, P.tw); break;
+                default: row2_pass<8>(in, out, n2, Ns, mag, P.tw); break;
+            }
+            __syncthreads();
+            float4* t = in;
+            in = out;
+            out = t;
+        }
+        // last pass (radix 8, sub-length ML, no shuffle: output t = jl + r ML),
+        // Voigt weights and accumulation in registers
+        const NodeV A0 = node_params(a, 2 * j), A1 = node_params(a, 2 * j + 1);
+        NodeV B0 = A0, B1 = A1;
+        if (two) {
+            B0 = node_params(a, 2 * j + 2);
+            B1 = node_params(a, 2 * j + 3);
+        }
 #pragma unroll
-        for (int q = 0; q < ACC; ++q) {
-            const int t = threadIdx.x + q * kRowThreads;
-            if (t < n2) {
-                const float f = fq[t];
-                const float va = voigt_eval(na, f, a.half_fs);
-                const float vb = voigt_eval(nb, f, a.half_fs);
-                const float2 z = res[padded ? rp(t) : t];
-                acc[q].x += z.x * va + z.y * vb;
-                acc[q].y += z.y * va - z.x * vb;
+        for (int it = 0; it < IT; ++it) {
+            const int jl = threadIdx.x + it * kRowThreads;
+            if (jl < ML) {
+                float2 A[8], B[8];
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    const float4 t = in[rp8(jl + r * ML)];
+                    A[r] = make_float2(t.x, t.y);
+                    B[r] = make_float2(t.z, t.w);
+                }
+                twiddle2<8>(A, B, P.tw, jl);   // w_{n2}^{r jl}
+                dft8(A);
+                dft8(B);
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    const float f = fb[it * 8 + r];
+                    const float va = voigt_eval(A0, f, a.half_fs);
+                    const float vb = voigt_eval(A1, f, a.half_fs);
+                    float2 c = acc[it * 8 + r];
+                    c.x += A[r].x * va + A[r].y * vb;
+                    c.y += A[r].y * va - A[r].x * vb;
+                    if (two) {
+                        const float wa = voigt_eval(B0, f, a.half_fs);
+                        const float wb = voigt_eval(B1, f, a.half_fs);
+                        c.x += B[r].x * wa + B[r].y * wb;
+                        c.y += B[r].y * wa - B[r].x * wb;
+                    }
+                    acc[it * 8 + r] = c;
+                }
             }
         }
         __syncthreads();
     }
     float2* g = a.g + (int64_t)k1 * n2;
 #pragma unroll
-    for (int q = 0; q < ACC; ++q) {
-        const int t = threadIdx.x + q * kRowThreads;
-        if (t < n2) atomicAdd(&g[t], acc[q]);
+    for (int it = 0; it < IT; ++it) {
+        const int jl = threadIdx.x + it * kRowThreads;
+        if (jl < ML) {
+#pragma unroll
+            for (int r = 0; r < 8; ++r) atomicAdd(&g[jl + r * ML], acc[it * 8 + r]);
+        }
     }
 }
 
@@ -847,11 +976,11 @@ static int row_voigt(const VoigtArgs& a, cudaStream_t st) {
 }
 
 int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st) {
-    const int per = (a.n2 + kRowThreads - 1) / kRowThreads;
-    if (per <= 8) return row_voigt<8>(a, st);
-    if (per <= 16) return row_voigt<16>(a, st);
-    if (per <= 24) return row_voigt<24>(a, st);
-    if (per <= 32) return row_voigt<32>(a, st);
+    if (a.f2.npass < 2 || a.f2.radix[a.f2.npass - 1] != 8) return RG_ERR_RANGE;
+    const int per = (a.n2 / 8 + kRowThreads - 1) / kRowThreads;
+    if (per <= 1) return row_voigt<1>(a, st);
+    if (per <= 2) return row_voigt<2>(a, st);
+    if (per <= 4) return row_voigt<4>(a, st);
     return RG_ERR_RANGE;
 }
 
