@@ -117,7 +117,7 @@ struct rg_plan {
     // workspace (grow-only)
     int nodes_cap = 0;
     int64_t row_stride = 0;
-    float* ldm = nullptr;
+    unsigned* ldm = nullptr;          // LDM as fixed-point words of the scatter
     float2* y = nullptr;
     float2* g = nullptr;
     float* out_d = nullptr;
@@ -125,6 +125,7 @@ struct rg_plan {
     unsigned* err = nullptr;          // device flag set by a bounded wait that gave up
     unsigned* err_host = nullptr;     // pinned copy of err, refreshed after every spectrum
     int64_t cmax = 0;                 // max lines that can touch one grid column
+    float last_fx_scale = 1.f;        // fixed-point scale of the last scatter
     cudaEvent_t ev[6] = {nullptr};
     // ring of per-stage events recorded without synchronisation (timing == 2)
     static constexpr int kRing = 256;
@@ -399,7 +400,7 @@ int ensure_workspace(rg_plan* P, int n_nodes) {
     dfree(P->ldm);
     dfree(P->y);
     P->nodes_cap = 0;
-    CU(cudaMalloc(&P->ldm, sizeof(float) * (size_t)cap * P->row_stride));
+    CU(cudaMalloc(&P->ldm, sizeof(unsigned) * (size_t)cap * P->row_stride));
     CU(cudaMalloc(&P->y, sizeof(float2) * (size_t)(cap / 2) * P->n));
     P->nodes_cap = cap;
     return RG_OK;
@@ -555,6 +556,7 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
     if (timing) CU(cudaEventRecord(ev[0], st));
     CU(cudaMemsetAsync(P->counter, 0, sizeof(unsigned long long), st));
     RG(launch_scatter(sa, grid, smem, st));
+    P->last_fx_scale = sa.fx_scale;
     if (timing) CU(cudaEventRecord(ev[1], st));
     if (!ldm_only) {
         const rg_grid& g = s.grid;
@@ -570,6 +572,7 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
         ca.row_stride = P->row_stride;
         ca.n_pairs = s.n_nodes / 2;
         ca.ldm = P->ldm;
+        ca.inv_fx_scale = 1.f / sa.fx_scale;
         ca.y = P->y;
         ca.tw_hi = P->tw_hi;
         ca.tw_lo = P->tw_lo;
@@ -580,6 +583,7 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
         if (!va) return fail(RG_ERR_OOM, "host allocation failed");
         std::unique_ptr<VoigtArgs> vguard(va);
         va->f2 = P->f2;
+        va->threads = row_threads(P->f2);
         va->n1 = P->n1;
         va->n2 = P->n2;
         va->n = P->n;
@@ -1030,10 +1034,15 @@ int rg_debug_ldm(rg_plan* P, const rg_conditions* c, float* ldm_host, int64_t ca
     const int nodes = inf->grid.n_G * inf->grid.n_L;
     if (capacity < (int64_t)nodes * P->desc.n_v)
         return fail(RG_ERR_ARG, "capacity %lld < %lld", (long long)capacity, (long long)nodes * P->desc.n_v);
-    CU(cudaMemcpy2DAsync(ldm_host, sizeof(float) * P->desc.n_v, P->ldm, sizeof(float) * P->row_stride,
+    CU(cudaMemcpy2DAsync(ldm_host, sizeof(float) * P->desc.n_v, P->ldm, sizeof(unsigned) * P->row_stride,
                          sizeof(float) * P->desc.n_v, nodes, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
-    return take_err(P);
+    RG(take_err(P));
+    // the device LDM holds fixed-point words: convert in place
+    const float inv = 1.f / P->last_fx_scale;
+    unsigned* w = reinterpret_cast<unsigned*>(ldm_host);
+    for (int64_t i = 0; i < (int64_t)nodes * P->desc.n_v; ++i) ldm_host[i] = (float)w[i] * inv;
+    return RG_OK;
 }
 
 }  // extern "C"

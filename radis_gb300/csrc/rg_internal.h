@@ -86,7 +86,7 @@ struct ScatterArgs {
     int n_nodes;          // padded to even
     int NG, NL;
     int64_t row_stride;
-    float* ldm;
+    unsigned* ldm;        // fixed-point words, value = word / fx_scale
     int margin_cols;
     float vmin_hi, vmin_lo;
     float inv_dv_hi, inv_dv_lo;
@@ -132,7 +132,8 @@ struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
     int64_t n;            // n_ft
     int64_t row_stride;
     int n_pairs;
-    const float* ldm;     // K2 input
+    const unsigned* ldm;  // K2 input: fixed-point words of the scatter
+    float inv_fx_scale;   // 1 / fixed-point scale
     float2* y;            // K2 output [pair][n1][n2]
     const float2* tw_hi;  // exp(-2 pi i 1024 t / N)
     const float2* tw_lo;  // exp(-2 pi i t / N), t < 1024
@@ -143,6 +144,7 @@ struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
 
 struct VoigtArgs {        // K3 (row FFT + Voigt weights + pair reduction)
     FftLen f2;
+    int threads;          // block size (row_threads)
     int n1, n2;
     int64_t n;
     int n_pairs;
@@ -182,6 +184,7 @@ int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st);
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st);
 int launch_col_ifft(const ColFftArgs& a, cudaStream_t st);
 int col_block(int n1);               // columns per CTA of the column FFTs
+int row_threads(const FftLen& f);    // block size of the forward row kernel
 size_t scatter_smem_floats(int n_nodes, int TK);
 
 }  // namespace rg

@@ -557,19 +557,18 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
             __syncthreads();   // stage[g & 1] free again
             ++g;
         }
-        // flush the finished tile (plain stores: this CTA owns its columns) and re-zero it
-        const float inv = 1.f / a.fx_scale;
+        // flush the finished tile as raw fixed-point words (plain stores: this
+        // CTA owns its columns; the column FFT converts them) and re-zero it
         const int tk4 = (tk + 3) >> 2;
         const int per_row = a.TK >> 2;
-        for (int i = threadIdx.x; i < n4; i += blockDim.x) {
-            const int node = i / per_row;
-            const int c4 = i - node * per_row;
-            if (c4 < tk4) {
-                const int si = node * per_row + (c4 ^ (node & 7));
-                const uint4 u = tile4[si];
-                tile4[si] = make_uint4(0u, 0u, 0u, 0u);
-                *reinterpret_cast<float4*>(&a.ldm[node * a.row_stride + k_start + 4 * c4]) =
-                    make_float4((float)u.x * inv, (float)u.y * inv, (float)u.z * inv, (float)u.w * inv);
+        const int lane = threadIdx.x & 31;
+        for (int node = threadIdx.x >> 5; node < a.n_nodes; node += blockDim.x >> 5) {
+            uint4* row = tile4 + node * per_row;
+            uint4* dst = reinterpret_cast<uint4*>(a.ldm + node * a.row_stride + k_start);
+            const int sw = node & 7;
+            for (int c4 = lane; c4 < tk4; c4 += 32) {
+                dst[c4] = row[c4 ^ sw];
+                row[c4 ^ sw] = make_uint4(0u, 0u, 0u, 0u);
             }
         }
         __syncthreads();
@@ -589,14 +588,17 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_fft_fwd(const Col
     const int j = threadIdx.x / B;
     const int c0 = blockIdx.x * B;
     const int pair = blockIdx.y;
-    const float* ra = a.ldm + (int64_t)(2 * pair) * a.row_stride;
-    const float* rb = ra + a.row_stride;
+    // the LDM holds the scatter's fixed-point words: value = word / fx_scale
+    const unsigned* ra = a.ldm + (int64_t)(2 * pair) * a.row_stride;
+    const unsigned* rb = ra + a.row_stride;
+    const float inv = a.inv_fx_scale;
     const int n2i = c0 + b;
     float2 v[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int64_t nidx = (int64_t)(j + q * TPC) * a.n2 + n2i;
-        v[q] = nidx < a.n_v ? make_float2(__ldg(&ra[nidx]), __ldg(&rb[nidx])) : make_float2(0.f, 0.f);
+        v[q] = nidx < a.n_v ? make_float2((float)__ldg(&ra[nidx]) * inv, (float)__ldg(&rb[nidx]) * inv)
+                            : make_float2(0.f, 0.f);
     }
     col_fft8<N1>(v, sm, j, b, a.f1.tw);
     // the four-step twiddle w_N^{n2 k1} is applied by the row kernel
@@ -608,7 +610,8 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_fft_fwd(const Col
 // ---------------------------------------------------------------------------
 // K3: row FFT (length n2) of each pair, Voigt-FT weights, sum over pairs
 // ---------------------------------------------------------------------------
-constexpr int kRowThreads = 256;
+constexpr int kRowThreads = 256;      // inverse row kernel
+constexpr int kRowMaxThreads = 384;   // forward row kernel (per-plan count, see row_threads)
 
 struct NodeV {
     float al, bm, nrm;
@@ -626,13 +629,20 @@ __device__ __forceinline__ NodeV node_params(const VoigtArgs& a, int node) {
     return n;
 }
 
+// folded copies of the Voigt FT (broadening.py:1914-1926): alias frequencies
+// q/(2 dv) + (f or 1/(2 dv) - f); rare, kept out of line
+__device__ __noinline__ float voigt_folds(float al, float bm, int nf, float f, float half_fs) {
+    float v = 0.f;
+    for (int q = 1; q <= nf; ++q) {
+        const float fq = q * half_fs + ((q & 1) ? half_fs - f : f);
+        v += ex2(-fmaf(al * fq, fq, bm * fq));
+    }
+    return v;
+}
+
 __device__ __forceinline__ float voigt_eval(const NodeV& n, float f, float half_fs) {
     float v = ex2(-fmaf(n.al * f, f, n.bm * f));
-    for (int q = 1; q <= n.nf; ++q) {
-        // alias frequency (broadening.py:1914-1926): q/(2 dv) + (f or 1/(2 dv) - f)
-        const float fq = q * half_fs + ((q & 1) ? half_fs - f : f);
-        v += ex2(-fmaf(n.al * fq, fq, n.bm * fq));
-    }
+    if (n.nf) v += voigt_folds(n.al, n.bm, n.nf, f, half_fs);
     return v * n.nrm;
 }
 
@@ -715,7 +725,7 @@ __host__ __device__ inline size_t row_voigt_smem(int n2) {
 
 // IT = iterations of the last (radix-8) pass per thread: IT * kRowThreads * 8 >= n2
 template <int IT>
-__global__ void __launch_bounds__(kRowThreads, IT == 1 ? 3 : 1) k_row_fft_voigt(const VoigtArgs a) {
+__global__ void __launch_bounds__(kRowMaxThreads, IT == 1 ? 2 : 1) k_row_fft_voigt(const VoigtArgs a) {
     extern __shared__ float4 sm4[];
     const int n2 = a.n2;
     const int len = row4_len(n2);
@@ -735,7 +745,7 @@ __global__ void __launch_bounds__(kRowThreads, IT == 1 ? 3 : 1) k_row_fft_voigt(
     float2 acc[IT * 8];
 #pragma unroll
     for (int it = 0; it < IT; ++it) {
-        const int jl = threadIdx.x + it * kRowThreads;
+        const int jl = threadIdx.x + it * blockDim.x;
 #pragma unroll
         for (int r = 0; r < 8; ++r) {
             const int kk = k1 + a.n1 * (jl + r * ML);
@@ -784,7 +794,7 @@ __global__ void __launch_bounds__(kRowThreads, IT == 1 ? 3 : 1) k_row_fft_voigt(
         }
 #pragma unroll
         for (int it = 0; it < IT; ++it) {
-            const int jl = threadIdx.x + it * kRowThreads;
+            const int jl = threadIdx.x + it * blockDim.x;
             if (jl < ML) {
                 float2 A[8], B[8];
 #pragma unroll
@@ -819,7 +829,7 @@ __global__ void __launch_bounds__(kRowThreads, IT == 1 ? 3 : 1) k_row_fft_voigt(
     float2* g = a.g + (int64_t)k1 * n2;
 #pragma unroll
     for (int it = 0; it < IT; ++it) {
-        const int jl = threadIdx.x + it * kRowThreads;
+        const int jl = threadIdx.x + it * blockDim.x;
         if (jl < ML) {
 #pragma unroll
             for (int r = 0; r < 8; ++r) atomicAdd(&g[jl + r * ML], acc[it * 8 + r]);
@@ -971,13 +981,14 @@ static int row_voigt(const VoigtArgs& a, cudaStream_t st) {
     const size_t smem = row_voigt_smem(a.n2);
     ALLOW_SMEM(k_row_fft_voigt<ACC>, smem);
     dim3 grid(a.n1, (a.n_pairs + kPairGroup - 1) / kPairGroup);
-    k_row_fft_voigt<ACC><<<grid, kRowThreads, smem, st>>>(a);
+    k_row_fft_voigt<ACC><<<grid, a.threads, smem, st>>>(a);
     return check_launch();
 }
 
 int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st) {
     if (a.f2.npass < 2 || a.f2.radix[a.f2.npass - 1] != 8) return RG_ERR_RANGE;
-    const int per = (a.n2 / 8 + kRowThreads - 1) / kRowThreads;
+    if (a.threads < 32 || a.threads > kRowMaxThreads || a.threads % 32) return RG_ERR_RANGE;
+    const int per = (a.n2 / 8 + a.threads - 1) / a.threads;
     if (per <= 1) return row_voigt<1>(a, st);
     if (per <= 2) return row_voigt<2>(a, st);
     if (per <= 4) return row_voigt<4>(a, st);
@@ -1007,4 +1018,28 @@ int launch_col_ifft(const ColFftArgs& a, cudaStream_t st) {
     }
 }
 
+}  // namespace rg
+
+namespace rg {
+// Thread count of the forward row kernel for a row plan: the multiple of 32 in
+// [128, kRowMaxThreads] that wastes the fewest butterfly slots over the passes
+// (ties -> more threads).
+int row_threads(const FftLen& f) {
+    int best = 256;
+    double best_eff = -1.0;
+    for (int T = 128; T <= kRowMaxThreads; T += 32) {
+        long slots = 0, work = 0;
+        for (int p = 0; p < f.npass; ++p) {
+            const int M = f.L / f.radix[p];
+            slots += (long)((M + T - 1) / T) * T;
+            work += M;
+        }
+        const double eff = (double)work / (double)slots;
+        if (eff > best_eff + 1e-9 || (eff > best_eff - 1e-9 && T > best)) {
+            best_eff = eff;
+            best = T;
+        }
+    }
+    return best;
+}
 }  // namespace rg
