@@ -2,6 +2,7 @@
 """Benchmark: equilibrium LDM spectra/s on the 5M-line CO2-like workload.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload co2_5M|h2o_100M]
 
 One step = one spectrum (scatter -> FFT/Voigt reduce -> IFFT) of the 5M-line
 CO2-like list over 2000-2400 cm-1 at 0.001 cm-1 (400 001 points), 8 x 16 LDM
@@ -37,12 +38,21 @@ KERNELS_PER_STEP = 5
 STAGES = ["k_scatter", "k_col_fft_fwd", "k_row_fft_voigt", "k_row_ifft", "k_col_ifft"]
 
 
-def workload_desc(n_lines, n_v, grid):
+# name: (label, lines factory, molar mass, vmin, vmax, wstep, T, p_bar, x, n_G, n_L)
+WORKLOADS = {
+    "co2_5M": ("CO2-like", "co2_like", 44.0, 2000.0, 2400.0, 0.001, 1500.0, 1.0, 0.1, 8, 16),
+    "h2o_100M": ("H2O-like", "h2o_like", 18.0, 500.0, 8000.0, 0.005, 2000.0, 1.0, 0.2, 12, 24),
+}
+
+
+def workload_desc(name, n_lines, n_v, grid, nbytes):
+    label, _, _, vmin, vmax, ws, T, p, x, _, _ = WORKLOADS[name]
     return {
-        "workload": (f"CO2-like synthetic list, {n_lines} lines, 2000-2400 cm-1 at 0.001 cm-1 "
-                     f"({n_v} points), {grid[0]}x{grid[1]} LDM nodes, T=1500 K, p=1 bar, x=0.1"),
+        "workload": (f"{label} synthetic list, {n_lines} lines, {vmin:g}-{vmax:g} cm-1 at {ws:g} cm-1 "
+                     f"({n_v} points), {grid[0]}x{grid[1]} LDM nodes, T={T:g} K, p={p:g} bar, x={x:g}"),
         "n_lines": n_lines, "n_v": n_v, "n_ft": grid[2], "ldm_nodes": [grid[0], grid[1]],
-        "l2": "inputs larger than L2 (line list 160 MB, LDM 205 MB, FFT workspace 420 MB)",
+        "l2": ("inputs larger than L2 (line list %d MB, LDM %d MB, FFT workspace %d MB)"
+               % tuple(b // 1000000 for b in nbytes)),
         "parallelism": "replicas",
     }
 
@@ -138,65 +148,68 @@ def load_traffic():
     return {}
 
 
-def cpu_baseline_sample(lines, grid, workers, frac=20):
+def cpu_baseline_sample(wl, lines, grid, n_ft, workers, frac=20):
     """Oracle timing on a bounded sample: the per-line stages (scaling +
     scatter) on 1/frac of the lines (contiguous block), scaled by frac, plus
     the full FFT/convolution stage (independent of the line count)."""
     import numpy as np
 
     from oracle import ldm_oracle as O
+    _, _, M, vmin, vmax, ws, T, p, x, _, _ = WORKLOADS[wl]
+    n_v = int(round((vmax - vmin) / ws)) + 1
     n = len(lines["v0"])
     m = n // frac
     lo = (n - m) // 2
     sub = {k: np.asarray(v)[lo:lo + m] for k, v in lines.items()}
     t0 = time.perf_counter()
-    kpos, lgG, lgL, S = O.line_quantities(sub, 1500.0, 1.0, 0.1, 2000.0, 0.001, molar_mass=44.0)
-    LDM = O.ldm_scatter(kpos, lgG, lgL, S, 400001, grid)
+    kpos, lgG, lgL, S = O.line_quantities(sub, T, p, x, vmin, ws, molar_mass=M)
+    LDM = O.ldm_scatter(kpos, lgG, lgL, S, n_v, grid)
     t1 = time.perf_counter()
-    O.ldm_convolve(LDM, 400001, 0.001, grid, int(grid_nft(grid)), fft_workers=workers)
+    O.ldm_convolve(LDM, n_v, ws, grid, int(n_ft), fft_workers=workers)
     t2 = time.perf_counter()
     return (t1 - t0) * (n / m) + (t2 - t1), (t1 - t0), (t2 - t1), m
 
 
-_NFT = {}
-
-
-def grid_nft(grid):
-    return _NFT["n_ft"]
+def load_workload(wl):
+    from radis_gb300 import synthetic as S
+    _, fac, M, vmin, vmax, ws, T, p, x, nG, nL = WORKLOADS[wl]
+    lines = getattr(S, fac)()
+    return lines, M, vmin, ws, S.grid_points(vmin, vmax, ws), T, p, x, nG, nL
 
 
 def run_reference(args):
-    ws, rank, _ = dist_env()
+    ws_, rank, _ = dist_env()
     if rank != 0:
         return 0
-    from radis_gb300 import _build, _lib as L, synthetic as S
+    from radis_gb300 import _build, _lib as L
     _build.build()
-    lines = S.co2_like()
-    n_v = S.grid_points(2000.0, 2400.0, 0.001)
-    g = L.grid_estimate(lines, 44.0, 2000.0, 0.001, n_v, 1500.0, 1.0, 0.1, n_G=8, n_L=16)
-    _NFT["n_ft"] = g.n_ft
+    wl = args.workload
+    lines, M, vmin, dv, n_v, T, p, x, nG, nL = load_workload(wl)
+    g = L.grid_estimate(lines, M, vmin, dv, n_v, T, p, x, n_G=nG, n_L=nL)
     workers = os.cpu_count() or 1
     times = []
     parts = []
     for i in range(args.warmup + args.steps):
-        t, tl, tc, m = cpu_baseline_sample(lines, g.axes(), workers)
+        t, tl, tc, m = cpu_baseline_sample(wl, lines, g.axes(), g.n_ft, workers)
         if i >= args.warmup:
             times.append(t)
             parts.append((tl, tc))
     step = statistics.mean(times)
     value = 1.0 / step
-    sample = (f"per step: scaling+scatter of {m} of {len(lines['v0'])} lines (x{len(lines['v0']) / m:.0f}) "
+    n = len(lines["v0"])
+    sample = (f"per step: scaling+scatter of {m} of {n} lines (x{n / m:.0f}) "
               f"+ full FFT/Voigt stage ({g.n_G * g.n_L} node rows of {g.n_ft}); numpy/scipy FP64")
+    nbytes = (n * 32, g.n_G * g.n_L * n_v * 4, g.n_G * g.n_L * g.n_ft * 4)
     out = {
-        "metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": ws, "steps": args.steps,
+        "metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": ws_, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": workload_desc(len(lines["v0"]), n_v, (g.n_G, g.n_L, g.n_ft)),
+        "config": workload_desc(wl, n, n_v, (g.n_G, g.n_L, g.n_ft), nbytes),
         "cpu_baseline": {"value": value, "unit": "spectra/s", "cores": workers, "kind": "port",
                          "sample": sample + f"; FFT threads {workers}, add.at single-threaded"},
         "e2e": {"value": value, "unit": "spectra/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "stage_s": {"lines_scaled": statistics.mean(p[0] for p in parts) * len(lines["v0"]) / m,
-                    "fft_voigt": statistics.mean(p[1] for p in parts)},
+        "stage_s": {"lines_scaled": statistics.mean(q[0] for q in parts) * n / m,
+                    "fft_voigt": statistics.mean(q[1] for q in parts)},
     }
     print(json.dumps(out))
     return 0
@@ -217,15 +230,13 @@ def run_ours(args):
         dist.barrier()
     from radis_gb300 import _lib as L, synthetic as S
 
-    T, p, x = 1500.0, 1.0, 0.1
-    vmin, vmax, dv = 2000.0, 2400.0, 0.001
-    n_v = S.grid_points(vmin, vmax, dv)
-    lines = S.co2_like()
+    wl = args.workload
+    lines, M, vmin, dv, n_v, T, p, x, nG, nL = load_workload(wl)
     n_lines = len(lines["v0"])
     ctx = L.Context(local)
     t0 = time.perf_counter()
-    ln = L.Lines(ctx, lines, 44.0)
-    plan = L.Plan(ln, vmin, dv, n_v, n_G=8, n_L=16)
+    ln = L.Lines(ctx, lines, M)
+    plan = L.Plan(ln, vmin, dv, n_v, n_G=nG, n_L=nL)
     setup_s = time.perf_counter() - t0
     g = plan.grid(T, p, x)
     n_nodes = g.n_G * g.n_L + (g.n_G * g.n_L) % 2
@@ -285,10 +296,10 @@ def run_ours(args):
         e2e_ms = float(t.item())
     # cold path: upload from host arrays + plan + one spectrum (eq_spectrum_gpu with exit_gpu)
     cold = []
-    for _ in range(2):
+    for _ in range(2 if n_lines <= 10_000_000 else 1):
         t0 = time.perf_counter()
-        ln2 = L.Lines(ctx, lines, 44.0)
-        pl2 = L.Plan(ln2, vmin, dv, n_v, n_G=8, n_L=16)
+        ln2 = L.Lines(ctx, lines, M)
+        pl2 = L.Plan(ln2, vmin, dv, n_v, n_G=nG, n_L=nL)
         pl2.synthesize_host(T, p, x, out=host)
         cold.append(time.perf_counter() - t0)
         pl2.close()
@@ -310,7 +321,8 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": ws, "steps": K,
             "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_desc(n_lines, n_v, (g.n_G, g.n_L, g.n_ft)),
+            "config": workload_desc(wl, n_lines, n_v, (g.n_G, g.n_L, g.n_ft),
+                                    (n_lines * 32, n_nodes * n_v * 4, n_nodes * g.n_ft * 4)),
             "clocks": clk.summary(),
             "gpu_launches": KERNELS_PER_STEP * K,
             "e2e": {"value": ws * 1000.0 / e2e_ms, "unit": "spectra/s",
@@ -329,9 +341,8 @@ def run_ours(args):
             "setup_s": setup_s,
         }
         if ws == 1 and not args.no_cpu_baseline:
-            _NFT["n_ft"] = g.n_ft
             workers = os.cpu_count() or 1
-            t, tl, tc, m = cpu_baseline_sample(lines, g.axes(), workers)
+            t, tl, tc, m = cpu_baseline_sample(wl, lines, g.axes(), g.n_ft, workers)
             res["cpu_baseline"] = {
                 "value": 1.0 / t, "unit": "spectra/s", "cores": workers, "kind": "port",
                 "sample": (f"oracle (FP64 numpy restatement of the reference CPU LDM path): scaling+scatter "
@@ -353,6 +364,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -542,7 +542,9 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
                 if (next_chunk(q, cs, nq2, ncs))
                     issue_chunk(a, stage[(g + 1) & 1], &bar[(g + 1) & 1], ncs, min(ch, rng[nq2].y - ncs));
             }
-            if (!mbar_wait(&bar[g & 1], (g >> 1) & 1)) bad = true;
+            // one thread polls the mbarrier (acquiring the TMA data); the others
+            // block on the CTA barrier, which orders that data for them too
+            if (threadIdx.x == 0 && !mbar_wait(&bar[g & 1], (g >> 1) & 1)) bad = true;
             if (__syncthreads_or(bad)) {
                 // give up: report, let the copies in flight land (bounded), leave
                 if (threadIdx.x == 0) {
