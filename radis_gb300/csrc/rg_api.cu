@@ -584,6 +584,7 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
         std::unique_ptr<VoigtArgs> vguard(va);
         va->f2 = P->f2;
         va->threads = row_threads(P->f2);
+        row_voigt_layout(P->n2, &va->pairs_per_pass, &va->row_twiddle_table);
         va->n1 = P->n1;
         va->n2 = P->n2;
         va->n = P->n;

@@ -145,6 +145,8 @@ struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
 struct VoigtArgs {        // K3 (row FFT + Voigt weights + pair reduction)
     FftLen f2;
     int threads;          // block size (row_threads)
+    int pairs_per_pass;   // 2: two pairs as float4 elements; 1: one pair (long rows)
+    int row_twiddle_table;// 1: per-row four-step twiddle table in shared memory
     int n1, n2;
     int64_t n;
     int n_pairs;
@@ -185,6 +187,7 @@ int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st);
 int launch_col_ifft(const ColFftArgs& a, cudaStream_t st);
 int col_block(int n1);               // columns per CTA of the column FFTs
 int row_threads(const FftLen& f);    // block size of the forward row kernel
+void row_voigt_layout(int n2, int* pairs, int* with_twr);
 size_t scatter_smem_floats(int n_nodes, int TK);
 
 }  // namespace rg

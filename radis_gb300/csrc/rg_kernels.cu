@@ -648,15 +648,37 @@ __device__ __forceinline__ float voigt_eval(const NodeV& n, float f, float half_
     return v * n.nrm;
 }
 
-// Two pairs travel together through the row transform as float4 elements
-// (row A in .xy, row B in .zw): they share the index arithmetic, the twiddle
-// loads and the shared-memory instructions.  Buffers use rp8(i) = i + i/8,
-// which keeps every 16-byte access pattern of the passes conflict-free.
+// PAIRS = 2: two pairs travel together through the row transform as float4
+// elements (row A in .xy, row B in .zw), sharing index arithmetic, twiddle
+// loads and shared-memory instructions; buffers use rp8(i) = i + i/8, which
+// keeps every 16-byte access pattern of the passes conflict-free.
+// PAIRS = 1 (long rows): float2 elements, rp16(i) = i + i/16.
 __device__ __forceinline__ int rp8(int i) { return i + (i >> 3); }
-__host__ __device__ constexpr int row4_len(int n) { return n + (n >> 3) + 1; }
+__device__ __forceinline__ int rp16(int i) { return i + (i >> 4); }
+template <int PAIRS> struct RowT;
+template <> struct RowT<2> {
+    using E = float4;
+    __device__ static int pad(int i) { return rp8(i); }
+    __host__ __device__ static constexpr int len(int n) { return n + (n >> 3) + 1; }
+    __device__ static void split(E t, float2& a, float2& b) {
+        a = make_float2(t.x, t.y);
+        b = make_float2(t.z, t.w);
+    }
+    __device__ static E join(float2 a, float2 b) { return make_float4(a.x, a.y, b.x, b.y); }
+};
+template <> struct RowT<1> {
+    using E = float2;
+    __device__ static int pad(int i) { return rp16(i); }
+    __host__ __device__ static constexpr int len(int n) { return n + (n >> 4) + 1; }
+    __device__ static void split(E t, float2& a, float2& b) {
+        a = t;
+        b = make_float2(0.f, 0.f);
+    }
+    __device__ static E join(float2 a, float2) { return a; }
+};
 
-template <int R>
-__device__ __forceinline__ void twiddle2(float2* A, float2* B, const float2* __restrict__ tw, int s) {
+template <int R, int PAIRS>
+__device__ __forceinline__ void twiddleP(float2* A, float2* B, const float2* __restrict__ tw, int s) {
     float2 w[R];
     w[0] = make_float2(1.f, 0.f);
     w[1] = __ldg(&tw[s]);
@@ -672,34 +694,38 @@ __device__ __forceinline__ void twiddle2(float2* A, float2* B, const float2* __r
 #pragma unroll
     for (int r = 1; r < R; ++r) {
         A[r] = cmul(A[r], w[r]);
-        B[r] = cmul(B[r], w[r]);
+        if (PAIRS == 2) B[r] = cmul(B[r], w[r]);
     }
 }
 
-// first pass (sub-transform length 1): global rows -> registers -> smem
-template <int R>
-__device__ __forceinline__ void row2_first(const float2* __restrict__ ya, const float2* __restrict__ yb,
-                                           const float2* twr, float4* out, int L) {
+// first pass (sub-transform length 1): global rows x four-step twiddle ->
+// registers -> smem.  twr: per-row twiddle table in smem, or nullptr to use
+// the global two-level table.
+template <int R, int PAIRS>
+__device__ __forceinline__ void row_first(const float2* __restrict__ ya, const float2* __restrict__ yb,
+                                          const float2* twr, const VoigtArgs& a, int k1,
+                                          typename RowT<PAIRS>::E* out, int L) {
     const int M = L / R;
     for (int j = threadIdx.x; j < M; j += blockDim.x) {
         float2 A[R], B[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const int i = j + r * M;
-            const float2 w = twr[i];
+            const float2 w = twr ? twr[i] : ((k1 && i) ? twiddle_n(a.tw_hi, a.tw_lo, k1 * i) : make_float2(1.f, 0.f));
             A[r] = cmul(__ldg(&ya[i]), w);
-            B[r] = yb ? cmul(__ldg(&yb[i]), w) : make_float2(0.f, 0.f);
+            if (PAIRS == 2) B[r] = yb ? cmul(__ldg(&yb[i]), w) : make_float2(0.f, 0.f);
         }
         dftR<R>(A);
-        dftR<R>(B);
+        if (PAIRS == 2) dftR<R>(B);
 #pragma unroll
-        for (int r = 0; r < R; ++r) out[rp8(j * R + r)] = make_float4(A[r].x, A[r].y, B[r].x, B[r].y);
+        for (int r = 0; r < R; ++r) out[RowT<PAIRS>::pad(j * R + r)] = RowT<PAIRS>::join(A[r], B[r]);
     }
 }
 
-template <int R>
-__device__ __forceinline__ void row2_pass(const float4* __restrict__ in, float4* __restrict__ out, int L, int Ns,
-                                          unsigned mag, const float2* __restrict__ tw) {
+template <int R, int PAIRS>
+__device__ __forceinline__ void row_mid(const typename RowT<PAIRS>::E* __restrict__ in,
+                                        typename RowT<PAIRS>::E* __restrict__ out, int L, int Ns, unsigned mag,
+                                        const float2* __restrict__ tw) {
     const int M = L / R;
     const int twstep = L / (Ns * R);
     for (int j = threadIdx.x; j < M; j += blockDim.x) {
@@ -707,41 +733,41 @@ __device__ __forceinline__ void row2_pass(const float4* __restrict__ in, float4*
         const int k = j - q * Ns;
         float2 A[R], B[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const float4 t = in[rp8(j + r * M)];
-            A[r] = make_float2(t.x, t.y);
-            B[r] = make_float2(t.z, t.w);
-        }
-        if (Ns > 1) twiddle2<R>(A, B, tw, k * twstep);
+        for (int r = 0; r < R; ++r) RowT<PAIRS>::split(in[RowT<PAIRS>::pad(j + r * M)], A[r], B[r]);
+        if (Ns > 1) twiddleP<R, PAIRS>(A, B, tw, k * twstep);
         dftR<R>(A);
-        dftR<R>(B);
+        if (PAIRS == 2) dftR<R>(B);
         const int base = q * Ns * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) out[rp8(base + r * Ns)] = make_float4(A[r].x, A[r].y, B[r].x, B[r].y);
+        for (int r = 0; r < R; ++r) out[RowT<PAIRS>::pad(base + r * Ns)] = RowT<PAIRS>::join(A[r], B[r]);
     }
 }
 
-__host__ __device__ inline size_t row_voigt_smem(int n2) {
-    return 2 * (size_t)row4_len(n2) * sizeof(float4) + (size_t)n2 * sizeof(float2);
+template <int PAIRS>
+__host__ __device__ inline size_t row_voigt_smem(int n2, bool with_twr) {
+    return 2 * (size_t)RowT<PAIRS>::len(n2) * sizeof(typename RowT<PAIRS>::E) +
+           (with_twr ? (size_t)n2 * sizeof(float2) : 0);
 }
 
-// IT = iterations of the last (radix-8) pass per thread: IT * kRowThreads * 8 >= n2
-template <int IT>
+// IT = iterations of the last (radix-8) pass per thread: IT * blockDim * 8 >= n2
+template <int IT, int PAIRS>
 __global__ void __launch_bounds__(kRowMaxThreads, IT == 1 ? 2 : 1) k_row_fft_voigt(const VoigtArgs a) {
+    using E = typename RowT<PAIRS>::E;
     extern __shared__ float4 sm4[];
     const int n2 = a.n2;
-    const int len = row4_len(n2);
-    float4* buf0 = sm4;
-    float4* buf1 = sm4 + len;
-    float2* twr = reinterpret_cast<float2*>(sm4 + 2 * len);
+    const int len = RowT<PAIRS>::len(n2);
+    E* buf0 = reinterpret_cast<E*>(sm4);
+    E* buf1 = buf0 + len;
+    float2* twr = a.row_twiddle_table ? reinterpret_cast<float2*>(buf1 + len) : nullptr;
     const int k1 = blockIdx.x;
     const int n = (int)a.n;
     const int j0 = blockIdx.y * kPairGroup;
     const int j1 = min(j0 + kPairGroup, a.n_pairs);
     const FftLen& P = a.f2;
     const int ML = n2 / 8;    // butterflies of the last pass (radix 8, sub-length ML)
-    for (int t = threadIdx.x; t < n2; t += blockDim.x)
-        twr[t] = (k1 && t) ? twiddle_n(a.tw_hi, a.tw_lo, k1 * t) : make_float2(1.f, 0.f);
+    if (twr)
+        for (int t = threadIdx.x; t < n2; t += blockDim.x)
+            twr[t] = (k1 && t) ? twiddle_n(a.tw_hi, a.tw_lo, k1 * t) : make_float2(1.f, 0.f);
     // frequencies of the bins this thread owns in the last pass: t = jl + r ML
     float fb[IT * 8];
     float2 acc[IT * 8];
@@ -757,32 +783,32 @@ __global__ void __launch_bounds__(kRowMaxThreads, IT == 1 ? 2 : 1) k_row_fft_voi
     }
     __syncthreads();
 
-    for (int j = j0; j < j1; j += 2) {
-        const bool two = j + 1 < j1;
+    for (int j = j0; j < j1; j += PAIRS) {
+        const bool two = PAIRS == 2 && j + 1 < j1;
         const float2* ya = a.y + ((int64_t)j * a.n1 + k1) * n2;
         const float2* yb = two ? a.y + ((int64_t)(j + 1) * a.n1 + k1) * n2 : nullptr;
         switch (P.radix[0]) {
-            case 2: row2_first<2>(ya, yb, twr, buf0, n2); break;
-            case 3: row2_first<3>(ya, yb, twr, buf0, n2); break;
-            case 4: row2_first<4>(ya, yb, twr, buf0, n2); break;
-            case 5: row2_first<5>(ya, yb, twr, buf0, n2); break;
-            default: row2_first<8>(ya, yb, twr, buf0, n2); break;
+            case 2: row_first<2, PAIRS>(ya, yb, twr, a, k1, buf0, n2); break;
+            case 3: row_first<3, PAIRS>(ya, yb, twr, a, k1, buf0, n2); break;
+            case 4: row_first<4, PAIRS>(ya, yb, twr, a, k1, buf0, n2); break;
+            case 5: row_first<5, PAIRS>(ya, yb, twr, a, k1, buf0, n2); break;
+            default: row_first<8, PAIRS>(ya, yb, twr, a, k1, buf0, n2); break;
         }
         __syncthreads();
-        float4* in = buf0;
-        float4* out = buf1;
+        E* in = buf0;
+        E* out = buf1;
         for (int p = 1; p < P.npass - 1; ++p) {
             const int Ns = P.ns[p];
             const unsigned mag = P.mag[p];
             switch (P.radix[p]) {
-                case 2: row2_pass<2>(in, out, n2, Ns, mag, P.tw); break;
-                case 3: row2_pass<3>(in, out, n2, Ns, mag, P.tw); break;
-                case 4: row2_pass<4>(in, out, n2, Ns, mag, P.tw); break;
-                case 5: row2_pass<5>(in, out, n2, Ns, mag, P.tw); break;
-                default: row2_pass<8>(in, out, n2, Ns, mag, P.tw); break;
+                case 2: row_mid<2, PAIRS>(in, out, n2, Ns, mag, P.tw); break;
+                case 3: row_mid<3, PAIRS>(in, out, n2, Ns, mag, P.tw); break;
+                case 4: row_mid<4, PAIRS>(in, out, n2, Ns, mag, P.tw); break;
+                case 5: row_mid<5, PAIRS>(in, out, n2, Ns, mag, P.tw); break;
+                default: row_mid<8, PAIRS>(in, out, n2, Ns, mag, P.tw); break;
             }
             __syncthreads();
-            float4* t = in;
+            E* t = in;
             in = out;
             out = t;
         }
@@ -800,14 +826,10 @@ __global__ void __launch_bounds__(kRowMaxThreads, IT == 1 ? 2 : 1) k_row_fft_voi
             if (jl < ML) {
                 float2 A[8], B[8];
 #pragma unroll
-                for (int r = 0; r < 8; ++r) {
-                    const float4 t = in[rp8(jl + r * ML)];
-                    A[r] = make_float2(t.x, t.y);
-                    B[r] = make_float2(t.z, t.w);
-                }
-                twiddle2<8>(A, B, P.tw, jl);   // w_{n2}^{r jl}
+                for (int r = 0; r < 8; ++r) RowT<PAIRS>::split(in[RowT<PAIRS>::pad(jl + r * ML)], A[r], B[r]);
+                twiddleP<8, PAIRS>(A, B, P.tw, jl);   // w_{n2}^{r jl}
                 dft8(A);
-                dft8(B);
+                if (PAIRS == 2) dft8(B);
 #pragma unroll
                 for (int r = 0; r < 8; ++r) {
                     const float f = fb[it * 8 + r];
@@ -978,23 +1000,45 @@ int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st) {
     }
 }
 
-template <int ACC>
+template <int IT, int PAIRS>
 static int row_voigt(const VoigtArgs& a, cudaStream_t st) {
-    const size_t smem = row_voigt_smem(a.n2);
-    ALLOW_SMEM(k_row_fft_voigt<ACC>, smem);
+    const size_t smem = row_voigt_smem<PAIRS>(a.n2, a.row_twiddle_table != 0);
+    ALLOW_SMEM((k_row_fft_voigt<IT, PAIRS>), smem);
     dim3 grid(a.n1, (a.n_pairs + kPairGroup - 1) / kPairGroup);
-    k_row_fft_voigt<ACC><<<grid, a.threads, smem, st>>>(a);
+    k_row_fft_voigt<IT, PAIRS><<<grid, a.threads, smem, st>>>(a);
     return check_launch();
+}
+
+template <int PAIRS>
+static int row_voigt_it(const VoigtArgs& a, cudaStream_t st) {
+    const int per = (a.n2 / 8 + a.threads - 1) / a.threads;
+    if (per <= 1) return row_voigt<1, PAIRS>(a, st);
+    if (per <= 2) return row_voigt<2, PAIRS>(a, st);
+    if (per <= 4) return row_voigt<4, PAIRS>(a, st);
+    return RG_ERR_RANGE;
+}
+
+// Shared memory per CTA of the forward row kernel and its layout choice:
+// two pairs per pass when that fits two CTAs per SM, else one pair; the
+// per-row twiddle table only where it still fits.
+void row_voigt_layout(int n2, int* pairs, int* with_twr) {
+    const size_t two_ctas = 113 * 1024;
+    if (row_voigt_smem<2>(n2, true) <= two_ctas) {
+        *pairs = 2;
+        *with_twr = 1;
+    } else if (row_voigt_smem<1>(n2, true) <= two_ctas) {
+        *pairs = 1;
+        *with_twr = 1;
+    } else {
+        *pairs = 1;
+        *with_twr = 0;
+    }
 }
 
 int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st) {
     if (a.f2.npass < 2 || a.f2.radix[a.f2.npass - 1] != 8) return RG_ERR_RANGE;
     if (a.threads < 32 || a.threads > kRowMaxThreads || a.threads % 32) return RG_ERR_RANGE;
-    const int per = (a.n2 / 8 + a.threads - 1) / a.threads;
-    if (per <= 1) return row_voigt<1>(a, st);
-    if (per <= 2) return row_voigt<2>(a, st);
-    if (per <= 4) return row_voigt<4>(a, st);
-    return RG_ERR_RANGE;
+    return a.pairs_per_pass == 2 ? row_voigt_it<2>(a, st) : row_voigt_it<1>(a, st);
 }
 
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st) {

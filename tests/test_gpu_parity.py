@@ -181,3 +181,14 @@ def test_co2_5M_full_size(ctx):
     assert np.max(np.abs(gpu2 - 2 * gpu)) <= 1e-5 * np.max(np.abs(gpu2))
     for o in (plan2, ln2, plan, ln):
         o.close()
+
+
+@pytest.mark.parametrize("n_v", [800001, 1200001])
+def test_long_rows(ctx, n_v):
+    """Long spectra: the row transform runs one pair per pass (n2 = 3200 with
+    the per-row twiddle table, n2 = 4800 without it)."""
+    lines = S.uniform_lines(200_000, 2000.0, 2000.0 + (n_v - 1) * 0.001, seed=30)
+    args = (44.0, 2000.0, 0.001, n_v, 1200.0, 0.8, 0.2)
+    gpu, info = run_gpu(ctx, lines, *args, n_G=4, n_L=8)
+    assert info.grid.n2 in (3200, 4800)
+    assert rel_err(gpu, oracle(lines, *args, info)) <= TOL
