@@ -215,6 +215,105 @@ def run_reference(args):
     return 0
 
 
+def serving_requests(lists, n, seed):
+    """Seeded request stream of the serving configuration: list uniform, window
+    width log-uniform 50-2000 cm-1 (clipped to the list), wstep in
+    {0.001, 0.002, 0.005, 0.01}, T log-U[300, 3000] K, p log-U[0.1, 10] bar,
+    x log-U[0.01, 1]."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        name = list(lists)[int(rng.integers(len(lists)))]
+        lines, lo, hi = lists[name]
+        dv = float(rng.choice([0.001, 0.002, 0.005, 0.01]))
+        width = min(float(np.exp(rng.uniform(np.log(50.0), np.log(2000.0)))), hi - lo)
+        vmin = float(np.floor(rng.uniform(lo, hi - width) / dv) * dv)
+        n_v = int(width / dv) + 1
+        T = float(np.exp(rng.uniform(np.log(300.0), np.log(3000.0))))
+        p = float(np.exp(rng.uniform(np.log(0.1), np.log(10.0))))
+        x = float(np.exp(rng.uniform(np.log(0.01), np.log(1.0))))
+        out.append((name, lines, vmin, dv, n_v, T, p, x))
+    return out
+
+
+def run_serving(ctx, L, lists, n_req, slots, seed=11):
+    """Served (continuous batching, rg_server) vs plain per-request form (a
+    fresh plan per request, synchronous), on the same request stream:
+    capacity with every request queued at t = 0, then latency under Poisson
+    arrivals at 0.8 x the plain capacity."""
+    import threading
+
+    import numpy as np
+    from radis_gb300 import synthetic as S
+    reqs = serving_requests(lists, n_req, seed)
+    dx = dict(dxG=S.DXG_DEFAULT, dxL=S.DXL_DEFAULT)
+
+    def plain(arrivals):
+        outs, lat = [], []
+        t0 = time.perf_counter()
+        for (name, lines, vmin, dv, n_v, T, p, x), ta in zip(reqs, arrivals):
+            now = time.perf_counter() - t0
+            if ta > now:
+                time.sleep(ta - now)
+            plan = L.Plan(lines, vmin, dv, n_v, **dx)
+            o, info = plan.synthesize_host(T, p, x)
+            plan.close()
+            outs.append(o.astype(np.float64) * np.exp(info.log_scale))
+            lat.append(time.perf_counter() - t0 - ta)
+        return outs, lat, time.perf_counter() - t0
+
+    def served(arrivals):
+        srv = L.Server(ctx, slots=slots, mem_budget=96 << 30)
+        tickets = [None] * len(reqs)
+        t0 = time.perf_counter()
+
+        def submitter():
+            for i, ((name, lines, vmin, dv, n_v, T, p, x), ta) in enumerate(zip(reqs, arrivals)):
+                now = time.perf_counter() - t0
+                if ta > now:
+                    time.sleep(ta - now)
+                tickets[i] = srv.submit(lines, vmin, dv, n_v, T, p, x, **dx)
+        th = threading.Thread(target=submitter)
+        th.start()
+        outs, lat = [], []
+        for i in range(len(reqs)):
+            while tickets[i] is None:
+                time.sleep(1e-5)
+            o, info, (ts, t_start, t_done) = srv.wait(tickets[i])
+            lat.append(time.perf_counter() - t0 - arrivals[i])
+            outs.append(o.astype(np.float64) * np.exp(info.log_scale))
+        th.join()
+        total = time.perf_counter() - t0
+        srv.close()
+        return outs, lat, total
+
+    zero = [0.0] * len(reqs)
+    plain(zero[:4])                      # warm-up (tables, allocator pools)
+    p_out, _, p_total = plain(zero)
+    s_out, _, s_total = served(zero)
+    plain_sps, served_sps = len(reqs) / p_total, len(reqs) / s_total
+    err = max(float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)) for a, b in zip(s_out, p_out))
+    rate = 0.8 * plain_sps
+    rng = np.random.default_rng(seed + 1)
+    arrivals = list(np.cumsum(rng.exponential(1.0 / rate, len(reqs))))
+    _, p_lat, _ = plain(arrivals)
+    _, s_lat, _ = served(arrivals)
+    pct = lambda v, q: float(np.percentile(np.asarray(v) * 1e3, q))
+    npts = [r[4] for r in reqs]
+    return {
+        "requests": len(reqs), "slots": slots,
+        "served_spectra_per_s": served_sps, "plain_spectra_per_s": plain_sps,
+        "served_over_plain": served_sps / plain_sps,
+        "max_rel_err_served_vs_alone": err,
+        "poisson_rate_per_s": rate,
+        "latency_ms": {"served_p50": pct(s_lat, 50), "served_p99": pct(s_lat, 99),
+                       "plain_p50": pct(p_lat, 50), "plain_p99": pct(p_lat, 99)},
+        "request_points": {"min": int(min(npts)), "median": int(np.median(npts)), "max": int(max(npts))},
+        "plain_form": "fresh plan (FFT tables, line index, workspace) + synchronous spectrum per request",
+    }
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -348,6 +447,18 @@ def run_ours(args):
                 "sample": (f"oracle (FP64 numpy restatement of the reference CPU LDM path): scaling+scatter "
                            f"of {m} of {n_lines} lines scaled x{n_lines / m:.0f} ({tl:.2f} s) + full FFT/Voigt "
                            f"stage ({tc:.2f} s, scipy.fft workers={workers}); add.at single-threaded")}
+        if ws == 1 and not args.no_serving:
+            co = L.Lines(ctx, S.co_like(), 28.0)
+            h2o_lines = S.h2o_like(args.serve_h2o_lines)
+            h2o = L.Lines(ctx, h2o_lines, 18.0)
+            del h2o_lines
+            lists = {"co_10k": (co, 1900.0, 2300.0), "co2_5M": (ln, 2000.0, 2400.0),
+                     "h2o": (h2o, 500.0, 8000.0)}
+            sv = run_serving(ctx, L, lists, args.serve_requests, args.serve_slots)
+            sv["lists"] = {"co_10k": 10_000, "co2_5M": n_lines, "h2o": args.serve_h2o_lines}
+            res["serving"] = sv
+            h2o.close()
+            co.close()
         print(json.dumps(res))
     plan.close()
     ln.close()
@@ -365,6 +476,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=120)
+    ap.add_argument("--serve-slots", type=int, default=8)
+    ap.add_argument("--serve-h2o-lines", type=int, default=100_000_000)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -166,6 +166,42 @@ int rg_synthesize_host(rg_plan* plan, const rg_conditions* cond, float* out_host
 int rg_debug_ldm(rg_plan* plan, const rg_conditions* cond, float* ldm_host, int64_t capacity,
                  rg_spectrum_info* info);
 
+/* ---------------------------------------------------------------------------
+ * Serving: continuous batching of spectrum requests over resident line lists.
+ * No reference counterpart (the reference runs one blocking gpuApp.iterate at a
+ * time, radis/gpu/gpu.py:302-370); this is the request-level equivalent of
+ * SpectrumFactory.eq_spectrum_gpu + Spectrum.recalc_gpu for many clients.
+ * A worker thread admits queued requests (FIFO) into `slots` CUDA streams as
+ * slots and device memory (LDM + FFT workspace, within `mem_budget` bytes)
+ * free up; admitted requests run concurrently on the device.  Results are
+ * copied to each request's host buffer (pinned memory recommended).
+ * ------------------------------------------------------------------------- */
+typedef struct rg_server rg_server;
+
+typedef struct {
+    rg_lines* lines;           /* resident line list                            */
+    rg_plan_desc grid;         /* spectral grid + LDM node policy               */
+    rg_conditions cond;        /* q_ratio is copied at submission               */
+    float* out_host;           /* n_v floats: abscoeff x exp(-info.log_scale)    */
+} rg_request;
+
+typedef struct {
+    int64_t submitted, completed, failed, in_flight, queued;
+    int64_t device_bytes;      /* workspace currently held by the slots         */
+} rg_server_stats;
+
+int rg_server_create(rg_ctx* ctx, int slots, int64_t mem_budget, rg_server** out);
+/* Queue a request; returns at once with a ticket (>= 1). */
+int rg_server_submit(rg_server* srv, const rg_request* req, int64_t* ticket);
+/* Wait for a ticket (timeout_ms < 0: no limit); fills info and the request's
+ * timestamps (seconds on the server's clock: submitted, started, finished).
+ * Returns the request's own status (RG_ERR_TIMEOUT if the wait expired). */
+int rg_server_wait(rg_server* srv, int64_t ticket, double timeout_ms, rg_spectrum_info* info,
+                   double* t_submit, double* t_start, double* t_done);
+int rg_server_stats_get(rg_server* srv, rg_server_stats* st);
+/* Finish the requests in flight and queued, then release everything. */
+int rg_server_destroy(rg_server* srv);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,6 +23,7 @@ EXPORTS = [
     "rg_abi_version", "rg_last_error", "rg_ctx_create", "rg_ctx_destroy", "rg_lines_upload",
     "rg_lines_free", "rg_lines_count", "rg_plan_create", "rg_plan_free", "rg_plan_grid", "rg_grid_estimate",
     "rg_synthesize", "rg_synthesize_host", "rg_debug_ldm", "rg_plan_stage_times",
+    "rg_server_create", "rg_server_submit", "rg_server_wait", "rg_server_stats_get", "rg_server_destroy",
 ]
 
 
@@ -72,6 +73,15 @@ class SpectrumInfo(C.Structure):
                 ("lines_in_window", C.c_int64)]
 
 
+class Request(C.Structure):
+    _fields_ = [("lines", C.c_void_p), ("grid", PlanDesc), ("cond", Conditions), ("out_host", C.c_void_p)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
+                ("in_flight", C.c_int64), ("queued", C.c_int64), ("device_bytes", C.c_int64)]
+
+
 _lib = None
 
 
@@ -108,6 +118,12 @@ def load(path: str | None = None):
                                C.c_int),
         "rg_plan_stage_times": ([vp, C.POINTER(C.c_double), C.POINTER(i64)], C.c_int),
         "rg_debug_ldm": ([vp, C.POINTER(Conditions), vp, i64, C.POINTER(SpectrumInfo)], C.c_int),
+        "rg_server_create": ([vp, C.c_int, i64, C.POINTER(vp)], C.c_int),
+        "rg_server_submit": ([vp, C.POINTER(Request), C.POINTER(i64)], C.c_int),
+        "rg_server_wait": ([vp, i64, C.c_double, C.POINTER(SpectrumInfo), C.POINTER(C.c_double),
+                            C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
+        "rg_server_stats_get": ([vp, C.POINTER(ServerStats)], C.c_int),
+        "rg_server_destroy": ([vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -353,3 +369,67 @@ def grid_estimate(lines: dict, molar_mass, vmin, dv, n_v, T, p_bar, x, dxG=None,
     g = Grid()
     check(load().rg_grid_estimate(C.byref(la), C.byref(iso_s), C.byref(d), C.byref(c), C.byref(g)))
     return g
+
+
+class Server:
+    """Continuous-batching spectrum server over resident line lists
+    (rg_server_*): ``submit`` queues a request and returns a ticket at once;
+    the native worker admits requests into CUDA stream slots as slots and
+    device memory free up; ``wait`` returns the spectrum."""
+
+    def __init__(self, ctx: Context, slots: int = 8, mem_budget: int = 16 << 30):
+        h = C.c_void_p()
+        check(load().rg_server_create(ctx.handle, int(slots), int(mem_budget), C.byref(h)))
+        self._h = h
+        self.ctx = ctx
+        self._keep = {}
+        ctx._children.add(self)
+
+    @property
+    def handle(self):
+        if not self._h:
+            raise RgError(7, "server is closed")
+        return self._h
+
+    def submit(self, lines: Lines, vmin, dv, n_v, T, p_bar, x, dxG=None, dxL=None, n_G=None,
+               n_L=None, q_ratio=None, out=None, folding_thresh=1e-6) -> int:
+        if out is None:
+            out = np.empty(int(n_v), dtype=np.float32)
+        q = None if q_ratio is None else np.ascontiguousarray(
+            np.broadcast_to(np.asarray(q_ratio, np.float64), (lines.n_iso,)))
+        req = Request(lines.handle.value,
+                      PlanDesc(float(vmin), float(dv), int(n_v), float(dxG or 0.0), float(dxL or 0.0),
+                               int(n_G or 0), int(n_L or 0), float(folding_thresh), 0),
+                      Conditions(float(T), float(p_bar), float(x), ptr(q)), out.ctypes.data)
+        t = C.c_int64()
+        check(load().rg_server_submit(self.handle, C.byref(req), C.byref(t)))
+        self._keep[t.value] = (out, q, lines)
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: float = -1.0):
+        """(spectrum float32 array, SpectrumInfo, (t_submit, t_start, t_done))."""
+        info = SpectrumInfo()
+        ts, t0, t1 = C.c_double(), C.c_double(), C.c_double()
+        try:
+            check(load().rg_server_wait(self.handle, int(ticket), float(timeout_ms), C.byref(info),
+                                        C.byref(ts), C.byref(t0), C.byref(t1)))
+        finally:
+            kept = self._keep.pop(ticket, None)
+        return kept[0], info, (ts.value, t0.value, t1.value)
+
+    def stats(self) -> ServerStats:
+        st = ServerStats()
+        check(load().rg_server_stats_get(self.handle, C.byref(st)))
+        return st
+
+    def close(self):
+        if getattr(self, "_h", None):
+            check(load().rg_server_destroy(self._h))
+            self._h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -19,6 +19,12 @@
 #include <limits>
 #include <memory>
 #include <new>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <thread>
 
 #include "rg_internal.h"
 
@@ -96,36 +102,44 @@ struct rg_lines {
     int n_iso = 1;
     double t_ref = 296.0;
     Envelope env;
-    int plans = 0;
+    std::atomic<int> plans{0};      // plans and server requests referencing the list
     uint32_t magic = 0x52474C4E;
 };
 
-struct rg_plan {
-    rg_lines* lines = nullptr;
+// Geometry and device buffers of one spectrum in flight: a plan owns one, a
+// server slot owns one per request it runs (tables may be shared).
+struct Work {
     rg_plan_desc desc{};
-    std::mutex mu;
-    // FFT factorisation
+    // FFT factorisation n = n1 n2 and its tables
     int64_t n = 0;
     int n1 = 0, n2 = 0, B = 0;
     FftLen f1, f2;
-    float2* tw_hi = nullptr;
-    float2* tw_lo = nullptr;
-    // column index
+    const float2* tw_hi = nullptr;
+    const float2* tw_lo = nullptr;
+    // line index per grid column and the fixed-point bound
     int64_t* col_start = nullptr;
-    int col_off = 0, col_count = 0;
+    int col_off = 0, col_count = 0, E = 0;
     double p_atm_max = 0.0;
-    // workspace (grow-only)
+    int* cmax_dev = nullptr;
+    int64_t cmax_host = -1;           // known on the host (plans), -1 otherwise
+    // grow-only buffers
     int nodes_cap = 0;
     int64_t row_stride = 0;
     unsigned* ldm = nullptr;          // LDM as fixed-point words of the scatter
     float2* y = nullptr;
     float2* g = nullptr;
-    float* out_d = nullptr;
     unsigned long long* counter = nullptr;
     unsigned* err = nullptr;          // device flag set by a bounded wait that gave up
     unsigned* err_host = nullptr;     // pinned copy of err, refreshed after every spectrum
-    int64_t cmax = 0;                 // max lines that can touch one grid column
-    float last_fx_scale = 1.f;        // fixed-point scale of the last scatter
+};
+
+struct rg_plan {
+    rg_lines* lines = nullptr;
+    std::mutex mu;
+    Work w;
+    float2* tw_hi_own = nullptr;
+    float2* tw_lo_own = nullptr;
+    float* out_d = nullptr;
     cudaEvent_t ev[6] = {nullptr};
     // ring of per-stage events recorded without synchronisation (timing == 2)
     static constexpr int kRing = 256;
@@ -323,8 +337,8 @@ int compute_grid_env(const Envelope& E, const rg_plan_desc& d, int64_t n_ft, int
     return RG_OK;
 }
 
-int compute_grid(rg_plan* P, const rg_conditions* c, SpecHost* s) {
-    return compute_grid_env(P->lines->env, P->desc, P->n, P->n1, P->n2, c, s);
+int compute_grid(const rg_lines* L, const Work& W, const rg_conditions* c, SpecHost* s) {
+    return compute_grid_env(L->env, W.desc, W.n, W.n1, W.n2, c, s);
 }
 
 // Envelope of a host line list (per-iso v0 range, width and intensity hulls).
@@ -392,17 +406,19 @@ int build_envelope(const rg_line_arrays* in, const rg_isotopes* iso, Envelope* E
     return RG_OK;
 }
 
-int ensure_workspace(rg_plan* P, int n_nodes) {
-    if (n_nodes <= P->nodes_cap) return RG_OK;
-    int cap = std::min(kMaxNodes, std::max(n_nodes, (int)(P->nodes_cap * 1.25) + 2));
+// Grow-only LDM / FFT workspace for n_nodes (x1.25 margin), stream ordered.
+int ensure_workspace(Work& W, int n_nodes, cudaStream_t st) {
+    if (n_nodes <= W.nodes_cap) return RG_OK;
+    int cap = std::min(kMaxNodes, std::max(n_nodes, (int)(W.nodes_cap * 1.25) + 2));
     cap = (cap + 1) & ~1;
-    CU(cudaStreamSynchronize(P->lines->ctx->stream));
-    dfree(P->ldm);
-    dfree(P->y);
-    P->nodes_cap = 0;
-    CU(cudaMalloc(&P->ldm, sizeof(unsigned) * (size_t)cap * P->row_stride));
-    CU(cudaMalloc(&P->y, sizeof(float2) * (size_t)(cap / 2) * P->n));
-    P->nodes_cap = cap;
+    if (W.ldm) CU(cudaFreeAsync(W.ldm, st));
+    if (W.y) CU(cudaFreeAsync(W.y, st));
+    W.ldm = nullptr;
+    W.y = nullptr;
+    W.nodes_cap = 0;
+    CU(cudaMallocAsync((void**)&W.ldm, sizeof(unsigned) * (size_t)cap * W.row_stride, st));
+    CU(cudaMallocAsync((void**)&W.y, sizeof(float2) * (size_t)(cap / 2) * W.n, st));
+    W.nodes_cap = cap;
     return RG_OK;
 }
 
@@ -429,8 +445,8 @@ int scatter_shape(int n_nodes, int* chunk, int* TK, size_t* smem) {
     return fail(RG_ERR_RANGE, "LDM grid of %d nodes does not fit a shared-memory tile", n_nodes);
 }
 
-int build_scatter_args(rg_plan* P, const rg_conditions* c, const SpecHost& s, ScatterArgs* a) {
-    const rg_lines* L = P->lines;
+int build_scatter_args(const rg_lines* L, const Work& W, const rg_conditions* c, const SpecHost& s,
+                       ScatterArgs* a) {
     const rg_grid& g = s.grid;
     std::memset(a, 0, sizeof *a);
     a->v0 = L->v0;
@@ -441,32 +457,25 @@ int build_scatter_args(rg_plan* P, const rg_conditions* c, const SpecHost& s, Sc
     a->na = L->na;
     a->dl = L->dl;
     a->iso = L->n_iso > 1 ? L->iso : nullptr;
-    a->col_start = P->col_start;
-    a->col_off = P->col_off;
-    a->col_count = P->col_count;
-    a->n_v = (int)P->desc.n_v;
+    a->col_start = W.col_start;
+    a->col_off = W.col_off;
+    a->col_count = W.col_count;
+    a->n_v = (int)W.desc.n_v;
     a->n_nodes = s.n_nodes;
     a->NG = g.n_G;
     a->NL = g.n_L;
-    a->row_stride = P->row_stride;
-    a->ldm = P->ldm;
+    a->row_stride = W.row_stride;
+    a->ldm = W.ldm;
     size_t smem_unused;
     RG(scatter_shape(s.n_nodes, &a->chunk, &a->TK, &smem_unused));
-    a->n_tiles = (int)((P->desc.n_v + a->TK - 1) / a->TK);
-    // fixed point: cmax lines of (scaled) intensity <= 1 must stay below 2^31
-    {
-        const int64_t m = P->cmax + 1;
-        int bits = 0;
-        while (bits < 62 && ((int64_t)1 << bits) <= m) ++bits;
-        a->fx_scale = std::ldexp(1.f, std::max(0, 31 - bits));
-    }
-    a->err = P->err;
-    if (s.p_atm > P->p_atm_max)
-        return fail(RG_ERR_RANGE, "pressure %g atm above the plan's shift-index limit %g atm", s.p_atm,
-                    P->p_atm_max);
-    a->margin_cols = (int)std::ceil(L->env.max_abs_delta * s.p_atm / P->desc.dv) + 1;
-    split(P->desc.vmin, &a->vmin_hi, &a->vmin_lo);
-    split(1.0 / P->desc.dv, &a->inv_dv_hi, &a->inv_dv_lo);
+    a->n_tiles = (int)((W.desc.n_v + a->TK - 1) / a->TK);
+    a->cmax = W.cmax_dev;
+    a->err = W.err;
+    if (s.p_atm > W.p_atm_max)
+        return fail(RG_ERR_RANGE, "pressure %g atm above the shift-index limit %g atm", s.p_atm, W.p_atm_max);
+    a->margin_cols = (int)std::ceil(L->env.max_abs_delta * s.p_atm / W.desc.dv) + 1;
+    split(W.desc.vmin, &a->vmin_hi, &a->vmin_lo);
+    split(1.0 / W.desc.dv, &a->inv_dv_hi, &a->inv_dv_lo);
     a->p_atm = (float)s.p_atm;
     a->x_self = (float)c->x;
     const double T = c->T;
@@ -493,7 +502,7 @@ int build_scatter_args(rg_plan* P, const rg_conditions* c, const SpecHost& s, Sc
         split(b, &a->bI_hi[i], &a->bI_lo[i]);
     }
     a->stim_c = (float)(kC2 / T * kLog2e);
-    a->in_window = P->counter;
+    a->in_window = W.counter;
     return RG_OK;
 }
 
@@ -516,88 +525,71 @@ void node_fold(double dv, double wG, double wL, double thresh, int* nfold, doubl
 }
 
 // After a synchronisation: report (once) a bounded device wait that gave up.
-int take_err(rg_plan* P) {
-    if (*P->err_host) {
-        *P->err_host = 0;
+int take_err(Work& W) {
+    if (*W.err_host) {
+        *W.err_host = 0;
         return fail(RG_ERR_TIMEOUT, "a bounded device wait in the scatter gave up; the spectrum is invalid");
     }
     return RG_OK;
 }
 
-int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st, int timing, bool ldm_only,
-                 rg_spectrum_info* info) {
-    SpecHost s;
-    RG(compute_grid(P, c, &s));
-    RG(ensure_workspace(P, s.n_nodes));
+// Enqueue one spectrum on `st` into W's buffers: scatter, the four FFT/Voigt
+// stages (unless ldm_only), and the publication of the device error flag.
+// ev: 6 events recorded between stages (nullable).
+int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const SpecHost& s, float* out,
+                     cudaStream_t st, cudaEvent_t* ev, bool ldm_only) {
+    RG(ensure_workspace(W, s.n_nodes, st));
     ScatterArgs sa;
-    RG(build_scatter_args(P, c, s, &sa));
-    const int n_v = (int)P->desc.n_v;
+    RG(build_scatter_args(L, W, c, s, &sa));
+    const int n_v = (int)W.desc.n_v;
     int ch_unused, tk_unused;
     size_t smem;
     RG(scatter_shape(s.n_nodes, &ch_unused, &tk_unused, &smem));
-    const int sms = P->lines->ctx->sms;
+    const int sms = L->ctx->sms;
     const int grid = std::max(std::min(sa.n_tiles, sms),
                               (sa.n_tiles + kScatMaxTilesPerCta - 1) / kScatMaxTilesPerCta);
-    cudaEvent_t* ev = P->ev;
-    if (timing == 2) {
-        if (P->ring.empty()) {
-            P->ring.assign(rg_plan::kRing * 6, nullptr);
-            for (auto& e : P->ring) CU(cudaEventCreate(&e));
-        }
-        if (P->ring_used >= rg_plan::kRing) return fail(RG_ERR_RANGE, "stage-timing ring full: read it first");
-        ev = &P->ring[6 * P->ring_used];
-        P->ring_ldm_only[P->ring_used] = ldm_only;
-        P->ring_used++;
-        P->ring_stream = st;
-    } else if (timing) {
-        for (auto& e : P->ev)
-            if (!e) CU(cudaEventCreate(&e));
-    }
-    if (timing) CU(cudaEventRecord(ev[0], st));
-    CU(cudaMemsetAsync(P->counter, 0, sizeof(unsigned long long), st));
+    if (ev) CU(cudaEventRecord(ev[0], st));
+    CU(cudaMemsetAsync(W.counter, 0, sizeof(unsigned long long), st));
     RG(launch_scatter(sa, grid, smem, st));
-    P->last_fx_scale = sa.fx_scale;
-    if (timing) CU(cudaEventRecord(ev[1], st));
+    if (ev) CU(cudaEventRecord(ev[1], st));
     if (!ldm_only) {
         const rg_grid& g = s.grid;
-        // K2
         ColFftArgs ca;
         std::memset(&ca, 0, sizeof ca);
-        ca.f1 = P->f1;
-        ca.n1 = P->n1;
-        ca.n2 = P->n2;
-        ca.B = P->B;
+        ca.f1 = W.f1;
+        ca.n1 = W.n1;
+        ca.n2 = W.n2;
+        ca.B = W.B;
         ca.n_v = n_v;
-        ca.n = P->n;
-        ca.row_stride = P->row_stride;
+        ca.n = W.n;
+        ca.row_stride = W.row_stride;
         ca.n_pairs = s.n_nodes / 2;
-        ca.ldm = P->ldm;
-        ca.inv_fx_scale = 1.f / sa.fx_scale;
-        ca.y = P->y;
-        ca.tw_hi = P->tw_hi;
-        ca.tw_lo = P->tw_lo;
+        ca.ldm = W.ldm;
+        ca.cmax = W.cmax_dev;
+        ca.y = W.y;
+        ca.tw_hi = W.tw_hi;
+        ca.tw_lo = W.tw_lo;
         RG(launch_col_fft_fwd(ca, st));
-        if (timing) CU(cudaEventRecord(ev[2], st));
-        // K3
+        if (ev) CU(cudaEventRecord(ev[2], st));
         VoigtArgs* va = new (std::nothrow) VoigtArgs();
         if (!va) return fail(RG_ERR_OOM, "host allocation failed");
         std::unique_ptr<VoigtArgs> vguard(va);
-        va->f2 = P->f2;
-        va->threads = row_threads(P->f2);
-        row_voigt_layout(P->n2, &va->pairs_per_pass, &va->row_twiddle_table);
-        va->n1 = P->n1;
-        va->n2 = P->n2;
-        va->n = P->n;
+        va->f2 = W.f2;
+        va->threads = row_threads(W.f2);
+        row_voigt_layout(W.n2, &va->pairs_per_pass, &va->row_twiddle_table);
+        va->n1 = W.n1;
+        va->n2 = W.n2;
+        va->n = W.n;
         va->n_pairs = s.n_nodes / 2;
         va->n_nodes = s.n_nodes;
         va->NL = g.n_L;
-        va->y = P->y;
-        va->g = P->g;
-        va->tw_hi = P->tw_hi;
-        va->tw_lo = P->tw_lo;
-        va->inv_ndv = (float)(1.0 / ((double)P->n * P->desc.dv));
-        va->half_fs = (float)(0.5 / P->desc.dv);
-        const double thresh = P->desc.folding_thresh > 0 ? P->desc.folding_thresh : 1e-6;
+        va->y = W.y;
+        va->g = W.g;
+        va->tw_hi = W.tw_hi;
+        va->tw_lo = W.tw_lo;
+        va->inv_ndv = (float)(1.0 / ((double)W.n * W.desc.dv));
+        va->half_fs = (float)(0.5 / W.desc.dv);
+        const double thresh = W.desc.folding_thresh > 0 ? W.desc.folding_thresh : 1e-6;
         for (int l = 0; l < g.n_G; ++l) {
             double wG = std::exp(g.log_wG_min + l * g.dxG);
             va->alpha[l] = (float)(std::pow(kPi * wG, 2) / (4.0 * kLn2) * kLog2e);
@@ -616,58 +608,108 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
             int l = node / g.n_L, m = node % g.n_L;
             int nf;
             double nrm;
-            node_fold(P->desc.dv, std::exp(g.log_wG_min + l * g.dxG), std::exp(g.log_wL_min + m * g.dxL), thresh,
+            node_fold(W.desc.dv, std::exp(g.log_wG_min + l * g.dxG), std::exp(g.log_wL_min + m * g.dxL), thresh,
                       &nf, &nrm);
             va->norm[node] = (float)nrm;
             va->nfold[node] = (unsigned char)nf;
             if (nf) va->any_fold = 1;
         }
-        CU(cudaMemsetAsync(P->g, 0, sizeof(float2) * (size_t)P->n, st));
+        CU(cudaMemsetAsync(W.g, 0, sizeof(float2) * (size_t)W.n, st));
         RG(launch_row_fft_voigt(*va, st));
-        if (timing) CU(cudaEventRecord(ev[3], st));
-        // K3b
+        if (ev) CU(cudaEventRecord(ev[3], st));
         RowIfftArgs ra;
-        ra.f2 = P->f2;
-        ra.n1 = P->n1;
-        ra.n2 = P->n2;
-        ra.n = P->n;
-        ra.g = P->g;
-        ra.tw_hi = P->tw_hi;
-        ra.tw_lo = P->tw_lo;
+        ra.f2 = W.f2;
+        ra.n1 = W.n1;
+        ra.n2 = W.n2;
+        ra.n = W.n;
+        ra.g = W.g;
+        ra.tw_hi = W.tw_hi;
+        ra.tw_lo = W.tw_lo;
         RG(launch_row_ifft(ra, st));
-        if (timing) CU(cudaEventRecord(ev[4], st));
-        // K4
-        ca.h = P->g;
+        if (ev) CU(cudaEventRecord(ev[4], st));
+        ca.h = W.g;
         ca.out = out;
-        ca.out_scale = (float)(std::exp(s.log_scale_int - s.log_scale_out) / ((double)P->n * P->desc.dv));
+        ca.out_scale = (float)(std::exp(s.log_scale_int - s.log_scale_out) / ((double)W.n * W.desc.dv));
         RG(launch_col_ifft(ca, st));
-        if (timing) CU(cudaEventRecord(ev[5], st));
+        if (ev) CU(cudaEventRecord(ev[5], st));
     }
     // publish the device error flag to pinned host memory and clear it
-    CU(cudaMemcpyAsync(P->err_host, P->err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-    CU(cudaMemsetAsync(P->err, 0, sizeof(unsigned), st));
+    CU(cudaMemcpyAsync(W.err_host, W.err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    CU(cudaMemsetAsync(W.err, 0, sizeof(unsigned), st));
+    return RG_OK;
+}
+
+int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st, int timing, bool ldm_only,
+                 rg_spectrum_info* info) {
+    SpecHost s;
+    RG(compute_grid(P->lines, P->w, c, &s));
+    cudaEvent_t* ev = nullptr;
+    if (timing == 2) {
+        if (P->ring.empty()) {
+            P->ring.assign(rg_plan::kRing * 6, nullptr);
+            for (auto& e : P->ring) CU(cudaEventCreate(&e));
+        }
+        if (P->ring_used >= rg_plan::kRing) return fail(RG_ERR_RANGE, "stage-timing ring full: read it first");
+        ev = &P->ring[6 * P->ring_used];
+        P->ring_ldm_only[P->ring_used] = ldm_only;
+        P->ring_used++;
+        P->ring_stream = st;
+    } else if (timing) {
+        for (auto& e : P->ev)
+            if (!e) CU(cudaEventCreate(&e));
+        ev = P->ev;
+    }
+    RG(enqueue_spectrum(P->lines, P->w, c, s, out, st, ev, ldm_only));
     if (info) {
         std::memset(info, 0, sizeof *info);
         info->grid = s.grid;
         info->log_scale = ldm_only ? s.log_scale_int : s.log_scale_out;
+        info->lines_in_window = -1;
     }
     if (timing == 1 && info) {
         CU(cudaStreamSynchronize(st));
-        RG(take_err(P));
+        RG(take_err(P->w));
         int last = ldm_only ? 1 : 5;
         for (int i = 0; i < last; ++i) CU(cudaEventElapsedTime(&info->stage_ms[i], P->ev[i], P->ev[i + 1]));
         CU(cudaEventElapsedTime(&info->stage_ms[5], P->ev[0], P->ev[last]));
-    }
-    if (info) {
         unsigned long long cnt = 0;
-        if (timing == 1) {
-            CU(cudaMemcpy(&cnt, P->counter, sizeof cnt, cudaMemcpyDeviceToHost));
-            info->lines_in_window = (int64_t)cnt;
-        } else {
-            info->lines_in_window = -1;
-        }
+        CU(cudaMemcpy(&cnt, P->w.counter, sizeof cnt, cudaMemcpyDeviceToHost));
+        info->lines_in_window = (int64_t)cnt;
     }
     return RG_OK;
+}
+
+// FFT factorisation, twiddle tables (device, owned by the caller) and line
+// index geometry of a spectral grid.
+int tw_n_tables(int64_t n, float2** hi_out, float2** lo_out) {
+    const int nh = (int)(n / 1024) + 2;
+    std::vector<float2> hi(nh), lo(1024);
+    for (int t = 0; t < nh; ++t) {
+        double ang = -2.0 * kPi * (double)((int64_t)t * 1024 % n) / (double)n;
+        hi[t].x = (float)std::cos(ang);
+        hi[t].y = (float)std::sin(ang);
+    }
+    for (int t = 0; t < 1024; ++t) {
+        double ang = -2.0 * kPi * (double)t / (double)n;
+        lo[t].x = (float)std::cos(ang);
+        lo[t].y = (float)std::sin(ang);
+    }
+    CU(cudaMalloc(hi_out, sizeof(float2) * nh));
+    CU(cudaMalloc(lo_out, sizeof(float2) * 1024));
+    CU(cudaMemcpy(*hi_out, hi.data(), sizeof(float2) * nh, cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(*lo_out, lo.data(), sizeof(float2) * 1024, cudaMemcpyHostToDevice));
+    return RG_OK;
+}
+
+// Shift-index margin (columns) for pressures up to p_atm_max.
+void shift_margin(const rg_lines* L, double dv, int* E, double* p_atm_max) {
+    *p_atm_max = 200.0;
+    double e = std::ceil(L->env.max_abs_delta * *p_atm_max / dv) + 2;
+    if (e > (double)(1 << 22)) {
+        *p_atm_max = ((double)(1 << 22) - 2) * dv / L->env.max_abs_delta;
+        e = (double)(1 << 22);
+    }
+    *E = (int)e;
 }
 
 bool valid(const rg_ctx* c) { return c && c->magic == 0x52474358; }
@@ -813,7 +855,7 @@ int rg_lines_free(rg_lines* L) {
     g_err.clear();
     if (!L) return RG_OK;
     if (!valid(L)) return fail(RG_ERR_STATE, "invalid line list");
-    if (L->plans) return fail(RG_ERR_STATE, "line list still has %d plan(s)", L->plans);
+    if (L->plans.load()) return fail(RG_ERR_STATE, "line list still has %d plan(s) or queued request(s)", L->plans.load());
     cudaSetDevice(L->ctx->device);
     cudaStreamSynchronize(L->ctx->stream);
     dfree(L->v0);
@@ -850,71 +892,58 @@ int rg_plan_create(rg_lines* L, const rg_plan_desc* d, rg_plan** out) {
     if (!P) return fail(RG_ERR_OOM, "host allocation failed");
     std::unique_ptr<rg_plan> guard(P);
     P->lines = L;
-    P->desc = *d;
+    Work& W = P->w;
+    W.desc = *d;
     int n1, n2;
     if (!choose_fft(2 * d->n_v, d->n_ft, &n1, &n2))
         return fail(RG_ERR_RANGE, "no supported FFT length >= %lld (n_ft=%lld)", (long long)(2 * d->n_v),
                     (long long)d->n_ft);
-    P->n1 = n1;
-    P->n2 = n2;
-    P->n = (int64_t)n1 * n2;
-    P->B = col_block(n1);
-    RG(make_fftlen(n1, &P->f1));
-    RG(make_fftlen(n2, &P->f2));
-    {
-        const int nh = (int)(P->n / 1024) + 2;
-        std::vector<float2> hi(nh), lo(1024);
-        for (int t = 0; t < nh; ++t) {
-            double ang = -2.0 * kPi * (double)((int64_t)t * 1024 % P->n) / (double)P->n;
-            hi[t].x = (float)std::cos(ang);
-            hi[t].y = (float)std::sin(ang);
-        }
-        for (int t = 0; t < 1024; ++t) {
-            double ang = -2.0 * kPi * (double)t / (double)P->n;
-            lo[t].x = (float)std::cos(ang);
-            lo[t].y = (float)std::sin(ang);
-        }
-        CU(cudaMalloc(&P->tw_hi, sizeof(float2) * nh));
-        CU(cudaMalloc(&P->tw_lo, sizeof(float2) * 1024));
-        CU(cudaMemcpy(P->tw_hi, hi.data(), sizeof(float2) * nh, cudaMemcpyHostToDevice));
-        CU(cudaMemcpy(P->tw_lo, lo.data(), sizeof(float2) * 1024, cudaMemcpyHostToDevice));
-    }
+    W.n1 = n1;
+    W.n2 = n2;
+    W.n = (int64_t)n1 * n2;
+    W.B = col_block(n1);
+    RG(make_fftlen(n1, &W.f1));
+    RG(make_fftlen(n2, &W.f2));
+    RG(tw_n_tables(W.n, &P->tw_hi_own, &P->tw_lo_own));
+    W.tw_hi = P->tw_hi_own;
+    W.tw_lo = P->tw_lo_own;
     // line index per grid column, with a margin for pressure shifts up to p_atm_max
-    P->p_atm_max = 200.0;
-    int E = (int)std::ceil(L->env.max_abs_delta * P->p_atm_max / d->dv) + 2;
-    if (E > (1 << 22)) {
-        P->p_atm_max = ((double)(1 << 22) - 2) * d->dv / L->env.max_abs_delta;
-        E = 1 << 22;
-    }
-    P->col_off = E;
-    P->col_count = (int)d->n_v + 1 + 2 * E;
-    CU(cudaMalloc(&P->col_start, sizeof(int64_t) * P->col_count));
-    RG(launch_col_index(L->v0, L->n, d->vmin, d->dv, -E, P->col_count, P->col_start, L->ctx->stream));
-    P->row_stride = (d->n_v + 31) / 32 * 32;
-    CU(cudaMalloc(&P->g, sizeof(float2) * (size_t)P->n));
+    shift_margin(L, d->dv, &W.E, &W.p_atm_max);
+    W.col_off = W.E;
+    W.col_count = (int)d->n_v + 1 + 2 * W.E;
+    cudaStream_t st = L->ctx->stream;
+    CU(cudaMalloc(&W.col_start, sizeof(int64_t) * W.col_count));
+    RG(launch_col_index(L->v0, L->n, d->vmin, d->dv, -W.E, W.col_count, W.col_start, st));
+    CU(cudaMalloc(&W.cmax_dev, sizeof(int)));
+    RG(launch_col_cmax(W.col_start, W.col_off, W.col_count, (int)d->n_v, W.E, W.cmax_dev, st));
+    W.row_stride = (d->n_v + 31) / 32 * 32;
+    CU(cudaMalloc(&W.g, sizeof(float2) * (size_t)W.n));
     CU(cudaMalloc(&P->out_d, sizeof(float) * (size_t)d->n_v));
-    CU(cudaMalloc(&P->counter, sizeof(unsigned long long)));
-    CU(cudaMalloc(&P->err, sizeof(unsigned)));
-    CU(cudaHostAlloc(&P->err_host, sizeof(unsigned), cudaHostAllocDefault));
-    *P->err_host = 0;
-    CU(cudaMemsetAsync(P->err, 0, sizeof(unsigned), L->ctx->stream));
-    {   // most lines that can touch one column (k0 in {c-1, c}, shifts up to E columns)
-        std::vector<int64_t> cs(P->col_count);
-        CU(cudaMemcpyAsync(cs.data(), P->col_start, sizeof(int64_t) * P->col_count, cudaMemcpyDeviceToHost,
-                           L->ctx->stream));
-        CU(cudaStreamSynchronize(L->ctx->stream));
-        int64_t m = 0;
-        for (int c = 0; c < (int)d->n_v; ++c) {
-            const int lo = std::max(0, c - 1 - E + P->col_off);
-            const int hi = std::min(P->col_count - 1, c + 1 + E + P->col_off);
-            m = std::max(m, cs[hi] - cs[lo]);
-        }
-        P->cmax = m;
-    }
-    CU(cudaStreamSynchronize(L->ctx->stream));
+    CU(cudaMalloc(&W.counter, sizeof(unsigned long long)));
+    CU(cudaMalloc(&W.err, sizeof(unsigned)));
+    CU(cudaHostAlloc(&W.err_host, sizeof(unsigned), cudaHostAllocDefault));
+    *W.err_host = 0;
+    CU(cudaMemsetAsync(W.err, 0, sizeof(unsigned), st));
+    int cm = 0;
+    CU(cudaMemcpyAsync(&cm, W.cmax_dev, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    W.cmax_host = cm;
     L->plans++;
     *out = guard.release();
     return RG_OK;
+}
+
+void free_work(Work& W) {
+    dfree(W.col_start);
+    dfree(W.cmax_dev);
+    dfree(W.ldm);
+    dfree(W.y);
+    dfree(W.g);
+    dfree(W.counter);
+    dfree(W.err);
+    if (W.err_host) cudaFreeHost(W.err_host);
+    W.err_host = nullptr;
+    W.nodes_cap = 0;
 }
 
 int rg_plan_free(rg_plan* P) {
@@ -926,18 +955,12 @@ int rg_plan_free(rg_plan* P) {
         cudaSetDevice(P->lines->ctx->device);
         cudaStreamSynchronize(P->lines->ctx->stream);
         cudaDeviceSynchronize();
-        dfree(P->f1.tw);
-        dfree(P->f2.tw);
-        dfree(P->tw_hi);
-        dfree(P->tw_lo);
-        dfree(P->col_start);
-        dfree(P->ldm);
-        dfree(P->y);
-        dfree(P->g);
+        dfree(P->w.f1.tw);
+        dfree(P->w.f2.tw);
+        dfree(P->tw_hi_own);
+        dfree(P->tw_lo_own);
+        free_work(P->w);
         dfree(P->out_d);
-        dfree(P->counter);
-        dfree(P->err);
-        if (P->err_host) cudaFreeHost(P->err_host);
         for (auto& e : P->ev)
             if (e) cudaEventDestroy(e);
         for (auto& e : P->ring)
@@ -953,7 +976,7 @@ int rg_plan_grid(rg_plan* P, const rg_conditions* c, rg_grid* out) {
     g_err.clear();
     if (!valid(P) || !c || !out) return fail(RG_ERR_ARG, "invalid argument");
     SpecHost s;
-    RG(compute_grid(P, c, &s));
+    RG(compute_grid(P->lines, P->w, c, &s));
     *out = s.grid;
     return RG_OK;
 }
@@ -1006,7 +1029,7 @@ int rg_plan_stage_times(rg_plan* P, double* sum_ms, int64_t* count) {
         sum_ms[5] += ms;
     }
     P->ring_used = 0;
-    return take_err(P);
+    return take_err(P->w);
 }
 
 int rg_synthesize_host(rg_plan* P, const rg_conditions* c, float* out_host, void* stream, int timing,
@@ -1017,9 +1040,9 @@ int rg_synthesize_host(rg_plan* P, const rg_conditions* c, float* out_host, void
     CU(cudaSetDevice(P->lines->ctx->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
     RG(run_spectrum(P, c, P->out_d, st, (timing && info) ? 1 : 0, false, info));
-    CU(cudaMemcpyAsync(out_host, P->out_d, sizeof(float) * (size_t)P->desc.n_v, cudaMemcpyDeviceToHost, st));
+    CU(cudaMemcpyAsync(out_host, P->out_d, sizeof(float) * (size_t)P->w.desc.n_v, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
-    return take_err(P);
+    return take_err(P->w);
 }
 
 int rg_debug_ldm(rg_plan* P, const rg_conditions* c, float* ldm_host, int64_t capacity,
@@ -1032,17 +1055,424 @@ int rg_debug_ldm(rg_plan* P, const rg_conditions* c, float* ldm_host, int64_t ca
     rg_spectrum_info tmp;
     rg_spectrum_info* inf = info ? info : &tmp;
     RG(run_spectrum(P, c, nullptr, st, 1, true, inf));
+    const int64_t nv = P->w.desc.n_v;
     const int nodes = inf->grid.n_G * inf->grid.n_L;
-    if (capacity < (int64_t)nodes * P->desc.n_v)
-        return fail(RG_ERR_ARG, "capacity %lld < %lld", (long long)capacity, (long long)nodes * P->desc.n_v);
-    CU(cudaMemcpy2DAsync(ldm_host, sizeof(float) * P->desc.n_v, P->ldm, sizeof(unsigned) * P->row_stride,
-                         sizeof(float) * P->desc.n_v, nodes, cudaMemcpyDeviceToHost, st));
+    if (capacity < (int64_t)nodes * nv)
+        return fail(RG_ERR_ARG, "capacity %lld < %lld", (long long)capacity, (long long)nodes * nv);
+    CU(cudaMemcpy2DAsync(ldm_host, sizeof(float) * nv, P->w.ldm, sizeof(unsigned) * P->w.row_stride,
+                         sizeof(float) * nv, nodes, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
-    RG(take_err(P));
+    RG(take_err(P->w));
     // the device LDM holds fixed-point words: convert in place
-    const float inv = 1.f / P->last_fx_scale;
+    const float inv = 1.f / fx_scale_of((int)P->w.cmax_host);
     unsigned* w = reinterpret_cast<unsigned*>(ldm_host);
-    for (int64_t i = 0; i < (int64_t)nodes * P->desc.n_v; ++i) ldm_host[i] = (float)w[i] * inv;
+    for (int64_t i = 0; i < (int64_t)nodes * nv; ++i) ldm_host[i] = (float)w[i] * inv;
+    return RG_OK;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Serving engine
+// ===========================================================================
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct ServerReq {
+    int64_t ticket = 0;
+    rg_lines* lines = nullptr;
+    rg_plan_desc desc{};
+    rg_conditions cond{};
+    std::vector<double> q;
+    float* out_host = nullptr;
+    // results
+    bool done = false;
+    int status = RG_OK;
+    std::string msg;
+    rg_spectrum_info info{};
+    double t_submit = 0, t_start = 0, t_done = 0;
+};
+
+struct Slot {
+    cudaStream_t st = nullptr;
+    Work w;
+    float* out_d = nullptr;
+    int64_t out_cap = 0, col_cap = 0, g_cap = 0;
+    std::shared_ptr<ServerReq> req;
+    bool notified = false;
+    size_t bytes() const {
+        return (size_t)out_cap * 4 + (size_t)col_cap * 8 + (size_t)g_cap * 8 +
+               (size_t)w.nodes_cap * ((size_t)w.row_stride * 4 + (size_t)w.n * 4);
+    }
+};
+
+}  // namespace
+
+struct rg_server {
+    rg_ctx* ctx = nullptr;
+    int64_t budget = 0;
+    std::vector<Slot> slots;
+    std::deque<std::shared_ptr<ServerReq>> pending;
+    std::map<int64_t, std::shared_ptr<ServerReq>> reqs;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::thread worker;
+    bool stop = false;
+    int64_t next_ticket = 1, completed = 0, failed = 0;
+    std::map<int, FftLen> fft;
+    std::map<int64_t, std::pair<float2*, float2*>> twn;
+    Clock::time_point t0 = Clock::now();
+    uint32_t magic = 0x52475356;
+
+    double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+    int64_t used_bytes() const {
+        int64_t u = 0;
+        for (const Slot& sl : slots) u += (int64_t)sl.bytes();
+        return u;
+    }
+};
+
+namespace {
+
+struct HostNote {
+    rg_server* srv;
+    int slot;
+};
+
+void CUDART_CB slot_done_cb(void* p) {
+    // runs on a CUDA driver thread: no CUDA calls here, only wake the worker
+    auto* hn = static_cast<HostNote*>(p);
+    {
+        std::lock_guard<std::mutex> lk(hn->srv->mu);
+        hn->srv->slots[hn->slot].notified = true;
+    }
+    hn->srv->cv_work.notify_one();
+    delete hn;
+}
+
+int server_tables(rg_server* S, Work& W) {
+    for (int L : {W.n1, W.n2}) {
+        auto it = S->fft.find(L);
+        if (it == S->fft.end()) {
+            FftLen f;
+            RG(make_fftlen(L, &f));
+            it = S->fft.emplace(L, f).first;
+        }
+        (L == W.n1 ? W.f1 : W.f2) = it->second;
+    }
+    if (W.n1 == W.n2) W.f2 = W.f1;
+    auto t = S->twn.find(W.n);
+    if (t == S->twn.end()) {
+        float2 *hi = nullptr, *lo = nullptr;
+        RG(tw_n_tables(W.n, &hi, &lo));
+        t = S->twn.emplace(W.n, std::make_pair(hi, lo)).first;
+    }
+    W.tw_hi = t->second.first;
+    W.tw_lo = t->second.second;
+    return RG_OK;
+}
+
+// Workspace bytes a request needs on a slot (for admission).
+int request_need(rg_server* S, const ServerReq& r, SpecHost* sh, int64_t* need, int* n1o, int* n2o) {
+    int n1, n2;
+    if (!choose_fft(2 * r.desc.n_v, r.desc.n_ft, &n1, &n2))
+        return fail(RG_ERR_RANGE, "no supported FFT length >= %lld", (long long)(2 * r.desc.n_v));
+    RG(compute_grid_env(r.lines->env, r.desc, (int64_t)n1 * n2, n1, n2, &r.cond, sh));
+    const int64_t n = (int64_t)n1 * n2, rs = (r.desc.n_v + 31) / 32 * 32;
+    int E;
+    double pmax;
+    shift_margin(r.lines, r.desc.dv, &E, &pmax);
+    *need = r.desc.n_v * 4 + (r.desc.n_v + 1 + 2 * (int64_t)E) * 8 + n * 8 +
+            (int64_t)sh->n_nodes * (rs * 4 + n * 4);
+    *n1o = n1;
+    *n2o = n2;
+    (void)S;
+    return RG_OK;
+}
+
+template <typename T>
+int grow(T** p, int64_t* cap, int64_t want, cudaStream_t st) {
+    if (want <= *cap) return RG_OK;
+    if (*p) CU(cudaFreeAsync(*p, st));
+    *p = nullptr;
+    *cap = 0;
+    CU(cudaMallocAsync((void**)p, sizeof(T) * (size_t)want, st));
+    *cap = want;
+    return RG_OK;
+}
+
+void release_slot_buffers(Slot& sl) {
+    if (sl.w.ldm) cudaFreeAsync(sl.w.ldm, sl.st);
+    if (sl.w.y) cudaFreeAsync(sl.w.y, sl.st);
+    if (sl.w.g) cudaFreeAsync(sl.w.g, sl.st);
+    if (sl.w.col_start) cudaFreeAsync(sl.w.col_start, sl.st);
+    if (sl.out_d) cudaFreeAsync(sl.out_d, sl.st);
+    sl.w.ldm = nullptr;
+    sl.w.y = nullptr;
+    sl.w.g = nullptr;
+    sl.w.col_start = nullptr;
+    sl.out_d = nullptr;
+    sl.w.nodes_cap = 0;
+    sl.out_cap = sl.col_cap = sl.g_cap = 0;
+}
+
+// Launch request r on slot `si` (called by the worker with the lock held).
+int start_on_slot(rg_server* S, int si, const std::shared_ptr<ServerReq>& r, const SpecHost& sh, int n1, int n2) {
+    Slot& sl = S->slots[si];
+    Work& W = sl.w;
+    const rg_plan_desc& d = r->desc;
+    const bool new_geom = W.n != (int64_t)n1 * n2 || W.row_stride != (d.n_v + 31) / 32 * 32;
+    W.desc = d;
+    W.n1 = n1;
+    W.n2 = n2;
+    W.n = (int64_t)n1 * n2;
+    W.B = col_block(n1);
+    RG(server_tables(S, W));
+    shift_margin(r->lines, d.dv, &W.E, &W.p_atm_max);
+    W.col_off = W.E;
+    W.col_count = (int)d.n_v + 1 + 2 * W.E;
+    if (new_geom) {   // LDM rows / FFT rows change shape: drop the node buffers
+        if (W.ldm) CU(cudaFreeAsync(W.ldm, sl.st));
+        if (W.y) CU(cudaFreeAsync(W.y, sl.st));
+        W.ldm = nullptr;
+        W.y = nullptr;
+        W.nodes_cap = 0;
+    }
+    W.row_stride = (d.n_v + 31) / 32 * 32;
+    RG(grow(&W.col_start, &sl.col_cap, W.col_count, sl.st));
+    RG(grow(&W.g, &sl.g_cap, W.n, sl.st));
+    RG(grow(&sl.out_d, &sl.out_cap, d.n_v, sl.st));
+    const rg_lines* L = r->lines;
+    RG(launch_col_index(L->v0, L->n, d.vmin, d.dv, -W.E, W.col_count, W.col_start, sl.st));
+    RG(launch_col_cmax(W.col_start, W.col_off, W.col_count, (int)d.n_v, W.E, W.cmax_dev, sl.st));
+    RG(enqueue_spectrum(L, W, &r->cond, sh, sl.out_d, sl.st, nullptr, false));
+    CU(cudaMemcpyAsync(r->out_host, sl.out_d, sizeof(float) * (size_t)d.n_v, cudaMemcpyDeviceToHost, sl.st));
+    r->info.grid = sh.grid;
+    r->info.log_scale = sh.log_scale_out;
+    r->info.lines_in_window = -1;
+    sl.req = r;
+    sl.notified = false;
+    auto* hn = new HostNote{S, si};
+    CU(cudaLaunchHostFunc(sl.st, slot_done_cb, hn));
+    return RG_OK;
+}
+
+void finish_request(rg_server* S, const std::shared_ptr<ServerReq>& r, int status, const std::string& msg) {
+    r->lines->plans--;
+    r->status = status;
+    r->msg = msg;
+    r->done = true;
+    r->t_done = S->now();
+    if (status == RG_OK)
+        S->completed++;
+    else
+        S->failed++;
+}
+
+void worker_loop(rg_server* S) {
+    cudaSetDevice(S->ctx->device);
+    std::unique_lock<std::mutex> lk(S->mu);
+    for (;;) {
+        // completions
+        bool any_busy = false;
+        for (size_t i = 0; i < S->slots.size(); ++i) {
+            Slot& sl = S->slots[i];
+            if (!sl.req) continue;
+            if (sl.notified) {
+                const bool bad = *sl.w.err_host != 0;
+                *sl.w.err_host = 0;
+                finish_request(S, sl.req, bad ? RG_ERR_TIMEOUT : RG_OK,
+                               bad ? "a bounded device wait in the scatter gave up" : "");
+                sl.req.reset();
+                sl.notified = false;
+                S->cv_done.notify_all();
+            } else {
+                any_busy = true;
+            }
+        }
+        // admissions (FIFO: the head waits for a slot and for memory)
+        while (!S->pending.empty()) {
+            auto r = S->pending.front();
+            SpecHost sh;
+            int64_t need;
+            int n1, n2;
+            g_err.clear();
+            int rc = request_need(S, *r, &sh, &need, &n1, &n2);
+            if (rc != RG_OK) {
+                S->pending.pop_front();
+                finish_request(S, r, rc, g_err);
+                S->cv_done.notify_all();
+                continue;
+            }
+            if (need > S->budget) {
+                S->pending.pop_front();
+                finish_request(S, r, RG_ERR_OOM, "request needs more device memory than the server budget");
+                S->cv_done.notify_all();
+                continue;
+            }
+            int si = -1;
+            for (size_t i = 0; i < S->slots.size(); ++i)
+                if (!S->slots[i].req) {
+                    si = (int)i;
+                    break;
+                }
+            if (si < 0) break;
+            const int64_t others = S->used_bytes() - (int64_t)S->slots[si].bytes();
+            if (others + need > S->budget) {
+                // release idle slots' buffers first; then wait for running ones
+                for (Slot& sl : S->slots)
+                    if (!sl.req) release_slot_buffers(sl);
+                if (S->used_bytes() + need > S->budget) break;
+            }
+            S->pending.pop_front();
+            r->t_start = S->now();
+            g_err.clear();
+            rc = start_on_slot(S, si, r, sh, n1, n2);
+            if (rc != RG_OK) {
+                finish_request(S, r, rc, g_err);
+                S->slots[si].req.reset();
+                S->cv_done.notify_all();
+                continue;
+            }
+            any_busy = true;
+        }
+        if (S->stop && S->pending.empty() && !any_busy) break;
+        S->cv_work.wait_for(lk, std::chrono::milliseconds(50));
+    }
+}
+
+bool valid(const rg_server* s) { return s && s->magic == 0x52475356; }
+
+}  // namespace
+
+extern "C" {
+
+int rg_server_create(rg_ctx* ctx, int slots, int64_t mem_budget, rg_server** out) {
+    g_err.clear();
+    if (!valid(ctx) || !out) return fail(RG_ERR_ARG, "invalid argument");
+    if (slots < 1 || slots > 64) return fail(RG_ERR_ARG, "slots must be in [1, 64]");
+    if (mem_budget <= 0) return fail(RG_ERR_ARG, "mem_budget must be positive");
+    CU(cudaSetDevice(ctx->device));
+    auto* S = new (std::nothrow) rg_server();
+    if (!S) return fail(RG_ERR_OOM, "host allocation failed");
+    std::unique_ptr<rg_server> guard(S);
+    S->ctx = ctx;
+    S->budget = mem_budget;
+    S->slots.resize(slots);
+    for (Slot& sl : S->slots) {
+        CU(cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking));
+        CU(cudaMalloc(&sl.w.cmax_dev, sizeof(int)));
+        CU(cudaMalloc(&sl.w.counter, sizeof(unsigned long long)));
+        CU(cudaMalloc(&sl.w.err, sizeof(unsigned)));
+        CU(cudaMemset(sl.w.err, 0, sizeof(unsigned)));
+        CU(cudaHostAlloc(&sl.w.err_host, sizeof(unsigned), cudaHostAllocDefault));
+        *sl.w.err_host = 0;
+    }
+    ctx->lines++;   // the context stays alive while the server exists
+    S->worker = std::thread(worker_loop, S);
+    *out = guard.release();
+    return RG_OK;
+}
+
+int rg_server_submit(rg_server* S, const rg_request* req, int64_t* ticket) {
+    g_err.clear();
+    if (!valid(S) || !req || !ticket) return fail(RG_ERR_ARG, "invalid argument");
+    if (!valid(req->lines) || !req->out_host) return fail(RG_ERR_ARG, "invalid line list or output buffer");
+    const rg_plan_desc& d = req->grid;
+    if (!(d.dv > 0) || d.n_v < 2 || d.n_v > ((int64_t)1 << 30)) return fail(RG_ERR_ARG, "bad grid");
+    if (!((d.n_G > 1) || d.dxG > 0) || !((d.n_L > 1) || d.dxL > 0))
+        return fail(RG_ERR_ARG, "give dxG/dxL > 0 or node counts n_G/n_L > 1");
+    auto r = std::make_shared<ServerReq>();
+    r->lines = req->lines;
+    r->desc = d;
+    r->cond = req->cond;
+    if (req->cond.q_ratio) {
+        r->q.assign(req->cond.q_ratio, req->cond.q_ratio + req->lines->n_iso);
+        r->cond.q_ratio = r->q.data();
+    }
+    r->out_host = req->out_host;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (S->stop) return fail(RG_ERR_STATE, "server is shutting down");
+        r->lines->plans++;   // the list must outlive the request
+        r->ticket = S->next_ticket++;
+        r->t_submit = S->now();
+        S->reqs[r->ticket] = r;
+        S->pending.push_back(r);
+        *ticket = r->ticket;
+    }
+    S->cv_work.notify_one();
+    return RG_OK;
+}
+
+int rg_server_wait(rg_server* S, int64_t ticket, double timeout_ms, rg_spectrum_info* info, double* t_submit,
+                   double* t_start, double* t_done) {
+    g_err.clear();
+    if (!valid(S)) return fail(RG_ERR_ARG, "invalid server");
+    std::unique_lock<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(ticket);
+    if (it == S->reqs.end()) return fail(RG_ERR_ARG, "unknown ticket %lld", (long long)ticket);
+    std::shared_ptr<ServerReq> r = it->second;
+    auto ready = [&] { return r->done; };
+    if (timeout_ms < 0) {
+        S->cv_done.wait(lk, ready);
+    } else if (!S->cv_done.wait_for(lk, std::chrono::duration<double, std::milli>(timeout_ms), ready)) {
+        return fail(RG_ERR_TIMEOUT, "ticket %lld not finished within %g ms", (long long)ticket, timeout_ms);
+    }
+    if (info) *info = r->info;
+    if (t_submit) *t_submit = r->t_submit;
+    if (t_start) *t_start = r->t_start;
+    if (t_done) *t_done = r->t_done;
+    S->reqs.erase(ticket);
+    if (r->status != RG_OK) return fail(r->status, "%s", r->msg.c_str());
+    return RG_OK;
+}
+
+int rg_server_stats_get(rg_server* S, rg_server_stats* st) {
+    g_err.clear();
+    if (!valid(S) || !st) return fail(RG_ERR_ARG, "invalid argument");
+    std::lock_guard<std::mutex> lk(S->mu);
+    st->completed = S->completed;
+    st->failed = S->failed;
+    st->queued = (int64_t)S->pending.size();
+    st->in_flight = 0;
+    for (const Slot& sl : S->slots)
+        if (sl.req) st->in_flight++;
+    st->submitted = S->next_ticket - 1;
+    st->device_bytes = S->used_bytes();
+    return RG_OK;
+}
+
+int rg_server_destroy(rg_server* S) {
+    g_err.clear();
+    if (!S) return RG_OK;
+    if (!valid(S)) return fail(RG_ERR_STATE, "invalid server");
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->stop = true;
+    }
+    S->cv_work.notify_one();
+    if (S->worker.joinable()) S->worker.join();
+    cudaSetDevice(S->ctx->device);
+    for (Slot& sl : S->slots) {
+        cudaStreamSynchronize(sl.st);
+        release_slot_buffers(sl);
+        cudaStreamSynchronize(sl.st);
+        dfree(sl.w.cmax_dev);
+        dfree(sl.w.counter);
+        dfree(sl.w.err);
+        if (sl.w.err_host) cudaFreeHost(sl.w.err_host);
+        cudaStreamDestroy(sl.st);
+    }
+    for (auto& kv : S->fft) dfree(kv.second.tw);
+    for (auto& kv : S->twn) {
+        dfree(kv.second.first);
+        dfree(kv.second.second);
+    }
+    S->ctx->lines--;
+    S->magic = 0;
+    delete S;
     return RG_OK;
 }
 

@@ -103,7 +103,7 @@ struct ScatterArgs {
     float stim_c;             // c2/T log2e
     unsigned long long* in_window;   // nullable counter of lines in the window
     // persistent TMA-fed scatter
-    float fx_scale;           // fixed-point scale 2^e of the tile accumulator
+    const int* cmax;          // device: most lines that can touch one column (sets the fixed-point scale)
     int n_tiles;
     int chunk;                // lines per staged chunk (multiple of 16)
     unsigned* err;            // set to 1 when a bounded wait gives up
@@ -133,7 +133,7 @@ struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
     int64_t row_stride;
     int n_pairs;
     const unsigned* ldm;  // K2 input: fixed-point words of the scatter
-    float inv_fx_scale;   // 1 / fixed-point scale
+    const int* cmax;      // device: fixed-point bound of the scatter (scale = fx_scale(*cmax))
     float2* y;            // K2 output [pair][n1][n2]
     const float2* tw_hi;  // exp(-2 pi i 1024 t / N)
     const float2* tw_lo;  // exp(-2 pi i t / N), t < 1024
@@ -174,11 +174,24 @@ struct RowIfftArgs {      // K3b (inverse row FFT + twiddle, in place)
     const float2* tw_lo;
 };
 
+// Fixed-point scale of the scatter accumulator: 2^e with (cmax + 1) 2^e <= 2^31.
+RG_HD inline float fx_scale_of(int cmax) {
+    int bits = 0;
+    while (bits < 31 && (1u << bits) <= (unsigned)(cmax + 1)) ++bits;
+    const int e = 31 - bits;
+    float s = 1.f;
+    for (int i = 0; i < e; ++i) s *= 2.f;
+    return s;
+}
+
 // --- launchers (rg_kernels.cu) ---------------------------------------------------
 int launch_prepare_lines(const double* v0_d, const double* s_d, int64_t n, double c2_tref,
                          float2* v0_out, float* ls2_out, int* unsorted_flag, cudaStream_t st);
 int launch_col_index(const float2* v0, int64_t n, double vmin, double dv, int c_min, int count,
                      int64_t* col_start, cudaStream_t st);
+// max over grid columns of the lines within E columns (fixed-point bound), into *cmax
+int launch_col_cmax(const int64_t* col_start, int col_off, int col_count, int n_v, int E, int* cmax,
+                    cudaStream_t st);
 int launch_scatter(const ScatterArgs& a, int grid, size_t smem, cudaStream_t st);
 int scatter_smem_optin(size_t* avail);
 int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st);

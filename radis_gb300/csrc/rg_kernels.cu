@@ -17,6 +17,7 @@
 // the Hermitian pairing of bins k and N-k is absorbed by taking the real part.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 
 #include "rg_internal.h"
@@ -316,6 +317,19 @@ __global__ void k_col_index(const float2* __restrict__ v0, int64_t n, double vmi
     col_start[idx] = lo;
 }
 
+// most lines with v0 in columns [c - 1 - E, c + 1 + E) over the grid columns
+__global__ void k_col_cmax(const int64_t* __restrict__ col_start, int col_off, int col_count, int n_v, int E,
+                           int* __restrict__ cmax) {
+    int m = 0;
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n_v; c += gridDim.x * blockDim.x) {
+        const int lo = max(0, min(c - 1 - E + col_off, col_count - 1));
+        const int hi = max(0, min(c + 1 + E + col_off, col_count - 1));
+        m = max(m, (int)min(col_start[hi] - col_start[lo], (int64_t)0x3fffffff));
+    }
+    for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m) atomicMax(cmax, m);
+}
+
 // ---------------------------------------------------------------------------
 // K1: fused line scaling + LDM scatter into a shared-memory tile
 // ---------------------------------------------------------------------------
@@ -407,7 +421,7 @@ __device__ __forceinline__ void issue_chunk(const ScatterArgs& a, unsigned char*
 
 // Scale + scatter of the lines of one staged chunk into the tile accumulator.
 __device__ __forceinline__ unsigned scatter_chunk(const ScatterArgs& a, const Stage& st, int count, int k_start,
-                                                  int tk, unsigned* tile) {
+                                                  int tk, unsigned* tile, float fxs) {
     unsigned counted = 0;
     for (int j = threadIdx.x; j < count; j += blockDim.x) {
         const float2 v = st.v0[j];
@@ -449,7 +463,7 @@ __device__ __forceinline__ unsigned scatter_chunk(const ScatterArgs& a, const St
         two_sum(ph, a.bI_hi[is], s1, f1);
         two_sum(s1, st.ls2[j], s2, f2);
         const float arg = s2 + (f1 + f2 + pe2 + a.bI_lo[is]);
-        const float I = ex2(arg) * (1.f - ex2(-a.stim_c * v.x)) * a.fx_scale;
+        const float I = ex2(arg) * (1.f - ex2(-a.stim_c * v.x)) * fxs;
         const float I1 = tv * I;
         const float I0 = I - I1;
         const float w11 = tG * tL;
@@ -490,6 +504,7 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
     unsigned* tile = reinterpret_cast<unsigned*>(tile4);
     const int G = gridDim.x;
     const int nq = (a.n_tiles - (int)blockIdx.x + G - 1) / G;   // tiles of this CTA (<= kScatMaxTilesPerCta)
+    const float fxs = fx_scale_of(*a.cmax);
     const int n4 = a.n_nodes * a.TK / 4;
     const bool has_dl = a.dl != nullptr, has_iso = a.iso != nullptr;
 
@@ -555,7 +570,7 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
                 return;
             }
             counted += scatter_chunk(a, stage_view(stage[g & 1], ch, has_dl, has_iso), min(ch, b - cs), k_start, tk,
-                                     tile);
+                                     tile, fxs);
             __syncthreads();   // stage[g & 1] free again
             ++g;
         }
@@ -593,7 +608,7 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_fft_fwd(const Col
     // the LDM holds the scatter's fixed-point words: value = word / fx_scale
     const unsigned* ra = a.ldm + (int64_t)(2 * pair) * a.row_stride;
     const unsigned* rb = ra + a.row_stride;
-    const float inv = a.inv_fx_scale;
+    const float inv = 1.f / fx_scale_of(*a.cmax);
     const int n2i = c0 + b;
     float2 v[8];
 #pragma unroll
@@ -701,7 +716,7 @@ __device__ __forceinline__ void twiddleP(float2* A, float2* B, const float2* __r
 // first pass (sub-transform length 1): global rows x four-step twiddle ->
 // registers -> smem.  twr: per-row twiddle table in smem, or nullptr to use
 // the global two-level table.
-template <int R, int PAIRS>
+template <int R, int PAIRS, bool TWR>
 __device__ __forceinline__ void row_first(const float2* __restrict__ ya, const float2* __restrict__ yb,
                                           const float2* twr, const VoigtArgs& a, int k1,
                                           typename RowT<PAIRS>::E* out, int L) {
@@ -711,7 +726,7 @@ __device__ __forceinline__ void row_first(const float2* __restrict__ ya, const f
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const int i = j + r * M;
-            const float2 w = twr ? twr[i] : ((k1 && i) ? twiddle_n(a.tw_hi, a.tw_lo, k1 * i) : make_float2(1.f, 0.f));
+            const float2 w = TWR ? twr[i] : ((k1 && i) ? twiddle_n(a.tw_hi, a.tw_lo, k1 * i) : make_float2(1.f, 0.f));
             A[r] = cmul(__ldg(&ya[i]), w);
             if (PAIRS == 2) B[r] = yb ? cmul(__ldg(&yb[i]), w) : make_float2(0.f, 0.f);
         }
@@ -750,7 +765,7 @@ __host__ __device__ inline size_t row_voigt_smem(int n2, bool with_twr) {
 }
 
 // IT = iterations of the last (radix-8) pass per thread: IT * blockDim * 8 >= n2
-template <int IT, int PAIRS>
+template <int IT, int PAIRS, bool TWR>
 __global__ void __launch_bounds__(kRowMaxThreads, IT == 1 ? 2 : 1) k_row_fft_voigt(const VoigtArgs a) {
     using E = typename RowT<PAIRS>::E;
     extern __shared__ float4 sm4[];
@@ -758,14 +773,14 @@ __global__ void __launch_bounds__(kRowMaxThreads, IT == 1 ? 2 : 1) k_row_fft_voi
     const int len = RowT<PAIRS>::len(n2);
     E* buf0 = reinterpret_cast<E*>(sm4);
     E* buf1 = buf0 + len;
-    float2* twr = a.row_twiddle_table ? reinterpret_cast<float2*>(buf1 + len) : nullptr;
+    float2* twr = TWR ? reinterpret_cast<float2*>(buf1 + len) : nullptr;
     const int k1 = blockIdx.x;
     const int n = (int)a.n;
     const int j0 = blockIdx.y * kPairGroup;
     const int j1 = min(j0 + kPairGroup, a.n_pairs);
     const FftLen& P = a.f2;
     const int ML = n2 / 8;    // butterflies of the last pass (radix 8, sub-length ML)
-    if (twr)
+    if (TWR)
         for (int t = threadIdx.x; t < n2; t += blockDim.x)
             twr[t] = (k1 && t) ? twiddle_n(a.tw_hi, a.tw_lo, k1 * t) : make_float2(1.f, 0.f);
     // frequencies of the bins this thread owns in the last pass: t = jl + r ML
@@ -788,11 +803,11 @@ __global__ void __launch_bounds__(kRowMaxThreads, IT == 1 ? 2 : 1) k_row_fft_voi
         const float2* ya = a.y + ((int64_t)j * a.n1 + k1) * n2;
         const float2* yb = two ? a.y + ((int64_t)(j + 1) * a.n1 + k1) * n2 : nullptr;
         switch (P.radix[0]) {
-            case 2: row_first<2, PAIRS>(ya, yb, twr, a, k1, buf0, n2); break;
-            case 3: row_first<3, PAIRS>(ya, yb, twr, a, k1, buf0, n2); break;
-            case 4: row_first<4, PAIRS>(ya, yb, twr, a, k1, buf0, n2); break;
-            case 5: row_first<5, PAIRS>(ya, yb, twr, a, k1, buf0, n2); break;
-            default: row_first<8, PAIRS>(ya, yb, twr, a, k1, buf0, n2); break;
+            case 2: row_first<2, PAIRS, TWR>(ya, yb, twr, a, k1, buf0, n2); break;
+            case 3: row_first<3, PAIRS, TWR>(ya, yb, twr, a, k1, buf0, n2); break;
+            case 4: row_first<4, PAIRS, TWR>(ya, yb, twr, a, k1, buf0, n2); break;
+            case 5: row_first<5, PAIRS, TWR>(ya, yb, twr, a, k1, buf0, n2); break;
+            default: row_first<8, PAIRS, TWR>(ya, yb, twr, a, k1, buf0, n2); break;
         }
         __syncthreads();
         E* in = buf0;
@@ -966,6 +981,14 @@ int launch_col_index(const float2* v0, int64_t n, double vmin, double dv, int c_
     return check_launch();
 }
 
+int launch_col_cmax(const int64_t* col_start, int col_off, int col_count, int n_v, int E, int* cmax,
+                    cudaStream_t st) {
+    if (cudaMemsetAsync(cmax, 0, sizeof(int), st) != cudaSuccess) return RG_ERR_CUDA;
+    const int blocks = std::min((n_v + 255) / 256, 1024);
+    k_col_cmax<<<std::max(blocks, 1), 256, 0, st>>>(col_start, col_off, col_count, n_v, E, cmax);
+    return check_launch();
+}
+
 int launch_scatter(const ScatterArgs& a, int grid, size_t smem, cudaStream_t st) {
     ALLOW_SMEM(k_scatter, smem);
     k_scatter<<<grid, kScatThreads, smem, st>>>(a);
@@ -1000,21 +1023,21 @@ int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st) {
     }
 }
 
-template <int IT, int PAIRS>
+template <int IT, int PAIRS, bool TWR>
 static int row_voigt(const VoigtArgs& a, cudaStream_t st) {
-    const size_t smem = row_voigt_smem<PAIRS>(a.n2, a.row_twiddle_table != 0);
-    ALLOW_SMEM((k_row_fft_voigt<IT, PAIRS>), smem);
+    const size_t smem = row_voigt_smem<PAIRS>(a.n2, TWR);
+    ALLOW_SMEM((k_row_fft_voigt<IT, PAIRS, TWR>), smem);
     dim3 grid(a.n1, (a.n_pairs + kPairGroup - 1) / kPairGroup);
-    k_row_fft_voigt<IT, PAIRS><<<grid, a.threads, smem, st>>>(a);
+    k_row_fft_voigt<IT, PAIRS, TWR><<<grid, a.threads, smem, st>>>(a);
     return check_launch();
 }
 
-template <int PAIRS>
+template <int PAIRS, bool TWR>
 static int row_voigt_it(const VoigtArgs& a, cudaStream_t st) {
     const int per = (a.n2 / 8 + a.threads - 1) / a.threads;
-    if (per <= 1) return row_voigt<1, PAIRS>(a, st);
-    if (per <= 2) return row_voigt<2, PAIRS>(a, st);
-    if (per <= 4) return row_voigt<4, PAIRS>(a, st);
+    if (per <= 1) return row_voigt<1, PAIRS, TWR>(a, st);
+    if (per <= 2) return row_voigt<2, PAIRS, TWR>(a, st);
+    if (per <= 4) return row_voigt<4, PAIRS, TWR>(a, st);
     return RG_ERR_RANGE;
 }
 
@@ -1038,7 +1061,8 @@ void row_voigt_layout(int n2, int* pairs, int* with_twr) {
 int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st) {
     if (a.f2.npass < 2 || a.f2.radix[a.f2.npass - 1] != 8) return RG_ERR_RANGE;
     if (a.threads < 32 || a.threads > kRowMaxThreads || a.threads % 32) return RG_ERR_RANGE;
-    return a.pairs_per_pass == 2 ? row_voigt_it<2>(a, st) : row_voigt_it<1>(a, st);
+    if (a.pairs_per_pass == 2) return row_voigt_it<2, true>(a, st);
+    return a.row_twiddle_table ? row_voigt_it<1, true>(a, st) : row_voigt_it<1, false>(a, st);
 }
 
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st) {
