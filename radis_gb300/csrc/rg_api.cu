@@ -1099,8 +1099,8 @@ struct Slot {
     Work w;
     float* out_d = nullptr;
     int64_t out_cap = 0, col_cap = 0, g_cap = 0;
-    std::shared_ptr<ServerReq> req;
-    bool notified = false;
+    std::shared_ptr<ServerReq> req;       // owned by the worker thread
+    std::atomic<bool> notified{false};    // set by the stream's host callback
     size_t bytes() const {
         return (size_t)out_cap * 4 + (size_t)col_cap * 8 + (size_t)g_cap * 8 +
                (size_t)w.nodes_cap * ((size_t)w.row_stride * 4 + (size_t)w.n * 4);
@@ -1109,6 +1109,11 @@ struct Slot {
 
 }  // namespace
 
+// Locking: `mu` guards the queue, the ticket map, request results and the
+// counters; it is never held across a CUDA call.  The worker thread alone
+// owns the slots.  Host callbacks on the slot streams touch only atomics and
+// `sig_mu` (the worker's doorbell), so they can never wait on a thread that
+// is itself inside a CUDA call.
 struct rg_server {
     rg_ctx* ctx = nullptr;
     int64_t budget = 0;
@@ -1116,14 +1121,26 @@ struct rg_server {
     std::deque<std::shared_ptr<ServerReq>> pending;
     std::map<int64_t, std::shared_ptr<ServerReq>> reqs;
     std::mutex mu;
-    std::condition_variable cv_work, cv_done;
+    std::condition_variable cv_done;
+    std::mutex sig_mu;
+    std::condition_variable cv_sig;
+    uint64_t sig_count = 0;                // guarded by sig_mu
+    std::atomic<int64_t> dev_bytes{0};
     std::thread worker;
     bool stop = false;
     int64_t next_ticket = 1, completed = 0, failed = 0;
-    std::map<int, FftLen> fft;
-    std::map<int64_t, std::pair<float2*, float2*>> twn;
+    std::map<int, FftLen> fft;                              // worker only
+    std::map<int64_t, std::pair<float2*, float2*>> twn;     // worker only
     Clock::time_point t0 = Clock::now();
     uint32_t magic = 0x52475356;
+
+    void ring() {
+        {
+            std::lock_guard<std::mutex> lk(sig_mu);
+            ++sig_count;
+        }
+        cv_sig.notify_one();
+    }
 
     double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
     int64_t used_bytes() const {
@@ -1141,13 +1158,10 @@ struct HostNote {
 };
 
 void CUDART_CB slot_done_cb(void* p) {
-    // runs on a CUDA driver thread: no CUDA calls here, only wake the worker
+    // runs on a CUDA driver thread: no CUDA calls and no `mu` here
     auto* hn = static_cast<HostNote*>(p);
-    {
-        std::lock_guard<std::mutex> lk(hn->srv->mu);
-        hn->srv->slots[hn->slot].notified = true;
-    }
-    hn->srv->cv_work.notify_one();
+    hn->srv->slots[hn->slot].notified.store(true);
+    hn->srv->ring();
     delete hn;
 }
 
@@ -1251,13 +1265,13 @@ int start_on_slot(rg_server* S, int si, const std::shared_ptr<ServerReq>& r, con
     r->info.grid = sh.grid;
     r->info.log_scale = sh.log_scale_out;
     r->info.lines_in_window = -1;
-    sl.req = r;
-    sl.notified = false;
+    sl.notified.store(false);
     auto* hn = new HostNote{S, si};
     CU(cudaLaunchHostFunc(sl.st, slot_done_cb, hn));
     return RG_OK;
 }
 
+// With `mu` held.
 void finish_request(rg_server* S, const std::shared_ptr<ServerReq>& r, int status, const std::string& msg) {
     r->lines->plans--;
     r->status = status;
@@ -1272,73 +1286,105 @@ void finish_request(rg_server* S, const std::shared_ptr<ServerReq>& r, int statu
 
 void worker_loop(rg_server* S) {
     cudaSetDevice(S->ctx->device);
-    std::unique_lock<std::mutex> lk(S->mu);
+    uint64_t seen = 0;
     for (;;) {
-        // completions
+        // 1. completions (slots are the worker's; the flags come from callbacks)
+        std::vector<std::pair<std::shared_ptr<ServerReq>, bool>> finished;
         bool any_busy = false;
-        for (size_t i = 0; i < S->slots.size(); ++i) {
-            Slot& sl = S->slots[i];
+        for (Slot& sl : S->slots) {
             if (!sl.req) continue;
-            if (sl.notified) {
+            if (sl.notified.load()) {
                 const bool bad = *sl.w.err_host != 0;
                 *sl.w.err_host = 0;
-                finish_request(S, sl.req, bad ? RG_ERR_TIMEOUT : RG_OK,
-                               bad ? "a bounded device wait in the scatter gave up" : "");
+                finished.emplace_back(sl.req, bad);
                 sl.req.reset();
-                sl.notified = false;
+                sl.notified.store(false);
+            } else {
+                any_busy = true;
+            }
+        }
+        // 2. take admissible requests off the queue (FIFO: the head waits)
+        struct Start {
+            int si;
+            std::shared_ptr<ServerReq> r;
+            SpecHost sh;
+            int n1, n2;
+        };
+        std::vector<Start> starts;
+        bool stopping, release_idle = false;
+        {
+            std::lock_guard<std::mutex> lk(S->mu);
+            for (auto& f : finished)
+                finish_request(S, f.first, f.second ? RG_ERR_TIMEOUT : RG_OK,
+                               f.second ? "a bounded device wait in the scatter gave up" : "");
+            int64_t planned = 0;   // bytes the starts below may add
+            while (!S->pending.empty()) {
+                auto r = S->pending.front();
+                Start st;
+                int64_t need;
+                g_err.clear();
+                int rc = request_need(S, *r, &st.sh, &need, &st.n1, &st.n2);
+                if (rc != RG_OK || need > S->budget) {
+                    S->pending.pop_front();
+                    finish_request(S, r, rc != RG_OK ? rc : RG_ERR_OOM,
+                                   rc != RG_OK ? g_err : "request needs more device memory than the server budget");
+                    continue;
+                }
+                int si = -1;
+                for (size_t i = 0; i < S->slots.size(); ++i) {
+                    bool taken = S->slots[i].req != nullptr;
+                    for (const Start& o : starts) taken |= o.si == (int)i;
+                    if (!taken) {
+                        si = (int)i;
+                        break;
+                    }
+                }
+                if (si < 0) break;
+                const int64_t others = S->used_bytes() - (int64_t)S->slots[si].bytes() + planned;
+                if (others + need > S->budget) {
+                    // nothing runs: give the idle slots' memory back (outside `mu`), retry
+                    if (!any_busy && starts.empty() && S->used_bytes() > 0) release_idle = true;
+                    break;
+                }
+                S->pending.pop_front();
+                r->t_start = S->now();
+                st.si = si;
+                st.r = r;
+                planned += need;
+                starts.push_back(std::move(st));
+            }
+            stopping = S->stop && S->pending.empty();
+        }
+        if (!finished.empty()) S->cv_done.notify_all();
+        if (release_idle) {
+            for (Slot& sl : S->slots)
+                if (!sl.req) release_slot_buffers(sl);
+            S->dev_bytes.store(S->used_bytes());
+            continue;
+        }
+        // 3. launch outside `mu`
+        for (Start& st : starts) {
+            g_err.clear();
+            S->slots[st.si].req = st.r;
+            const int rc = start_on_slot(S, st.si, st.r, st.sh, st.n1, st.n2);
+            if (rc != RG_OK) {
+                S->slots[st.si].req.reset();
+                const std::string msg = g_err;
+                {
+                    std::lock_guard<std::mutex> lk(S->mu);
+                    finish_request(S, st.r, rc, msg);
+                }
                 S->cv_done.notify_all();
             } else {
                 any_busy = true;
             }
         }
-        // admissions (FIFO: the head waits for a slot and for memory)
-        while (!S->pending.empty()) {
-            auto r = S->pending.front();
-            SpecHost sh;
-            int64_t need;
-            int n1, n2;
-            g_err.clear();
-            int rc = request_need(S, *r, &sh, &need, &n1, &n2);
-            if (rc != RG_OK) {
-                S->pending.pop_front();
-                finish_request(S, r, rc, g_err);
-                S->cv_done.notify_all();
-                continue;
-            }
-            if (need > S->budget) {
-                S->pending.pop_front();
-                finish_request(S, r, RG_ERR_OOM, "request needs more device memory than the server budget");
-                S->cv_done.notify_all();
-                continue;
-            }
-            int si = -1;
-            for (size_t i = 0; i < S->slots.size(); ++i)
-                if (!S->slots[i].req) {
-                    si = (int)i;
-                    break;
-                }
-            if (si < 0) break;
-            const int64_t others = S->used_bytes() - (int64_t)S->slots[si].bytes();
-            if (others + need > S->budget) {
-                // release idle slots' buffers first; then wait for running ones
-                for (Slot& sl : S->slots)
-                    if (!sl.req) release_slot_buffers(sl);
-                if (S->used_bytes() + need > S->budget) break;
-            }
-            S->pending.pop_front();
-            r->t_start = S->now();
-            g_err.clear();
-            rc = start_on_slot(S, si, r, sh, n1, n2);
-            if (rc != RG_OK) {
-                finish_request(S, r, rc, g_err);
-                S->slots[si].req.reset();
-                S->cv_done.notify_all();
-                continue;
-            }
-            any_busy = true;
-        }
-        if (S->stop && S->pending.empty() && !any_busy) break;
-        S->cv_work.wait_for(lk, std::chrono::milliseconds(50));
+        S->dev_bytes.store(S->used_bytes());
+        if (stopping && !any_busy) break;
+        // 4. sleep until a submission or a completion rings (or 50 ms)
+        std::unique_lock<std::mutex> lk(S->sig_mu);
+        S->cv_sig.wait_for(lk, std::chrono::milliseconds(50), [&] { return S->sig_count != seen; });
+        seen = S->sig_count;
     }
 }
 
@@ -1359,7 +1405,7 @@ int rg_server_create(rg_ctx* ctx, int slots, int64_t mem_budget, rg_server** out
     std::unique_ptr<rg_server> guard(S);
     S->ctx = ctx;
     S->budget = mem_budget;
-    S->slots.resize(slots);
+    S->slots = std::vector<Slot>(slots);
     for (Slot& sl : S->slots) {
         CU(cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking));
         CU(cudaMalloc(&sl.w.cmax_dev, sizeof(int)));
@@ -1402,7 +1448,7 @@ int rg_server_submit(rg_server* S, const rg_request* req, int64_t* ticket) {
         S->pending.push_back(r);
         *ticket = r->ticket;
     }
-    S->cv_work.notify_one();
+    S->ring();
     return RG_OK;
 }
 
@@ -1436,11 +1482,9 @@ int rg_server_stats_get(rg_server* S, rg_server_stats* st) {
     st->completed = S->completed;
     st->failed = S->failed;
     st->queued = (int64_t)S->pending.size();
-    st->in_flight = 0;
-    for (const Slot& sl : S->slots)
-        if (sl.req) st->in_flight++;
     st->submitted = S->next_ticket - 1;
-    st->device_bytes = S->used_bytes();
+    st->in_flight = st->submitted - st->completed - st->failed - st->queued;
+    st->device_bytes = S->dev_bytes.load();
     return RG_OK;
 }
 
@@ -1452,7 +1496,7 @@ int rg_server_destroy(rg_server* S) {
         std::lock_guard<std::mutex> lk(S->mu);
         S->stop = true;
     }
-    S->cv_work.notify_one();
+    S->ring();
     if (S->worker.joinable()) S->worker.join();
     cudaSetDevice(S->ctx->device);
     for (Slot& sl : S->slots) {

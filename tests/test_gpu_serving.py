@@ -6,7 +6,8 @@ import pytest
 from radis_gb300 import _lib as L
 from radis_gb300 import synthetic as S
 
-pytestmark = pytest.mark.gpu
+# a hard per-test limit that also ends a test blocked inside a native call
+pytestmark = [pytest.mark.gpu, pytest.mark.timeout(240, method="thread")]
 TOL = 1e-4
 
 
