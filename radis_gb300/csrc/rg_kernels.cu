@@ -1095,9 +1095,11 @@ namespace rg {
 // [128, kRowMaxThreads] that wastes the fewest butterfly slots over the passes
 // (ties -> more threads).
 int row_threads(const FftLen& f) {
-    int best = 256;
+    // at most 4 last-pass (radix-8) butterflies per thread: T >= L / 32
+    const int t_min = std::max(128, (f.L / 32 + 31) / 32 * 32);
+    int best = std::max(256, t_min);
     double best_eff = -1.0;
-    for (int T = 128; T <= kRowMaxThreads; T += 32) {
+    for (int T = t_min; T <= kRowMaxThreads; T += 32) {
         long slots = 0, work = 0;
         for (int p = 0; p < f.npass; ++p) {
             const int M = f.L / f.radix[p];

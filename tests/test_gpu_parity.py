@@ -183,12 +183,12 @@ def test_co2_5M_full_size(ctx):
         o.close()
 
 
-@pytest.mark.parametrize("n_v", [800001, 1200001])
+@pytest.mark.parametrize("n_v", [800001, 1200001, 2000001])
 def test_long_rows(ctx, n_v):
     """Long spectra: the row transform runs one pair per pass (n2 = 3200 with
-    the per-row twiddle table, n2 = 4800 without it)."""
+    the per-row twiddle table, n2 = 4800 and 8000 without it)."""
     lines = S.uniform_lines(200_000, 2000.0, 2000.0 + (n_v - 1) * 0.001, seed=30)
     args = (44.0, 2000.0, 0.001, n_v, 1200.0, 0.8, 0.2)
     gpu, info = run_gpu(ctx, lines, *args, n_G=4, n_L=8)
-    assert info.grid.n2 in (3200, 4800)
+    assert info.grid.n2 in (3200, 4800, 8000)
     assert rel_err(gpu, oracle(lines, *args, info)) <= TOL
