@@ -166,6 +166,23 @@ int rg_synthesize_host(rg_plan* plan, const rg_conditions* cond, float* out_host
 int rg_debug_ldm(rg_plan* plan, const rg_conditions* cond, float* ldm_host, int64_t capacity,
                  rg_spectrum_info* info);
 
+/* Allocation-free spectrum.  No counterpart in the reference: it exists for
+ * callers that may not allocate device memory when they ask for a spectrum
+ * (a framework's caching allocator owns the device memory, a service forbids
+ * cudaMalloc/cudaFree on its request path, a pre-sized job).  The line list
+ * must already be resident (rg_lines_upload at setup) and `out_dev` holds
+ * n_v floats (abscoeff x exp(-info.log_scale)).  All scratch of the spectrum
+ * (line index, LDM, FFT workspace, twiddle tables, flags) is carved from one
+ * static device array of 64 MiB that every GPU loading this library keeps
+ * until the process exits; a spectrum that needs more returns RG_ERR_RANGE.
+ * Calls no cudaMalloc or cudaFree.  The first call on a device resolves the
+ * array's device address, so make it before any stream capture.  Blocking:
+ * returns when the spectrum is in out_dev.  Calls share the array and are
+ * serialised by a lock; work of two calls overlapping on the GPU (e.g. the
+ * same array used from two processes' streams) would race. */
+int rg_synthesize_static(rg_lines* lines, const rg_plan_desc* grid, const rg_conditions* cond,
+                         float* out_dev, void* stream, rg_spectrum_info* info);
+
 /* ---------------------------------------------------------------------------
  * Serving: continuous batching of spectrum requests over resident line lists.
  * No reference counterpart (the reference runs one blocking gpuApp.iterate at a

@@ -24,6 +24,7 @@ EXPORTS = [
     "rg_lines_free", "rg_lines_count", "rg_plan_create", "rg_plan_free", "rg_plan_grid", "rg_grid_estimate",
     "rg_synthesize", "rg_synthesize_host", "rg_debug_ldm", "rg_plan_stage_times",
     "rg_server_create", "rg_server_submit", "rg_server_wait", "rg_server_stats_get", "rg_server_destroy",
+    "rg_synthesize_static",
 ]
 
 
@@ -124,6 +125,8 @@ def load(path: str | None = None):
                             C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
         "rg_server_stats_get": ([vp, C.POINTER(ServerStats)], C.c_int),
         "rg_server_destroy": ([vp], C.c_int),
+        "rg_synthesize_static": ([vp, C.POINTER(PlanDesc), C.POINTER(Conditions), vp, vp,
+                                  C.POINTER(SpectrumInfo)], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -433,3 +436,21 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def synthesize_static(lines: Lines, vmin, dv, n_v, T, p_bar, x, out_dev_ptr: int, dxG=None, dxL=None,
+                      n_G=None, n_L=None, q_ratio=None, stream_ptr: int | None = None,
+                      folding_thresh=1e-6) -> SpectrumInfo:
+    """Allocation-free spectrum (rg_synthesize_static): every scratch buffer
+    comes from the library's static 64 MiB device array, so nothing is
+    allocated on the device during the call.  ``out_dev_ptr``: caller-owned
+    device buffer of n_v floats.  Blocking."""
+    d = PlanDesc(float(vmin), float(dv), int(n_v), float(dxG or 0.0), float(dxL or 0.0),
+                 int(n_G or 0), int(n_L or 0), float(folding_thresh), 0)
+    q = None if q_ratio is None else np.ascontiguousarray(
+        np.broadcast_to(np.asarray(q_ratio, np.float64), (lines.n_iso,)))
+    c = Conditions(float(T), float(p_bar), float(x), ptr(q))
+    info = SpectrumInfo()
+    check(load().rg_synthesize_static(lines.handle, C.byref(d), C.byref(c), C.c_void_p(out_dev_ptr),
+                                      C.c_void_p(stream_ptr) if stream_ptr else None, C.byref(info)))
+    return info

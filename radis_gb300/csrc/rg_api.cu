@@ -1521,3 +1521,144 @@ int rg_server_destroy(rg_server* S) {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Allocation-free synthesis over a static device scratch array
+// ===========================================================================
+// For callers that must not allocate device memory at the time they ask for a
+// spectrum: code running while a framework's caching allocator owns the
+// device memory, inside a memory-accounted service that forbids
+// cudaMalloc/cudaFree on the request path, or between setup and teardown of
+// a pre-sized job.  Every scratch buffer of one spectrum lives in this array;
+// every GPU that loads this library holds it until the process exits.
+constexpr size_t kStaticScratchBytes = (size_t)64 << 20;   // 64 MiB
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+namespace {
+
+std::mutex g_static_mu;                      // serialises calls (they share the array)
+void* g_static_ptr[64] = {nullptr};          // device address of the array, per device
+unsigned g_static_err_host = 0;              // host word the device error flag lands in
+
+// exp(-2 pi i t / L) for t < count (FP64 sincospi, rounded to FP32)
+__global__ void k_static_twiddles(float2* tw, int count, long long L, long long stride) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const long long q = ((long long)t * stride) % L;
+    double s, c;
+    sincospi(2.0 * (double)q / (double)L, &s, &c);
+    tw[t] = make_float2((float)c, (float)-s);
+}
+
+int static_twiddles(float2* tw, int count, long long L, long long stride, cudaStream_t st) {
+    k_static_twiddles<<<(count + 255) / 256, 256, 0, st>>>(tw, count, L, stride);
+    return cudaGetLastError() == cudaSuccess ? RG_OK : RG_ERR_CUDA;
+}
+
+// radix plan of one FFT length without any table (the table goes to scratch)
+int static_fftlen(int L, FftLen* f) {
+    f->L = L;
+    if (!radices(L, f->radix, &f->npass)) return fail(RG_ERR_RANGE, "FFT length %d not factorable", L);
+    int ns = 1;
+    for (int p = 0; p < f->npass; ++p) {
+        f->ns[p] = ns;
+        f->mag[p] = ns == 1 ? 0u : (unsigned)(((1ull << 32) + ns - 1) / (unsigned long long)ns);
+        ns *= f->radix[p];
+    }
+    return RG_OK;
+}
+
+}  // namespace
+
+extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg_conditions* c, float* out_dev,
+                                    void* stream, rg_spectrum_info* info) {
+    g_err.clear();
+    if (!valid(L) || !d || !c || !out_dev) return fail(RG_ERR_ARG, "invalid argument");
+    if (!(d->dv > 0) || d->n_v < 2 || d->n_v > ((int64_t)1 << 30)) return fail(RG_ERR_ARG, "bad grid");
+    if (!((d->n_G > 1) || d->dxG > 0) || !((d->n_L > 1) || d->dxL > 0))
+        return fail(RG_ERR_ARG, "give dxG/dxL > 0 or node counts n_G/n_L > 1");
+    const int dev = L->ctx->device;
+    if (dev < 0 || dev >= 64) return fail(RG_ERR_ARG, "device ordinal %d not supported", dev);
+    std::lock_guard<std::mutex> lk(g_static_mu);
+    CU(cudaSetDevice(dev));
+    if (!g_static_ptr[dev]) {
+        // once per device, with the device current: host code cannot use the
+        // array's name as an address, it needs the device address
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(RG_ERR_CUDA, "cudaGetSymbolAddress(static scratch): %s", cudaGetErrorString(e));
+        g_static_ptr[dev] = p;
+    }
+    unsigned char* base = static_cast<unsigned char*>(g_static_ptr[dev]);
+    cudaStream_t st = stream ? (cudaStream_t)stream : L->ctx->stream;
+
+    Work W;
+    W.desc = *d;
+    int n1, n2;
+    if (!choose_fft(2 * d->n_v, d->n_ft, &n1, &n2))
+        return fail(RG_ERR_RANGE, "no supported FFT length >= %lld", (long long)(2 * d->n_v));
+    W.n1 = n1;
+    W.n2 = n2;
+    W.n = (int64_t)n1 * n2;
+    W.B = col_block(n1);
+    RG(static_fftlen(n1, &W.f1));
+    RG(static_fftlen(n2, &W.f2));
+    shift_margin(L, d->dv, &W.E, &W.p_atm_max);
+    W.col_off = W.E;
+    W.col_count = (int)d->n_v + 1 + 2 * W.E;
+    W.row_stride = (d->n_v + 31) / 32 * 32;
+    SpecHost s;
+    RG(compute_grid_env(L->env, W.desc, W.n, W.n1, W.n2, c, &s));
+
+    // carve the scratch (256-byte aligned pieces)
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        void* q = base + off;
+        off += (bytes + 255) / 256 * 256;
+        return q;
+    };
+    const int nh = (int)(W.n / 1024) + 2;
+    W.col_start = static_cast<int64_t*>(take(sizeof(int64_t) * (size_t)W.col_count));
+    W.cmax_dev = static_cast<int*>(take(sizeof(int)));
+    W.counter = static_cast<unsigned long long*>(take(sizeof(unsigned long long)));
+    W.err = static_cast<unsigned*>(take(sizeof(unsigned)));
+    W.f1.tw = static_cast<float2*>(take(sizeof(float2) * (size_t)n1));
+    W.f2.tw = static_cast<float2*>(take(sizeof(float2) * (size_t)n2));
+    float2* twh = static_cast<float2*>(take(sizeof(float2) * (size_t)nh));
+    float2* twl = static_cast<float2*>(take(sizeof(float2) * 1024));
+    W.tw_hi = twh;
+    W.tw_lo = twl;
+    W.nodes_cap = s.n_nodes;   // sized here: the workspace step allocates nothing
+    W.ldm = static_cast<unsigned*>(take(sizeof(unsigned) * (size_t)s.n_nodes * (size_t)W.row_stride));
+    W.y = static_cast<float2*>(take(sizeof(float2) * (size_t)(s.n_nodes / 2) * (size_t)W.n));
+    W.g = static_cast<float2*>(take(sizeof(float2) * (size_t)W.n));
+    if (off > kStaticScratchBytes)
+        return fail(RG_ERR_RANGE,
+                    "spectrum needs %zu bytes of scratch, more than the %zu-byte static array of the "
+                    "allocation-free path (use a plan)",
+                    off, kStaticScratchBytes);
+    W.err_host = &g_static_err_host;
+
+    // every piece starts from what the previous call left: clear what must be zero
+    CU(cudaMemsetAsync(W.err, 0, sizeof(unsigned), st));
+    RG(static_twiddles(W.f1.tw, n1, n1, 1, st));
+    RG(static_twiddles(W.f2.tw, n2, n2, 1, st));
+    RG(static_twiddles(twh, nh, W.n, 1024, st));
+    RG(static_twiddles(twl, 1024, W.n, 1, st));
+    RG(launch_col_index(L->v0, L->n, d->vmin, d->dv, -W.E, W.col_count, W.col_start, st));
+    RG(launch_col_cmax(W.col_start, W.col_off, W.col_count, (int)d->n_v, W.E, W.cmax_dev, st));
+    RG(enqueue_spectrum(L, W, c, s, out_dev, st, nullptr, false));
+    CU(cudaStreamSynchronize(st));
+    if (g_static_err_host) {
+        g_static_err_host = 0;
+        return fail(RG_ERR_TIMEOUT, "a bounded device wait in the scatter gave up; the spectrum is invalid");
+    }
+    if (info) {
+        std::memset(info, 0, sizeof *info);
+        info->grid = s.grid;
+        info->log_scale = s.log_scale_out;
+        info->lines_in_window = -1;
+    }
+    return RG_OK;
+}
