@@ -139,13 +139,18 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def load_traffic():
-    """Per-launch DRAM traffic of the dominant kernel from the committed ncu
-    summary (profiles/*.json), if present."""
-    p = os.path.join(ROOT, "profiles", "traffic_co2_5M.json")
+def load_traffic(workload):
+    """Per-launch DRAM traffic (bytes) per kernel from the committed ncu
+    summary profiles/traffic_<workload>.txt ("kernel bytes" lines), if
+    present."""
+    p = os.path.join(ROOT, "profiles", f"traffic_{workload}.txt")
+    out = {}
     if os.path.exists(p):
-        return json.load(open(p))
-    return {}
+        for line in open(p):
+            f = line.split()
+            if len(f) == 2 and not line.startswith("#"):
+                out[f[0]] = int(f[1])
+    return out
 
 
 def cpu_baseline_sample(wl, lines, grid, n_ft, workers, frac=20):
@@ -409,7 +414,7 @@ def run_ours(args):
     dom = max(range(5), key=lambda i: stage_avg[i])
     name = STAGES[dom]
     achieved = ab[name] / (stage_avg[dom] * 1e-3) / 1e9
-    traffic = load_traffic().get(name)
+    traffic = load_traffic(wl).get(name)
     stages = {STAGES[i]: {"ms": stage_avg[i], "algorithmic_bytes": ab[STAGES[i]],
                           "GB/s": ab[STAGES[i]] / (stage_avg[i] * 1e-3) / 1e9 if stage_avg[i] else None}
               for i in range(5)}
