@@ -20,11 +20,17 @@
  *   rg_grid_estimate                <- the same rules on host arrays, no device
  *   rg_debug_ldm                    <- no reference entry point: reads back the
  *        LDM tensor so the scatter can be checked on its own
+ *   rg_backward / rg_jvp            <- no reference entry point: derivatives of
+ *        the spectrum with respect to (T, p, x) (reverse and forward mode)
  *
  * Every function returns an int status (RG_OK = 0); none aborts.  The text of
  * the last error on the calling thread is returned by rg_last_error().
  * A plan is not re-entrant: calls on one plan are serialised by an internal
- * mutex.  Distinct plans may be used concurrently from different threads.
+ * mutex, and its device work is ordered across streams (work enqueued on a
+ * stream other than the plan's previous one waits for that work first).
+ * Distinct plans may be used concurrently from different threads.  A NULL
+ * stream means the context's own stream; pass cudaStreamLegacy ((void*)1)
+ * for the legacy default stream.
  */
 #ifndef RADIS_GB300_H
 #define RADIS_GB300_H
@@ -165,6 +171,28 @@ int rg_synthesize_host(rg_plan* plan, const rg_conditions* cond, float* out_host
  * exp(info.log_scale) cm-1 . cm (times dv: no 1/dv yet).  capacity in floats. */
 int rg_debug_ldm(rg_plan* plan, const rg_conditions* cond, float* ldm_host, int64_t capacity,
                  rg_spectrum_info* info);
+
+/* Derivatives of the absorption coefficient with respect to the conditions
+ * theta = (T [K], p_bar [bar], x), with the LDM node axes held at the values
+ * the conditions give (the axes are a discretisation choice, not physics).
+ * The reference has no derivatives; these differentiate the same FP32 LDM
+ * synthesis that rg_synthesize computes.  dlnq_dT: per isotopologue
+ * d ln(Q(Tref)/Q(T)) / dT (NULL = 0, i.e. cond->q_ratio held constant).
+ *
+ * rg_backward (reverse mode, the adjoint): grad[q] = sum_k g[k] dA_k/dtheta_q
+ * for an upstream gradient g of n_v floats on the device (dL/dabscoeff in
+ * cm).  Runs the transposed synthesis (FFT of g, per-node Voigt multiply and
+ * inverse FFTs, gather at each line's LDM cells) and waits for it; the plan's
+ * workspace is reused.  grad is in true units; info (nullable) receives the
+ * grid, log_scale 0.
+ *
+ * rg_jvp (forward mode): out_dev[q n_v + k] = dA_k/dtheta_q x
+ * exp(-info.log_scale), three rows of n_v floats on the device (asynchronous
+ * on `stream`, like rg_synthesize). */
+int rg_backward(rg_plan* plan, const rg_conditions* cond, const double* dlnq_dT,
+                const float* grad_out_dev, double grad[3], void* stream, rg_spectrum_info* info);
+int rg_jvp(rg_plan* plan, const rg_conditions* cond, const double* dlnq_dT, float* out_dev,
+           void* stream, rg_spectrum_info* info);
 
 /* Allocation-free spectrum.  No counterpart in the reference: it exists for
  * callers that may not allocate device memory when they ask for a spectrum

@@ -24,7 +24,7 @@ EXPORTS = [
     "rg_lines_free", "rg_lines_count", "rg_plan_create", "rg_plan_free", "rg_plan_grid", "rg_grid_estimate",
     "rg_synthesize", "rg_synthesize_host", "rg_debug_ldm", "rg_plan_stage_times",
     "rg_server_create", "rg_server_submit", "rg_server_wait", "rg_server_stats_get", "rg_server_destroy",
-    "rg_synthesize_static",
+    "rg_synthesize_static", "rg_backward", "rg_jvp",
 ]
 
 
@@ -127,6 +127,9 @@ def load(path: str | None = None):
         "rg_server_destroy": ([vp], C.c_int),
         "rg_synthesize_static": ([vp, C.POINTER(PlanDesc), C.POINTER(Conditions), vp, vp,
                                   C.POINTER(SpectrumInfo)], C.c_int),
+        "rg_backward": ([vp, C.POINTER(Conditions), vp, vp, C.POINTER(C.c_double), vp,
+                         C.POINTER(SpectrumInfo)], C.c_int),
+        "rg_jvp": ([vp, C.POINTER(Conditions), vp, vp, vp, C.POINTER(SpectrumInfo)], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -295,6 +298,34 @@ class Plan:
         check(load().rg_synthesize(self.handle, C.byref(c), C.c_void_p(out_dev_ptr),
                                    C.c_void_p(stream_ptr) if stream_ptr else None,
                                    int(timing), C.byref(info)))
+        return info
+
+    def _dlnq(self, dlnq_dT):
+        if dlnq_dT is None:
+            return None
+        return np.ascontiguousarray(np.broadcast_to(np.asarray(dlnq_dT, np.float64), (self.lines.n_iso,)))
+
+    def backward(self, T, p_bar, x, grad_out_dev_ptr: int, q_ratio=None, dlnq_dT=None,
+                 stream_ptr: int | None = None):
+        """Reverse mode: sum_k g[k] d abscoeff_k / d(T, p_bar, x) for the n_v
+        floats g at ``grad_out_dev_ptr`` (node axes fixed at these conditions).
+        ``dlnq_dT``: d ln(Q(Tref)/Q(T))/dT per isotopologue.  Blocking; returns
+        a float64 array of 3."""
+        c, _q = self._cond(T, p_bar, x, q_ratio)
+        dq = self._dlnq(dlnq_dT)
+        out = (C.c_double * 3)()
+        check(load().rg_backward(self.handle, C.byref(c), ptr(dq), C.c_void_p(grad_out_dev_ptr), out,
+                                 C.c_void_p(stream_ptr) if stream_ptr else None, None))
+        return np.array(list(out))
+
+    def jvp(self, T, p_bar, x, out_dev_ptr: int, q_ratio=None, dlnq_dT=None, stream_ptr: int | None = None):
+        """Forward mode: enqueue d abscoeff / d(T, p_bar, x) x exp(-info.log_scale)
+        into 3 rows of n_v floats at ``out_dev_ptr``; returns the info."""
+        c, _q = self._cond(T, p_bar, x, q_ratio)
+        dq = self._dlnq(dlnq_dT)
+        info = SpectrumInfo()
+        check(load().rg_jvp(self.handle, C.byref(c), ptr(dq), C.c_void_p(out_dev_ptr),
+                            C.c_void_p(stream_ptr) if stream_ptr else None, C.byref(info)))
         return info
 
     def stage_times(self):

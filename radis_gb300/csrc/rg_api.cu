@@ -140,6 +140,7 @@ struct rg_plan {
     float2* tw_hi_own = nullptr;
     float2* tw_lo_own = nullptr;
     float* out_d = nullptr;
+    double* grad_d = nullptr;           // 3 sums of the adjoint gather, allocated on first use
     cudaEvent_t ev[6] = {nullptr};
     // ring of per-stage events recorded without synchronisation (timing == 2)
     static constexpr int kRing = 256;
@@ -147,6 +148,11 @@ struct rg_plan {
     int ring_used = 0;
     bool ring_ldm_only[kRing] = {false};
     cudaStream_t ring_stream = nullptr;
+    // device work of the plan is serialised across streams: work enqueued on a
+    // stream other than the last one waits for `done` (recorded after each call)
+    cudaEvent_t done = nullptr;
+    cudaStream_t last_stream = nullptr;
+    bool any = false;
     uint32_t magic = 0x52475041;
 };
 
@@ -524,6 +530,52 @@ void node_fold(double dv, double wG, double wL, double thresh, int* nfold, doubl
     *norm = 1.0 / v0;
 }
 
+// Row-kernel arguments of one spectrum: FFT geometry and the folded,
+// normalised Voigt FT parameters of every node of the grid.
+void fill_voigt_args(const Work& W, const SpecHost& s, VoigtArgs* va) {
+    const rg_grid& g = s.grid;
+    va->f2 = W.f2;
+    va->threads = row_threads(W.f2);
+    row_voigt_layout(W.n2, &va->pairs_per_pass, &va->row_twiddle_table);
+    va->n1 = W.n1;
+    va->n2 = W.n2;
+    va->n = W.n;
+    va->n_pairs = s.n_nodes / 2;
+    va->n_nodes = s.n_nodes;
+    va->NL = g.n_L;
+    va->y = W.y;
+    va->g = W.g;
+    va->tw_hi = W.tw_hi;
+    va->tw_lo = W.tw_lo;
+    va->inv_ndv = (float)(1.0 / ((double)W.n * W.desc.dv));
+    va->half_fs = (float)(0.5 / W.desc.dv);
+    const double thresh = W.desc.folding_thresh > 0 ? W.desc.folding_thresh : 1e-6;
+    for (int l = 0; l < g.n_G; ++l) {
+        double wG = std::exp(g.log_wG_min + l * g.dxG);
+        va->alpha[l] = (float)(std::pow(kPi * wG, 2) / (4.0 * kLn2) * kLog2e);
+    }
+    for (int m = 0; m < g.n_L; ++m) {
+        double wL = std::exp(g.log_wL_min + m * g.dxL);
+        va->beta[m] = (float)(kPi * wL * kLog2e);
+    }
+    va->any_fold = 0;
+    for (int node = 0; node < s.n_nodes; ++node) {
+        if (node >= g.n_G * g.n_L) {
+            va->norm[node] = 0.f;
+            va->nfold[node] = 0;
+            continue;
+        }
+        int l = node / g.n_L, m = node % g.n_L;
+        int nf;
+        double nrm;
+        node_fold(W.desc.dv, std::exp(g.log_wG_min + l * g.dxG), std::exp(g.log_wL_min + m * g.dxL), thresh, &nf,
+                  &nrm);
+        va->norm[node] = (float)nrm;
+        va->nfold[node] = (unsigned char)nf;
+        if (nf) va->any_fold = 1;
+    }
+}
+
 // After a synchronisation: report (once) a bounded device wait that gave up.
 int take_err(Work& W) {
     if (*W.err_host) {
@@ -553,7 +605,6 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
     RG(launch_scatter(sa, grid, smem, st));
     if (ev) CU(cudaEventRecord(ev[1], st));
     if (!ldm_only) {
-        const rg_grid& g = s.grid;
         ColFftArgs ca;
         std::memset(&ca, 0, sizeof ca);
         ca.f1 = W.f1;
@@ -574,46 +625,7 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
         VoigtArgs* va = new (std::nothrow) VoigtArgs();
         if (!va) return fail(RG_ERR_OOM, "host allocation failed");
         std::unique_ptr<VoigtArgs> vguard(va);
-        va->f2 = W.f2;
-        va->threads = row_threads(W.f2);
-        row_voigt_layout(W.n2, &va->pairs_per_pass, &va->row_twiddle_table);
-        va->n1 = W.n1;
-        va->n2 = W.n2;
-        va->n = W.n;
-        va->n_pairs = s.n_nodes / 2;
-        va->n_nodes = s.n_nodes;
-        va->NL = g.n_L;
-        va->y = W.y;
-        va->g = W.g;
-        va->tw_hi = W.tw_hi;
-        va->tw_lo = W.tw_lo;
-        va->inv_ndv = (float)(1.0 / ((double)W.n * W.desc.dv));
-        va->half_fs = (float)(0.5 / W.desc.dv);
-        const double thresh = W.desc.folding_thresh > 0 ? W.desc.folding_thresh : 1e-6;
-        for (int l = 0; l < g.n_G; ++l) {
-            double wG = std::exp(g.log_wG_min + l * g.dxG);
-            va->alpha[l] = (float)(std::pow(kPi * wG, 2) / (4.0 * kLn2) * kLog2e);
-        }
-        for (int m = 0; m < g.n_L; ++m) {
-            double wL = std::exp(g.log_wL_min + m * g.dxL);
-            va->beta[m] = (float)(kPi * wL * kLog2e);
-        }
-        va->any_fold = 0;
-        for (int node = 0; node < s.n_nodes; ++node) {
-            if (node >= g.n_G * g.n_L) {
-                va->norm[node] = 0.f;
-                va->nfold[node] = 0;
-                continue;
-            }
-            int l = node / g.n_L, m = node % g.n_L;
-            int nf;
-            double nrm;
-            node_fold(W.desc.dv, std::exp(g.log_wG_min + l * g.dxG), std::exp(g.log_wL_min + m * g.dxL), thresh,
-                      &nf, &nrm);
-            va->norm[node] = (float)nrm;
-            va->nfold[node] = (unsigned char)nf;
-            if (nf) va->any_fold = 1;
-        }
+        fill_voigt_args(W, s, va);
         CU(cudaMemsetAsync(W.g, 0, sizeof(float2) * (size_t)W.n, st));
         RG(launch_row_fft_voigt(*va, st));
         if (ev) CU(cudaEventRecord(ev[3], st));
@@ -639,6 +651,148 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
     return RG_OK;
 }
 
+// Derivative coefficients of every line at the conditions (node axes of s
+// held fixed); dlnq_dT[iso] = d ln(Q(Tref)/Q(T))/dT (NULL: 0).
+int fill_grad_args(const rg_lines* L, const Work& W, const rg_conditions* c, const SpecHost& s,
+                   const double* dlnq_dT, GradArgs* g) {
+    std::memset(g, 0, sizeof *g);
+    RG(build_scatter_args(L, W, c, s, &g->s));
+    if (!(c->x > 0)) return fail(RG_ERR_ARG, "derivatives need a mole fraction x > 0");
+    const double T = c->T, p = c->p_bar;
+    g->n_lines = L->n;
+    g->row_stride = W.row_stride;
+    g->c2_T = (float)(kC2 / T);
+    g->c2_T2 = (float)(kC2 / (T * T));
+    for (int i = 0; i < L->n_iso; ++i) g->cT0[i] = (float)((dlnq_dT ? dlnq_dT[i] : 0.0) - 1.0 / T);
+    g->gT = (float)(0.5 / (T * s.grid.dxG));
+    g->lT = (float)(1.0 / (T * s.grid.dxL));
+    g->lP = (float)(1.0 / (p * s.grid.dxL));
+    g->lX = (float)(1.0 / s.grid.dxL);
+    g->kP = (float)(1.0 / (1.01325 * W.desc.dv));
+    g->iP = (float)(1.0 / p);
+    g->iX = (float)(1.0 / c->x);
+    return RG_OK;
+}
+
+ColFftArgs col_args(const Work& W, const SpecHost& s) {
+    ColFftArgs ca;
+    std::memset(&ca, 0, sizeof ca);
+    ca.f1 = W.f1;
+    ca.n1 = W.n1;
+    ca.n2 = W.n2;
+    ca.B = W.B;
+    ca.n_v = (int)W.desc.n_v;
+    ca.n = W.n;
+    ca.row_stride = W.row_stride;
+    ca.n_pairs = s.n_nodes / 2;
+    ca.tw_hi = W.tw_hi;
+    ca.tw_lo = W.tw_lo;
+    return ca;
+}
+
+// Reverse mode: enqueue grad_d[0..2] = sum_k g[k] d(abscoeff_k)/d(T, p_bar, x)
+// / exp(log_scale_int), g = n_v floats on the device.  The plan's LDM buffer
+// holds the adjoint LDM (float) afterwards.
+int enqueue_backward(const rg_lines* L, Work& W, const rg_conditions* c, const SpecHost& s, const double* dlnq_dT,
+                     const float* g_dev, double* grad_d, cudaStream_t st) {
+    RG(ensure_workspace(W, s.n_nodes, st));
+    auto ga = std::make_unique<GradArgs>();
+    RG(fill_grad_args(L, W, c, s, dlnq_dT, ga.get()));
+    // Ghat = FFT(g): one real row through the column stage and the row stage
+    // with unit weights (node 0: V = 1, node 1: V = 0)
+    ColFftArgs ca = col_args(W, s);
+    ca.src = g_dev;
+    ca.single = 1;
+    ca.n_pairs = 1;
+    ca.y = W.y;
+    RG(launch_col_fft_fwd_f(ca, st));
+    auto ar = std::make_unique<AdjRowArgs>();
+    VoigtArgs& u = ar->v;
+    fill_voigt_args(W, s, &u);
+    VoigtArgs* unit = new (std::nothrow) VoigtArgs(u);
+    if (!unit) return fail(RG_ERR_OOM, "host allocation failed");
+    std::unique_ptr<VoigtArgs> uguard(unit);
+    unit->n_pairs = 1;
+    unit->n_nodes = 2;
+    unit->NL = 2;
+    unit->alpha[0] = 0.f;
+    unit->beta[0] = unit->beta[1] = 0.f;
+    unit->norm[0] = 1.f;
+    unit->norm[1] = 0.f;
+    unit->nfold[0] = unit->nfold[1] = 0;
+    unit->any_fold = 0;
+    CU(cudaMemsetAsync(W.g, 0, sizeof(float2) * (size_t)W.n, st));
+    RG(launch_row_fft_voigt(*unit, st));
+    // adjoint LDM rows: Re / Im of IFFT(Ghat (V_a + i V_b)) / (N dv), per pair
+    ar->y = W.y;
+    RG(launch_row_ifft_adj(*ar, st));
+    ColFftArgs cb = col_args(W, s);
+    cb.h = W.y;
+    cb.out = reinterpret_cast<float*>(W.ldm);
+    cb.out_scale = (float)(1.0 / ((double)W.n * W.desc.dv));
+    RG(launch_col_ifft_adj(cb, st));
+    // per-line chain rule gathered at the lines' cells
+    ga->adj = reinterpret_cast<const float*>(W.ldm);
+    ga->out = grad_d;
+    CU(cudaMemsetAsync(grad_d, 0, 3 * sizeof(double), st));
+    RG(launch_gather_grad(*ga, L->ctx->sms * 8, st));
+    return RG_OK;
+}
+
+// Forward mode: enqueue out + q n_v = d(abscoeff)/d(theta_q) exp(-log_scale_out)
+// for theta = (T, p_bar, x), through the float-LDM tangent scatter and the
+// ordinary FFT / Voigt / inverse FFT stages.
+int enqueue_tangent(const rg_lines* L, Work& W, const rg_conditions* c, const SpecHost& s, const double* dlnq_dT,
+                    float* out, cudaStream_t st) {
+    RG(ensure_workspace(W, s.n_nodes, st));
+    auto ga = std::make_unique<GradArgs>();
+    RG(fill_grad_args(L, W, c, s, dlnq_dT, ga.get()));
+    auto va = std::make_unique<VoigtArgs>();
+    fill_voigt_args(W, s, va.get());
+    float* tan = reinterpret_cast<float*>(W.ldm);
+    ga->tan = tan;
+    const int n_v = (int)W.desc.n_v;
+    for (int q = 0; q < 3; ++q) {
+        ga->theta = q;
+        CU(cudaMemsetAsync(tan, 0, sizeof(float) * (size_t)s.n_nodes * W.row_stride, st));
+        RG(launch_scatter_tangent(*ga, L->ctx->sms * 8, st));
+        ColFftArgs ca = col_args(W, s);
+        ca.src = tan;
+        ca.y = W.y;
+        RG(launch_col_fft_fwd_f(ca, st));
+        CU(cudaMemsetAsync(W.g, 0, sizeof(float2) * (size_t)W.n, st));
+        RG(launch_row_fft_voigt(*va, st));
+        RowIfftArgs ra;
+        ra.f2 = W.f2;
+        ra.n1 = W.n1;
+        ra.n2 = W.n2;
+        ra.n = W.n;
+        ra.g = W.g;
+        ra.tw_hi = W.tw_hi;
+        ra.tw_lo = W.tw_lo;
+        RG(launch_row_ifft(ra, st));
+        ca.h = W.g;
+        ca.out = out + (size_t)q * n_v;
+        ca.out_scale = (float)(std::exp(s.log_scale_int - s.log_scale_out) / ((double)W.n * W.desc.dv));
+        RG(launch_col_ifft(ca, st));
+    }
+    return RG_OK;
+}
+
+// The plan's workspace is shared by everything enqueued on it: order work on
+// a new stream after the plan's previous work (begin) and mark the end (end).
+int plan_stream_begin(rg_plan* P, cudaStream_t st) {
+    if (!P->done) CU(cudaEventCreateWithFlags(&P->done, cudaEventDisableTiming));
+    if (P->any && st != P->last_stream) CU(cudaStreamWaitEvent(st, P->done, 0));
+    return RG_OK;
+}
+int plan_stream_end(rg_plan* P, cudaStream_t st) {
+    CU(cudaEventRecord(P->done, st));
+    P->last_stream = st;
+    P->any = true;
+    return RG_OK;
+}
+
 int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st, int timing, bool ldm_only,
                  rg_spectrum_info* info) {
     SpecHost s;
@@ -659,7 +813,9 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
             if (!e) CU(cudaEventCreate(&e));
         ev = P->ev;
     }
+    RG(plan_stream_begin(P, st));
     RG(enqueue_spectrum(P->lines, P->w, c, s, out, st, ev, ldm_only));
+    RG(plan_stream_end(P, st));
     if (info) {
         std::memset(info, 0, sizeof *info);
         info->grid = s.grid;
@@ -961,10 +1117,12 @@ int rg_plan_free(rg_plan* P) {
         dfree(P->tw_lo_own);
         free_work(P->w);
         dfree(P->out_d);
+        dfree(P->grad_d);
         for (auto& e : P->ev)
             if (e) cudaEventDestroy(e);
         for (auto& e : P->ring)
             if (e) cudaEventDestroy(e);
+        if (P->done) cudaEventDestroy(P->done);
         P->lines->plans--;
         P->magic = 0;
     }
@@ -1067,6 +1225,54 @@ int rg_debug_ldm(rg_plan* P, const rg_conditions* c, float* ldm_host, int64_t ca
     const float inv = 1.f / fx_scale_of((int)P->w.cmax_host);
     unsigned* w = reinterpret_cast<unsigned*>(ldm_host);
     for (int64_t i = 0; i < (int64_t)nodes * nv; ++i) ldm_host[i] = (float)w[i] * inv;
+    return RG_OK;
+}
+
+int rg_backward(rg_plan* P, const rg_conditions* c, const double* dlnq_dT, const float* grad_out_dev,
+                double grad[3], void* stream, rg_spectrum_info* info) {
+    g_err.clear();
+    if (!valid(P) || !c || !grad_out_dev || !grad) return fail(RG_ERR_ARG, "invalid argument");
+    std::lock_guard<std::mutex> lk(P->mu);
+    CU(cudaSetDevice(P->lines->ctx->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
+    SpecHost s;
+    RG(compute_grid(P->lines, P->w, c, &s));
+    if (!P->grad_d) CU(cudaMalloc((void**)&P->grad_d, 3 * sizeof(double)));
+    RG(plan_stream_begin(P, st));
+    RG(enqueue_backward(P->lines, P->w, c, s, dlnq_dT, grad_out_dev, P->grad_d, st));
+    RG(plan_stream_end(P, st));
+    double h[3];
+    CU(cudaMemcpyAsync(h, P->grad_d, sizeof h, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    const double sc = std::exp(s.log_scale_int);
+    for (int q = 0; q < 3; ++q) grad[q] = h[q] * sc;
+    if (info) {
+        std::memset(info, 0, sizeof *info);
+        info->grid = s.grid;
+        info->log_scale = 0.0;
+        info->lines_in_window = -1;
+    }
+    return RG_OK;
+}
+
+int rg_jvp(rg_plan* P, const rg_conditions* c, const double* dlnq_dT, float* out_dev, void* stream,
+           rg_spectrum_info* info) {
+    g_err.clear();
+    if (!valid(P) || !c || !out_dev) return fail(RG_ERR_ARG, "invalid argument");
+    std::lock_guard<std::mutex> lk(P->mu);
+    CU(cudaSetDevice(P->lines->ctx->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
+    SpecHost s;
+    RG(compute_grid(P->lines, P->w, c, &s));
+    RG(plan_stream_begin(P, st));
+    RG(enqueue_tangent(P->lines, P->w, c, s, dlnq_dT, out_dev, st));
+    RG(plan_stream_end(P, st));
+    if (info) {
+        std::memset(info, 0, sizeof *info);
+        info->grid = s.grid;
+        info->log_scale = s.log_scale_out;
+        info->lines_in_window = -1;
+    }
     return RG_OK;
 }
 

@@ -140,6 +140,9 @@ struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
     const float2* h;      // K4 input [n1][n2]
     float* out;           // K4 output (n_v)
     float out_scale;
+    // float-row variants (tangent and adjoint paths)
+    const float* src;     // K2 input rows [node][row_stride] (float), or one row when single
+    int single;           // K2: one real row (partner row zero), n_pairs = 1
 };
 
 struct VoigtArgs {        // K3 (row FFT + Voigt weights + pair reduction)
@@ -174,6 +177,27 @@ struct RowIfftArgs {      // K3b (inverse row FFT + twiddle, in place)
     const float2* tw_lo;
 };
 
+struct AdjRowArgs {       // adjoint row stage: per pair, IFFT_row(Ghat (V_a + i V_b)) x twiddle
+    VoigtArgs v;          // v.g holds Ghat [n1][n2] (FFT of the upstream gradient)
+    float2* y;            // output [pair][n1][n2]
+};
+
+struct GradArgs {         // adjoint gather (reverse mode) and tangent scatter (forward mode)
+    ScatterArgs s;        // per-line coefficients at the conditions (fixed point unused)
+    int64_t n_lines;
+    const float* adj;     // gather input: adjoint LDM rows [node][row_stride]
+    float* tan;           // tangent output: LDM rows [node][row_stride], zeroed
+    int64_t row_stride;
+    int theta;            // tangent direction: 0 = T, 1 = p_bar, 2 = x
+    float c2_T, c2_T2;    // c2 / T, c2 / T^2
+    float cT0[kMaxIso];   // d ln(Qref/Q)/dT - 1/T (partition ratio and number density)
+    float gT;             // d(log-wG node coordinate)/dT = 0.5 / (T dxG)
+    float lT, lP, lX;     // 1/(T dxL), 1/(p_bar dxL), 1/dxL
+    float kP;             // d(grid position)/d(p_bar) per unit shift = 1 / (1.01325 dv)
+    float iP, iX;         // 1/p_bar, 1/x
+    double* out;          // gather output: d/dT, d/dp_bar, d/dx sums, zeroed
+};
+
 // Fixed-point scale of the scatter accumulator: 2^e with (cmax + 1) 2^e <= 2^31.
 RG_HD inline float fx_scale_of(int cmax) {
     int bits = 0;
@@ -198,6 +222,12 @@ int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st);
 int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st);
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st);
 int launch_col_ifft(const ColFftArgs& a, cudaStream_t st);
+// tangent / adjoint path (forward-mode and reverse-mode derivatives)
+int launch_col_fft_fwd_f(const ColFftArgs& a, cudaStream_t st);
+int launch_row_ifft_adj(const AdjRowArgs& a, cudaStream_t st);
+int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st);
+int launch_gather_grad(const GradArgs& a, int grid, cudaStream_t st);
+int launch_scatter_tangent(const GradArgs& a, int grid, cudaStream_t st);
 int col_block(int n1);               // columns per CTA of the column FFTs
 int row_threads(const FftLen& f);    // block size of the forward row kernel
 void row_voigt_layout(int n2, int* pairs, int* with_twr);

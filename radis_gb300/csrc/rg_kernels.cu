@@ -419,6 +419,50 @@ __device__ __forceinline__ void issue_chunk(const ScatterArgs& a, unsigned char*
     if (a.iso) tma_load_1d(base + 32 * ch, a.iso + start, cp, bar);
 }
 
+// --- per-line quantities at the conditions of a ScatterArgs -----------------
+// (shared by the scatter, the tangent scatter and the adjoint gather)
+
+// Fractional grid position of the (pressure-shifted) line centre, in
+// double-float: ((hi - vmin_hi) + (lo - vmin_lo + shift)) / dv = fk + tv,
+// fk integral, tv in [0, 1).
+__device__ __forceinline__ void line_position(const ScatterArgs& a, float2 v, float dl, float& fk, float& tv) {
+    float s, e1;
+    two_sum(v.x, -a.vmin_hi, s, e1);
+    e1 += (v.y - a.vmin_lo) + dl * a.p_atm;
+    const float p = s * a.inv_dv_hi;
+    const float pe = fmaf(s, a.inv_dv_hi, -p) + fmaf(s, a.inv_dv_lo, e1 * a.inv_dv_hi);
+    fk = floorf(p);
+    tv = (p - fk) + pe;
+    const float fl = floorf(tv);
+    fk += fl;
+    tv -= fl;
+}
+
+// Gaussian / Lorentzian node cell and fractions (FWHM, log space); log v0 is
+// taken relative to v_ref so the FP32 log and offset do not cancel.
+__device__ __forceinline__ void line_nodes(const ScatterArgs& a, float v0, float ga, float gs, float na, int is,
+                                           int& l0, int& m0, float& tG, float& tL) {
+    const float pl = fmaf(lg2(v0 * a.inv_vref), a.lgG_scale, a.cG[is]);
+    const float gam = fmaf(a.x_self, gs - ga, ga);
+    const float pm = fmaf(lg2(gam), a.lgL_scale, fmaf(na, a.tL, a.cL));
+    l0 = min(max((int)floorf(pl), 0), a.NG - 2);
+    m0 = min(max((int)floorf(pm), 0), a.NL - 2);
+    tG = pl - (float)l0;
+    tL = pm - (float)m0;
+}
+
+// Scaled intensity S(T) N x Qr exp(-log_scale): exponent log2(S') + a_T El +
+// b_iso in double-float, times the stimulated-emission factor.
+__device__ __forceinline__ float line_intensity(const ScatterArgs& a, float v0, float el, float ls2, int is) {
+    const float ph = el * a.aT_hi;
+    const float pe2 = fmaf(el, a.aT_hi, -ph) + el * a.aT_lo;
+    float s1, f1, s2, f2;
+    two_sum(ph, a.bI_hi[is], s1, f1);
+    two_sum(s1, ls2, s2, f2);
+    const float arg = s2 + (f1 + f2 + pe2 + a.bI_lo[is]);
+    return ex2(arg) * (1.f - ex2(-a.stim_c * v0));
+}
+
 // Scale + scatter of the lines of one staged chunk into the tile accumulator.
 __device__ __forceinline__ unsigned scatter_chunk(const ScatterArgs& a, const Stage& st, int count, int k_start,
                                                   int tk, unsigned* tile, float fxs) {
@@ -426,17 +470,8 @@ __device__ __forceinline__ unsigned scatter_chunk(const ScatterArgs& a, const St
     for (int j = threadIdx.x; j < count; j += blockDim.x) {
         const float2 v = st.v0[j];
         const float dl = st.dl ? st.dl[j] : 0.f;
-        // k position in double-float: ((hi - vmin_hi) + (lo - vmin_lo + shift)) / dv
-        float s, e1;
-        two_sum(v.x, -a.vmin_hi, s, e1);
-        e1 += (v.y - a.vmin_lo) + dl * a.p_atm;
-        const float p = s * a.inv_dv_hi;
-        const float pe = fmaf(s, a.inv_dv_hi, -p) + fmaf(s, a.inv_dv_lo, e1 * a.inv_dv_hi);
-        float fk = floorf(p);
-        float tv = (p - fk) + pe;
-        const float fl = floorf(tv);
-        fk += fl;
-        tv -= fl;
+        float fk, tv;
+        line_position(a, v, dl, fk, tv);
         if (!(fk >= 0.f) || fk + 1.f >= (float)a.n_v) continue;   // drop (cmdFillLDM.comp:102)
         const int k0 = (int)fk;
         const int c0 = k0 - k_start;
@@ -445,25 +480,10 @@ __device__ __forceinline__ unsigned scatter_chunk(const ScatterArgs& a, const St
         if (!(own0 || own1)) continue;
         if (own0) ++counted;
         const int is = st.iso ? (int)st.iso[j] : 0;
-        // Gaussian / Lorentzian node coordinates (FWHM, log space); log v0 is
-        // taken relative to v_ref so the FP32 log and offset do not cancel
-        const float pl = fmaf(lg2(v.x * a.inv_vref), a.lgG_scale, a.cG[is]);
-        const float ga = st.ga[j];
-        const float gam = fmaf(a.x_self, st.gs[j] - ga, ga);
-        const float pm = fmaf(lg2(gam), a.lgL_scale, fmaf(st.na[j], a.tL, a.cL));
-        const int l0 = min(max((int)floorf(pl), 0), a.NG - 2);
-        const int m0 = min(max((int)floorf(pm), 0), a.NL - 2);
-        const float tG = pl - (float)l0;
-        const float tL = pm - (float)m0;
-        // intensity: exponent log2(S') + a_T El + b_iso in double-float
-        const float el = st.el[j];
-        const float ph = el * a.aT_hi;
-        const float pe2 = fmaf(el, a.aT_hi, -ph) + el * a.aT_lo;
-        float s1, f1, s2, f2;
-        two_sum(ph, a.bI_hi[is], s1, f1);
-        two_sum(s1, st.ls2[j], s2, f2);
-        const float arg = s2 + (f1 + f2 + pe2 + a.bI_lo[is]);
-        const float I = ex2(arg) * (1.f - ex2(-a.stim_c * v.x)) * fxs;
+        int l0, m0;
+        float tG, tL;
+        line_nodes(a, v.x, st.ga[j], st.gs[j], st.na[j], is, l0, m0, tG, tL);
+        const float I = line_intensity(a, v.x, st.el[j], st.ls2[j], is) * fxs;
         const float I1 = tv * I;
         const float I0 = I - I1;
         const float w11 = tG * tL;
@@ -921,6 +941,239 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_ifft(const ColFft
 }
 
 // ---------------------------------------------------------------------------
+// Derivatives with respect to (T, p, x), node axes held fixed.
+//
+// With the axes fixed the Voigt weights of the nodes are constants, so the
+// spectrum is a fixed linear map C of the LDM and only the LDM depends on
+// (T, p, x): dA/dtheta = C dLDM/dtheta.  Per line, the LDM holds
+// I w(tv, tG, tL) in 8 cells (trilinear weights of the three fractional
+// coordinates), so dLDM/dtheta is a scatter of
+//   I (dlnI/dtheta w + dw/dtv dtv/dtheta + dw/dtG dtG/dtheta + dw/dtL dtL/dtheta).
+// Forward mode (tangent): scatter that into a float LDM and run it through C
+// (the ordinary FFT / Voigt / inverse FFT kernels).
+// Reverse mode (adjoint): C restricted to one node is a symmetric circular
+// convolution (V is real and even), so C^T g for node n is the same
+// convolution of the upstream gradient g: Re(IFFT(FFT(g) V_n)) / (N dv).  The
+// adjoint LDM for all nodes comes from one forward FFT of g and one inverse
+// FFT per node pair (k_row_ifft_adj, k_col_ifft_adj; V_a + i V_b puts node a
+// in the real and node b in the imaginary part), and the per-line chain rule
+// gathers it back at each line's 8 cells (k_gather_grad).
+// ---------------------------------------------------------------------------
+
+// K2 on float rows: rows 2 pair and 2 pair + 1 of a.src, or (a.single) the
+// single row a.src with a zero partner.
+template <int N1>
+__global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_fft_fwd_f(const ColFftArgs a) {
+    constexpr int TPC = ColShape<N1>::TPC;
+    constexpr int B = ColShape<N1>::B;
+    extern __shared__ float2 sm[];
+    const int b = threadIdx.x % B;
+    const int j = threadIdx.x / B;
+    const int pair = blockIdx.y;
+    const float* ra = a.src + (a.single ? 0 : (int64_t)(2 * pair) * a.row_stride);
+    const float* rb = a.single ? nullptr : ra + a.row_stride;
+    const int n2i = blockIdx.x * B + b;
+    float2 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int64_t nidx = (int64_t)(j + q * TPC) * a.n2 + n2i;
+        v[q] = nidx < a.n_v ? make_float2(__ldg(&ra[nidx]), rb ? __ldg(&rb[nidx]) : 0.f) : make_float2(0.f, 0.f);
+    }
+    col_fft8<N1>(v, sm, j, b, a.f1.tw);
+    float2* y = a.y + (int64_t)pair * N1 * a.n2;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) y[(j + r * TPC) * a.n2 + n2i] = v[r];
+}
+
+// Adjoint row stage, one CTA per (row k1, pair j): H = Ghat (V_2j + i V_2j+1)
+// on the row's bins k = k1 + n1 t, inverse row DFT, inverse four-step twiddle
+// w_N^{-t k1}; output y[j][k1][t].
+__global__ void __launch_bounds__(kRowThreads) k_row_ifft_adj(const AdjRowArgs a) {
+    extern __shared__ float2 sm[];
+    const VoigtArgs& v = a.v;
+    const int n2 = v.n2;
+    float2* buf0 = sm;
+    float2* buf1 = sm + row_buf_len(n2);
+    const int k1 = blockIdx.x;
+    const int j = blockIdx.y;
+    const int n = (int)v.n;
+    const NodeV A = node_params(v, 2 * j), B = node_params(v, 2 * j + 1);
+    const float2* gh = v.g + (int64_t)k1 * n2;
+    for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+        const int kk = k1 + v.n1 * t;
+        const float f = (float)min(kk, n - kk) * v.inv_ndv;
+        const float va = voigt_eval(A, f, v.half_fs);
+        const float vb = voigt_eval(B, f, v.half_fs);
+        const float2 z = gh[t];
+        // inverse DFT = conj(forward DFT(conj(x)))
+        buf0[t] = make_float2(z.x * va - z.y * vb, -(z.y * va + z.x * vb));
+    }
+    __syncthreads();
+    bool padded;
+    const float2* res = fft_row(buf0, buf1, v.f2, &padded);
+    float2* y = a.y + ((int64_t)j * v.n1 + k1) * n2;
+    for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+        float2 z = conjf2(res[padded ? rp(t) : t]);
+        if (k1 && t) z = cmul(z, conjf2(twiddle_n(v.tw_hi, v.tw_lo, t * k1)));
+        y[t] = z;
+    }
+}
+
+// Adjoint column stage: inverse column DFT (length n1) of pair `blockIdx.y`;
+// real part -> float row 2 pair, imaginary part -> row 2 pair + 1 of a.out
+// (first n_v samples, x out_scale).
+template <int N1>
+__global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_ifft_adj(const ColFftArgs a) {
+    constexpr int TPC = ColShape<N1>::TPC;
+    constexpr int B = ColShape<N1>::B;
+    extern __shared__ float2 sm[];
+    const int b = threadIdx.x % B;
+    const int j = threadIdx.x / B;
+    const int pair = blockIdx.y;
+    const int n2i = blockIdx.x * B + b;
+    const float2* h = a.h + (int64_t)pair * N1 * a.n2;
+    float2 v[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) v[q] = conjf2(h[(int64_t)(j + q * TPC) * a.n2 + n2i]);
+    col_fft8<N1>(v, sm, j, b, a.f1.tw);
+    float* oa = a.out + (int64_t)(2 * pair) * a.row_stride;
+    float* ob = oa + a.row_stride;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        const int64_t nidx = (int64_t)(j + r * TPC) * a.n2 + n2i;
+        if (nidx < a.n_v) {
+            oa[nidx] = v[r].x * a.out_scale;     // Re(conj(z))
+            ob[nidx] = -v[r].y * a.out_scale;    // Im(conj(z))
+        }
+    }
+}
+
+// Per-line derivative coefficients: dlnI/dtheta and the rates of the three
+// fractional coordinates, for theta = T, p_bar, x (radis/lbl/base.py:2664-2677
+// for I, broadening.py:170-172 and 368-381 for the widths, base.py:2351-2370
+// for the shift; number density p x / (k T)).
+struct LineRates {
+    float lnI[3], tv[3], tG[3], tL[3];
+};
+
+__device__ __forceinline__ LineRates line_rates(const GradArgs& g, float v0, float el, float ga, float gs, float na,
+                                                float dl, int is) {
+    LineRates r;
+    const float x = g.c2_T * v0;
+    // d/dT of ln(exp(-c2 El/T) (1 - exp(-c2 v0/T))), partition ratio and density
+    r.lnI[0] = g.c2_T2 * el - g.c2_T2 * v0 / expm1f(x) + g.cT0[is];
+    r.lnI[1] = g.iP;
+    r.lnI[2] = g.iX;
+    r.tv[0] = 0.f;
+    r.tv[1] = dl * g.kP;
+    r.tv[2] = 0.f;
+    r.tG[0] = g.gT;
+    r.tG[1] = 0.f;
+    r.tG[2] = 0.f;
+    const float gam = fmaf(g.s.x_self, gs - ga, ga);
+    r.tL[0] = -na * g.lT;
+    r.tL[1] = g.lP;
+    r.tL[2] = (gs - ga) / gam * g.lX;
+    return r;
+}
+
+// Reverse mode: out[theta] += sum over lines of I (dlnI S0 + dtv Sk + dtG SG +
+// dtL SL), with S0 the adjoint LDM interpolated at the line and Sk, SG, SL its
+// differences along the three cell axes.  One FP64 atomic per block and theta.
+__global__ void __launch_bounds__(256) k_gather_grad(const GradArgs g) {
+    const ScatterArgs& a = g.s;
+    float acc[3] = {0.f, 0.f, 0.f};
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < g.n_lines; i += stride) {
+        const float2 v = a.v0[i];
+        const float dl = a.dl ? a.dl[i] : 0.f;
+        float fk, tv;
+        line_position(a, v, dl, fk, tv);
+        if (!(fk >= 0.f) || fk + 1.f >= (float)a.n_v) continue;
+        const int k0 = (int)fk;
+        const int is = a.iso ? (int)a.iso[i] : 0;
+        const float ga = a.ga[i], gs = a.gs[i], na = a.na[i], el = a.el[i];
+        int l0, m0;
+        float tG, tL;
+        line_nodes(a, v.x, ga, gs, na, is, l0, m0, tG, tL);
+        const float I = line_intensity(a, v.x, el, a.ls2[i], is);
+        if (!(I > 0.f)) continue;
+        const float* r00 = g.adj + (int64_t)(l0 * a.NL + m0) * g.row_stride + k0;
+        const float* r01 = r00 + g.row_stride;
+        const float* r10 = r00 + (int64_t)a.NL * g.row_stride;
+        const float* r11 = r10 + g.row_stride;
+        const float d00 = r00[1] - r00[0], d01 = r01[1] - r01[0];
+        const float d10 = r10[1] - r10[0], d11 = r11[1] - r11[0];
+        const float e00 = fmaf(tv, d00, r00[0]), e01 = fmaf(tv, d01, r01[0]);
+        const float e10 = fmaf(tv, d10, r10[0]), e11 = fmaf(tv, d11, r11[0]);
+        const float uG = 1.f - tG, uL = 1.f - tL;
+        const float S0 = uG * (uL * e00 + tL * e01) + tG * (uL * e10 + tL * e11);
+        const float Sk = uG * (uL * d00 + tL * d01) + tG * (uL * d10 + tL * d11);
+        const float SG = uL * (e10 - e00) + tL * (e11 - e01);
+        const float SL = uG * (e01 - e00) + tG * (e11 - e10);
+        const LineRates r = line_rates(g, v.x, el, ga, gs, na, dl, is);
+#pragma unroll
+        for (int q = 0; q < 3; ++q) acc[q] += I * (r.lnI[q] * S0 + r.tv[q] * Sk + r.tG[q] * SG + r.tL[q] * SL);
+    }
+    __shared__ double part[3][8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        double s = acc[q];
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) part[q][warp] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += part[threadIdx.x][w];
+        atomicAdd(&g.out[threadIdx.x], s);
+    }
+}
+
+// Forward mode: scatter the tangent of each line's 8 LDM values in direction
+// g.theta into the float rows g.tan (FP32 global atomics).
+__global__ void __launch_bounds__(256) k_scatter_tangent(const GradArgs g) {
+    const ScatterArgs& a = g.s;
+    const int th = g.theta;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < g.n_lines; i += stride) {
+        const float2 v = a.v0[i];
+        const float dl = a.dl ? a.dl[i] : 0.f;
+        float fk, tv;
+        line_position(a, v, dl, fk, tv);
+        if (!(fk >= 0.f) || fk + 1.f >= (float)a.n_v) continue;
+        const int k0 = (int)fk;
+        const int is = a.iso ? (int)a.iso[i] : 0;
+        const float ga = a.ga[i], gs = a.gs[i], na = a.na[i], el = a.el[i];
+        int l0, m0;
+        float tG, tL;
+        line_nodes(a, v.x, ga, gs, na, is, l0, m0, tG, tL);
+        const float I = line_intensity(a, v.x, el, a.ls2[i], is);
+        if (!(I > 0.f)) continue;
+        const LineRates r = line_rates(g, v.x, el, ga, gs, na, dl, is);
+        const float K[2] = {1.f - tv, tv}, dK[2] = {-r.tv[th], r.tv[th]};
+        const float Gw[2] = {1.f - tG, tG}, dG[2] = {-r.tG[th], r.tG[th]};
+        const float Lw[2] = {1.f - tL, tL}, dL[2] = {-r.tL[th], r.tL[th]};
+        const float ln = r.lnI[th];
+#pragma unroll
+        for (int cl = 0; cl < 2; ++cl)
+#pragma unroll
+            for (int cm = 0; cm < 2; ++cm) {
+                float* row = g.tan + (int64_t)((l0 + cl) * a.NL + m0 + cm) * g.row_stride + k0;
+                const float gl = Gw[cl] * Lw[cm];
+                const float dgl = dG[cl] * Lw[cm] + Gw[cl] * dL[cm];
+#pragma unroll
+                for (int ck = 0; ck < 2; ++ck) {
+                    const float w = K[ck] * gl;
+                    const float dw = dK[ck] * gl + K[ck] * dgl;
+                    atomicAdd(&row[ck], I * fmaf(ln, w, dw));
+                }
+            }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 static int check_launch() {
@@ -1086,6 +1339,60 @@ int launch_col_ifft(const ColFftArgs& a, cudaStream_t st) {
         case 512: return col_inv<512>(a, st);
         default: return RG_ERR_RANGE;
     }
+}
+
+template <int N1>
+static int col_fwd_f(const ColFftArgs& a, cudaStream_t st) {
+    ALLOW_SMEM(k_col_fft_fwd_f<N1>, N1 * ColShape<N1>::B * sizeof(float2));
+    dim3 grid(a.n2 / ColShape<N1>::B, a.single ? 1 : a.n_pairs);
+    k_col_fft_fwd_f<N1><<<grid, ColShape<N1>::THREADS, N1 * ColShape<N1>::B * sizeof(float2), st>>>(a);
+    return check_launch();
+}
+
+int launch_col_fft_fwd_f(const ColFftArgs& a, cudaStream_t st) {
+    switch (a.n1) {
+        case 8: return col_fwd_f<8>(a, st);
+        case 64: return col_fwd_f<64>(a, st);
+        case 512: return col_fwd_f<512>(a, st);
+        default: return RG_ERR_RANGE;
+    }
+}
+
+int launch_row_ifft_adj(const AdjRowArgs& a, cudaStream_t st) {
+    const size_t smem = 2 * (size_t)row_buf_len(a.v.n2) * sizeof(float2);
+    ALLOW_SMEM(k_row_ifft_adj, smem);
+    dim3 grid(a.v.n1, a.v.n_pairs);
+    k_row_ifft_adj<<<grid, kRowThreads, smem, st>>>(a);
+    return check_launch();
+}
+
+template <int N1>
+static int col_inv_adj(const ColFftArgs& a, cudaStream_t st) {
+    ALLOW_SMEM(k_col_ifft_adj<N1>, N1 * ColShape<N1>::B * sizeof(float2));
+    dim3 grid(a.n2 / ColShape<N1>::B, a.n_pairs);
+    k_col_ifft_adj<N1><<<grid, ColShape<N1>::THREADS, N1 * ColShape<N1>::B * sizeof(float2), st>>>(a);
+    return check_launch();
+}
+
+int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st) {
+    switch (a.n1) {
+        case 8: return col_inv_adj<8>(a, st);
+        case 64: return col_inv_adj<64>(a, st);
+        case 512: return col_inv_adj<512>(a, st);
+        default: return RG_ERR_RANGE;
+    }
+}
+
+int launch_gather_grad(const GradArgs& a, int grid, cudaStream_t st) {
+    if (a.n_lines <= 0) return RG_OK;
+    k_gather_grad<<<grid, 256, 0, st>>>(a);
+    return check_launch();
+}
+
+int launch_scatter_tangent(const GradArgs& a, int grid, cudaStream_t st) {
+    if (a.n_lines <= 0) return RG_OK;
+    k_scatter_tangent<<<grid, 256, 0, st>>>(a);
+    return check_launch();
 }
 
 }  // namespace rg
