@@ -536,7 +536,7 @@ void fill_voigt_args(const Work& W, const SpecHost& s, VoigtArgs* va) {
     const rg_grid& g = s.grid;
     va->f2 = W.f2;
     va->threads = row_threads(W.f2);
-    row_voigt_layout(W.n2, &va->pairs_per_pass, &va->row_twiddle_table);
+    row_layout(W.n2, &va->pairs_per_pass, &va->row_twiddle_table);
     va->n1 = W.n1;
     va->n2 = W.n2;
     va->n = W.n;
@@ -617,6 +617,9 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
         ca.n_pairs = s.n_nodes / 2;
         ca.ldm = W.ldm;
         ca.cmax = W.cmax_dev;
+        int pairs_unused, twr;
+        row_layout(W.n2, &pairs_unused, &twr);
+        ca.twiddle = !twr;
         ca.y = W.y;
         ca.tw_hi = W.tw_hi;
         ca.tw_lo = W.tw_lo;
@@ -687,6 +690,9 @@ ColFftArgs col_args(const Work& W, const SpecHost& s) {
     ca.n_pairs = s.n_nodes / 2;
     ca.tw_hi = W.tw_hi;
     ca.tw_lo = W.tw_lo;
+    int pairs_unused, twr;
+    row_layout(W.n2, &pairs_unused, &twr);
+    ca.twiddle = !twr;
     return ca;
 }
 

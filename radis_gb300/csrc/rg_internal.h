@@ -143,13 +143,15 @@ struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
     // float-row variants (tangent and adjoint paths)
     const float* src;     // K2 input rows [node][row_stride] (float), or one row when single
     int single;           // K2: one real row (partner row zero), n_pairs = 1
+    int twiddle;          // K2: apply the four-step twiddle (row kernel without table)
 };
 
 struct VoigtArgs {        // K3 (row FFT + Voigt weights + pair reduction)
     FftLen f2;
-    int threads;          // block size (row_threads)
+    int threads;          // block size (row_threads), >= n2 / 8
     int pairs_per_pass;   // 2: two pairs as float4 elements; 1: one pair (long rows)
-    int row_twiddle_table;// 1: per-row four-step twiddle table in shared memory
+    int row_twiddle_table;// 1: the row kernel applies the four-step twiddle from a
+                          // per-row shared table; 0: the column stage applies it
     int n1, n2;
     int64_t n;
     int n_pairs;
@@ -230,7 +232,7 @@ int launch_gather_grad(const GradArgs& a, int grid, cudaStream_t st);
 int launch_scatter_tangent(const GradArgs& a, int grid, cudaStream_t st);
 int col_block(int n1);               // columns per CTA of the column FFTs
 int row_threads(const FftLen& f);    // block size of the forward row kernel
-void row_voigt_layout(int n2, int* pairs, int* with_twr);
+void row_layout(int n2, int* pairs, int* with_twr);   // forward row kernel layout
 size_t scatter_smem_floats(int n_nodes, int TK);
 
 }  // namespace rg

@@ -616,8 +616,29 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
 // ---------------------------------------------------------------------------
 // K2: forward column FFT (length n1) of packed node pairs
 // ---------------------------------------------------------------------------
+// Column-stage output X[k1] of column n2i into y[pair][k1][n2i], times the
+// four-step twiddle w_N^{n2i k1} when the row stage does not apply it
+// (a.twiddle): w for k1 = j + r N1/8 is w_N^{n2i j} (w_N^{n2i N1/8})^r, two
+// table reads and a product recurrence (rounding grows to ~8 ulp at r = 7).
 template <int N1>
-__global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_fft_fwd(const ColFftArgs a) {
+__device__ __forceinline__ void store_twiddled(float2 (&v)[8], const ColFftArgs& a, int pair, int j, int n2i) {
+    constexpr int TPC = ColShape<N1>::TPC;
+    float2* y = a.y + (int64_t)pair * N1 * a.n2;
+    if (a.twiddle) {
+        float2 w = twiddle_n(a.tw_hi, a.tw_lo, n2i * j);
+        const float2 step = twiddle_n(a.tw_hi, a.tw_lo, n2i * TPC);
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+            v[r] = cmul(v[r], w);
+            w = cmul(w, step);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < 8; ++r) y[(int64_t)(j + r * TPC) * a.n2 + n2i] = v[r];
+}
+
+template <int N1>
+__global__ void __launch_bounds__(ColShape<N1>::THREADS, 3) k_col_fft_fwd(const ColFftArgs a) {
     constexpr int TPC = ColShape<N1>::TPC;
     constexpr int B = ColShape<N1>::B;
     extern __shared__ float2 sm[];
@@ -638,17 +659,13 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_fft_fwd(const Col
                             : make_float2(0.f, 0.f);
     }
     col_fft8<N1>(v, sm, j, b, a.f1.tw);
-    // the four-step twiddle w_N^{n2 k1} is applied by the row kernel
-    float2* y = a.y + (int64_t)pair * N1 * a.n2;
-#pragma unroll
-    for (int r = 0; r < 8; ++r) y[(j + r * TPC) * a.n2 + n2i] = v[r];
+    store_twiddled<N1>(v, a, pair, j, n2i);
 }
 
 // ---------------------------------------------------------------------------
 // K3: row FFT (length n2) of each pair, Voigt-FT weights, sum over pairs
 // ---------------------------------------------------------------------------
 constexpr int kRowThreads = 256;      // inverse row kernel
-constexpr int kRowMaxThreads = 384;   // forward row kernel (per-plan count, see row_threads)
 
 struct NodeV {
     float al, bm, nrm;
@@ -733,22 +750,24 @@ __device__ __forceinline__ void twiddleP(float2* A, float2* B, const float2* __r
     }
 }
 
-// first pass (sub-transform length 1): global rows x four-step twiddle ->
-// registers -> smem.  twr: per-row twiddle table in smem, or nullptr to use
-// the global two-level table.
+// first pass (sub-transform length 1): global rows -> (x four-step twiddle
+// from the per-row table twr, when TWR; otherwise the column stage applied
+// it) -> registers -> smem
 template <int R, int PAIRS, bool TWR>
 __device__ __forceinline__ void row_first(const float2* __restrict__ ya, const float2* __restrict__ yb,
-                                          const float2* twr, const VoigtArgs& a, int k1,
-                                          typename RowT<PAIRS>::E* out, int L) {
+                                          const float2* twr, typename RowT<PAIRS>::E* out, int L) {
     const int M = L / R;
     for (int j = threadIdx.x; j < M; j += blockDim.x) {
         float2 A[R], B[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-            const int i = j + r * M;
-            const float2 w = TWR ? twr[i] : ((k1 && i) ? twiddle_n(a.tw_hi, a.tw_lo, k1 * i) : make_float2(1.f, 0.f));
-            A[r] = cmul(__ldg(&ya[i]), w);
-            if (PAIRS == 2) B[r] = yb ? cmul(__ldg(&yb[i]), w) : make_float2(0.f, 0.f);
+            A[r] = __ldg(&ya[j + r * M]);
+            if (PAIRS == 2) B[r] = yb ? __ldg(&yb[j + r * M]) : make_float2(0.f, 0.f);
+            if (TWR) {
+                const float2 w = twr[j + r * M];
+                A[r] = cmul(A[r], w);
+                if (PAIRS == 2) B[r] = cmul(B[r], w);
+            }
         }
         dftR<R>(A);
         if (PAIRS == 2) dftR<R>(B);
@@ -784,9 +803,14 @@ __host__ __device__ inline size_t row_voigt_smem(int n2, bool with_twr) {
            (with_twr ? (size_t)n2 * sizeof(float2) : 0);
 }
 
-// IT = iterations of the last (radix-8) pass per thread: IT * blockDim * 8 >= n2
-template <int IT, int PAIRS, bool TWR>
-__global__ void __launch_bounds__(kRowMaxThreads, IT == 1 ? 2 : 1) k_row_fft_voigt(const VoigtArgs a) {
+// Layouts of the forward row kernel: MAXT threads at most, and the block is
+// at least the n2/8 butterflies of the last (radix-8) pass, so each thread
+// owns one butterfly's 8 output bins and their accumulators.
+constexpr int kRowMaxT2 = 384;    // PAIRS = 2, two CTAs per SM (n2 <= 3072)
+constexpr int kRowMaxT1 = 1024;   // PAIRS = 1, long rows (n2 <= 8192)
+
+template <int PAIRS, int MAXT, bool TWR>
+__global__ void __launch_bounds__(MAXT, PAIRS == 2 ? 2 : 1) k_row_fft_voigt(const VoigtArgs a) {
     using E = typename RowT<PAIRS>::E;
     extern __shared__ float4 sm4[];
     const int n2 = a.n2;
@@ -795,39 +819,29 @@ __global__ void __launch_bounds__(kRowMaxThreads, IT == 1 ? 2 : 1) k_row_fft_voi
     E* buf1 = buf0 + len;
     float2* twr = TWR ? reinterpret_cast<float2*>(buf1 + len) : nullptr;
     const int k1 = blockIdx.x;
+    if (TWR)
+        for (int t = threadIdx.x; t < n2; t += blockDim.x) twr[t] = twiddle_n(a.tw_hi, a.tw_lo, k1 * t);
     const int n = (int)a.n;
     const int j0 = blockIdx.y * kPairGroup;
     const int j1 = min(j0 + kPairGroup, a.n_pairs);
     const FftLen& P = a.f2;
     const int ML = n2 / 8;    // butterflies of the last pass (radix 8, sub-length ML)
-    if (TWR)
-        for (int t = threadIdx.x; t < n2; t += blockDim.x)
-            twr[t] = (k1 && t) ? twiddle_n(a.tw_hi, a.tw_lo, k1 * t) : make_float2(1.f, 0.f);
-    // frequencies of the bins this thread owns in the last pass: t = jl + r ML
-    float fb[IT * 8];
-    float2 acc[IT * 8];
+    const int jl = threadIdx.x;
+    float2 acc[8];
 #pragma unroll
-    for (int it = 0; it < IT; ++it) {
-        const int jl = threadIdx.x + it * blockDim.x;
-#pragma unroll
-        for (int r = 0; r < 8; ++r) {
-            const int kk = k1 + a.n1 * (jl + r * ML);
-            fb[it * 8 + r] = jl < ML ? (float)min(kk, n - kk) * a.inv_ndv : 0.f;
-            acc[it * 8 + r] = make_float2(0.f, 0.f);
-        }
-    }
-    __syncthreads();
+    for (int r = 0; r < 8; ++r) acc[r] = make_float2(0.f, 0.f);
 
     for (int j = j0; j < j1; j += PAIRS) {
         const bool two = PAIRS == 2 && j + 1 < j1;
         const float2* ya = a.y + ((int64_t)j * a.n1 + k1) * n2;
         const float2* yb = two ? a.y + ((int64_t)(j + 1) * a.n1 + k1) * n2 : nullptr;
+        if (TWR && j == j0) __syncthreads();   // twr complete
         switch (P.radix[0]) {
-            case 2: row_first<2, PAIRS, TWR>(ya, yb, twr, a, k1, buf0, n2); break;
-            case 3: row_first<3, PAIRS, TWR>(ya, yb, twr, a, k1, buf0, n2); break;
-            case 4: row_first<4, PAIRS, TWR>(ya, yb, twr, a, k1, buf0, n2); break;
-            case 5: row_first<5, PAIRS, TWR>(ya, yb, twr, a, k1, buf0, n2); break;
-            default: row_first<8, PAIRS, TWR>(ya, yb, twr, a, k1, buf0, n2); break;
+            case 2: row_first<2, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
+            case 3: row_first<3, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
+            case 4: row_first<4, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
+            case 5: row_first<5, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
+            default: row_first<8, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
         }
         __syncthreads();
         E* in = buf0;
@@ -849,50 +863,46 @@ __global__ void __launch_bounds__(kRowMaxThreads, IT == 1 ? 2 : 1) k_row_fft_voi
         }
         // last pass (radix 8, sub-length ML, no shuffle: output t = jl + r ML),
         // Voigt weights and accumulation in registers
-        const NodeV A0 = node_params(a, 2 * j), A1 = node_params(a, 2 * j + 1);
-        NodeV B0 = A0, B1 = A1;
-        if (two) {
-            B0 = node_params(a, 2 * j + 2);
-            B1 = node_params(a, 2 * j + 3);
-        }
+        if (jl < ML) {
+            float2 A[8], B[8];
 #pragma unroll
-        for (int it = 0; it < IT; ++it) {
-            const int jl = threadIdx.x + it * blockDim.x;
-            if (jl < ML) {
-                float2 A[8], B[8];
+            for (int r = 0; r < 8; ++r) RowT<PAIRS>::split(in[RowT<PAIRS>::pad(jl + r * ML)], A[r], B[r]);
+            twiddleP<8, PAIRS>(A, B, P.tw, jl);   // w_{n2}^{r jl}
+            dft8(A);
+            if (PAIRS == 2) dft8(B);
+            const NodeV A0 = node_params(a, 2 * j), A1 = node_params(a, 2 * j + 1);
 #pragma unroll
-                for (int r = 0; r < 8; ++r) RowT<PAIRS>::split(in[RowT<PAIRS>::pad(jl + r * ML)], A[r], B[r]);
-                twiddleP<8, PAIRS>(A, B, P.tw, jl);   // w_{n2}^{r jl}
-                dft8(A);
-                if (PAIRS == 2) dft8(B);
+            for (int r = 0; r < 8; ++r) {
+                const int kk = k1 + a.n1 * (jl + r * ML);
+                const float f = (float)min(kk, n - kk) * a.inv_ndv;
+                const float va = voigt_eval(A0, f, a.half_fs);
+                const float vb = voigt_eval(A1, f, a.half_fs);
+                float2 c = acc[r];
+                c.x += A[r].x * va + A[r].y * vb;
+                c.y += A[r].y * va - A[r].x * vb;
+                acc[r] = c;
+            }
+            if (two) {
+                const NodeV B0 = node_params(a, 2 * j + 2), B1 = node_params(a, 2 * j + 3);
 #pragma unroll
                 for (int r = 0; r < 8; ++r) {
-                    const float f = fb[it * 8 + r];
-                    const float va = voigt_eval(A0, f, a.half_fs);
-                    const float vb = voigt_eval(A1, f, a.half_fs);
-                    float2 c = acc[it * 8 + r];
-                    c.x += A[r].x * va + A[r].y * vb;
-                    c.y += A[r].y * va - A[r].x * vb;
-                    if (two) {
-                        const float wa = voigt_eval(B0, f, a.half_fs);
-                        const float wb = voigt_eval(B1, f, a.half_fs);
-                        c.x += B[r].x * wa + B[r].y * wb;
-                        c.y += B[r].y * wa - B[r].x * wb;
-                    }
-                    acc[it * 8 + r] = c;
+                    const int kk = k1 + a.n1 * (jl + r * ML);
+                    const float f = (float)min(kk, n - kk) * a.inv_ndv;
+                    const float wa = voigt_eval(B0, f, a.half_fs);
+                    const float wb = voigt_eval(B1, f, a.half_fs);
+                    float2 c = acc[r];
+                    c.x += B[r].x * wa + B[r].y * wb;
+                    c.y += B[r].y * wa - B[r].x * wb;
+                    acc[r] = c;
                 }
             }
         }
         __syncthreads();
     }
-    float2* g = a.g + (int64_t)k1 * n2;
+    if (jl < ML) {
+        float2* g = a.g + (int64_t)k1 * n2;
 #pragma unroll
-    for (int it = 0; it < IT; ++it) {
-        const int jl = threadIdx.x + it * blockDim.x;
-        if (jl < ML) {
-#pragma unroll
-            for (int r = 0; r < 8; ++r) atomicAdd(&g[jl + r * ML], acc[it * 8 + r]);
-        }
+        for (int r = 0; r < 8; ++r) atomicAdd(&g[jl + r * ML], acc[r]);
     }
 }
 
@@ -980,9 +990,7 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_fft_fwd_f(const C
         v[q] = nidx < a.n_v ? make_float2(__ldg(&ra[nidx]), rb ? __ldg(&rb[nidx]) : 0.f) : make_float2(0.f, 0.f);
     }
     col_fft8<N1>(v, sm, j, b, a.f1.tw);
-    float2* y = a.y + (int64_t)pair * N1 * a.n2;
-#pragma unroll
-    for (int r = 0; r < 8; ++r) y[(j + r * TPC) * a.n2 + n2i] = v[r];
+    store_twiddled<N1>(v, a, pair, j, n2i);
 }
 
 // Adjoint row stage, one CTA per (row k1, pair j): H = Ghat (V_2j + i V_2j+1)
@@ -1276,46 +1284,32 @@ int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st) {
     }
 }
 
-template <int IT, int PAIRS, bool TWR>
+template <int PAIRS, int MAXT, bool TWR>
 static int row_voigt(const VoigtArgs& a, cudaStream_t st) {
     const size_t smem = row_voigt_smem<PAIRS>(a.n2, TWR);
-    ALLOW_SMEM((k_row_fft_voigt<IT, PAIRS, TWR>), smem);
+    ALLOW_SMEM((k_row_fft_voigt<PAIRS, MAXT, TWR>), smem);
     dim3 grid(a.n1, (a.n_pairs + kPairGroup - 1) / kPairGroup);
-    k_row_fft_voigt<IT, PAIRS, TWR><<<grid, a.threads, smem, st>>>(a);
+    k_row_fft_voigt<PAIRS, MAXT, TWR><<<grid, a.threads, smem, st>>>(a);
     return check_launch();
 }
 
-template <int PAIRS, bool TWR>
-static int row_voigt_it(const VoigtArgs& a, cudaStream_t st) {
-    const int per = (a.n2 / 8 + a.threads - 1) / a.threads;
-    if (per <= 1) return row_voigt<1, PAIRS, TWR>(a, st);
-    if (per <= 2) return row_voigt<2, PAIRS, TWR>(a, st);
-    if (per <= 4) return row_voigt<4, PAIRS, TWR>(a, st);
-    return RG_ERR_RANGE;
-}
-
-// Shared memory per CTA of the forward row kernel and its layout choice:
-// two pairs per pass when that fits two CTAs per SM, else one pair; the
-// per-row twiddle table only where it still fits.
-void row_voigt_layout(int n2, int* pairs, int* with_twr) {
-    const size_t two_ctas = 113 * 1024;
-    if (row_voigt_smem<2>(n2, true) <= two_ctas) {
-        *pairs = 2;
-        *with_twr = 1;
-    } else if (row_voigt_smem<1>(n2, true) <= two_ctas) {
-        *pairs = 1;
-        *with_twr = 1;
-    } else {
-        *pairs = 1;
-        *with_twr = 0;
-    }
+// Layout of the forward row kernel: two pairs per element (float4) while the
+// block limit of that layout covers the n2/8 last-pass butterflies, else one;
+// the per-row four-step twiddle table only with two pairs and while two CTAs
+// still fit an SM (otherwise the column stage applies the twiddle).
+void row_layout(int n2, int* pairs, int* with_twr) {
+    *pairs = n2 / 8 <= kRowMaxT2 ? 2 : 1;
+    *with_twr = *pairs == 2 && row_voigt_smem<2>(n2, true) <= 113 * 1024;
 }
 
 int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st) {
     if (a.f2.npass < 2 || a.f2.radix[a.f2.npass - 1] != 8) return RG_ERR_RANGE;
-    if (a.threads < 32 || a.threads > kRowMaxThreads || a.threads % 32) return RG_ERR_RANGE;
-    if (a.pairs_per_pass == 2) return row_voigt_it<2, true>(a, st);
-    return a.row_twiddle_table ? row_voigt_it<1, true>(a, st) : row_voigt_it<1, false>(a, st);
+    const int maxt = a.pairs_per_pass == 2 ? kRowMaxT2 : kRowMaxT1;
+    if (a.threads < a.n2 / 8 || a.threads > maxt || a.threads % 32) return RG_ERR_RANGE;
+    if (a.pairs_per_pass == 2)
+        return a.row_twiddle_table ? row_voigt<2, kRowMaxT2, true>(a, st) : row_voigt<2, kRowMaxT2, false>(a, st);
+    if (a.row_twiddle_table) return RG_ERR_RANGE;
+    return row_voigt<1, kRowMaxT1, false>(a, st);
 }
 
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st) {
@@ -1398,15 +1392,17 @@ int launch_scatter_tangent(const GradArgs& a, int grid, cudaStream_t st) {
 }  // namespace rg
 
 namespace rg {
-// Thread count of the forward row kernel for a row plan: the multiple of 32 in
-// [128, kRowMaxThreads] that wastes the fewest butterfly slots over the passes
-// (ties -> more threads).
+// Thread count of the forward row kernel for a row plan: the multiple of 32
+// in [max(128, n2/8), layout limit] that wastes the fewest butterfly slots
+// over the passes (ties -> fewer threads).
 int row_threads(const FftLen& f) {
-    // at most 4 last-pass (radix-8) butterflies per thread: T >= L / 32
-    const int t_min = std::max(128, (f.L / 32 + 31) / 32 * 32);
-    int best = std::max(256, t_min);
+    int pairs, twr;
+    row_layout(f.L, &pairs, &twr);
+    const int maxt = pairs == 2 ? kRowMaxT2 : kRowMaxT1;
+    const int t_min = std::max(128, (f.L / 8 + 31) / 32 * 32);
+    int best = t_min;
     double best_eff = -1.0;
-    for (int T = t_min; T <= kRowMaxThreads; T += 32) {
+    for (int T = t_min; T <= maxt; T += 32) {
         long slots = 0, work = 0;
         for (int p = 0; p < f.npass; ++p) {
             const int M = f.L / f.radix[p];
@@ -1414,7 +1410,7 @@ int row_threads(const FftLen& f) {
             work += M;
         }
         const double eff = (double)work / (double)slots;
-        if (eff > best_eff + 1e-9 || (eff > best_eff - 1e-9 && T > best)) {
+        if (eff > best_eff + 1e-9) {
             best_eff = eff;
             best = T;
         }
