@@ -562,6 +562,7 @@ void fill_voigt_args(const Work& W, const SpecHost& s, VoigtArgs* va) {
     for (int node = 0; node < s.n_nodes; ++node) {
         if (node >= g.n_G * g.n_L) {
             va->norm[node] = 0.f;
+            va->lnorm[node] = -std::numeric_limits<float>::infinity();
             va->nfold[node] = 0;
             continue;
         }
@@ -571,6 +572,7 @@ void fill_voigt_args(const Work& W, const SpecHost& s, VoigtArgs* va) {
         node_fold(W.desc.dv, std::exp(g.log_wG_min + l * g.dxG), std::exp(g.log_wL_min + m * g.dxL), thresh, &nf,
                   &nrm);
         va->norm[node] = (float)nrm;
+        va->lnorm[node] = (float)std::log2(nrm);
         va->nfold[node] = (unsigned char)nf;
         if (nf) va->any_fold = 1;
     }
@@ -725,6 +727,8 @@ int enqueue_backward(const rg_lines* L, Work& W, const rg_conditions* c, const S
     unit->beta[0] = unit->beta[1] = 0.f;
     unit->norm[0] = 1.f;
     unit->norm[1] = 0.f;
+    unit->lnorm[0] = 0.f;
+    unit->lnorm[1] = -std::numeric_limits<float>::infinity();
     unit->nfold[0] = unit->nfold[1] = 0;
     unit->any_fold = 0;
     CU(cudaMemsetAsync(W.g, 0, sizeof(float2) * (size_t)W.n, st));

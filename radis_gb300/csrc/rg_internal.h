@@ -166,6 +166,7 @@ struct VoigtArgs {        // K3 (row FFT + Voigt weights + pair reduction)
     float alpha[kMaxAxis];    // (pi wG_l)^2 / (4 ln 2) * log2e
     float beta[kMaxAxis];     // pi wL_m * log2e
     float norm[kMaxNodes];    // 1 / folded profile at f = 0 (0 for padding node)
+    float lnorm[kMaxNodes];   // log2(norm) (-inf for padding node)
     unsigned char nfold[kMaxNodes];
     int any_fold;
 };

@@ -700,6 +700,23 @@ __device__ __forceinline__ float voigt_eval(const NodeV& n, float f, float half_
     return v * n.nrm;
 }
 
+// Unfolded Voigt FT with the normalisation folded into the exponent:
+// nrm 2^-(al f^2 + bm f) = 2^(lnrm - bm f - al f^2), two FMAs and one ex2.
+struct NodeF {
+    float nal, nbm, lnrm;
+};
+__device__ __forceinline__ NodeF node_fast(const VoigtArgs& a, int node) {
+    const int l = node / a.NL;
+    NodeF n;
+    n.nal = -a.alpha[l];
+    n.nbm = -a.beta[node - l * a.NL];
+    n.lnrm = a.lnorm[node];
+    return n;
+}
+__device__ __forceinline__ float voigt_fast(const NodeF& n, float f, float f2) {
+    return ex2(fmaf(n.nal, f2, fmaf(n.nbm, f, n.lnrm)));
+}
+
 // PAIRS = 2: two pairs travel together through the row transform as float4
 // elements (row A in .xy, row B in .zw), sharing index arithmetic, twiddle
 // loads and shared-memory instructions; buffers use rp8(i) = i + i/8, which
@@ -797,10 +814,12 @@ __device__ __forceinline__ void row_mid(const typename RowT<PAIRS>::E* __restric
     }
 }
 
+// two work buffers, the optional twiddle table, and (two pairs) the staging
+// buffer of the next two rows
 template <int PAIRS>
 __host__ __device__ inline size_t row_voigt_smem(int n2, bool with_twr) {
     return 2 * (size_t)RowT<PAIRS>::len(n2) * sizeof(typename RowT<PAIRS>::E) +
-           (with_twr ? (size_t)n2 * sizeof(float2) : 0);
+           (with_twr ? (size_t)n2 * sizeof(float2) : 0) + (PAIRS == 2 ? 2 * (size_t)n2 * sizeof(float2) : 0);
 }
 
 // Layouts of the forward row kernel: MAXT threads at most, and the block is
@@ -808,6 +827,45 @@ __host__ __device__ inline size_t row_voigt_smem(int n2, bool with_twr) {
 // owns one butterfly's 8 output bins and their accumulators.
 constexpr int kRowMaxT2 = 384;    // PAIRS = 2, two CTAs per SM (n2 <= 3072)
 constexpr int kRowMaxT1 = 1024;   // PAIRS = 1, long rows (n2 <= 8192)
+
+// cp.async staging of the next rows of a pair group (16-byte copies that
+// bypass L1, completed with wait_group before the first pass reads them)
+__device__ __forceinline__ void stage_rows(float2* dst, const float2* ya, const float2* yb, int n2) {
+    const int chunks = n2 / 2;   // 16-byte chunks per row
+    for (int c = threadIdx.x; c < 2 * chunks; c += blockDim.x) {
+        const bool second = c >= chunks;
+        const float2* src = (second ? yb : ya) + 2 * (c - (second ? chunks : 0));
+        if (second && !yb) continue;
+        const uint32_t d = smem_u32(dst + 2 * c);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// first pass from the staged rows (stage = [row a | row b], n2 each)
+template <int R, bool TWR>
+__device__ __forceinline__ void row_first_staged(const float2* stage, bool two, const float2* twr, float4* out,
+                                                 int L) {
+    const int M = L / R;
+    for (int j = threadIdx.x; j < M; j += blockDim.x) {
+        float2 A[R], B[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            A[r] = stage[j + r * M];
+            B[r] = two ? stage[L + j + r * M] : make_float2(0.f, 0.f);
+            if (TWR) {
+                const float2 w = twr[j + r * M];
+                A[r] = cmul(A[r], w);
+                B[r] = cmul(B[r], w);
+            }
+        }
+        dftR<R>(A);
+        dftR<R>(B);
+#pragma unroll
+        for (int r = 0; r < R; ++r) out[rp8(j * R + r)] = make_float4(A[r].x, A[r].y, B[r].x, B[r].y);
+    }
+}
 
 template <int PAIRS, int MAXT, bool TWR>
 __global__ void __launch_bounds__(MAXT, PAIRS == 2 ? 2 : 1) k_row_fft_voigt(const VoigtArgs a) {
@@ -818,6 +876,8 @@ __global__ void __launch_bounds__(MAXT, PAIRS == 2 ? 2 : 1) k_row_fft_voigt(cons
     E* buf0 = reinterpret_cast<E*>(sm4);
     E* buf1 = buf0 + len;
     float2* twr = TWR ? reinterpret_cast<float2*>(buf1 + len) : nullptr;
+    // PAIRS = 2: the next two rows are staged with cp.async during the passes
+    float2* stage = PAIRS == 2 ? reinterpret_cast<float2*>(buf1 + len) + (TWR ? n2 : 0) : nullptr;
     const int k1 = blockIdx.x;
     if (TWR)
         for (int t = threadIdx.x; t < n2; t += blockDim.x) twr[t] = twiddle_n(a.tw_hi, a.tw_lo, k1 * t);
@@ -831,19 +891,34 @@ __global__ void __launch_bounds__(MAXT, PAIRS == 2 ? 2 : 1) k_row_fft_voigt(cons
 #pragma unroll
     for (int r = 0; r < 8; ++r) acc[r] = make_float2(0.f, 0.f);
 
+    auto row_ptr = [&](int jj) { return a.y + ((int64_t)jj * a.n1 + k1) * n2; };
+    if (PAIRS == 2 && j0 < j1) stage_rows(stage, row_ptr(j0), j0 + 1 < j1 ? row_ptr(j0 + 1) : nullptr, n2);
     for (int j = j0; j < j1; j += PAIRS) {
         const bool two = PAIRS == 2 && j + 1 < j1;
-        const float2* ya = a.y + ((int64_t)j * a.n1 + k1) * n2;
-        const float2* yb = two ? a.y + ((int64_t)(j + 1) * a.n1 + k1) * n2 : nullptr;
-        if (TWR && j == j0) __syncthreads();   // twr complete
-        switch (P.radix[0]) {
-            case 2: row_first<2, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
-            case 3: row_first<3, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
-            case 4: row_first<4, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
-            case 5: row_first<5, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
-            default: row_first<8, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
+        if (PAIRS == 2) {
+            stage_wait();
+            __syncthreads();   // staged rows (and twr) visible to all threads
+            switch (P.radix[0]) {
+                case 2: row_first_staged<2, TWR>(stage, two, twr, reinterpret_cast<float4*>(buf0), n2); break;
+                case 3: row_first_staged<3, TWR>(stage, two, twr, reinterpret_cast<float4*>(buf0), n2); break;
+                case 4: row_first_staged<4, TWR>(stage, two, twr, reinterpret_cast<float4*>(buf0), n2); break;
+                case 5: row_first_staged<5, TWR>(stage, two, twr, reinterpret_cast<float4*>(buf0), n2); break;
+                default: row_first_staged<8, TWR>(stage, two, twr, reinterpret_cast<float4*>(buf0), n2); break;
+            }
+            __syncthreads();   // stage consumed: prefetch the next two rows under the remaining passes
+            if (j + 2 < j1) stage_rows(stage, row_ptr(j + 2), j + 3 < j1 ? row_ptr(j + 3) : nullptr, n2);
+        } else {
+            const float2* ya = row_ptr(j);
+            if (TWR && j == j0) __syncthreads();   // twr complete
+            switch (P.radix[0]) {
+                case 2: row_first<2, PAIRS, TWR>(ya, nullptr, twr, buf0, n2); break;
+                case 3: row_first<3, PAIRS, TWR>(ya, nullptr, twr, buf0, n2); break;
+                case 4: row_first<4, PAIRS, TWR>(ya, nullptr, twr, buf0, n2); break;
+                case 5: row_first<5, PAIRS, TWR>(ya, nullptr, twr, buf0, n2); break;
+                default: row_first<8, PAIRS, TWR>(ya, nullptr, twr, buf0, n2); break;
+            }
+            __syncthreads();
         }
-        __syncthreads();
         E* in = buf0;
         E* out = buf1;
         for (int p = 1; p < P.npass - 1; ++p) {
@@ -870,30 +945,55 @@ __global__ void __launch_bounds__(MAXT, PAIRS == 2 ? 2 : 1) k_row_fft_voigt(cons
             twiddleP<8, PAIRS>(A, B, P.tw, jl);   // w_{n2}^{r jl}
             dft8(A);
             if (PAIRS == 2) dft8(B);
-            const NodeV A0 = node_params(a, 2 * j), A1 = node_params(a, 2 * j + 1);
-#pragma unroll
-            for (int r = 0; r < 8; ++r) {
-                const int kk = k1 + a.n1 * (jl + r * ML);
-                const float f = (float)min(kk, n - kk) * a.inv_ndv;
-                const float va = voigt_eval(A0, f, a.half_fs);
-                const float vb = voigt_eval(A1, f, a.half_fs);
-                float2 c = acc[r];
-                c.x += A[r].x * va + A[r].y * vb;
-                c.y += A[r].y * va - A[r].x * vb;
-                acc[r] = c;
-            }
-            if (two) {
-                const NodeV B0 = node_params(a, 2 * j + 2), B1 = node_params(a, 2 * j + 3);
+            if (!a.any_fold) {
+                const NodeF A0 = node_fast(a, 2 * j), A1 = node_fast(a, 2 * j + 1);
+                NodeF B0 = A0, B1 = A1;
+                if (two) {
+                    B0 = node_fast(a, 2 * j + 2);
+                    B1 = node_fast(a, 2 * j + 3);
+                }
 #pragma unroll
                 for (int r = 0; r < 8; ++r) {
                     const int kk = k1 + a.n1 * (jl + r * ML);
                     const float f = (float)min(kk, n - kk) * a.inv_ndv;
-                    const float wa = voigt_eval(B0, f, a.half_fs);
-                    const float wb = voigt_eval(B1, f, a.half_fs);
+                    const float f2 = f * f;
+                    const float va = voigt_fast(A0, f, f2), vb = voigt_fast(A1, f, f2);
                     float2 c = acc[r];
-                    c.x += B[r].x * wa + B[r].y * wb;
-                    c.y += B[r].y * wa - B[r].x * wb;
+                    c.x += A[r].x * va + A[r].y * vb;
+                    c.y += A[r].y * va - A[r].x * vb;
+                    if (two) {
+                        const float wa = voigt_fast(B0, f, f2), wb = voigt_fast(B1, f, f2);
+                        c.x += B[r].x * wa + B[r].y * wb;
+                        c.y += B[r].y * wa - B[r].x * wb;
+                    }
                     acc[r] = c;
+                }
+            } else {
+                const NodeV A0 = node_params(a, 2 * j), A1 = node_params(a, 2 * j + 1);
+#pragma unroll
+                for (int r = 0; r < 8; ++r) {
+                    const int kk = k1 + a.n1 * (jl + r * ML);
+                    const float f = (float)min(kk, n - kk) * a.inv_ndv;
+                    const float va = voigt_eval(A0, f, a.half_fs);
+                    const float vb = voigt_eval(A1, f, a.half_fs);
+                    float2 c = acc[r];
+                    c.x += A[r].x * va + A[r].y * vb;
+                    c.y += A[r].y * va - A[r].x * vb;
+                    acc[r] = c;
+                }
+                if (two) {
+                    const NodeV B0 = node_params(a, 2 * j + 2), B1 = node_params(a, 2 * j + 3);
+#pragma unroll
+                    for (int r = 0; r < 8; ++r) {
+                        const int kk = k1 + a.n1 * (jl + r * ML);
+                        const float f = (float)min(kk, n - kk) * a.inv_ndv;
+                        const float wa = voigt_eval(B0, f, a.half_fs);
+                        const float wb = voigt_eval(B1, f, a.half_fs);
+                        float2 c = acc[r];
+                        c.x += B[r].x * wa + B[r].y * wb;
+                        c.y += B[r].y * wa - B[r].x * wb;
+                        acc[r] = c;
+                    }
                 }
             }
         }
