@@ -219,8 +219,8 @@ int launch_col_index(const float2* v0, int64_t n, double vmin, double dv, int c_
 // max over grid columns of the lines within E columns (fixed-point bound), into *cmax
 int launch_col_cmax(const int64_t* col_start, int col_off, int col_count, int n_v, int E, int* cmax,
                     cudaStream_t st);
-int launch_scatter(const ScatterArgs& a, int grid, size_t smem, cudaStream_t st);
-int scatter_smem_optin(size_t* avail);
+int launch_scatter(const ScatterArgs& a, int grid, int threads, size_t smem, cudaStream_t st);
+int scatter_smem_optin(size_t* avail, size_t* avail_two);
 int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st);
 int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st);
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st);

@@ -1350,20 +1350,27 @@ int launch_col_cmax(const int64_t* col_start, int col_off, int col_count, int n_
     return check_launch();
 }
 
-int launch_scatter(const ScatterArgs& a, int grid, size_t smem, cudaStream_t st) {
+int launch_scatter(const ScatterArgs& a, int grid, int threads, size_t smem, cudaStream_t st) {
     ALLOW_SMEM(k_scatter, smem);
-    k_scatter<<<grid, kScatThreads, smem, st>>>(a);
+    k_scatter<<<grid, threads, smem, st>>>(a);
     return check_launch();
 }
 
-int scatter_smem_optin(size_t* avail) {
-    int dev = 0, optin = 0;
+// Dynamic shared memory of the scatter: the most one CTA may have, and the
+// most each of two CTAs on one SM may have.
+int scatter_smem_optin(size_t* avail, size_t* avail_two) {
+    int dev = 0, optin = 0, per_sm = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return RG_ERR_CUDA;
     if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+        return RG_ERR_CUDA;
+    if (cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess)
         return RG_ERR_CUDA;
     cudaFuncAttributes fa;
     if (cudaFuncGetAttributes(&fa, k_scatter) != cudaSuccess) return RG_ERR_CUDA;
     *avail = (size_t)optin - fa.sharedSizeBytes;
+    // each resident CTA also reserves 1 KB of the SM's shared memory
+    const size_t half = (size_t)per_sm / 2 - 1024 - fa.sharedSizeBytes;
+    *avail_two = std::min(*avail, half);
     return RG_OK;
 }
 
