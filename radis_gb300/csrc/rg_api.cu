@@ -545,7 +545,9 @@ void fill_voigt_args(const Work& W, const SpecHost& s, VoigtArgs* va) {
     const rg_grid& g = s.grid;
     va->f2 = W.f2;
     va->threads = row_threads(W.f2);
-    row_layout(W.n2, &va->pairs_per_pass, &va->row_twiddle_table);
+    const RowLayout rl = row_layout(W.n2);
+    va->pairs_per_pass = rl.pairs;
+    va->row_twiddle_table = rl.twr;
     va->n1 = W.n1;
     va->n2 = W.n2;
     va->n = W.n;
@@ -628,9 +630,7 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
         ca.n_pairs = s.n_nodes / 2;
         ca.ldm = W.ldm;
         ca.cmax = W.cmax_dev;
-        int pairs_unused, twr;
-        row_layout(W.n2, &pairs_unused, &twr);
-        ca.twiddle = !twr;
+        ca.twiddle = !row_layout(W.n2).twr;
         ca.y = W.y;
         ca.tw_hi = W.tw_hi;
         ca.tw_lo = W.tw_lo;
@@ -701,9 +701,7 @@ ColFftArgs col_args(const Work& W, const SpecHost& s) {
     ca.n_pairs = s.n_nodes / 2;
     ca.tw_hi = W.tw_hi;
     ca.tw_lo = W.tw_lo;
-    int pairs_unused, twr;
-    row_layout(W.n2, &pairs_unused, &twr);
-    ca.twiddle = !twr;
+    ca.twiddle = !row_layout(W.n2).twr;
     return ca;
 }
 

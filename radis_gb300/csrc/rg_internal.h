@@ -233,7 +233,13 @@ int launch_gather_grad(const GradArgs& a, int grid, cudaStream_t st);
 int launch_scatter_tangent(const GradArgs& a, int grid, cudaStream_t st);
 int col_block(int n1);               // columns per CTA of the column FFTs
 int row_threads(const FftLen& f);    // block size of the forward row kernel
-void row_layout(int n2, int* pairs, int* with_twr);   // forward row kernel layout
+struct RowLayout {         // forward row kernel layout for rows of n2 points
+    int pairs;            // node pairs per element (2: float4, 1: float2)
+    int maxt;             // block size limit
+    int twr;              // per-row four-step twiddle table (else the column stage twiddles)
+    int stage;            // cp.async staging of the next two rows
+};
+RowLayout row_layout(int n2);
 size_t scatter_smem_floats(int n_nodes, int TK);
 
 }  // namespace rg

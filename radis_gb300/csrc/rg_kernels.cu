@@ -814,18 +814,19 @@ __device__ __forceinline__ void row_mid(const typename RowT<PAIRS>::E* __restric
     }
 }
 
-// two work buffers, the optional twiddle table, and (two pairs) the staging
+// two work buffers, the optional twiddle table, and the optional staging
 // buffer of the next two rows
 template <int PAIRS>
-__host__ __device__ inline size_t row_voigt_smem(int n2, bool with_twr) {
+__host__ __device__ inline size_t row_voigt_smem(int n2, bool with_twr, bool with_stage) {
     return 2 * (size_t)RowT<PAIRS>::len(n2) * sizeof(typename RowT<PAIRS>::E) +
-           (with_twr ? (size_t)n2 * sizeof(float2) : 0) + (PAIRS == 2 ? 2 * (size_t)n2 * sizeof(float2) : 0);
+           (with_twr ? (size_t)n2 * sizeof(float2) : 0) + (with_stage ? 2 * (size_t)n2 * sizeof(float2) : 0);
 }
 
 // Layouts of the forward row kernel: MAXT threads at most, and the block is
 // at least the n2/8 butterflies of the last (radix-8) pass, so each thread
 // owns one butterfly's 8 output bins and their accumulators.
 constexpr int kRowMaxT2 = 384;    // PAIRS = 2, two CTAs per SM (n2 <= 3072)
+constexpr int kRowMaxT2L = 768;   // PAIRS = 2, one CTA per SM (n2 <= 6144, work buffers only)
 constexpr int kRowMaxT1 = 1024;   // PAIRS = 1, long rows (n2 <= 8192)
 
 // cp.async staging of the next rows of a pair group (16-byte copies that
@@ -867,8 +868,8 @@ __device__ __forceinline__ void row_first_staged(const float2* stage, bool two, 
     }
 }
 
-template <int PAIRS, int MAXT, bool TWR>
-__global__ void __launch_bounds__(MAXT, PAIRS == 2 ? 2 : 1) k_row_fft_voigt(const VoigtArgs a) {
+template <int PAIRS, int MAXT, bool TWR, bool STAGE>
+__global__ void __launch_bounds__(MAXT, MAXT <= 384 ? 2 : 1) k_row_fft_voigt(const VoigtArgs a) {
     using E = typename RowT<PAIRS>::E;
     extern __shared__ float4 sm4[];
     const int n2 = a.n2;
@@ -876,8 +877,8 @@ __global__ void __launch_bounds__(MAXT, PAIRS == 2 ? 2 : 1) k_row_fft_voigt(cons
     E* buf0 = reinterpret_cast<E*>(sm4);
     E* buf1 = buf0 + len;
     float2* twr = TWR ? reinterpret_cast<float2*>(buf1 + len) : nullptr;
-    // PAIRS = 2: the next two rows are staged with cp.async during the passes
-    float2* stage = PAIRS == 2 ? reinterpret_cast<float2*>(buf1 + len) + (TWR ? n2 : 0) : nullptr;
+    // STAGE (two pairs): the next two rows are staged with cp.async during the passes
+    float2* stage = STAGE ? reinterpret_cast<float2*>(buf1 + len) + (TWR ? n2 : 0) : nullptr;
     const int k1 = blockIdx.x;
     if (TWR)
         for (int t = threadIdx.x; t < n2; t += blockDim.x) twr[t] = twiddle_n(a.tw_hi, a.tw_lo, k1 * t);
@@ -892,10 +893,10 @@ __global__ void __launch_bounds__(MAXT, PAIRS == 2 ? 2 : 1) k_row_fft_voigt(cons
     for (int r = 0; r < 8; ++r) acc[r] = make_float2(0.f, 0.f);
 
     auto row_ptr = [&](int jj) { return a.y + ((int64_t)jj * a.n1 + k1) * n2; };
-    if (PAIRS == 2 && j0 < j1) stage_rows(stage, row_ptr(j0), j0 + 1 < j1 ? row_ptr(j0 + 1) : nullptr, n2);
+    if (STAGE && j0 < j1) stage_rows(stage, row_ptr(j0), j0 + 1 < j1 ? row_ptr(j0 + 1) : nullptr, n2);
     for (int j = j0; j < j1; j += PAIRS) {
         const bool two = PAIRS == 2 && j + 1 < j1;
-        if (PAIRS == 2) {
+        if (STAGE) {
             stage_wait();
             __syncthreads();   // staged rows (and twr) visible to all threads
             switch (P.radix[0]) {
@@ -909,13 +910,14 @@ __global__ void __launch_bounds__(MAXT, PAIRS == 2 ? 2 : 1) k_row_fft_voigt(cons
             if (j + 2 < j1) stage_rows(stage, row_ptr(j + 2), j + 3 < j1 ? row_ptr(j + 3) : nullptr, n2);
         } else {
             const float2* ya = row_ptr(j);
+            const float2* yb = two ? row_ptr(j + 1) : nullptr;
             if (TWR && j == j0) __syncthreads();   // twr complete
             switch (P.radix[0]) {
-                case 2: row_first<2, PAIRS, TWR>(ya, nullptr, twr, buf0, n2); break;
-                case 3: row_first<3, PAIRS, TWR>(ya, nullptr, twr, buf0, n2); break;
-                case 4: row_first<4, PAIRS, TWR>(ya, nullptr, twr, buf0, n2); break;
-                case 5: row_first<5, PAIRS, TWR>(ya, nullptr, twr, buf0, n2); break;
-                default: row_first<8, PAIRS, TWR>(ya, nullptr, twr, buf0, n2); break;
+                case 2: row_first<2, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
+                case 3: row_first<3, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
+                case 4: row_first<4, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
+                case 5: row_first<5, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
+                default: row_first<8, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
             }
             __syncthreads();
         }
@@ -1391,32 +1393,49 @@ int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st) {
     }
 }
 
-template <int PAIRS, int MAXT, bool TWR>
+template <int PAIRS, int MAXT, bool TWR, bool STAGE>
 static int row_voigt(const VoigtArgs& a, cudaStream_t st) {
-    const size_t smem = row_voigt_smem<PAIRS>(a.n2, TWR);
-    ALLOW_SMEM((k_row_fft_voigt<PAIRS, MAXT, TWR>), smem);
+    const size_t smem = row_voigt_smem<PAIRS>(a.n2, TWR, STAGE);
+    ALLOW_SMEM((k_row_fft_voigt<PAIRS, MAXT, TWR, STAGE>), smem);
     dim3 grid(a.n1, (a.n_pairs + kPairGroup - 1) / kPairGroup);
-    k_row_fft_voigt<PAIRS, MAXT, TWR><<<grid, a.threads, smem, st>>>(a);
+    k_row_fft_voigt<PAIRS, MAXT, TWR, STAGE><<<grid, a.threads, smem, st>>>(a);
     return check_launch();
 }
 
-// Layout of the forward row kernel: two pairs per element (float4) while the
-// block limit of that layout covers the n2/8 last-pass butterflies, else one;
-// the per-row four-step twiddle table only with two pairs and while two CTAs
-// still fit an SM (otherwise the column stage applies the twiddle).
-void row_layout(int n2, int* pairs, int* with_twr) {
-    *pairs = n2 / 8 <= kRowMaxT2 ? 2 : 1;
-    *with_twr = *pairs == 2 && row_voigt_smem<2>(n2, true) <= 113 * 1024;
+// Layout of the forward row kernel for rows of n2 points:
+//  * n2 <= 3072: two pairs per float4 element, <= 384 threads, the next two
+//    rows staged under the passes, and the per-row four-step twiddle table
+//    while two CTAs still fit an SM;
+//  * n2 <= 6144 (and the two work buffers fit): two pairs, <= 768 threads,
+//    one CTA per SM, nothing else in shared memory;
+//  * else one pair per element, <= 1024 threads.
+// Without the table the column stage applies the four-step twiddle.
+RowLayout row_layout(int n2) {
+    RowLayout L{};
+    if (n2 / 8 <= kRowMaxT2) {
+        L.pairs = 2;
+        L.maxt = kRowMaxT2;
+        L.stage = 1;
+        L.twr = row_voigt_smem<2>(n2, true, true) <= 113 * 1024;
+    } else if (n2 / 8 <= kRowMaxT2L && row_voigt_smem<2>(n2, false, false) <= 227 * 1024) {
+        L.pairs = 2;
+        L.maxt = kRowMaxT2L;
+    } else {
+        L.pairs = 1;
+        L.maxt = kRowMaxT1;
+    }
+    return L;
 }
 
 int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st) {
     if (a.f2.npass < 2 || a.f2.radix[a.f2.npass - 1] != 8) return RG_ERR_RANGE;
-    const int maxt = a.pairs_per_pass == 2 ? kRowMaxT2 : kRowMaxT1;
-    if (a.threads < a.n2 / 8 || a.threads > maxt || a.threads % 32) return RG_ERR_RANGE;
-    if (a.pairs_per_pass == 2)
-        return a.row_twiddle_table ? row_voigt<2, kRowMaxT2, true>(a, st) : row_voigt<2, kRowMaxT2, false>(a, st);
-    if (a.row_twiddle_table) return RG_ERR_RANGE;
-    return row_voigt<1, kRowMaxT1, false>(a, st);
+    const RowLayout L = row_layout(a.n2);
+    if (a.threads < a.n2 / 8 || a.threads > L.maxt || a.threads % 32) return RG_ERR_RANGE;
+    if (L.pairs != a.pairs_per_pass || L.twr != a.row_twiddle_table) return RG_ERR_RANGE;
+    if (L.maxt == kRowMaxT2)
+        return L.twr ? row_voigt<2, kRowMaxT2, true, true>(a, st) : row_voigt<2, kRowMaxT2, false, true>(a, st);
+    if (L.maxt == kRowMaxT2L) return row_voigt<2, kRowMaxT2L, false, false>(a, st);
+    return row_voigt<1, kRowMaxT1, false, false>(a, st);
 }
 
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st) {
@@ -1503,9 +1522,7 @@ namespace rg {
 // in [max(128, n2/8), layout limit] that wastes the fewest butterfly slots
 // over the passes (ties -> fewer threads).
 int row_threads(const FftLen& f) {
-    int pairs, twr;
-    row_layout(f.L, &pairs, &twr);
-    const int maxt = pairs == 2 ? kRowMaxT2 : kRowMaxT1;
+    const int maxt = row_layout(f.L).maxt;
     const int t_min = std::max(128, (f.L / 8 + 31) / 32 * 32);
     int best = t_min;
     double best_eff = -1.0;
