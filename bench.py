@@ -319,6 +319,69 @@ def run_serving(ctx, L, lists, n_req, slots, seed=11):
     }
 
 
+def run_autodiff(ctx, L, n_cond=64, seed=12):
+    """Derivative configuration: 64 seeded conditions on the CO-like 10k list
+    at 0.001 cm-1 (1900-2300, 400 001 points), T log-U[300, 3000] K, p
+    log-U[0.1, 10] bar, x log-U[0.01, 1].  Times, per condition, the FP32
+    forward, forward + adjoint (gradient of a scalar loss), forward + the
+    three tangent spectra, and finite differences by forward runs (a central
+    difference per parameter: 6 extra spectra)."""
+    import numpy as np
+    import torch
+
+    from radis_gb300 import synthetic as S
+    from radis_gb300.autodiff import absorbance, jacobian
+    rng = np.random.default_rng(seed)
+    conds = [(float(np.exp(rng.uniform(np.log(300), np.log(3000)))),
+              float(np.exp(rng.uniform(np.log(0.1), np.log(10.0)))),
+              float(np.exp(rng.uniform(np.log(0.01), np.log(1.0))))) for _ in range(n_cond)]
+    ln = L.Lines(ctx, S.co_like(), 28.0)
+    n_v = 400001
+    plan = L.Plan(ln, 1900.0, 0.001, n_v, dxG=S.DXG_DEFAULT, dxL=S.DXL_DEFAULT)
+    out = torch.empty(n_v, dtype=torch.float32, device="cuda")
+    w = torch.rand(n_v, device="cuda")
+
+    def fwd(c):
+        plan.synthesize_device(*c, out.data_ptr(), torch.cuda.current_stream().cuda_stream or 1)
+
+    def fwd_bwd(c):
+        T, p, x = (torch.tensor(v, dtype=torch.float64, requires_grad=True) for v in c)
+        (absorbance(plan, T, p, x) * w).sum().backward()
+
+    def fwd_jvp(c):
+        jacobian(plan, *c)
+
+    def fd(c):
+        fwd(c)
+        for i in range(3):
+            for sgn in (1.0, -1.0):
+                cc = list(c)
+                cc[i] *= 1.0 + sgn * 1e-4
+                fwd(tuple(cc))
+
+    res = {"workload": ("CO-like synthetic list, 10000 lines, 1900-2300 cm-1 at 0.001 cm-1 (400001 points), "
+                        f"{n_cond} conditions T log-U[300,3000] K, p log-U[0.1,10] bar, x log-U[0.01,1]"),
+           "conditions": n_cond}
+    for name, f in (("forward", fwd), ("forward_adjoint", fwd_bwd), ("forward_tangent3", fwd_jvp),
+                    ("fd_by_forward", fd)):
+        for c in conds[:3]:
+            f(c)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for c in conds:
+            f(c)
+        torch.cuda.synchronize()
+        res[name + "_ms"] = (time.perf_counter() - t0) * 1e3 / n_cond
+    res["adjoint_speedup_vs_fd"] = res["fd_by_forward_ms"] / res["forward_adjoint_ms"]
+    res["tangent_speedup_vs_fd"] = res["fd_by_forward_ms"] / res["forward_tangent3_ms"]
+    res["note"] = ("per-condition wall time (host API calls, device work synchronised per batch); node axes "
+                   "follow each condition; accuracy vs central FD of the FP64 oracle is checked in "
+                   "tests/test_gpu_autodiff.py")
+    plan.close()
+    ln.close()
+    return res
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -452,6 +515,8 @@ def run_ours(args):
                 "sample": (f"oracle (FP64 numpy restatement of the reference CPU LDM path): scaling+scatter "
                            f"of {m} of {n_lines} lines scaled x{n_lines / m:.0f} ({tl:.2f} s) + full FFT/Voigt "
                            f"stage ({tc:.2f} s, scipy.fft workers={workers}); add.at single-threaded")}
+        if ws == 1 and not args.no_autodiff:
+            res["autodiff"] = run_autodiff(ctx, L)
         if ws == 1 and not args.no_serving:
             co = L.Lines(ctx, S.co_like(), 28.0)
             h2o_lines = S.h2o_like(args.serve_h2o_lines)
@@ -482,6 +547,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-autodiff", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=120)
     ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--serve-h2o-lines", type=int, default=100_000_000)

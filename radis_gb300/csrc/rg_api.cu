@@ -428,34 +428,30 @@ int ensure_workspace(Work& W, int n_nodes, cudaStream_t st) {
     return RG_OK;
 }
 
-// Shape of the persistent scatter: CTAs per SM, stage chunk (lines) and tile
-// width (columns, a multiple of 32 for the bank swizzle).  Two 512-thread CTAs
-// per SM (one scatters while the other waits on its copies or flushes a
-// tile) when a tile of >= 64 columns fits next to their stage buffers in half
-// an SM's shared memory, else one 1024-thread CTA; within the budget, the
-// largest chunk that leaves a tile of >= 128 columns (else 64, then 32).
-int scatter_shape(int n_nodes, int* chunk, int* TK, size_t* smem, int* ctas) {
-    size_t avail1 = 0, avail2 = 0;
-    RG(scatter_smem_optin(&avail1, &avail2));
-    for (int per_sm : {2, 1}) {
-        const size_t avail = per_sm == 2 ? avail2 : avail1;
-        for (int min_tk : {128, 64, 32}) {
-            if (per_sm == 2 && min_tk < 64) break;
-            for (int ch : {2048, 1024, 512, 256}) {
-                const size_t fixed = scatter_fixed_smem(ch);
-                if (fixed >= avail) continue;
-                int tk = (int)((avail - fixed) / (4 * (size_t)n_nodes)) / 32 * 32;
-                tk = std::min(tk, 1024);
-                if (tk >= min_tk) {
-                    *chunk = ch;
-                    *TK = tk;
-                    *smem = fixed + (size_t)4 * n_nodes * tk;
-                    *ctas = per_sm;
-                    return RG_OK;
-                }
+// Shape of the persistent scatter (one 1024-thread CTA per SM): TMA ring
+// stages, chunk (lines) and tile width (columns, a multiple of 32 for the bank
+// swizzle).  Each chunk costs two CTA barriers, so the chunk is as large as
+// possible (two stages, 2048 lines = 2 lines per thread when a tile of >= 64
+// columns still fits; measured faster than deeper rings of smaller chunks),
+// then smaller chunks for wider node grids.
+int scatter_shape(int n_nodes, int* chunk, int* TK, int* stages, size_t* smem) {
+    size_t avail = 0;
+    RG(scatter_smem_optin(&avail));
+    const int S = 2;
+    for (int min_tk : {64, 32})
+        for (int ch : {2048, 1024, 512, 256}) {
+            const size_t fixed = scatter_fixed_smem(ch, S);
+            if (fixed >= avail) continue;
+            int tk = (int)((avail - fixed) / (4 * (size_t)n_nodes)) / 32 * 32;
+            tk = std::min(tk, 1024);
+            if (tk >= min_tk) {
+                *chunk = ch;
+                *TK = tk;
+                *stages = S;
+                *smem = fixed + (size_t)4 * n_nodes * tk;
+                return RG_OK;
             }
         }
-    }
     return fail(RG_ERR_RANGE, "LDM grid of %d nodes does not fit a shared-memory tile", n_nodes);
 }
 
@@ -481,8 +477,7 @@ int build_scatter_args(const rg_lines* L, const Work& W, const rg_conditions* c,
     a->row_stride = W.row_stride;
     a->ldm = W.ldm;
     size_t smem_unused;
-    int ctas_unused;
-    RG(scatter_shape(s.n_nodes, &a->chunk, &a->TK, &smem_unused, &ctas_unused));
+    RG(scatter_shape(s.n_nodes, &a->chunk, &a->TK, &a->stages, &smem_unused));
     a->n_tiles = (int)((W.desc.n_v + a->TK - 1) / a->TK);
     a->cmax = W.cmax_dev;
     a->err = W.err;
@@ -607,15 +602,15 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
     ScatterArgs sa;
     RG(build_scatter_args(L, W, c, s, &sa));
     const int n_v = (int)W.desc.n_v;
-    int ch_unused, tk_unused, ctas;
+    int ch_unused, tk_unused, st_unused;
     size_t smem;
-    RG(scatter_shape(s.n_nodes, &ch_unused, &tk_unused, &smem, &ctas));
+    RG(scatter_shape(s.n_nodes, &ch_unused, &tk_unused, &st_unused, &smem));
     const int sms = L->ctx->sms;
-    const int grid = std::max(std::min(sa.n_tiles, sms * ctas),
+    const int grid = std::max(std::min(sa.n_tiles, sms),
                               (sa.n_tiles + kScatMaxTilesPerCta - 1) / kScatMaxTilesPerCta);
     if (ev) CU(cudaEventRecord(ev[0], st));
     CU(cudaMemsetAsync(W.counter, 0, sizeof(unsigned long long), st));
-    RG(launch_scatter(sa, grid, kScatThreads / ctas, smem, st));
+    RG(launch_scatter(sa, grid, kScatThreads, smem, st));
     if (ev) CU(cudaEventRecord(ev[1], st));
     if (!ldm_only) {
         ColFftArgs ca;

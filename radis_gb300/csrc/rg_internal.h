@@ -106,6 +106,7 @@ struct ScatterArgs {
     const int* cmax;          // device: most lines that can touch one column (sets the fixed-point scale)
     int n_tiles;
     int chunk;                // lines per staged chunk (multiple of 16)
+    int stages;               // chunk buffers in the TMA ring (2..kScatMaxStages)
     unsigned* err;            // set to 1 when a bounded wait gives up
 };
 
@@ -119,9 +120,11 @@ constexpr int kScatMaxTilesPerCta = 512;
 #else
 #define RG_HD
 #endif
+constexpr int kScatMaxStages = 4;
 RG_HD inline size_t scatter_stage_bytes(int chunk) { return (size_t)33 * chunk; }
-RG_HD inline size_t scatter_fixed_smem(int chunk) {
-    return 2 * scatter_stage_bytes(chunk) + 16 + 8 * kScatMaxTilesPerCta;
+// stage ring, its mbarriers (one 32-byte block) and the per-tile line ranges
+RG_HD inline size_t scatter_fixed_smem(int chunk, int stages) {
+    return stages * scatter_stage_bytes(chunk) + 8 * kScatMaxStages + 8 * kScatMaxTilesPerCta;
 }
 
 struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
@@ -220,7 +223,7 @@ int launch_col_index(const float2* v0, int64_t n, double vmin, double dv, int c_
 int launch_col_cmax(const int64_t* col_start, int col_off, int col_count, int n_v, int E, int* cmax,
                     cudaStream_t st);
 int launch_scatter(const ScatterArgs& a, int grid, int threads, size_t smem, cudaStream_t st);
-int scatter_smem_optin(size_t* avail, size_t* avail_two);
+int scatter_smem_optin(size_t* avail);
 int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st);
 int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st);
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st);

@@ -333,11 +333,15 @@ __global__ void k_col_cmax(const int64_t* __restrict__ col_start, int col_off, i
 // ---------------------------------------------------------------------------
 // K1: fused line scaling + LDM scatter into a shared-memory tile
 // ---------------------------------------------------------------------------
-// Tile layout [node][TK] with the column XOR-swizzled by (node & 7) << 2: lanes
-// of a warp hold neighbouring (sorted) lines, i.e. the same few columns, so
-// without the swizzle their atomics would pile onto the same banks.  The XOR
-// keeps aligned groups of four columns together for the float4 flush.
-__device__ __forceinline__ int tile_addr(int node, int c, int TK) { return node * TK + (c ^ ((node & 7) << 2)); }
+// Tile layout [node][TK] with the columns permuted per node row: the lanes of
+// a warp hold neighbouring (sorted) lines, i.e. the same few columns at random
+// nodes, so an unpermuted tile would pile their atomics onto one bank.  Groups
+// of four columns (one uint4 of the flush) are XOR-swizzled by node & 7 (bank
+// group) and the words inside a group rotated by (node >> 3) & 3, so one
+// column maps to all 32 banks across 32 consecutive nodes.
+__device__ __forceinline__ int tile_addr(int node, int c, int TK) {
+    return node * TK + ((((c >> 2) ^ (node & 7)) << 2) | ((c + (node >> 3)) & 3));
+}
 
 // --- TMA (cp.async.bulk) + mbarrier helpers ---------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -509,18 +513,20 @@ __device__ __forceinline__ unsigned scatter_chunk(const ScatterArgs& a, const St
 }
 
 // Persistent scatter: CTA b owns tiles b, b + G, b + 2G, ...  Thread 0 streams
-// the tiles' line records chunk by chunk into two stage buffers with TMA bulk
-// copies (mbarrier completion), one chunk ahead of the consumers, across tile
-// boundaries; all threads scatter the current chunk into the tile
-// accumulator (32-bit fixed point, native integer shared atomics,
-// deterministic) and flush each finished tile to HBM with plain stores.
+// the tiles' line records chunk by chunk into a ring of `stages` buffers with
+// TMA bulk copies (mbarrier completion), up to stages - 1 chunks ahead of the
+// consumers, across tile boundaries; all threads scatter the current chunk
+// into the tile accumulator (32-bit fixed point, native integer shared
+// atomics, deterministic) and flush each finished tile to HBM with plain
+// stores.
 __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int ch = a.chunk;
-    unsigned char* stage[2] = {smem, smem + scatter_stage_bytes(ch)};
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + 2 * scatter_stage_bytes(ch));
-    int2* rng = reinterpret_cast<int2*>(smem + 2 * scatter_stage_bytes(ch) + 16);
-    uint4* tile4 = reinterpret_cast<uint4*>(smem + scatter_fixed_smem(ch));
+    const int S = a.stages;
+    const size_t sb = scatter_stage_bytes(ch);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + S * sb);
+    int2* rng = reinterpret_cast<int2*>(smem + S * sb + 8 * kScatMaxStages);
+    uint4* tile4 = reinterpret_cast<uint4*>(smem + scatter_fixed_smem(ch, S));
     unsigned* tile = reinterpret_cast<unsigned*>(tile4);
     const int G = gridDim.x;
     const int nq = (a.n_tiles - (int)blockIdx.x + G - 1) / G;   // tiles of this CTA (<= kScatMaxTilesPerCta)
@@ -538,31 +544,28 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
     }
     for (int i = threadIdx.x; i < n4; i += blockDim.x) tile4[i] = make_uint4(0u, 0u, 0u, 0u);
     if (threadIdx.x == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        for (int b = 0; b < S; ++b) mbar_init(&bar[b], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
 
-    // successor of chunk (q, cs) in this CTA's chunk order, skipping empty tiles
-    auto next_chunk = [&](int q, int cs, int& nq2, int& ncs) -> bool {
-        if (q >= 0 && cs + ch < rng[q].y) {
-            nq2 = q;
-            ncs = cs + ch;
-            return true;
+    // producer (thread 0): the next chunk to copy, in this CTA's chunk order
+    // (tiles in order, chunks of ch lines, empty tiles skipped)
+    int pq = 0, pcs = nq > 0 ? rng[0].x : 0;
+    uint32_t issued = 0;    // chunks issued (thread 0)
+    auto produce = [&](int buf) -> bool {
+        while (pq < nq && pcs >= rng[pq].y) {
+            if (++pq < nq) pcs = rng[pq].x;
         }
-        for (int r = q + 1; r < nq; ++r)
-            if (rng[r].x < rng[r].y) {
-                nq2 = r;
-                ncs = rng[r].x;
-                return true;
-            }
-        return false;
+        if (pq >= nq) return false;
+        issue_chunk(a, smem + buf * sb, &bar[buf], pcs, min(ch, rng[pq].y - pcs));
+        pcs += ch;
+        ++issued;
+        return true;
     };
-    if (threadIdx.x == 0) {
-        int fq, fcs;
-        if (next_chunk(-1, 0, fq, fcs)) issue_chunk(a, stage[0], &bar[0], fcs, min(ch, rng[fq].y - fcs));
-    }
+    if (threadIdx.x == 0)
+        for (int b = 0; b < S; ++b)
+            if (!produce(b)) break;
 
     uint32_t g = 0;         // chunks consumed so far
     bool bad = false;
@@ -572,26 +575,24 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
         const int tk = min(a.TK, a.n_v - k_start);
         const int b = rng[q].y;
         for (int cs = rng[q].x; cs < b; cs += ch) {
-            if (threadIdx.x == 0) {
-                int nq2, ncs;   // refill the other buffer, released at the end of the last chunk
-                if (next_chunk(q, cs, nq2, ncs))
-                    issue_chunk(a, stage[(g + 1) & 1], &bar[(g + 1) & 1], ncs, min(ch, rng[nq2].y - ncs));
-            }
+            const int buf = (int)(g % (uint32_t)S);
             // one thread polls the mbarrier (acquiring the TMA data); the others
             // block on the CTA barrier, which orders that data for them too
-            if (threadIdx.x == 0 && !mbar_wait(&bar[g & 1], (g >> 1) & 1)) bad = true;
+            if (threadIdx.x == 0 && !mbar_wait(&bar[buf], (g / (uint32_t)S) & 1)) bad = true;
             if (__syncthreads_or(bad)) {
-                // give up: report, let the copies in flight land (bounded), leave
+                // give up: report, let the other copies in flight land (bounded), leave
                 if (threadIdx.x == 0) {
                     atomicExch(a.err, 1u);
-                    mbar_wait(&bar[(g + 1) & 1], ((g + 1) >> 1) & 1);
+                    for (uint32_t gk = g + 1; gk < issued; ++gk)
+                        mbar_wait(&bar[gk % (uint32_t)S], (gk / (uint32_t)S) & 1);
                 }
                 __syncthreads();
                 return;
             }
-            counted += scatter_chunk(a, stage_view(stage[g & 1], ch, has_dl, has_iso), min(ch, b - cs), k_start, tk,
-                                     tile, fxs);
-            __syncthreads();   // stage[g & 1] free again
+            counted += scatter_chunk(a, stage_view(smem + buf * sb, ch, has_dl, has_iso), min(ch, b - cs), k_start,
+                                     tk, tile, fxs);
+            __syncthreads();   // buffer `buf` free again: refill it, S chunks ahead
+            if (threadIdx.x == 0) produce(buf);
             ++g;
         }
         // flush the finished tile as raw fixed-point words (plain stores: this
@@ -602,9 +603,15 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
         for (int node = threadIdx.x >> 5; node < a.n_nodes; node += blockDim.x >> 5) {
             uint4* row = tile4 + node * per_row;
             uint4* dst = reinterpret_cast<uint4*>(a.ldm + node * a.row_stride + k_start);
-            const int sw = node & 7;
+            const int sw = node & 7, rot = (node >> 3) & 3;
             for (int c4 = lane; c4 < tk4; c4 += 32) {
-                dst[c4] = row[c4 ^ sw];
+                const uint4 t = row[c4 ^ sw];   // word w holds column 4 c4 + ((w - rot) & 3)
+                uint4 o;
+                if (rot == 0) o = t;
+                else if (rot == 1) o = make_uint4(t.y, t.z, t.w, t.x);
+                else if (rot == 2) o = make_uint4(t.z, t.w, t.x, t.y);
+                else o = make_uint4(t.w, t.x, t.y, t.z);
+                dst[c4] = o;
                 row[c4 ^ sw] = make_uint4(0u, 0u, 0u, 0u);
             }
         }
@@ -1358,21 +1365,15 @@ int launch_scatter(const ScatterArgs& a, int grid, int threads, size_t smem, cud
     return check_launch();
 }
 
-// Dynamic shared memory of the scatter: the most one CTA may have, and the
-// most each of two CTAs on one SM may have.
-int scatter_smem_optin(size_t* avail, size_t* avail_two) {
-    int dev = 0, optin = 0, per_sm = 0;
+// Dynamic shared memory the scatter may have (one CTA per SM).
+int scatter_smem_optin(size_t* avail) {
+    int dev = 0, optin = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return RG_ERR_CUDA;
     if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
-        return RG_ERR_CUDA;
-    if (cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess)
         return RG_ERR_CUDA;
     cudaFuncAttributes fa;
     if (cudaFuncGetAttributes(&fa, k_scatter) != cudaSuccess) return RG_ERR_CUDA;
     *avail = (size_t)optin - fa.sharedSizeBytes;
-    // each resident CTA also reserves 1 KB of the SM's shared memory
-    const size_t half = (size_t)per_sm / 2 - 1024 - fa.sharedSizeBytes;
-    *avail_two = std::min(*avail, half);
     return RG_OK;
 }
 
