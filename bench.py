@@ -264,9 +264,12 @@ def run_serving(ctx, L, lists, n_req, slots, seed=11):
             plan = L.Plan(lines, vmin, dv, n_v, **dx)
             o, info = plan.synthesize_host(T, p, x)
             plan.close()
-            outs.append(o.astype(np.float64) * np.exp(info.log_scale))
+            outs.append((o, info.log_scale))
             lat.append(time.perf_counter() - t0 - ta)
-        return outs, lat, time.perf_counter() - t0
+        total = time.perf_counter() - t0
+        return [o.astype(np.float64) * np.exp(ls) for o, ls in outs], lat, total
+
+    worker_ms = {}
 
     def served(arrivals):
         srv = L.Server(ctx, slots=slots, mem_budget=96 << 30)
@@ -287,16 +290,19 @@ def run_serving(ctx, L, lists, n_req, slots, seed=11):
                 time.sleep(1e-5)
             o, info, (ts, t_start, t_done) = srv.wait(tickets[i])
             lat.append(time.perf_counter() - t0 - arrivals[i])
-            outs.append(o.astype(np.float64) * np.exp(info.log_scale))
+            outs.append((o, info.log_scale))
         th.join()
         total = time.perf_counter() - t0
+        st = srv.stats()
+        worker_ms.update(need=st.host_need_ms, launch=st.host_launch_ms, copy=st.host_copy_ms)
         srv.close()
-        return outs, lat, total
+        return [o.astype(np.float64) * np.exp(ls) for o, ls in outs], lat, total
 
     zero = [0.0] * len(reqs)
     plain(zero[:4])                      # warm-up (tables, allocator pools)
     p_out, _, p_total = plain(zero)
     s_out, _, s_total = served(zero)
+    worker_capacity_ms = dict(worker_ms)
     plain_sps, served_sps = len(reqs) / p_total, len(reqs) / s_total
     err = max(float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)) for a, b in zip(s_out, p_out))
     rate = 0.8 * plain_sps
@@ -306,6 +312,21 @@ def run_serving(ctx, L, lists, n_req, slots, seed=11):
     _, s_lat, _ = served(arrivals)
     pct = lambda v, q: float(np.percentile(np.asarray(v) * 1e3, q))
     npts = [r[4] for r in reqs]
+    # where the plain time goes, per line list: plan creation (host clock,
+    # includes its device work and synchronisation) and the spectrum's device
+    # time (stage events)
+    brk = {}
+    for (name, lines, vmin, dv, n_v, T, p, x) in reqs:
+        t_a = time.perf_counter()
+        plan = L.Plan(lines, vmin, dv, n_v, **dx)
+        t_b = time.perf_counter()
+        _, info = plan.synthesize_host(T, p, x, timing=True)
+        plan.close()
+        b = brk.setdefault(name, {"requests": 0, "plan_ms": 0.0, "spectrum_gpu_ms": 0.0, "points": 0})
+        b["requests"] += 1
+        b["plan_ms"] += (t_b - t_a) * 1e3
+        b["spectrum_gpu_ms"] += float(info.stage_ms[5])
+        b["points"] += n_v
     return {
         "requests": len(reqs), "slots": slots,
         "served_spectra_per_s": served_sps, "plain_spectra_per_s": plain_sps,
@@ -316,6 +337,8 @@ def run_serving(ctx, L, lists, n_req, slots, seed=11):
                        "plain_p50": pct(p_lat, 50), "plain_p99": pct(p_lat, 99)},
         "request_points": {"min": int(min(npts)), "median": int(np.median(npts)), "max": int(max(npts))},
         "plain_form": "fresh plan (FFT tables, line index, workspace) + synchronous spectrum per request",
+        "plain_breakdown": brk,
+        "served_worker_host_ms": worker_capacity_ms,
     }
 
 

@@ -218,8 +218,9 @@ int rg_synthesize_static(rg_lines* lines, const rg_plan_desc* grid, const rg_con
  * SpectrumFactory.eq_spectrum_gpu + Spectrum.recalc_gpu for many clients.
  * A worker thread admits queued requests (FIFO) into `slots` CUDA streams as
  * slots and device memory (LDM + FFT workspace, within `mem_budget` bytes)
- * free up; admitted requests run concurrently on the device.  Results are
- * copied to each request's host buffer (pinned memory recommended).
+ * free up; admitted requests run concurrently on the device.  Each result is
+ * copied device -> pinned staging buffer of its slot (asynchronous) and, once
+ * the request is complete, to the request's host buffer (any host memory).
  * ------------------------------------------------------------------------- */
 typedef struct rg_server rg_server;
 
@@ -233,6 +234,9 @@ typedef struct {
 typedef struct {
     int64_t submitted, completed, failed, in_flight, queued;
     int64_t device_bytes;      /* workspace currently held by the slots         */
+    /* worker thread host time so far (ms): sizing requests (grid, memory),
+     * launching them, copying results to the callers' buffers */
+    double host_need_ms, host_launch_ms, host_copy_ms;
 } rg_server_stats;
 
 int rg_server_create(rg_ctx* ctx, int slots, int64_t mem_budget, rg_server** out);

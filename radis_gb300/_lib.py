@@ -80,7 +80,8 @@ class Request(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
-                ("in_flight", C.c_int64), ("queued", C.c_int64), ("device_bytes", C.c_int64)]
+                ("in_flight", C.c_int64), ("queued", C.c_int64), ("device_bytes", C.c_int64),
+                ("host_need_ms", C.c_double), ("host_launch_ms", C.c_double), ("host_copy_ms", C.c_double)]
 
 
 _lib = None

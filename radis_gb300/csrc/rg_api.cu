@@ -123,7 +123,8 @@ struct Work {
     int* cmax_dev = nullptr;
     int64_t cmax_host = -1;           // known on the host (plans), -1 otherwise
     // grow-only buffers
-    int nodes_cap = 0;
+    int nodes_cap = 0;                // node rows the LDM / FFT workspace holds at this geometry
+    size_t ldm_bytes = 0, y_bytes = 0;   // allocated sizes of ldm and y
     int64_t row_stride = 0;
     unsigned* ldm = nullptr;          // LDM as fixed-point words of the scatter
     float2* y = nullptr;
@@ -412,19 +413,28 @@ int build_envelope(const rg_line_arrays* in, const rg_isotopes* iso, Envelope* E
     return RG_OK;
 }
 
-// Grow-only LDM / FFT workspace for n_nodes (x1.25 margin), stream ordered.
+// LDM / FFT workspace for n_nodes rows at the current geometry (row_stride,
+// n), stream ordered.  The buffers grow by bytes (x1.25 margin) and are
+// reused across geometries, so a server slot that runs requests of many sizes
+// reallocates only when a request is larger than any before it.
 int ensure_workspace(Work& W, int n_nodes, cudaStream_t st) {
-    if (n_nodes <= W.nodes_cap) return RG_OK;
-    int cap = std::min(kMaxNodes, std::max(n_nodes, (int)(W.nodes_cap * 1.25) + 2));
-    cap = (cap + 1) & ~1;
-    if (W.ldm) CU(cudaFreeAsync(W.ldm, st));
-    if (W.y) CU(cudaFreeAsync(W.y, st));
-    W.ldm = nullptr;
-    W.y = nullptr;
-    W.nodes_cap = 0;
-    CU(cudaMallocAsync((void**)&W.ldm, sizeof(unsigned) * (size_t)cap * W.row_stride, st));
-    CU(cudaMallocAsync((void**)&W.y, sizeof(float2) * (size_t)(cap / 2) * W.n, st));
-    W.nodes_cap = cap;
+    const size_t per_l = sizeof(unsigned) * (size_t)W.row_stride, per_y = sizeof(float2) * (size_t)W.n;
+    auto fits = [&](int nodes) { return nodes * per_l <= W.ldm_bytes && (size_t)(nodes / 2) * per_y <= W.y_bytes; };
+    if (!fits(n_nodes)) {
+        const size_t want_l = std::max<size_t>((size_t)n_nodes * per_l, (size_t)(W.ldm_bytes * 1.25));
+        const size_t want_y = std::max<size_t>((size_t)(n_nodes / 2) * per_y, (size_t)(W.y_bytes * 1.25));
+        if (W.ldm) CU(cudaFreeAsync(W.ldm, st));
+        if (W.y) CU(cudaFreeAsync(W.y, st));
+        W.ldm = nullptr;
+        W.y = nullptr;
+        W.ldm_bytes = W.y_bytes = 0;
+        W.nodes_cap = 0;
+        CU(cudaMallocAsync((void**)&W.ldm, want_l, st));
+        W.ldm_bytes = want_l;
+        CU(cudaMallocAsync((void**)&W.y, want_y, st));
+        W.y_bytes = want_y;
+    }
+    W.nodes_cap = (int)std::min<size_t>(W.ldm_bytes / per_l, 2 * (W.y_bytes / per_y)) & ~1;
     return RG_OK;
 }
 
@@ -912,6 +922,15 @@ int rg_ctx_create(int device, rg_ctx** out) {
         delete c;
         return fail(RG_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
     }
+    // workspaces come from the device's default stream-ordered pool: keep freed
+    // blocks cached in this process (no return to the driver at every
+    // synchronisation) so plans and server slots of changing sizes reuse them;
+    // trimmed when the context is destroyed
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+        uint64_t keep = std::numeric_limits<uint64_t>::max();
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     *out = c;
     return RG_OK;
 }
@@ -924,6 +943,11 @@ int rg_ctx_destroy(rg_ctx* c) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     cudaStreamDestroy(c->stream);
+    cudaMemPool_t pool;   // hand the cached pool memory back
+    if (cudaDeviceGetDefaultMemPool(&pool, c->device) == cudaSuccess) {
+        cudaDeviceSynchronize();
+        cudaMemPoolTrimTo(pool, 0);
+    }
     c->magic = 0;
     delete c;
     return RG_OK;
@@ -1112,6 +1136,7 @@ void free_work(Work& W) {
     if (W.err_host) cudaFreeHost(W.err_host);
     W.err_host = nullptr;
     W.nodes_cap = 0;
+    W.ldm_bytes = W.y_bytes = 0;
 }
 
 int rg_plan_free(rg_plan* P) {
@@ -1317,11 +1342,16 @@ struct Slot {
     Work w;
     float* out_d = nullptr;
     int64_t out_cap = 0, col_cap = 0, g_cap = 0;
+    // pinned staging of the spectrum: the device-to-host copy of a request
+    // stays asynchronous (a copy into pageable caller memory would block the
+    // worker until the request finished); copied to the caller at harvest
+    float* pin = nullptr;
+    int64_t pin_cap = 0;
     std::shared_ptr<ServerReq> req;       // owned by the worker thread
     std::atomic<bool> notified{false};    // set by the stream's host callback
     size_t bytes() const {
         return (size_t)out_cap * 4 + (size_t)col_cap * 8 + (size_t)g_cap * 8 +
-               (size_t)w.nodes_cap * ((size_t)w.row_stride * 4 + (size_t)w.n * 4);
+               w.ldm_bytes + w.y_bytes;
     }
 };
 
@@ -1344,6 +1374,8 @@ struct rg_server {
     std::condition_variable cv_sig;
     uint64_t sig_count = 0;                // guarded by sig_mu
     std::atomic<int64_t> dev_bytes{0};
+    // worker host time (seconds): request sizing, launching, result copies
+    std::atomic<double> t_need{0.0}, t_launch{0.0}, t_copy{0.0};
     std::thread worker;
     bool stop = false;
     int64_t next_ticket = 1, completed = 0, failed = 0;
@@ -1446,6 +1478,7 @@ void release_slot_buffers(Slot& sl) {
     sl.w.col_start = nullptr;
     sl.out_d = nullptr;
     sl.w.nodes_cap = 0;
+    sl.w.ldm_bytes = sl.w.y_bytes = 0;
     sl.out_cap = sl.col_cap = sl.g_cap = 0;
 }
 
@@ -1454,7 +1487,6 @@ int start_on_slot(rg_server* S, int si, const std::shared_ptr<ServerReq>& r, con
     Slot& sl = S->slots[si];
     Work& W = sl.w;
     const rg_plan_desc& d = r->desc;
-    const bool new_geom = W.n != (int64_t)n1 * n2 || W.row_stride != (d.n_v + 31) / 32 * 32;
     W.desc = d;
     W.n1 = n1;
     W.n2 = n2;
@@ -1464,22 +1496,23 @@ int start_on_slot(rg_server* S, int si, const std::shared_ptr<ServerReq>& r, con
     shift_margin(r->lines, d.dv, &W.E, &W.p_atm_max);
     W.col_off = W.E;
     W.col_count = (int)d.n_v + 1 + 2 * W.E;
-    if (new_geom) {   // LDM rows / FFT rows change shape: drop the node buffers
-        if (W.ldm) CU(cudaFreeAsync(W.ldm, sl.st));
-        if (W.y) CU(cudaFreeAsync(W.y, sl.st));
-        W.ldm = nullptr;
-        W.y = nullptr;
-        W.nodes_cap = 0;
-    }
     W.row_stride = (d.n_v + 31) / 32 * 32;
     RG(grow(&W.col_start, &sl.col_cap, W.col_count, sl.st));
     RG(grow(&W.g, &sl.g_cap, W.n, sl.st));
     RG(grow(&sl.out_d, &sl.out_cap, d.n_v, sl.st));
+    if (d.n_v > sl.pin_cap) {   // grow-only, at least 2M points (8 MB)
+        const int64_t cap = std::max<int64_t>({d.n_v, sl.pin_cap * 3 / 2, (int64_t)1 << 21});
+        if (sl.pin) CU(cudaFreeHost(sl.pin));
+        sl.pin = nullptr;
+        sl.pin_cap = 0;
+        CU(cudaHostAlloc((void**)&sl.pin, sizeof(float) * (size_t)cap, cudaHostAllocDefault));
+        sl.pin_cap = cap;
+    }
     const rg_lines* L = r->lines;
     RG(launch_col_index(L->v0, L->n, d.vmin, d.dv, -W.E, W.col_count, W.col_start, sl.st));
     RG(launch_col_cmax(W.col_start, W.col_off, W.col_count, (int)d.n_v, W.E, W.cmax_dev, sl.st));
     RG(enqueue_spectrum(L, W, &r->cond, sh, sl.out_d, sl.st, nullptr, false));
-    CU(cudaMemcpyAsync(r->out_host, sl.out_d, sizeof(float) * (size_t)d.n_v, cudaMemcpyDeviceToHost, sl.st));
+    CU(cudaMemcpyAsync(sl.pin, sl.out_d, sizeof(float) * (size_t)d.n_v, cudaMemcpyDeviceToHost, sl.st));
     r->info.grid = sh.grid;
     r->info.log_scale = sh.log_scale_out;
     r->info.lines_in_window = -1;
@@ -1514,6 +1547,11 @@ void worker_loop(rg_server* S) {
             if (sl.notified.load()) {
                 const bool bad = *sl.w.err_host != 0;
                 *sl.w.err_host = 0;
+                if (!bad) {
+                    const double tc = S->now();
+                    std::memcpy(sl.req->out_host, sl.pin, sizeof(float) * (size_t)sl.req->desc.n_v);
+                    S->t_copy.store(S->t_copy.load() + (S->now() - tc));
+                }
                 finished.emplace_back(sl.req, bad);
                 sl.req.reset();
                 sl.notified.store(false);
@@ -1541,7 +1579,9 @@ void worker_loop(rg_server* S) {
                 Start st;
                 int64_t need;
                 g_err.clear();
+                const double tn = S->now();
                 int rc = request_need(S, *r, &st.sh, &need, &st.n1, &st.n2);
+                S->t_need.store(S->t_need.load() + (S->now() - tn));
                 if (rc != RG_OK || need > S->budget) {
                     S->pending.pop_front();
                     finish_request(S, r, rc != RG_OK ? rc : RG_ERR_OOM,
@@ -1558,8 +1598,9 @@ void worker_loop(rg_server* S) {
                     }
                 }
                 if (si < 0) break;
-                const int64_t others = S->used_bytes() - (int64_t)S->slots[si].bytes() + planned;
-                if (others + need > S->budget) {
+                const int64_t held = (int64_t)S->slots[si].bytes();   // buffers are reused, grow-only
+                const int64_t others = S->used_bytes() - held + planned;
+                if (others + std::max(need, held) > S->budget) {
                     // nothing runs: give the idle slots' memory back (outside `mu`), retry
                     if (!any_busy && starts.empty() && S->used_bytes() > 0) release_idle = true;
                     break;
@@ -1584,7 +1625,9 @@ void worker_loop(rg_server* S) {
         for (Start& st : starts) {
             g_err.clear();
             S->slots[st.si].req = st.r;
+            const double tl = S->now();
             const int rc = start_on_slot(S, st.si, st.r, st.sh, st.n1, st.n2);
+            S->t_launch.store(S->t_launch.load() + (S->now() - tl));
             if (rc != RG_OK) {
                 S->slots[st.si].req.reset();
                 const std::string msg = g_err;
@@ -1703,6 +1746,9 @@ int rg_server_stats_get(rg_server* S, rg_server_stats* st) {
     st->submitted = S->next_ticket - 1;
     st->in_flight = st->submitted - st->completed - st->failed - st->queued;
     st->device_bytes = S->dev_bytes.load();
+    st->host_need_ms = S->t_need.load() * 1e3;
+    st->host_launch_ms = S->t_launch.load() * 1e3;
+    st->host_copy_ms = S->t_copy.load() * 1e3;
     return RG_OK;
 }
 
@@ -1725,6 +1771,7 @@ int rg_server_destroy(rg_server* S) {
         dfree(sl.w.counter);
         dfree(sl.w.err);
         if (sl.w.err_host) cudaFreeHost(sl.w.err_host);
+        if (sl.pin) cudaFreeHost(sl.pin);
         cudaStreamDestroy(sl.st);
     }
     for (auto& kv : S->fft) dfree(kv.second.tw);
@@ -1847,9 +1894,11 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
     float2* twl = static_cast<float2*>(take(sizeof(float2) * 1024));
     W.tw_hi = twh;
     W.tw_lo = twl;
-    W.nodes_cap = s.n_nodes;   // sized here: the workspace step allocates nothing
-    W.ldm = static_cast<unsigned*>(take(sizeof(unsigned) * (size_t)s.n_nodes * (size_t)W.row_stride));
-    W.y = static_cast<float2*>(take(sizeof(float2) * (size_t)(s.n_nodes / 2) * (size_t)W.n));
+    // sized here: the workspace step finds them large enough and allocates nothing
+    W.ldm_bytes = sizeof(unsigned) * (size_t)s.n_nodes * (size_t)W.row_stride;
+    W.y_bytes = sizeof(float2) * (size_t)(s.n_nodes / 2) * (size_t)W.n;
+    W.ldm = static_cast<unsigned*>(take(W.ldm_bytes));
+    W.y = static_cast<float2*>(take(W.y_bytes));
     W.g = static_cast<float2*>(take(sizeof(float2) * (size_t)W.n));
     if (off > kStaticScratchBytes)
         return fail(RG_ERR_RANGE,

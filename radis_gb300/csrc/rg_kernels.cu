@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 
 #include "rg_internal.h"
@@ -1309,32 +1310,31 @@ int col_block(int n1) {
 
 // Opt the kernel in to the largest dynamic shared memory the device allows
 // next to the kernel's own static shared memory; checks that `need` fits.
+// (first call per kernel: queries the attributes and sets the limit; later
+// calls only compare `need` with the cached limit)
 template <typename K>
-static int allow_smem(K kernel, bool& done, size_t need) {
-    static int optin = 0;
-    if (!optin) {
-        int dev = 0;
+static int allow_smem(K kernel, std::atomic<size_t>& avail_cache, size_t need) {
+    size_t avail = avail_cache.load();
+    if (!avail) {
+        int dev = 0, optin = 0;
         if (cudaGetDevice(&dev) != cudaSuccess) return RG_ERR_CUDA;
         if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
             return RG_ERR_CUDA;
-    }
-    cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return RG_ERR_CUDA;
-    const size_t avail = (size_t)optin - fa.sharedSizeBytes;
-    if (need > avail) return RG_ERR_RANGE;
-    if (!done) {
+        cudaFuncAttributes fa;
+        if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return RG_ERR_CUDA;
+        avail = (size_t)optin - fa.sharedSizeBytes;
         if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)avail) != cudaSuccess)
             return RG_ERR_CUDA;
-        done = true;
+        avail_cache.store(avail);
     }
-    return RG_OK;
+    return need > avail ? RG_ERR_RANGE : RG_OK;
 }
 
-#define ALLOW_SMEM(kernel, need)                        \
-    do {                                                 \
-        static bool done_ = false;                       \
-        int r_ = allow_smem(kernel, done_, (need));      \
-        if (r_ != RG_OK) return r_;                      \
+#define ALLOW_SMEM(kernel, need)                          \
+    do {                                                   \
+        static std::atomic<size_t> avail_{0};              \
+        int r_ = allow_smem(kernel, avail_, (need));       \
+        if (r_ != RG_OK) return r_;                        \
     } while (0)
 
 int launch_prepare_lines(const double* v0_d, const double* s_d, int64_t n, double c2_tref, float2* v0_out,
@@ -1367,13 +1367,19 @@ int launch_scatter(const ScatterArgs& a, int grid, int threads, size_t smem, cud
 
 // Dynamic shared memory the scatter may have (one CTA per SM).
 int scatter_smem_optin(size_t* avail) {
-    int dev = 0, optin = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return RG_ERR_CUDA;
-    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
-        return RG_ERR_CUDA;
-    cudaFuncAttributes fa;
-    if (cudaFuncGetAttributes(&fa, k_scatter) != cudaSuccess) return RG_ERR_CUDA;
-    *avail = (size_t)optin - fa.sharedSizeBytes;
+    static std::atomic<size_t> cached{0};   // one GPU model per process
+    size_t a = cached.load();
+    if (!a) {
+        int dev = 0, optin = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess) return RG_ERR_CUDA;
+        if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+            return RG_ERR_CUDA;
+        cudaFuncAttributes fa;
+        if (cudaFuncGetAttributes(&fa, k_scatter) != cudaSuccess) return RG_ERR_CUDA;
+        a = (size_t)optin - fa.sharedSizeBytes;
+        cached.store(a);
+    }
+    *avail = a;
     return RG_OK;
 }
 
