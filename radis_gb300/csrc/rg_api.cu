@@ -125,6 +125,10 @@ struct Work {
     // grow-only buffers
     int nodes_cap = 0;                // node rows the LDM / FFT workspace holds at this geometry
     size_t ldm_bytes = 0, y_bytes = 0;   // allocated sizes of ldm and y
+    // merged layout (Gaussian stage in real space): its rows, grow-only
+    bool allow_merge = true;
+    float* mrow = nullptr;
+    size_t mrow_bytes = 0;
     int64_t row_stride = 0;
     unsigned* ldm = nullptr;          // LDM as fixed-point words of the scatter
     float2* y = nullptr;
@@ -594,6 +598,65 @@ void fill_voigt_args(const Work& W, const SpecHost& s, VoigtArgs* va) {
     }
 }
 
+// Merged layout of one spectrum.  Without folding, the Voigt FT of node
+// (l, m) factors into the Gaussian FT of l times the Lorentzian FT of m.
+// Where the Gaussian FT of node l is below 2^-30 at the Nyquist frequency,
+// multiplying by it equals a real-space convolution with the sampled Gaussian
+// profile (its inverse DFT, Poisson summation; truncated where the profile
+// falls below 1e-9 of its peak).  The node rows of those "wide" l are
+// convolved and summed into one row per wL node before the FFT, so only
+// n_L x (1 + narrow l) rows are transformed instead of n_G x n_L; the other
+// rows keep the full Voigt FT.  Used when at least two l are wide.
+bool plan_merge(const Work& W, const SpecHost& s, const VoigtArgs& va, GaussArgs* ga, VoigtArgs* vm,
+                int* out_rows) {
+    if (!W.allow_merge || va.any_fold) return false;
+    const rg_grid& g = s.grid;
+    const double dv = W.desc.dv;
+    std::memset(ga, 0, sizeof *ga);
+    int K_max = 0;
+    for (int l = 0; l < g.n_G; ++l) {
+        const double wG = std::exp(g.log_wG_min + l * g.dxG);
+        const double nyq = std::pow(kPi * wG / (2.0 * dv), 2) / (4.0 * kLn2) * kLog2e;   // -log2 G(f_nyq)
+        const int K = (int)std::ceil(2.7284 * wG / dv);   // exp(-4 ln2 (K dv / wG)^2) <= 1e-9
+        if (nyq >= 30.0 && K <= kGaussMaxK) {
+            const int w = ga->n_wide++;
+            ga->wide_l[w] = l;
+            ga->K[w] = K;
+            ga->c[w] = (float)(dv * 2.0 * std::sqrt(kLn2 / kPi) / wG);
+            ga->a2[w] = (float)(4.0 * kLn2 * (dv / wG) * (dv / wG) * kLog2e);
+            K_max = std::max(K_max, K);
+        } else {
+            ga->narrow_l[ga->n_narrow++] = l;
+        }
+    }
+    if (ga->n_wide < 2) return false;
+    const int NL = g.n_L;
+    ga->NL = NL;
+    ga->rows = NL * (1 + ga->n_narrow);
+    *out_rows = (ga->rows + 1) & ~1;
+    ga->n_v = (int)W.desc.n_v;
+    ga->ext = K_max;
+    ga->out_stride = (ga->n_v + 2 * K_max + 31) / 32 * 32;
+    ga->ldm = W.ldm;
+    ga->row_stride = W.row_stride;
+    ga->cmax = W.cmax_dev;
+    *vm = va;
+    vm->n_nodes = *out_rows;
+    vm->n_pairs = *out_rows / 2;
+    vm->NL = NL;
+    vm->alpha[0] = 0.f;   // merged rows: the Gaussian factor is applied already
+    for (int i = 0; i < ga->n_narrow; ++i) vm->alpha[1 + i] = va.alpha[ga->narrow_l[i]];
+    vm->alpha[1 + ga->n_narrow] = 0.f;
+    for (int r = 0; r < *out_rows; ++r) {
+        const bool real = r < ga->rows;
+        vm->norm[r] = real ? 1.f : 0.f;   // no folding: 1 / V(0) = 1
+        vm->lnorm[r] = real ? 0.f : -std::numeric_limits<float>::infinity();
+        vm->nfold[r] = 0;
+    }
+    vm->any_fold = 0;
+    return true;
+}
+
 // After a synchronisation: report (once) a bounded device wait that gave up.
 int take_err(Work& W) {
     if (*W.err_host) {
@@ -639,14 +702,36 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
         ca.y = W.y;
         ca.tw_hi = W.tw_hi;
         ca.tw_lo = W.tw_lo;
-        RG(launch_col_fft_fwd(ca, st));
+        auto va = std::make_unique<VoigtArgs>();
+        auto vm = std::make_unique<VoigtArgs>();
+        auto ga = std::make_unique<GaussArgs>();
+        fill_voigt_args(W, s, va.get());
+        int m_rows = 0;
+        const bool merged = plan_merge(W, s, *va, ga.get(), vm.get(), &m_rows);
+        if (merged) {
+            const size_t need = sizeof(float) * (size_t)m_rows * (size_t)ga->out_stride;
+            if (need > W.mrow_bytes) {
+                const size_t want = std::max(need, (size_t)(W.mrow_bytes * 1.25));
+                if (W.mrow) CU(cudaFreeAsync(W.mrow, st));
+                W.mrow = nullptr;
+                W.mrow_bytes = 0;
+                CU(cudaMallocAsync((void**)&W.mrow, want, st));
+                W.mrow_bytes = want;
+            }
+            ga->out = W.mrow;
+            RG(launch_gauss_merge(*ga, m_rows, st));
+            ColFftArgs cm = ca;
+            cm.src = W.mrow;
+            cm.row_stride = ga->out_stride;
+            cm.ext = ga->ext;
+            cm.n_pairs = m_rows / 2;
+            RG(launch_col_fft_fwd_f(cm, st));
+        } else {
+            RG(launch_col_fft_fwd(ca, st));
+        }
         if (ev) CU(cudaEventRecord(ev[2], st));
-        VoigtArgs* va = new (std::nothrow) VoigtArgs();
-        if (!va) return fail(RG_ERR_OOM, "host allocation failed");
-        std::unique_ptr<VoigtArgs> vguard(va);
-        fill_voigt_args(W, s, va);
         CU(cudaMemsetAsync(W.g, 0, sizeof(float2) * (size_t)W.n, st));
-        RG(launch_row_fft_voigt(*va, st));
+        RG(launch_row_fft_voigt(merged ? *vm : *va, st));
         if (ev) CU(cudaEventRecord(ev[3], st));
         RowIfftArgs ra;
         ra.f2 = W.f2;
@@ -1137,6 +1222,8 @@ void free_work(Work& W) {
     W.err_host = nullptr;
     W.nodes_cap = 0;
     W.ldm_bytes = W.y_bytes = 0;
+    dfree(W.mrow);
+    W.mrow_bytes = 0;
 }
 
 int rg_plan_free(rg_plan* P) {
@@ -1351,7 +1438,7 @@ struct Slot {
     std::atomic<bool> notified{false};    // set by the stream's host callback
     size_t bytes() const {
         return (size_t)out_cap * 4 + (size_t)col_cap * 8 + (size_t)g_cap * 8 +
-               w.ldm_bytes + w.y_bytes;
+               w.ldm_bytes + w.y_bytes + w.mrow_bytes;
     }
 };
 
@@ -1448,7 +1535,8 @@ int request_need(rg_server* S, const ServerReq& r, SpecHost* sh, int64_t* need, 
     double pmax;
     shift_margin(r.lines, r.desc.dv, &E, &pmax);
     *need = r.desc.n_v * 4 + (r.desc.n_v + 1 + 2 * (int64_t)E) * 8 + n * 8 +
-            (int64_t)sh->n_nodes * (rs * 4 + n * 4);
+            (int64_t)sh->n_nodes * (rs * 4 + n * 4) +
+            (int64_t)sh->n_nodes * (rs + 2 * kGaussMaxK + 32) * 4;   // merged rows (at most one per node)
     *n1o = n1;
     *n2o = n2;
     (void)S;
@@ -1477,6 +1565,9 @@ void release_slot_buffers(Slot& sl) {
     sl.w.g = nullptr;
     sl.w.col_start = nullptr;
     sl.out_d = nullptr;
+    if (sl.w.mrow) cudaFreeAsync(sl.w.mrow, sl.st);
+    sl.w.mrow = nullptr;
+    sl.w.mrow_bytes = 0;
     sl.w.nodes_cap = 0;
     sl.w.ldm_bytes = sl.w.y_bytes = 0;
     sl.out_cap = sl.col_cap = sl.g_cap = 0;
@@ -1894,7 +1985,9 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
     float2* twl = static_cast<float2*>(take(sizeof(float2) * 1024));
     W.tw_hi = twh;
     W.tw_lo = twl;
-    // sized here: the workspace step finds them large enough and allocates nothing
+    // sized here: the workspace step finds them large enough and allocates nothing;
+    // the merged layout (its own row buffer) is not used on this path
+    W.allow_merge = false;
     W.ldm_bytes = sizeof(unsigned) * (size_t)s.n_nodes * (size_t)W.row_stride;
     W.y_bytes = sizeof(float2) * (size_t)(s.n_nodes / 2) * (size_t)W.n;
     W.ldm = static_cast<unsigned*>(take(W.ldm_bytes));

@@ -147,6 +147,8 @@ struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
     const float* src;     // K2 input rows [node][row_stride] (float), or one row when single
     int single;           // K2: one real row (partner row zero), n_pairs = 1
     int twiddle;          // K2: apply the four-step twiddle (row kernel without table)
+    int ext;              // K2 float rows: 0, or the rows hold k in [-ext, n_v + ext) at offset k + ext
+                          // (circular: k < 0 is FFT index n + k)
 };
 
 struct VoigtArgs {        // K3 (row FFT + Voigt weights + pair reduction)
@@ -181,6 +183,28 @@ struct RowIfftArgs {      // K3b (inverse row FFT + twiddle, in place)
     float2* g;
     const float2* tw_hi;
     const float2* tw_lo;
+};
+
+// Gaussian stage of the merged layout: node rows of equal wL whose Gaussian
+// FT is negligible at the Nyquist frequency are convolved in real space with
+// their Gaussian kernel and summed into one row per wL node; the other
+// (narrow-Gaussian) node rows are copied.  Output rows [row][out_stride]
+// hold k in [-ext, n_v + ext) at offset k + ext.
+constexpr int kGaussPer = 8;          // outputs per thread
+constexpr int kGaussTile = 256 * kGaussPer;   // outputs per CTA (256 threads)
+constexpr int kGaussMaxK = 256;       // widest kernel half-width (points)
+struct GaussArgs {
+    const unsigned* ldm;  // fixed-point LDM words [node][row_stride]
+    int64_t row_stride;
+    const int* cmax;      // fixed-point bound (scale)
+    float* out;
+    int64_t out_stride;
+    int n_v, ext, NL;
+    int rows;             // real output rows: NL (merged) + NL * n_narrow; rows beyond are zero
+    int n_wide, n_narrow;
+    int wide_l[kMaxAxis], K[kMaxAxis];       // wide nodes and kernel half-widths
+    float c[kMaxAxis], a2[kMaxAxis];         // taps c ex2(-a2 j^2), |j| <= K
+    int narrow_l[kMaxAxis];
 };
 
 struct AdjRowArgs {       // adjoint row stage: per pair, IFFT_row(Ghat (V_a + i V_b)) x twiddle
@@ -233,6 +257,7 @@ int launch_col_fft_fwd_f(const ColFftArgs& a, cudaStream_t st);
 int launch_row_ifft_adj(const AdjRowArgs& a, cudaStream_t st);
 int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st);
 int launch_gather_grad(const GradArgs& a, int grid, cudaStream_t st);
+int launch_gauss_merge(const GaussArgs& a, int out_rows, cudaStream_t st);
 int launch_scatter_tangent(const GradArgs& a, int grid, cudaStream_t st);
 int col_block(int n1);               // columns per CTA of the column FFTs
 int row_threads(const FftLen& f);    // block size of the forward row kernel

@@ -1097,10 +1097,140 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_fft_fwd_f(const C
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int64_t nidx = (int64_t)(j + q * TPC) * a.n2 + n2i;
-        v[q] = nidx < a.n_v ? make_float2(__ldg(&ra[nidx]), rb ? __ldg(&rb[nidx]) : 0.f) : make_float2(0.f, 0.f);
+        // buffer offset of FFT index nidx, or -1 where the row is zero
+        int64_t off = -1;
+        if (a.ext == 0) {
+            if (nidx < a.n_v) off = nidx;
+        } else if (nidx < a.n_v + a.ext) {
+            off = nidx + a.ext;
+        } else if (nidx >= a.n - a.ext) {
+            off = nidx - (a.n - a.ext);
+        }
+        v[q] = off >= 0 ? make_float2(__ldg(&ra[off]), rb ? __ldg(&rb[off]) : 0.f) : make_float2(0.f, 0.f);
     }
     col_fft8<N1>(v, sm, j, b, a.f1.tw);
     store_twiddled<N1>(v, a, pair, j, n2i);
+}
+
+// Gaussian stage of the merged layout (see GaussArgs).  One CTA: one output
+// row, kGaussTile consecutive outputs, kGaussPer per thread.  A merged row is
+// sum over wide nodes l of (g_l conv LDM_{l,m}) with the symmetric kernel
+// g_l[j] = c_l 2^(-a2_l j^2), |j| <= K_l, i.e. out[p] = sum_jj g[jj] x[p - ext
+// - K + jj]; each thread keeps its outputs' input window in registers and
+// advances it 8 taps at a time (two half-windows used alternately, so the
+// window never moves between registers).
+template <int P>
+__device__ __forceinline__ void gauss_step(float (&acc)[P], const float (&lo)[P], const float (&hi)[8],
+                                           const float (&g)[8]) {
+    // window = lo[0..P) followed by hi[0..8): acc[i] += sum_u g[u] window[i + u]
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+#pragma unroll
+        for (int i = 0; i < P; ++i) acc[i] = fmaf(g[u], i + u < P ? lo[i + u] : hi[i + u - P], acc[i]);
+}
+
+__device__ __forceinline__ void load8(float (&d)[8], const float* s) {
+    const float4 a = *reinterpret_cast<const float4*>(s);
+    const float4 b = *reinterpret_cast<const float4*>(s + 4);
+    d[0] = a.x; d[1] = a.y; d[2] = a.z; d[3] = a.w;
+    d[4] = b.x; d[5] = b.y; d[6] = b.z; d[7] = b.w;
+}
+
+__global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
+    extern __shared__ __align__(16) float gsm[];
+    constexpr int TW = kGaussTile;
+    constexpr int P = kGaussPer;                     // outputs per thread (multiple of 8)
+    float* taps = gsm;                               // KP <= 2 kGaussMaxK + 16
+    float* xs = gsm + (2 * kGaussMaxK + 16);         // TW + KP + 8 <= TW + 2 kGaussMaxK + 24
+    const int r = blockIdx.y;
+    const int p0 = blockIdx.x * TW;
+    const int Lr = a.n_v + 2 * a.ext;
+    float* orow = a.out + (int64_t)r * a.out_stride;
+    const int lp = r / a.NL, m = r - lp * a.NL;
+    if (r >= a.rows) {
+        for (int p = p0 + threadIdx.x; p < min(p0 + TW, Lr); p += blockDim.x) orow[p] = 0.f;
+        return;
+    }
+    const float inv = 1.f / fx_scale_of(*a.cmax);
+    if (lp > 0) {   // narrow-Gaussian node row: copy (the row FFT applies its full Voigt FT)
+        const unsigned* src = a.ldm + (int64_t)(a.narrow_l[lp - 1] * a.NL + m) * a.row_stride;
+        for (int p = p0 + threadIdx.x; p < min(p0 + TW, Lr); p += blockDim.x) {
+            const int k = p - a.ext;
+            orow[p] = (k >= 0 && k < a.n_v) ? (float)__ldg(&src[k]) * inv : 0.f;
+        }
+        return;
+    }
+    float acc[P];
+#pragma unroll
+    for (int i = 0; i < P; ++i) acc[i] = 0.f;
+    const int t0 = threadIdx.x * P;
+    // the next node's input tile is fetched into registers while the current
+    // one is convolved (NPRE words per thread cover TW + KP + 8 <= the xs buffer)
+    constexpr int NPRE = (TW + 2 * kGaussMaxK + 24 + 255) / 256;
+    unsigned pre[NPRE];
+    auto fetch = [&](int w) {
+        const int K = a.K[w];
+        const int KP = (2 * K + 1 + 15) & ~15;
+        const unsigned* src = a.ldm + (int64_t)(a.wide_l[w] * a.NL + m) * a.row_stride;
+        const int base = p0 - a.ext - K;   // LDM index of xs[0]
+#pragma unroll
+        for (int u = 0; u < NPRE; ++u) {
+            const int q = threadIdx.x + u * 256;
+            const int k = base + q;
+            pre[u] = (q < TW + KP + 8 && k >= 0 && k < a.n_v) ? __ldg(&src[k]) : 0u;
+        }
+    };
+    fetch(0);
+    for (int w = 0; w < a.n_wide; ++w) {
+        const int K = a.K[w];
+        const int KP = (2 * K + 1 + 15) & ~15;   // taps padded with zeros to a multiple of 16
+        __syncthreads();   // previous node's taps and tile consumed
+        for (int jj = threadIdx.x; jj < KP; jj += blockDim.x) {
+            const float j = (float)(jj - K);
+            taps[jj] = jj <= 2 * K ? a.c[w] * ex2(-a.a2[w] * j * j) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < NPRE; ++u) {
+            const int q = threadIdx.x + u * 256;
+            if (q < TW + KP + 8) xs[q] = (float)pre[u] * inv;
+        }
+        if (w + 1 < a.n_wide) fetch(w + 1);
+        __syncthreads();
+        float wa[P], wb[P];
+#pragma unroll
+        for (int i = 0; i < P; i += 8) {
+            float t[8];
+            load8(t, &xs[t0 + i]);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) wa[i + u] = t[u];
+        }
+        for (int jj = 0; jj < KP; jj += 16) {
+            float hi[8], g[8];
+            // taps jj..jj+7: window wa (x[t0 + jj ..]) followed by the next 8
+            load8(hi, &xs[t0 + jj + P]);
+            load8(g, &taps[jj]);
+            gauss_step<P>(acc, wa, hi, g);
+            // shift by 8 into wb: wb = wa[8..P) ++ hi
+#pragma unroll
+            for (int i = 0; i < P; ++i) wb[i] = i + 8 < P ? wa[i + 8] : hi[i + 8 - P];
+            load8(hi, &xs[t0 + jj + 8 + P]);
+            load8(g, &taps[jj + 8]);
+            gauss_step<P>(acc, wb, hi, g);
+#pragma unroll
+            for (int i = 0; i < P; ++i) wa[i] = i + 8 < P ? wb[i + 8] : hi[i + 8 - P];
+        }
+    }
+    const int p = p0 + t0;
+#pragma unroll
+    for (int i = 0; i < P; i += 4) {
+        if (p + i + 4 <= Lr) {
+            *reinterpret_cast<float4*>(&orow[p + i]) = make_float4(acc[i], acc[i + 1], acc[i + 2], acc[i + 3]);
+        } else {
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (p + i + u < Lr) orow[p + i + u] = acc[i + u];
+        }
+    }
 }
 
 // Adjoint row stage, one CTA per (row k1, pair j): H = Ghat (V_2j + i V_2j+1)
@@ -1508,6 +1638,14 @@ int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st) {
         case 512: return col_inv_adj<512>(a, st);
         default: return RG_ERR_RANGE;
     }
+}
+
+int launch_gauss_merge(const GaussArgs& a, int out_rows, cudaStream_t st) {
+    const size_t smem = sizeof(float) * ((2 * kGaussMaxK + 16) + (kGaussTile + 2 * kGaussMaxK + 24));
+    const int Lr = a.n_v + 2 * a.ext;
+    dim3 grid((Lr + kGaussTile - 1) / kGaussTile, out_rows);
+    k_gauss_merge<<<grid, 256, smem, st>>>(a);
+    return check_launch();
 }
 
 int launch_gather_grad(const GradArgs& a, int grid, cudaStream_t st) {
