@@ -1170,7 +1170,7 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
     unsigned pre[NPRE];
     auto fetch = [&](int w) {
         const int K = a.K[w];
-        const int KP = (2 * K + 1 + 15) & ~15;
+        const int KP = (2 * K + 1 + 23) / 24 * 24;
         const unsigned* src = a.ldm + (int64_t)(a.wide_l[w] * a.NL + m) * a.row_stride;
         const int base = p0 - a.ext - K;   // LDM index of xs[0]
 #pragma unroll
@@ -1183,41 +1183,33 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
     fetch(0);
     for (int w = 0; w < a.n_wide; ++w) {
         const int K = a.K[w];
-        const int KP = (2 * K + 1 + 15) & ~15;   // taps padded with zeros to a multiple of 16
+        const int KP = (2 * K + 1 + 23) / 24 * 24;   // taps padded with zeros to a multiple of 24
         __syncthreads();   // previous node's taps and tile consumed
         for (int jj = threadIdx.x; jj < KP; jj += blockDim.x) {
             const float j = (float)(jj - K);
-            taps[jj] = jj <= 2 * K ? a.c[w] * ex2(-a.a2[w] * j * j) : 0.f;
+            taps[jj] = jj <= 2 * K ? a.c[w] * inv * ex2(-a.a2[w] * j * j) : 0.f;   // x inv: xs holds raw words
         }
 #pragma unroll
         for (int u = 0; u < NPRE; ++u) {
             const int q = threadIdx.x + u * 256;
-            if (q < TW + KP + 8) xs[q] = (float)pre[u] * inv;
+            if (q < TW + KP + 8) xs[q] = (float)pre[u];
         }
         if (w + 1 < a.n_wide) fetch(w + 1);
         __syncthreads();
-        float wa[P], wb[P];
-#pragma unroll
-        for (int i = 0; i < P; i += 8) {
-            float t[8];
-            load8(t, &xs[t0 + i]);
-#pragma unroll
-            for (int u = 0; u < 8; ++u) wa[i + u] = t[u];
-        }
-        for (int jj = 0; jj < KP; jj += 16) {
-            float hi[8], g[8];
-            // taps jj..jj+7: window wa (x[t0 + jj ..]) followed by the next 8
-            load8(hi, &xs[t0 + jj + P]);
+        // three 8-value register blocks rotate through the window (no moves):
+        // taps jj..jj+7 use A ++ B, jj+8.. use B ++ C, jj+16.. use C ++ A'
+        float A[8], B[8], C[8], g[8];
+        load8(A, &xs[t0]);
+        for (int jj = 0; jj < KP; jj += 24) {
+            load8(B, &xs[t0 + jj + 8]);
             load8(g, &taps[jj]);
-            gauss_step<P>(acc, wa, hi, g);
-            // shift by 8 into wb: wb = wa[8..P) ++ hi
-#pragma unroll
-            for (int i = 0; i < P; ++i) wb[i] = i + 8 < P ? wa[i + 8] : hi[i + 8 - P];
-            load8(hi, &xs[t0 + jj + 8 + P]);
+            gauss_step<8>(acc, A, B, g);
+            load8(C, &xs[t0 + jj + 16]);
             load8(g, &taps[jj + 8]);
-            gauss_step<P>(acc, wb, hi, g);
-#pragma unroll
-            for (int i = 0; i < P; ++i) wa[i] = i + 8 < P ? wb[i + 8] : hi[i + 8 - P];
+            gauss_step<8>(acc, B, C, g);
+            load8(A, &xs[t0 + jj + 24]);
+            load8(g, &taps[jj + 16]);
+            gauss_step<8>(acc, C, A, g);
         }
     }
     const int p = p0 + t0;
