@@ -603,13 +603,15 @@ void fill_voigt_args(const Work& W, const SpecHost& s, VoigtArgs* va) {
 // Where the Gaussian FT of node l is below 2^-30 at the Nyquist frequency,
 // multiplying by it equals a real-space convolution with the sampled Gaussian
 // profile (its inverse DFT, Poisson summation; truncated where the profile
-// falls below 1e-9 of its peak).  The node rows of those "wide" l are
+// falls below 1e-8 of its peak).  The node rows of those "wide" l are
 // convolved and summed into one row per wL node before the FFT, so only
 // n_L x (1 + narrow l) rows are transformed instead of n_G x n_L; the other
-// rows keep the full Voigt FT.  Used when at least two l are wide.
+// rows keep the full (folded, normalised) Voigt FT.  Wide nodes have no folded
+// copies (their FT is below 2^-30 beyond the Nyquist frequency).  Used when
+// at least two l are wide.
 bool plan_merge(const Work& W, const SpecHost& s, const VoigtArgs& va, GaussArgs* ga, VoigtArgs* vm,
                 int* out_rows) {
-    if (!W.allow_merge || va.any_fold) return false;
+    if (!W.allow_merge) return false;
     const rg_grid& g = s.grid;
     const double dv = W.desc.dv;
     std::memset(ga, 0, sizeof *ga);
@@ -617,8 +619,10 @@ bool plan_merge(const Work& W, const SpecHost& s, const VoigtArgs& va, GaussArgs
     for (int l = 0; l < g.n_G; ++l) {
         const double wG = std::exp(g.log_wG_min + l * g.dxG);
         const double nyq = std::pow(kPi * wG / (2.0 * dv), 2) / (4.0 * kLn2) * kLog2e;   // -log2 G(f_nyq)
-        const int K = (int)std::ceil(2.7284 * wG / dv);   // exp(-4 ln2 (K dv / wG)^2) <= 1e-9
-        if (nyq >= 30.0 && K <= kGaussMaxK) {
+        const int K = (int)std::ceil(2.5770 * wG / dv);   // exp(-4 ln2 (K dv / wG)^2) <= 1e-8
+        bool unfolded = true;   // folded copies are below 2^-30 here unless the threshold is lower still
+        for (int m = 0; m < g.n_L; ++m) unfolded &= va.nfold[l * g.n_L + m] == 0;
+        if (nyq >= 30.0 && K <= kGaussMaxK && unfolded) {
             const int w = ga->n_wide++;
             ga->wide_l[w] = l;
             ga->K[w] = K;
@@ -629,7 +633,7 @@ bool plan_merge(const Work& W, const SpecHost& s, const VoigtArgs& va, GaussArgs
             ga->narrow_l[ga->n_narrow++] = l;
         }
     }
-    if (ga->n_wide < 2) return false;
+    if (ga->n_wide < 2 || g.n_L % 2) return false;   // pairs must not straddle merged and narrow rows
     const int NL = g.n_L;
     ga->NL = NL;
     ga->rows = NL * (1 + ga->n_narrow);
@@ -648,14 +652,27 @@ bool plan_merge(const Work& W, const SpecHost& s, const VoigtArgs& va, GaussArgs
     for (int i = 0; i < ga->n_narrow; ++i) vm->alpha[1 + i] = va.alpha[ga->narrow_l[i]];
     vm->alpha[1 + ga->n_narrow] = 0.f;
     for (int r = 0; r < *out_rows; ++r) {
-        const bool real = r < ga->rows;
-        vm->norm[r] = real ? 1.f : 0.f;   // no folding: 1 / V(0) = 1
-        vm->lnorm[r] = real ? 0.f : -std::numeric_limits<float>::infinity();
-        vm->nfold[r] = 0;
+        if (r < NL) {   // merged rows: unfolded, 1 / V(0) = 1
+            vm->norm[r] = 1.f;
+            vm->lnorm[r] = 0.f;
+            vm->nfold[r] = 0;
+        } else if (r < ga->rows) {   // narrow node rows keep their folded, normalised Voigt FT
+            const int node = ga->narrow_l[r / NL - 1] * NL + r % NL;
+            vm->norm[r] = va.norm[node];
+            vm->lnorm[r] = va.lnorm[node];
+            vm->nfold[r] = va.nfold[node];
+        } else {
+            vm->norm[r] = 0.f;
+            vm->lnorm[r] = -std::numeric_limits<float>::infinity();
+            vm->nfold[r] = 0;
+        }
     }
-    vm->any_fold = 0;
     return true;
 }
+
+// rows the Gaussian stage writes (one per wL node; the narrow rows are read
+// from the LDM by the column FFT directly)
+int NL_merged(const GaussArgs& ga) { return ga.NL; }
 
 // After a synchronisation: report (once) a bounded device wait that gave up.
 int take_err(Work& W) {
@@ -709,7 +726,7 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
         int m_rows = 0;
         const bool merged = plan_merge(W, s, *va, ga.get(), vm.get(), &m_rows);
         if (merged) {
-            const size_t need = sizeof(float) * (size_t)m_rows * (size_t)ga->out_stride;
+            const size_t need = sizeof(float) * (size_t)NL_merged(*ga) * (size_t)ga->out_stride;
             if (need > W.mrow_bytes) {
                 const size_t want = std::max(need, (size_t)(W.mrow_bytes * 1.25));
                 if (W.mrow) CU(cudaFreeAsync(W.mrow, st));
@@ -719,13 +736,22 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
                 W.mrow_bytes = want;
             }
             ga->out = W.mrow;
-            RG(launch_gauss_merge(*ga, m_rows, st));
-            ColFftArgs cm = ca;
+            RG(launch_gauss_merge(*ga, NL_merged(*ga), st));
+            ColFftArgs cm = ca;   // merged rows (float, extended): pairs [0, n_L / 2)
             cm.src = W.mrow;
             cm.row_stride = ga->out_stride;
             cm.ext = ga->ext;
-            cm.n_pairs = m_rows / 2;
+            cm.n_pairs = ga->NL / 2;
             RG(launch_col_fft_fwd_f(cm, st));
+            if (ga->n_narrow) {   // narrow node rows straight from the LDM: the following pairs
+                ColFftArgs cn = ca;
+                cn.pair_base = ga->NL / 2;
+                cn.n_pairs = ga->n_narrow * ga->NL / 2;
+                cn.map_n = ga->n_narrow;
+                cn.map_NL = ga->NL;
+                for (int i = 0; i < ga->n_narrow; ++i) cn.map_l[i] = (unsigned char)ga->narrow_l[i];
+                RG(launch_col_fft_fwd(cn, st));
+            }
         } else {
             RG(launch_col_fft_fwd(ca, st));
         }

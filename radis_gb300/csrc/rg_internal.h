@@ -149,6 +149,10 @@ struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
     int twiddle;          // K2: apply the four-step twiddle (row kernel without table)
     int ext;              // K2 float rows: 0, or the rows hold k in [-ext, n_v + ext) at offset k + ext
                           // (circular: k < 0 is FFT index n + k)
+    int pair_base;        // K2: first output pair in y
+    int map_n;            // K2 fixed point: 0, or virtual row v reads LDM node
+    int map_NL;           //   map_l[v / map_NL] * map_NL + v % map_NL (narrow rows of the merged layout)
+    unsigned char map_l[kMaxAxis];
 };
 
 struct VoigtArgs {        // K3 (row FFT + Voigt weights + pair reduction)
@@ -187,8 +191,8 @@ struct RowIfftArgs {      // K3b (inverse row FFT + twiddle, in place)
 
 // Gaussian stage of the merged layout: node rows of equal wL whose Gaussian
 // FT is negligible at the Nyquist frequency are convolved in real space with
-// their Gaussian kernel and summed into one row per wL node; the other
-// (narrow-Gaussian) node rows are copied.  Output rows [row][out_stride]
+// their Gaussian kernel and summed into one row per wL node (the other,
+// narrow-Gaussian node rows stay in the LDM).  Output rows [m][out_stride]
 // hold k in [-ext, n_v + ext) at offset k + ext.
 constexpr int kGaussPer = 8;          // outputs per thread
 constexpr int kGaussTile = 256 * kGaussPer;   // outputs per CTA (256 threads)
@@ -200,7 +204,7 @@ struct GaussArgs {
     float* out;
     int64_t out_stride;
     int n_v, ext, NL;
-    int rows;             // real output rows: NL (merged) + NL * n_narrow; rows beyond are zero
+    int rows;             // rows of the merged layout: NL (merged) + NL * n_narrow (LDM rows)
     int n_wide, n_narrow;
     int wide_l[kMaxAxis], K[kMaxAxis];       // wide nodes and kernel half-widths
     float c[kMaxAxis], a2[kMaxAxis];         // taps c ex2(-a2 j^2), |j| <= K

@@ -631,7 +631,7 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
 template <int N1>
 __device__ __forceinline__ void store_twiddled(float2 (&v)[8], const ColFftArgs& a, int pair, int j, int n2i) {
     constexpr int TPC = ColShape<N1>::TPC;
-    float2* y = a.y + (int64_t)pair * N1 * a.n2;
+    float2* y = a.y + (int64_t)(a.pair_base + pair) * N1 * a.n2;
     if (a.twiddle) {
         float2 w = twiddle_n(a.tw_hi, a.tw_lo, n2i * j);
         const float2 step = twiddle_n(a.tw_hi, a.tw_lo, n2i * TPC);
@@ -655,8 +655,9 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS, 3) k_col_fft_fwd(const 
     const int c0 = blockIdx.x * B;
     const int pair = blockIdx.y;
     // the LDM holds the scatter's fixed-point words: value = word / fx_scale
-    const unsigned* ra = a.ldm + (int64_t)(2 * pair) * a.row_stride;
-    const unsigned* rb = ra + a.row_stride;
+    auto node_of = [&](int v) { return a.map_n ? a.map_l[v / a.map_NL] * a.map_NL + v % a.map_NL : v; };
+    const unsigned* ra = a.ldm + (int64_t)node_of(2 * pair) * a.row_stride;
+    const unsigned* rb = a.ldm + (int64_t)node_of(2 * pair + 1) * a.row_stride;
     const float inv = 1.f / fx_scale_of(*a.cmax);
     const int n2i = c0 + b;
     float2 v[8];
@@ -1112,8 +1113,8 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_fft_fwd_f(const C
     store_twiddled<N1>(v, a, pair, j, n2i);
 }
 
-// Gaussian stage of the merged layout (see GaussArgs).  One CTA: one output
-// row, kGaussTile consecutive outputs, kGaussPer per thread.  A merged row is
+// Gaussian stage of the merged layout (see GaussArgs).  One CTA: one merged
+// row (wL node), kGaussTile consecutive outputs, kGaussPer per thread.  A merged row is
 // sum over wide nodes l of (g_l conv LDM_{l,m}) with the symmetric kernel
 // g_l[j] = c_l 2^(-a2_l j^2), |j| <= K_l, i.e. out[p] = sum_jj g[jj] x[p - ext
 // - K + jj]; each thread keeps its outputs' input window in registers and
@@ -1146,20 +1147,8 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
     const int p0 = blockIdx.x * TW;
     const int Lr = a.n_v + 2 * a.ext;
     float* orow = a.out + (int64_t)r * a.out_stride;
-    const int lp = r / a.NL, m = r - lp * a.NL;
-    if (r >= a.rows) {
-        for (int p = p0 + threadIdx.x; p < min(p0 + TW, Lr); p += blockDim.x) orow[p] = 0.f;
-        return;
-    }
+    const int m = r;   // merged row of wL node m
     const float inv = 1.f / fx_scale_of(*a.cmax);
-    if (lp > 0) {   // narrow-Gaussian node row: copy (the row FFT applies its full Voigt FT)
-        const unsigned* src = a.ldm + (int64_t)(a.narrow_l[lp - 1] * a.NL + m) * a.row_stride;
-        for (int p = p0 + threadIdx.x; p < min(p0 + TW, Lr); p += blockDim.x) {
-            const int k = p - a.ext;
-            orow[p] = (k >= 0 && k < a.n_v) ? (float)__ldg(&src[k]) * inv : 0.f;
-        }
-        return;
-    }
     float acc[P];
 #pragma unroll
     for (int i = 0; i < P; ++i) acc[i] = 0.f;
@@ -1170,7 +1159,7 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
     unsigned pre[NPRE];
     auto fetch = [&](int w) {
         const int K = a.K[w];
-        const int KP = (2 * K + 1 + 23) / 24 * 24;
+        const int KP = (2 * K + 1 + 7) & ~7;
         const unsigned* src = a.ldm + (int64_t)(a.wide_l[w] * a.NL + m) * a.row_stride;
         const int base = p0 - a.ext - K;   // LDM index of xs[0]
 #pragma unroll
@@ -1183,7 +1172,7 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
     fetch(0);
     for (int w = 0; w < a.n_wide; ++w) {
         const int K = a.K[w];
-        const int KP = (2 * K + 1 + 23) / 24 * 24;   // taps padded with zeros to a multiple of 24
+        const int KP = (2 * K + 1 + 7) & ~7;   // taps padded with zeros to a multiple of 8
         __syncthreads();   // previous node's taps and tile consumed
         for (int jj = threadIdx.x; jj < KP; jj += blockDim.x) {
             const float j = (float)(jj - K);
@@ -1197,10 +1186,12 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
         if (w + 1 < a.n_wide) fetch(w + 1);
         __syncthreads();
         // three 8-value register blocks rotate through the window (no moves):
-        // taps jj..jj+7 use A ++ B, jj+8.. use B ++ C, jj+16.. use C ++ A'
+        // taps jj..jj+7 use A ++ B, jj+8.. use B ++ C, jj+16.. use C ++ A';
+        // a tail of 8 or 16 taps ends the row of taps (KP is a multiple of 8)
         float A[8], B[8], C[8], g[8];
         load8(A, &xs[t0]);
-        for (int jj = 0; jj < KP; jj += 24) {
+        int jj = 0;
+        for (; jj + 24 <= KP; jj += 24) {
             load8(B, &xs[t0 + jj + 8]);
             load8(g, &taps[jj]);
             gauss_step<8>(acc, A, B, g);
@@ -1210,6 +1201,16 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
             load8(A, &xs[t0 + jj + 24]);
             load8(g, &taps[jj + 16]);
             gauss_step<8>(acc, C, A, g);
+        }
+        if (jj < KP) {
+            load8(B, &xs[t0 + jj + 8]);
+            load8(g, &taps[jj]);
+            gauss_step<8>(acc, A, B, g);
+            if (jj + 8 < KP) {
+                load8(C, &xs[t0 + jj + 16]);
+                load8(g, &taps[jj + 8]);
+                gauss_step<8>(acc, B, C, g);
+            }
         }
     }
     const int p = p0 + t0;

@@ -86,6 +86,22 @@ def test_isotopes_qratio_shift(ctx):
     assert rel_err(gpu, oracle(lines, *args, info, q=q)) <= TOL
 
 
+def test_merged_layout_wide_and_folded_narrow_nodes(ctx):
+    """Doppler widths from 2 to 7 grid steps at 0.2 bar: the three widest wG
+    nodes go through the real-space Gaussian stage (merged rows), the five
+    narrow ones keep their full Voigt FT, with folded copies active."""
+    lines = S.uniform_lines(30_000, 1500.0, 4500.0, seed=32)
+    args = (18.0, 1500.0, 0.005, 600001, 2000.0, 0.2, 0.2)
+    gpu, info = run_gpu(ctx, lines, *args, n_G=8, n_L=8)
+    g = info.grid
+    wG = O.axis_values(g.log_wG_min, g.dxG, g.n_G)
+    wL = O.axis_values(g.log_wL_min, g.dxL, g.n_L)
+    below = (np.pi * wG / (2 * 0.005)) ** 2 / (4 * np.log(2)) * np.log2(np.e)   # -log2 G(f_Nyquist)
+    assert 2 <= np.sum(below >= 30) < g.n_G
+    assert O.fold_count(0.005, wG[0], wL[0]) > 0
+    assert rel_err(gpu, oracle(lines, *args, info)) <= TOL
+
+
 def test_odd_node_count_padding(ctx):
     lines = S.uniform_lines(20_000, 2000.0, 2020.0, seed=24)
     args = (28.0, 2000.0, 0.001, 20001, 400.0, 0.5, 0.05)
