@@ -120,6 +120,10 @@ typedef struct {
     float stage_ms[6];         /* scatter, fft-col, fft-row+voigt, ifft-row,
                                   ifft-col, total (filled when timing != 0)    */
     int64_t lines_in_window;   /* lines whose k0 >= 0 and k0+1 < n_v          */
+    /* layout of the FFT stage: rows transformed (node rows, or with the merged
+     * layout n_L merged rows + the narrow-Gaussian node rows), how many of them
+     * are merged rows and the half-width (points) of their widest Gaussian */
+    int32_t fft_rows, merged_rows, merged_ext;
 } rg_spectrum_info;
 
 int rg_abi_version(void);

@@ -71,7 +71,8 @@ class Grid(C.Structure):
 
 class SpectrumInfo(C.Structure):
     _fields_ = [("grid", Grid), ("log_scale", C.c_double), ("stage_ms", C.c_float * 6),
-                ("lines_in_window", C.c_int64)]
+                ("lines_in_window", C.c_int64), ("fft_rows", C.c_int32), ("merged_rows", C.c_int32),
+                ("merged_ext", C.c_int32)]
 
 
 class Request(C.Structure):

@@ -129,6 +129,7 @@ struct Work {
     bool allow_merge = true;
     float* mrow = nullptr;
     size_t mrow_bytes = 0;
+    int last_fft_rows = 0, last_merged_rows = 0, last_ext = 0;   // layout of the last spectrum
     int64_t row_stride = 0;
     unsigned* ldm = nullptr;          // LDM as fixed-point words of the scatter
     float2* y = nullptr;
@@ -725,6 +726,9 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
         fill_voigt_args(W, s, va.get());
         int m_rows = 0;
         const bool merged = plan_merge(W, s, *va, ga.get(), vm.get(), &m_rows);
+        W.last_fft_rows = merged ? m_rows : s.n_nodes;
+        W.last_merged_rows = merged ? ga->NL : 0;
+        W.last_ext = merged ? ga->ext : 0;
         if (merged) {
             const size_t need = sizeof(float) * (size_t)NL_merged(*ga) * (size_t)ga->out_stride;
             if (need > W.mrow_bytes) {
@@ -954,6 +958,9 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
         info->grid = s.grid;
         info->log_scale = ldm_only ? s.log_scale_int : s.log_scale_out;
         info->lines_in_window = -1;
+        info->fft_rows = ldm_only ? 0 : P->w.last_fft_rows;
+        info->merged_rows = ldm_only ? 0 : P->w.last_merged_rows;
+        info->merged_ext = ldm_only ? 0 : P->w.last_ext;
     }
     if (timing == 1 && info) {
         CU(cudaStreamSynchronize(st));
@@ -1633,6 +1640,9 @@ int start_on_slot(rg_server* S, int si, const std::shared_ptr<ServerReq>& r, con
     r->info.grid = sh.grid;
     r->info.log_scale = sh.log_scale_out;
     r->info.lines_in_window = -1;
+    r->info.fft_rows = W.last_fft_rows;
+    r->info.merged_rows = W.last_merged_rows;
+    r->info.merged_ext = W.last_ext;
     sl.notified.store(false);
     auto* hn = new HostNote{S, si};
     CU(cudaLaunchHostFunc(sl.st, slot_done_cb, hn));
@@ -2045,6 +2055,7 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
         info->grid = s.grid;
         info->log_scale = s.log_scale_out;
         info->lines_in_window = -1;
+        info->fft_rows = W.last_fft_rows;
     }
     return RG_OK;
 }
