@@ -457,13 +457,14 @@ int scatter_shape(int n_nodes, int* chunk, int* TK, int* stages, size_t* smem) {
         for (int ch : {2048, 1024, 512, 256}) {
             const size_t fixed = scatter_fixed_smem(ch, S);
             if (fixed >= avail) continue;
-            int tk = (int)((avail - fixed) / (4 * (size_t)n_nodes)) / 32 * 32;
+            // tile rows have an odd pitch of tk + 1 words
+            int tk = ((int)((avail - fixed) / (4 * (size_t)n_nodes)) - 1) / 32 * 32;
             tk = std::min(tk, 1024);
             if (tk >= min_tk) {
                 *chunk = ch;
                 *TK = tk;
                 *stages = S;
-                *smem = fixed + (size_t)4 * n_nodes * tk;
+                *smem = fixed + (size_t)4 * n_nodes * (tk + 1);
                 return RG_OK;
             }
         }

@@ -334,15 +334,10 @@ __global__ void k_col_cmax(const int64_t* __restrict__ col_start, int col_off, i
 // ---------------------------------------------------------------------------
 // K1: fused line scaling + LDM scatter into a shared-memory tile
 // ---------------------------------------------------------------------------
-// Tile layout [node][TK] with the columns permuted per node row: the lanes of
-// a warp hold neighbouring (sorted) lines, i.e. the same few columns at random
-// nodes, so an unpermuted tile would pile their atomics onto one bank.  Groups
-// of four columns (one uint4 of the flush) are XOR-swizzled by node & 7 (bank
-// group) and the words inside a group rotated by (node >> 3) & 3, so one
-// column maps to all 32 banks across 32 consecutive nodes.
-__device__ __forceinline__ int tile_addr(int node, int c, int TK) {
-    return node * TK + ((((c >> 2) ^ (node & 7)) << 2) | ((c + (node >> 3)) & 3));
-}
+// Tile layout [node][TK + 1]: the odd row pitch puts column c of node n on
+// bank (n + c) mod 32.  The lanes of a warp hold neighbouring (sorted) lines,
+// i.e. the same few columns at scattered nodes, so their atomics spread over
+// the banks, and every address is a row base plus a column offset.
 
 // --- TMA (cp.async.bulk) + mbarrier helpers ---------------------------------
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -495,19 +490,20 @@ __device__ __forceinline__ unsigned scatter_chunk(const ScatterArgs& a, const St
         const float w10 = tG - w11;          // tG (1 - tL)
         const float w01 = tL - w11;          // (1 - tG) tL
         const float w00 = 1.f - tG - w01;    // (1 - tG)(1 - tL)
-        const int n00 = l0 * a.NL + m0;
-        const int n10 = n00 + a.NL;
+        const int pitch = a.TK + 1;
+        const int dL = a.NL * pitch;                          // next wG node
+        unsigned* t = tile + (l0 * a.NL + m0) * pitch + c0;   // (l0, m0) at column c0
         if (own0) {
-            atomicAdd(&tile[tile_addr(n00, c0, a.TK)], __float2uint_rn(I0 * w00));
-            atomicAdd(&tile[tile_addr(n00 + 1, c0, a.TK)], __float2uint_rn(I0 * w01));
-            atomicAdd(&tile[tile_addr(n10, c0, a.TK)], __float2uint_rn(I0 * w10));
-            atomicAdd(&tile[tile_addr(n10 + 1, c0, a.TK)], __float2uint_rn(I0 * w11));
+            atomicAdd(t, __float2uint_rn(I0 * w00));
+            atomicAdd(t + pitch, __float2uint_rn(I0 * w01));
+            atomicAdd(t + dL, __float2uint_rn(I0 * w10));
+            atomicAdd(t + dL + pitch, __float2uint_rn(I0 * w11));
         }
         if (own1) {
-            atomicAdd(&tile[tile_addr(n00, c0 + 1, a.TK)], __float2uint_rn(I1 * w00));
-            atomicAdd(&tile[tile_addr(n00 + 1, c0 + 1, a.TK)], __float2uint_rn(I1 * w01));
-            atomicAdd(&tile[tile_addr(n10, c0 + 1, a.TK)], __float2uint_rn(I1 * w10));
-            atomicAdd(&tile[tile_addr(n10 + 1, c0 + 1, a.TK)], __float2uint_rn(I1 * w11));
+            atomicAdd(t + 1, __float2uint_rn(I1 * w00));
+            atomicAdd(t + 1 + pitch, __float2uint_rn(I1 * w01));
+            atomicAdd(t + 1 + dL, __float2uint_rn(I1 * w10));
+            atomicAdd(t + 1 + dL + pitch, __float2uint_rn(I1 * w11));
         }
     }
     return counted;
@@ -527,12 +523,12 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
     const size_t sb = scatter_stage_bytes(ch);
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + S * sb);
     int2* rng = reinterpret_cast<int2*>(smem + S * sb + 8 * kScatMaxStages);
-    uint4* tile4 = reinterpret_cast<uint4*>(smem + scatter_fixed_smem(ch, S));
-    unsigned* tile = reinterpret_cast<unsigned*>(tile4);
+    unsigned* tile = reinterpret_cast<unsigned*>(smem + scatter_fixed_smem(ch, S));
+    const int pitch = a.TK + 1;
     const int G = gridDim.x;
     const int nq = (a.n_tiles - (int)blockIdx.x + G - 1) / G;   // tiles of this CTA (<= kScatMaxTilesPerCta)
     const float fxs = fx_scale_of(*a.cmax);
-    const int n4 = a.n_nodes * a.TK / 4;
+    const int n_words = a.n_nodes * pitch;
     const bool has_dl = a.dl != nullptr, has_iso = a.iso != nullptr;
 
     auto col_idx = [&](int c) { return max(0, min(c + a.col_off, a.col_count - 1)); };
@@ -543,7 +539,7 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
         const int hi = (int)a.col_start[col_idx(k_start + tk + a.margin_cols)];
         rng[q] = make_int2(lo / kLinePad * kLinePad, hi);   // 16-line aligned start
     }
-    for (int i = threadIdx.x; i < n4; i += blockDim.x) tile4[i] = make_uint4(0u, 0u, 0u, 0u);
+    for (int i = threadIdx.x; i < n_words; i += blockDim.x) tile[i] = 0u;
     if (threadIdx.x == 0) {
         for (int b = 0; b < S; ++b) mbar_init(&bar[b], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -598,22 +594,13 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
         }
         // flush the finished tile as raw fixed-point words (plain stores: this
         // CTA owns its columns; the column FFT converts them) and re-zero it
-        const int tk4 = (tk + 3) >> 2;
-        const int per_row = a.TK >> 2;
         const int lane = threadIdx.x & 31;
         for (int node = threadIdx.x >> 5; node < a.n_nodes; node += blockDim.x >> 5) {
-            uint4* row = tile4 + node * per_row;
-            uint4* dst = reinterpret_cast<uint4*>(a.ldm + node * a.row_stride + k_start);
-            const int sw = node & 7, rot = (node >> 3) & 3;
-            for (int c4 = lane; c4 < tk4; c4 += 32) {
-                const uint4 t = row[c4 ^ sw];   // word w holds column 4 c4 + ((w - rot) & 3)
-                uint4 o;
-                if (rot == 0) o = t;
-                else if (rot == 1) o = make_uint4(t.y, t.z, t.w, t.x);
-                else if (rot == 2) o = make_uint4(t.z, t.w, t.x, t.y);
-                else o = make_uint4(t.w, t.x, t.y, t.z);
-                dst[c4] = o;
-                row[c4 ^ sw] = make_uint4(0u, 0u, 0u, 0u);
+            unsigned* row = tile + node * pitch;
+            unsigned* dst = a.ldm + node * a.row_stride + k_start;
+            for (int c = lane; c < tk; c += 32) {   // one 128-byte store per warp step
+                dst[c] = row[c];
+                row[c] = 0u;
             }
         }
         __syncthreads();
