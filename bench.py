@@ -327,11 +327,17 @@ def run_serving(ctx, L, lists, n_req, slots, seed=11):
         t_b = time.perf_counter()
         _, info = plan.synthesize_host(T, p, x, timing=True)
         plan.close()
-        b = brk.setdefault(name, {"requests": 0, "plan_ms": 0.0, "spectrum_gpu_ms": 0.0, "points": 0})
+        b = brk.setdefault(name, {"requests": 0, "plan_ms": 0.0, "spectrum_gpu_ms": 0.0, "points": 0,
+                                  "stage_ms": [0.0] * 5, "merged": 0, "fft_rows": 0, "nodes": 0})
         b["requests"] += 1
         b["plan_ms"] += (t_b - t_a) * 1e3
         b["spectrum_gpu_ms"] += float(info.stage_ms[5])
         b["points"] += n_v
+        for i in range(5):
+            b["stage_ms"][i] += float(info.stage_ms[i])
+        b["merged"] += int(info.merged_rows > 0)
+        b["fft_rows"] += int(info.fft_rows)
+        b["nodes"] += int(info.grid.n_G * info.grid.n_L)
     return {
         "requests": len(reqs), "slots": slots,
         "served_spectra_per_s": served_sps, "plain_spectra_per_s": plain_sps,
