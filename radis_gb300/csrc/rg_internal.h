@@ -122,9 +122,10 @@ constexpr int kScatMaxTilesPerCta = 512;
 #endif
 constexpr int kScatMaxStages = 4;
 RG_HD inline size_t scatter_stage_bytes(int chunk) { return (size_t)33 * chunk; }
-// stage ring, its mbarriers (one 32-byte block) and the per-tile line ranges
+// stage ring, its full and empty mbarriers (one 64-byte block) and the
+// per-tile line ranges
 RG_HD inline size_t scatter_fixed_smem(int chunk, int stages) {
-    return stages * scatter_stage_bytes(chunk) + 8 * kScatMaxStages + 8 * kScatMaxTilesPerCta;
+    return stages * scatter_stage_bytes(chunk) + 16 * kScatMaxStages + 8 * kScatMaxTilesPerCta;
 }
 
 struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)

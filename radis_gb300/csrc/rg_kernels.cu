@@ -365,6 +365,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
 // Bounded wait (about one second of SM clocks); false when it gives up.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
     const long long t0 = clock64();
@@ -465,9 +468,9 @@ __device__ __forceinline__ float line_intensity(const ScatterArgs& a, float v0, 
 
 // Scale + scatter of the lines of one staged chunk into the tile accumulator.
 __device__ __forceinline__ unsigned scatter_chunk(const ScatterArgs& a, const Stage& st, int count, int k_start,
-                                                  int tk, unsigned* tile, float fxs) {
+                                                  int tk, unsigned* tile, float fxs, int t0, int nt) {
     unsigned counted = 0;
-    for (int j = threadIdx.x; j < count; j += blockDim.x) {
+    for (int j = t0; j < count; j += nt) {
         const float2 v = st.v0[j];
         const float dl = st.dl ? st.dl[j] : 0.f;
         float fk, tv;
@@ -509,27 +512,32 @@ __device__ __forceinline__ unsigned scatter_chunk(const ScatterArgs& a, const St
     return counted;
 }
 
-// Persistent scatter: CTA b owns tiles b, b + G, b + 2G, ...  Thread 0 streams
-// the tiles' line records chunk by chunk into a ring of `stages` buffers with
-// TMA bulk copies (mbarrier completion), up to stages - 1 chunks ahead of the
-// consumers, across tile boundaries; all threads scatter the current chunk
-// into the tile accumulator (32-bit fixed point, native integer shared
-// atomics, deterministic) and flush each finished tile to HBM with plain
-// stores.
+// Persistent, warp-specialised scatter: CTA b owns tiles b, b + G, b + 2G,
+// ...  Warp 0 (one thread) is the producer: it streams the tiles' line
+// records chunk by chunk into a ring of `stages` buffers with TMA bulk copies,
+// each buffer guarded by a "full" mbarrier (TMA completion) and an "empty"
+// one (one arrival per consumer warp).  Warps 1..31 consume: each waits for a
+// chunk, scatters its share of the lines into the tile accumulator (32-bit
+// fixed point, native integer shared atomics, deterministic) and releases the
+// buffer; warps meet only at tile boundaries (a named barrier of the consumer
+// warps) to flush the finished tile to HBM with plain stores.  Every wait is
+// bounded; a wait that gives up sets the error flag and the CTA stops after
+// the copies it issued have landed (bounded).
 __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int ch = a.chunk;
     const int S = a.stages;
     const size_t sb = scatter_stage_bytes(ch);
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + S * sb);
-    int2* rng = reinterpret_cast<int2*>(smem + S * sb + 8 * kScatMaxStages);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * sb);
+    uint64_t* empty = full + kScatMaxStages;
+    int2* rng = reinterpret_cast<int2*>(smem + S * sb + 16 * kScatMaxStages);
     unsigned* tile = reinterpret_cast<unsigned*>(smem + scatter_fixed_smem(ch, S));
     const int pitch = a.TK + 1;
     const int G = gridDim.x;
     const int nq = (a.n_tiles - (int)blockIdx.x + G - 1) / G;   // tiles of this CTA (<= kScatMaxTilesPerCta)
-    const float fxs = fx_scale_of(*a.cmax);
     const int n_words = a.n_nodes * pitch;
-    const bool has_dl = a.dl != nullptr, has_iso = a.iso != nullptr;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n_cons_warps = (blockDim.x >> 5) - 1;
 
     auto col_idx = [&](int c) { return max(0, min(c + a.col_off, a.col_count - 1)); };
     for (int q = threadIdx.x; q < nq; q += blockDim.x) {
@@ -541,61 +549,76 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
     }
     for (int i = threadIdx.x; i < n_words; i += blockDim.x) tile[i] = 0u;
     if (threadIdx.x == 0) {
-        for (int b = 0; b < S; ++b) mbar_init(&bar[b], 1);
+        for (int b = 0; b < S; ++b) {
+            mbar_init(&full[b], 1);
+            mbar_init(&empty[b], n_cons_warps);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
 
-    // producer (thread 0): the next chunk to copy, in this CTA's chunk order
-    // (tiles in order, chunks of ch lines, empty tiles skipped)
-    int pq = 0, pcs = nq > 0 ? rng[0].x : 0;
-    uint32_t issued = 0;    // chunks issued (thread 0)
-    auto produce = [&](int buf) -> bool {
-        while (pq < nq && pcs >= rng[pq].y) {
-            if (++pq < nq) pcs = rng[pq].x;
-        }
-        if (pq >= nq) return false;
-        issue_chunk(a, smem + buf * sb, &bar[buf], pcs, min(ch, rng[pq].y - pcs));
-        pcs += ch;
-        ++issued;
-        return true;
-    };
-    if (threadIdx.x == 0)
-        for (int b = 0; b < S; ++b)
-            if (!produce(b)) break;
+    if (warp == 0) {   // producer
+        if (lane != 0) return;
+        uint32_t c = 0;   // chunks issued
+        bool bad = false;
+        for (int q = 0; q < nq && !bad; ++q)
+            for (int cs = rng[q].x; cs < rng[q].y; cs += ch) {
+                const int buf = (int)(c % (uint32_t)S);
+                if (c >= (uint32_t)S && !mbar_wait(&empty[buf], ((c / (uint32_t)S) - 1) & 1)) {
+                    bad = true;
+                    break;
+                }
+                issue_chunk(a, smem + buf * sb, &full[buf], cs, min(ch, rng[q].y - cs));
+                ++c;
+            }
+        if (bad) atomicExch(a.err, 1u);
+        // the last copies must land before the CTA may end (normally already consumed)
+        for (uint32_t k = c > (uint32_t)S ? c - S : 0; k < c; ++k)
+            mbar_wait(&full[k % (uint32_t)S], (k / (uint32_t)S) & 1);
+        return;
+    }
 
+    // consumers
+    const float fxs = fx_scale_of(*a.cmax);
+    const bool has_dl = a.dl != nullptr, has_iso = a.iso != nullptr;
+    const int ct = threadIdx.x - 32, nct = blockDim.x - 32;
+    const int cw = warp - 1;
     uint32_t g = 0;         // chunks consumed so far
-    bool bad = false;
     unsigned counted = 0;
+    bool bad = false;
     for (int q = 0; q < nq; ++q) {
         const int k_start = ((int)blockIdx.x + q * G) * a.TK;
         const int tk = min(a.TK, a.n_v - k_start);
         const int b = rng[q].y;
-        for (int cs = rng[q].x; cs < b; cs += ch) {
+        for (int cs = rng[q].x; cs < b && !bad; cs += ch) {
             const int buf = (int)(g % (uint32_t)S);
-            // one thread polls the mbarrier (acquiring the TMA data); the others
-            // block on the CTA barrier, which orders that data for them too
-            if (threadIdx.x == 0 && !mbar_wait(&bar[buf], (g / (uint32_t)S) & 1)) bad = true;
-            if (__syncthreads_or(bad)) {
-                // give up: report, let the other copies in flight land (bounded), leave
-                if (threadIdx.x == 0) {
-                    atomicExch(a.err, 1u);
-                    for (uint32_t gk = g + 1; gk < issued; ++gk)
-                        mbar_wait(&bar[gk % (uint32_t)S], (gk / (uint32_t)S) & 1);
-                }
-                __syncthreads();
-                return;
+            // every lane acquires the TMA data through the mbarrier itself
+            const bool ok = mbar_wait(&full[buf], (g / (uint32_t)S) & 1);
+            if (!__all_sync(0xffffffffu, ok)) {
+                bad = true;
+                break;
             }
             counted += scatter_chunk(a, stage_view(smem + buf * sb, ch, has_dl, has_iso), min(ch, b - cs), k_start,
-                                     tk, tile, fxs);
-            __syncthreads();   // buffer `buf` free again: refill it, S chunks ahead
-            if (threadIdx.x == 0) produce(buf);
+                                     tk, tile, fxs, ct, nct);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[buf]);   // this warp is done with the buffer
             ++g;
+        }
+        // all consumer warps done with the tile (and agree on failures)
+        int any_bad;
+        asm volatile(
+            "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n barrier.cta.red.or.pred q, 1, %2, p;\n"
+            " selp.u32 %0, 1, 0, q;\n}\n"
+            : "=r"(any_bad)
+            : "r"((unsigned)bad), "r"(nct)
+            : "memory");
+        if (any_bad) {
+            if (threadIdx.x == 32) atomicExch(a.err, 1u);
+            return;
         }
         // flush the finished tile as raw fixed-point words (plain stores: this
         // CTA owns its columns; the column FFT converts them) and re-zero it
-        const int lane = threadIdx.x & 31;
-        for (int node = threadIdx.x >> 5; node < a.n_nodes; node += blockDim.x >> 5) {
+        for (int node = cw; node < a.n_nodes; node += n_cons_warps) {
             unsigned* row = tile + node * pitch;
             unsigned* dst = a.ldm + node * a.row_stride + k_start;
             for (int c = lane; c < tk; c += 32) {   // one 128-byte store per warp step
@@ -603,7 +626,7 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
                 row[c] = 0u;
             }
         }
-        __syncthreads();
+        asm volatile("bar.sync 1, %0;" ::"r"(nct) : "memory");
     }
     if (a.in_window && counted) atomicAdd(a.in_window, (unsigned long long)counted);
 }
