@@ -445,29 +445,31 @@ int ensure_workspace(Work& W, int n_nodes, cudaStream_t st) {
 
 // Shape of the persistent scatter (one 1024-thread CTA per SM): TMA ring
 // stages, chunk (lines) and tile width (columns, a multiple of 32 for the bank
-// swizzle).  Each chunk costs two CTA barriers, so the chunk is as large as
-// possible (two stages, 2048 lines = 2 lines per thread when a tile of >= 64
-// columns still fits; measured faster than deeper rings of smaller chunks),
-// then smaller chunks for wider node grids.
+// swizzle).  Measured on GB300 (warp-specialised kernel): a three-stage ring
+// of 512-line chunks wins while it leaves tiles of >= 256 columns (few nodes:
+// CO2 5M, 8x16 nodes: 0.14 ms vs 0.19 ms with 2 x 2048 lines and 160
+// columns); with wide node grids the tile narrows and two 2048-line chunks
+// per stage ring win (H2O 100M, 12x24 nodes: 1.35 ms vs 1.45 ms); smaller
+// chunks only when even those do not fit.
 int scatter_shape(int n_nodes, int* chunk, int* TK, int* stages, size_t* smem) {
     size_t avail = 0;
     RG(scatter_smem_optin(&avail));
-    const int S = 2;
+    auto tile_cols = [&](int S, int ch) {   // widest tile next to the ring (rows of tk + 1 words)
+        const size_t fixed = scatter_fixed_smem(ch, S);
+        if (fixed >= avail) return 0;
+        return std::min(1024, ((int)((avail - fixed) / (4 * (size_t)n_nodes)) - 1) / 32 * 32);
+    };
+    auto take = [&](int S, int ch, int tk) {
+        *chunk = ch;
+        *TK = tk;
+        *stages = S;
+        *smem = scatter_fixed_smem(ch, S) + (size_t)4 * n_nodes * (tk + 1);
+        return RG_OK;
+    };
+    if (tile_cols(3, 512) >= 256) return take(3, 512, tile_cols(3, 512));
     for (int min_tk : {64, 32})
-        for (int ch : {2048, 1024, 512, 256}) {
-            const size_t fixed = scatter_fixed_smem(ch, S);
-            if (fixed >= avail) continue;
-            // tile rows have an odd pitch of tk + 1 words
-            int tk = ((int)((avail - fixed) / (4 * (size_t)n_nodes)) - 1) / 32 * 32;
-            tk = std::min(tk, 1024);
-            if (tk >= min_tk) {
-                *chunk = ch;
-                *TK = tk;
-                *stages = S;
-                *smem = fixed + (size_t)4 * n_nodes * (tk + 1);
-                return RG_OK;
-            }
-        }
+        for (int ch : {2048, 1024, 512, 256})
+            if (tile_cols(2, ch) >= min_tk) return take(2, ch, tile_cols(2, ch));
     return fail(RG_ERR_RANGE, "LDM grid of %d nodes does not fit a shared-memory tile", n_nodes);
 }
 
