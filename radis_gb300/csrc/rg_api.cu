@@ -638,6 +638,44 @@ bool plan_merge(const Work& W, const SpecHost& s, const VoigtArgs& va, GaussArgs
         }
     }
     if (ga->n_wide < 2 || g.n_L % 2) return false;   // pairs must not straddle merged and narrow rows
+    // two-stage form when it needs fewer taps: g_l = d_l conv g_b with
+    // sigma_b^2 = sigma_min^2 - 1.2^2 and every sigma_d, sigma_b >= 1.2 steps
+    // (composition error of sampled Gaussians ~exp(-2 pi^2 sigma^2) < 1e-12)
+    ga->tile_out = kGaussTile;
+    {
+        const double kSigMin = 1.2, kTail = std::sqrt(2.0 * std::log(1e8));   // taps to 1e-8 of the peak
+        auto sig = [&](int w) { return std::exp(g.log_wG_min + ga->wide_l[w] * g.dxG) / dv / (2.0 * std::sqrt(2.0 * kLn2)); };
+        auto padded = [](int K) { return (2 * K + 1 + 7) & ~7; };
+        double smin = 1e300;
+        for (int w = 0; w < ga->n_wide; ++w) smin = std::min(smin, sig(w));
+        const double sb2 = smin * smin - kSigMin * kSigMin;
+        if (sb2 >= kSigMin * kSigMin) {
+            const int Kb = (int)std::ceil(kTail * std::sqrt(sb2));
+            const int tile_out = (kGaussTile - 2 * Kb) & ~7;
+            long single = 0, two = 0;
+            int Kd[kMaxAxis], ext2 = 0;
+            for (int w = 0; w < ga->n_wide; ++w) {
+                single += padded(ga->K[w]);
+                Kd[w] = (int)std::ceil(kTail * std::sqrt(sig(w) * sig(w) - sb2));
+                two += padded(Kd[w]);
+                ext2 = std::max(ext2, Kd[w] + Kb);
+            }
+            const double two_cost = (double)(two + padded(Kb)) * kGaussTile / std::max(tile_out, 8);
+            if (Kb <= kGaussMaxK && tile_out >= kGaussTile / 2 && two_cost < 0.9 * single) {
+                for (int w = 0; w < ga->n_wide; ++w) {
+                    const double sd2 = sig(w) * sig(w) - sb2;
+                    ga->K[w] = Kd[w];
+                    ga->c[w] = (float)(1.0 / std::sqrt(2.0 * kPi * sd2));
+                    ga->a2[w] = (float)(kLog2e / (2.0 * sd2));
+                }
+                ga->Kb = Kb;
+                ga->cb = (float)(1.0 / std::sqrt(2.0 * kPi * sb2));
+                ga->a2b = (float)(kLog2e / (2.0 * sb2));
+                ga->tile_out = tile_out;
+                K_max = ext2;
+            }
+        }
+    }
     const int NL = g.n_L;
     ga->NL = NL;
     ga->rows = NL * (1 + ga->n_narrow);

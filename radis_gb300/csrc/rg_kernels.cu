@@ -1147,14 +1147,46 @@ __device__ __forceinline__ void load8(float (&d)[8], const float* s) {
     d[4] = b.x; d[5] = b.y; d[6] = b.z; d[7] = b.w;
 }
 
+// acc[i] += sum_jj taps[jj] xs[t0 + i + jj], jj < KP (a multiple of 8; xs
+// readable up to t0 + KP + 7): three 8-value register blocks rotate through
+// the window (no moves): taps jj..jj+7 use A ++ B, jj+8.. use B ++ C, jj+16..
+// use C ++ A'; a tail of 8 or 16 taps ends the row of taps.
+__device__ __forceinline__ void conv_window(float (&acc)[8], const float* xs, const float* taps, int t0, int KP) {
+    float A[8], B[8], C[8], g[8];
+    load8(A, &xs[t0]);
+    int jj = 0;
+    for (; jj + 24 <= KP; jj += 24) {
+        load8(B, &xs[t0 + jj + 8]);
+        load8(g, &taps[jj]);
+        gauss_step<8>(acc, A, B, g);
+        load8(C, &xs[t0 + jj + 16]);
+        load8(g, &taps[jj + 8]);
+        gauss_step<8>(acc, B, C, g);
+        load8(A, &xs[t0 + jj + 24]);
+        load8(g, &taps[jj + 16]);
+        gauss_step<8>(acc, C, A, g);
+    }
+    if (jj < KP) {
+        load8(B, &xs[t0 + jj + 8]);
+        load8(g, &taps[jj]);
+        gauss_step<8>(acc, A, B, g);
+        if (jj + 8 < KP) {
+            load8(C, &xs[t0 + jj + 16]);
+            load8(g, &taps[jj + 8]);
+            gauss_step<8>(acc, B, C, g);
+        }
+    }
+}
+
 __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
     extern __shared__ __align__(16) float gsm[];
     constexpr int TW = kGaussTile;
-    constexpr int P = kGaussPer;                     // outputs per thread (multiple of 8)
+    constexpr int P = kGaussPer;                     // outputs per thread (8)
     float* taps = gsm;                               // KP <= 2 kGaussMaxK + 16
     float* xs = gsm + (2 * kGaussMaxK + 16);         // TW + KP + 8 <= TW + 2 kGaussMaxK + 24
     const int r = blockIdx.y;
-    const int p0 = blockIdx.x * TW;
+    const int p0 = blockIdx.x * a.tile_out;          // first output (buffer position)
+    const int q0 = p0 - a.Kb;                        // first position of the per-thread accumulators
     const int Lr = a.n_v + 2 * a.ext;
     float* orow = a.out + (int64_t)r * a.out_stride;
     const int m = r;   // merged row of wL node m
@@ -1171,7 +1203,7 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
         const int K = a.K[w];
         const int KP = (2 * K + 1 + 7) & ~7;
         const unsigned* src = a.ldm + (int64_t)(a.wide_l[w] * a.NL + m) * a.row_stride;
-        const int base = p0 - a.ext - K;   // LDM index of xs[0]
+        const int base = q0 - a.ext - K;   // LDM index of xs[0]
 #pragma unroll
         for (int u = 0; u < NPRE; ++u) {
             const int q = threadIdx.x + u * 256;
@@ -1195,43 +1227,35 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
         }
         if (w + 1 < a.n_wide) fetch(w + 1);
         __syncthreads();
-        // three 8-value register blocks rotate through the window (no moves):
-        // taps jj..jj+7 use A ++ B, jj+8.. use B ++ C, jj+16.. use C ++ A';
-        // a tail of 8 or 16 taps ends the row of taps (KP is a multiple of 8)
-        float A[8], B[8], C[8], g[8];
-        load8(A, &xs[t0]);
-        int jj = 0;
-        for (; jj + 24 <= KP; jj += 24) {
-            load8(B, &xs[t0 + jj + 8]);
-            load8(g, &taps[jj]);
-            gauss_step<8>(acc, A, B, g);
-            load8(C, &xs[t0 + jj + 16]);
-            load8(g, &taps[jj + 8]);
-            gauss_step<8>(acc, B, C, g);
-            load8(A, &xs[t0 + jj + 24]);
-            load8(g, &taps[jj + 16]);
-            gauss_step<8>(acc, C, A, g);
+        conv_window(acc, xs, taps, t0, KP);
+    }
+    int n_out = TW;
+    if (a.Kb > 0) {   // second stage: the summed row convolved once with g_b
+        const int KPb = (2 * a.Kb + 1 + 7) & ~7;
+        __syncthreads();   // last node's tile and taps consumed
+#pragma unroll
+        for (int i = 0; i < P; ++i) xs[t0 + i] = acc[i];
+        for (int q = TW + threadIdx.x; q < TW + KPb + 8; q += blockDim.x) xs[q] = 0.f;
+        for (int jj = threadIdx.x; jj < KPb; jj += blockDim.x) {
+            const float j = (float)(jj - a.Kb);
+            taps[jj] = jj <= 2 * a.Kb ? a.cb * ex2(-a.a2b * j * j) : 0.f;
         }
-        if (jj < KP) {
-            load8(B, &xs[t0 + jj + 8]);
-            load8(g, &taps[jj]);
-            gauss_step<8>(acc, A, B, g);
-            if (jj + 8 < KP) {
-                load8(C, &xs[t0 + jj + 16]);
-                load8(g, &taps[jj + 8]);
-                gauss_step<8>(acc, B, C, g);
-            }
-        }
+        __syncthreads();
+#pragma unroll
+        for (int i = 0; i < P; ++i) acc[i] = 0.f;
+        n_out = a.tile_out;
+        if (t0 < n_out) conv_window(acc, xs, taps, t0, KPb);
     }
     const int p = p0 + t0;
+    if (t0 >= n_out) return;
 #pragma unroll
     for (int i = 0; i < P; i += 4) {
-        if (p + i + 4 <= Lr) {
+        if (p + i + 4 <= Lr && t0 + i + 4 <= n_out) {
             *reinterpret_cast<float4*>(&orow[p + i]) = make_float4(acc[i], acc[i + 1], acc[i + 2], acc[i + 3]);
         } else {
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if (p + i + u < Lr) orow[p + i + u] = acc[i + u];
+                if (p + i + u < Lr && t0 + i + u < n_out) orow[p + i + u] = acc[i + u];
         }
     }
 }
@@ -1646,7 +1670,8 @@ int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st) {
 int launch_gauss_merge(const GaussArgs& a, int out_rows, cudaStream_t st) {
     const size_t smem = sizeof(float) * ((2 * kGaussMaxK + 16) + (kGaussTile + 2 * kGaussMaxK + 24));
     const int Lr = a.n_v + 2 * a.ext;
-    dim3 grid((Lr + kGaussTile - 1) / kGaussTile, out_rows);
+    if (a.tile_out <= 0 || a.tile_out > kGaussTile || a.tile_out % 8 || a.Kb > kGaussMaxK) return RG_ERR_RANGE;
+    dim3 grid((Lr + a.tile_out - 1) / a.tile_out, out_rows);
     k_gauss_merge<<<grid, 256, smem, st>>>(a);
     return check_launch();
 }
