@@ -14,6 +14,8 @@
  *        pre-recorded command list (gpu.py:133-141, 205-284)
  *   rg_plan_grid                    <- set_pTQ/set_G_params/set_L_params +
  *        get_griddims (params.py:89-155, gpu.py:372-374)
+ *   rg_synthesize_quantities <- gpuApp.iterate + the host post-processing of
+ *        eq_spectrum_gpu (radis/lbl/factory.py:1284-1297), on the device
  *   rg_synthesize / rg_synthesize_host <- gpuApp.iterate (gpu.py:302-370):
  *        clear -> FillLDM (cmdFillLDM.comp) -> R2C FFT -> ApplyLineshapes
  *        (cmdApplyLineshapes.comp) -> C2R IFFT -> D2H
@@ -157,6 +159,14 @@ int rg_grid_estimate(const rg_line_arrays* lines, const rg_isotopes* iso, const 
  * `stream` into a ring of 256 spectra read back by rg_plan_stage_times. */
 int rg_synthesize(rg_plan* plan, const rg_conditions* cond, float* out_dev, void* stream,
                   int timing, rg_spectrum_info* info);
+
+/* As rg_synthesize, plus the post-processing epilogue of eq_spectrum_gpu on
+ * the device (radis/lbl/factory.py:1284-1297): out_dev holds 5 rows of n_v
+ * floats: abscoeff and absorbance (x exp(-info.log_scale), path length in
+ * cm), then emissivity, transmittance and radiance (mW/cm2/sr/nm, Planck at
+ * cond->T) in physical units.  Asynchronous on `stream`. */
+int rg_synthesize_quantities(rg_plan* plan, const rg_conditions* cond, double path_length, float* out_dev,
+                             void* stream, rg_spectrum_info* info);
 
 /* Sums (ms) of the stage times recorded with timing = 2 since the last call:
  * scatter, fft-col, fft-row+voigt, ifft-row, ifft-col, total; *count =

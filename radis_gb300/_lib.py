@@ -24,7 +24,7 @@ EXPORTS = [
     "rg_lines_free", "rg_lines_count", "rg_plan_create", "rg_plan_free", "rg_plan_grid", "rg_grid_estimate",
     "rg_synthesize", "rg_synthesize_host", "rg_debug_ldm", "rg_plan_stage_times",
     "rg_server_create", "rg_server_submit", "rg_server_wait", "rg_server_stats_get", "rg_server_destroy",
-    "rg_synthesize_static", "rg_backward", "rg_jvp",
+    "rg_synthesize_static", "rg_backward", "rg_jvp", "rg_synthesize_quantities",
 ]
 
 
@@ -132,6 +132,8 @@ def load(path: str | None = None):
         "rg_backward": ([vp, C.POINTER(Conditions), vp, vp, C.POINTER(C.c_double), vp,
                          C.POINTER(SpectrumInfo)], C.c_int),
         "rg_jvp": ([vp, C.POINTER(Conditions), vp, vp, vp, C.POINTER(SpectrumInfo)], C.c_int),
+        "rg_synthesize_quantities": ([vp, C.POINTER(Conditions), C.c_double, vp, vp, C.POINTER(SpectrumInfo)],
+                                     C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -328,6 +330,18 @@ class Plan:
         info = SpectrumInfo()
         check(load().rg_jvp(self.handle, C.byref(c), ptr(dq), C.c_void_p(out_dev_ptr),
                             C.c_void_p(stream_ptr) if stream_ptr else None, C.byref(info)))
+        return info
+
+    def synthesize_quantities(self, T, p_bar, x, path_length, out_dev_ptr: int, stream_ptr: int | None = None,
+                              q_ratio=None):
+        """Enqueue the spectrum and the device post-processing into 5 rows of
+        n_v floats at ``out_dev_ptr``: abscoeff, absorbance (both x
+        exp(-info.log_scale)), emissivity, transmittance, radiance."""
+        c, _q = self._cond(T, p_bar, x, q_ratio)
+        info = SpectrumInfo()
+        check(load().rg_synthesize_quantities(self.handle, C.byref(c), float(path_length),
+                                              C.c_void_p(out_dev_ptr),
+                                              C.c_void_p(stream_ptr) if stream_ptr else None, C.byref(info)))
         return info
 
     def stage_times(self):

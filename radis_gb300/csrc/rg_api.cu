@@ -1365,6 +1365,32 @@ int rg_synthesize(rg_plan* P, const rg_conditions* c, float* out_dev, void* stre
     return run_spectrum(P, c, out_dev, st, timing, false, info);
 }
 
+int rg_synthesize_quantities(rg_plan* P, const rg_conditions* c, double path_length, float* out_dev, void* stream,
+                             rg_spectrum_info* info) {
+    g_err.clear();
+    if (!valid(P) || !c || !out_dev) return fail(RG_ERR_ARG, "invalid argument");
+    if (!(path_length > 0)) return fail(RG_ERR_ARG, "path_length must be positive");
+    std::lock_guard<std::mutex> lk(P->mu);
+    CU(cudaSetDevice(P->lines->ctx->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
+    rg_spectrum_info inf;
+    RG(run_spectrum(P, c, out_dev, st, 0, false, &inf));
+    QuantArgs q;
+    q.abscoeff = out_dev;
+    q.out = out_dev + P->w.desc.n_v;
+    q.n_v = (int)P->w.desc.n_v;
+    q.vmin = P->w.desc.vmin;
+    q.dv = P->w.desc.dv;
+    q.scale = (float)std::exp(inf.log_scale);
+    q.path_length = (float)path_length;
+    q.c2_T = (float)(kC2 / c->T);
+    RG(plan_stream_begin(P, st));
+    RG(launch_quantities(q, st));
+    RG(plan_stream_end(P, st));
+    if (info) *info = inf;
+    return RG_OK;
+}
+
 int rg_plan_stage_times(rg_plan* P, double* sum_ms, int64_t* count) {
     g_err.clear();
     if (!valid(P) || !sum_ms || !count) return fail(RG_ERR_ARG, "invalid argument");

@@ -219,6 +219,16 @@ struct GaussArgs {
     int tile_out;         // outputs per CTA (kGaussTile, or less the 2 Kb halo, multiple of 8)
 };
 
+struct QuantArgs {         // post-processing epilogue (radis/lbl/factory.py:1284-1297)
+    const float* abscoeff;    // n_v, in units of exp(log_scale)
+    float* out;               // 4 rows of n_v: absorbance (same units), emissivity, transmittance, radiance
+    int n_v;
+    double vmin, dv;
+    float scale;              // exp(log_scale) (may be inf when the spectrum exceeds FP32)
+    float path_length;        // cm
+    float c2_T;               // hc / (k T) in cm (x nu in cm-1)
+};
+
 struct AdjRowArgs {       // adjoint row stage: per pair, IFFT_row(Ghat (V_a + i V_b)) x twiddle
     VoigtArgs v;          // v.g holds Ghat [n1][n2] (FFT of the upstream gradient)
     float2* y;            // output [pair][n1][n2]
@@ -270,6 +280,7 @@ int launch_row_ifft_adj(const AdjRowArgs& a, cudaStream_t st);
 int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st);
 int launch_gather_grad(const GradArgs& a, int grid, cudaStream_t st);
 int launch_gauss_merge(const GaussArgs& a, int out_rows, cudaStream_t st);
+int launch_quantities(const QuantArgs& a, cudaStream_t st);
 int launch_scatter_tangent(const GradArgs& a, int grid, cudaStream_t st);
 int col_block(int n1);               // columns per CTA of the column FFTs
 int row_threads(const FftLen& f);    // block size of the forward row kernel

@@ -1449,6 +1449,29 @@ __global__ void __launch_bounds__(256) k_scatter_tangent(const GradArgs g) {
 }
 
 // ---------------------------------------------------------------------------
+// Post-processing epilogue (radis/lbl/factory.py:1284-1297 and
+// radis/spectrum/equations.py:21-44): absorbance A L, emissivity
+// -expm1(-A L), transmittance 1 - emissivity, radiance emissivity x Planck
+// (radis/phys/blackbody.py:35-74, mW / cm2 / sr / nm at lambda = 1e7/nu nm).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_quantities(const QuantArgs a) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n_v) return;
+    const float A = a.abscoeff[k];
+    const float tau = A * a.scale * a.path_length;   // absorbance in physical units
+    const float eps = -expm1f(-tau);
+    const float nu = (float)(a.vmin + a.dv * (double)k);
+    const float lam = 0.01f / nu;                     // m
+    // 2 h c^2 / lambda^5 / expm1(h c / (lambda k T)) W m-3 sr-1 -> mW cm-2 sr-1 nm-1 (x 1e-10)
+    const float l2 = lam * lam;
+    const float planck = 1.19104297e-16f / (l2 * l2 * lam) / expm1f(a.c2_T * nu) * 1e-10f;
+    a.out[k] = A * a.path_length;
+    a.out[a.n_v + k] = eps;
+    a.out[2 * (int64_t)a.n_v + k] = 1.f - eps;
+    a.out[3 * (int64_t)a.n_v + k] = eps * planck;
+}
+
+// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 static int check_launch() {
@@ -1673,6 +1696,12 @@ int launch_gauss_merge(const GaussArgs& a, int out_rows, cudaStream_t st) {
     if (a.tile_out <= 0 || a.tile_out > kGaussTile || a.tile_out % 8 || a.Kb > kGaussMaxK) return RG_ERR_RANGE;
     dim3 grid((Lr + a.tile_out - 1) / a.tile_out, out_rows);
     k_gauss_merge<<<grid, 256, smem, st>>>(a);
+    return check_launch();
+}
+
+int launch_quantities(const QuantArgs& a, cudaStream_t st) {
+    if (a.n_v <= 0) return RG_OK;
+    k_quantities<<<(a.n_v + 255) / 256, 256, 0, st>>>(a);
     return check_launch();
 }
 

@@ -102,6 +102,30 @@ def test_merged_layout_wide_and_folded_narrow_nodes(ctx):
     assert rel_err(gpu, oracle(lines, *args, info)) <= TOL
 
 
+def test_device_quantities(ctx):
+    """rg_synthesize_quantities: the eq_spectrum_gpu post-processing on the
+    device against the host formulas (float64) on the same abscoeff."""
+    torch = pytest.importorskip("torch")
+    from radis_gb300.spectrum import derived_quantities
+    lines = S.uniform_lines(20_000, 2000.0, 2050.0, seed=51)
+    n_v, T, p, x, Lp = 50001, 1200.0, 1.0, 0.1, 5.0
+    ln = L.Lines(ctx, lines, 44.0)
+    plan = L.Plan(ln, 2000.0, 0.001, n_v, n_G=6, n_L=8)
+    buf = torch.empty(5 * n_v, dtype=torch.float32, device="cuda")
+    info = plan.synthesize_quantities(T, p, x, Lp, buf.data_ptr())
+    torch.cuda.synchronize()
+    q = buf.cpu().numpy().astype(np.float64).reshape(5, n_v)
+    plan.close()
+    ln.close()
+    scale = np.exp(info.log_scale)
+    wn = 2000.0 + 0.001 * np.arange(n_v)
+    want = derived_quantities(wn, q[0] * scale, Lp, T)
+    got = (q[1] * scale, q[2], q[3], q[4])
+    assert np.max(want[0]) > 1.0    # optically thick somewhere: transmittance goes to 0
+    for gq, wq in zip(got, want):
+        assert np.max(np.abs(gq - wq)) <= 1e-5 * np.max(np.abs(wq))
+
+
 def test_odd_node_count_padding(ctx):
     lines = S.uniform_lines(20_000, 2000.0, 2020.0, seed=24)
     args = (28.0, 2000.0, 0.001, 20001, 400.0, 0.5, 0.05)
