@@ -637,7 +637,7 @@ bool plan_merge(const Work& W, const SpecHost& s, const VoigtArgs& va, GaussArgs
             ga->narrow_l[ga->n_narrow++] = l;
         }
     }
-    if (ga->n_wide < 2 || g.n_L % 2) return false;   // pairs must not straddle merged and narrow rows
+    if (ga->n_wide < 2) return false;
     // two-stage form when it needs fewer taps: g_l = d_l conv g_b with
     // sigma_b^2 = sigma_min^2 - 1.2^2 and every sigma_d, sigma_b >= 1.2 steps
     // (composition error of sampled Gaussians ~exp(-2 pi^2 sigma^2) < 1e-12)
@@ -676,10 +676,14 @@ bool plan_merge(const Work& W, const SpecHost& s, const VoigtArgs& va, GaussArgs
             }
         }
     }
-    const int NL = g.n_L;
+    // rows come in blocks of NLv = n_L rounded up to even (a zero row pads odd
+    // n_L) so that no pair straddles the merged and a narrow block
+    const int NL = g.n_L, NLv = NL + (NL & 1);
     ga->NL = NL;
-    ga->rows = NL * (1 + ga->n_narrow);
-    *out_rows = (ga->rows + 1) & ~1;
+    ga->NLv = NLv;
+    ga->rows = NLv * (1 + ga->n_narrow);
+    if (ga->rows >= s.n_nodes) return false;   // no fewer rows (and the FFT workspace holds n_nodes)
+    *out_rows = ga->rows;
     ga->n_v = (int)W.desc.n_v;
     ga->ext = K_max;
     ga->out_stride = (ga->n_v + 2 * K_max + 31) / 32 * 32;
@@ -689,17 +693,18 @@ bool plan_merge(const Work& W, const SpecHost& s, const VoigtArgs& va, GaussArgs
     *vm = va;
     vm->n_nodes = *out_rows;
     vm->n_pairs = *out_rows / 2;
-    vm->NL = NL;
+    vm->NL = NLv;
     vm->alpha[0] = 0.f;   // merged rows: the Gaussian factor is applied already
     for (int i = 0; i < ga->n_narrow; ++i) vm->alpha[1 + i] = va.alpha[ga->narrow_l[i]];
     vm->alpha[1 + ga->n_narrow] = 0.f;
     for (int r = 0; r < *out_rows; ++r) {
-        if (r < NL) {   // merged rows: unfolded, 1 / V(0) = 1
+        const int lp = r / NLv, m = r % NLv;
+        if (m < NL && lp == 0) {   // merged rows: unfolded, 1 / V(0) = 1
             vm->norm[r] = 1.f;
             vm->lnorm[r] = 0.f;
             vm->nfold[r] = 0;
-        } else if (r < ga->rows) {   // narrow node rows keep their folded, normalised Voigt FT
-            const int node = ga->narrow_l[r / NL - 1] * NL + r % NL;
+        } else if (m < NL) {   // narrow node rows keep their folded, normalised Voigt FT
+            const int node = ga->narrow_l[lp - 1] * NL + m;
             vm->norm[r] = va.norm[node];
             vm->lnorm[r] = va.lnorm[node];
             vm->nfold[r] = va.nfold[node];
@@ -712,9 +717,9 @@ bool plan_merge(const Work& W, const SpecHost& s, const VoigtArgs& va, GaussArgs
     return true;
 }
 
-// rows the Gaussian stage writes (one per wL node; the narrow rows are read
-// from the LDM by the column FFT directly)
-int NL_merged(const GaussArgs& ga) { return ga.NL; }
+// rows of the merged-row buffer (one per wL node, plus a zero row for odd
+// n_L; the narrow rows are read from the LDM by the column FFT directly)
+int NL_merged(const GaussArgs& ga) { return ga.NLv; }
 
 // After a synchronisation: report (once) a bounded device wait that gave up.
 int take_err(Work& W) {
@@ -781,19 +786,22 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
                 W.mrow_bytes = want;
             }
             ga->out = W.mrow;
-            RG(launch_gauss_merge(*ga, NL_merged(*ga), st));
-            ColFftArgs cm = ca;   // merged rows (float, extended): pairs [0, n_L / 2)
+            if (ga->NLv > ga->NL)   // zero pad row of odd n_L
+                CU(cudaMemsetAsync(W.mrow + (size_t)ga->NL * ga->out_stride, 0, sizeof(float) * ga->out_stride, st));
+            RG(launch_gauss_merge(*ga, ga->NL, st));
+            ColFftArgs cm = ca;   // merged rows (float, extended): pairs [0, NLv / 2)
             cm.src = W.mrow;
             cm.row_stride = ga->out_stride;
             cm.ext = ga->ext;
-            cm.n_pairs = ga->NL / 2;
+            cm.n_pairs = ga->NLv / 2;
             RG(launch_col_fft_fwd_f(cm, st));
             if (ga->n_narrow) {   // narrow node rows straight from the LDM: the following pairs
                 ColFftArgs cn = ca;
-                cn.pair_base = ga->NL / 2;
-                cn.n_pairs = ga->n_narrow * ga->NL / 2;
+                cn.pair_base = ga->NLv / 2;
+                cn.n_pairs = ga->n_narrow * ga->NLv / 2;
                 cn.map_n = ga->n_narrow;
                 cn.map_NL = ga->NL;
+                cn.map_NLv = ga->NLv;
                 for (int i = 0; i < ga->n_narrow; ++i) cn.map_l[i] = (unsigned char)ga->narrow_l[i];
                 RG(launch_col_fft_fwd(cn, st));
             }

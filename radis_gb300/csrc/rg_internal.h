@@ -151,8 +151,8 @@ struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
     int ext;              // K2 float rows: 0, or the rows hold k in [-ext, n_v + ext) at offset k + ext
                           // (circular: k < 0 is FFT index n + k)
     int pair_base;        // K2: first output pair in y
-    int map_n;            // K2 fixed point: 0, or virtual row v reads LDM node
-    int map_NL;           //   map_l[v / map_NL] * map_NL + v % map_NL (narrow rows of the merged layout)
+    int map_n;            // K2 fixed point: 0, or virtual row v (blocks of map_NLv rows) reads LDM
+    int map_NL, map_NLv;  //   node map_l[v / map_NLv] * map_NL + v % map_NLv, zero when v % map_NLv >= map_NL
     unsigned char map_l[kMaxAxis];
 };
 
@@ -205,7 +205,8 @@ struct GaussArgs {
     float* out;
     int64_t out_stride;
     int n_v, ext, NL;
-    int rows;             // rows of the merged layout: NL (merged) + NL * n_narrow (LDM rows)
+    int NLv;              // NL rounded up to even: rows per block of the merged layout
+    int rows;             // rows of the merged layout: NLv (merged) + NLv * n_narrow (LDM rows)
     int n_wide, n_narrow;
     int wide_l[kMaxAxis], K[kMaxAxis];       // wide nodes and kernel half-widths
     float c[kMaxAxis], a2[kMaxAxis];         // taps c ex2(-a2 j^2), |j| <= K

@@ -665,16 +665,22 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS, 3) k_col_fft_fwd(const 
     const int c0 = blockIdx.x * B;
     const int pair = blockIdx.y;
     // the LDM holds the scatter's fixed-point words: value = word / fx_scale
-    auto node_of = [&](int v) { return a.map_n ? a.map_l[v / a.map_NL] * a.map_NL + v % a.map_NL : v; };
-    const unsigned* ra = a.ldm + (int64_t)node_of(2 * pair) * a.row_stride;
-    const unsigned* rb = a.ldm + (int64_t)node_of(2 * pair + 1) * a.row_stride;
+    auto node_of = [&](int v) {   // -1: zero row (padding of an odd n_L block)
+        if (!a.map_n) return v;
+        const int m = v % a.map_NLv;
+        return m < a.map_NL ? a.map_l[v / a.map_NLv] * a.map_NL + m : -1;
+    };
+    const int na = node_of(2 * pair), nb = node_of(2 * pair + 1);
+    const unsigned* ra = na >= 0 ? a.ldm + (int64_t)na * a.row_stride : nullptr;
+    const unsigned* rb = nb >= 0 ? a.ldm + (int64_t)nb * a.row_stride : nullptr;
     const float inv = 1.f / fx_scale_of(*a.cmax);
     const int n2i = c0 + b;
     float2 v[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int64_t nidx = (int64_t)(j + q * TPC) * a.n2 + n2i;
-        v[q] = nidx < a.n_v ? make_float2((float)__ldg(&ra[nidx]) * inv, (float)__ldg(&rb[nidx]) * inv)
+        v[q] = nidx < a.n_v ? make_float2(ra ? (float)__ldg(&ra[nidx]) * inv : 0.f,
+                                          rb ? (float)__ldg(&rb[nidx]) * inv : 0.f)
                             : make_float2(0.f, 0.f);
     }
     col_fft8<N1>(v, sm, j, b, a.f1.tw);

@@ -102,6 +102,16 @@ def test_merged_layout_wide_and_folded_narrow_nodes(ctx):
     assert rel_err(gpu, oracle(lines, *args, info)) <= TOL
 
 
+def test_merged_layout_odd_lorentz_count(ctx):
+    """Merged layout with an odd number of wL nodes (a zero row pads each
+    block of rows), wide and narrow Gaussian nodes mixed."""
+    lines = S.uniform_lines(30_000, 1500.0, 4500.0, seed=33)
+    args = (18.0, 1500.0, 0.005, 600001, 2000.0, 0.2, 0.2)
+    gpu, info = run_gpu(ctx, lines, *args, n_G=8, n_L=7)
+    assert info.merged_rows == 7 and 0 < info.fft_rows < 56
+    assert rel_err(gpu, oracle(lines, *args, info)) <= TOL
+
+
 def test_device_quantities(ctx):
     """rg_synthesize_quantities: the eq_spectrum_gpu post-processing on the
     device against the host formulas (float64) on the same abscoeff."""
