@@ -131,7 +131,7 @@ struct Work {
     size_t mrow_bytes = 0;
     int last_fft_rows = 0, last_merged_rows = 0, last_ext = 0;   // layout of the last spectrum
     int64_t row_stride = 0;
-    unsigned* ldm = nullptr;          // LDM as fixed-point words of the scatter
+    float* ldm = nullptr;             // LDM [node][row_stride] (the scatter's float values)
     float2* y = nullptr;
     float2* g = nullptr;
     unsigned long long* counter = nullptr;
@@ -423,7 +423,7 @@ int build_envelope(const rg_line_arrays* in, const rg_isotopes* iso, Envelope* E
 // reused across geometries, so a server slot that runs requests of many sizes
 // reallocates only when a request is larger than any before it.
 int ensure_workspace(Work& W, int n_nodes, cudaStream_t st) {
-    const size_t per_l = sizeof(unsigned) * (size_t)W.row_stride, per_y = sizeof(float2) * (size_t)W.n;
+    const size_t per_l = sizeof(float) * (size_t)W.row_stride, per_y = sizeof(float2) * (size_t)W.n;
     auto fits = [&](int nodes) { return nodes * per_l <= W.ldm_bytes && (size_t)(nodes / 2) * per_y <= W.y_bytes; };
     if (!fits(n_nodes)) {
         const size_t want_l = std::max<size_t>((size_t)n_nodes * per_l, (size_t)(W.ldm_bytes * 1.25));
@@ -914,11 +914,11 @@ int enqueue_backward(const rg_lines* L, Work& W, const rg_conditions* c, const S
     RG(launch_row_ifft_adj(*ar, st));
     ColFftArgs cb = col_args(W, s);
     cb.h = W.y;
-    cb.out = reinterpret_cast<float*>(W.ldm);
+    cb.out = W.ldm;
     cb.out_scale = (float)(1.0 / ((double)W.n * W.desc.dv));
     RG(launch_col_ifft_adj(cb, st));
     // per-line chain rule gathered at the lines' cells
-    ga->adj = reinterpret_cast<const float*>(W.ldm);
+    ga->adj = W.ldm;
     ga->out = grad_d;
     CU(cudaMemsetAsync(grad_d, 0, 3 * sizeof(double), st));
     RG(launch_gather_grad(*ga, L->ctx->sms * 8, st));
@@ -935,7 +935,7 @@ int enqueue_tangent(const rg_lines* L, Work& W, const rg_conditions* c, const Sp
     RG(fill_grad_args(L, W, c, s, dlnq_dT, ga.get()));
     auto va = std::make_unique<VoigtArgs>();
     fill_voigt_args(W, s, va.get());
-    float* tan = reinterpret_cast<float*>(W.ldm);
+    float* tan = W.ldm;
     ga->tan = tan;
     const int n_v = (int)W.desc.n_v;
     for (int q = 0; q < 3; ++q) {
@@ -1449,15 +1449,10 @@ int rg_debug_ldm(rg_plan* P, const rg_conditions* c, float* ldm_host, int64_t ca
     const int nodes = inf->grid.n_G * inf->grid.n_L;
     if (capacity < (int64_t)nodes * nv)
         return fail(RG_ERR_ARG, "capacity %lld < %lld", (long long)capacity, (long long)nodes * nv);
-    CU(cudaMemcpy2DAsync(ldm_host, sizeof(float) * nv, P->w.ldm, sizeof(unsigned) * P->w.row_stride,
+    CU(cudaMemcpy2DAsync(ldm_host, sizeof(float) * nv, P->w.ldm, sizeof(float) * P->w.row_stride,
                          sizeof(float) * nv, nodes, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
-    RG(take_err(P->w));
-    // the device LDM holds fixed-point words: convert in place
-    const float inv = 1.f / fx_scale_of((int)P->w.cmax_host);
-    unsigned* w = reinterpret_cast<unsigned*>(ldm_host);
-    for (int64_t i = 0; i < (int64_t)nodes * nv; ++i) ldm_host[i] = (float)w[i] * inv;
-    return RG_OK;
+    return take_err(P->w);
 }
 
 int rg_backward(rg_plan* P, const rg_conditions* c, const double* dlnq_dT, const float* grad_out_dev,
@@ -2099,9 +2094,9 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
     // sized here: the workspace step finds them large enough and allocates nothing;
     // the merged layout (its own row buffer) is not used on this path
     W.allow_merge = false;
-    W.ldm_bytes = sizeof(unsigned) * (size_t)s.n_nodes * (size_t)W.row_stride;
+    W.ldm_bytes = sizeof(float) * (size_t)s.n_nodes * (size_t)W.row_stride;
     W.y_bytes = sizeof(float2) * (size_t)(s.n_nodes / 2) * (size_t)W.n;
-    W.ldm = static_cast<unsigned*>(take(W.ldm_bytes));
+    W.ldm = static_cast<float*>(take(W.ldm_bytes));
     W.y = static_cast<float2*>(take(W.y_bytes));
     W.g = static_cast<float2*>(take(sizeof(float2) * (size_t)W.n));
     if (off > kStaticScratchBytes)

@@ -86,7 +86,7 @@ struct ScatterArgs {
     int n_nodes;          // padded to even
     int NG, NL;
     int64_t row_stride;
-    unsigned* ldm;        // fixed-point words, value = word / fx_scale
+    float* ldm;           // LDM values: the tile's fixed-point sums / fx_scale, converted at the flush
     int margin_cols;
     float vmin_hi, vmin_lo;
     float inv_dv_hi, inv_dv_lo;
@@ -136,7 +136,7 @@ struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
     int64_t n;            // n_ft
     int64_t row_stride;
     int n_pairs;
-    const unsigned* ldm;  // K2 input: fixed-point words of the scatter
+    const float* ldm;     // K2 input: the scatter's LDM [node][row_stride]
     const int* cmax;      // device: fixed-point bound of the scatter (scale = fx_scale(*cmax))
     float2* y;            // K2 output [pair][n1][n2]
     const float2* tw_hi;  // exp(-2 pi i 1024 t / N)
@@ -199,7 +199,7 @@ constexpr int kGaussPer = 8;          // outputs per thread
 constexpr int kGaussTile = 256 * kGaussPer;   // outputs per CTA (256 threads)
 constexpr int kGaussMaxK = 256;       // widest kernel half-width (points)
 struct GaussArgs {
-    const unsigned* ldm;  // fixed-point LDM words [node][row_stride]
+    const float* ldm;     // LDM [node][row_stride]
     int64_t row_stride;
     const int* cmax;      // fixed-point bound (scale)
     float* out;

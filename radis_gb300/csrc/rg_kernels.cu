@@ -580,6 +580,7 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
 
     // consumers
     const float fxs = fx_scale_of(*a.cmax);
+    const float inv_fx = 1.f / fxs;
     const bool has_dl = a.dl != nullptr, has_iso = a.iso != nullptr;
     const int ct = threadIdx.x - 32, nct = blockDim.x - 32;
     const int cw = warp - 1;
@@ -616,13 +617,14 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
             if (threadIdx.x == 32) atomicExch(a.err, 1u);
             return;
         }
-        // flush the finished tile as raw fixed-point words (plain stores: this
-        // CTA owns its columns; the column FFT converts them) and re-zero it
+        // flush the finished tile as floats, word / fx_scale (a power of two:
+        // exact scaling of the rounded word), with plain stores (this CTA owns
+        // its columns), and re-zero it
         for (int node = cw; node < a.n_nodes; node += n_cons_warps) {
             unsigned* row = tile + node * pitch;
-            unsigned* dst = a.ldm + node * a.row_stride + k_start;
+            float* dst = a.ldm + node * a.row_stride + k_start;
             for (int c = lane; c < tk; c += 32) {   // one 128-byte store per warp step
-                dst[c] = row[c];
+                dst[c] = __uint2float_rn(row[c]) * inv_fx;
                 row[c] = 0u;
             }
         }
@@ -664,23 +666,20 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS, 3) k_col_fft_fwd(const 
     const int j = threadIdx.x / B;
     const int c0 = blockIdx.x * B;
     const int pair = blockIdx.y;
-    // the LDM holds the scatter's fixed-point words: value = word / fx_scale
     auto node_of = [&](int v) {   // -1: zero row (padding of an odd n_L block)
         if (!a.map_n) return v;
         const int m = v % a.map_NLv;
         return m < a.map_NL ? a.map_l[v / a.map_NLv] * a.map_NL + m : -1;
     };
     const int na = node_of(2 * pair), nb = node_of(2 * pair + 1);
-    const unsigned* ra = na >= 0 ? a.ldm + (int64_t)na * a.row_stride : nullptr;
-    const unsigned* rb = nb >= 0 ? a.ldm + (int64_t)nb * a.row_stride : nullptr;
-    const float inv = 1.f / fx_scale_of(*a.cmax);
+    const float* ra = na >= 0 ? a.ldm + (int64_t)na * a.row_stride : nullptr;
+    const float* rb = nb >= 0 ? a.ldm + (int64_t)nb * a.row_stride : nullptr;
     const int n2i = c0 + b;
     float2 v[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
         const int64_t nidx = (int64_t)(j + q * TPC) * a.n2 + n2i;
-        v[q] = nidx < a.n_v ? make_float2(ra ? (float)__ldg(&ra[nidx]) * inv : 0.f,
-                                          rb ? (float)__ldg(&rb[nidx]) * inv : 0.f)
+        v[q] = nidx < a.n_v ? make_float2(ra ? __ldg(&ra[nidx]) : 0.f, rb ? __ldg(&rb[nidx]) : 0.f)
                             : make_float2(0.f, 0.f);
     }
     col_fft8<N1>(v, sm, j, b, a.f1.tw);
@@ -1153,6 +1152,8 @@ __device__ __forceinline__ void load8(float (&d)[8], const float* s) {
     d[4] = b.x; d[5] = b.y; d[6] = b.z; d[7] = b.w;
 }
 
+constexpr int kGaussXs = kGaussTile + 2 * kGaussMaxK + 24;   // window buffer floats
+
 // acc[i] += sum_jj taps[jj] xs[t0 + i + jj], jj < KP (a multiple of 8; xs
 // readable up to t0 + KP + 7): three 8-value register blocks rotate through
 // the window (no moves): taps jj..jj+7 use A ++ B, jj+8.. use B ++ C, jj+16..
@@ -1188,48 +1189,63 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
     extern __shared__ __align__(16) float gsm[];
     constexpr int TW = kGaussTile;
     constexpr int P = kGaussPer;                     // outputs per thread (8)
-    float* taps = gsm;                               // KP <= 2 kGaussMaxK + 16
-    float* xs = gsm + (2 * kGaussMaxK + 16);         // TW + KP + 8 <= TW + 2 kGaussMaxK + 24
+    float* taps = gsm;                               // KP <= 2 kGaussMaxK + 8 (K <= kGaussMaxK, shift <= 3)
+    float* xs = gsm + (2 * kGaussMaxK + 16);         // 4 n4 <= TW + KP + 11 <= kGaussXs
     const int r = blockIdx.y;
     const int p0 = blockIdx.x * a.tile_out;          // first output (buffer position)
     const int q0 = p0 - a.Kb;                        // first position of the per-thread accumulators
     const int Lr = a.n_v + 2 * a.ext;
     float* orow = a.out + (int64_t)r * a.out_stride;
     const int m = r;   // merged row of wL node m
-    const float inv = 1.f / fx_scale_of(*a.cmax);
     float acc[P];
 #pragma unroll
     for (int i = 0; i < P; ++i) acc[i] = 0.f;
     const int t0 = threadIdx.x * P;
-    // the next node's input tile is fetched into registers while the current
-    // one is convolved (NPRE words per thread cover TW + KP + 8 <= the xs buffer)
-    constexpr int NPRE = (TW + 2 * kGaussMaxK + 24 + 255) / 256;
-    unsigned pre[NPRE];
+    // Node w's window starts at LDM index base = q0 - ext - K_w; it is staged
+    // from the 16-byte aligned index base & ~3, and the offset s = base & 3 is
+    // absorbed by s leading zero taps.  The next node's window is fetched into
+    // registers (NPRE float4 per thread) while the current one is convolved.
+    constexpr int NPRE = ((TW + 2 * kGaussMaxK + 24) / 4 + 255) / 256;
+    float4 pre[NPRE];
+    auto shift_of = [&](int w) { return (q0 - a.ext - a.K[w]) & 3; };
+    auto taps_of = [&](int w) { return (2 * a.K[w] + 1 + shift_of(w) + 7) & ~7; };   // multiple of 8
     auto fetch = [&](int w) {
-        const int K = a.K[w];
-        const int KP = (2 * K + 1 + 7) & ~7;
-        const unsigned* src = a.ldm + (int64_t)(a.wide_l[w] * a.NL + m) * a.row_stride;
-        const int base = q0 - a.ext - K;   // LDM index of xs[0]
+        const int k0 = (q0 - a.ext - a.K[w]) & ~3;   // LDM index of xs[0]
+        const int n4 = (TW + taps_of(w) + 8 + 3) / 4;
+        const float* src = a.ldm + (int64_t)(a.wide_l[w] * a.NL + m) * a.row_stride;
 #pragma unroll
         for (int u = 0; u < NPRE; ++u) {
             const int q = threadIdx.x + u * 256;
-            const int k = base + q;
-            pre[u] = (q < TW + KP + 8 && k >= 0 && k < a.n_v) ? __ldg(&src[k]) : 0u;
+            const int k = k0 + 4 * q;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (q < n4) {
+                if (k >= 0 && k + 3 < a.n_v) {
+                    v = __ldg(reinterpret_cast<const float4*>(src + k));   // rows start 128-byte aligned
+                } else {   // row ends: zeros outside [0, n_v)
+                    if (k >= 0 && k < a.n_v) v.x = __ldg(&src[k]);
+                    if (k + 1 >= 0 && k + 1 < a.n_v) v.y = __ldg(&src[k + 1]);
+                    if (k + 2 >= 0 && k + 2 < a.n_v) v.z = __ldg(&src[k + 2]);
+                    if (k + 3 >= 0 && k + 3 < a.n_v) v.w = __ldg(&src[k + 3]);
+                }
+            }
+            pre[u] = v;
         }
     };
     fetch(0);
     for (int w = 0; w < a.n_wide; ++w) {
         const int K = a.K[w];
-        const int KP = (2 * K + 1 + 7) & ~7;   // taps padded with zeros to a multiple of 8
+        const int sh = shift_of(w);
+        const int KP = taps_of(w);
+        const int n4 = (TW + KP + 8 + 3) / 4;
         __syncthreads();   // previous node's taps and tile consumed
         for (int jj = threadIdx.x; jj < KP; jj += blockDim.x) {
-            const float j = (float)(jj - K);
-            taps[jj] = jj <= 2 * K ? a.c[w] * inv * ex2(-a.a2[w] * j * j) : 0.f;   // x inv: xs holds raw words
+            const float j = (float)(jj - sh - K);
+            taps[jj] = jj >= sh && jj <= sh + 2 * K ? a.c[w] * ex2(-a.a2[w] * j * j) : 0.f;
         }
 #pragma unroll
         for (int u = 0; u < NPRE; ++u) {
             const int q = threadIdx.x + u * 256;
-            if (q < TW + KP + 8) xs[q] = (float)pre[u];
+            if (q < n4) reinterpret_cast<float4*>(xs)[q] = pre[u];
         }
         if (w + 1 < a.n_wide) fetch(w + 1);
         __syncthreads();
@@ -1697,9 +1713,12 @@ int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st) {
 }
 
 int launch_gauss_merge(const GaussArgs& a, int out_rows, cudaStream_t st) {
-    const size_t smem = sizeof(float) * ((2 * kGaussMaxK + 16) + (kGaussTile + 2 * kGaussMaxK + 24));
+    const size_t smem = sizeof(float) * ((2 * kGaussMaxK + 16) + kGaussXs);
     const int Lr = a.n_v + 2 * a.ext;
     if (a.tile_out <= 0 || a.tile_out > kGaussTile || a.tile_out % 8 || a.Kb > kGaussMaxK) return RG_ERR_RANGE;
+    if (a.n_wide < 0 || a.n_wide > kMaxAxis || a.row_stride % 4) return RG_ERR_RANGE;
+    for (int w = 0; w < a.n_wide; ++w)
+        if (a.K[w] < 0 || a.K[w] > kGaussMaxK) return RG_ERR_RANGE;
     dim3 grid((Lr + a.tile_out - 1) / a.tile_out, out_rows);
     k_gauss_merge<<<grid, 256, smem, st>>>(a);
     return check_launch();
