@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdio>
+#include <type_traits>
 
 #include "rg_internal.h"
 
@@ -773,16 +774,30 @@ template <> struct RowT<1> {
     __device__ static E join(float2 a, float2) { return a; }
 };
 
-template <int R, int PAIRS>
-__device__ __forceinline__ void twiddleP(float2* A, float2* B, const float2* __restrict__ tw, int s) {
+// Row-pass twiddle sources, tw(t) = exp(-2 pi i t / n2): the global table,
+// or a two-level table in shared memory, hi[t / 32] lo[t % 32] (one more
+// rounding; used by the long-row layouts, whose n2-point table would not stay
+// in the L1 left beside their work buffers).
+struct TwGlobal {
+    const float2* __restrict__ tw;
+    __device__ __forceinline__ float2 operator()(int t) const { return __ldg(&tw[t]); }
+};
+struct TwShared {
+    const float2* hi;
+    const float2* lo;
+    __device__ __forceinline__ float2 operator()(int t) const { return cmul(hi[t >> 5], lo[t & 31]); }
+};
+
+template <int R, int PAIRS, class TW>
+__device__ __forceinline__ void twiddleP(float2* A, float2* B, const TW& tw, int s) {
     float2 w[R];
     w[0] = make_float2(1.f, 0.f);
-    w[1] = __ldg(&tw[s]);
-    if (R >= 3) w[2] = __ldg(&tw[2 * s]);
+    w[1] = tw(s);
+    if (R >= 3) w[2] = tw(2 * s);
     if (R >= 4) w[3] = cmul(w[1], w[2]);
     if (R == 5) w[4] = cmul(w[2], w[2]);
     if (R == 8) {
-        w[4] = __ldg(&tw[4 * s]);
+        w[4] = tw(4 * s);
         w[5] = cmul(w[1], w[4]);
         w[6] = cmul(w[2], w[4]);
         w[7] = cmul(w[3], w[4]);
@@ -820,10 +835,10 @@ __device__ __forceinline__ void row_first(const float2* __restrict__ ya, const f
     }
 }
 
-template <int R, int PAIRS>
+template <int R, int PAIRS, class TW>
 __device__ __forceinline__ void row_mid(const typename RowT<PAIRS>::E* __restrict__ in,
                                         typename RowT<PAIRS>::E* __restrict__ out, int L, int Ns, unsigned mag,
-                                        const float2* __restrict__ tw) {
+                                        const TW& tw) {
     const int M = L / R;
     const int twstep = L / (Ns * R);
     for (int j = threadIdx.x; j < M; j += blockDim.x) {
@@ -832,7 +847,7 @@ __device__ __forceinline__ void row_mid(const typename RowT<PAIRS>::E* __restric
         float2 A[R], B[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) RowT<PAIRS>::split(in[RowT<PAIRS>::pad(j + r * M)], A[r], B[r]);
-        if (Ns > 1) twiddleP<R, PAIRS>(A, B, tw, k * twstep);
+        if (Ns > 1) twiddleP<R, PAIRS, TW>(A, B, tw, k * twstep);
         dftR<R>(A);
         if (PAIRS == 2) dftR<R>(B);
         const int base = q * Ns * R + k;
@@ -844,9 +859,10 @@ __device__ __forceinline__ void row_mid(const typename RowT<PAIRS>::E* __restric
 // two work buffers, the optional twiddle table, and the optional staging
 // buffer of the next two rows
 template <int PAIRS>
-__host__ __device__ inline size_t row_voigt_smem(int n2, bool with_twr, bool with_stage) {
+__host__ __device__ inline size_t row_voigt_smem(int n2, bool with_twr, bool with_stage, bool with_tws = false) {
     return 2 * (size_t)RowT<PAIRS>::len(n2) * sizeof(typename RowT<PAIRS>::E) +
-           (with_twr ? (size_t)n2 * sizeof(float2) : 0) + (with_stage ? 2 * (size_t)n2 * sizeof(float2) : 0);
+           (with_twr ? (size_t)n2 * sizeof(float2) : 0) + (with_stage ? 2 * (size_t)n2 * sizeof(float2) : 0) +
+           (with_tws ? (size_t)(n2 / 32 + 32) * sizeof(float2) : 0);
 }
 
 // Layouts of the forward row kernel: MAXT threads at most, and the block is
@@ -895,7 +911,7 @@ __device__ __forceinline__ void row_first_staged(const float2* stage, bool two, 
     }
 }
 
-template <int PAIRS, int MAXT, bool TWR, bool STAGE>
+template <int PAIRS, int MAXT, bool TWR, bool STAGE, bool TWS>
 __global__ void __launch_bounds__(MAXT, MAXT <= 384 ? 2 : 1) k_row_fft_voigt(const VoigtArgs a) {
     using E = typename RowT<PAIRS>::E;
     extern __shared__ float4 sm4[];
@@ -907,12 +923,23 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 384 ? 2 : 1) k_row_fft_voigt(con
     // STAGE (two pairs): the next two rows are staged with cp.async during the passes
     float2* stage = STAGE ? reinterpret_cast<float2*>(buf1 + len) + (TWR ? n2 : 0) : nullptr;
     const int k1 = blockIdx.x;
+    const FftLen& P = a.f2;
+    // TWS: two-level pass twiddle table after the other buffers (made visible
+    // by the barrier after the first pass)
+    float2* tws = TWS ? reinterpret_cast<float2*>(buf1 + len) + (TWR ? n2 : 0) + (STAGE ? 2 * n2 : 0) : nullptr;
+    if (TWS) {
+        for (int t = threadIdx.x; t < n2 / 32; t += blockDim.x) tws[t] = __ldg(&P.tw[32 * t]);
+        for (int t = threadIdx.x; t < 32; t += blockDim.x) tws[n2 / 32 + t] = __ldg(&P.tw[t]);
+    }
+    using TwT = typename std::conditional<TWS, TwShared, TwGlobal>::type;
+    TwT twp;
+    if constexpr (TWS) twp = TwShared{tws, tws + n2 / 32};
+    else twp = TwGlobal{P.tw};
     if (TWR)
         for (int t = threadIdx.x; t < n2; t += blockDim.x) twr[t] = twiddle_n(a.tw_hi, a.tw_lo, k1 * t);
     const int n = (int)a.n;
     const int j0 = blockIdx.y * kPairGroup;
     const int j1 = min(j0 + kPairGroup, a.n_pairs);
-    const FftLen& P = a.f2;
     const int ML = n2 / 8;    // butterflies of the last pass (radix 8, sub-length ML)
     const int jl = threadIdx.x;
     float2 acc[8];
@@ -954,11 +981,11 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 384 ? 2 : 1) k_row_fft_voigt(con
             const int Ns = P.ns[p];
             const unsigned mag = P.mag[p];
             switch (P.radix[p]) {
-                case 2: row_mid<2, PAIRS>(in, out, n2, Ns, mag, P.tw); break;
-                case 3: row_mid<3, PAIRS>(in, out, n2, Ns, mag, P.tw); break;
-                case 4: row_mid<4, PAIRS>(in, out, n2, Ns, mag, P.tw); break;
-                case 5: row_mid<5, PAIRS>(in, out, n2, Ns, mag, P.tw); break;
-                default: row_mid<8, PAIRS>(in, out, n2, Ns, mag, P.tw); break;
+                case 2: row_mid<2, PAIRS, TwT>(in, out, n2, Ns, mag, twp); break;
+                case 3: row_mid<3, PAIRS, TwT>(in, out, n2, Ns, mag, twp); break;
+                case 4: row_mid<4, PAIRS, TwT>(in, out, n2, Ns, mag, twp); break;
+                case 5: row_mid<5, PAIRS, TwT>(in, out, n2, Ns, mag, twp); break;
+                default: row_mid<8, PAIRS, TwT>(in, out, n2, Ns, mag, twp); break;
             }
             __syncthreads();
             E* t = in;
@@ -971,7 +998,7 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 384 ? 2 : 1) k_row_fft_voigt(con
             float2 A[8], B[8];
 #pragma unroll
             for (int r = 0; r < 8; ++r) RowT<PAIRS>::split(in[RowT<PAIRS>::pad(jl + r * ML)], A[r], B[r]);
-            twiddleP<8, PAIRS>(A, B, P.tw, jl);   // w_{n2}^{r jl}
+            twiddleP<8, PAIRS, TwT>(A, B, twp, jl);   // w_{n2}^{r jl}
             dft8(A);
             if (PAIRS == 2) dft8(B);
             if (!a.any_fold) {
@@ -1605,12 +1632,12 @@ int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st) {
     }
 }
 
-template <int PAIRS, int MAXT, bool TWR, bool STAGE>
+template <int PAIRS, int MAXT, bool TWR, bool STAGE, bool TWS>
 static int row_voigt(const VoigtArgs& a, cudaStream_t st) {
-    const size_t smem = row_voigt_smem<PAIRS>(a.n2, TWR, STAGE);
-    ALLOW_SMEM((k_row_fft_voigt<PAIRS, MAXT, TWR, STAGE>), smem);
+    const size_t smem = row_voigt_smem<PAIRS>(a.n2, TWR, STAGE, TWS);
+    ALLOW_SMEM((k_row_fft_voigt<PAIRS, MAXT, TWR, STAGE, TWS>), smem);
     dim3 grid(a.n1, (a.n_pairs + kPairGroup - 1) / kPairGroup);
-    k_row_fft_voigt<PAIRS, MAXT, TWR, STAGE><<<grid, a.threads, smem, st>>>(a);
+    k_row_fft_voigt<PAIRS, MAXT, TWR, STAGE, TWS><<<grid, a.threads, smem, st>>>(a);
     return check_launch();
 }
 
@@ -1629,7 +1656,7 @@ RowLayout row_layout(int n2) {
         L.maxt = kRowMaxT2;
         L.stage = 1;
         L.twr = row_voigt_smem<2>(n2, true, true) <= 113 * 1024;
-    } else if (n2 / 8 <= kRowMaxT2L && row_voigt_smem<2>(n2, false, false) <= 227 * 1024) {
+    } else if (n2 / 8 <= kRowMaxT2L && row_voigt_smem<2>(n2, false, false, true) <= 227 * 1024) {
         L.pairs = 2;
         L.maxt = kRowMaxT2L;
     } else {
@@ -1645,9 +1672,10 @@ int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st) {
     if (a.threads < a.n2 / 8 || a.threads > L.maxt || a.threads % 32) return RG_ERR_RANGE;
     if (L.pairs != a.pairs_per_pass || L.twr != a.row_twiddle_table) return RG_ERR_RANGE;
     if (L.maxt == kRowMaxT2)
-        return L.twr ? row_voigt<2, kRowMaxT2, true, true>(a, st) : row_voigt<2, kRowMaxT2, false, true>(a, st);
-    if (L.maxt == kRowMaxT2L) return row_voigt<2, kRowMaxT2L, false, false>(a, st);
-    return row_voigt<1, kRowMaxT1, false, false>(a, st);
+        return L.twr ? row_voigt<2, kRowMaxT2, true, true, false>(a, st)
+                     : row_voigt<2, kRowMaxT2, false, true, false>(a, st);
+    if (L.maxt == kRowMaxT2L) return row_voigt<2, kRowMaxT2L, false, false, true>(a, st);
+    return row_voigt<1, kRowMaxT1, false, false, true>(a, st);
 }
 
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st) {
