@@ -766,7 +766,8 @@ template <> struct RowT<2> {
 template <> struct RowT<1> {
     using E = float2;
     __device__ static int pad(int i) { return rp16(i); }
-    __host__ __device__ static constexpr int len(int n) { return n + (n >> 4) + 1; }
+    // even, so the second work buffer starts 16-byte aligned (cp.async staging)
+    __host__ __device__ static constexpr int len(int n) { return n + (n >> 4) + 2; }
     __device__ static void split(E t, float2& a, float2& b) {
         a = t;
         b = make_float2(0.f, 0.f);
@@ -887,17 +888,18 @@ __device__ __forceinline__ void stage_rows(float2* dst, const float2* ya, const 
 }
 __device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
-// first pass from the staged rows (stage = [row a | row b], n2 each)
-template <int R, bool TWR>
-__device__ __forceinline__ void row_first_staged(const float2* stage, bool two, const float2* twr, float4* out,
-                                                 int L) {
+// first pass from the staged rows (stage = [row a | row b], n2 each; row a
+// only for PAIRS = 1)
+template <int R, int PAIRS, bool TWR>
+__device__ __forceinline__ void row_first_staged(const float2* stage, bool two, const float2* twr,
+                                                 typename RowT<PAIRS>::E* out, int L) {
     const int M = L / R;
     for (int j = threadIdx.x; j < M; j += blockDim.x) {
         float2 A[R], B[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             A[r] = stage[j + r * M];
-            B[r] = two ? stage[L + j + r * M] : make_float2(0.f, 0.f);
+            B[r] = PAIRS == 2 && two ? stage[L + j + r * M] : make_float2(0.f, 0.f);
             if (TWR) {
                 const float2 w = twr[j + r * M];
                 A[r] = cmul(A[r], w);
@@ -905,13 +907,16 @@ __device__ __forceinline__ void row_first_staged(const float2* stage, bool two, 
             }
         }
         dftR<R>(A);
-        dftR<R>(B);
+        if (PAIRS == 2) dftR<R>(B);
 #pragma unroll
-        for (int r = 0; r < R; ++r) out[rp8(j * R + r)] = make_float4(A[r].x, A[r].y, B[r].x, B[r].y);
+        for (int r = 0; r < R; ++r) out[RowT<PAIRS>::pad(j * R + r)] = RowT<PAIRS>::join(A[r], B[r]);
     }
 }
 
-template <int PAIRS, int MAXT, bool TWR, bool STAGE, bool TWS>
+// STAGE: the next two rows are staged in a buffer of their own.  SF: the next
+// rows are staged in the work buffer that the last pass does not read, and
+// the first pass reads them from there (the buffers swap roles).
+template <int PAIRS, int MAXT, bool TWR, bool STAGE, bool TWS, bool SF>
 __global__ void __launch_bounds__(MAXT, MAXT <= 384 ? 2 : 1) k_row_fft_voigt(const VoigtArgs a) {
     using E = typename RowT<PAIRS>::E;
     extern __shared__ float4 sm4[];
@@ -947,21 +952,28 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 384 ? 2 : 1) k_row_fft_voigt(con
     for (int r = 0; r < 8; ++r) acc[r] = make_float2(0.f, 0.f);
 
     auto row_ptr = [&](int jj) { return a.y + ((int64_t)jj * a.n1 + k1) * n2; };
-    if (STAGE && j0 < j1) stage_rows(stage, row_ptr(j0), j0 + 1 < j1 ? row_ptr(j0 + 1) : nullptr, n2);
+    auto stage_group = [&](float2* dst, int jj) {   // rows of pair group jj (two for PAIRS = 2)
+        stage_rows(dst, row_ptr(jj), PAIRS == 2 && jj + 1 < j1 ? row_ptr(jj + 1) : nullptr, n2);
+    };
+    E* wbuf = buf0;   // first-pass output
+    E* fbuf = buf1;   // SF: the staged rows of the current pair group
+    if (STAGE && j0 < j1) stage_group(stage, j0);
+    if (SF && j0 < j1) stage_group(reinterpret_cast<float2*>(fbuf), j0);
     for (int j = j0; j < j1; j += PAIRS) {
         const bool two = PAIRS == 2 && j + 1 < j1;
-        if (STAGE) {
+        if (STAGE || SF) {
+            const float2* src = STAGE ? stage : reinterpret_cast<const float2*>(fbuf);
             stage_wait();
-            __syncthreads();   // staged rows (and twr) visible to all threads
+            __syncthreads();   // staged rows (and the twiddle tables) visible to all threads
             switch (P.radix[0]) {
-                case 2: row_first_staged<2, TWR>(stage, two, twr, reinterpret_cast<float4*>(buf0), n2); break;
-                case 3: row_first_staged<3, TWR>(stage, two, twr, reinterpret_cast<float4*>(buf0), n2); break;
-                case 4: row_first_staged<4, TWR>(stage, two, twr, reinterpret_cast<float4*>(buf0), n2); break;
-                case 5: row_first_staged<5, TWR>(stage, two, twr, reinterpret_cast<float4*>(buf0), n2); break;
-                default: row_first_staged<8, TWR>(stage, two, twr, reinterpret_cast<float4*>(buf0), n2); break;
+                case 2: row_first_staged<2, PAIRS, TWR>(src, two, twr, wbuf, n2); break;
+                case 3: row_first_staged<3, PAIRS, TWR>(src, two, twr, wbuf, n2); break;
+                case 4: row_first_staged<4, PAIRS, TWR>(src, two, twr, wbuf, n2); break;
+                case 5: row_first_staged<5, PAIRS, TWR>(src, two, twr, wbuf, n2); break;
+                default: row_first_staged<8, PAIRS, TWR>(src, two, twr, wbuf, n2); break;
             }
             __syncthreads();   // stage consumed: prefetch the next two rows under the remaining passes
-            if (j + 2 < j1) stage_rows(stage, row_ptr(j + 2), j + 3 < j1 ? row_ptr(j + 3) : nullptr, n2);
+            if (STAGE && j + 2 < j1) stage_group(stage, j + 2);
         } else {
             const float2* ya = row_ptr(j);
             const float2* yb = two ? row_ptr(j + 1) : nullptr;
@@ -975,8 +987,8 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 384 ? 2 : 1) k_row_fft_voigt(con
             }
             __syncthreads();
         }
-        E* in = buf0;
-        E* out = buf1;
+        E* in = wbuf;
+        E* out = fbuf;
         for (int p = 1; p < P.npass - 1; ++p) {
             const int Ns = P.ns[p];
             const unsigned mag = P.mag[p];
@@ -992,6 +1004,8 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 384 ? 2 : 1) k_row_fft_voigt(con
             in = out;
             out = t;
         }
+        // `out` is free until the next first pass: stage the next pair group there
+        if (SF && j + PAIRS < j1) stage_group(reinterpret_cast<float2*>(out), j + PAIRS);
         // last pass (radix 8, sub-length ML, no shuffle: output t = jl + r ML),
         // Voigt weights and accumulation in registers
         if (jl < ML) {
@@ -1054,6 +1068,10 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 384 ? 2 : 1) k_row_fft_voigt(con
             }
         }
         __syncthreads();
+        if (SF) {   // the staged rows are in `out`; the next first pass writes `in`
+            wbuf = in;
+            fbuf = out;
+        }
     }
     if (jl < ML) {
         float2* g = a.g + (int64_t)k1 * n2;
@@ -1632,12 +1650,12 @@ int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st) {
     }
 }
 
-template <int PAIRS, int MAXT, bool TWR, bool STAGE, bool TWS>
+template <int PAIRS, int MAXT, bool TWR, bool STAGE, bool TWS, bool SF>
 static int row_voigt(const VoigtArgs& a, cudaStream_t st) {
     const size_t smem = row_voigt_smem<PAIRS>(a.n2, TWR, STAGE, TWS);
-    ALLOW_SMEM((k_row_fft_voigt<PAIRS, MAXT, TWR, STAGE, TWS>), smem);
+    ALLOW_SMEM((k_row_fft_voigt<PAIRS, MAXT, TWR, STAGE, TWS, SF>), smem);
     dim3 grid(a.n1, (a.n_pairs + kPairGroup - 1) / kPairGroup);
-    k_row_fft_voigt<PAIRS, MAXT, TWR, STAGE, TWS><<<grid, a.threads, smem, st>>>(a);
+    k_row_fft_voigt<PAIRS, MAXT, TWR, STAGE, TWS, SF><<<grid, a.threads, smem, st>>>(a);
     return check_launch();
 }
 
@@ -1672,10 +1690,10 @@ int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st) {
     if (a.threads < a.n2 / 8 || a.threads > L.maxt || a.threads % 32) return RG_ERR_RANGE;
     if (L.pairs != a.pairs_per_pass || L.twr != a.row_twiddle_table) return RG_ERR_RANGE;
     if (L.maxt == kRowMaxT2)
-        return L.twr ? row_voigt<2, kRowMaxT2, true, true, false>(a, st)
-                     : row_voigt<2, kRowMaxT2, false, true, false>(a, st);
-    if (L.maxt == kRowMaxT2L) return row_voigt<2, kRowMaxT2L, false, false, true>(a, st);
-    return row_voigt<1, kRowMaxT1, false, false, true>(a, st);
+        return L.twr ? row_voigt<2, kRowMaxT2, true, true, false, false>(a, st)
+                     : row_voigt<2, kRowMaxT2, false, true, false, false>(a, st);
+    if (L.maxt == kRowMaxT2L) return row_voigt<2, kRowMaxT2L, false, false, true, true>(a, st);
+    return row_voigt<1, kRowMaxT1, false, false, true, true>(a, st);
 }
 
 int launch_row_ifft(const RowIfftArgs& a, cudaStream_t st) {
