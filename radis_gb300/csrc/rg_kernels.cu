@@ -563,17 +563,22 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
 
     if (warp == 0) {   // producer
         if (lane != 0) return;
-        uint32_t c = 0;   // chunks issued
+        uint32_t c = 0;       // chunks issued
+        int buf = 0;          // ring slot of chunk c (c mod S, kept incrementally)
+        uint32_t round = 0;   // c / S: slot reuse number
         bool bad = false;
         for (int q = 0; q < nq && !bad; ++q)
             for (int cs = rng[q].x; cs < rng[q].y; cs += ch) {
-                const int buf = (int)(c % (uint32_t)S);
-                if (c >= (uint32_t)S && !mbar_wait(&empty[buf], ((c / (uint32_t)S) - 1) & 1)) {
+                if (round > 0 && !mbar_wait(&empty[buf], (round - 1) & 1)) {
                     bad = true;
                     break;
                 }
                 issue_chunk(a, smem + buf * sb, &full[buf], cs, min(ch, rng[q].y - cs));
                 ++c;
+                if (++buf == S) {
+                    buf = 0;
+                    ++round;
+                }
             }
         if (bad) atomicExch(a.err, 1u);
         // the last copies must land before the CTA may end (normally already consumed)
@@ -588,7 +593,8 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
     const bool has_dl = a.dl != nullptr, has_iso = a.iso != nullptr;
     const int ct = threadIdx.x - 32, nct = blockDim.x - 32;
     const int cw = warp - 1;
-    uint32_t g = 0;         // chunks consumed so far
+    int buf = 0;            // ring slot of the next chunk (chunks consumed mod S)
+    uint32_t par = 0;       // phase parity of its "full" barrier
     unsigned counted = 0;
     bool bad = false;
     for (int q = 0; q < nq; ++q) {
@@ -596,9 +602,8 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
         const int tk = min(a.TK, a.n_v - k_start);
         const int b = rng[q].y;
         for (int cs = rng[q].x; cs < b && !bad; cs += ch) {
-            const int buf = (int)(g % (uint32_t)S);
             // every lane acquires the TMA data through the mbarrier itself
-            const bool ok = mbar_wait(&full[buf], (g / (uint32_t)S) & 1);
+            const bool ok = mbar_wait(&full[buf], par);
             if (!__all_sync(0xffffffffu, ok)) {
                 bad = true;
                 break;
@@ -607,7 +612,10 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
                                      tk, tile, fxs, ct, nct);
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[buf]);   // this warp is done with the buffer
-            ++g;
+            if (++buf == S) {
+                buf = 0;
+                par ^= 1u;
+            }
         }
         // all consumer warps done with the tile (and agree on failures)
         int any_bad;
