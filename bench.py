@@ -353,6 +353,49 @@ def run_serving(ctx, L, lists, n_req, slots, seed=11):
     }
 
 
+def run_slit(ctx, abscoeff_dev, vmin, dv, path_length=1.0, fwhm=0.5, reps=20):
+    """Instrument slit on the spectrum of the bench workload: transmittance
+    exp(-abscoeff L) convolved with a triangular slit of ``fwhm`` cm-1
+    (generated and resampled on the host as the reference does), the
+    convolution on the GPU (rg_slit_convolve).  Times the device convolution
+    with CUDA events and, for comparison, the reference's own CPU algorithm
+    for it (scipy.signal.oaconvolve, radis/tools/slit.py:737) on the host."""
+    import numpy as np
+    import torch
+    from scipy.signal import oaconvolve
+
+    from radis_gb300 import slit as S
+    n = abscoeff_dev.numel()
+    wstep = dv
+    w_s, I_s = S.triangular_slit(fwhm, wstep, center=vmin + dv * (n // 2))
+    taps = S.slit_on_grid(w_s, I_s, wstep)
+    tr = torch.exp(-abscoeff_dev.double() * path_length).float()
+    out = torch.empty_like(tr)
+    st = torch.cuda.current_stream()
+    for _ in range(3):
+        S.convolve_device(tr, taps, wstep, mode="valid", out=out, ctx=ctx)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        S.convolve_device(tr, taps, wstep, mode="valid", out=out, ctx=ctx)
+    e1.record(st)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    host = tr.double().cpu().numpy()
+    t0 = time.perf_counter()
+    ref = oaconvolve(host, taps, mode="same") * wstep
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    got = out.double().cpu().numpy()
+    ok = ~np.isnan(got)
+    err = float(np.max(np.abs(got[ok] - ref[ok])) / np.max(np.abs(ref[ok])))
+    return {"workload": f"transmittance of the bench spectrum ({n} points, L = {path_length} cm) with a "
+                        f"triangular slit of FWHM {fwhm} cm-1 ({len(taps)} taps on the {dv} cm-1 step), "
+                        "mode 'valid'",
+            "taps": int(len(taps)), "gpu_ms": ms, "gflop_s": 2.0 * n * len(taps) / (ms * 1e-3) / 1e9,
+            "cpu_reference_ms": cpu_ms, "cpu_reference": "scipy.signal.oaconvolve (FFT overlap-add), 1 core",
+            "max_rel_err_vs_cpu": err}
+
+
 def run_autodiff(ctx, L, n_cond=64, seed=12):
     """Derivative configuration: 64 seeded conditions on the CO-like 10k list
     at 0.001 cm-1 (1900-2300, 400 001 points), T log-U[300, 3000] K, p
@@ -557,6 +600,9 @@ def run_ours(args):
                 "sample": (f"oracle (FP64 numpy restatement of the reference CPU LDM path): scaling+scatter "
                            f"of {m} of {n_lines} lines scaled x{n_lines / m:.0f} ({tl:.2f} s) + full FFT/Voigt "
                            f"stage ({tc:.2f} s, scipy.fft workers={workers}); add.at single-threaded")}
+        if ws == 1 and not args.no_slit:
+            plan.synthesize_device(T, p, x, out.data_ptr(), torch.cuda.current_stream().cuda_stream or 1)
+            res["slit"] = run_slit(ctx, out, vmin, dv)
         if ws == 1 and not args.no_autodiff:
             res["autodiff"] = run_autodiff(ctx, L)
         if ws == 1 and not args.no_serving:
@@ -590,6 +636,7 @@ def main():
     ap.add_argument("--workload", default=WORKLOAD, choices=sorted(WORKLOADS))
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-autodiff", action="store_true")
+    ap.add_argument("--no-slit", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=120)
     ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--serve-h2o-lines", type=int, default=100_000_000)

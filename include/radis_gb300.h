@@ -16,6 +16,8 @@
  *        get_griddims (params.py:89-155, gpu.py:372-374)
  *   rg_synthesize_quantities <- gpuApp.iterate + the host post-processing of
  *        eq_spectrum_gpu (radis/lbl/factory.py:1284-1297), on the device
+ *   rg_slit_convolve <- radis/tools/slit.py:convolve_with_slit (the CPU
+ *        instrument slit the reference applies after the GPU path)
  *   rg_synthesize / rg_synthesize_host <- gpuApp.iterate (gpu.py:302-370):
  *        clear -> FillLDM (cmdFillLDM.comp) -> R2C FFT -> ApplyLineshapes
  *        (cmdApplyLineshapes.comp) -> C2R IFFT -> D2H
@@ -167,6 +169,20 @@ int rg_synthesize(rg_plan* plan, const rg_conditions* cond, float* out_dev, void
  * cond->T) in physical units.  Asynchronous on `stream`. */
 int rg_synthesize_quantities(rg_plan* plan, const rg_conditions* cond, double path_length, float* out_dev,
                              void* stream, rg_spectrum_info* info);
+
+/* Instrument slit on the device (replaces the convolution of
+ * radis/tools/slit.py:convolve_with_slit, :737, and remove_boundary,
+ * :1063-1072; the reference's GPU path leaves it to the CPU, gpu.py:308-310):
+ * out[i] = wstep * sum_j slit[j] in[i + (n_slit-1)/2 - j], zero outside
+ * [0, n) -- the 'same' part of the full convolution.  RG_SLIT_VALID also sets
+ * the first (la-1)/2 and last la/2 outputs to NaN, la = min(n, n_slit).
+ * `slit_dev` is the slit sampled on the spectrum's step (n_slit floats);
+ * `out_dev` must not overlap `in_dev`.  Asynchronous on `stream` (NULL: the
+ * context's stream). */
+#define RG_SLIT_SAME 0
+#define RG_SLIT_VALID 1
+int rg_slit_convolve(rg_ctx* ctx, const float* in_dev, int64_t n, const float* slit_dev, int32_t n_slit,
+                     double wstep, int32_t mode, float* out_dev, void* stream);
 
 /* Sums (ms) of the stage times recorded with timing = 2 since the last call:
  * scatter, fft-col, fft-row+voigt, ifft-row, ifft-col, total; *count =

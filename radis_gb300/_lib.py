@@ -24,7 +24,7 @@ EXPORTS = [
     "rg_lines_free", "rg_lines_count", "rg_plan_create", "rg_plan_free", "rg_plan_grid", "rg_grid_estimate",
     "rg_synthesize", "rg_synthesize_host", "rg_debug_ldm", "rg_plan_stage_times",
     "rg_server_create", "rg_server_submit", "rg_server_wait", "rg_server_stats_get", "rg_server_destroy",
-    "rg_synthesize_static", "rg_backward", "rg_jvp", "rg_synthesize_quantities",
+    "rg_synthesize_static", "rg_backward", "rg_jvp", "rg_synthesize_quantities", "rg_slit_convolve",
 ]
 
 
@@ -134,6 +134,7 @@ def load(path: str | None = None):
         "rg_jvp": ([vp, C.POINTER(Conditions), vp, vp, vp, C.POINTER(SpectrumInfo)], C.c_int),
         "rg_synthesize_quantities": ([vp, C.POINTER(Conditions), C.c_double, vp, vp, C.POINTER(SpectrumInfo)],
                                      C.c_int),
+        "rg_slit_convolve": ([vp, vp, i64, vp, C.c_int32, C.c_double, C.c_int32, vp, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -169,6 +170,14 @@ class Context:
         if not self._h:
             raise RgError(7, "context is closed")
         return self._h
+
+    def slit_convolve(self, in_dev_ptr: int, n: int, slit_dev_ptr: int, n_slit: int, wstep: float,
+                      valid: bool, out_dev_ptr: int, stream_ptr: int | None = None):
+        """rg_slit_convolve: out = wstep * (in conv slit)['same'] on the device,
+        NaN on the boundary points when ``valid``."""
+        check(load().rg_slit_convolve(self.handle, C.c_void_p(in_dev_ptr), int(n), C.c_void_p(slit_dev_ptr),
+                                      int(n_slit), float(wstep), 1 if valid else 0, C.c_void_p(out_dev_ptr),
+                                      C.c_void_p(stream_ptr) if stream_ptr else None))
 
     def close(self):
         """Close the line lists (and their plans) still open, then the context."""

@@ -1399,6 +1399,28 @@ int rg_synthesize_quantities(rg_plan* P, const rg_conditions* c, double path_len
     return RG_OK;
 }
 
+int rg_slit_convolve(rg_ctx* ctx, const float* in_dev, int64_t n, const float* slit_dev, int32_t n_slit,
+                     double wstep, int32_t mode, float* out_dev, void* stream) {
+    g_err.clear();
+    if (!valid(ctx) || !in_dev || !slit_dev || !out_dev) return fail(RG_ERR_ARG, "invalid argument");
+    if (n < 0 || n_slit <= 0) return fail(RG_ERR_ARG, "n = %lld, n_slit = %d", (long long)n, (int)n_slit);
+    if (mode != RG_SLIT_SAME && mode != RG_SLIT_VALID) return fail(RG_ERR_ARG, "unknown slit mode %d", (int)mode);
+    if (!(wstep > 0)) return fail(RG_ERR_ARG, "wstep must be positive");
+    if (in_dev < out_dev + n && out_dev < in_dev + n) return fail(RG_ERR_ARG, "out_dev overlaps in_dev");
+    CU(cudaSetDevice(ctx->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    SlitArgs a;
+    a.in = in_dev;
+    a.slit = slit_dev;
+    a.out = out_dev;
+    a.n = n;
+    a.m = n_slit;
+    a.scale = (float)wstep;
+    a.valid = mode == RG_SLIT_VALID;
+    RG(launch_slit_conv(a, st));
+    return RG_OK;
+}
+
 int rg_plan_stage_times(rg_plan* P, double* sum_ms, int64_t* count) {
     g_err.clear();
     if (!valid(P) || !sum_ms || !count) return fail(RG_ERR_ARG, "invalid argument");

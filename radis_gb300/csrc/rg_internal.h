@@ -220,6 +220,18 @@ struct GaussArgs {
     int tile_out;         // outputs per CTA (kGaussTile, or less the 2 Kb halo, multiple of 8)
 };
 
+// Instrument slit convolution ('same' part of the full convolution, x scale)
+constexpr int kSlitPass = 512;        // slit taps staged per pass
+struct SlitArgs {
+    const float* in;      // spectrum [n]
+    const float* slit;    // slit sampled on the spectrum step [m]
+    float* out;           // [n], not aliasing in
+    int64_t n;
+    int m;
+    float scale;          // wstep (slit.py:737)
+    int valid;            // 1: NaN on the boundary points (remove_boundary 'valid')
+};
+
 struct QuantArgs {         // post-processing epilogue (radis/lbl/factory.py:1284-1297)
     const float* abscoeff;    // n_v, in units of exp(log_scale)
     float* out;               // 4 rows of n_v: absorbance (same units), emissivity, transmittance, radiance
@@ -281,6 +293,7 @@ int launch_row_ifft_adj(const AdjRowArgs& a, cudaStream_t st);
 int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st);
 int launch_gather_grad(const GradArgs& a, int grid, cudaStream_t st);
 int launch_gauss_merge(const GaussArgs& a, int out_rows, cudaStream_t st);
+int launch_slit_conv(const SlitArgs& a, cudaStream_t st);
 int launch_quantities(const QuantArgs& a, cudaStream_t st);
 int launch_scatter_tangent(const GradArgs& a, int grid, cudaStream_t st);
 int col_block(int n1);               // columns per CTA of the column FFTs

@@ -1338,6 +1338,48 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
     }
 }
 
+// Instrument slit (radis/tools/slit.py:737 and remove_boundary, :1063-1072):
+// out[i] = scale sum_j slit[j] in[i + (m-1)/2 - j], the 'same' part of the
+// full convolution, zero outside [0, n); written as a correlation with the
+// reversed slit r[u] = slit[m-1-u]: out[i] = scale sum_u r[u] in[i - m/2 + u].
+// One CTA: kGaussTile outputs (8 per thread); taps in passes of kSlitPass,
+// each with its own staged input window, through the same register-window
+// convolution as the Gaussian stage.  'valid' mode: the first (la-1)/2 and
+// last la/2 outputs are NaN, la = min(n, m).
+__global__ void __launch_bounds__(256) k_slit_conv(const SlitArgs a) {
+    extern __shared__ __align__(16) float ssm[];
+    constexpr int TW = kGaussTile;
+    constexpr int P = kGaussPer;
+    float* taps = ssm;                       // kSlitPass (padded to 8)
+    float* xs = ssm + kSlitPass + 16;        // TW + KP + 8 <= TW + kSlitPass + 16
+    const int64_t p0 = (int64_t)blockIdx.x * TW;
+    const int t0 = threadIdx.x * P;
+    const int64_t half = a.m / 2;
+    float acc[P];
+#pragma unroll
+    for (int i = 0; i < P; ++i) acc[i] = 0.f;
+    for (int u0 = 0; u0 < a.m; u0 += kSlitPass) {
+        const int kb = min(kSlitPass, a.m - u0);
+        const int KP = (kb + 7) & ~7;
+        const int64_t base = p0 - half + u0;   // input index of xs[0]
+        __syncthreads();   // previous pass consumed
+        for (int jj = threadIdx.x; jj < KP; jj += blockDim.x) taps[jj] = jj < kb ? a.slit[a.m - 1 - (u0 + jj)] : 0.f;
+        for (int t = threadIdx.x; t < TW + KP + 8; t += blockDim.x) {
+            const int64_t k = base + t;
+            xs[t] = k >= 0 && k < a.n ? __ldg(&a.in[k]) : 0.f;
+        }
+        __syncthreads();
+        conv_window(acc, xs, taps, t0, KP);
+    }
+    const int64_t la = a.n < (int64_t)a.m ? a.n : (int64_t)a.m;
+    const int64_t ea = a.valid ? (la - 1) / 2 : 0, eb = a.valid ? la / 2 : 0;
+#pragma unroll
+    for (int i = 0; i < P; ++i) {
+        const int64_t idx = p0 + t0 + i;
+        if (idx < a.n) a.out[idx] = idx < ea || idx >= a.n - eb ? __int_as_float(0x7fc00000) : acc[i] * a.scale;
+    }
+}
+
 // Adjoint row stage, one CTA per (row k1, pair j): H = Ghat (V_2j + i V_2j+1)
 // on the row's bins k = k1 + n1 t, inverse row DFT, inverse four-step twiddle
 // w_N^{-t k1}; output y[j][k1][t].
@@ -1778,6 +1820,16 @@ int launch_gauss_merge(const GaussArgs& a, int out_rows, cudaStream_t st) {
         if (a.K[w] < 0 || a.K[w] > kGaussMaxK) return RG_ERR_RANGE;
     dim3 grid((Lr + a.tile_out - 1) / a.tile_out, out_rows);
     k_gauss_merge<<<grid, 256, smem, st>>>(a);
+    return check_launch();
+}
+
+int launch_slit_conv(const SlitArgs& a, cudaStream_t st) {
+    if (a.n <= 0) return RG_OK;
+    if (a.m <= 0) return RG_ERR_RANGE;
+    const size_t smem = sizeof(float) * ((kSlitPass + 16) + (kGaussTile + kSlitPass + 16));
+    const int64_t blocks = (a.n + kGaussTile - 1) / kGaussTile;
+    if (blocks > 0x7fffffff) return RG_ERR_RANGE;
+    k_slit_conv<<<(unsigned)blocks, 256, smem, st>>>(a);
     return check_launch();
 }
 

@@ -103,7 +103,9 @@ class Spectrum:
                    mole_fraction=None, path_length=None, slit_function=None, verbose=False):
         """Re-run the resident GPU application at new conditions and return
         ``var`` (spectrum.py:6438-6572).  Only abscoeff comes from the GPU; the
-        other quantities are re-derived on request."""
+        other quantities are re-derived on request.  With ``slit_function``
+        the slit is applied on the GPU (``apply_slit``) and a convolved
+        quantity (transmittance, radiance, emissivity) is returned."""
         if self.gpu_app is None:
             warnings.warn("no GPU application attached to this Spectrum (exit_gpu was "
                           "called or exit_gpu=True was used)", GPUInitWarning)
@@ -127,9 +129,60 @@ class Spectrum:
         self._q["abscoeff"] = abscoeff
         n_L, n_G = self.gpu_app.get_griddims()
         c.update(NwL=n_L, NwG=n_G, gpu_times=times)
+        if slit_function is not None:
+            # the reference stores the slit and leaves its application as a TODO
+            # (spectrum.py:6527-6534); here the GPU slit applies it
+            c["slit_function"] = slit_function
+            self.apply_slit(slit_function, shape=c.get("slit_shape", "triangular"))
+            if var in self._q:
+                return self.get(var)[1]
         key = {"transmittance": "transmittance_noslit", "radiance": "radiance_noslit",
                "emissivity": "emissivity_noslit"}.get(var, var)
         return self.get(key)[1]
+
+    def apply_slit(self, slit_function, unit="cm-1", shape="triangular", center_wavespace=None, norm_by="area",
+                   mode="valid", store=True, slit_dispersion=None, assert_evenly_spaced=True, verbose=False,
+                   inplace=True, calc_range=4):
+        """Convolve every ``*_noslit`` quantity with the instrument slit and
+        store it without the suffix (radis/spectrum/spectrum.py:3127-3579),
+        the convolution on the GPU (``radis_gb300.slit``).  ``slit_function``:
+        FWHM (``shape`` 'triangular' or 'gaussian'), (top, base) for
+        'trapezoidal', or sampled (w, I) arrays; given in the spectrum's
+        wavespace (cm-1).  Slit dispersion is not provided."""
+        import torch
+
+        from . import slit as S
+
+        if slit_dispersion is not None:
+            raise NotImplementedError("slit dispersion is not provided")
+        if "abscoeff" in self._q and "transmittance_noslit" not in self._q:
+            self._update("transmittance_noslit")
+        varlist = [k for k in self.get_vars() if k.endswith("_noslit")]
+        if not varlist:
+            raise AssertionError("No spectral arrays to apply slit on. Spectral arrays to be convolved "
+                                 f"should end with _noslit. Available arrays in Spectrum : {self.get_vars()}")
+        w = np.asarray(self._q["wavenumber"], dtype=np.float64)
+        wstep = np.abs(np.diff(w)).min()
+        if assert_evenly_spaced and not np.allclose(np.diff(w), np.diff(w).mean(), atol=wstep * 1e-3):
+            raise ValueError("Spectrum is not evenly spaced. Cannot apply slit function.")
+        if center_wavespace is None:
+            center_wavespace = w[len(w) // 2]
+        w_slit, I_slit = S.get_slit_function(slit_function, unit=unit, norm_by=norm_by, shape=shape,
+                                             center_wavespace=center_wavespace, return_unit="cm-1",
+                                             wstep=wstep, calc_range=calc_range)
+        taps = S.slit_on_grid(w_slit, I_slit, wstep)
+        s = self if inplace else Spectrum(dict(self._q), self.units, self.conditions, self.cond_units,
+                                          name=self.name)
+        dev = torch.device("cuda", getattr(getattr(self.gpu_app, "ctx", None), "device", 0) or 0)
+        ctx = getattr(self.gpu_app, "ctx", None)
+        for qns in varlist:
+            I_dev = torch.as_tensor(np.asarray(self._q[qns], dtype=np.float32), device=dev)
+            out = S.convolve_device(I_dev, taps, wstep, mode=mode, ctx=ctx)
+            s._q[qns[:-7]] = out.cpu().numpy()
+            s.units[qns[:-7]] = self.units.get(qns, "")
+        s.conditions.update(slit_function=slit_function, slit_unit=unit, slit_shape=shape, norm_by=norm_by,
+                            slit_dispersion=slit_dispersion)
+        return s
 
     def exit_gpu(self):
         """Release the GPU application (spectrum.py:6574-6577)."""
