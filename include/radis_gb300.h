@@ -18,6 +18,10 @@
  *        eq_spectrum_gpu (radis/lbl/factory.py:1284-1297), on the device
  *   rg_slit_convolve <- radis/tools/slit.py:convolve_with_slit (the CPU
  *        instrument slit the reference applies after the GPU path)
+ *   rg_lines_set_partition / rg_partition_eval <- the tabulated partition
+ *        functions behind eq_spectrum_gpu's Q(T) callables
+ *        (radis/levels/partfunc.py:1191-1192, partfunc_cdsd.py:84-117;
+ *        gpuApp evaluates them per iterate, radis/gpu/params.py:154-155)
  *   rg_synthesize / rg_synthesize_host <- gpuApp.iterate (gpu.py:302-370):
  *        clear -> FillLDM (cmdFillLDM.comp) -> R2C FFT -> ApplyLineshapes
  *        (cmdApplyLineshapes.comp) -> C2R IFFT -> D2H
@@ -169,6 +173,27 @@ int rg_synthesize(rg_plan* plan, const rg_conditions* cond, float* out_dev, void
  * cond->T) in physical units.  Asynchronous on `stream`. */
 int rg_synthesize_quantities(rg_plan* plan, const rg_conditions* cond, double path_length, float* out_dev,
                              void* stream, rg_spectrum_info* info);
+
+/* Tabulated partition function Q(T) of isotopologue `iso` (0-based, < the
+ * list's n_iso), copied from n points (T strictly increasing, Q > 0):
+ *   RG_Q_LINEAR  np.interp, clamped outside the table
+ *                (radis/levels/partfunc.py:1191-1192, PartFuncExoMol);
+ *   RG_Q_CUBIC   interpolating cubic spline as scipy splrep/splev (n >= 4),
+ *                refused beyond [0.95 Tmin, 1.05 Tmax] with RG_ERR_RANGE
+ *                (radis/levels/partfunc_cdsd.py:84-117, PartFuncCO2_CDSDtab).
+ * Once every isotopologue of the list has a table, rg_conditions.q_ratio =
+ * NULL means Q(Tref)/Q(T) from the tables (instead of 1), and rg_backward /
+ * rg_jvp with dlnq_dT = NULL take d ln(Q(Tref)/Q(T))/dT from them.  Not to be
+ * called while spectra of the list are in flight. */
+#define RG_Q_LINEAR 0
+#define RG_Q_CUBIC 1
+int rg_lines_set_partition(rg_lines* lines, int32_t iso, int64_t n, const double* T, const double* Q,
+                           int32_t interp);
+
+/* Host-only evaluation of a partition table (no device involved): Q(t) and
+ * dQ/dT(t) (dq_dt may be NULL). */
+int rg_partition_eval(int64_t n, const double* T, const double* Q, int32_t interp, double t, double* q,
+                      double* dq_dt);
 
 /* Instrument slit on the device (replaces the convolution of
  * radis/tools/slit.py:convolve_with_slit, :737, and remove_boundary,

@@ -25,6 +25,7 @@ EXPORTS = [
     "rg_synthesize", "rg_synthesize_host", "rg_debug_ldm", "rg_plan_stage_times",
     "rg_server_create", "rg_server_submit", "rg_server_wait", "rg_server_stats_get", "rg_server_destroy",
     "rg_synthesize_static", "rg_backward", "rg_jvp", "rg_synthesize_quantities", "rg_slit_convolve",
+    "rg_lines_set_partition", "rg_partition_eval",
 ]
 
 
@@ -135,6 +136,9 @@ def load(path: str | None = None):
         "rg_synthesize_quantities": ([vp, C.POINTER(Conditions), C.c_double, vp, vp, C.POINTER(SpectrumInfo)],
                                      C.c_int),
         "rg_slit_convolve": ([vp, vp, i64, vp, C.c_int32, C.c_double, C.c_int32, vp, vp], C.c_int),
+        "rg_lines_set_partition": ([vp, C.c_int32, i64, vp, vp, C.c_int32], C.c_int),
+        "rg_partition_eval": ([i64, vp, vp, C.c_int32, C.c_double, C.POINTER(C.c_double),
+                               C.POINTER(C.c_double)], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -152,6 +156,19 @@ def check(code: int):
 
 def ptr(a: np.ndarray | None):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+PARTITION_KINDS = {"linear": 0, "cubic": 1}   # RG_Q_LINEAR, RG_Q_CUBIC
+
+
+def partition_eval(T, Q, kind: str, t: float):
+    """Host-only rg_partition_eval: (Q(t), dQ/dT(t)) of a table."""
+    T = np.ascontiguousarray(T, dtype=np.float64)
+    Q = np.ascontiguousarray(Q, dtype=np.float64)
+    q, dq = C.c_double(), C.c_double()
+    check(load().rg_partition_eval(len(T), ptr(T), ptr(Q), PARTITION_KINDS[kind], float(t), C.byref(q),
+                                   C.byref(dq)))
+    return q.value, dq.value
 
 
 class Context:
@@ -240,6 +257,16 @@ class Lines:
         if not self._h:
             raise RgError(7, "line list is closed")
         return self._h
+
+    def set_partition(self, iso: int, T, Q, kind: str = "cubic"):
+        """Tabulated Q(T) of isotopologue ``iso`` (rg_lines_set_partition):
+        'cubic' (CDSD-style spline) or 'linear' (np.interp).  With a table for
+        every isotopologue, q_ratio=None means Q(Tref)/Q(T) from the tables."""
+        T = np.ascontiguousarray(T, dtype=np.float64)
+        Q = np.ascontiguousarray(Q, dtype=np.float64)
+        if T.shape != Q.shape or T.ndim != 1:
+            raise ValueError("T and Q must be 1-D arrays of the same length")
+        check(load().rg_lines_set_partition(self.handle, int(iso), len(T), ptr(T), ptr(Q), PARTITION_KINDS[kind]))
 
     def close(self):
         """Close the plans still open on this list, then the list."""

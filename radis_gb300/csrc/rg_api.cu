@@ -102,6 +102,7 @@ struct rg_lines {
     int n_iso = 1;
     double t_ref = 296.0;
     Envelope env;
+    std::vector<QTable> qtab;       // optional tabulated Q(T) per isotopologue
     std::atomic<int> plans{0};      // plans and server requests referencing the list
     uint32_t magic = 0x52474C4E;
 };
@@ -177,6 +178,42 @@ int64_t next_smooth(int64_t x) {
 // Radix plan of a length L = 2^a 3^b 5^c: the leftover 2 or 4 first, then the
 // 3s and 5s, then radix 8 -- the last pass is radix 8 whenever 8 divides L,
 // which the row kernel relies on (n2 is a multiple of 32).
+// Partition-function ratio Q(Tref)/Q(T) of isotopologue i: the caller's,
+// else the list's tables when every isotopologue has one, else 1.
+bool have_qtables(const rg_lines* L) {
+    if ((int)L->qtab.size() != L->n_iso) return false;
+    for (const QTable& t : L->qtab)
+        if (t.T.size() < 2) return false;
+    return true;
+}
+int q_ratio_of(const rg_lines* L, const rg_conditions* c, int i, double* q) {
+    if (c->q_ratio) {
+        *q = c->q_ratio[i];
+        return RG_OK;
+    }
+    *q = 1.0;
+    if (!have_qtables(L)) return RG_OK;
+    double q_ref, q_t;
+    std::string e;
+    int rc = qtable_eval(L->qtab[i], L->t_ref, &q_ref, nullptr, &e);
+    if (!rc) rc = qtable_eval(L->qtab[i], c->T, &q_t, nullptr, &e);
+    if (rc) return fail(rc, "isotopologue %d: %s", i, e.c_str());
+    *q = q_ref / q_t;
+    return RG_OK;
+}
+// d ln(Q(Tref)/Q(T))/dT of isotopologue i: the caller's, else -Q'(T)/Q(T)
+// from the tables, else 0.
+int dlnq_of(const rg_lines* L, const double* dlnq_dT, double T, int i, double* out) {
+    *out = dlnq_dT ? dlnq_dT[i] : 0.0;
+    if (dlnq_dT || !have_qtables(L)) return RG_OK;
+    double q, dq;
+    std::string e;
+    const int rc = qtable_eval(L->qtab[i], T, &q, &dq, &e);
+    if (rc) return fail(rc, "isotopologue %d: %s", i, e.c_str());
+    *out = -dq / q;
+    return RG_OK;
+}
+
 bool radices(int L, int* rad, int* np) {
     int r = L, k = 0;
     int a = 0, b = 0, c = 0;
@@ -280,7 +317,8 @@ struct SpecHost {
     int n_nodes;       // padded to even
 };
 
-int compute_grid_env(const Envelope& E, const rg_plan_desc& d, int64_t n_ft, int n1, int n2,
+// `lines` (may be NULL: host-only estimate) supplies tabulated Q(T).
+int compute_grid_env(const Envelope& E, const rg_lines* lines, const rg_plan_desc& d, int64_t n_ft, int n1, int n2,
                      const rg_conditions* c, SpecHost* s) {
     const Envelope* L = &E;
     if (!(c->T > 0) || !(c->p_bar > 0) || !(c->x >= 0 && c->x <= 1))
@@ -339,6 +377,7 @@ int compute_grid_env(const Envelope& E, const rg_plan_desc& d, int64_t n_ft, int
     double lq = -std::numeric_limits<double>::infinity();
     for (int i = 0; i < L->n_iso; ++i) {
         double q = c->q_ratio ? c->q_ratio[i] : 1.0;
+        if (lines) RG(q_ratio_of(lines, c, i, &q));
         if (q > 0) lq = std::max(lq, std::log(q));
     }
     double smax = L->s_hi.max_at(aT);
@@ -350,7 +389,7 @@ int compute_grid_env(const Envelope& E, const rg_plan_desc& d, int64_t n_ft, int
 }
 
 int compute_grid(const rg_lines* L, const Work& W, const rg_conditions* c, SpecHost* s) {
-    return compute_grid_env(L->env, W.desc, W.n, W.n1, W.n2, c, s);
+    return compute_grid_env(L->env, L, W.desc, W.n, W.n1, W.n2, c, s);
 }
 
 // Envelope of a host line list (per-iso v0 range, width and intensity hulls).
@@ -524,7 +563,8 @@ int build_scatter_args(const rg_lines* L, const Work& W, const rg_conditions* c,
     split(-kC2 * (1.0 / T - 1.0 / L->t_ref) * kLog2e, &a->aT_hi, &a->aT_lo);
     const double dens = (c->p_bar * 1e5) / (kKb * T) * 1e-6 * c->x;
     for (int i = 0; i < L->n_iso; ++i) {
-        double q = c->q_ratio ? c->q_ratio[i] : 1.0;
+        double q;
+        RG(q_ratio_of(L, c, i, &q));
         double b = (q > 0 && dens > 0) ? (std::log(q * dens) - s.log_scale_int) * kLog2e : -1e30;
         if (b < -1e30) b = -1e30;
         split(b, &a->bI_hi[i], &a->bI_lo[i]);
@@ -846,7 +886,11 @@ int fill_grad_args(const rg_lines* L, const Work& W, const rg_conditions* c, con
     g->row_stride = W.row_stride;
     g->c2_T = (float)(kC2 / T);
     g->c2_T2 = (float)(kC2 / (T * T));
-    for (int i = 0; i < L->n_iso; ++i) g->cT0[i] = (float)((dlnq_dT ? dlnq_dT[i] : 0.0) - 1.0 / T);
+    for (int i = 0; i < L->n_iso; ++i) {
+        double dl;
+        RG(dlnq_of(L, dlnq_dT, T, i, &dl));
+        g->cT0[i] = (float)(dl - 1.0 / T);
+    }
     g->gT = (float)(0.5 / (T * s.grid.dxG));
     g->lT = (float)(1.0 / (T * s.grid.dxL));
     g->lP = (float)(1.0 / (p * s.grid.dxL));
@@ -1358,7 +1402,7 @@ int rg_grid_estimate(const rg_line_arrays* lines, const rg_isotopes* iso, const 
     auto env = std::make_unique<Envelope>();
     RG(build_envelope(lines, iso, env.get()));
     SpecHost s;
-    RG(compute_grid_env(*env, *d, (int64_t)n1 * n2, n1, n2, c, &s));
+    RG(compute_grid_env(*env, nullptr, *d, (int64_t)n1 * n2, n1, n2, c, &s));
     *out = s.grid;
     return RG_OK;
 }
@@ -1396,6 +1440,31 @@ int rg_synthesize_quantities(rg_plan* P, const rg_conditions* c, double path_len
     RG(launch_quantities(q, st));
     RG(plan_stream_end(P, st));
     if (info) *info = inf;
+    return RG_OK;
+}
+
+int rg_lines_set_partition(rg_lines* L, int32_t iso, int64_t n, const double* T, const double* Q, int32_t interp) {
+    g_err.clear();
+    if (!valid(L)) return fail(RG_ERR_ARG, "invalid line list");
+    if (iso < 0 || iso >= L->n_iso) return fail(RG_ERR_ARG, "isotopologue %d not in [0, %d)", (int)iso, L->n_iso);
+    QTable t;
+    std::string e;
+    const int rc = qtable_build(n, T, Q, interp, &t, &e);
+    if (rc) return fail(rc, "%s", e.c_str());
+    if ((int)L->qtab.size() != L->n_iso) L->qtab.resize(L->n_iso);
+    L->qtab[iso] = std::move(t);
+    return RG_OK;
+}
+
+int rg_partition_eval(int64_t n, const double* T, const double* Q, int32_t interp, double t, double* q,
+                      double* dq_dt) {
+    g_err.clear();
+    if (!q) return fail(RG_ERR_ARG, "invalid argument");
+    QTable tab;
+    std::string e;
+    int rc = qtable_build(n, T, Q, interp, &tab, &e);
+    if (!rc) rc = qtable_eval(tab, t, q, dq_dt, &e);
+    if (rc) return fail(rc, "%s", e.c_str());
     return RG_OK;
 }
 
@@ -1654,7 +1723,7 @@ int request_need(rg_server* S, const ServerReq& r, SpecHost* sh, int64_t* need, 
     int n1, n2;
     if (!choose_fft(2 * r.desc.n_v, r.desc.n_ft, &n1, &n2))
         return fail(RG_ERR_RANGE, "no supported FFT length >= %lld", (long long)(2 * r.desc.n_v));
-    RG(compute_grid_env(r.lines->env, r.desc, (int64_t)n1 * n2, n1, n2, &r.cond, sh));
+    RG(compute_grid_env(r.lines->env, r.lines, r.desc, (int64_t)n1 * n2, n1, n2, &r.cond, sh));
     const int64_t n = (int64_t)n1 * n2, rs = (r.desc.n_v + 31) / 32 * 32;
     int E;
     double pmax;
@@ -2093,7 +2162,7 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
     W.col_count = (int)d->n_v + 1 + 2 * W.E;
     W.row_stride = (d->n_v + 31) / 32 * 32;
     SpecHost s;
-    RG(compute_grid_env(L->env, W.desc, W.n, W.n1, W.n2, c, &s));
+    RG(compute_grid_env(L->env, L, W.desc, W.n, W.n1, W.n2, c, &s));
 
     // carve the scratch (256-byte aligned pieces)
     size_t off = 0;

@@ -220,6 +220,14 @@ struct GaussArgs {
     int tile_out;         // outputs per CTA (kGaussTile, or less the 2 Kb halo, multiple of 8)
 };
 
+// Tabulated partition function of one isotopologue (rg_partition.cpp)
+struct QTable {
+    int interp = RG_Q_LINEAR;
+    std::vector<double> T, Q, M;   // M: spline second derivatives (RG_Q_CUBIC)
+};
+int qtable_build(int64_t n, const double* T, const double* Q, int interp, QTable* out, std::string* err);
+int qtable_eval(const QTable& t, double T, double* q, double* dq_dT, std::string* err);
+
 // Instrument slit convolution ('same' part of the full convolution, x scale)
 constexpr int kSlitPass = 512;        // slit taps staged per pass
 struct SlitArgs {

@@ -78,6 +78,13 @@ class gpuApp:
         self.lines = L.Lines(self.ctx, lines, Mm, t_ref=TREF)
         self.plan = L.Plan(self.lines, vmin, dv, int(Nv), dxG=dxG, dxL=dxL, n_G=n_G, n_L=n_L,
                            folding_thresh=folding_thresh)
+        # tables the library can evaluate itself: Q(Tref)/Q(T) per spectrum
+        # without calling back into Python
+        from .partition import TabulatedQ
+        self._q_in_lib = all(isinstance(q, TabulatedQ) for q in self._Q)
+        if self._q_in_lib:
+            for i, q in enumerate(self._Q):
+                self.lines.set_partition(i, q.T, q.Q, q.kind)
         self._freed = False
         self.Nv, self.vmin, self.dv = int(Nv), float(vmin), float(dv)
         self._griddims = (0, 0)
@@ -93,8 +100,8 @@ class gpuApp:
         (gpu.py:308-311)."""
         if self._freed:
             raise RuntimeError("gpuApp was freed (exit_gpu)")
-        out, info = self.plan.synthesize_host(T, p, mole_fraction, q_ratio=self.q_ratio(T),
-                                              timing=True)
+        q = None if self._q_in_lib else self.q_ratio(T)
+        out, info = self.plan.synthesize_host(T, p, mole_fraction, q_ratio=q, timing=True)
         g = info.grid
         self._griddims = (g.n_L, g.n_G)
         self.last_info = info
