@@ -138,6 +138,8 @@ struct Work {
     unsigned long long* counter = nullptr;
     unsigned* err = nullptr;          // device flag set by a bounded wait that gave up
     unsigned* err_host = nullptr;     // pinned copy of err, refreshed after every spectrum
+    unsigned* err_pub = nullptr;      // device view of err_host when it is mapped (the last kernel writes it)
+    bool count_lines = false;         // count the lines in the window (timing = 1 reports it)
 };
 
 struct rg_plan {
@@ -570,7 +572,7 @@ int build_scatter_args(const rg_lines* L, const Work& W, const rg_conditions* c,
         split(b, &a->bI_hi[i], &a->bI_lo[i]);
     }
     a->stim_c = (float)(kC2 / T * kLog2e);
-    a->in_window = W.counter;
+    a->in_window = W.count_lines ? W.counter : nullptr;
     return RG_OK;
 }
 
@@ -786,7 +788,7 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
     const int grid = std::max(std::min(sa.n_tiles, sms),
                               (sa.n_tiles + kScatMaxTilesPerCta - 1) / kScatMaxTilesPerCta);
     if (ev) CU(cudaEventRecord(ev[0], st));
-    CU(cudaMemsetAsync(W.counter, 0, sizeof(unsigned long long), st));
+    if (W.count_lines) CU(cudaMemsetAsync(W.counter, 0, sizeof(unsigned long long), st));
     RG(launch_scatter(sa, grid, kScatThreads, smem, st));
     if (ev) CU(cudaEventRecord(ev[1], st));
     if (!ldm_only) {
@@ -849,8 +851,10 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
             RG(launch_col_fft_fwd(ca, st));
         }
         if (ev) CU(cudaEventRecord(ev[2], st));
-        CU(cudaMemsetAsync(W.g, 0, sizeof(float2) * (size_t)W.n, st));
-        RG(launch_row_fft_voigt(merged ? *vm : *va, st));
+        VoigtArgs& vr = merged ? *vm : *va;
+        vr.store_g = vr.n_pairs <= kPairGroup;   // one pair group per row: it stores G itself
+        if (!vr.store_g) CU(cudaMemsetAsync(W.g, 0, sizeof(float2) * (size_t)W.n, st));
+        RG(launch_row_fft_voigt(vr, st));
         if (ev) CU(cudaEventRecord(ev[3], st));
         RowIfftArgs ra;
         ra.f2 = W.f2;
@@ -865,8 +869,11 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
         ca.h = W.g;
         ca.out = out;
         ca.out_scale = (float)(std::exp(s.log_scale_int - s.log_scale_out) / ((double)W.n * W.desc.dv));
+        ca.err = W.err;
+        ca.err_pub = W.err_pub;   // mapped: the kernel publishes and clears the flag
         RG(launch_col_ifft(ca, st));
         if (ev) CU(cudaEventRecord(ev[5], st));
+        if (W.err_pub) return RG_OK;
     }
     // publish the device error flag to pinned host memory and clear it
     CU(cudaMemcpyAsync(W.err_host, W.err, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
@@ -1043,6 +1050,7 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
             if (!e) CU(cudaEventCreate(&e));
         ev = P->ev;
     }
+    P->w.count_lines = (timing == 1 && info) || ldm_only;
     RG(plan_stream_begin(P, st));
     RG(enqueue_spectrum(P->lines, P->w, c, s, out, st, ev, ldm_only));
     RG(plan_stream_end(P, st));
@@ -1324,8 +1332,9 @@ int rg_plan_create(rg_lines* L, const rg_plan_desc* d, rg_plan** out) {
     CU(cudaMalloc(&P->out_d, sizeof(float) * (size_t)d->n_v));
     CU(cudaMalloc(&W.counter, sizeof(unsigned long long)));
     CU(cudaMalloc(&W.err, sizeof(unsigned)));
-    CU(cudaHostAlloc(&W.err_host, sizeof(unsigned), cudaHostAllocDefault));
+    CU(cudaHostAlloc(&W.err_host, sizeof(unsigned), cudaHostAllocMapped));
     *W.err_host = 0;
+    CU(cudaHostGetDevicePointer((void**)&W.err_pub, W.err_host, 0));
     CU(cudaMemsetAsync(W.err, 0, sizeof(unsigned), st));
     int cm = 0;
     CU(cudaMemcpyAsync(&cm, W.cmax_dev, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -1961,8 +1970,9 @@ int rg_server_create(rg_ctx* ctx, int slots, int64_t mem_budget, rg_server** out
         CU(cudaMalloc(&sl.w.counter, sizeof(unsigned long long)));
         CU(cudaMalloc(&sl.w.err, sizeof(unsigned)));
         CU(cudaMemset(sl.w.err, 0, sizeof(unsigned)));
-        CU(cudaHostAlloc(&sl.w.err_host, sizeof(unsigned), cudaHostAllocDefault));
+        CU(cudaHostAlloc(&sl.w.err_host, sizeof(unsigned), cudaHostAllocMapped));
         *sl.w.err_host = 0;
+        CU(cudaHostGetDevicePointer((void**)&sl.w.err_pub, sl.w.err_host, 0));
     }
     ctx->lines++;   // the context stays alive while the server exists
     S->worker = std::thread(worker_loop, S);

@@ -154,10 +154,13 @@ struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
     int map_n;            // K2 fixed point: 0, or virtual row v (blocks of map_NLv rows) reads LDM
     int map_NL, map_NLv;  //   node map_l[v / map_NLv] * map_NL + v % map_NLv, zero when v % map_NLv >= map_NL
     unsigned char map_l[kMaxAxis];
+    unsigned* err;        // K4: non-null with err_pub: publish the device error flag
+    unsigned* err_pub;    //   into host-mapped memory and clear it (one thread)
 };
 
 struct VoigtArgs {        // K3 (row FFT + Voigt weights + pair reduction)
     FftLen f2;
+    int store_g;          // 1: one pair group: store the sums into G (no zeroing, no atomics)
     int threads;          // block size (row_threads), >= n2 / 8
     int pairs_per_pass;   // 2: two pairs as float4 elements; 1: one pair (long rows)
     int row_twiddle_table;// 1: the row kernel applies the four-step twiddle from a

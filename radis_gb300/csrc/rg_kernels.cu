@@ -1083,8 +1083,13 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 384 ? 2 : 1) k_row_fft_voigt(con
     }
     if (jl < ML) {
         float2* g = a.g + (int64_t)k1 * n2;
+        if (a.store_g && gridDim.y == 1) {   // the only pair group of this row: plain stores
 #pragma unroll
-        for (int r = 0; r < 8; ++r) atomicAdd(&g[jl + r * ML], acc[r]);
+            for (int r = 0; r < 8; ++r) g[jl + r * ML] = acc[r];
+        } else {
+#pragma unroll
+            for (int r = 0; r < 8; ++r) atomicAdd(&g[jl + r * ML], acc[r]);
+        }
     }
 }
 
@@ -1129,6 +1134,12 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_ifft(const ColFft
     for (int r = 0; r < 8; ++r) {
         const int64_t nidx = (int64_t)(j + r * TPC) * a.n2 + n2i;
         if (nidx < a.n_v) a.out[nidx] = v[r].x * a.out_scale;   // Re(conj(z)) = Re(z)
+    }
+    // last kernel of the spectrum: hand the error flag to the host (mapped
+    // memory, read after the stream synchronises) and clear it
+    if (a.err_pub && blockIdx.x == 0 && threadIdx.x == 0) {
+        *a.err_pub = *a.err;
+        *a.err = 0u;
     }
 }
 
