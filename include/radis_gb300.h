@@ -132,6 +132,8 @@ typedef struct {
      * layout n_L merged rows + the narrow-Gaussian node rows), how many of them
      * are merged rows and the half-width (points) of their widest Gaussian */
     int32_t fft_rows, merged_rows, merged_ext;
+    float gauss_ms;            /* merged layout: the real-space Gaussian stage's
+                                  part of stage_ms[1] (timing = 1), else 0     */
 } rg_spectrum_info;
 
 int rg_abi_version(void);
@@ -214,6 +216,10 @@ int rg_slit_convolve(rg_ctx* ctx, const float* in_dev, int64_t n, const float* s
  * spectra recorded.  Synchronises the recording stream and empties the ring.
  * (The reference's per-command Vulkan timestamps, gpu.py:260-280, 360.) */
 int rg_plan_stage_times(rg_plan* plan, double* sum_ms, int64_t* count);
+
+/* The Gaussian-stage part (merged layout) of the fft-col sum that the last
+ * rg_plan_stage_times call returned, in ms (0 without the merged layout). */
+int rg_plan_stage_times_gauss(rg_plan* plan, double* gauss_sum_ms);
 
 /* As rg_synthesize, then copies the n_v floats to `out_host` (pinned or
  * pageable) and waits for the copy: the drop-in `iterate()` form.  timing = 1

@@ -25,7 +25,7 @@ EXPORTS = [
     "rg_synthesize", "rg_synthesize_host", "rg_debug_ldm", "rg_plan_stage_times",
     "rg_server_create", "rg_server_submit", "rg_server_wait", "rg_server_stats_get", "rg_server_destroy",
     "rg_synthesize_static", "rg_backward", "rg_jvp", "rg_synthesize_quantities", "rg_slit_convolve",
-    "rg_lines_set_partition", "rg_partition_eval",
+    "rg_lines_set_partition", "rg_partition_eval", "rg_plan_stage_times_gauss",
 ]
 
 
@@ -73,7 +73,7 @@ class Grid(C.Structure):
 class SpectrumInfo(C.Structure):
     _fields_ = [("grid", Grid), ("log_scale", C.c_double), ("stage_ms", C.c_float * 6),
                 ("lines_in_window", C.c_int64), ("fft_rows", C.c_int32), ("merged_rows", C.c_int32),
-                ("merged_ext", C.c_int32)]
+                ("merged_ext", C.c_int32), ("gauss_ms", C.c_float)]
 
 
 class Request(C.Structure):
@@ -121,6 +121,7 @@ def load(path: str | None = None):
         "rg_synthesize_host": ([vp, C.POINTER(Conditions), vp, vp, C.c_int, C.POINTER(SpectrumInfo)],
                                C.c_int),
         "rg_plan_stage_times": ([vp, C.POINTER(C.c_double), C.POINTER(i64)], C.c_int),
+        "rg_plan_stage_times_gauss": ([vp, C.POINTER(C.c_double)], C.c_int),
         "rg_debug_ldm": ([vp, C.POINTER(Conditions), vp, i64, C.POINTER(SpectrumInfo)], C.c_int),
         "rg_server_create": ([vp, C.c_int, i64, C.POINTER(vp)], C.c_int),
         "rg_server_submit": ([vp, C.POINTER(Request), C.POINTER(i64)], C.c_int),
@@ -379,6 +380,13 @@ class Plan:
                                               C.c_void_p(out_dev_ptr),
                                               C.c_void_p(stream_ptr) if stream_ptr else None, C.byref(info)))
         return info
+
+    def gauss_time(self):
+        """Gaussian-stage part (ms, summed) of the fft-col sum that the last
+        ``stage_times`` call returned (merged layout; 0 otherwise)."""
+        g = C.c_double()
+        check(load().rg_plan_stage_times_gauss(self.handle, C.byref(g)))
+        return g.value
 
     def stage_times(self):
         """(sum of ms per stage [scatter, fft-col, fft-row+voigt, ifft-row,

@@ -150,10 +150,14 @@ struct rg_plan {
     float2* tw_lo_own = nullptr;
     float* out_d = nullptr;
     double* grad_d = nullptr;           // 3 sums of the adjoint gather, allocated on first use
-    cudaEvent_t ev[6] = {nullptr};
+    // stage events: start, after scatter, fft-col, fft-row, ifft-row, ifft-col,
+    // and [6] after the Gaussian stage inside fft-col (at [1] without it)
+    static constexpr int kEv = 7;
+    cudaEvent_t ev[kEv] = {nullptr};
     // ring of per-stage events recorded without synchronisation (timing == 2)
     static constexpr int kRing = 256;
-    std::vector<cudaEvent_t> ring;      // kRing * 6 events, created lazily
+    std::vector<cudaEvent_t> ring;      // kRing * kEv events, created lazily
+    double last_gauss_sum = 0.0;        // Gaussian-stage part of the last ring read
     int ring_used = 0;
     bool ring_ldm_only[kRing] = {false};
     cudaStream_t ring_stream = nullptr;
@@ -831,6 +835,7 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
             if (ga->NLv > ga->NL)   // zero pad row of odd n_L
                 CU(cudaMemsetAsync(W.mrow + (size_t)ga->NL * ga->out_stride, 0, sizeof(float) * ga->out_stride, st));
             RG(launch_gauss_merge(*ga, ga->NL, st));
+            if (ev) CU(cudaEventRecord(ev[6], st));
             ColFftArgs cm = ca;   // merged rows (float, extended): pairs [0, NLv / 2)
             cm.src = W.mrow;
             cm.row_stride = ga->out_stride;
@@ -848,6 +853,7 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
                 RG(launch_col_fft_fwd(cn, st));
             }
         } else {
+            if (ev) CU(cudaEventRecord(ev[6], st));
             RG(launch_col_fft_fwd(ca, st));
         }
         if (ev) CU(cudaEventRecord(ev[2], st));
@@ -1037,11 +1043,11 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
     cudaEvent_t* ev = nullptr;
     if (timing == 2) {
         if (P->ring.empty()) {
-            P->ring.assign(rg_plan::kRing * 6, nullptr);
+            P->ring.assign(rg_plan::kRing * rg_plan::kEv, nullptr);
             for (auto& e : P->ring) CU(cudaEventCreate(&e));
         }
         if (P->ring_used >= rg_plan::kRing) return fail(RG_ERR_RANGE, "stage-timing ring full: read it first");
-        ev = &P->ring[6 * P->ring_used];
+        ev = &P->ring[rg_plan::kEv * P->ring_used];
         P->ring_ldm_only[P->ring_used] = ldm_only;
         P->ring_used++;
         P->ring_stream = st;
@@ -1069,6 +1075,7 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
         int last = ldm_only ? 1 : 5;
         for (int i = 0; i < last; ++i) CU(cudaEventElapsedTime(&info->stage_ms[i], P->ev[i], P->ev[i + 1]));
         CU(cudaEventElapsedTime(&info->stage_ms[5], P->ev[0], P->ev[last]));
+        if (!ldm_only) CU(cudaEventElapsedTime(&info->gauss_ms, P->ev[1], P->ev[6]));
         unsigned long long cnt = 0;
         CU(cudaMemcpy(&cnt, P->w.counter, sizeof cnt, cudaMemcpyDeviceToHost));
         info->lines_in_window = (int64_t)cnt;
@@ -1504,11 +1511,12 @@ int rg_plan_stage_times(rg_plan* P, double* sum_ms, int64_t* count) {
     if (!valid(P) || !sum_ms || !count) return fail(RG_ERR_ARG, "invalid argument");
     std::lock_guard<std::mutex> lk(P->mu);
     for (int k = 0; k < 6; ++k) sum_ms[k] = 0.0;
+    P->last_gauss_sum = 0.0;
     *count = P->ring_used;
     if (!P->ring_used) return RG_OK;
     CU(cudaStreamSynchronize(P->ring_stream));
     for (int r = 0; r < P->ring_used; ++r) {
-        cudaEvent_t* ev = &P->ring[6 * r];
+        cudaEvent_t* ev = &P->ring[rg_plan::kEv * r];
         int last = P->ring_ldm_only[r] ? 1 : 5;
         float ms;
         for (int i = 0; i < last; ++i) {
@@ -1517,9 +1525,21 @@ int rg_plan_stage_times(rg_plan* P, double* sum_ms, int64_t* count) {
         }
         CU(cudaEventElapsedTime(&ms, ev[0], ev[last]));
         sum_ms[5] += ms;
+        if (!P->ring_ldm_only[r]) {
+            CU(cudaEventElapsedTime(&ms, ev[1], ev[6]));
+            P->last_gauss_sum += ms;
+        }
     }
     P->ring_used = 0;
     return take_err(P->w);
+}
+
+int rg_plan_stage_times_gauss(rg_plan* P, double* gauss_sum_ms) {
+    g_err.clear();
+    if (!valid(P) || !gauss_sum_ms) return fail(RG_ERR_ARG, "invalid argument");
+    std::lock_guard<std::mutex> lk(P->mu);
+    *gauss_sum_ms = P->last_gauss_sum;
+    return RG_OK;
 }
 
 int rg_synthesize_host(rg_plan* P, const rg_conditions* c, float* out_host, void* stream, int timing,

@@ -642,7 +642,10 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
         }
         asm volatile("bar.sync 1, %0;" ::"r"(nct) : "memory");
     }
-    if (a.in_window && counted) atomicAdd(a.in_window, (unsigned long long)counted);
+    if (a.in_window) {   // one atomic per warp: per-thread atomics on one word serialise in L2
+        const unsigned tot = __reduce_add_sync(0xffffffffu, counted);
+        if (lane == 0 && tot) atomicAdd(a.in_window, (unsigned long long)tot);
+    }
 }
 
 // ---------------------------------------------------------------------------
