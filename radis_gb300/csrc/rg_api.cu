@@ -511,9 +511,13 @@ int scatter_shape(int n_nodes, int* chunk, int* TK, int* stages, size_t* smem) {
         *smem = scatter_fixed_smem(ch, S) + (size_t)4 * n_nodes * (tk + 1);
         return RG_OK;
     };
-    if (tile_cols(3, 512) >= 256) return take(3, 512, tile_cols(3, 512));
+    // GB300 sweeps (CO2 5M / 128 nodes, H2O 100M / 288 nodes): one line per
+    // consumer thread per chunk (992 = 31 warps) in three stages while the tile
+    // keeps >= 256 columns; else two 1536-line stages (wider tiles than 2048)
+    if (tile_cols(3, 992) >= 256) return take(3, 992, tile_cols(3, 992));
+    if (tile_cols(2, 1536) >= 64) return take(2, 1536, tile_cols(2, 1536));
     for (int min_tk : {64, 32})
-        for (int ch : {2048, 1024, 512, 256})
+        for (int ch : {1024, 512, 256})
             if (tile_cols(2, ch) >= min_tk) return take(2, ch, tile_cols(2, ch));
     return fail(RG_ERR_RANGE, "LDM grid of %d nodes does not fit a shared-memory tile", n_nodes);
 }
