@@ -1998,6 +1998,18 @@ int rg_server_create(rg_ctx* ctx, int slots, int64_t mem_budget, rg_server** out
         *sl.w.err_host = 0;
         CU(cudaHostGetDevicePointer((void**)&sl.w.err_pub, sl.w.err_host, 0));
     }
+    // the FFT tables of every factorisation choose_fft can pick (n1 in {8, 64,
+    // 512}, n2 = 32 x 5-smooth <= kN2Max), built before the worker starts: a
+    // request never waits for a table upload (an allocation and a blocking
+    // copy) on the worker thread
+    for (int64_t m = 1; 32 * m <= kN2Max; m = next_smooth(m + 1))
+        for (int n1 : {8, 64, 512}) {
+            Work t;
+            t.n1 = n1;
+            t.n2 = (int)(32 * m);
+            t.n = (int64_t)t.n1 * t.n2;
+            RG(server_tables(S, t));
+        }
     ctx->lines++;   // the context stays alive while the server exists
     S->worker = std::thread(worker_loop, S);
     *out = guard.release();
