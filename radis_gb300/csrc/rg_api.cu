@@ -695,7 +695,7 @@ bool plan_merge(const Work& W, const SpecHost& s, const VoigtArgs& va, GaussArgs
     {
         const double kSigMin = 1.2, kTail = std::sqrt(2.0 * std::log(1e8));   // taps to 1e-8 of the peak
         auto sig = [&](int w) { return std::exp(g.log_wG_min + ga->wide_l[w] * g.dxG) / dv / (2.0 * std::sqrt(2.0 * kLn2)); };
-        auto padded = [](int K) { return (2 * K + 1 + 7) & ~7; };
+        auto padded = [](int K) { return (2 * K + 1 + 3) & ~3; };   // taps the kernel runs
         double smin = 1e300;
         for (int w = 0; w < ga->n_wide; ++w) smin = std::min(smin, sig(w));
         const double sb2 = smin * smin - kSigMin * kSigMin;

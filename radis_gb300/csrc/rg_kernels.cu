@@ -1224,10 +1224,22 @@ __device__ __forceinline__ void load8(float (&d)[8], const float* s) {
 
 constexpr int kGaussXs = kGaussTile + 2 * kGaussMaxK + 24;   // window buffer floats
 
-// acc[i] += sum_jj taps[jj] xs[t0 + i + jj], jj < KP (a multiple of 8; xs
+// acc[i] += sum_jj taps[jj] xs[t0 + i + jj], jj < KP (a multiple of 4; xs
 // readable up to t0 + KP + 7): three 8-value register blocks rotate through
 // the window (no moves): taps jj..jj+7 use A ++ B, jj+8.. use B ++ C, jj+16..
-// use C ++ A'; a tail of 8 or 16 taps ends the row of taps.
+// use C ++ A'; a tail of up to two 8-tap steps and one 4-tap step ends the
+// row of taps.
+// Four taps on the same window form (the tail of a row of taps whose count
+// is 4 mod 8): acc[i] += sum_{u < 4} g[u] window[i + u], window = lo ++ hi.
+__device__ __forceinline__ void gauss_step4(float (&acc)[8], const float (&lo)[8], const float4 hi, const float4 g4) {
+    const float hv[3] = {hi.x, hi.y, hi.z};
+    const float g[4] = {g4.x, g4.y, g4.z, g4.w};
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int i = 0; i < 8; ++i) acc[i] = fmaf(g[u], i + u < 8 ? lo[i + u] : hv[i + u - 8], acc[i]);
+}
+
 __device__ __forceinline__ void conv_window(float (&acc)[8], const float* xs, const float* taps, int t0, int KP) {
     float A[8], B[8], C[8], g[8];
     load8(A, &xs[t0]);
@@ -1243,15 +1255,26 @@ __device__ __forceinline__ void conv_window(float (&acc)[8], const float* xs, co
         load8(g, &taps[jj + 16]);
         gauss_step<8>(acc, C, A, g);
     }
-    if (jj < KP) {
+    // tail of 0-20 taps: up to two 8-tap steps, then one 4-tap step
+    const int r = KP - jj;
+    if (r >= 8) {
         load8(B, &xs[t0 + jj + 8]);
         load8(g, &taps[jj]);
         gauss_step<8>(acc, A, B, g);
-        if (jj + 8 < KP) {
+        if (r >= 16) {
             load8(C, &xs[t0 + jj + 16]);
             load8(g, &taps[jj + 8]);
             gauss_step<8>(acc, B, C, g);
+            if (r & 4)
+                gauss_step4(acc, C, *reinterpret_cast<const float4*>(&xs[t0 + jj + 24]),
+                            *reinterpret_cast<const float4*>(&taps[jj + 16]));
+        } else if (r & 4) {
+            gauss_step4(acc, B, *reinterpret_cast<const float4*>(&xs[t0 + jj + 16]),
+                        *reinterpret_cast<const float4*>(&taps[jj + 8]));
         }
+    } else if (r & 4) {
+        gauss_step4(acc, A, *reinterpret_cast<const float4*>(&xs[t0 + jj + 8]),
+                    *reinterpret_cast<const float4*>(&taps[jj]));
     }
 }
 
@@ -1259,7 +1282,7 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
     extern __shared__ __align__(16) float gsm[];
     constexpr int TW = kGaussTile;
     constexpr int P = kGaussPer;                     // outputs per thread (8)
-    float* taps = gsm;                               // KP <= 2 kGaussMaxK + 8 (K <= kGaussMaxK, shift <= 3)
+    float* taps = gsm;                               // KP <= 2 kGaussMaxK + 4 (K <= kGaussMaxK, shift <= 3)
     float* xs = gsm + (2 * kGaussMaxK + 16);         // 4 n4 <= TW + KP + 11 <= kGaussXs
     const int r = blockIdx.y;
     const int p0 = blockIdx.x * a.tile_out;          // first output (buffer position)
@@ -1278,7 +1301,7 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
     constexpr int NPRE = ((TW + 2 * kGaussMaxK + 24) / 4 + 255) / 256;
     float4 pre[NPRE];
     auto shift_of = [&](int w) { return (q0 - a.ext - a.K[w]) & 3; };
-    auto taps_of = [&](int w) { return (2 * a.K[w] + 1 + shift_of(w) + 7) & ~7; };   // multiple of 8
+    auto taps_of = [&](int w) { return (2 * a.K[w] + 1 + shift_of(w) + 3) & ~3; };   // multiple of 4
     auto fetch = [&](int w) {
         const int k0 = (q0 - a.ext - a.K[w]) & ~3;   // LDM index of xs[0]
         const int n4 = (TW + taps_of(w) + 8 + 3) / 4;
@@ -1323,7 +1346,7 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
     }
     int n_out = TW;
     if (a.Kb > 0) {   // second stage: the summed row convolved once with g_b
-        const int KPb = (2 * a.Kb + 1 + 7) & ~7;
+        const int KPb = (2 * a.Kb + 1 + 3) & ~3;
         __syncthreads();   // last node's tile and taps consumed
 #pragma unroll
         for (int i = 0; i < P; ++i) xs[t0 + i] = acc[i];
@@ -1364,7 +1387,7 @@ __global__ void __launch_bounds__(256) k_slit_conv(const SlitArgs a) {
     extern __shared__ __align__(16) float ssm[];
     constexpr int TW = kGaussTile;
     constexpr int P = kGaussPer;
-    float* taps = ssm;                       // kSlitPass (padded to 8)
+    float* taps = ssm;                       // kSlitPass (padded to 4)
     float* xs = ssm + kSlitPass + 16;        // TW + KP + 8 <= TW + kSlitPass + 16
     const int64_t p0 = (int64_t)blockIdx.x * TW;
     const int t0 = threadIdx.x * P;
@@ -1374,7 +1397,7 @@ __global__ void __launch_bounds__(256) k_slit_conv(const SlitArgs a) {
     for (int i = 0; i < P; ++i) acc[i] = 0.f;
     for (int u0 = 0; u0 < a.m; u0 += kSlitPass) {
         const int kb = min(kSlitPass, a.m - u0);
-        const int KP = (kb + 7) & ~7;
+        const int KP = (kb + 3) & ~3;
         const int64_t base = p0 - half + u0;   // input index of xs[0]
         __syncthreads();   // previous pass consumed
         for (int jj = threadIdx.x; jj < KP; jj += blockDim.x) taps[jj] = jj < kb ? a.slit[a.m - 1 - (u0 + jj)] : 0.f;
