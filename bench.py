@@ -590,7 +590,7 @@ def run_ours(args):
             "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": workload_desc(wl, n_lines, n_v, (g.n_G, g.n_L, g.n_ft),
-                                    (n_lines * 32, n_nodes * n_v * 4, n_nodes * g.n_ft * 4)),
+                                    (n_lines * 32, n_nodes * n_v * 4, int(info.fft_rows or n_nodes) * g.n_ft * 4)),
             "clocks": clk.summary(),
             "gpu_launches": kernels_per_step(info) * K,
             "e2e": {"value": ws * 1000.0 / e2e_ms, "unit": "spectra/s",
