@@ -61,7 +61,7 @@ def workload_desc(name, n_lines, n_v, grid, nbytes):
         "workload": (f"{label} synthetic list, {n_lines} lines, {vmin:g}-{vmax:g} cm-1 at {ws:g} cm-1 "
                      f"({n_v} points), {grid[0]}x{grid[1]} LDM nodes, T={T:g} K, p={p:g} bar, x={x:g}"),
         "n_lines": n_lines, "n_v": n_v, "n_ft": grid[2], "ldm_nodes": [grid[0], grid[1]],
-        "l2": ("inputs larger than L2 (line list %d MB, LDM %d MB, FFT workspace %d MB)"
+        "l2": ("inputs larger than L2 (line list %d MB, LDM %d MB, packed FFT rows %d MB)"
                % tuple(b // 1000000 for b in nbytes)),
         "parallelism": "replicas",
     }
