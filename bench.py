@@ -67,6 +67,18 @@ def workload_desc(name, n_lines, n_v, grid, nbytes):
     }
 
 
+def max_over_ranks(x, ws, device):
+    """The slowest rank's time (the job's time): all-reduce MAX over the
+    process group (NCCL on the GPUs; any backend works, the CPU tests use gloo)."""
+    if ws <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -536,11 +548,8 @@ def run_ours(args):
     stage_sum, stage_n = plan.stage_times()
     stage_avg = [s / max(stage_n, 1) for s in stage_sum]
     gauss_avg = plan.gauss_time() / max(stage_n, 1)
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = ws * 1000.0 / ms
+    ms = max_over_ranks(ms, ws, "cuda")
+    value = ws * 1000.0 / ms   # replicas: every rank synthesises one spectrum per step
 
     # e2e through the host API: conditions in, spectrum out to pinned memory
     host = torch.empty(n_v, dtype=torch.float32, pin_memory=True).numpy()
@@ -554,10 +563,7 @@ def run_ours(args):
     lat_ms = sorted(v * 1e3 for v in lat)
     p50 = lat_ms[len(lat_ms) // 2]
     p99 = lat_ms[min(len(lat_ms) - 1, int(math.ceil(0.99 * len(lat_ms))) - 1)]
-    if ws > 1:
-        t = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e2e_ms, ws, "cuda")
     # cold path: upload from host arrays + plan + one spectrum (eq_spectrum_gpu with exit_gpu)
     cold = []
     for _ in range(2 if n_lines <= 10_000_000 else 1):

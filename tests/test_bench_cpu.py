@@ -1,0 +1,84 @@
+"""bench.py's launch contract on the CPU.
+
+* The reference arm under torchrun with two ranks (127.0.0.1, gloo-free: the
+  arm needs no process group): rank 0 alone times the reference algorithm on
+  the host cores and prints one JSON line carrying impl, cpu_baseline and an
+  e2e object with zero copy bytes; the other rank exits 0 without work.
+* The kernel-launch claim (gpu_launches = kernels per spectrum x steps) for
+  the plain, merged and merged-with-narrow-rows FFT layouts.
+* The multi-rank timing reduction of the GPU arm (max over ranks) on two
+  gloo ranks.
+"""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def test_reference_arm_two_ranks():
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes", "1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), "bench.py",
+           "--impl", "reference", "--steps", "1", "--warmup", "0"]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-3000:]
+    out = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(out) == 1, r.stdout[-2000:]
+    d = json.loads(out[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+
+
+def test_kernels_per_step():
+    sys.path.insert(0, ROOT)
+    import bench
+
+    class Info:
+        def __init__(self, merged_rows, fft_rows):
+            self.merged_rows, self.fft_rows = merged_rows, fft_rows
+
+    assert bench.kernels_per_step(Info(0, 128)) == 5     # plain layout
+    assert bench.kernels_per_step(Info(16, 16)) == 6     # CO2 5M: all Gaussian nodes wide
+    assert bench.kernels_per_step(Info(24, 216)) == 7    # H2O 100M: merged + narrow-node rows
+    assert bench.kernels_per_step(Info(7, 8)) == 6       # odd n_L padded with a zero row
+    assert bench.kernels_per_step(Info(7, 16)) == 7
+
+
+def _max_worker(rank, port, q):
+    import torch.distributed as dist
+
+    sys.path.insert(0, ROOT)
+    import bench
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=2)
+    try:
+        q.put((rank, bench.max_over_ranks(1.5 + rank, 2, "cpu"), bench.max_over_ranks(7.0, 1, "cpu")))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_max_over_ranks_gloo_two_ranks():
+    """The multi-rank timing reduction of bench.py (the slowest rank's time)
+    on two gloo ranks: every rank gets the max; one rank is a no-op."""
+    import torch.multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_max_worker, args=(r, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=120)
+        assert p.exitcode == 0
+    assert got == [(0, 2.5, 7.0), (1, 2.5, 7.0)]
