@@ -1,6 +1,6 @@
 """CPU oracle for the equilibrium LDM/DIT synthesis -- TEST INFRASTRUCTURE ONLY.
 
-This module is the checker, never the product: only ``tests/``, the smoke
+This module checks the product and is never part of it: only ``tests/``, the smoke
 check in ``__graft_entry__`` and the ``cpu_baseline`` / ``--impl reference``
 legs of ``bench.py`` may import it.  The GPU product path never calls it and
 fails loudly when its CUDA library is missing.

@@ -184,7 +184,7 @@ def calc_spectrum(wavenum_min=None, wavenum_max=None, Tgas=None, pressure=1.0132
     """One-molecule front end (radis/lbl/calc.py:37; mode dispatch :1016-1028).
     ``databank``: path of a HITRAN-160 file or a column dict."""
     if mode != "gpu":
-        raise NotImplementedError("this build implements mode='gpu' only")
+        raise NotImplementedError("radis_gb300 implements mode='gpu' only")
     sf = SpectrumFactory(wavenum_min=wavenum_min, wavenum_max=wavenum_max, wstep=wstep,
                          molecule=molecule, isotope=isotope, pressure=pressure,
                          mole_fraction=mole_fraction, path_length=path_length, verbose=verbose,

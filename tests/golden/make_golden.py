@@ -1,7 +1,7 @@
 """Generate golden vectors by RUNNING the reference's own code (RADIS 0.17.1).
 
 Run in a container where the reference tree is mounted (default path below, or
-``--ref``); the GPU machine never runs this script, it only reads the committed
+``--ref``); the GPU tests never run this script, they only read the committed
 ``golden_ldm.npz``.  The full ``radis`` package cannot be imported here (pandas,
 astropy, numba, hapi are absent), so the few reference functions on the LDM
 path are pulled out of their source files with ``ast`` and executed unchanged

@@ -2,7 +2,7 @@
 tabulators (RADIS 0.17.1).
 
 Run where the reference tree is mounted (default path below, or ``--ref``);
-the GPU machine only reads the committed ``golden_partition.npz``.  The methods
+the tests only read the committed ``golden_partition.npz``.  The methods
 are pulled out of their source files with ``ast`` and executed unchanged; the
 CDSD tabulator reads its table with ``pandas.read_csv``, which is absent here,
 so a minimal stand-in parses the same whitespace table with numpy.

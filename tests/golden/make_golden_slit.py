@@ -1,7 +1,7 @@
 """Generate slit golden vectors by RUNNING the reference's own code (RADIS 0.17.1).
 
 Run in a container where the reference tree is mounted (default path below, or
-``--ref``); the GPU machine only reads the committed ``golden_slit.npz``.  The
+``--ref``); the tests only read the committed ``golden_slit.npz``.  The
 ``radis`` package cannot be imported here (pandas, astropy, numba, hapi are
 absent), so the slit functions are pulled out of their source file with
 ``ast`` and executed unchanged in a namespace that provides the module-level
