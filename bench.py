@@ -620,7 +620,8 @@ def run_ours(args):
         }
         if name == "k_gauss_merge":
             res["roofline"]["note"] = ("the real-space Gaussian stage is FP32-FMA-bound (a banded convolution of "
-                                       "each wide-node row, ~300 FMA per output point): frac is the HBM fraction "
+                                       "each wide-node row with its residual Gaussian, ~220 FMA per merged "
+                                       "output point on the 8 wide nodes of this grid): frac is the HBM fraction "
                                        "of the bytes it must move")
         if ws == 1 and not args.no_cpu_baseline:
             workers = os.cpu_count() or 1

@@ -688,44 +688,32 @@ bool plan_merge(const Work& W, const SpecHost& s, const VoigtArgs& va, GaussArgs
         }
     }
     if (ga->n_wide < 2) return false;
-    // two-stage form when it needs fewer taps: g_l = d_l conv g_b with
-    // sigma_b^2 = sigma_min^2 - 1.2^2 and every sigma_d, sigma_b >= 1.2 steps
-    // (sampled Gaussians of variances d, b compose up to aliases of at most
-    // exp(-2 pi^2 d b / (d + b)): ~1e-11 for CO2 5M, <= ~1e-8 for the narrowest
-    // wide node, variance 4.2)
-    ga->tile_out = kGaussTile;
+    // Base Gaussian in Fourier space: g_l = d_l conv g_b with sigma_b^2 =
+    // sigma_min^2 - 1.2^2, so every residual sigma_d >= 1.2 steps.  The merged
+    // rows carry sum_l d_l conv LDM_{l,m} (real space, this stage) and the row
+    // kernel multiplies their FT by the base's 2^(-alpha_b f^2) together with
+    // the Lorentzian FT.  A sampled residual times the base FT differs from the
+    // node's Gaussian FT by the residual's first alias, at most
+    // exp(-2 pi^2 d b / (d + b)) for variances d, b in steps^2: ~1e-11 for the
+    // CO2 5M grid, <= ~8e-9 for the narrowest wide node (variance 4.2).
+    double alpha_b = 0.0;
     {
         const double kSigMin = 1.2, kTail = std::sqrt(2.0 * std::log(1e8));   // taps to 1e-8 of the peak
         auto sig = [&](int w) { return std::exp(g.log_wG_min + ga->wide_l[w] * g.dxG) / dv / (2.0 * std::sqrt(2.0 * kLn2)); };
-        auto padded = [](int K) { return (2 * K + 1 + 3) & ~3; };   // taps the kernel runs
         double smin = 1e300;
         for (int w = 0; w < ga->n_wide; ++w) smin = std::min(smin, sig(w));
         const double sb2 = smin * smin - kSigMin * kSigMin;
-        if (sb2 >= kSigMin * kSigMin) {
-            const int Kb = (int)std::ceil(kTail * std::sqrt(sb2));
-            const int tile_out = (kGaussTile - 2 * Kb) & ~7;
-            long single = 0, two = 0;
-            int Kd[kMaxAxis], ext2 = 0;
+        if (sb2 > 0) {   // always: a wide node has sigma >= 2 steps
+            int ext2 = 0;
             for (int w = 0; w < ga->n_wide; ++w) {
-                single += padded(ga->K[w]);
-                Kd[w] = (int)std::ceil(kTail * std::sqrt(sig(w) * sig(w) - sb2));
-                two += padded(Kd[w]);
-                ext2 = std::max(ext2, Kd[w] + Kb);
+                const double sd2 = sig(w) * sig(w) - sb2;
+                ga->K[w] = (int)std::ceil(kTail * std::sqrt(sd2));
+                ga->c[w] = (float)(1.0 / std::sqrt(2.0 * kPi * sd2));
+                ga->a2[w] = (float)(kLog2e / (2.0 * sd2));
+                ext2 = std::max(ext2, ga->K[w]);
             }
-            const double two_cost = (double)(two + padded(Kb)) * kGaussTile / std::max(tile_out, 8);
-            if (Kb <= kGaussMaxK && tile_out >= kGaussTile / 2 && two_cost < 0.9 * single) {
-                for (int w = 0; w < ga->n_wide; ++w) {
-                    const double sd2 = sig(w) * sig(w) - sb2;
-                    ga->K[w] = Kd[w];
-                    ga->c[w] = (float)(1.0 / std::sqrt(2.0 * kPi * sd2));
-                    ga->a2[w] = (float)(kLog2e / (2.0 * sd2));
-                }
-                ga->Kb = Kb;
-                ga->cb = (float)(1.0 / std::sqrt(2.0 * kPi * sb2));
-                ga->a2b = (float)(kLog2e / (2.0 * sb2));
-                ga->tile_out = tile_out;
-                K_max = ext2;
-            }
+            K_max = ext2;
+            alpha_b = 2.0 * kPi * kPi * sb2 * dv * dv * kLog2e;   // (pi wG_b)^2 / (4 ln 2) log2 e
         }
     }
     // rows come in blocks of NLv = n_L rounded up to even (a zero row pads odd
@@ -746,7 +734,7 @@ bool plan_merge(const Work& W, const SpecHost& s, const VoigtArgs& va, GaussArgs
     vm->n_nodes = *out_rows;
     vm->n_pairs = *out_rows / 2;
     vm->NL = NLv;
-    vm->alpha[0] = 0.f;   // merged rows: the Gaussian factor is applied already
+    vm->alpha[0] = (float)alpha_b;   // merged rows: the base Gaussian's FT (residuals applied already)
     for (int i = 0; i < ga->n_narrow; ++i) vm->alpha[1 + i] = va.alpha[ga->narrow_l[i]];
     vm->alpha[1 + ga->n_narrow] = 0.f;
     for (int r = 0; r < *out_rows; ++r) {

@@ -214,13 +214,10 @@ struct GaussArgs {
     int wide_l[kMaxAxis], K[kMaxAxis];       // wide nodes and kernel half-widths
     float c[kMaxAxis], a2[kMaxAxis];         // taps c ex2(-a2 j^2), |j| <= K
     int narrow_l[kMaxAxis];
-    // two-stage form (Kb > 0): the wide kernels are g_l = d_l conv g_b (sampled
-    // Gaussians compose exactly above ~1 grid step: sigma_l^2 = sigma_d^2 +
-    // sigma_b^2); c/a2/K above then describe d_l, and the sum over l is
-    // convolved once with g_b = cb 2^(-a2b j^2), |j| <= Kb
-    int Kb;
-    float cb, a2b;
-    int tile_out;         // outputs per CTA (kGaussTile, or less the 2 Kb halo, multiple of 8)
+    // The wide Gaussians are split as g_l = d_l conv g_b (sigma_l^2 = sigma_d^2 +
+    // sigma_b^2, one base g_b shared by all wide l): c/a2/K above describe the
+    // residual d_l, and the base is applied to the merged rows in Fourier space
+    // by the row kernel (its alpha of the merged block)
 };
 
 // Tabulated partition function of one isotopologue (rg_partition.cpp)

@@ -1200,11 +1200,12 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_fft_fwd_f(const C
 
 // Gaussian stage of the merged layout (see GaussArgs).  One CTA: one merged
 // row (wL node), kGaussTile consecutive outputs, kGaussPer per thread.  A merged row is
-// sum over wide nodes l of (g_l conv LDM_{l,m}) with the symmetric kernel
-// g_l[j] = c_l 2^(-a2_l j^2), |j| <= K_l, i.e. out[p] = sum_jj g[jj] x[p - ext
-// - K + jj]; each thread keeps its outputs' input window in registers and
-// advances it 8 taps at a time (two half-windows used alternately, so the
-// window never moves between registers).
+// sum over wide nodes l of (d_l conv LDM_{l,m}) with the symmetric residual
+// kernel d_l[j] = c_l 2^(-a2_l j^2), |j| <= K_l, i.e. out[p] = sum_jj d[jj]
+// x[p - ext - K + jj]; each thread keeps its outputs' input window in registers
+// and advances it 8 taps at a time (two half-windows used alternately, so the
+// window never moves between registers).  The shared base Gaussian of the
+// wide nodes is applied after the FFT, by the row kernel.
 template <int P>
 __device__ __forceinline__ void gauss_step(float (&acc)[P], const float (&lo)[P], const float (&hi)[8],
                                            const float (&g)[8]) {
@@ -1285,8 +1286,8 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
     float* taps = gsm;                               // KP <= 2 kGaussMaxK + 4 (K <= kGaussMaxK, shift <= 3)
     float* xs = gsm + (2 * kGaussMaxK + 16);         // 4 n4 <= TW + KP + 11 <= kGaussXs
     const int r = blockIdx.y;
-    const int p0 = blockIdx.x * a.tile_out;          // first output (buffer position)
-    const int q0 = p0 - a.Kb;                        // first position of the per-thread accumulators
+    const int p0 = blockIdx.x * TW;                  // first output (buffer position)
+    const int q0 = p0;                               // first position of the per-thread accumulators
     const int Lr = a.n_v + 2 * a.ext;
     float* orow = a.out + (int64_t)r * a.out_stride;
     const int m = r;   // merged row of wL node m
@@ -1344,33 +1345,15 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
         __syncthreads();
         conv_window(acc, xs, taps, t0, KP);
     }
-    int n_out = TW;
-    if (a.Kb > 0) {   // second stage: the summed row convolved once with g_b
-        const int KPb = (2 * a.Kb + 1 + 3) & ~3;
-        __syncthreads();   // last node's tile and taps consumed
-#pragma unroll
-        for (int i = 0; i < P; ++i) xs[t0 + i] = acc[i];
-        for (int q = TW + threadIdx.x; q < TW + KPb + 8; q += blockDim.x) xs[q] = 0.f;
-        for (int jj = threadIdx.x; jj < KPb; jj += blockDim.x) {
-            const float j = (float)(jj - a.Kb);
-            taps[jj] = jj <= 2 * a.Kb ? a.cb * ex2(-a.a2b * j * j) : 0.f;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int i = 0; i < P; ++i) acc[i] = 0.f;
-        n_out = a.tile_out;
-        if (t0 < n_out) conv_window(acc, xs, taps, t0, KPb);
-    }
     const int p = p0 + t0;
-    if (t0 >= n_out) return;
 #pragma unroll
     for (int i = 0; i < P; i += 4) {
-        if (p + i + 4 <= Lr && t0 + i + 4 <= n_out) {
+        if (p + i + 4 <= Lr) {
             *reinterpret_cast<float4*>(&orow[p + i]) = make_float4(acc[i], acc[i + 1], acc[i + 2], acc[i + 3]);
         } else {
 #pragma unroll
             for (int u = 0; u < 4; ++u)
-                if (p + i + u < Lr && t0 + i + u < n_out) orow[p + i + u] = acc[i + u];
+                if (p + i + u < Lr) orow[p + i + u] = acc[i + u];
         }
     }
 }
@@ -1851,11 +1834,10 @@ int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st) {
 int launch_gauss_merge(const GaussArgs& a, int out_rows, cudaStream_t st) {
     const size_t smem = sizeof(float) * ((2 * kGaussMaxK + 16) + kGaussXs);
     const int Lr = a.n_v + 2 * a.ext;
-    if (a.tile_out <= 0 || a.tile_out > kGaussTile || a.tile_out % 8 || a.Kb > kGaussMaxK) return RG_ERR_RANGE;
     if (a.n_wide < 0 || a.n_wide > kMaxAxis || a.row_stride % 4) return RG_ERR_RANGE;
     for (int w = 0; w < a.n_wide; ++w)
         if (a.K[w] < 0 || a.K[w] > kGaussMaxK) return RG_ERR_RANGE;
-    dim3 grid((Lr + a.tile_out - 1) / a.tile_out, out_rows);
+    dim3 grid((Lr + kGaussTile - 1) / kGaussTile, out_rows);
     k_gauss_merge<<<grid, 256, smem, st>>>(a);
     return check_launch();
 }
