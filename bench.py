@@ -16,6 +16,8 @@ independent replicas, one per GPU (the path needs no exchange between GPUs).
 ``--impl reference`` times the CPU oracle (an FP64 numpy restatement of the
 reference's CPU LDM path; the reference itself needs pandas/astropy/numba and
 its GPU path needs Vulkan, neither of which exists here) on rank 0 only.
+
+``--ingest-only`` times the host-side HITRAN-160 ingestion instead (no GPU).
 """
 from __future__ import annotations
 
@@ -657,6 +659,68 @@ def run_ours(args):
     return 0
 
 
+def run_ingest(args):
+    """``--ingest-only`` (host only, no GPU): HITRAN-160 ingestion of a seeded
+    synthetic file of ``--ingest-records`` CO-like records.  Times the
+    library's parser (all host threads, and one), the numpy fixed-record
+    restatement of the reference's parse (parse_hitran_file:
+    numpy.fromfile + cast, radis/api/tools.py:25-78) as the CPU baseline,
+    and the columnar cache (first load: parse + write; later loads:
+    memory-mapped).  Checks the parser against the baseline bit for bit."""
+    import numpy as np
+    from oracle import hitran_oracle as HO
+    from radis_gb300 import hitran as H
+    n = args.ingest_records
+    rng = np.random.default_rng(31)
+    lines = {"v0": np.sort(rng.uniform(1900.0, 2400.0, n)), "S_ref": 10 ** rng.uniform(-30, -18, n),
+             "A": 10 ** rng.uniform(-3, 2, n), "g_air": rng.uniform(0.03, 0.09, n),
+             "g_self": rng.uniform(0.05, 0.11, n), "El": np.minimum(rng.exponential(3000.0, n), 40000.0),
+             "n_air": rng.uniform(0.5, 0.8, n), "delta": rng.uniform(-0.008, 0.004, n),
+             "iso": rng.integers(1, 10, n), "gp": rng.integers(1, 200, n).astype(float),
+             "gpp": rng.integers(1, 200, n).astype(float)}
+    with tempfile.TemporaryDirectory() as d:
+        p = os.path.join(d, "lines.par")
+        H.write_hitran160(p, lines)
+        size = os.path.getsize(p)
+        text = open(p, "rb").read()
+
+        def best(fn, reps=3):
+            t = []
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                r = fn()
+                t.append(time.perf_counter() - t0)
+            return min(t), r
+
+        cores = os.cpu_count() or 1
+        t_all, cols = best(lambda: H.read_hitran160(p, threads=0))
+        t_one, _ = best(lambda: H.read_hitran160(p, threads=1))
+        t_ref, ref = best(lambda: HO.read_fixed_records(text), reps=1)
+        exact = all(np.array_equal(cols[k].view(np.int64) if cols[k].dtype == np.float64 else cols[k],
+                                   ref[k].view(np.int64) if ref[k].dtype == np.float64 else ref[k]) for k in ref)
+        t_first, _ = best(lambda: H.load_hitran(p, cache="regen"), reps=1)
+
+        def cached():
+            c = H.load_hitran(p)
+            return float(np.asarray(c["v0"]).sum() + np.asarray(c["S_ref"]).sum())
+        t_cached, _ = best(cached)
+    rate = lambda t: n / t / 1e6
+    print(json.dumps({
+        "metric": "HITRAN-160 ingestion (records parsed to columns)", "value": rate(t_all), "unit": "M records/s",
+        "higher_is_better": True, "records": n, "bytes": size, "GB/s": size / t_all / 1e9, "threads": cores,
+        "ms": t_all * 1e3, "single_thread": {"value": rate(t_one), "ms": t_one * 1e3},
+        "bit_exact_vs_baseline": bool(exact),
+        "cpu_baseline": {"value": rate(t_ref), "unit": "M records/s", "cores": 1, "kind": "port",
+                         "ms": t_ref * 1e3,
+                         "sample": "numpy fixed-record parse of the same file (the reference's fromfile + cast)"},
+        "cache": {"first_load_ms": t_first * 1e3, "cached_load_ms": t_cached * 1e3,
+                  "note": "first load = parse + write of the columnar cache; cached = memory-mapped, "
+                          "v0 and S_ref read"},
+        "data": "synthetic", "config": {"workload": f"CO-like HITRAN-160 file, {n} records, "
+                                                    f"{size / 1e6:.0f} MB, isotopologues 1-9"}}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -671,7 +735,12 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=120)
     ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--serve-h2o-lines", type=int, default=100_000_000)
+    ap.add_argument("--ingest-only", action="store_true",
+                    help="host only: time HITRAN-160 ingestion (parser, baseline, cache) and exit")
+    ap.add_argument("--ingest-records", type=int, default=1_000_000)
     args = ap.parse_args()
+    if args.ingest_only:
+        return run_ingest(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

@@ -26,6 +26,9 @@
  *        clear -> FillLDM (cmdFillLDM.comp) -> R2C FFT -> ApplyLineshapes
  *        (cmdApplyLineshapes.comp) -> C2R IFFT -> D2H
  *   rg_grid_estimate                <- the same rules on host arrays, no device
+ *   rg_hitran_count / rg_hitran_parse <- the HITRAN-160 column parse of hit2df
+ *        (radis/api/hitranapi.py:82-105, 182-380; parse_hitran_file,
+ *        radis/api/tools.py:25-78), host only
  *   rg_debug_ldm                    <- no reference entry point: reads back the
  *        LDM tensor so the scatter can be checked on its own
  *   rg_backward / rg_jvp            <- no reference entry point: derivatives of
@@ -159,6 +162,32 @@ int rg_plan_grid(rg_plan* plan, const rg_conditions* cond, rg_grid* out);
  * request before any device memory is touched. */
 int rg_grid_estimate(const rg_line_arrays* lines, const rg_isotopes* iso, const rg_plan_desc* desc,
                      const rg_conditions* cond, rg_grid* out);
+
+/* Host-only, no device needed: HITRAN-2004 160-character records -> columns.
+ * `text`: the file's bytes (ASCII).  A record ends at "\n", "\r\n" or "\r";
+ * records shorter than 67 characters are skipped; blank numeric fields read as
+ * NaN; every value is the correctly rounded double of its decimal field.
+ * rg_hitran_count: the number of records.  rg_hitran_parse: fills the non-NULL
+ * columns of `out` (out->n must equal the count); RG_ERR_ARG names the line and
+ * field of the first field that does not convert.  threads <= 0: one per host
+ * core (at most one per MB of text). */
+typedef struct {
+    int64_t n;
+    int32_t* id;      /* molecule number                                   */
+    int32_t* iso;     /* isotopologue number: '1'-'9', '0' = 10, 'A' = 11 .. */
+    double* v0;       /* wav (cm-1)                                        */
+    double* s_ref;    /* int (cm-1/(molecule cm-2)) at 296 K               */
+    double* a;        /* A (s-1)                                           */
+    double* g_air;    /* airbrd (cm-1/atm)                                 */
+    double* g_self;   /* selbrd (cm-1/atm)                                 */
+    double* e_low;    /* El (cm-1)                                         */
+    double* n_air;    /* Tdpair                                            */
+    double* delta;    /* Pshft (cm-1/atm)                                  */
+    double* gp;       /* upper-state degeneracy                            */
+    double* gpp;      /* lower-state degeneracy                            */
+} rg_hitran_columns;
+int rg_hitran_count(const char* text, int64_t nbytes, int32_t threads, int64_t* n_records);
+int rg_hitran_parse(const char* text, int64_t nbytes, int32_t threads, const rg_hitran_columns* out);
 
 /* Enqueue one spectrum on `stream` (NULL = the context's stream).
  * `out_dev`: device array of n_v floats (abscoeff in cm-1 times

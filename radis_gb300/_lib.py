@@ -26,6 +26,7 @@ EXPORTS = [
     "rg_server_create", "rg_server_submit", "rg_server_wait", "rg_server_stats_get", "rg_server_destroy",
     "rg_synthesize_static", "rg_backward", "rg_jvp", "rg_synthesize_quantities", "rg_slit_convolve",
     "rg_lines_set_partition", "rg_partition_eval", "rg_plan_stage_times_gauss",
+    "rg_hitran_count", "rg_hitran_parse",
 ]
 
 
@@ -43,6 +44,11 @@ class LineArrays(C.Structure):
     _fields_ = [("n", C.c_int64), ("v0", C.c_void_p), ("s_ref", C.c_void_p),
                 ("e_low", C.c_void_p), ("g_air", C.c_void_p), ("g_self", C.c_void_p),
                 ("n_air", C.c_void_p), ("delta", C.c_void_p), ("iso", C.c_void_p)]
+
+
+class HitranColumns(C.Structure):
+    _fields_ = [("n", C.c_int64), ("id", C.c_void_p), ("iso", C.c_void_p)] + \
+        [(k, C.c_void_p) for k in ("v0", "s_ref", "a", "g_air", "g_self", "e_low", "n_air", "delta", "gp", "gpp")]
 
 
 class Isotopes(C.Structure):
@@ -140,6 +146,8 @@ def load(path: str | None = None):
         "rg_lines_set_partition": ([vp, C.c_int32, i64, vp, vp, C.c_int32], C.c_int),
         "rg_partition_eval": ([i64, vp, vp, C.c_int32, C.c_double, C.POINTER(C.c_double),
                                C.POINTER(C.c_double)], C.c_int),
+        "rg_hitran_count": ([vp, i64, C.c_int32, C.POINTER(i64)], C.c_int),
+        "rg_hitran_parse": ([vp, i64, C.c_int32, C.POINTER(HitranColumns)], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -170,6 +178,37 @@ def partition_eval(T, Q, kind: str, t: float):
     check(load().rg_partition_eval(len(T), ptr(T), ptr(Q), PARTITION_KINDS[kind], float(t), C.byref(q),
                                    C.byref(dq)))
     return q.value, dq.value
+
+
+# HitranColumns field -> column name of the line dicts used in this package
+HITRAN_COLUMNS = {"id": "id", "iso": "iso", "v0": "v0", "s_ref": "S_ref", "a": "A", "g_air": "g_air",
+                  "g_self": "g_self", "e_low": "El", "n_air": "n_air", "delta": "delta", "gp": "gp",
+                  "gpp": "gpp"}
+
+
+def hitran_parse(text, threads: int = 0, columns=None) -> dict:
+    """Host-only rg_hitran_count + rg_hitran_parse over the bytes of a
+    HITRAN-160 file (any 1-D uint8 buffer).  Returns {name: array}: id and iso
+    int64, the rest float64; ``columns`` restricts the columns converted."""
+    buf = np.frombuffer(text, dtype=np.uint8) if not isinstance(text, np.ndarray) else text
+    if buf.ndim != 1 or buf.dtype != np.uint8 or not buf.flags.c_contiguous:
+        raise ValueError("text must be a contiguous 1-D uint8 buffer")
+    lib = load()
+    addr = buf.ctypes.data_as(C.c_void_p) if buf.size else None
+    n = C.c_int64()
+    check(lib.rg_hitran_count(addr, buf.size, int(threads), C.byref(n)))
+    want = HITRAN_COLUMNS if columns is None else {k: v for k, v in HITRAN_COLUMNS.items() if v in columns}
+    out = {}
+    cols = HitranColumns(n=n.value)
+    for field, name in want.items():
+        a = np.empty(n.value, dtype=np.int32 if field in ("id", "iso") else np.float64)
+        out[name] = a
+        setattr(cols, field, a.ctypes.data_as(C.c_void_p).value if n.value else None)
+    check(lib.rg_hitran_parse(addr, buf.size, int(threads), C.byref(cols)))
+    for k in ("id", "iso"):
+        if k in out:
+            out[k] = out[k].astype(np.int64)
+    return out
 
 
 class Context:

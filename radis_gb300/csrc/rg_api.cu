@@ -1478,6 +1478,21 @@ int rg_partition_eval(int64_t n, const double* T, const double* Q, int32_t inter
     return RG_OK;
 }
 
+int rg_hitran_count(const char* text, int64_t nbytes, int32_t threads, int64_t* n_records) {
+    g_err.clear();
+    if (!n_records || nbytes < 0 || (!text && nbytes > 0)) return fail(RG_ERR_ARG, "invalid argument");
+    return hitran_count(text, nbytes, threads, n_records);
+}
+
+int rg_hitran_parse(const char* text, int64_t nbytes, int32_t threads, const rg_hitran_columns* out) {
+    g_err.clear();
+    if (!out || nbytes < 0 || (!text && nbytes > 0) || out->n < 0) return fail(RG_ERR_ARG, "invalid argument");
+    std::string e;
+    const int rc = hitran_parse(text, nbytes, threads, out, &e);
+    if (rc) return fail(rc, "%s", e.c_str());
+    return RG_OK;
+}
+
 int rg_slit_convolve(rg_ctx* ctx, const float* in_dev, int64_t n, const float* slit_dev, int32_t n_slit,
                      double wstep, int32_t mode, float* out_dev, void* stream) {
     g_err.clear();

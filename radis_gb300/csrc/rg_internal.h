@@ -228,6 +228,10 @@ struct QTable {
 int qtable_build(int64_t n, const double* T, const double* Q, int interp, QTable* out, std::string* err);
 int qtable_eval(const QTable& t, double T, double* q, double* dq_dT, std::string* err);
 
+// HITRAN-160 records -> columns (rg_hitran.cpp)
+int hitran_count(const char* text, int64_t nbytes, int threads, int64_t* n_records);
+int hitran_parse(const char* text, int64_t nbytes, int threads, const rg_hitran_columns* out, std::string* err);
+
 // Instrument slit convolution ('same' part of the full convolution, x scale)
 constexpr int kSlitPass = 512;        // slit taps staged per pass
 struct SlitArgs {

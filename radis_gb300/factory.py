@@ -73,12 +73,15 @@ class SpectrumFactory:
         self.wavenumber = self.wavenumber_calc[m:m + n_out]
 
     # --- line databases -----------------------------------------------------------
-    def load_databank(self, path=None, format="hitran", **kwargs):
-        """Load a HITRAN-160 file (radis/lbl/loader.py:1715 load_databank)."""
+    def load_databank(self, path=None, format="hitran", db_use_cached=True, **kwargs):
+        """Load a HITRAN-160 file (radis/lbl/loader.py:1715 load_databank):
+        parsed by the library's parser and cached as columns beside the file
+        (``db_use_cached``: True, False, 'regen' or 'force', as hit2df's
+        ``cache``, radis/api/hitranapi.py:182-380)."""
         if format not in ("hitran", "hitran160", "par"):
             raise NotImplementedError(f"format {format!r}: only HITRAN-160 files are read here")
-        from .hitran import read_hitran160
-        d = read_hitran160(path)
+        from .hitran import load_hitran
+        d = load_hitran(path, cache=db_use_cached if db_use_cached is not None else True)
         return self.load_lines(d)
 
     def load_lines(self, lines: dict):

@@ -8,6 +8,7 @@
   the plain, merged and merged-with-narrow-rows FFT layouts.
 * The multi-rank timing reduction of the GPU arm (max over ranks) on two
   gloo ranks.
+* The host-only ingestion mode (--ingest-only) on a small file.
 """
 import json
 import os
@@ -82,3 +83,13 @@ def test_max_over_ranks_gloo_two_ranks():
         p.join(timeout=120)
         assert p.exitcode == 0
     assert got == [(0, 2.5, 7.0), (1, 2.5, 7.0)]
+
+
+def test_ingest_mode():
+    """bench.py --ingest-only: the host-side HITRAN-160 ingestion line (no GPU)."""
+    r = subprocess.run([sys.executable, "bench.py", "--ingest-only", "--ingest-records", "20000"], cwd=ROOT,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    d = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1])
+    assert d["records"] == 20000 and d["bytes"] == 20000 * 161 and d["bit_exact_vs_baseline"] is True
+    assert d["value"] > 0 and d["cpu_baseline"]["kind"] == "port" and d["cache"]["cached_load_ms"] > 0
