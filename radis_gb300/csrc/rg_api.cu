@@ -418,14 +418,45 @@ int build_envelope(const rg_line_arrays* in, const rg_isotopes* iso, Envelope* E
         E->lv_max[i] = -std::numeric_limits<double>::infinity();
     }
     E->max_abs_delta = 0.0;
-    for (int64_t i = 0; i < n; ++i) {
-        int k = in->iso ? in->iso[i] : 0;
-        if (k >= E->n_iso) return fail(RG_ERR_ARG, "iso[%lld] = %d >= n_iso", (long long)i, k);
-        if (!(in->v0[i] > 0)) return fail(RG_ERR_ARG, "v0[%lld] must be positive", (long long)i);
-        double lv = std::log(in->v0[i]);
-        E->lv_min[k] = std::min(E->lv_min[k], lv);
-        E->lv_max[k] = std::max(E->lv_max[k], lv);
-        if (in->delta) E->max_abs_delta = std::max(E->max_abs_delta, (double)std::fabs(in->delta[i]));
+    {   // per-isotope log v0 range and the largest |shift|, over host threads;
+        // the first bad line (lowest index) is reported
+        struct Part {
+            double lmin[kMaxIso], lmax[kMaxIso], dmax = 0.0;
+            int64_t bad = -1;
+        };
+        const int T = host_chunk_count(n, kHostMinPerThread);
+        std::vector<Part> part(T);
+        run_host_chunks(T, n, [&](int t, int64_t i0, int64_t i1) {
+            Part& p = part[t];
+            for (int k = 0; k < kMaxIso; ++k) {
+                p.lmin[k] = std::numeric_limits<double>::infinity();
+                p.lmax[k] = -std::numeric_limits<double>::infinity();
+            }
+            for (int64_t i = i0; i < i1; ++i) {
+                const int k = in->iso ? in->iso[i] : 0;
+                if (k >= E->n_iso || !(in->v0[i] > 0)) {
+                    p.bad = i;
+                    return;
+                }
+                const double lv = std::log(in->v0[i]);
+                p.lmin[k] = std::min(p.lmin[k], lv);
+                p.lmax[k] = std::max(p.lmax[k], lv);
+                if (in->delta) p.dmax = std::max(p.dmax, (double)std::fabs(in->delta[i]));
+            }
+        });
+        for (const Part& p : part) {
+            if (p.bad >= 0) {
+                const int64_t i = p.bad;
+                const int k = in->iso ? in->iso[i] : 0;
+                if (k >= E->n_iso) return fail(RG_ERR_ARG, "iso[%lld] = %d >= n_iso", (long long)i, k);
+                return fail(RG_ERR_ARG, "v0[%lld] must be positive", (long long)i);
+            }
+            for (int k = 0; k < E->n_iso; ++k) {
+                E->lv_min[k] = std::min(E->lv_min[k], p.lmin[k]);
+                E->lv_max[k] = std::max(E->lv_max[k], p.lmax[k]);
+            }
+            E->max_abs_delta = std::max(E->max_abs_delta, p.dmax);
+        }
     }
     struct WidthSrc : PointSource {
         const rg_line_arrays* in;

@@ -1,5 +1,5 @@
-// Exact convex envelopes of large point sets, O(n) passes plus a sort of the
-// few survivors.
+// Exact convex envelopes of large point sets, O(n) passes (split over host
+// threads) plus a sort of the few survivors.
 //
 // The reference bounds the Lorentzian node axis by the lower/upper envelope of
 // the lines' (n_air, log gamma) pairs as a function of log(296/T)
@@ -72,62 +72,87 @@ struct NegSource : PointSource {
 Hull lower_impl(const PointSource& src) {
     const int64_t n = src.size();
     Hull out;
-    double amin = std::numeric_limits<double>::infinity(), amax = -amin;
-    for (int64_t i = 0; i < n; ++i) {
-        double a, b;
-        src.get(i, &a, &b);
-        if (!std::isfinite(a) || !std::isfinite(b)) continue;
-        amin = std::min(amin, a);
-        amax = std::max(amax, a);
-    }
+    constexpr double kInf = std::numeric_limits<double>::infinity();
+    // Three passes over the points, each split over host threads; the merges
+    // (min / max, the per-bucket minimum under the total order (b, a), the
+    // survivors concatenated in chunk order) give the sequential result.
+    const int T = host_chunk_count(n, kHostMinPerThread);
+    std::vector<double> lo(T, kInf), hi(T, -kInf);
+    run_host_chunks(T, n, [&](int t, int64_t i0, int64_t i1) {
+        double amin = kInf, amax = -kInf;
+        for (int64_t i = i0; i < i1; ++i) {
+            double a, b;
+            src.get(i, &a, &b);
+            if (!std::isfinite(a) || !std::isfinite(b)) continue;
+            amin = std::min(amin, a);
+            amax = std::max(amax, a);
+        }
+        lo[t] = amin;
+        hi[t] = amax;
+    });
+    const double amin = *std::min_element(lo.begin(), lo.end());
+    const double amax = *std::max_element(hi.begin(), hi.end());
     if (!(amin <= amax)) return out;   // no finite point
     const int K = 4096;
-    std::vector<Pt> bucket(K, Pt{0, std::numeric_limits<double>::infinity()});
     const double span = amax - amin;
     const double scale = span > 0 ? K / span : 0.0;
     auto bucket_of = [&](double a) {
         int k = (int)((a - amin) * scale);
         return k < 0 ? 0 : (k >= K ? K - 1 : k);
     };
-    for (int64_t i = 0; i < n; ++i) {
-        double a, b;
-        src.get(i, &a, &b);
-        if (!std::isfinite(a) || !std::isfinite(b)) continue;
-        Pt& q = bucket[bucket_of(a)];
-        if (b < q.b || (b == q.b && a < q.a)) q = Pt{a, b};
-    }
+    auto lower = [](const Pt& p, const Pt& q) { return p.b < q.b || (p.b == q.b && p.a < q.a); };
+    std::vector<std::vector<Pt>> part(T, std::vector<Pt>(K, Pt{0, kInf}));
+    run_host_chunks(T, n, [&](int t, int64_t i0, int64_t i1) {
+        std::vector<Pt>& bk = part[t];
+        for (int64_t i = i0; i < i1; ++i) {
+            double a, b;
+            src.get(i, &a, &b);
+            if (!std::isfinite(a) || !std::isfinite(b)) continue;
+            Pt& q = bk[bucket_of(a)];
+            if (lower(Pt{a, b}, q)) q = Pt{a, b};
+        }
+    });
     std::vector<Pt> mins;
-    for (const Pt& q : bucket)
+    for (int k = 0; k < K; ++k) {
+        Pt q{0, kInf};
+        for (int t = 0; t < T; ++t)
+            if (lower(part[t][k], q)) q = part[t][k];
         if (std::isfinite(q.b)) mins.push_back(q);
+    }
     std::vector<Pt> chain = monotone_lower(mins);
     // survivors: on/below the chain or outside its a-range
-    std::vector<Pt> keep;
     const double a_lo = chain.front().a, a_hi = chain.back().a;
-    for (int64_t i = 0; i < n; ++i) {
-        double a, b;
-        src.get(i, &a, &b);
-        if (!std::isfinite(a) || !std::isfinite(b)) continue;
-        if (a < a_lo || a > a_hi) {
-            keep.push_back(Pt{a, b});
-            continue;
+    std::vector<std::vector<Pt>> kept(T);
+    run_host_chunks(T, n, [&](int t, int64_t i0, int64_t i1) {
+        std::vector<Pt>& keep = kept[t];
+        for (int64_t i = i0; i < i1; ++i) {
+            double a, b;
+            src.get(i, &a, &b);
+            if (!std::isfinite(a) || !std::isfinite(b)) continue;
+            if (a < a_lo || a > a_hi) {
+                keep.push_back(Pt{a, b});
+                continue;
+            }
+            // segment of the chain containing a
+            size_t up = std::upper_bound(chain.begin(), chain.end(), a,
+                                         [](double v, const Pt& p) { return v < p.a; }) -
+                        chain.begin();
+            double cb;
+            if (up == 0) {
+                cb = chain[0].b;
+            } else if (up >= chain.size()) {
+                cb = chain.back().b;
+            } else {
+                const Pt& p = chain[up - 1];
+                const Pt& q = chain[up];
+                cb = p.b + (q.b - p.b) * (a - p.a) / (q.a - p.a);
+            }
+            // keep with a relative margin so that rounding never drops a vertex
+            if (b <= cb + 1e-12 * (1.0 + std::fabs(cb))) keep.push_back(Pt{a, b});
         }
-        // segment of the chain containing a
-        size_t hi = std::upper_bound(chain.begin(), chain.end(), a,
-                                     [](double v, const Pt& p) { return v < p.a; }) -
-                    chain.begin();
-        double cb;
-        if (hi == 0) {
-            cb = chain[0].b;
-        } else if (hi >= chain.size()) {
-            cb = chain.back().b;
-        } else {
-            const Pt& p = chain[hi - 1];
-            const Pt& q = chain[hi];
-            cb = p.b + (q.b - p.b) * (a - p.a) / (q.a - p.a);
-        }
-        // keep with a relative margin so that rounding never drops a vertex
-        if (b <= cb + 1e-12 * (1.0 + std::fabs(cb))) keep.push_back(Pt{a, b});
-    }
+    });
+    std::vector<Pt> keep;
+    for (const auto& v : kept) keep.insert(keep.end(), v.begin(), v.end());
     keep.insert(keep.end(), chain.begin(), chain.end());
     std::vector<Pt> h = monotone_lower(keep);
     for (const Pt& p : h) {

@@ -2,9 +2,11 @@
 // kernels (rg_kernels.cu).  Not part of the public ABI.
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/radis_gb300.h"
@@ -36,6 +38,25 @@ constexpr int kMaxAxis = 64;        // max nodes along one LDM axis
 constexpr int kMaxNodes = 1024;     // max N_G * N_L (padded to even)
 constexpr int kPairGroup = 16;      // node pairs per Voigt-reduce work item
 constexpr int kMaxPasses = 16;
+
+// --- host work over line arrays ------------------------------------------------
+// [0, n) in T contiguous chunks, chunk t = [n t / T, n (t + 1) / T): one per
+// host thread, each of at least min_per items (T = 1 for small n).  Per-chunk
+// partial results merged in chunk order reproduce the sequential pass.
+inline int host_chunk_count(int64_t n, int64_t min_per) {
+    const int64_t hc = std::max(1u, std::thread::hardware_concurrency());
+    return (int)std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(hc, 64), n / std::max<int64_t>(min_per, 1)));
+}
+// Runs f(t, begin, end) for the T chunks of [0, n), chunk 0 on the calling thread.
+template <typename F>
+void run_host_chunks(int T, int64_t n, F&& f) {
+    std::vector<std::thread> th;
+    th.reserve(T > 1 ? T - 1 : 0);
+    for (int t = 1; t < T; ++t) th.emplace_back([&f, t, T, n] { f(t, n * t / T, n * (t + 1) / T); });
+    f(0, (int64_t)0, T > 1 ? n / T : n);
+    for (auto& x : th) x.join();
+}
+constexpr int64_t kHostMinPerThread = 1 << 18;
 
 // --- host-side convex envelopes (rg_hull.cpp) ---------------------------------
 // Lower convex hull of points (a_i, b_i): min_i (b_i + a_i t) for every t is

@@ -124,3 +124,24 @@ def test_missing_library_fails_loudly(tmp_path):
             L.load(str(tmp_path / "nope.so"))
         finally:
             L._lib = saved
+
+
+def test_grid_independent_of_line_order(native_lib):
+    """The host envelopes split their passes over threads (>= 2^18 lines per
+    chunk); the merges reproduce the sequential result, so the grid does not
+    depend on how the lines fall into chunks: a shuffled list of 600k lines
+    (several chunks) gives the same grid bit for bit, and so do the error
+    reports of a bad line in a late chunk."""
+    lines = S.co2_like(600_000, seed=3)
+    perm = np.random.default_rng(4).permutation(600_000)
+    shuf = {k: (v[perm] if isinstance(v, np.ndarray) else v) for k, v in lines.items()}
+    for kw in (dict(n_G=8, n_L=16), dict(dxG=0.1, dxL=0.2)):
+        for T, p, x in ((296.0, 1.0, 0.1), (2500.0, 0.2, 0.7)):
+            a = L.grid_estimate(lines, 44.0, 2000.0, 0.001, 400001, T, p, x, **kw)
+            b = L.grid_estimate(shuf, 44.0, 2000.0, 0.001, 400001, T, p, x, **kw)
+            assert bytes(a) == bytes(b)
+    bad = dict(lines)
+    bad["v0"] = lines["v0"].copy()
+    bad["v0"][[555_555, 555_556]] = -1.0
+    with pytest.raises(L.RgError, match=r"v0\[555555\]"):
+        L.grid_estimate(bad, 44.0, 2000.0, 0.001, 400001, 296.0, 1.0, 0.1, n_G=8, n_L=16)
