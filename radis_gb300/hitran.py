@@ -23,6 +23,7 @@ from __future__ import annotations
 import json
 import mmap
 import os
+import threading
 import warnings
 
 import numpy as np
@@ -49,36 +50,18 @@ class IrrelevantFileWarning(UserWarning):
     the reference's load_h5_cache_file, so that callers skip the file."""
 
 
-def _file_bytes(path):
-    """(uint8 array over the file's bytes, closer)."""
-    size = os.path.getsize(path)
-    if size == 0:
-        return np.zeros(0, dtype=np.uint8), (lambda: None)
-    f = open(path, "rb")
-    try:
-        m = mmap.mmap(f.fileno(), 0, access=mmap.ACCESS_READ)
-    finally:
-        f.close()
-    buf = np.frombuffer(m, dtype=np.uint8)
-
-    def close():
-        nonlocal buf
-        del buf
-        try:
-            m.close()
-        except BufferError:   # an exported view is still alive: the map closes with it
-            pass
-    return buf, close
-
-
 def read_hitran160(path, threads: int = 0) -> dict:
     """Parse a .par file into numpy columns (float64; id/iso int64) with the
-    library's parser; threads <= 0: one per host core."""
-    buf, close = _file_bytes(path)
-    try:
-        return _lib.hitran_parse(buf, threads=threads)
-    finally:
-        close()
+    library's parser over a read-only memory map of the file; threads <= 0:
+    one per host core."""
+    if os.path.getsize(path) == 0:
+        return _lib.hitran_parse(np.zeros(0, dtype=np.uint8), threads=threads)
+    with open(path, "rb") as f, mmap.mmap(f.fileno(), 0, access=mmap.ACCESS_READ) as m:
+        buf = np.frombuffer(m, dtype=np.uint8)
+        try:
+            return _lib.hitran_parse(buf, threads=threads)
+        finally:
+            del buf   # the map closes only once no view of it is left
 
 
 def cache_file(path, cache_directory_path=None):
@@ -107,7 +90,7 @@ def write_cache(fcache, cols: dict, meta: dict):
                   wavenum_max=float(np.max(v0)) if v0 is not None and n else None)
     hb = json.dumps(header).encode()
     data0 = (16 + len(hb) + 63) // 64 * 64
-    tmp = fcache + f".tmp{os.getpid()}"
+    tmp = fcache + f".tmp{os.getpid()}.{threading.get_ident()}"
     with open(tmp, "wb") as f:
         f.write(CACHE_MAGIC + len(hb).to_bytes(8, "little") + hb)
         for t, a in zip(table, cols.values()):
