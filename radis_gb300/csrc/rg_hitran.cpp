@@ -7,7 +7,8 @@
 // and casts each field (radis/api/tools.py:25-78, 111-151); here the text is
 // split into records at line terminators and the numeric fields are converted
 // in parallel, each with a correctly rounded decimal-to-double conversion
-// (std::from_chars), so every value equals Python's float() of the field.
+// (Clinger's exact fast path for short decimals, std::from_chars for the
+// rest), so every value equals Python's float() of the field.
 //
 // Record rules: a record ends at "\n", "\r\n" or a lone "\r" (or the end of
 // the text); records shorter than 67 characters (the end of the Pshft field)
@@ -55,6 +56,67 @@ inline void field(const char* rec, int64_t len, const Fld& f, const char** b, co
     *e = q;
 }
 
+// Exact powers of ten (10^22 is the largest that a double holds exactly).
+constexpr double kPow10[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
+                               1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+
+// Clinger's fast path (W. D. Clinger, "How to read floating point numbers
+// accurately", PLDI 1990): a decimal m 10^q with at most 15 significant digits
+// (m < 2^53) and |q| <= 22 is m * 10^q or m / 10^-q of two exact doubles, one
+// correctly rounded operation.  Returns false (the caller converts with
+// from_chars) for anything else: more digits, larger exponents, inf/nan,
+// malformed text.
+inline bool fast_decimal(const char* b, const char* e, double* out) {
+    const char* p = b;
+    bool neg = false;
+    if (p < e && (*p == '+' || *p == '-')) {
+        neg = *p == '-';
+        ++p;
+    }
+    uint64_t m = 0;
+    int digits = 0, frac = 0;
+    bool any = false, dot = false;
+    for (; p < e; ++p) {
+        const char c = *p;
+        if (c >= '0' && c <= '9') {
+            any = true;
+            if (dot) ++frac;
+            if (m == 0 && c == '0') continue;   // leading zeros are not significant
+            if (++digits > 15) return false;
+            m = m * 10 + (uint64_t)(c - '0');
+        } else if (c == '.' && !dot) {
+            dot = true;
+        } else {
+            break;
+        }
+    }
+    if (!any) return false;
+    int x = 0;
+    if (p < e) {
+        if (*p != 'e' && *p != 'E') return false;
+        ++p;
+        bool xneg = false;
+        if (p < e && (*p == '+' || *p == '-')) {
+            xneg = *p == '-';
+            ++p;
+        }
+        if (p == e) return false;
+        for (; p < e; ++p) {
+            if (*p < '0' || *p > '9' || x > 1000) return false;
+            x = x * 10 + (*p - '0');
+        }
+        if (xneg) x = -x;
+    }
+    const int q = x - frac;
+    double v;
+    if (m == 0) v = 0.0;
+    else if (q >= 0 && q <= 22) v = (double)m * kPow10[q];
+    else if (q < 0 && q >= -22) v = (double)m / kPow10[-q];
+    else return false;
+    *out = neg ? -v : v;
+    return true;
+}
+
 // float() of a stripped field: optional sign, decimal or exponent form,
 // inf/nan; the whole field must convert (no digit-group underscores, as in
 // numpy's cast of the byte fields).
@@ -63,6 +125,7 @@ inline bool to_double(const char* b, const char* e, double* out) {
         *out = std::numeric_limits<double>::quiet_NaN();
         return true;
     }
+    if (fast_decimal(b, e, out)) return true;
     bool neg = false;
     if (*b == '+' || *b == '-') {
         neg = *b == '-';
@@ -116,14 +179,21 @@ inline bool to_iso(const char* b, const char* e, int32_t* out) {
     return true;
 }
 
+// End of the line starting at p (the first '\n' or '\r' in [p, e), or e).
+inline int64_t line_end(const char* t, int64_t p, int64_t e) {
+    const void* nl = std::memchr(t + p, '\n', (size_t)(e - p));
+    const int64_t q = nl ? (const char*)nl - t : e;
+    const void* cr = std::memchr(t + p, '\r', (size_t)(q - p));
+    return cr ? (const char*)cr - t : q;
+}
+
 // Start of the first record at or after byte s (s = 0 or just past a terminator).
 int64_t record_start(const char* t, int64_t n, int64_t s) {
     if (s <= 0) return 0;
     if (s >= n) return n;
     if (t[s - 1] == '\n') return s;
     if (t[s - 1] == '\r' && t[s] != '\n') return s;
-    int64_t p = s;
-    while (p < n && t[p] != '\n' && t[p] != '\r') ++p;
+    const int64_t p = line_end(t, s, n);
     if (p >= n) return n;
     if (t[p] == '\r' && p + 1 < n && t[p + 1] == '\n') return p + 2;
     return p + 1;
@@ -134,8 +204,7 @@ template <typename F>
 void for_lines(const char* t, int64_t b, int64_t e, F&& f) {
     int64_t p = b;
     while (p < e) {
-        int64_t q = p;
-        while (q < e && t[q] != '\n' && t[q] != '\r') ++q;
+        int64_t q = line_end(t, p, e);
         if (!f(t + p, q - p)) return;
         if (q < e && t[q] == '\r' && q + 1 < e && t[q + 1] == '\n') q += 2;
         else q += 1;

@@ -248,3 +248,42 @@ def test_factory_load_databank_uses_cache(native_lib, tmp_path):
     sf2 = SpectrumFactory(wavenum_min=2050, wavenum_max=2250, wstep=0.01, molecule="CO")
     sf2.load_databank(p, db_use_cached=False)
     assert len(sf2.df0["v0"]) == int(((ref["v0"] >= lo) & (ref["v0"] <= hi)).sum())
+
+
+def _decimal_strings(n, seed):
+    """Decimal fields of at most 12 characters on both sides of the exact fast
+    path's limits (15 significant digits, |power of ten| <= 22)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        kind = rng.integers(0, 6)
+        if kind == 0:     # fixed point, 1-11 digits
+            d = int(rng.integers(1, 12))
+            f = int(rng.integers(0, d + 1))
+            s = "".join(str(x) for x in rng.integers(0, 10, d))
+            s = s[:d - f] + "." + s[d - f:] if f else s
+        elif kind == 1:   # leading / trailing zeros
+            s = "0" * int(rng.integers(0, 4)) + "." + "0" * int(rng.integers(0, 5)) + str(rng.integers(1, 10 ** 5))
+        elif kind == 2:   # mantissa + exponent near the fast path's limits
+            s = f"{rng.integers(1, 10**6)}E{rng.integers(-30, 31):+d}"
+        elif kind == 3:   # HITRAN intensity style
+            s = f"{rng.uniform(1, 10):.3f}E{rng.integers(-40, 5):+03d}"
+        elif kind == 4:   # 14-17 significant digits (around the 15-digit limit)
+            s = str(rng.integers(10 ** 13, 10 ** 16))[: int(rng.integers(10, 12))]
+            s = s[:3] + "." + s[3:]
+        else:             # exponent without a sign, lower case
+            s = f"{rng.integers(1, 999)}.{rng.integers(0, 99)}e{rng.integers(0, 25)}"
+        if rng.integers(0, 3) == 0:
+            s = ("-" if rng.integers(0, 2) else "+") + s
+        out.append(s[:12])
+    return out
+
+
+def test_decimal_conversion_matches_float(native_lib):
+    """Every field value equals Python's float() of its text, bit for bit, on
+    both sides of the exact fast path's limits."""
+    vals = _decimal_strings(20000, 9)
+    text = "".join(_rec(v0=v) + "\n" for v in vals).encode()
+    got = L.hitran_parse(np.frombuffer(text, dtype=np.uint8), columns=("v0",))["v0"]
+    want = np.array([float(v) for v in vals])
+    assert _same(got, want)
