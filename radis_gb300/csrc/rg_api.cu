@@ -26,6 +26,8 @@
 #include <map>
 #include <thread>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "rg_internal.h"
 
 using namespace rg;
@@ -34,6 +36,16 @@ using namespace rg;
 // error reporting
 // ---------------------------------------------------------------------------
 static thread_local std::string g_err;
+
+// NVTX range over a host stage (upload, envelopes, plan, spectrum, served
+// request, HITRAN parse): a profiler attached through NVTX (ncu --nvtx) sees
+// the stage names; without one a push/pop is a no-op call.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 static int fail(int code, const char* fmt, ...) {
     char buf[512];
@@ -400,6 +412,7 @@ int compute_grid(const rg_lines* L, const Work& W, const rg_conditions* c, SpecH
 
 // Envelope of a host line list (per-iso v0 range, width and intensity hulls).
 int build_envelope(const rg_line_arrays* in, const rg_isotopes* iso, Envelope* E) {
+    NvtxRange nvtx_("rg/envelopes");
     if (!in || !iso) return fail(RG_ERR_ARG, "NULL argument");
     if (in->n <= 0) return fail(RG_ERR_ARG, "empty line list");
     if (!in->v0 || !in->s_ref || !in->e_low || !in->g_air || !in->g_self || !in->n_air)
@@ -1063,6 +1076,7 @@ int plan_stream_end(rg_plan* P, cudaStream_t st) {
 
 int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st, int timing, bool ldm_only,
                  rg_spectrum_info* info) {
+    NvtxRange nvtx_("rg/spectrum");
     SpecHost s;
     RG(compute_grid(P->lines, P->w, c, &s));
     cudaEvent_t* ev = nullptr;
@@ -1205,6 +1219,7 @@ int rg_ctx_destroy(rg_ctx* c) {
 }
 
 int rg_lines_upload(rg_ctx* ctx, const rg_line_arrays* in, const rg_isotopes* iso, rg_lines** out) {
+    NvtxRange nvtx_("rg/lines_upload");
     g_err.clear();
     if (!valid(ctx)) return fail(RG_ERR_STATE, "invalid context");
     if (!in || !iso || !out) return fail(RG_ERR_ARG, "NULL argument");
@@ -1323,6 +1338,7 @@ int rg_lines_count(const rg_lines* L, int64_t* n) {
 }
 
 int rg_plan_create(rg_lines* L, const rg_plan_desc* d, rg_plan** out) {
+    NvtxRange nvtx_("rg/plan_create");
     g_err.clear();
     if (!valid(L)) return fail(RG_ERR_STATE, "invalid line list");
     if (!d || !out) return fail(RG_ERR_ARG, "NULL argument");
@@ -1516,6 +1532,7 @@ int rg_hitran_count(const char* text, int64_t nbytes, int32_t threads, int64_t* 
 }
 
 int rg_hitran_parse(const char* text, int64_t nbytes, int32_t threads, const rg_hitran_columns* out) {
+    NvtxRange nvtx_("rg/hitran_parse");
     g_err.clear();
     if (!out || nbytes < 0 || (!text && nbytes > 0) || out->n < 0) return fail(RG_ERR_ARG, "invalid argument");
     std::string e;
@@ -1617,6 +1634,7 @@ int rg_debug_ldm(rg_plan* P, const rg_conditions* c, float* ldm_host, int64_t ca
 
 int rg_backward(rg_plan* P, const rg_conditions* c, const double* dlnq_dT, const float* grad_out_dev,
                 double grad[3], void* stream, rg_spectrum_info* info) {
+    NvtxRange nvtx_("rg/backward");
     g_err.clear();
     if (!valid(P) || !c || !grad_out_dev || !grad) return fail(RG_ERR_ARG, "invalid argument");
     std::lock_guard<std::mutex> lk(P->mu);
@@ -1644,6 +1662,7 @@ int rg_backward(rg_plan* P, const rg_conditions* c, const double* dlnq_dT, const
 
 int rg_jvp(rg_plan* P, const rg_conditions* c, const double* dlnq_dT, float* out_dev, void* stream,
            rg_spectrum_info* info) {
+    NvtxRange nvtx_("rg/jvp");
     g_err.clear();
     if (!valid(P) || !c || !out_dev) return fail(RG_ERR_ARG, "invalid argument");
     std::lock_guard<std::mutex> lk(P->mu);
@@ -1838,6 +1857,7 @@ void release_slot_buffers(Slot& sl) {
 
 // Launch request r on slot `si` (called by the worker with the lock held).
 int start_on_slot(rg_server* S, int si, const std::shared_ptr<ServerReq>& r, const SpecHost& sh, int n1, int n2) {
+    NvtxRange nvtx_("rg/serve_request");
     Slot& sl = S->slots[si];
     Work& W = sl.w;
     const rg_plan_desc& d = r->desc;
