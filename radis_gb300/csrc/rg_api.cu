@@ -480,6 +480,11 @@ int build_envelope(const rg_line_arrays* in, const rg_isotopes* iso, Envelope* E
             float g = lo ? std::min(in->g_self[i], in->g_air[i]) : std::max(in->g_self[i], in->g_air[i]);
             *b = g > 0 ? std::log((double)g) : -std::numeric_limits<double>::infinity();
         }
+        bool valid_a(int64_t i, double* a) const override {   // log g finite <=> 0 < g < inf
+            *a = in->n_air[i];
+            const float g = lo ? std::min(in->g_self[i], in->g_air[i]) : std::max(in->g_self[i], in->g_air[i]);
+            return std::isfinite(*a) && g > 0 && std::isfinite(g);
+        }
     };
     WidthSrc wlo, whi;
     wlo.in = whi.in = in;
@@ -498,6 +503,13 @@ int build_envelope(const rg_line_arrays* in, const rg_isotopes* iso, Envelope* E
             double s = in->s_ref[i];
             *b = s > 0 ? std::log(s) - std::log(-std::expm1(-c2_tref * in->v0[i]))
                        : -std::numeric_limits<double>::infinity();
+        }
+        // b finite <=> 0 < s < inf and -expm1(-x) > 0, x = c2 v0 / Tref (v0 > 0
+        // is checked before the hulls; expm1(-x) is nonzero for every x > 0)
+        bool valid_a(int64_t i, double* a) const override {
+            *a = in->e_low[i];
+            const double s = in->s_ref[i];
+            return std::isfinite(*a) && s > 0 && std::isfinite(s) && c2_tref * in->v0[i] > 0;
         }
     };
     SSrc ss;

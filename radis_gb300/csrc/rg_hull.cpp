@@ -67,6 +67,7 @@ struct NegSource : PointSource {
         s.get(i, pa, pb);
         *pb = -*pb;
     }
+    bool valid_a(int64_t i, double* pa) const override { return s.valid_a(i, pa); }
 };
 
 Hull lower_impl(const PointSource& src) {
@@ -81,9 +82,8 @@ Hull lower_impl(const PointSource& src) {
     run_host_chunks(T, n, [&](int t, int64_t i0, int64_t i1) {
         double amin = kInf, amax = -kInf;
         for (int64_t i = i0; i < i1; ++i) {
-            double a, b;
-            src.get(i, &a, &b);
-            if (!std::isfinite(a) || !std::isfinite(b)) continue;
+            double a;
+            if (!src.valid_a(i, &a)) continue;
             amin = std::min(amin, a);
             amax = std::max(amax, a);
         }

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <mutex>
 #include <string>
@@ -75,6 +76,14 @@ struct PointSource {
     virtual ~PointSource() {}
     virtual int64_t size() const = 0;
     virtual void get(int64_t i, double* a, double* b) const = 0;
+    // a of point i, and whether both coordinates are finite (the points the
+    // hull uses); an override must agree with get() exactly and may skip
+    // computing b
+    virtual bool valid_a(int64_t i, double* a) const {
+        double b;
+        get(i, a, &b);
+        return std::isfinite(*a) && std::isfinite(b);
+    }
 };
 Hull lower_hull_src(const PointSource& s);
 Hull upper_hull_src(const PointSource& s);
