@@ -10,6 +10,7 @@ pandas stand-in for the DataFrame that ``_ndarray2df`` builds.
 
 Reference code executed (paths relative to the radis project root):
   radis/api/hitranapi.py   columns_2004 (the HITRAN-2004 column table)
+  radis/api/cdsdapi.py     columns_cdsdhitemp (the CDSD-HITEMP column table)
   radis/api/tools.py       _get_linereturnformat, _ndarray2df, _read_hitran_file,
                            _create_dtype, _format_dtype, _cast_to_dtype
 (parse_hitran_file, tools.py:25-78, chains these; its only other work is the
@@ -21,6 +22,10 @@ Fixtures (seeded; written by radis_gb300.hitran.write_hitran160):
                       negative and positive pressure shifts
   hitran_co2_crlf.par 200 CO2-like records, "\\r\\n" line ends, isotopologues
                       1-9 and the HITEMP labels '0', 'A', 'B' (10, 11, 12)
+  hitemp_co2_cdsd.par 150 CO2-like records in the 127-character CDSD-HITEMP
+                      layout (radis/api/cdsdapi.py:47-85): the HITRAN-160
+                      fields up to Pshft, then Tdpsel and the CDSD quantum
+                      numbers; parsed by the reference with columns_cdsdhitemp
 """
 from __future__ import annotations
 
@@ -62,7 +67,23 @@ def write_fixtures():
         b = f.read()
     with open(p2, "wb") as f:
         f.write(b.replace(b"\n", b"\r\n"))
-    return {"CO": p1, "CO2": p2}
+    p3 = os.path.join(HERE, "hitemp_co2_cdsd.par")
+    tmp = p3 + ".tmp"
+    lines3 = _lines(rng, 150, "CO2")
+    write_hitran160(tmp, lines3, mol_id=2)
+    with open(tmp) as f:
+        recs = [r.rstrip("\n")[:67] for r in f]
+    os.remove(tmp)
+    nself = rng.uniform(0.5, 0.8, len(recs))
+    with open(p3, "w") as f:
+        for i, r in enumerate(recs):
+            j = int(rng.integers(0, 60))
+            tail = (f"{nself[i]:5.2f}" + "  1" + " 2" + " 2" + " 1" + "1" + "       0" + " 0" + " 0" + " 0" + "1"
+                    + "  3" + " 1" + f"{i % 9999:4d}" + "  0" + " 1" + "   1" + "  R" + f"{j:3d}" + "e" + "  750")
+            rec = r + tail
+            assert len(rec) == 127, len(rec)
+            f.write(rec + "\n")
+    return {"CO": p1, "CO2": p2, "CO2-CDSD": p3}
 
 
 class _Str:
@@ -109,6 +130,14 @@ class _DataFrame:
     def __contains__(self, k):
         return k in self.c
 
+    def __getattr__(self, k):   # df.branch (tools.py:148)
+        if k == "c":
+            raise AttributeError(k)
+        try:
+            return _Series(self.c[k])
+        except KeyError:
+            raise AttributeError(k) from None
+
 
 def _reference(ref):
     api = os.path.join(ref, "radis", "api")
@@ -117,6 +146,11 @@ def _reference(ref):
     for node in ast.parse(src).body:
         if isinstance(node, ast.Assign) and any(getattr(t, "id", None) == "columns_2004" for t in node.targets):
             exec(compile(ast.Module([node], []), "hitranapi.py", "exec"), ns)
+    src = open(os.path.join(api, "cdsdapi.py")).read()
+    for node in ast.parse(src).body:
+        if isinstance(node, ast.Assign) and any(getattr(t, "id", None) == "columns_cdsdhitemp"
+                                                for t in node.targets):
+            exec(compile(ast.Module([node], []), "cdsdapi.py", "exec"), ns)
     src = open(os.path.join(api, "tools.py")).read()
     names = {"_get_linereturnformat", "_ndarray2df", "_read_hitran_file", "_create_dtype", "_format_dtype",
              "_cast_to_dtype"}
@@ -132,15 +166,15 @@ def _reference(ref):
     return ns
 
 
-def parse_with_reference(ns, path, molecule):
+def parse_with_reference(ns, path, molecule, table="columns_2004"):
     """parse_hitran_file (tools.py:25-78) minus its vaex branch."""
-    cols = ns["columns_2004"]
+    cols = ns[table]
     data = ns["_read_hitran_file"](path, cols, count=1, linereturnformat="a2")
     lr = ns["_get_linereturnformat"](data, cols, path)
     data = ns["_read_hitran_file"](path, cols, -1, lr)
     df = ns["_ndarray2df"](data, cols, lr, molecule=molecule)
     return {COLS[k]: np.asarray(df.c[k].astype(np.int64 if k in ("id", "iso") else np.float64))
-            for k in COLS}
+            for k in COLS if k in df}
 
 
 def main():
@@ -152,7 +186,8 @@ def main():
     out = {}
     for mol, path in files.items():
         tag = os.path.basename(path)[:-4]
-        for k, v in parse_with_reference(ns, path, mol).items():
+        table = "columns_cdsdhitemp" if mol == "CO2-CDSD" else "columns_2004"
+        for k, v in parse_with_reference(ns, path, mol.split("-")[0], table).items():
             out[f"{tag}__{k}"] = v
     np.savez_compressed(os.path.join(HERE, "golden_hitran.npz"), **out)
     print("wrote", sorted(out)[:4], "...", len(out), "arrays")
