@@ -242,6 +242,11 @@ def main():
                        28.0, 0.2),
         "synth_1atm": (synthetic_co(300, 12), 296.0, 1.01325, 0.05, 2000.0, 2010.0, 0.005,
                        28.0, 1.0),
+        # high pressure: Lorentzian-dominated profiles, shifts of ~0.02 cm-1
+        "hitran_co_10bar": (hit, 1000.0, 10.0, 0.5, 2050.0, 2150.0, 0.01, 28.0, 0.2),
+        # pure self-broadening (x = 1: no air term) on a fine step, hot
+        "synth_self_hot": (synthetic_co(500, 14), 2500.0, 1.01325, 1.0, 2000.0, 2010.0, 0.002,
+                           28.0, 0.05),
     }
     out = {}
     for name, (lines, T, p, x, wmin, wmax, wstep, M, Qr) in cases.items():

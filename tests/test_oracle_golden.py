@@ -5,7 +5,7 @@ import pytest
 
 from oracle import ldm_oracle as O
 
-CASES = ["hitran_co_700K", "hitran_co_3000K", "synth_fold", "synth_1atm"]
+CASES = ["hitran_co_700K", "hitran_co_3000K", "synth_fold", "synth_1atm", "hitran_co_10bar", "synth_self_hot"]
 COLS = ["v0", "S_ref", "El", "g_air", "g_self", "n_air", "delta"]
 
 
