@@ -40,7 +40,7 @@ class SpectrumFactory:
                  pressure=1.01325, mole_fraction=1.0, path_length=1.0, Tref=296.0,
                  neighbour_lines=0.0, broadening_method="fft", folding_thresh=1e-6, dxG=None,
                  dxL=None, n_G=None, n_L=None, verbose=0, warnings=None, molar_mass=None,
-                 partition_functions=None, **kwargs):
+                 partition_functions=None, medium="air", **kwargs):
         if wavenum_min is None or wavenum_max is None or not wavenum_max > wavenum_min:
             raise ValueError("give wavenum_min < wavenum_max (cm-1)")
         if broadening_method != "fft":
@@ -49,7 +49,9 @@ class SpectrumFactory:
             wavenum_min=float(wavenum_min), wavenum_max=float(wavenum_max), molecule=molecule,
             isotope=isotope, pressure=float(pressure), mole_fraction=float(mole_fraction),
             path_length=float(path_length), Tref=float(Tref), Tgas=None, self_absorption=True,
-            isatom=False)
+            isatom=False, medium=medium)
+        if medium not in ("air", "vacuum"):
+            raise NotImplementedError(f"unknown propagating medium {medium!r}")
         self.params = types.SimpleNamespace(
             wstep=float(wstep), dxG=float(dxG or DXG_DEFAULT), dxL=float(dxL or DXL_DEFAULT),
             n_G=n_G, n_L=n_L, broadening_method=broadening_method,
@@ -169,7 +171,7 @@ class SpectrumFactory:
             thermal_equilibrium=True, diluents=diluent if diluent is not None else {"air": 1 - self.input.mole_fraction},
             radis_version=f"radis_gb300 {__version__}", gpu_backend=app.backend,
             spectral_points=len(self.wavenumber), add_at_used="gpu-backend", NwL=n_L, NwG=n_G,
-            gpu_times=times, default_output_unit="cm-1")
+            gpu_times=times, default_output_unit="cm-1", medium=self.input.medium)
         s = Spectrum(quantities=dict(wavenumber=self.wavenumber, abscoeff=abscoeff, absorbance=a,
                                      emissivity_noslit=e, transmittance_noslit=t,
                                      radiance_noslit=r),

@@ -14,6 +14,8 @@ import warnings
 
 import numpy as np
 
+from . import units as U
+
 # radis/phys/constants.py:22,33,38
 _H = 6.62607015e-34
 _C = 2.99792458e8
@@ -70,14 +72,49 @@ class Spectrum:
     def get_vars(self):
         return [k for k in self._q if k != "wavenumber"]
 
-    def get(self, var, wunit="cm-1", Iunit="default", copy=True):
+    def get(self, var, wunit="default", Iunit="default", copy=True):
+        """(wave axis, values) of ``var`` (radis/spectrum/spectrum.py:1183-1420).
+
+        ``wunit``: 'cm-1'; 'nm' (wavelength in the spectrum's medium,
+        ``conditions['medium']``, air by default); 'nm_air'; 'nm_vac';
+        'default' (``conditions['default_output_unit']``, else cm-1).
+        ``Iunit``: 'default' is the stored unit, with radiance switched to
+        per nm or per cm-1 to match ``wunit``; radiance converts between
+        W/mW/uW, cm2/m2 and per nm/um/cm-1 units, abscoeff between cm-1 and
+        m-1; unitless quantities take '' or '1'."""
         if var not in self._q:
             self._update(var)
-        w = self._q["wavenumber"]
+        if wunit == "default":
+            wunit = self.conditions.get("default_output_unit", "cm-1")
+        force_air = wunit == "nm_air"
+        wu = U.cast_waveunit(wunit)
+        nu = self._q["wavenumber"]
+        if wu == "cm-1":
+            w = nu
+        else:
+            w = 1e7 / np.asarray(nu, dtype=np.float64)    # vacuum wavelength
+            medium = "air" if force_air else self.conditions.get("medium", "air")
+            if wu == "nm" and medium == "air":
+                w = U.vacuum2air(w)
+            elif wu == "nm" and medium != "vacuum":
+                raise NotImplementedError(f"unknown propagating medium {medium!r}")
         v = self._q[var]
-        if wunit in ("nm", "nm_vac"):
-            w = 1e7 / w
-        return (w.copy(), v.copy()) if copy else (w, v)
+        unit0 = self.units.get(var, "")
+        radiance = var in ("radiance", "radiance_noslit")
+        if Iunit == "default":
+            Iunit = unit0
+            if radiance:
+                Iunit = unit0.replace("/cm-1", "/nm") if wu != "cm-1" else unit0.replace("/nm", "/cm-1")
+        if Iunit != unit0:
+            if radiance:
+                v = U.convert_radiance(v, unit0, Iunit, nu)
+            elif unit0 in ("", "1") and Iunit in ("", "1"):
+                pass
+            elif unit0 in ("", "1") or Iunit in ("", "1"):
+                raise ValueError(f"{var} is dimensionless: Iunit must be '' or '1', not {Iunit!r}")
+            else:
+                v = U.convert_per_length(v, unit0, Iunit)
+        return (np.array(w, copy=True), np.array(v, copy=True)) if copy else (w, v)
 
     def _update(self, var):
         if "abscoeff" not in self._q:
@@ -99,7 +136,7 @@ class Spectrum:
             self._q[k] = self._q[k][sel]
         return self
 
-    def recalc_gpu(self, var="transmittance", wunit=None, Iunit=None, pressure=None, Tgas=None,
+    def recalc_gpu(self, var="abscoeff", wunit="default", Iunit="default", pressure=None, Tgas=None,
                    mole_fraction=None, path_length=None, slit_function=None, verbose=False):
         """Re-run the resident GPU application at new conditions and return
         ``var`` (spectrum.py:6438-6572).  Only abscoeff comes from the GPU; the
@@ -135,10 +172,10 @@ class Spectrum:
             c["slit_function"] = slit_function
             self.apply_slit(slit_function, shape=c.get("slit_shape", "triangular"))
             if var in self._q:
-                return self.get(var)[1]
+                return self.get(var, wunit=wunit, Iunit=Iunit)[1]
         key = {"transmittance": "transmittance_noslit", "radiance": "radiance_noslit",
                "emissivity": "emissivity_noslit"}.get(var, var)
-        return self.get(key)[1]
+        return self.get(key, wunit=wunit, Iunit=Iunit)[1]
 
     def apply_slit(self, slit_function, unit="cm-1", shape="triangular", center_wavespace=None, norm_by="area",
                    mode="valid", store=True, slit_dispersion=None, assert_evenly_spaced=True, verbose=False,

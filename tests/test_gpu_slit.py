@@ -75,9 +75,11 @@ def test_spectrum_apply_slit(native_lib):
         # the slit is generated with the spectrum's smallest step, as apply_slit does (spectrum.py:3370)
         ws, Is = SO.triangular_slit(0.5, np.abs(np.diff(w)).min(), center=w[len(w) // 2])
         for q in ("transmittance", "radiance", "emissivity"):
-            ref_in = s.get(q + "_noslit")[1].astype(np.float32).astype(np.float64)
+            # in the stored units: get() on the cm-1 axis would give radiance per cm-1
+            # (x 1e7 / nu^2), which does not commute with the convolution
+            ref_in = s.get(q + "_noslit", Iunit=s.units[q + "_noslit"])[1].astype(np.float32).astype(np.float64)
             _, ref = SO.convolve_with_slit(w, ref_in, ws, Is, mode="valid")
-            _check(s.get(q)[1].astype(np.float64), ref)
+            _check(s.get(q, Iunit=s.units[q])[1].astype(np.float64), ref)
         assert s.conditions["slit_function"] == 0.5
         plan.close()
         ln.close()
