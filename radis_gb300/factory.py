@@ -18,6 +18,7 @@ import numpy as np
 from . import __version__
 from .gpu import gpuApp
 from .spectrum import DEFAULT_UNITS, Spectrum, derived_quantities
+from .units import get_wavenumber_range
 
 # default LDM steps (radis/lbl/loader.py:452-460, 538-543)
 DXL_DEFAULT = float(np.log((0.01 / 0.20) ** 0.5 + 1))
@@ -36,22 +37,30 @@ MOLAR_MASS = {
 class SpectrumFactory:
     """Subset of radis.lbl.factory.SpectrumFactory for eq_spectrum_gpu."""
 
-    def __init__(self, wavenum_min=None, wavenum_max=None, wstep=0.01, molecule=None, isotope="all",
-                 pressure=1.01325, mole_fraction=1.0, path_length=1.0, Tref=296.0,
-                 neighbour_lines=0.0, broadening_method="fft", folding_thresh=1e-6, dxG=None,
-                 dxL=None, n_G=None, n_L=None, verbose=0, warnings=None, molar_mass=None,
-                 partition_functions=None, medium="air", **kwargs):
-        if wavenum_min is None or wavenum_max is None or not wavenum_max > wavenum_min:
-            raise ValueError("give wavenum_min < wavenum_max (cm-1)")
-        if broadening_method != "fft":
-            raise NotImplementedError("the GPU path implements the FFT LDM method only")
+    def __init__(self, wmin=None, wmax=None, wunit=None, wavenum_min=None, wavenum_max=None,
+                 wavelength_min=None, wavelength_max=None, Tref=296.0, pressure=1.01325, mole_fraction=1.0,
+                 path_length=1.0, wstep=0.01, isotope="all", medium="air", neighbour_lines=0.0,
+                 folding_thresh=1e-6, broadening_method="voigt_poly", verbose=0, warnings=None,
+                 species=None, molecule=None, dxG=None, dxL=None, n_G=None, n_L=None, molar_mass=None,
+                 partition_functions=None, **kwargs):
+        """Arguments in the reference's order (radis/lbl/factory.py:419-470).
+        The range is one of wmin/wmax (``wunit``, cm-1 by default),
+        wavenum_min/wavenum_max (cm-1) or wavelength_min/wavelength_max (nm in
+        ``medium``); it also sets the spectra's default output unit.
+        ``broadening_method`` is recorded only: eq_spectrum_gpu always runs
+        the LDM with the FFT, as the reference's does.  ``molecule`` is an
+        alias of ``species``."""
+        if species is not None and molecule is not None and species != molecule:
+            raise ValueError("species and molecule (an alias) differ")
+        molecule = species if species is not None else molecule
+        wavenum_min, wavenum_max, input_wunit = get_wavenumber_range(
+            wmin, wmax, wunit, wavenum_min, wavenum_max, wavelength_min, wavelength_max, medium)
+        self.input_wunit = input_wunit
         self.input = types.SimpleNamespace(
             wavenum_min=float(wavenum_min), wavenum_max=float(wavenum_max), molecule=molecule,
             isotope=isotope, pressure=float(pressure), mole_fraction=float(mole_fraction),
             path_length=float(path_length), Tref=float(Tref), Tgas=None, self_absorption=True,
             isatom=False, medium=medium)
-        if medium not in ("air", "vacuum"):
-            raise NotImplementedError(f"unknown propagating medium {medium!r}")
         self.params = types.SimpleNamespace(
             wstep=float(wstep), dxG=float(dxG or DXG_DEFAULT), dxL=float(dxL or DXL_DEFAULT),
             n_G=n_G, n_L=n_L, broadening_method=broadening_method,
@@ -165,13 +174,13 @@ class SpectrumFactory:
             path_length=self.input.path_length, wavenum_min=self.input.wavenum_min,
             wavenum_max=self.input.wavenum_max, wstep=self.params.wstep,
             molecule=self.input.molecule, isotope=self.input.isotope, Tref=self.input.Tref,
-            dxG=self.params.dxG, dxL=self.params.dxL, broadening_method="fft",
+            dxG=self.params.dxG, dxL=self.params.dxL, broadening_method=self.params.broadening_method,
             folding_thresh=self.params.folding_thresh,
             calculation_time=time.perf_counter() - t0, lines_calculated=int(len(iso)),
             thermal_equilibrium=True, diluents=diluent if diluent is not None else {"air": 1 - self.input.mole_fraction},
             radis_version=f"radis_gb300 {__version__}", gpu_backend=app.backend,
             spectral_points=len(self.wavenumber), add_at_used="gpu-backend", NwL=n_L, NwG=n_G,
-            gpu_times=times, default_output_unit="cm-1", medium=self.input.medium)
+            gpu_times=times, default_output_unit=self.input_wunit, medium=self.input.medium)
         s = Spectrum(quantities=dict(wavenumber=self.wavenumber, abscoeff=abscoeff, absorbance=a,
                                      emissivity_noslit=e, transmittance_noslit=t,
                                      radiance_noslit=r),
@@ -183,19 +192,27 @@ class SpectrumFactory:
         return s
 
 
-def calc_spectrum(wavenum_min=None, wavenum_max=None, Tgas=None, pressure=1.01325,
-                  mole_fraction=1.0, path_length=1.0, molecule=None, isotope="all",
-                  databank=None, wstep=0.01, mode="gpu", name=None, verbose=0, **kwargs):
-    """One-molecule front end (radis/lbl/calc.py:37; mode dispatch :1016-1028).
-    ``databank``: path of a HITRAN-160 file or a column dict."""
+def calc_spectrum(wmin=None, wmax=None, wunit=None, Tgas=None, Tvib=None, Trot=None, Telec=None,
+                  pressure=1.01325, species=None, isotope="all", mole_fraction=1.0, diluent=None,
+                  path_length=1.0, databank=None, medium="air", wstep=0.01, name=None, mode="gpu",
+                  verbose=0, return_factory=False, **kwargs):
+    """One-molecule front end, arguments in the reference's order
+    (radis/lbl/calc.py:37-75; mode dispatch :1016-1028).  Equilibrium only
+    (Tvib / Trot / Telec absent or equal to Tgas); ``databank``: path of a
+    HITRAN-160 file or a column dict; ``molecule=`` is accepted as an alias
+    of ``species``; ``wavenum_min=`` / ``wavelength_min=`` ranges pass
+    through to the factory."""
     if mode != "gpu":
         raise NotImplementedError("radis_gb300 implements mode='gpu' only")
-    sf = SpectrumFactory(wavenum_min=wavenum_min, wavenum_max=wavenum_max, wstep=wstep,
-                         molecule=molecule, isotope=isotope, pressure=pressure,
-                         mole_fraction=mole_fraction, path_length=path_length, verbose=verbose,
-                         **kwargs)
+    for t in (Tvib, Trot, Telec):
+        if t is not None and t != Tgas:
+            raise NotImplementedError("non-equilibrium temperatures: the GPU path is equilibrium only")
+    sf = SpectrumFactory(wmin=wmin, wmax=wmax, wunit=wunit, wstep=wstep, species=species, isotope=isotope,
+                         pressure=pressure, mole_fraction=mole_fraction, path_length=path_length, medium=medium,
+                         verbose=verbose, **kwargs)
     if isinstance(databank, dict):
         sf.load_lines(databank)
     else:
         sf.load_databank(databank)
-    return sf.eq_spectrum_gpu(Tgas, name=name)
+    s = sf.eq_spectrum_gpu(Tgas, diluent=diluent, name=name)
+    return (s, sf) if return_factory else s

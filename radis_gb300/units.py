@@ -100,3 +100,70 @@ def convert_per_length(I, from_unit: str, to_unit: str):
         return np.asarray(I, dtype=np.float64) * _PER_WAVENUMBER[from_unit] / _PER_WAVENUMBER[to_unit]
     except KeyError:
         raise ValueError(f"cannot convert {from_unit!r} to {to_unit!r}") from None
+
+
+def air2vacuum(nm):
+    """Vacuum wavelength of air wavelength ``nm``: lambda n(lambda), the index
+    evaluated at the air wavelength (radis/phys/air.py:93-119, which notes
+    the approximation: the index varies little over the shift)."""
+    nm = np.asarray(nm, dtype=np.float64)
+    return air_index(nm * 1e-3) * nm
+
+
+def nm2cm(nm):
+    """Vacuum wavelength (nm) -> wavenumber (cm-1)."""
+    return 1e7 / np.asarray(nm, dtype=np.float64)
+
+
+def nm_air2cm(nm):
+    """Air wavelength (nm) -> vacuum wavenumber (cm-1)."""
+    return nm2cm(air2vacuum(nm))
+
+
+_RANGE_UNITS = {"cm-1": ("cm-1", 1.0), "1/cm": ("cm-1", 1.0), "m-1": ("cm-1", 1e-2), "1/m": ("cm-1", 1e-2),
+                "nm": ("nm", 1.0), "nm_air": ("nm", 1.0), "nm_vac": ("nm", 1.0), "nm_vacuum": ("nm", 1.0),
+                "um": ("nm", 1e3), "µm": ("nm", 1e3), "m": ("nm", 1e9)}
+
+
+def get_wavenumber_range(wmin=None, wmax=None, wunit=None, wavenum_min=None, wavenum_max=None,
+                         wavelength_min=None, wavelength_max=None, medium="air"):
+    """(wavenum_min, wavenum_max, input_wunit) from exactly one of: wmin/wmax
+    in ``wunit`` (default cm-1; wavelength units in ``medium``, or 'nm_air' /
+    'nm_vac'), wavenum_min/wavenum_max (cm-1), wavelength_min/wavelength_max
+    (nm in ``medium``).  Wavelengths in air go through air2vacuum
+    (radis/lbl/base.py get_wavenumber_range; input_wunit is 'cm-1', 'nm' or
+    'nm_vac', the default output unit of the spectra)."""
+    if medium not in ("air", "vacuum"):
+        raise NotImplementedError(f"unknown propagating medium {medium!r}: use 'air' or 'vacuum'")
+    given = [wmin is not None and wmax is not None, wavenum_min is not None and wavenum_max is not None,
+             wavelength_min is not None and wavelength_max is not None]
+    if sum(given) != 1:
+        raise ValueError("pass exactly one range: wmin/wmax (with wunit), wavenum_min/wavenum_max (cm-1) "
+                         "or wavelength_min/wavelength_max (nm)")
+    if wunit is not None and not given[0]:
+        raise ValueError("wunit goes with wmin/wmax")
+    if given[0]:
+        wu = "cm-1" if wunit is None else wunit
+        if wu not in _RANGE_UNITS:
+            raise ValueError(f"unknown range unit {wu!r}")
+        kind, f = _RANGE_UNITS[wu]
+        if wu in ("nm_vac", "nm_vacuum"):
+            medium = "vacuum"
+        elif wu == "nm_air":
+            medium = "air"
+        if kind == "cm-1":
+            wavenum_min, wavenum_max = float(wmin) * f, float(wmax) * f
+        else:
+            wavelength_min, wavelength_max = float(wmin) * f, float(wmax) * f
+    if wavenum_min is not None:
+        lo, hi, unit = float(wavenum_min), float(wavenum_max), "cm-1"
+    else:
+        a, b = float(wavelength_min), float(wavelength_max)
+        if not a < b:
+            raise ValueError("wavelength_min must be below wavelength_max")
+        conv = nm_air2cm if medium == "air" else nm2cm
+        lo, hi = float(conv(b)), float(conv(a))
+        unit = "nm" if medium == "air" else "nm_vac"
+    if not lo < hi:
+        raise ValueError("the range is empty: give min < max")
+    return lo, hi, unit

@@ -1,6 +1,6 @@
 """Generate air-wavelength golden vectors by RUNNING the reference's own
-functions (RADIS 0.17.1): air_index_dispersion and vacuum2air of
-radis/phys/air.py:16-90, pulled out of the source with ``ast`` and executed
+functions (RADIS 0.17.1): air_index_dispersion, vacuum2air and air2vacuum of
+radis/phys/air.py:16-119, pulled out of the source with ``ast`` and executed
 unchanged.  Run where the reference tree is mounted (default path below, or
 ``--ref``); the tests only read the committed ``golden_units.npz``."""
 from __future__ import annotations
@@ -23,7 +23,7 @@ def main():
     src = open(os.path.join(args.ref, "radis", "phys", "air.py")).read()
     ns = {"np": np}
     for node in ast.parse(src).body:
-        if isinstance(node, ast.FunctionDef) and node.name in ("air_index_dispersion", "vacuum2air"):
+        if isinstance(node, ast.FunctionDef) and node.name in ("air_index_dispersion", "vacuum2air", "air2vacuum"):
             exec(compile(ast.Module([node], []), "air.py", "exec"), ns)
     # vacuum wavelengths (nm): the infrared bands of the benchmarks, the visible, and
     # a few below the 300 nm validity limit (index 1 there)
@@ -33,7 +33,9 @@ def main():
         warnings.simplefilter("ignore")
         air = ns["vacuum2air"](nm)
         n = ns["air_index_dispersion"](nm * 1e-3)
-    np.savez_compressed(os.path.join(HERE, "golden_units.npz"), vac_nm=nm, air_nm=air, index=n)
+        vac_of_air = ns["air2vacuum"](nm)      # the same numbers taken as air wavelengths
+    np.savez_compressed(os.path.join(HERE, "golden_units.npz"), vac_nm=nm, air_nm=air, index=n,
+                        air2vac_nm=vac_of_air)
     print("wrote", len(nm), "wavelengths")
 
 

@@ -43,8 +43,37 @@ def test_factory_grid_and_margins():
     np.testing.assert_allclose(sf.wavenumber[-1], 2010.0)
     with pytest.raises(ValueError):
         sf.eq_spectrum_gpu(300.0)            # no database loaded
+    # the GPU path always runs the LDM with the FFT; the factory's method is only recorded
+    assert SpectrumFactory(2000, 2010, broadening_method="voigt").params.broadening_method == "voigt"
+
+
+def test_factory_ranges_and_output_unit():
+    """wmin/wmax + wunit, wavenum_*, wavelength_* in air or vacuum
+    (radis/lbl/base.py get_wavenumber_range); the input range sets the
+    spectra's default output unit."""
+    from radis_gb300 import units as U
+    sf = SpectrumFactory(wavelength_min=4500.0, wavelength_max=4600.0, wstep=0.01, molecule="CO")
+    assert sf.input_wunit == "nm"
+    assert sf.input.wavenum_min == pytest.approx(float(U.nm_air2cm(4600.0)), rel=1e-15)
+    assert sf.input.wavenum_max == pytest.approx(float(U.nm_air2cm(4500.0)), rel=1e-15)
+    assert sf.input.wavenum_min > 1e7 / 4600.0 * (1 - 3e-4)          # air -> vacuum shifts by ~2.7e-4
+    sv = SpectrumFactory(wavelength_min=4500.0, wavelength_max=4600.0, medium="vacuum", molecule="CO")
+    assert sv.input_wunit == "nm_vac" and sv.input.wavenum_min == pytest.approx(1e7 / 4600.0, rel=1e-15)
+    assert SpectrumFactory(4.5, 4.6, wunit="um", molecule="CO").input.wavenum_max == pytest.approx(
+        float(U.nm_air2cm(4500.0)), rel=1e-15)
+    assert SpectrumFactory(4500, 4600, wunit="nm_vac").input_wunit == "nm_vac"
+    assert SpectrumFactory(200000, 201000, wunit="m-1").input.wavenum_min == pytest.approx(2000.0)
+    assert SpectrumFactory(wavenum_min=2000, wavenum_max=2010).input_wunit == "cm-1"
+    with pytest.raises(ValueError):
+        SpectrumFactory(2000, 2010, wavenum_min=2000, wavenum_max=2010)
+    with pytest.raises(ValueError):
+        SpectrumFactory(2010, 2000)
+    with pytest.raises(ValueError):
+        SpectrumFactory(wavenum_min=2000, wavenum_max=2010, wunit="cm-1")
     with pytest.raises(NotImplementedError):
-        SpectrumFactory(2000, 2010, broadening_method="voigt")
+        SpectrumFactory(2000, 2010, medium="water")
+    with pytest.raises(ValueError):
+        SpectrumFactory(2000, 2010, species="CO", molecule="CO2")
 
 
 def test_derived_quantities():
@@ -72,3 +101,19 @@ def test_spectrum_get_and_crop():
     assert s.get("abscoeff")[0][0] == pytest.approx(2000.2)
     with pytest.warns(UserWarning):
         assert s.recalc_gpu("abscoeff", Tgas=600) is None
+
+
+def test_calc_spectrum_arguments():
+    """The reference's argument order (radis/lbl/calc.py:37-75) and the
+    checks made before any device work: GPU mode only, equilibrium only."""
+    import inspect
+
+    from radis_gb300.factory import calc_spectrum
+    names = list(inspect.signature(calc_spectrum).parameters)
+    assert names[:12] == ["wmin", "wmax", "wunit", "Tgas", "Tvib", "Trot", "Telec", "pressure", "species",
+                          "isotope", "mole_fraction", "diluent"]
+    lines = S.co_like(100)
+    with pytest.raises(NotImplementedError):
+        calc_spectrum(2000, 2010, Tgas=700.0, mode="cpu", databank=lines)
+    with pytest.raises(NotImplementedError):
+        calc_spectrum(2000, 2010, Tgas=700.0, Tvib=2000.0, databank=lines)

@@ -1,7 +1,8 @@
 """Wave units, media and quantity units of Spectrum.get (CPU).
 
-* Air wavelengths equal the reference's own vacuum2air / Ciddor index
-  (radis/phys/air.py, run by tests/golden/make_golden_units.py) bit for bit.
+* Air wavelengths equal the reference's own vacuum2air / air2vacuum /
+  Ciddor index (radis/phys/air.py, run by tests/golden/make_golden_units.py)
+  bit for bit.
 * Radiance per nm <-> per cm-1 keeps the integral over the band, the check
   the reference documents for convert_rad2cm (radis/phys/units.py); prefix
   changes are exact powers of ten; conversions round-trip.
@@ -28,6 +29,7 @@ def test_air_wavelengths_match_reference():
         warnings.simplefilter("ignore")
         assert np.array_equal(U.vacuum2air(G["vac_nm"]), G["air_nm"])
         assert np.array_equal(U.air_index(G["vac_nm"] * 1e-3), G["index"])
+        assert np.array_equal(U.air2vacuum(G["vac_nm"]), G["air2vac_nm"])
     with pytest.warns(UserWarning):
         assert U.air_index(np.array([0.25]))[0] == 1.0
 
