@@ -125,16 +125,44 @@ class Spectrum:
         if var not in self._q:
             raise KeyError(var)
 
-    def crop(self, wmin=None, wmax=None, wunit="cm-1"):
+    def get_wavenumber(self, copy=True):
+        """Vacuum wavenumber (cm-1)."""
         w = self._q["wavenumber"]
-        sel = np.ones(len(w), dtype=bool)
+        return np.array(w, copy=True) if copy else w
+
+    def get_wavelength(self, medium="air", copy=True):
+        """Wavelength (nm) in ``medium`` (spectrum.py:1421-1460)."""
+        if medium not in ("air", "vacuum"):
+            raise NotImplementedError(f"unknown propagating medium {medium!r}")
+        w = 1e7 / np.asarray(self._q["wavenumber"], dtype=np.float64)
+        return U.vacuum2air(w) if medium == "air" else w
+
+    def get_waveunit(self):
+        """'cm-1': the spectral axis is stored as wavenumbers."""
+        return "cm-1"
+
+    def crop(self, wmin=None, wmax=None, wunit="default", inplace=True):
+        """Keep the points inside [wmin, wmax] given in ``wunit`` ('cm-1';
+        'nm' in the spectrum's medium, 'nm_air', 'nm_vac'; 'default' = the
+        default output unit) (radis/spectrum/operations.py crop)."""
+        if wunit == "default":
+            wunit = self.conditions.get("default_output_unit", "cm-1")
+        wu = U.cast_waveunit(wunit)
+        medium = "air" if wunit == "nm_air" else self.conditions.get("medium", "air")
+        if wu == "cm-1":
+            axis = self._q["wavenumber"]
+        else:
+            axis = self.get_wavelength(medium="vacuum" if wu == "nm_vac" else medium, copy=False)
+        sel = np.ones(len(axis), dtype=bool)
         if wmin is not None:
-            sel &= w >= wmin
+            sel &= axis >= wmin
         if wmax is not None:
-            sel &= w <= wmax
-        for k in self._q:
-            self._q[k] = self._q[k][sel]
-        return self
+            sel &= axis <= wmax
+        s = self if inplace else Spectrum(dict(self._q), self.units, self.conditions, self.cond_units,
+                                          name=self.name)
+        for k in s._q:
+            s._q[k] = s._q[k][sel]
+        return s
 
     def recalc_gpu(self, var="abscoeff", wunit="default", Iunit="default", pressure=None, Tgas=None,
                    mole_fraction=None, path_length=None, slit_function=None, verbose=False):

@@ -97,3 +97,17 @@ def test_get_quantity_units():
     np.testing.assert_allclose(t, np.exp(-2.0 * k), rtol=1e-12)
     with pytest.raises(ValueError):
         s.get("transmittance_noslit", Iunit="cm-1")
+
+
+def test_crop_in_wavelength_and_accessors():
+    s, w = _spectrum()
+    lam_air = U.vacuum2air(1e7 / w)
+    np.testing.assert_array_equal(s.get_wavelength(), lam_air)
+    np.testing.assert_array_equal(s.get_wavelength("vacuum"), 1e7 / w)
+    assert s.get_waveunit() == "cm-1" and np.array_equal(s.get_wavenumber(), w)
+    lo, hi = lam_air[600], lam_air[400]                 # wavelength falls as wavenumber rises
+    c = s.crop(lo, hi, wunit="nm", inplace=False)
+    assert np.array_equal(c.get("abscoeff")[0], w[400:601])
+    assert len(s.get("abscoeff")[0]) == 1001            # not in place
+    v = s.crop(1e7 / w[700], 1e7 / w[300], wunit="nm_vac")
+    assert v is s and np.array_equal(s.get("abscoeff")[0], w[300:701])
