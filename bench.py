@@ -7,21 +7,31 @@
 One step = one spectrum (scatter -> FFT/Voigt reduce -> IFFT) of the 5M-line
 CO2-like list over 2000-2400 cm-1 at 0.001 cm-1 (400 001 points), 8 x 16 LDM
 nodes, T = 1500 K, p = 1 bar, x = 0.1.  ``value``: spectra/s with the line list
-resident in HBM, timed with CUDA events on the launching stream.  ``e2e``: the
-same through the host API (rg_synthesize_host: conditions in, float32
-spectrum copied back to pinned host memory, synchronous), plus the cold path
-(upload from host arrays + plan + spectrum) reported beside it.  N > 1 runs
-independent replicas, one per GPU (the path needs no exchange between GPUs).
+resident in HBM, timed with CUDA events on the launching stream (no per-stage
+events inside that region; a separate pass records them for the stage table
+and the roofline).  ``e2e``: the same through the host API
+(rg_synthesize_host: conditions in, float32 spectrum copied back to pinned
+host memory, synchronous), plus the cold path (upload from host arrays + plan
++ spectrum) reported beside it.  ``error``: the timed spectrum's
+abscoeff, absorbance, emissivity, transmittance and radiance against the
+reference's CPU path run on the whole workload (the same run is the
+``cpu_baseline`` timing).  ``c3``: the 100M-line H2O-like workload (1 500 001
+points, 12 x 24 nodes): stage times, scatter roofline and error against the
+oracle over the full spectrum.  ``fft_vs_cufft``: cuFFT (through torch) on
+the same batched rows as this library's FFT stages.  N > 1 runs independent
+replicas, one per GPU (the path needs no exchange between GPUs).
 
-``--impl reference`` times the CPU oracle (an FP64 numpy restatement of the
-reference's CPU LDM path; the reference itself needs pandas/astropy/numba and
-its GPU path needs Vulkan, neither of which exists here) on rank 0 only.
+``--impl reference`` runs the reference's CPU LDM path, restated in FP64
+numpy by the oracle (the reference itself needs pandas/astropy/numba and its
+GPU path needs Vulkan, neither of which exists here), on the whole workload
+every step, on rank 0 only; it imports nothing of this library.
 
 ``--ingest-only`` times the host-side HITRAN-160 ingestion instead (no GPU).
 """
 from __future__ import annotations
 
 import argparse
+import importlib.util
 import json
 import math
 import os
@@ -57,14 +67,28 @@ WORKLOADS = {
 }
 
 
-def workload_desc(name, n_lines, n_v, grid, nbytes):
-    label, _, _, vmin, vmax, ws, T, p, x, _, _ = WORKLOADS[name]
+def line_record_bytes(lines):
+    """Bytes the scatter reads per line: v0 as an FP32 (hi, lo) pair, then
+    log2 S', E_low, gamma_air, gamma_self, n_air (4 B each), the pressure
+    shift (4 B) and the isotopologue slot (1 B) only when the list has them."""
+    import numpy as np
+    b = 8 + 5 * 4
+    if lines.get("delta") is not None:
+        b += 4
+    if lines.get("iso") is not None and np.unique(np.asarray(lines["iso"])).size > 1:
+        b += 1
+    return b
+
+
+def workload_desc(name, n_lines, n_v, line_bytes):
+    """The workload a bench line measures (identical in both arms)."""
+    label, _, _, vmin, vmax, ws, T, p, x, nG, nL = WORKLOADS[name]
     return {
         "workload": (f"{label} synthetic list, {n_lines} lines, {vmin:g}-{vmax:g} cm-1 at {ws:g} cm-1 "
-                     f"({n_v} points), {grid[0]}x{grid[1]} LDM nodes, T={T:g} K, p={p:g} bar, x={x:g}"),
-        "n_lines": n_lines, "n_v": n_v, "n_ft": grid[2], "ldm_nodes": [grid[0], grid[1]],
-        "l2": ("inputs larger than L2 (line list %d MB, LDM %d MB, packed FFT rows %d MB)"
-               % tuple(b // 1000000 for b in nbytes)),
+                     f"({n_v} points), {nG}x{nL} LDM nodes, T={T:g} K, p={p:g} bar, x={x:g}"),
+        "n_lines": n_lines, "n_v": n_v, "ldm_nodes": [nG, nL],
+        "l2": ("inputs larger than L2 (129 MB): resident line list %d MB (%d B/line), LDM %d MB"
+               % (n_lines * line_bytes // 1000000, line_bytes, nG * nL * n_v * 4 // 1000000)),
         "parallelism": "replicas",
     }
 
@@ -142,17 +166,18 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def algorithmic_bytes(n_lines_read, n_nodes, n_v, n_ft, info):
-    """Bytes each kernel must move once (per spectrum): the line records and
-    the LDM written once (n_v columns, no zero padding); the column FFT reads
-    its node rows and writes the packed complex rows; the row stage reads them
-    (its accumulator G is stored once); the inverse stages read/write G and
-    the output.  With the merged layout the Gaussian stage reads the
-    wide-node LDM rows and writes the n_L merged rows (n_v + 2 ext points),
-    and the column FFT reads those and the narrow-node rows."""
+def algorithmic_bytes(n_lines_read, line_bytes, n_nodes, n_v, n_ft, info):
+    """Bytes each kernel must move once (per spectrum): the line records
+    (``line_bytes`` each) and the LDM written once (n_v columns, no zero
+    padding); the column FFT reads its node rows and writes the packed complex
+    rows; the row stage reads them (its accumulator G is stored once); the
+    inverse stages read/write G and the output.  With the merged layout the
+    Gaussian stage reads the wide-node LDM rows and writes the n_L merged rows
+    (n_v + 2 ext points), and the column FFT reads those and the narrow-node
+    rows."""
     pairs = int(info.fft_rows or n_nodes) // 2
     out = {
-        "k_scatter": n_lines_read * 32 + n_nodes * n_v * 4,
+        "k_scatter": n_lines_read * line_bytes + n_nodes * n_v * 4,
         "k_col_fft_fwd": n_nodes * n_v * 4 + pairs * n_ft * 8,
         "k_row_fft_voigt": pairs * n_ft * 8 + n_ft * 8,
         "k_row_ifft": 2 * n_ft * 8,
@@ -191,67 +216,88 @@ def load_traffic(workload):
     return out
 
 
-def cpu_baseline_sample(wl, lines, grid, n_ft, workers, frac=20):
-    """Oracle timing on a bounded sample: the per-line stages (scaling +
-    scatter) on 1/frac of the lines (contiguous block), scaled by frac, plus
-    the full FFT/convolution stage (independent of the line count)."""
-    import numpy as np
-
-    from oracle import ldm_oracle as O
-    _, _, M, vmin, vmax, ws, T, p, x, _, _ = WORKLOADS[wl]
-    n_v = int(round((vmax - vmin) / ws)) + 1
-    n = len(lines["v0"])
-    m = n // frac
-    lo = (n - m) // 2
-    sub = {k: np.asarray(v)[lo:lo + m] for k, v in lines.items()}
-    t0 = time.perf_counter()
-    kpos, lgG, lgL, S = O.line_quantities(sub, T, p, x, vmin, ws, molar_mass=M)
-    LDM = O.ldm_scatter(kpos, lgG, lgL, S, n_v, grid)
-    t1 = time.perf_counter()
-    O.ldm_convolve(LDM, n_v, ws, grid, int(n_ft), fft_workers=workers)
-    t2 = time.perf_counter()
-    return (t1 - t0) * (n / m) + (t2 - t1), (t1 - t0), (t2 - t1), m
+def _synthetic():
+    """The seeded workload generators (radis_gb300/synthetic.py, numpy only),
+    loaded from their file so that the reference arm imports nothing of the
+    library package."""
+    spec = importlib.util.spec_from_file_location("rg_bench_synthetic",
+                                                  os.path.join(ROOT, "radis_gb300", "synthetic.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
 
 
 def load_workload(wl):
-    from radis_gb300 import synthetic as S
+    S = _synthetic()
     _, fac, M, vmin, vmax, ws, T, p, x, nG, nL = WORKLOADS[wl]
     lines = getattr(S, fac)()
     return lines, M, vmin, ws, S.grid_points(vmin, vmax, ws), T, p, x, nG, nL
+
+
+def reference_spectrum(wl, lines, workers, axes=None, n_ft=None, line_chunk=None):
+    """The reference's CPU LDM path (broadening_method='fft') on the whole
+    line list, as the oracle restates it in FP64 numpy: per-line scaling, the
+    8 np.add.at of radis/lbl/broadening.py:2478-2485 (single-threaded, as in
+    the reference), per-node rfft x folded Voigt FT and one irfft
+    (:2521-2530; FFTs through scipy.fft on ``workers`` host threads), x the
+    number density.  Node axes from the oracle's own restatement of the
+    reference's envelope rule unless ``axes`` is given; the FFT length is the
+    CPU path's 2 n_v (broadening.py:2340) unless ``n_ft`` is given.  Returns
+    (abscoeff cm-1, seconds for scaling + scatter, seconds for the FFT stage)."""
+    import numpy as np
+
+    from oracle import ldm_oracle as O
+    _, _, M, vmin, vmax, ws, T, p, x, nG, nL = WORKLOADS[wl]
+    n_v = int(round((vmax - vmin) / ws)) + 1
+    if axes is None:
+        axes = O.envelope_axes(lines, T, p, x, NG=nG, NL=nL, molar_mass=M)
+    n_ft = 2 * n_v if n_ft is None else int(n_ft)
+    n = len(lines["v0"])
+    step = n if not line_chunk else int(line_chunk)
+    t0 = time.perf_counter()
+    LDM = None
+    for a in range(0, n, step):
+        part = lines if step >= n else {k: (np.asarray(v)[a:a + step] if np.ndim(v) == 1 else v)
+                                        for k, v in lines.items()}
+        kpos, lgG, lgL, S = O.line_quantities(part, T, p, x, vmin, ws, molar_mass=M)
+        LDM = O.ldm_scatter(kpos, lgG, lgL, S, n_v, axes, out=LDM)
+        del kpos, lgG, lgL, S
+    t1 = time.perf_counter()
+    spec = O.ldm_convolve(LDM, n_v, ws, axes, n_ft, fft_workers=workers)
+    t2 = time.perf_counter()
+    return spec * O.number_density(p, T, x), t1 - t0, t2 - t1
 
 
 def run_reference(args):
     ws_, rank, _ = dist_env()
     if rank != 0:
         return 0
-    from radis_gb300 import _build, _lib as L
-    _build.build()
     wl = args.workload
     lines, M, vmin, dv, n_v, T, p, x, nG, nL = load_workload(wl)
-    g = L.grid_estimate(lines, M, vmin, dv, n_v, T, p, x, n_G=nG, n_L=nL)
     workers = os.cpu_count() or 1
-    times = []
-    parts = []
+    times, parts = [], []
     for i in range(args.warmup + args.steps):
-        t, tl, tc, m = cpu_baseline_sample(wl, lines, g.axes(), g.n_ft, workers)
+        t0 = time.perf_counter()
+        _, tl, tc = reference_spectrum(wl, lines, workers)
+        t = time.perf_counter() - t0
         if i >= args.warmup:
             times.append(t)
             parts.append((tl, tc))
     step = statistics.mean(times)
     value = 1.0 / step
     n = len(lines["v0"])
-    sample = (f"per step: scaling+scatter of {m} of {n} lines (x{n / m:.0f}) "
-              f"+ full FFT/Voigt stage ({g.n_G * g.n_L} node rows of {g.n_ft}); numpy/scipy FP64")
-    nbytes = (n * 32, g.n_G * g.n_L * n_v * 4, g.n_G * g.n_L * g.n_ft * 4)
+    sample = (f"whole workload every step: all {n} lines scaled and scattered (8 np.add.at, one host thread, "
+              f"as the reference), {nG * nL} node rows of rfft length {2 * n_v} x folded Voigt FT + one irfft "
+              f"(scipy.fft, {workers} host threads); FP64")
     out = {
         "metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": ws_, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": workload_desc(wl, n, n_v, (g.n_G, g.n_L, g.n_ft), nbytes),
+        "config": workload_desc(wl, n, n_v, line_record_bytes(lines)),
         "cpu_baseline": {"value": value, "unit": "spectra/s", "cores": workers, "kind": "port",
-                         "sample": sample + f"; FFT threads {workers}, add.at single-threaded"},
+                         "sample": sample},
         "e2e": {"value": value, "unit": "spectra/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "stage_s": {"lines_scaled": statistics.mean(q[0] for q in parts) * n / m,
+        "stage_s": {"lines_scaled_scattered": statistics.mean(q[0] for q in parts),
                     "fft_voigt": statistics.mean(q[1] for q in parts)},
     }
     print(json.dumps(out))
@@ -492,6 +538,164 @@ def run_autodiff(ctx, L, n_cond=64, seed=12):
     return res
 
 
+def rel_err(got, ref):
+    """max |got - ref| / max |ref| (0 for an all-zero reference and result)."""
+    import numpy as np
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    den = float(np.max(np.abs(ref))) if ref.size else 0.0
+    num = float(np.max(np.abs(got - ref))) if ref.size else 0.0
+    return num / den if den > 0 else num
+
+
+def quantity_errors(plan, T, p, x, vmin, dv, n_v, ref_abscoeff, path_length=1.0):
+    """The spectrum at (T, p, x) with the device post-processing
+    (rg_synthesize_quantities: abscoeff, absorbance, emissivity,
+    transmittance, radiance) against the same quantities derived from the
+    reference abscoeff on the host in FP64; max |d| / max |ref| per output."""
+    import numpy as np
+    import torch
+
+    from oracle import ldm_oracle as O
+    buf = torch.empty(5 * n_v, dtype=torch.float32, device="cuda")
+    info = plan.synthesize_quantities(T, p, x, path_length, buf.data_ptr(),
+                                      torch.cuda.current_stream().cuda_stream or 1)
+    torch.cuda.synchronize()
+    rows = buf.double().cpu().numpy().reshape(5, n_v)
+    sc = math.exp(info.log_scale)
+    got = {"abscoeff": rows[0] * sc, "absorbance": rows[1] * sc, "emissivity_noslit": rows[2],
+           "transmittance_noslit": rows[3], "radiance_noslit": rows[4]}
+    ref = O.quantities(ref_abscoeff, vmin, dv, T, path_length)
+    return {k: rel_err(got[k], ref[k]) for k in got}
+
+
+def run_fft_compare(n_ft, rows, our_fwd_ms, our_inv_ms, reps=10):
+    """cuFFT, through torch.fft, on the batched rows this library's FFT stages
+    transform: R2C of ``rows`` real rows of length n_ft (the reference's
+    per-node rfft, radis/lbl/broadening.py:2521-2530), C2C of the rows packed
+    in complex pairs (what the four-step kernels transform), and the one C2R
+    of the summed spectrum.  Library calls, timed with CUDA events on the
+    current stream; outside the product path."""
+    import torch
+    st = torch.cuda.current_stream()
+    x = torch.randn(rows, n_ft, device="cuda", dtype=torch.float32)
+    z = torch.randn(max(rows // 2, 1), n_ft, device="cuda", dtype=torch.complex64)
+    h = torch.randn(n_ft // 2 + 1, device="cuda", dtype=torch.complex64)
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    r2c = timed(lambda: torch.fft.rfft(x, dim=1))
+    c2c = timed(lambda: torch.fft.fft(z, dim=1))
+    c2r = timed(lambda: torch.fft.irfft(h, n=n_ft))
+    gbs = lambda b, ms: b / (ms * 1e-3) / 1e9
+    half = n_ft // 2 + 1
+    out = {
+        "rows": rows, "n_ft": n_ft,
+        "cufft_r2c_rows_ms": r2c, "cufft_r2c_GB/s": gbs(rows * n_ft * 4 + rows * half * 8, r2c),
+        "cufft_c2c_pairs_ms": c2c, "cufft_c2c_GB/s": gbs(2 * (rows // 2) * n_ft * 8, c2c),
+        "cufft_c2r_ms": c2r,
+        "ours_forward_fft_voigt_ms": our_fwd_ms,
+        "ours_inverse_ms": our_inv_ms,
+        "note": ("ours = column FFT (+ twiddle) + row FFT fused with the Voigt multiply and the sum over "
+                 "nodes, on the same packed rows; cuFFT's figures exclude the Voigt multiply and node sum"),
+    }
+    del x, z, h
+    torch.cuda.empty_cache()
+    return out
+
+
+def time_plan(plan, T, p, x, n_v, K, stream, warm=3):
+    """(ms per spectrum over K spectra with no stage events, per-stage average
+    ms over a second pass with stage events, Gaussian-stage ms, info with the
+    lines in the window)."""
+    import torch
+    out = torch.empty(n_v, dtype=torch.float32, device="cuda")
+    sptr = stream.cuda_stream
+    for _ in range(warm):
+        plan.synthesize_device(T, p, x, out.data_ptr(), sptr)
+    info = plan.synthesize_device(T, p, x, out.data_ptr(), sptr, timing=1)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(K):
+        plan.synthesize_device(T, p, x, out.data_ptr(), sptr)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / K
+    for _ in range(min(K, 200)):
+        plan.synthesize_device(T, p, x, out.data_ptr(), sptr, timing=2)
+    stage_sum, stage_n = plan.stage_times()
+    stage_avg = [v / max(stage_n, 1) for v in stage_sum]
+    gauss = plan.gauss_time() / max(stage_n, 1)
+    return ms, stage_avg, gauss, info
+
+
+def kernel_times(stage_avg, gauss, info):
+    """Per-kernel ms from the stage events: with the merged layout the column
+    stage is the Gaussian stage (its own event) followed by the column FFT."""
+    kt = {STAGES[i]: stage_avg[i] for i in range(5)}
+    if info.merged_rows:
+        kt["k_gauss_merge"] = gauss
+        kt["k_col_fft_fwd"] = stage_avg[1] - gauss
+    return kt
+
+
+def run_c3(ctx, L, h2o_host, h2o, K, peak, peak_kind, workers, check=True):
+    """The 100M-line H2O-like workload (1 500 001 points at 0.005 cm-1,
+    12 x 24 nodes, T = 2000 K, p = 1 bar, x = 0.2) on the resident list:
+    spectra/s, stage times, the scatter's HBM roofline, and the error of the
+    full spectrum against the oracle (FP64, on the plan's node axes and FFT
+    length, lines scaled and scattered in blocks of 10M)."""
+    import torch
+    _, _, M, vmin, vmax, dv, T, p, x, nG, nL = WORKLOADS["h2o_100M"]
+    n_v = int(round((vmax - vmin) / dv)) + 1
+    plan = L.Plan(h2o, vmin, dv, n_v, n_G=nG, n_L=nL)
+    stream = torch.cuda.Stream()
+    ms, stage_avg, gauss, info = time_plan(plan, T, p, x, n_v, K, stream)
+    g = info.grid
+    n_nodes = g.n_G * g.n_L + (g.n_G * g.n_L) % 2
+    lb = line_record_bytes(h2o_host)
+    ab = algorithmic_bytes(info.lines_in_window, lb, n_nodes, n_v, g.n_ft, info)
+    kt = kernel_times(stage_avg, gauss, info)
+    stages = {k: {"ms": t, "algorithmic_bytes": ab[k], "GB/s": ab[k] / (t * 1e-3) / 1e9 if t > 0 else None}
+              for k, t in kt.items()}
+    sc_gbs = stages["k_scatter"]["GB/s"]
+    res = {
+        "workload": workload_desc("h2o_100M", len(h2o_host["v0"]), n_v, lb)["workload"],
+        "spectra_per_s": 1000.0 / ms, "ms_per_spectrum": ms, "spectra_timed": K,
+        "stages": stages,
+        "scatter_roofline": {"achieved": sc_gbs, "peak": peak, "unit": "GB/s", "frac": sc_gbs / peak,
+                             "peak_kind": peak_kind, "bytes_per_line": lb,
+                             "lines_read": int(info.lines_in_window)},
+        "fft_layout": {"fft_rows": int(info.fft_rows), "merged_rows": int(info.merged_rows),
+                       "n_ft": int(g.n_ft)},
+    }
+    if check:
+        import numpy as np
+
+        from oracle import ldm_oracle as O
+        host = np.empty(n_v, dtype=np.float32)
+        o, inf2 = plan.synthesize_host(T, p, x, out=host)
+        gpu = o.astype(np.float64) * math.exp(inf2.log_scale)
+        t0 = time.perf_counter()
+        ref = O.synthesize(h2o_host, T, p, x, vmin, dv, n_v, g.axes(), g.n_ft, molar_mass=M,
+                           fft_workers=workers, line_chunk=10_000_000)
+        res["error"] = {"abscoeff_max_rel": rel_err(gpu, ref),
+                        "vs": "FP64 oracle over the full 1 500 001-point spectrum, all lines",
+                        "oracle_s": time.perf_counter() - t0}
+    plan.close()
+    return res
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -510,6 +714,7 @@ def run_ours(args):
     wl = args.workload
     lines, M, vmin, dv, n_v, T, p, x, nG, nL = load_workload(wl)
     n_lines = len(lines["v0"])
+    lb = line_record_bytes(lines)
     ctx = L.Context(local)
     t0 = time.perf_counter()
     ln = L.Lines(ctx, lines, M)
@@ -520,8 +725,9 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     out = torch.empty(n_v, dtype=torch.float32, device="cuda")
     sptr = stream.cuda_stream
+    W = max(args.warmup, 3)
 
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(W):
         plan.synthesize_device(T, p, x, out.data_ptr(), sptr)
     torch.cuda.synchronize()
     # lines actually read by the scatter (window + shift margins): all of them here
@@ -532,7 +738,6 @@ def run_ours(args):
         dist.barrier()
 
     K = args.steps
-    ring_steps = min(K, 200)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
@@ -541,25 +746,28 @@ def run_ours(args):
             dist.barrier()
         e0.record(stream)
         for i in range(K):
-            plan.synthesize_device(T, p, x, out.data_ptr(), sptr, timing=2 if i < ring_steps else 0)
+            plan.synthesize_device(T, p, x, out.data_ptr(), sptr)
         e1.record(stream)
         torch.cuda.synchronize()
         if ws > 1:
             dist.barrier()
     ms = e0.elapsed_time(e1) / K
+    ms = max_over_ranks(ms, ws, "cuda")
+    value = ws * 1000.0 / ms   # replicas: every rank synthesises one spectrum per step
+    # per-stage times: a separate pass with stage events (not in the timed region above)
+    for _ in range(min(K, 200)):
+        plan.synthesize_device(T, p, x, out.data_ptr(), sptr, timing=2)
     stage_sum, stage_n = plan.stage_times()
     stage_avg = [s / max(stage_n, 1) for s in stage_sum]
     gauss_avg = plan.gauss_time() / max(stage_n, 1)
-    ms = max_over_ranks(ms, ws, "cuda")
-    value = ws * 1000.0 / ms   # replicas: every rank synthesises one spectrum per step
 
     # e2e through the host API: conditions in, spectrum out to pinned memory
     host = torch.empty(n_v, dtype=torch.float32, pin_memory=True).numpy()
     lat = []
-    for i in range(max(args.warmup, 3) + K):
+    for i in range(W + K):
         t0 = time.perf_counter()
         plan.synthesize_host(T, p, x, out=host)
-        if i >= max(args.warmup, 3):
+        if i >= W:
             lat.append(time.perf_counter() - t0)
     e2e_ms = statistics.mean(lat) * 1e3
     lat_ms = sorted(v * 1e3 for v in lat)
@@ -578,13 +786,8 @@ def run_ours(args):
         ln2.close()
 
     peak, peak_kind = load_peaks()
-    ab = algorithmic_bytes(lines_in_window, n_nodes, n_v, g.n_ft, info)
-    # per-kernel times: with the merged layout the column stage is the
-    # Gaussian stage (its own event) followed by the column FFT
-    kt = {STAGES[i]: stage_avg[i] for i in range(5)}
-    if info.merged_rows:
-        kt["k_gauss_merge"] = gauss_avg
-        kt["k_col_fft_fwd"] = stage_avg[1] - gauss_avg
+    ab = algorithmic_bytes(lines_in_window, lb, n_nodes, n_v, g.n_ft, info)
+    kt = kernel_times(stage_avg, gauss_avg, info)
     name = max(kt, key=kt.get)   # the dominant kernel
     achieved = ab[name] / (kt[name] * 1e-3) / 1e9
     traffic = load_traffic(wl).get(name)
@@ -595,16 +798,16 @@ def run_ours(args):
     if rank == 0:
         res = {
             "metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": ws, "steps": K,
-            "warmup": max(args.warmup, 3), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "warmup": W, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": workload_desc(wl, n_lines, n_v, (g.n_G, g.n_L, g.n_ft),
-                                    (n_lines * 32, n_nodes * n_v * 4, int(info.fft_rows or n_nodes) * g.n_ft * 4)),
+            "config": workload_desc(wl, n_lines, n_v, lb),
             "clocks": clk.summary(),
             "gpu_launches": kernels_per_step(info) * K,
             "e2e": {"value": ws * 1000.0 / e2e_ms, "unit": "spectra/s",
                     "h2d_bytes_per_step": 0, "d2h_bytes_per_step": n_v * 4,
-                    "note": ("resident line list; per step the conditions travel as kernel "
-                             "parameters and the float32 spectrum is copied to pinned host memory")},
+                    "note": ("resident line list (as the reference's gpuApp.iterate); per step the conditions "
+                             "travel as kernel parameters and the float32 spectrum is copied to pinned host "
+                             "memory")},
             "e2e_cold": {"value": 1.0 / statistics.mean(cold), "unit": "spectra/s",
                          "h2d_bytes_per_step": n_lines * (8 + 8 + 4 * 4), "d2h_bytes_per_step": n_v * 4,
                          "note": "line upload from host arrays + envelopes + plan + one spectrum"},
@@ -615,7 +818,7 @@ def run_ours(args):
                          "avg_launch_ms": kt[name]},
             "stages": stages,
             "fft_layout": {"fft_rows": int(info.fft_rows), "merged_rows": int(info.merged_rows),
-                           "gauss_halfwidth": int(info.merged_ext),
+                           "gauss_halfwidth": int(info.merged_ext), "n_ft": int(g.n_ft),
                            "note": ("k_col_fft_fwd covers the real-space Gaussian stage of the merged "
                                     "layout and the column FFTs")},
             "setup_s": setup_s,
@@ -625,31 +828,57 @@ def run_ours(args):
                                        "each wide-node row with its residual Gaussian, ~220 FMA per merged "
                                        "output point on the 8 wide nodes of this grid): frac is the HBM fraction "
                                        "of the bytes it must move")
+        workers = os.cpu_count() or 1
         if ws == 1 and not args.no_cpu_baseline:
-            workers = os.cpu_count() or 1
-            t, tl, tc, m = cpu_baseline_sample(wl, lines, g.axes(), g.n_ft, workers)
+            # the reference's CPU path on the whole workload, once: its time is the
+            # CPU baseline and its spectrum the reference for the timed spectrum's error
+            t0 = time.perf_counter()
+            ref, tl, tc = reference_spectrum(wl, lines, workers)
+            t = time.perf_counter() - t0
             res["cpu_baseline"] = {
                 "value": 1.0 / t, "unit": "spectra/s", "cores": workers, "kind": "port",
-                "sample": (f"oracle (FP64 numpy restatement of the reference CPU LDM path): scaling+scatter "
-                           f"of {m} of {n_lines} lines scaled x{n_lines / m:.0f} ({tl:.2f} s) + full FFT/Voigt "
-                           f"stage ({tc:.2f} s, scipy.fft workers={workers}); add.at single-threaded")}
+                "sample": (f"one spectrum of the whole workload: all {n_lines} lines scaled and scattered "
+                           f"(8 np.add.at, one host thread, as the reference; {tl:.2f} s), {nG * nL} node rows "
+                           f"of rfft length {2 * n_v} x folded Voigt FT + one irfft (scipy.fft, {workers} host "
+                           f"threads; {tc:.2f} s); FP64 oracle restatement of the reference's CPU path")}
+            res["error"] = quantity_errors(plan, T, p, x, vmin, dv, n_v, ref)
+            res["error"]["vs"] = ("reference CPU path (FP64 oracle) on the same workload, n_ft = 2 n_v as the "
+                                  "reference; max |gpu - ref| / max |ref| per output, path length 1 cm")
+            del ref
+        if ws == 1 and not args.no_fft_compare:
+            fwd = kt["k_col_fft_fwd"] + kt["k_row_fft_voigt"]
+            res["fft_vs_cufft"] = {wl: run_fft_compare(int(g.n_ft), int(info.fft_rows or n_nodes), fwd,
+                                                       kt["k_row_ifft"] + kt["k_col_ifft"])}
         if ws == 1 and not args.no_slit:
             plan.synthesize_device(T, p, x, out.data_ptr(), torch.cuda.current_stream().cuda_stream or 1)
             res["slit"] = run_slit(ctx, out, vmin, dv)
         if ws == 1 and not args.no_autodiff:
             res["autodiff"] = run_autodiff(ctx, L)
+        h2o = h2o_host = None
+        if ws == 1 and (not args.no_serving or not args.no_c3):
+            h2o_host = S.h2o_like(args.serve_h2o_lines)
+            h2o = L.Lines(ctx, h2o_host, 18.0)
+        if ws == 1 and not args.no_c3 and args.serve_h2o_lines == 100_000_000:
+            c3 = run_c3(ctx, L, h2o_host, h2o, 10, peak, peak_kind, workers, check=not args.no_c3_check)
+            if not args.no_fft_compare:
+                kt3 = {k: v["ms"] for k, v in c3["stages"].items()}
+                c3_rows = c3["fft_layout"]["fft_rows"]
+                res.setdefault("fft_vs_cufft", {})["h2o_100M"] = run_fft_compare(
+                    c3["fft_layout"]["n_ft"], c3_rows, kt3["k_col_fft_fwd"] + kt3["k_row_fft_voigt"],
+                    kt3["k_row_ifft"] + kt3["k_col_ifft"], reps=5)
+            res["c3"] = c3
+        if h2o_host is not None:
+            h2o_host = None
         if ws == 1 and not args.no_serving:
             co = L.Lines(ctx, S.co_like(), 28.0)
-            h2o_lines = S.h2o_like(args.serve_h2o_lines)
-            h2o = L.Lines(ctx, h2o_lines, 18.0)
-            del h2o_lines
             lists = {"co_10k": (co, 1900.0, 2300.0), "co2_5M": (ln, 2000.0, 2400.0),
                      "h2o": (h2o, 500.0, 8000.0)}
             sv = run_serving(ctx, L, lists, args.serve_requests, args.serve_slots)
             sv["lists"] = {"co_10k": 10_000, "co2_5M": n_lines, "h2o": args.serve_h2o_lines}
             res["serving"] = sv
-            h2o.close()
             co.close()
+        if h2o is not None:
+            h2o.close()
         print(json.dumps(res))
     plan.close()
     ln.close()
@@ -732,6 +961,9 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-autodiff", action="store_true")
     ap.add_argument("--no-slit", action="store_true")
+    ap.add_argument("--no-c3", action="store_true", help="skip the 100M-line H2O-like section")
+    ap.add_argument("--no-c3-check", action="store_true", help="skip its full-size oracle comparison")
+    ap.add_argument("--no-fft-compare", action="store_true", help="skip the cuFFT comparison")
     ap.add_argument("--serve-requests", type=int, default=120)
     ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--serve-h2o-lines", type=int, default=100_000_000)

@@ -294,10 +294,14 @@ int rg_jvp(rg_plan* plan, const rg_conditions* cond, const double* dlnq_dT, floa
  * static device array of 64 MiB that every GPU loading this library keeps
  * until the process exits; a spectrum that needs more returns RG_ERR_RANGE.
  * Calls no cudaMalloc or cudaFree.  The first call on a device resolves the
- * array's device address, so make it before any stream capture.  Blocking:
- * returns when the spectrum is in out_dev.  Calls share the array and are
- * serialised by a lock; work of two calls overlapping on the GPU (e.g. the
- * same array used from two processes' streams) would race. */
+ * array's device address, so make it before any stream capture.  The array
+ * belongs to this process and device (each process that loads the library
+ * has its own); all calls in the process share it and a lock serialises
+ * them.  Blocking: a call returns only after all the work it enqueued on
+ * `stream` has finished, on success and on error alike, so two calls never
+ * overlap on the GPU through the library.  The array keeps the last call's
+ * contents; a caller who still reads `out_dev` on another stream while the
+ * next call writes it must order the two itself. */
 int rg_synthesize_static(rg_lines* lines, const rg_plan_desc* grid, const rg_conditions* cond,
                          float* out_dev, void* stream, rg_spectrum_info* info);
 

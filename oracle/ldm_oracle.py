@@ -124,14 +124,15 @@ def axis_values(log_min, dx, n):
 
 
 # --- scatter + convolution ------------------------------------------------------
-def ldm_scatter(kpos, log_wG, log_wL, I, n_v, axes, n_rows=None):
+def ldm_scatter(kpos, log_wG, log_wL, I, n_v, axes, n_rows=None, out=None):
     """Distribute line intensities on the (k, l, m) grid with 2x2x2 linear
     weights: indices radis/lbl/broadening.py:2151-2154,2253-2263; simple
     weights :2305-2318; 8x add.at :2478-2485 (misc/arrays.py:472-502).
 
     ``kpos`` is the fractional spectral index (v - vmin)/dv.  ``axes`` =
     (log_wG_min, dxG, N_G, log_wL_min, dxL, N_L).  Returns LDM[n_rows, N_G, N_L]
-    (n_rows defaults to n_v) in FP64."""
+    (n_rows defaults to n_v) in FP64; with ``out`` (an LDM of that shape) the
+    lines are added to it instead."""
     lg0, dxG, NG, ll0, dxL, NL = axes
     n_rows = n_v if n_rows is None else n_rows
     k0 = np.floor(kpos).astype(np.int64)
@@ -151,7 +152,7 @@ def ldm_scatter(kpos, log_wG, log_wL, I, n_v, axes, n_rows=None):
     tG = pl - l0
     tL = pm - m0
     Ik = I[keep]
-    LDM = np.zeros((n_rows, NG, NL))
+    LDM = np.zeros((n_rows, NG, NL)) if out is None else out
     Iv0 = Ik * (1 - tv)
     Iv1 = Ik * tv
     w00 = (1 - tG) * (1 - tL)
@@ -211,19 +212,49 @@ def line_quantities(lines, T, p_bar, x, vmin, dv, Tref=TREF, Qref_Qgas=1.0,
 
 def synthesize(lines, T, p_bar, x, vmin, dv, n_v, axes, n_ft, Tref=TREF,
                Qref_Qgas=1.0, molar_mass=28.0, folding_thresh=1e-6, fft_workers=1,
-               return_ldm=False):
+               return_ldm=False, line_chunk=None):
     """Absorption coefficient (cm-1) on v = vmin + k dv, k < n_v, in FP64.
 
     Follows radis/lbl/factory.py:859-912 (linestrength -> HWHM -> lineshift ->
-    LDM broadening -> x density)."""
-    kpos, lgG, lgL, S = line_quantities(lines, T, p_bar, x, vmin, dv, Tref,
-                                        Qref_Qgas, molar_mass)
-    LDM = ldm_scatter(kpos, lgG, lgL, S, n_v, axes)
+    LDM broadening -> x density).  ``line_chunk``: scale and scatter the lines
+    in blocks of that many (bounds the host memory of very long lists; the
+    LDM is the same sum)."""
+    n = len(lines["v0"])
+    step = n if not line_chunk else int(line_chunk)
+    LDM = None
+    for a in range(0, max(n, 1), max(step, 1)):
+        part = lines if step >= n else {k: (v[a:a + step] if np.ndim(v) == 1 and len(v) == n else v)
+                                        for k, v in lines.items()}
+        kpos, lgG, lgL, S = line_quantities(part, T, p_bar, x, vmin, dv, Tref,
+                                            Qref_Qgas, molar_mass)
+        LDM = ldm_scatter(kpos, lgG, lgL, S, n_v, axes, out=LDM)
     spec = ldm_convolve(LDM, n_v, dv, axes, n_ft, folding_thresh, fft_workers)
     out = spec * number_density(p_bar, T, x)
     if return_ldm:
         return out, LDM * number_density(p_bar, T, x)
     return out
+
+
+def planck_nm(lambda_nm, T):
+    """Blackbody radiance in mW/cm2/sr/nm at wavelength ``lambda_nm`` (nm):
+    radis/phys/blackbody.py:35-74 (SI h, c, k; x 1e-10 from W/sr/m3)."""
+    lbd = np.asarray(lambda_nm, np.float64) * 1e-9
+    return (2 * H_SI * C_SI ** 2 / lbd ** 5) / np.expm1(H_SI * C_SI / (lbd * KB_SI * T)) * 1e-10
+
+
+def quantities(abscoeff, vmin, dv, T, path_length):
+    """The spectral quantities of eq_spectrum_gpu from the absorption
+    coefficient (cm-1) on v = vmin + k dv: absorbance = abscoeff L;
+    emissivity = -expm1(-absorbance); transmittance = 1 - emissivity;
+    radiance = emissivity x Planck(1e7 / v nm, T) in mW/cm2/sr/nm
+    (radis/lbl/factory.py:1284-1297, radis/spectrum/equations.py:21-44)."""
+    a = np.asarray(abscoeff, np.float64)
+    v = vmin + dv * np.arange(a.size)
+    absorbance = a * path_length
+    emissivity = -np.expm1(-absorbance)
+    return {"abscoeff": a, "absorbance": absorbance, "emissivity_noslit": emissivity,
+            "transmittance_noslit": 1.0 - emissivity,
+            "radiance_noslit": emissivity * planck_nm(1e7 / v, T)}
 
 
 def envelope_axes(lines, T, p_bar, x, dxG=None, dxL=None, NG=None, NL=None,
@@ -233,7 +264,9 @@ def envelope_axes(lines, T, p_bar, x, dxG=None, dxL=None, NG=None, NL=None,
     envelopes of log(min|max(g_self, g_air)) + n_air log(Tref/T) + log(2 p);
     log_wG bounds the min/max of log v0 + log_c2Mm + 0.5 log T; the top is
     raised by eps in log space; N = ceil(span/dx)+1, or dx = span/(N-1) when
-    the node count is fixed.  Pressure in atm (see DESIGN divergence 1)."""
+    the node count is fixed.  Pressure enters in atm, as in the CPU path's
+    widths (radis/lbl/broadening.py:1063); the Vulkan path uses bar there
+    (radis/gpu/params.py:144)."""
     p_atm = p_bar / 1.01325
     v0 = np.asarray(lines["v0"], np.float64)
     iso = lines.get("iso")

@@ -47,6 +47,27 @@ struct NvtxRange {
     NvtxRange& operator=(const NvtxRange&) = delete;
 };
 
+// Makes a device current for the life of one C entry point and restores the
+// caller's current device when the entry point returns (a caller working on
+// another device, e.g. a framework's current device, finds it unchanged).
+struct DeviceGuard {
+    int prev = -1;
+    bool changed = false;
+    cudaError_t use(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev == dev) return cudaSuccess;
+        const cudaError_t e = cudaSetDevice(dev);
+        changed = e == cudaSuccess && prev >= 0;
+        return e;
+    }
+    ~DeviceGuard() {
+        if (changed) cudaSetDevice(prev);
+    }
+    DeviceGuard() = default;
+    DeviceGuard(const DeviceGuard&) = delete;
+    DeviceGuard& operator=(const DeviceGuard&) = delete;
+};
+
 static int fail(int code, const char* fmt, ...) {
     char buf[512];
     va_list ap;
@@ -1188,7 +1209,8 @@ int rg_ctx_create(int device, rg_ctx** out) {
     int n = 0;
     CU(cudaGetDeviceCount(&n));
     if (device < 0 || device >= n) return fail(RG_ERR_ARG, "device %d not in [0, %d)", device, n);
-    CU(cudaSetDevice(device));
+    DeviceGuard dev_guard_;
+    CU(dev_guard_.use(device));
     auto* c = new (std::nothrow) rg_ctx();
     if (!c) return fail(RG_ERR_OOM, "host allocation failed");
     c->device = device;
@@ -1217,7 +1239,8 @@ int rg_ctx_destroy(rg_ctx* c) {
     if (!c) return RG_OK;
     if (!valid(c)) return fail(RG_ERR_STATE, "invalid context");
     if (c->lines) return fail(RG_ERR_STATE, "context still has %d line list(s)", c->lines);
-    cudaSetDevice(c->device);
+    DeviceGuard dev_guard_;
+    dev_guard_.use(c->device);
     cudaStreamSynchronize(c->stream);
     cudaStreamDestroy(c->stream);
     cudaMemPool_t pool;   // hand the cached pool memory back
@@ -1235,7 +1258,8 @@ int rg_lines_upload(rg_ctx* ctx, const rg_line_arrays* in, const rg_isotopes* is
     g_err.clear();
     if (!valid(ctx)) return fail(RG_ERR_STATE, "invalid context");
     if (!in || !iso || !out) return fail(RG_ERR_ARG, "NULL argument");
-    CU(cudaSetDevice(ctx->device));
+    DeviceGuard dev_guard_;
+    CU(dev_guard_.use(ctx->device));
     auto* L = new (std::nothrow) rg_lines();
     if (!L) return fail(RG_ERR_OOM, "host allocation failed");
     std::unique_ptr<rg_lines> guard(L);
@@ -1326,7 +1350,8 @@ int rg_lines_free(rg_lines* L) {
     if (!L) return RG_OK;
     if (!valid(L)) return fail(RG_ERR_STATE, "invalid line list");
     if (L->plans.load()) return fail(RG_ERR_STATE, "line list still has %d plan(s) or queued request(s)", L->plans.load());
-    cudaSetDevice(L->ctx->device);
+    DeviceGuard dev_guard_;
+    dev_guard_.use(L->ctx->device);
     cudaStreamSynchronize(L->ctx->stream);
     dfree(L->v0);
     dfree(L->ls2);
@@ -1358,7 +1383,8 @@ int rg_plan_create(rg_lines* L, const rg_plan_desc* d, rg_plan** out) {
     if (d->n_v > (int64_t)1 << 30) return fail(RG_ERR_RANGE, "n_v too large");
     if (!((d->n_G > 1) || d->dxG > 0) || !((d->n_L > 1) || d->dxL > 0))
         return fail(RG_ERR_ARG, "give dxG/dxL > 0 or node counts n_G/n_L > 1");
-    CU(cudaSetDevice(L->ctx->device));
+    DeviceGuard dev_guard_;
+    CU(dev_guard_.use(L->ctx->device));
     auto* P = new (std::nothrow) rg_plan();
     if (!P) return fail(RG_ERR_OOM, "host allocation failed");
     std::unique_ptr<rg_plan> guard(P);
@@ -1427,7 +1453,8 @@ int rg_plan_free(rg_plan* P) {
     if (!valid(P)) return fail(RG_ERR_STATE, "invalid plan");
     {
         std::lock_guard<std::mutex> lk(P->mu);
-        cudaSetDevice(P->lines->ctx->device);
+        DeviceGuard dev_guard_;
+        dev_guard_.use(P->lines->ctx->device);
         cudaStreamSynchronize(P->lines->ctx->stream);
         cudaDeviceSynchronize();
         dfree(P->w.f1.tw);
@@ -1481,7 +1508,8 @@ int rg_synthesize(rg_plan* P, const rg_conditions* c, float* out_dev, void* stre
     g_err.clear();
     if (!valid(P) || !c || !out_dev) return fail(RG_ERR_ARG, "invalid argument");
     std::lock_guard<std::mutex> lk(P->mu);
-    CU(cudaSetDevice(P->lines->ctx->device));
+    DeviceGuard dev_guard_;
+    CU(dev_guard_.use(P->lines->ctx->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
     return run_spectrum(P, c, out_dev, st, timing, false, info);
 }
@@ -1492,7 +1520,8 @@ int rg_synthesize_quantities(rg_plan* P, const rg_conditions* c, double path_len
     if (!valid(P) || !c || !out_dev) return fail(RG_ERR_ARG, "invalid argument");
     if (!(path_length > 0)) return fail(RG_ERR_ARG, "path_length must be positive");
     std::lock_guard<std::mutex> lk(P->mu);
-    CU(cudaSetDevice(P->lines->ctx->device));
+    DeviceGuard dev_guard_;
+    CU(dev_guard_.use(P->lines->ctx->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
     rg_spectrum_info inf;
     RG(run_spectrum(P, c, out_dev, st, 0, false, &inf));
@@ -1561,7 +1590,8 @@ int rg_slit_convolve(rg_ctx* ctx, const float* in_dev, int64_t n, const float* s
     if (mode != RG_SLIT_SAME && mode != RG_SLIT_VALID) return fail(RG_ERR_ARG, "unknown slit mode %d", (int)mode);
     if (!(wstep > 0)) return fail(RG_ERR_ARG, "wstep must be positive");
     if (in_dev < out_dev + n && out_dev < in_dev + n) return fail(RG_ERR_ARG, "out_dev overlaps in_dev");
-    CU(cudaSetDevice(ctx->device));
+    DeviceGuard dev_guard_;
+    CU(dev_guard_.use(ctx->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
     SlitArgs a;
     a.in = in_dev;
@@ -1616,7 +1646,8 @@ int rg_synthesize_host(rg_plan* P, const rg_conditions* c, float* out_host, void
     g_err.clear();
     if (!valid(P) || !c || !out_host) return fail(RG_ERR_ARG, "invalid argument");
     std::lock_guard<std::mutex> lk(P->mu);
-    CU(cudaSetDevice(P->lines->ctx->device));
+    DeviceGuard dev_guard_;
+    CU(dev_guard_.use(P->lines->ctx->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
     RG(run_spectrum(P, c, P->out_d, st, (timing && info) ? 1 : 0, false, info));
     CU(cudaMemcpyAsync(out_host, P->out_d, sizeof(float) * (size_t)P->w.desc.n_v, cudaMemcpyDeviceToHost, st));
@@ -1629,7 +1660,8 @@ int rg_debug_ldm(rg_plan* P, const rg_conditions* c, float* ldm_host, int64_t ca
     g_err.clear();
     if (!valid(P) || !c || !ldm_host) return fail(RG_ERR_ARG, "invalid argument");
     std::lock_guard<std::mutex> lk(P->mu);
-    CU(cudaSetDevice(P->lines->ctx->device));
+    DeviceGuard dev_guard_;
+    CU(dev_guard_.use(P->lines->ctx->device));
     cudaStream_t st = P->lines->ctx->stream;
     rg_spectrum_info tmp;
     rg_spectrum_info* inf = info ? info : &tmp;
@@ -1650,7 +1682,8 @@ int rg_backward(rg_plan* P, const rg_conditions* c, const double* dlnq_dT, const
     g_err.clear();
     if (!valid(P) || !c || !grad_out_dev || !grad) return fail(RG_ERR_ARG, "invalid argument");
     std::lock_guard<std::mutex> lk(P->mu);
-    CU(cudaSetDevice(P->lines->ctx->device));
+    DeviceGuard dev_guard_;
+    CU(dev_guard_.use(P->lines->ctx->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
     SpecHost s;
     RG(compute_grid(P->lines, P->w, c, &s));
@@ -1678,7 +1711,8 @@ int rg_jvp(rg_plan* P, const rg_conditions* c, const double* dlnq_dT, float* out
     g_err.clear();
     if (!valid(P) || !c || !out_dev) return fail(RG_ERR_ARG, "invalid argument");
     std::lock_guard<std::mutex> lk(P->mu);
-    CU(cudaSetDevice(P->lines->ctx->device));
+    DeviceGuard dev_guard_;
+    CU(dev_guard_.use(P->lines->ctx->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
     SpecHost s;
     RG(compute_grid(P->lines, P->w, c, &s));
@@ -2049,7 +2083,8 @@ int rg_server_create(rg_ctx* ctx, int slots, int64_t mem_budget, rg_server** out
     if (!valid(ctx) || !out) return fail(RG_ERR_ARG, "invalid argument");
     if (slots < 1 || slots > 64) return fail(RG_ERR_ARG, "slots must be in [1, 64]");
     if (mem_budget <= 0) return fail(RG_ERR_ARG, "mem_budget must be positive");
-    CU(cudaSetDevice(ctx->device));
+    DeviceGuard dev_guard_;
+    CU(dev_guard_.use(ctx->device));
     auto* S = new (std::nothrow) rg_server();
     if (!S) return fail(RG_ERR_OOM, "host allocation failed");
     std::unique_ptr<rg_server> guard(S);
@@ -2164,7 +2199,8 @@ int rg_server_destroy(rg_server* S) {
     }
     S->ring();
     if (S->worker.joinable()) S->worker.join();
-    cudaSetDevice(S->ctx->device);
+    DeviceGuard dev_guard_;
+    dev_guard_.use(S->ctx->device);
     for (Slot& sl : S->slots) {
         cudaStreamSynchronize(sl.st);
         release_slot_buffers(sl);
@@ -2247,7 +2283,8 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
     const int dev = L->ctx->device;
     if (dev < 0 || dev >= 64) return fail(RG_ERR_ARG, "device ordinal %d not supported", dev);
     std::lock_guard<std::mutex> lk(g_static_mu);
-    CU(cudaSetDevice(dev));
+    DeviceGuard dev_guard_;
+    CU(dev_guard_.use(dev));
     if (!g_static_ptr[dev]) {
         // once per device, with the device current: host code cannot use the
         // array's name as an address, it needs the device address
@@ -2311,6 +2348,17 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
                     off, kStaticScratchBytes);
     W.err_host = &g_static_err_host;
 
+    // From the first enqueue on, every return (an error included) waits for
+    // the work already on `st` before the lock is released, so that the next
+    // call never reuses the scratch while this call's kernels still run.
+    struct DrainOnExit {
+        cudaStream_t st;
+        bool armed = false;
+        ~DrainOnExit() {
+            if (armed) cudaStreamSynchronize(st);
+        }
+    } drain{st};
+    drain.armed = true;
     // every piece starts from what the previous call left: clear what must be zero
     CU(cudaMemsetAsync(W.err, 0, sizeof(unsigned), st));
     RG(static_twiddles(W.f1.tw, n1, n1, 1, st));
@@ -2320,6 +2368,7 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
     RG(launch_col_index(L->v0, L->n, d->vmin, d->dv, -W.E, W.col_count, W.col_start, st));
     RG(launch_col_cmax(W.col_start, W.col_off, W.col_count, (int)d->n_v, W.E, W.cmax_dev, st));
     RG(enqueue_spectrum(L, W, c, s, out_dev, st, nullptr, false));
+    drain.armed = false;
     CU(cudaStreamSynchronize(st));
     if (g_static_err_host) {
         g_static_err_host = 0;

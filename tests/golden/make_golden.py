@@ -1,6 +1,6 @@
 """Generate golden vectors by RUNNING the reference's own code (RADIS 0.17.1).
 
-Run in a container where the reference tree is mounted (default path below, or
+Run in a container where the reference tree is mounted ($RADIS_REFERENCE_ROOT names the radis project root, or
 ``--ref``); the GPU tests never run this script, they only read the committed
 ``golden_ldm.npz``.  The full ``radis`` package cannot be imported here (pandas,
 astropy, numba, hapi are absent), so the few reference functions on the LDM
@@ -35,7 +35,7 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_REF = "/root/reference"
+DEFAULT_REF = os.environ.get("RADIS_REFERENCE_ROOT")  # the radis project root
 
 
 def _extract(path, names, cls=None):
@@ -221,7 +221,8 @@ def synthetic_co(n, seed, lo=2000.0, hi=2010.0):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=DEFAULT_REF)
+    ap.add_argument("--ref", default=DEFAULT_REF, required=DEFAULT_REF is None,
+                    help="radis project root (default: $RADIS_REFERENCE_ROOT)")
     ap.add_argument("--out", default=os.path.join(HERE, "golden_ldm.npz"))
     a = ap.parse_args()
     ns, consts, gpu_params, gpu_structs = build_reference(a.ref)

@@ -1,7 +1,7 @@
 """Generate HITRAN-160 parse golden vectors by RUNNING the reference's own
 parser (RADIS 0.17.1) on synthetic .par files committed beside this script.
 
-Run where the reference tree is mounted (default path below, or ``--ref``);
+Run where the reference tree is mounted ($RADIS_REFERENCE_ROOT names the radis project root, or ``--ref``);
 the tests only read the committed ``hitran_*.par`` files and
 ``golden_hitran.npz``.  The ``radis`` package cannot be imported here
 (pandas, astropy, numba, hapi are absent), so the parse functions are pulled
@@ -39,7 +39,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-DEFAULT_REF = "/root/reference"
+DEFAULT_REF = os.environ.get("RADIS_REFERENCE_ROOT")  # the radis project root
 COLS = {"id": "id", "iso": "iso", "wav": "v0", "int": "S_ref", "A": "A", "airbrd": "g_air",
         "selbrd": "g_self", "El": "El", "Tdpair": "n_air", "Pshft": "delta", "gp": "gp", "gpp": "gpp"}
 
@@ -179,7 +179,8 @@ def parse_with_reference(ns, path, molecule, table="columns_2004"):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=DEFAULT_REF)
+    ap.add_argument("--ref", default=DEFAULT_REF, required=DEFAULT_REF is None,
+                    help="radis project root (default: $RADIS_REFERENCE_ROOT)")
     args = ap.parse_args()
     files = write_fixtures()
     ns = _reference(args.ref)

@@ -1,7 +1,7 @@
 """Generate partition-function golden vectors by RUNNING the reference's own
 tabulators (RADIS 0.17.1).
 
-Run where the reference tree is mounted (default path below, or ``--ref``);
+Run where the reference tree is mounted ($RADIS_REFERENCE_ROOT names the radis project root, or ``--ref``);
 the tests only read the committed ``golden_partition.npz``.  The methods
 are pulled out of their source files with ``ast`` and executed unchanged; the
 CDSD tabulator reads its table with ``pandas.read_csv``, which is absent here,
@@ -25,7 +25,7 @@ import textwrap
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_REF = "/root/reference"
+DEFAULT_REF = os.environ.get("RADIS_REFERENCE_ROOT")  # the radis project root
 
 
 def _methods(path, cls, names):
@@ -70,7 +70,8 @@ def build_class(name, methods, ns):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=DEFAULT_REF)
+    ap.add_argument("--ref", default=DEFAULT_REF, required=DEFAULT_REF is None,
+                    help="radis project root (default: $RADIS_REFERENCE_ROOT)")
     ap.add_argument("--out", default=os.path.join(HERE, "golden_partition.npz"))
     args = ap.parse_args()
     ns = {"np": np, "pd": _PandasStandIn, "OutOfBoundError": OutOfBoundError}

@@ -1,6 +1,6 @@
 """Generate slit golden vectors by RUNNING the reference's own code (RADIS 0.17.1).
 
-Run in a container where the reference tree is mounted (default path below, or
+Run in a container where the reference tree is mounted ($RADIS_REFERENCE_ROOT names the radis project root, or
 ``--ref``); the tests only read the committed ``golden_slit.npz``.  The
 ``radis`` package cannot be imported here (pandas, astropy, numba, hapi are
 absent), so the slit functions are pulled out of their source file with
@@ -24,7 +24,7 @@ import warnings
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_REF = "/root/reference"
+DEFAULT_REF = os.environ.get("RADIS_REFERENCE_ROOT")  # the radis project root
 
 
 def _extract(path, names):
@@ -70,7 +70,8 @@ def spectrum(n, w0, wstep, seed):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=DEFAULT_REF)
+    ap.add_argument("--ref", default=DEFAULT_REF, required=DEFAULT_REF is None,
+                    help="radis project root (default: $RADIS_REFERENCE_ROOT)")
     ap.add_argument("--out", default=os.path.join(HERE, "golden_slit.npz"))
     args = ap.parse_args()
     R = reference_namespace(args.ref)

@@ -1,7 +1,7 @@
 """Generate air-wavelength golden vectors by RUNNING the reference's own
 functions (RADIS 0.17.1): air_index_dispersion, vacuum2air and air2vacuum of
 radis/phys/air.py:16-119, pulled out of the source with ``ast`` and executed
-unchanged.  Run where the reference tree is mounted (default path below, or
+unchanged.  Run where the reference tree is mounted ($RADIS_REFERENCE_ROOT names the radis project root, or
 ``--ref``); the tests only read the committed ``golden_units.npz``."""
 from __future__ import annotations
 
@@ -13,12 +13,13 @@ import warnings
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_REF = "/root/reference"
+DEFAULT_REF = os.environ.get("RADIS_REFERENCE_ROOT")  # the radis project root
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=DEFAULT_REF)
+    ap.add_argument("--ref", default=DEFAULT_REF, required=DEFAULT_REF is None,
+                    help="radis project root (default: $RADIS_REFERENCE_ROOT)")
     args = ap.parse_args()
     src = open(os.path.join(args.ref, "radis", "phys", "air.py")).read()
     ns = {"np": np}

@@ -9,6 +9,11 @@
 * The multi-rank timing reduction of the GPU arm (max over ranks) on two
   gloo ranks.
 * The host-only ingestion mode (--ingest-only) on a small file.
+* The reference arm runs without this library: after a whole run in one
+  process no module of the package is imported and libradisgb.so is not
+  mapped; its config equals the GPU arm's description of the workload.
+* The oracle's node-axis rule (used by the reference arm) equals the
+  library's hull-based grid on the bench workloads' kind of list.
 """
 import json
 import os
@@ -38,6 +43,43 @@ def test_reference_arm_two_ranks():
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}
+    sys.path.insert(0, ROOT)
+    import bench
+    assert d["config"] == bench.workload_desc("co2_5M", 5_000_000, 400001, 28)
+
+
+def test_reference_arm_loads_nothing_of_the_library():
+    code = (
+        "import sys, runpy\n"
+        "sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0']\n"
+        "try:\n"
+        "    runpy.run_path('bench.py', run_name='__main__')\n"
+        "except SystemExit as e:\n"
+        "    assert not e.code, e.code\n"
+        "mods = [m for m in sys.modules if m == 'radis_gb300' or m.startswith('radis_gb300.')]\n"
+        "assert not mods, mods\n"
+        "assert 'libradisgb' not in open('/proc/self/maps').read()\n"
+        "print('REFERENCE_ARM_CLEAN')\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-3000:]
+    assert "REFERENCE_ARM_CLEAN" in r.stdout
+
+
+def test_oracle_axes_equal_library_grid(native_lib):
+    """The reference arm takes its node axes from the oracle's brute-force
+    envelope rule; the GPU arm from the library's hulls: the same axes."""
+    sys.path.insert(0, ROOT)
+    from oracle import ldm_oracle as O
+    from radis_gb300 import _lib as L
+    from radis_gb300 import synthetic as S
+    for lines, M, vmin, dv, n_v, T, p, x, nG, nL in (
+            (S.co2_like(200_000, seed=9), 44.0, 2000.0, 0.001, 400001, 1500.0, 1.0, 0.1, 8, 16),
+            (S.h2o_like(300_000, seed=9), 18.0, 500.0, 0.005, 1500001, 2000.0, 1.0, 0.2, 12, 24)):
+        g = L.grid_estimate(lines, M, vmin, dv, n_v, T, p, x, n_G=nG, n_L=nL)
+        ax = O.envelope_axes(lines, T, p, x, NG=nG, NL=nL, molar_mass=M)
+        assert (ax[2], ax[5]) == (g.n_G, g.n_L)
+        for a, b in zip((ax[0], ax[1], ax[3], ax[4]), (g.log_wG_min, g.dxG, g.log_wL_min, g.dxL)):
+            assert abs(a - b) <= 1e-12 * max(1.0, abs(b))
 
 
 def test_kernels_per_step():

@@ -9,7 +9,10 @@ from radis_gb300 import SpectrumFactory, hitran
 from radis_gb300 import synthetic as S
 from radis_gb300.spectrum import Spectrum, derived_quantities, planck_nm
 
-REF_FIXTURE = "/root/reference/radis/test/files/hitran_co_3iso_2000_2300cm.par"
+# The reference's own HITRAN fixture, read where the reference tree is available:
+# RADIS_REFERENCE_ROOT names the radis project root (the test is skipped without it).
+_REF_ROOT = os.environ.get("RADIS_REFERENCE_ROOT", "")
+REF_FIXTURE = os.path.join(_REF_ROOT, "radis", "test", "files", "hitran_co_3iso_2000_2300cm.par") if _REF_ROOT else ""
 
 
 def test_hitran_roundtrip_idempotent(tmp_path):
@@ -26,7 +29,8 @@ def test_hitran_roundtrip_idempotent(tmp_path):
     np.testing.assert_allclose(r1["n_air"], lines["n_air"], atol=5e-3)
 
 
-@pytest.mark.skipif(not os.path.exists(REF_FIXTURE), reason="reference tree not mounted")
+@pytest.mark.skipif(not REF_FIXTURE or not os.path.exists(REF_FIXTURE),
+                    reason="RADIS_REFERENCE_ROOT unset or the reference tree is absent")
 def test_hitran_reads_reference_fixture():
     d = hitran.read_hitran160(REF_FIXTURE)
     assert len(d["v0"]) == 573

@@ -8,7 +8,10 @@ buffer taken from one static 64 MiB device array.  This test calls that entry
 point twice in a row (different conditions, so the second call must not be
 fooled by what the first left in the shared array) and checks both spectra
 against the plan-based entry point within the parity tolerance, 1e-4 of the
-peak absorption coefficient.  A spectrum too large for the array must be
+peak absorption coefficient.  One more call runs on a stream the caller
+created, and the device's free memory must be the same before and after the
+calls (after one warm-up call has resolved the array's address), which is the
+entry point's whole contract.  A spectrum too large for the array must be
 refused with RG_ERR_RANGE.
 """
 import numpy as np
@@ -29,16 +32,27 @@ def test_static_scratch_matches_plan(native_lib):
     grid = dict(dxG=S.DXG_DEFAULT, dxL=S.DXL_DEFAULT)
     plan = L.Plan(lines, vmin, dv, n_v, **grid)
     out = torch.empty(n_v, dtype=torch.float32, device="cuda")   # caller-owned output
-    for T, p, x in ((700.0, 1.0, 0.1), (1800.0, 3.0, 0.5)):
-        ref, ref_info = plan.synthesize_host(T, p, x)
+    caller_stream = torch.cuda.Stream()
+    conds = ((700.0, 1.0, 0.1), (1800.0, 3.0, 0.5), (1200.0, 0.5, 0.3))
+    refs = [plan.synthesize_host(T, p, x) for T, p, x in conds]
+    # warm-up: resolves the array's device address and loads the kernels
+    L.synthesize_static(lines, vmin, dv, n_v, *conds[0], out.data_ptr(), **grid)
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    got = []
+    for i, (T, p, x) in enumerate(conds):
         out.fill_(-1.0)
         torch.cuda.synchronize()
-        info = L.synthesize_static(lines, vmin, dv, n_v, T, p, x, out.data_ptr(), **grid)
-        got = out.cpu().numpy()
+        sptr = caller_stream.cuda_stream if i == 2 else None
+        info = L.synthesize_static(lines, vmin, dv, n_v, T, p, x, out.data_ptr(), stream_ptr=sptr, **grid)
+        got.append((out.cpu().numpy(), info))
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
+    for (g, info), (ref, ref_info) in zip(got, refs):
         assert (info.grid.n_G, info.grid.n_L, info.grid.n_ft) == \
             (ref_info.grid.n_G, ref_info.grid.n_L, ref_info.grid.n_ft)
         assert info.log_scale == ref_info.log_scale
-        assert np.max(np.abs(got - ref)) <= TOL * np.max(np.abs(ref))
+        assert np.max(np.abs(g - ref)) <= TOL * np.max(np.abs(ref))
     big = torch.empty(2_000_001, dtype=torch.float32, device="cuda")
     with pytest.raises(L.RgError) as e:
         L.synthesize_static(lines, 2000.0, 0.001, 2_000_001, 700.0, 1.0, 0.1, big.data_ptr(),
