@@ -678,6 +678,7 @@ def run_c3(ctx, L, h2o_host, h2o, K, peak, peak_kind, workers, check=True):
                              "lines_read": int(info.lines_in_window)},
         "fft_layout": {"fft_rows": int(info.fft_rows), "merged_rows": int(info.merged_rows),
                        "n_ft": int(g.n_ft)},
+        "scatter_accumulator_bits": int(info.accum_bits),
     }
     if check:
         import numpy as np
@@ -817,6 +818,7 @@ def run_ours(args):
                          "traffic": traffic, "algorithmic_bytes_per_launch": ab[name],
                          "avg_launch_ms": kt[name]},
             "stages": stages,
+            "scatter_accumulator_bits": int(info.accum_bits),
             "fft_layout": {"fft_rows": int(info.fft_rows), "merged_rows": int(info.merged_rows),
                            "gauss_halfwidth": int(info.merged_ext), "n_ft": int(g.n_ft),
                            "note": ("k_col_fft_fwd covers the real-space Gaussian stage of the merged "

@@ -52,7 +52,7 @@
 extern "C" {
 #endif
 
-#define RG_ABI_VERSION 1
+#define RG_ABI_VERSION 2
 
 enum rg_status {
     RG_OK = 0,
@@ -105,6 +105,10 @@ typedef struct {
     int n_G, n_L;
     double folding_thresh;     /* <= 0 -> 1e-6 (factory.py:437)              */
     int64_t n_ft;              /* 0 -> smallest supported length >= 2 n_v     */
+    /* fixed-point width of the scatter's accumulator: 0 = chosen from the
+     * densest grid column (32 bits up to 8192 lines per column, else 64),
+     * 32 or 64 = forced */
+    int32_t accumulator;
 } rg_plan_desc;
 
 /* Gas conditions of one spectrum.  Pressure in bar (as the reference API);
@@ -137,6 +141,9 @@ typedef struct {
     int32_t fft_rows, merged_rows, merged_ext;
     float gauss_ms;            /* merged layout: the real-space Gaussian stage's
                                   part of stage_ms[1] (timing = 1), else 0     */
+    int32_t accum_bits;        /* the scatter's accumulator: 32 or 64 bits, or
+                                  0 when it was chosen on the device (served
+                                  and allocation-free spectra in auto mode)    */
 } rg_spectrum_info;
 
 int rg_abi_version(void);

@@ -58,7 +58,7 @@ class Isotopes(C.Structure):
 class PlanDesc(C.Structure):
     _fields_ = [("vmin", C.c_double), ("dv", C.c_double), ("n_v", C.c_int64),
                 ("dxG", C.c_double), ("dxL", C.c_double), ("n_G", C.c_int), ("n_L", C.c_int),
-                ("folding_thresh", C.c_double), ("n_ft", C.c_int64)]
+                ("folding_thresh", C.c_double), ("n_ft", C.c_int64), ("accumulator", C.c_int32)]
 
 
 class Conditions(C.Structure):
@@ -79,7 +79,7 @@ class Grid(C.Structure):
 class SpectrumInfo(C.Structure):
     _fields_ = [("grid", Grid), ("log_scale", C.c_double), ("stage_ms", C.c_float * 6),
                 ("lines_in_window", C.c_int64), ("fft_rows", C.c_int32), ("merged_rows", C.c_int32),
-                ("merged_ext", C.c_int32), ("gauss_ms", C.c_float)]
+                ("merged_ext", C.c_int32), ("gauss_ms", C.c_float), ("accum_bits", C.c_int32)]
 
 
 class Request(C.Structure):
@@ -327,11 +327,13 @@ class Plan:
     """Spectral grid + workspace over one line list (rg_plan)."""
 
     def __init__(self, lines: Lines, vmin: float, dv: float, n_v: int, dxG=None, dxL=None,
-                 n_G=None, n_L=None, folding_thresh: float = 1e-6, n_ft: int = 0):
+                 n_G=None, n_L=None, folding_thresh: float = 1e-6, n_ft: int = 0, accumulator: int = 0):
+        """``accumulator``: fixed-point width of the scatter (0: from the
+        densest grid column, 32 or 64: forced)."""
         lib = load()
         self.lines = lines
         d = PlanDesc(float(vmin), float(dv), int(n_v), float(dxG or 0.0), float(dxL or 0.0),
-                     int(n_G or 0), int(n_L or 0), float(folding_thresh), int(n_ft))
+                     int(n_G or 0), int(n_L or 0), float(folding_thresh), int(n_ft), int(accumulator))
         h = C.c_void_p()
         check(lib.rg_plan_create(lines.handle, C.byref(d), C.byref(h)))
         self._h = h
@@ -495,7 +497,7 @@ def grid_estimate(lines: dict, molar_mass, vmin, dv, n_v, T, p_bar, x, dxG=None,
         iso_s.molar_mass[i] = float(m)
     iso_s.t_ref = float(t_ref)
     d = PlanDesc(float(vmin), float(dv), int(n_v), float(dxG or 0.0), float(dxL or 0.0),
-                 int(n_G or 0), int(n_L or 0), 1e-6, int(n_ft))
+                 int(n_G or 0), int(n_L or 0), 1e-6, int(n_ft), 0)
     q = None if q_ratio is None else np.ascontiguousarray(
         np.broadcast_to(np.asarray(q_ratio, np.float64), (len(mm),)))
     c = Conditions(float(T), float(p_bar), float(x), ptr(q))
@@ -525,14 +527,14 @@ class Server:
         return self._h
 
     def submit(self, lines: Lines, vmin, dv, n_v, T, p_bar, x, dxG=None, dxL=None, n_G=None,
-               n_L=None, q_ratio=None, out=None, folding_thresh=1e-6) -> int:
+               n_L=None, q_ratio=None, out=None, folding_thresh=1e-6, accumulator=0) -> int:
         if out is None:
             out = np.empty(int(n_v), dtype=np.float32)
         q = None if q_ratio is None else np.ascontiguousarray(
             np.broadcast_to(np.asarray(q_ratio, np.float64), (lines.n_iso,)))
         req = Request(lines.handle.value,
                       PlanDesc(float(vmin), float(dv), int(n_v), float(dxG or 0.0), float(dxL or 0.0),
-                               int(n_G or 0), int(n_L or 0), float(folding_thresh), 0),
+                               int(n_G or 0), int(n_L or 0), float(folding_thresh), 0, int(accumulator)),
                       Conditions(float(T), float(p_bar), float(x), ptr(q)), out.ctypes.data)
         t = C.c_int64()
         check(load().rg_server_submit(self.handle, C.byref(req), C.byref(t)))
@@ -570,13 +572,13 @@ class Server:
 
 def synthesize_static(lines: Lines, vmin, dv, n_v, T, p_bar, x, out_dev_ptr: int, dxG=None, dxL=None,
                       n_G=None, n_L=None, q_ratio=None, stream_ptr: int | None = None,
-                      folding_thresh=1e-6) -> SpectrumInfo:
+                      folding_thresh=1e-6, accumulator=0) -> SpectrumInfo:
     """Allocation-free spectrum (rg_synthesize_static): every scratch buffer
     comes from the library's static 64 MiB device array, so nothing is
     allocated on the device during the call.  ``out_dev_ptr``: caller-owned
     device buffer of n_v floats.  Blocking."""
     d = PlanDesc(float(vmin), float(dv), int(n_v), float(dxG or 0.0), float(dxL or 0.0),
-                 int(n_G or 0), int(n_L or 0), float(folding_thresh), 0)
+                 int(n_G or 0), int(n_L or 0), float(folding_thresh), 0, int(accumulator))
     q = None if q_ratio is None else np.ascontiguousarray(
         np.broadcast_to(np.asarray(q_ratio, np.float64), (lines.n_iso,)))
     c = Conditions(float(T), float(p_bar), float(x), ptr(q))

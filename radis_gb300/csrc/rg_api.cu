@@ -164,6 +164,7 @@ struct Work {
     float* mrow = nullptr;
     size_t mrow_bytes = 0;
     int last_fft_rows = 0, last_merged_rows = 0, last_ext = 0;   // layout of the last spectrum
+    int last_accum = 0;               // accumulator bits of the last scatter (0: chosen on the device)
     int64_t row_stride = 0;
     float* ldm = nullptr;             // LDM [node][row_stride] (the scatter's float values)
     float2* y = nullptr;
@@ -573,19 +574,20 @@ int ensure_workspace(Work& W, int n_nodes, cudaStream_t st) {
 // columns); with wide node grids the tile narrows and two 2048-line chunks
 // per stage ring win (H2O 100M, 12x24 nodes: 1.35 ms vs 1.45 ms); smaller
 // chunks only when even those do not fit.
-int scatter_shape(int n_nodes, int* chunk, int* TK, int* stages, size_t* smem) {
+int scatter_shape(int n_nodes, bool wide, int* chunk, int* TK, int* stages, size_t* smem) {
     size_t avail = 0;
-    RG(scatter_smem_optin(&avail));
+    RG(scatter_smem_optin(&avail, wide));
+    const size_t word = wide ? 8 : 4;   // bytes per tile cell
     auto tile_cols = [&](int S, int ch) {   // widest tile next to the ring (rows of tk + 1 words)
         const size_t fixed = scatter_fixed_smem(ch, S);
         if (fixed >= avail) return 0;
-        return std::min(1024, ((int)((avail - fixed) / (4 * (size_t)n_nodes)) - 1) / 32 * 32);
+        return std::min(1024, ((int)((avail - fixed) / (word * (size_t)n_nodes)) - 1) / 32 * 32);
     };
     auto take = [&](int S, int ch, int tk) {
         *chunk = ch;
         *TK = tk;
         *stages = S;
-        *smem = scatter_fixed_smem(ch, S) + (size_t)4 * n_nodes * (tk + 1);
+        *smem = scatter_fixed_smem(ch, S) + word * n_nodes * (tk + 1);
         return RG_OK;
     };
     // GB300 sweeps (CO2 5M / 128 nodes, H2O 100M / 288 nodes): one line per
@@ -599,7 +601,7 @@ int scatter_shape(int n_nodes, int* chunk, int* TK, int* stages, size_t* smem) {
     return fail(RG_ERR_RANGE, "LDM grid of %d nodes does not fit a shared-memory tile", n_nodes);
 }
 
-int build_scatter_args(const rg_lines* L, const Work& W, const rg_conditions* c, const SpecHost& s,
+int build_scatter_args(const rg_lines* L, const Work& W, const rg_conditions* c, const SpecHost& s, bool wide,
                        ScatterArgs* a) {
     const rg_grid& g = s.grid;
     std::memset(a, 0, sizeof *a);
@@ -621,7 +623,7 @@ int build_scatter_args(const rg_lines* L, const Work& W, const rg_conditions* c,
     a->row_stride = W.row_stride;
     a->ldm = W.ldm;
     size_t smem_unused;
-    RG(scatter_shape(s.n_nodes, &a->chunk, &a->TK, &a->stages, &smem_unused));
+    RG(scatter_shape(s.n_nodes, wide, &a->chunk, &a->TK, &a->stages, &smem_unused));
     a->n_tiles = (int)((W.desc.n_v + a->TK - 1) / a->TK);
     a->cmax = W.cmax_dev;
     a->err = W.err;
@@ -850,21 +852,39 @@ int take_err(Work& W) {
 // Enqueue one spectrum on `st` into W's buffers: scatter, the four FFT/Voigt
 // stages (unless ldm_only), and the publication of the device error flag.
 // ev: 6 events recorded between stages (nullable).
-int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const SpecHost& s, float* out,
-                     cudaStream_t st, cudaEvent_t* ev, bool ldm_only) {
-    RG(ensure_workspace(W, s.n_nodes, st));
+// Launch the scatter with the 32- or 64-bit accumulator; check = 1: the
+// kernel compares the device-side column bound with the limit itself.
+int launch_scatter_acc(const rg_lines* L, const Work& W, const rg_conditions* c, const SpecHost& s, bool wide,
+                       int check, cudaStream_t st) {
     ScatterArgs sa;
-    RG(build_scatter_args(L, W, c, s, &sa));
-    const int n_v = (int)W.desc.n_v;
+    RG(build_scatter_args(L, W, c, s, wide, &sa));
+    sa.acc_check = check;
     int ch_unused, tk_unused, st_unused;
     size_t smem;
-    RG(scatter_shape(s.n_nodes, &ch_unused, &tk_unused, &st_unused, &smem));
+    RG(scatter_shape(s.n_nodes, wide, &ch_unused, &tk_unused, &st_unused, &smem));
     const int sms = L->ctx->sms;
     const int grid = std::max(std::min(sa.n_tiles, sms),
                               (sa.n_tiles + kScatMaxTilesPerCta - 1) / kScatMaxTilesPerCta);
+    return launch_scatter(sa, grid, kScatThreads, smem, wide, st);
+}
+
+int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const SpecHost& s, float* out,
+                     cudaStream_t st, cudaEvent_t* ev, bool ldm_only) {
+    RG(ensure_workspace(W, s.n_nodes, st));
+    const int n_v = (int)W.desc.n_v;
     if (ev) CU(cudaEventRecord(ev[0], st));
     if (W.count_lines) CU(cudaMemsetAsync(W.counter, 0, sizeof(unsigned long long), st));
-    RG(launch_scatter(sa, grid, kScatThreads, smem, st));
+    // accumulator width: forced, or from the densest column when the host knows
+    // it (plans); otherwise both variants are launched and the device decides
+    if (W.desc.accumulator || W.cmax_host >= 0) {
+        const bool wide = W.desc.accumulator ? W.desc.accumulator == 64 : fx_wide((int)W.cmax_host);
+        RG(launch_scatter_acc(L, W, c, s, wide, 0, st));
+        W.last_accum = wide ? 64 : 32;
+    } else {
+        RG(launch_scatter_acc(L, W, c, s, false, 1, st));
+        RG(launch_scatter_acc(L, W, c, s, true, 1, st));
+        W.last_accum = 0;
+    }
     if (ev) CU(cudaEventRecord(ev[1], st));
     if (!ldm_only) {
         ColFftArgs ca;
@@ -963,7 +983,7 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
 int fill_grad_args(const rg_lines* L, const Work& W, const rg_conditions* c, const SpecHost& s,
                    const double* dlnq_dT, GradArgs* g) {
     std::memset(g, 0, sizeof *g);
-    RG(build_scatter_args(L, W, c, s, &g->s));
+    RG(build_scatter_args(L, W, c, s, false, &g->s));
     if (!(c->x > 0)) return fail(RG_ERR_ARG, "derivatives need a mole fraction x > 0");
     const double T = c->T, p = c->p_bar;
     g->n_lines = L->n;
@@ -1140,6 +1160,7 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
         info->fft_rows = ldm_only ? 0 : P->w.last_fft_rows;
         info->merged_rows = ldm_only ? 0 : P->w.last_merged_rows;
         info->merged_ext = ldm_only ? 0 : P->w.last_ext;
+        info->accum_bits = P->w.last_accum;
     }
     if (timing == 1 && info) {
         CU(cudaStreamSynchronize(st));
@@ -1383,6 +1404,8 @@ int rg_plan_create(rg_lines* L, const rg_plan_desc* d, rg_plan** out) {
     if (d->n_v > (int64_t)1 << 30) return fail(RG_ERR_RANGE, "n_v too large");
     if (!((d->n_G > 1) || d->dxG > 0) || !((d->n_L > 1) || d->dxL > 0))
         return fail(RG_ERR_ARG, "give dxG/dxL > 0 or node counts n_G/n_L > 1");
+    if (d->accumulator != 0 && d->accumulator != 32 && d->accumulator != 64)
+        return fail(RG_ERR_ARG, "accumulator must be 0, 32 or 64 (got %d)", (int)d->accumulator);
     DeviceGuard dev_guard_;
     CU(dev_guard_.use(L->ctx->device));
     auto* P = new (std::nothrow) rg_plan();
@@ -1412,7 +1435,7 @@ int rg_plan_create(rg_lines* L, const rg_plan_desc* d, rg_plan** out) {
     CU(cudaMalloc(&W.col_start, sizeof(int64_t) * W.col_count));
     RG(launch_col_index(L->v0, L->n, d->vmin, d->dv, -W.E, W.col_count, W.col_start, st));
     CU(cudaMalloc(&W.cmax_dev, sizeof(int)));
-    RG(launch_col_cmax(W.col_start, W.col_off, W.col_count, (int)d->n_v, W.E, W.cmax_dev, st));
+    RG(launch_col_cmax(W.col_start, W.col_off, W.col_count, (int)d->n_v, W.E - 1, W.cmax_dev, st));
     W.row_stride = (d->n_v + 31) / 32 * 32;
     CU(cudaMalloc(&W.g, sizeof(float2) * (size_t)W.n));
     CU(cudaMalloc(&P->out_d, sizeof(float) * (size_t)d->n_v));
@@ -1930,7 +1953,7 @@ int start_on_slot(rg_server* S, int si, const std::shared_ptr<ServerReq>& r, con
     }
     const rg_lines* L = r->lines;
     RG(launch_col_index(L->v0, L->n, d.vmin, d.dv, -W.E, W.col_count, W.col_start, sl.st));
-    RG(launch_col_cmax(W.col_start, W.col_off, W.col_count, (int)d.n_v, W.E, W.cmax_dev, sl.st));
+    RG(launch_col_cmax(W.col_start, W.col_off, W.col_count, (int)d.n_v, W.E - 1, W.cmax_dev, sl.st));
     RG(enqueue_spectrum(L, W, &r->cond, sh, sl.out_d, sl.st, nullptr, false));
     CU(cudaMemcpyAsync(sl.pin, sl.out_d, sizeof(float) * (size_t)d.n_v, cudaMemcpyDeviceToHost, sl.st));
     r->info.grid = sh.grid;
@@ -1939,6 +1962,7 @@ int start_on_slot(rg_server* S, int si, const std::shared_ptr<ServerReq>& r, con
     r->info.fft_rows = W.last_fft_rows;
     r->info.merged_rows = W.last_merged_rows;
     r->info.merged_ext = W.last_ext;
+    r->info.accum_bits = W.last_accum;
     sl.notified.store(false);
     auto* hn = new HostNote{S, si};
     CU(cudaLaunchHostFunc(sl.st, slot_done_cb, hn));
@@ -2127,6 +2151,8 @@ int rg_server_submit(rg_server* S, const rg_request* req, int64_t* ticket) {
     if (!(d.dv > 0) || d.n_v < 2 || d.n_v > ((int64_t)1 << 30)) return fail(RG_ERR_ARG, "bad grid");
     if (!((d.n_G > 1) || d.dxG > 0) || !((d.n_L > 1) || d.dxL > 0))
         return fail(RG_ERR_ARG, "give dxG/dxL > 0 or node counts n_G/n_L > 1");
+    if (d.accumulator != 0 && d.accumulator != 32 && d.accumulator != 64)
+        return fail(RG_ERR_ARG, "accumulator must be 0, 32 or 64 (got %d)", (int)d.accumulator);
     auto r = std::make_shared<ServerReq>();
     r->lines = req->lines;
     r->desc = d;
@@ -2280,6 +2306,8 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
     if (!(d->dv > 0) || d->n_v < 2 || d->n_v > ((int64_t)1 << 30)) return fail(RG_ERR_ARG, "bad grid");
     if (!((d->n_G > 1) || d->dxG > 0) || !((d->n_L > 1) || d->dxL > 0))
         return fail(RG_ERR_ARG, "give dxG/dxL > 0 or node counts n_G/n_L > 1");
+    if (d->accumulator != 0 && d->accumulator != 32 && d->accumulator != 64)
+        return fail(RG_ERR_ARG, "accumulator must be 0, 32 or 64 (got %d)", (int)d->accumulator);
     const int dev = L->ctx->device;
     if (dev < 0 || dev >= 64) return fail(RG_ERR_ARG, "device ordinal %d not supported", dev);
     std::lock_guard<std::mutex> lk(g_static_mu);
@@ -2366,7 +2394,7 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
     RG(static_twiddles(twh, nh, W.n, 1024, st));
     RG(static_twiddles(twl, 1024, W.n, 1, st));
     RG(launch_col_index(L->v0, L->n, d->vmin, d->dv, -W.E, W.col_count, W.col_start, st));
-    RG(launch_col_cmax(W.col_start, W.col_off, W.col_count, (int)d->n_v, W.E, W.cmax_dev, st));
+    RG(launch_col_cmax(W.col_start, W.col_off, W.col_count, (int)d->n_v, W.E - 1, W.cmax_dev, st));
     RG(enqueue_spectrum(L, W, c, s, out_dev, st, nullptr, false));
     drain.armed = false;
     CU(cudaStreamSynchronize(st));
@@ -2380,6 +2408,7 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
         info->log_scale = s.log_scale_out;
         info->lines_in_window = -1;
         info->fft_rows = W.last_fft_rows;
+        info->accum_bits = W.last_accum;
     }
     return RG_OK;
 }

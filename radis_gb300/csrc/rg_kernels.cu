@@ -470,9 +470,24 @@ __device__ __forceinline__ float line_intensity(const ScatterArgs& a, float v0, 
     return ex2(arg) * (1.f - ex2(-a.stim_c * v0));
 }
 
+// Fixed-point words of the tile accumulator: 32 bits (one native shared
+// integer atomic per add) or 64 bits for dense columns (see fx_wide).
+template <typename Acc> struct Fx;
+template <> struct Fx<unsigned> {
+    static constexpr int kWidth = 31;
+    __device__ static unsigned to_fx(float v) { return __float2uint_rn(v); }
+    __device__ static float to_float(unsigned w) { return __uint2float_rn(w); }
+};
+template <> struct Fx<unsigned long long> {
+    static constexpr int kWidth = 63;
+    __device__ static unsigned long long to_fx(float v) { return __float2ull_rn(v); }
+    __device__ static float to_float(unsigned long long w) { return __ull2float_rn(w); }
+};
+
 // Scale + scatter of the lines of one staged chunk into the tile accumulator.
+template <typename Acc>
 __device__ __forceinline__ unsigned scatter_chunk(const ScatterArgs& a, const Stage& st, int count, int k_start,
-                                                  int tk, unsigned* tile, float fxs, int t0, int nt) {
+                                                  int tk, Acc* tile, float fxs, int t0, int nt) {
     unsigned counted = 0;
     for (int j = t0; j < count; j += nt) {
         const float2 v = st.v0[j];
@@ -499,18 +514,18 @@ __device__ __forceinline__ unsigned scatter_chunk(const ScatterArgs& a, const St
         const float w00 = 1.f - tG - w01;    // (1 - tG)(1 - tL)
         const int pitch = a.TK + 1;
         const int dL = a.NL * pitch;                          // next wG node
-        unsigned* t = tile + (l0 * a.NL + m0) * pitch + c0;   // (l0, m0) at column c0
+        Acc* t = tile + (l0 * a.NL + m0) * pitch + c0;   // (l0, m0) at column c0
         if (own0) {
-            atomicAdd(t, __float2uint_rn(I0 * w00));
-            atomicAdd(t + pitch, __float2uint_rn(I0 * w01));
-            atomicAdd(t + dL, __float2uint_rn(I0 * w10));
-            atomicAdd(t + dL + pitch, __float2uint_rn(I0 * w11));
+            atomicAdd(t, Fx<Acc>::to_fx(I0 * w00));
+            atomicAdd(t + pitch, Fx<Acc>::to_fx(I0 * w01));
+            atomicAdd(t + dL, Fx<Acc>::to_fx(I0 * w10));
+            atomicAdd(t + dL + pitch, Fx<Acc>::to_fx(I0 * w11));
         }
         if (own1) {
-            atomicAdd(t + 1, __float2uint_rn(I1 * w00));
-            atomicAdd(t + 1 + pitch, __float2uint_rn(I1 * w01));
-            atomicAdd(t + 1 + dL, __float2uint_rn(I1 * w10));
-            atomicAdd(t + 1 + dL + pitch, __float2uint_rn(I1 * w11));
+            atomicAdd(t + 1, Fx<Acc>::to_fx(I1 * w00));
+            atomicAdd(t + 1 + pitch, Fx<Acc>::to_fx(I1 * w01));
+            atomicAdd(t + 1 + dL, Fx<Acc>::to_fx(I1 * w10));
+            atomicAdd(t + 1 + dL + pitch, Fx<Acc>::to_fx(I1 * w11));
         }
     }
     return counted;
@@ -526,8 +541,12 @@ __device__ __forceinline__ unsigned scatter_chunk(const ScatterArgs& a, const St
 // buffer; warps meet only at tile boundaries (a named barrier of the consumer
 // warps) to flush the finished tile to HBM with plain stores.  Every wait is
 // bounded; a wait that gives up sets the error flag and the CTA stops after
-// the copies it issued have landed (bounded).
+// the copies it issued have landed (bounded).  Acc: the 32- or 64-bit
+// fixed-point word of the tile; with a.acc_check both variants are launched
+// and the one whose width *cmax does not call for returns before any work.
+template <typename Acc>
 __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a) {
+    if (a.acc_check && fx_wide(*a.cmax) != (sizeof(Acc) == 8)) return;
     extern __shared__ __align__(128) unsigned char smem[];
     const int ch = a.chunk;
     const int S = a.stages;
@@ -535,7 +554,7 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * sb);
     uint64_t* empty = full + kScatMaxStages;
     int2* rng = reinterpret_cast<int2*>(smem + S * sb + 16 * kScatMaxStages);
-    unsigned* tile = reinterpret_cast<unsigned*>(smem + scatter_fixed_smem(ch, S));
+    Acc* tile = reinterpret_cast<Acc*>(smem + scatter_fixed_smem(ch, S));
     const int pitch = a.TK + 1;
     const int G = gridDim.x;
     const int nq = (a.n_tiles - (int)blockIdx.x + G - 1) / G;   // tiles of this CTA (<= kScatMaxTilesPerCta)
@@ -551,7 +570,7 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
         const int hi = (int)a.col_start[col_idx(k_start + tk + a.margin_cols)];
         rng[q] = make_int2(lo / kLinePad * kLinePad, hi);   // 16-line aligned start
     }
-    for (int i = threadIdx.x; i < n_words; i += blockDim.x) tile[i] = 0u;
+    for (int i = threadIdx.x; i < n_words; i += blockDim.x) tile[i] = 0;
     if (threadIdx.x == 0) {
         for (int b = 0; b < S; ++b) {
             mbar_init(&full[b], 1);
@@ -588,7 +607,7 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
     }
 
     // consumers
-    const float fxs = fx_scale_of(*a.cmax);
+    const float fxs = fx_scale_of(*a.cmax, Fx<Acc>::kWidth);
     const float inv_fx = 1.f / fxs;
     const bool has_dl = a.dl != nullptr, has_iso = a.iso != nullptr;
     const int ct = threadIdx.x - 32, nct = blockDim.x - 32;
@@ -608,8 +627,8 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
                 bad = true;
                 break;
             }
-            counted += scatter_chunk(a, stage_view(smem + buf * sb, ch, has_dl, has_iso), min(ch, b - cs), k_start,
-                                     tk, tile, fxs, ct, nct);
+            counted += scatter_chunk<Acc>(a, stage_view(smem + buf * sb, ch, has_dl, has_iso), min(ch, b - cs),
+                                          k_start, tk, tile, fxs, ct, nct);
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[buf]);   // this warp is done with the buffer
             if (++buf == S) {
@@ -633,11 +652,11 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
         // exact scaling of the rounded word), with plain stores (this CTA owns
         // its columns), and re-zero it
         for (int node = cw; node < a.n_nodes; node += n_cons_warps) {
-            unsigned* row = tile + node * pitch;
+            Acc* row = tile + node * pitch;
             float* dst = a.ldm + node * a.row_stride + k_start;
             for (int c = lane; c < tk; c += 32) {   // one 128-byte store per warp step
-                dst[c] = __uint2float_rn(row[c]) * inv_fx;
-                row[c] = 0u;
+                dst[c] = Fx<Acc>::to_float(row[c]) * inv_fx;
+                row[c] = 0;
             }
         }
         asm volatile("bar.sync 1, %0;" ::"r"(nct) : "memory");
@@ -1679,14 +1698,20 @@ int launch_col_cmax(const int64_t* col_start, int col_off, int col_count, int n_
     return check_launch();
 }
 
-int launch_scatter(const ScatterArgs& a, int grid, int threads, size_t smem, cudaStream_t st) {
-    ALLOW_SMEM(k_scatter, smem);
-    k_scatter<<<grid, threads, smem, st>>>(a);
+int launch_scatter(const ScatterArgs& a, int grid, int threads, size_t smem, bool wide, cudaStream_t st) {
+    if (wide) {
+        ALLOW_SMEM(k_scatter<unsigned long long>, smem);
+        k_scatter<unsigned long long><<<grid, threads, smem, st>>>(a);
+    } else {
+        ALLOW_SMEM(k_scatter<unsigned>, smem);
+        k_scatter<unsigned><<<grid, threads, smem, st>>>(a);
+    }
     return check_launch();
 }
 
-// Dynamic shared memory the scatter may have (one CTA per SM).
-int scatter_smem_optin(size_t* avail) {
+// Dynamic shared memory a scatter variant may have (one CTA per SM).
+template <typename Acc>
+static int scatter_optin(size_t* avail) {
     static std::atomic<size_t> cached{0};   // one GPU model per process
     size_t a = cached.load();
     if (!a) {
@@ -1695,12 +1720,15 @@ int scatter_smem_optin(size_t* avail) {
         if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
             return RG_ERR_CUDA;
         cudaFuncAttributes fa;
-        if (cudaFuncGetAttributes(&fa, k_scatter) != cudaSuccess) return RG_ERR_CUDA;
+        if (cudaFuncGetAttributes(&fa, k_scatter<Acc>) != cudaSuccess) return RG_ERR_CUDA;
         a = (size_t)optin - fa.sharedSizeBytes;
         cached.store(a);
     }
     *avail = a;
     return RG_OK;
+}
+int scatter_smem_optin(size_t* avail, bool wide) {
+    return wide ? scatter_optin<unsigned long long>(avail) : scatter_optin<unsigned>(avail);
 }
 
 template <int N1>

@@ -292,3 +292,73 @@ def test_long_rows(ctx, n_v):
     gpu, info = run_gpu(ctx, lines, *args, n_G=4, n_L=8)
     assert info.grid.n2 in (3200, 4800, 8000)
     assert rel_err(gpu, oracle(lines, *args, info)) <= TOL
+
+
+def dense_forest(n_weak, n_strong, seed):
+    """A dense forest of weak lines (S_ref log-uniform 1e-27..1e-25) over
+    2000-2002 cm-1 with a few strong lines (1e-20) inside it: at 0.01 cm-1 the
+    10M-line list puts 50 000 lines in every grid column."""
+    rng = np.random.default_rng(seed)
+    n = n_weak + n_strong
+    v0 = np.concatenate([rng.uniform(2000.0, 2001.98, n_weak), rng.uniform(2000.5, 2001.5, n_strong)])
+    s = np.concatenate([10.0 ** rng.uniform(-27.0, -25.0, n_weak), np.full(n_strong, 1e-20)])
+    order = np.argsort(v0, kind="stable")
+    return dict(v0=v0[order], S_ref=s[order],
+                El=np.minimum(rng.exponential(3000.0, n), 20000.0).astype(np.float32)[order],
+                g_air=rng.uniform(0.03, 0.08, n).astype(np.float32)[order],
+                g_self=rng.uniform(0.05, 0.1, n).astype(np.float32)[order],
+                n_air=rng.uniform(0.5, 0.8, n).astype(np.float32)[order])
+
+
+@pytest.mark.timeout(900, method="thread")
+def test_dense_columns_wide_accumulator(ctx):
+    """10^4+ lines per grid column: 10M lines in 2 cm-1 at 0.01 cm-1.  The
+    32-bit fixed-point scatter rounds every add to 2^-e of the strongest
+    line with 2^e ~ 2^31 / (lines per column); past 8192 lines per column
+    the plan switches to the 64-bit accumulator and reports it.  The plan
+    (host-side choice), a served request and the allocation-free entry point
+    (both choosing on the device) match the FP64 oracle; the forced 32-bit
+    accumulator is shown to be the coarser one on this list."""
+    lines = dense_forest(10_000_000, 20, seed=71)
+    M, vmin, dv, n_v, T, p, x = 28.0, 2000.0, 0.01, 201, 1000.0, 1.0, 0.1
+    grid = dict(n_G=8, n_L=16)
+    ln = L.Lines(ctx, lines, M)
+    plan = L.Plan(ln, vmin, dv, n_v, **grid)
+    out, info = plan.synthesize_host(T, p, x)
+    assert info.accum_bits == 64
+    gpu = out.astype(np.float64) * np.exp(info.log_scale)
+    ref = O.synthesize(lines, T, p, x, vmin, dv, n_v, info.grid.axes(), info.grid.n_ft, molar_mass=M,
+                       fft_workers=WORKERS, line_chunk=2_000_000)
+    err64 = rel_err(gpu, ref)
+    assert err64 <= 1e-5, err64
+    plan32 = L.Plan(ln, vmin, dv, n_v, accumulator=32, **grid)
+    o32, i32 = plan32.synthesize_host(T, p, x)
+    assert i32.accum_bits == 32
+    err32 = rel_err(o32.astype(np.float64) * np.exp(i32.log_scale), ref)
+    assert err32 > 5 * err64, (err32, err64)
+    plan32.close()
+    # device-side choice: a served request and the allocation-free path
+    srv = L.Server(ctx, slots=2, mem_budget=4 << 30)
+    t = srv.submit(ln, vmin, dv, n_v, T, p, x, **grid)
+    o_s, i_s, _ = srv.wait(t)
+    srv.close()
+    assert i_s.accum_bits == 0
+    assert rel_err(o_s.astype(np.float64) * np.exp(i_s.log_scale), ref) <= 1e-5
+    torch = pytest.importorskip("torch")
+    dev = torch.empty(n_v, dtype=torch.float32, device="cuda")
+    i_st = L.synthesize_static(ln, vmin, dv, n_v, T, p, x, dev.data_ptr(), **grid)
+    torch.cuda.synchronize()
+    assert rel_err(dev.cpu().numpy().astype(np.float64) * np.exp(i_st.log_scale), ref) <= 1e-5
+    plan.close()
+    ln.close()
+
+
+def test_sparse_list_keeps_32_bit_accumulator(ctx):
+    """The CO-like 10k list (a few lines per column) stays on 32 bits."""
+    lines = S.co_like()
+    ln = L.Lines(ctx, lines, 28.0)
+    plan = L.Plan(ln, 1900.0, 0.002, 200001, dxG=S.DXG_DEFAULT, dxL=S.DXL_DEFAULT)
+    _, info = plan.synthesize_host(700.0, 1.01325, 0.1)
+    assert info.accum_bits == 32
+    plan.close()
+    ln.close()
