@@ -109,6 +109,13 @@ typedef struct {
      * densest grid column (32 bits up to 8192 lines per column, else 64),
      * 32 or 64 = forced */
     int32_t accumulator;
+    /* Gaussian node axis: 0 = from every line of the list (the reference's
+     * rule over the lines it was given, radis/gpu/params.py:70-81); 1 = from
+     * the lines that can reach the window (v0 within the window widened by the
+     * largest pressure shift) -- what the reference computes when its factory
+     * loads only the window's lines, and far fewer nodes for a narrow window
+     * of a wide list */
+    int32_t axes_window;
 } rg_plan_desc;
 
 /* Gas conditions of one spectrum.  Pressure in bar (as the reference API);
@@ -204,13 +211,19 @@ int rg_hitran_parse(const char* text, int64_t nbytes, int32_t threads, const rg_
 int rg_synthesize(rg_plan* plan, const rg_conditions* cond, float* out_dev, void* stream,
                   int timing, rg_spectrum_info* info);
 
-/* As rg_synthesize, plus the post-processing epilogue of eq_spectrum_gpu on
- * the device (radis/lbl/factory.py:1284-1297): out_dev holds 5 rows of n_v
- * floats: abscoeff and absorbance (x exp(-info.log_scale), path length in
- * cm), then emissivity, transmittance and radiance (mW/cm2/sr/nm, Planck at
- * cond->T) in physical units.  Asynchronous on `stream`. */
+/* As rg_synthesize, plus the post-processing of eq_spectrum_gpu
+ * (radis/lbl/factory.py:1284-1297) fused into the spectrum's last kernel:
+ * out_dev holds 5 rows of n_v floats: abscoeff and absorbance
+ * (x exp(-info.log_scale), path length in cm), then emissivity = -expm1(-A L),
+ * transmittance = 1 - emissivity and radiance (mW/cm2/sr/nm, emissivity x
+ * Planck at cond->T) in physical units.  Asynchronous on `stream`. */
 int rg_synthesize_quantities(rg_plan* plan, const rg_conditions* cond, double path_length, float* out_dev,
                              void* stream, rg_spectrum_info* info);
+/* The same into host memory (5 n_v floats, pinned or pageable), blocking:
+ * the drop-in form of gpuApp.iterate + the host post-processing of
+ * eq_spectrum_gpu (factory.py:1247-1297).  timing = 1 fills info->stage_ms. */
+int rg_synthesize_quantities_host(rg_plan* plan, const rg_conditions* cond, double path_length,
+                                  float* out_host, void* stream, int timing, rg_spectrum_info* info);
 
 /* Tabulated partition function Q(T) of isotopologue `iso` (0-based, < the
  * list's n_iso), copied from n points (T strictly increasing, Q > 0):
@@ -246,6 +259,17 @@ int rg_partition_eval(int64_t n, const double* T, const double* Q, int32_t inter
 #define RG_SLIT_VALID 1
 int rg_slit_convolve(rg_ctx* ctx, const float* in_dev, int64_t n, const float* slit_dev, int32_t n_slit,
                      double wstep, int32_t mode, float* out_dev, void* stream);
+
+/* Test hook of the failure path, no counterpart in the reference (whose
+ * analogue is the bounded fence wait of
+ * radis/gpu/vulkan/vulkan_compute_lib.py:898).  withhold != 0: the scatter's
+ * producer issues no line copies in the plan's following spectra, so every
+ * consumer's wait for its first chunk runs out; the kernels finish, the
+ * spectrum call returns RG_ERR_TIMEOUT and the plan stays usable.
+ * wait_cycles: bound of the scatter's producer/consumer handshake waits in SM
+ * clock cycles (0 = the default, about one second; at most the default).  The
+ * wait for copies already in flight always keeps the default bound. */
+int rg_plan_test_scatter_stall(rg_plan* plan, int32_t withhold, int64_t wait_cycles);
 
 /* Sums (ms) of the stage times recorded with timing = 2 since the last call:
  * scatter, fft-col, fft-row+voigt, ifft-row, ifft-col, total; *count =

@@ -24,8 +24,9 @@ EXPORTS = [
     "rg_lines_free", "rg_lines_count", "rg_plan_create", "rg_plan_free", "rg_plan_grid", "rg_grid_estimate",
     "rg_synthesize", "rg_synthesize_host", "rg_debug_ldm", "rg_plan_stage_times",
     "rg_server_create", "rg_server_submit", "rg_server_wait", "rg_server_stats_get", "rg_server_destroy",
-    "rg_synthesize_static", "rg_backward", "rg_jvp", "rg_synthesize_quantities", "rg_slit_convolve",
-    "rg_lines_set_partition", "rg_partition_eval", "rg_plan_stage_times_gauss",
+    "rg_synthesize_static", "rg_backward", "rg_jvp", "rg_synthesize_quantities",
+    "rg_synthesize_quantities_host", "rg_slit_convolve",
+    "rg_lines_set_partition", "rg_partition_eval", "rg_plan_stage_times_gauss", "rg_plan_test_scatter_stall",
     "rg_hitran_count", "rg_hitran_parse",
 ]
 
@@ -58,7 +59,8 @@ class Isotopes(C.Structure):
 class PlanDesc(C.Structure):
     _fields_ = [("vmin", C.c_double), ("dv", C.c_double), ("n_v", C.c_int64),
                 ("dxG", C.c_double), ("dxL", C.c_double), ("n_G", C.c_int), ("n_L", C.c_int),
-                ("folding_thresh", C.c_double), ("n_ft", C.c_int64), ("accumulator", C.c_int32)]
+                ("folding_thresh", C.c_double), ("n_ft", C.c_int64), ("accumulator", C.c_int32),
+                ("axes_window", C.c_int32)]
 
 
 class Conditions(C.Structure):
@@ -128,6 +130,7 @@ def load(path: str | None = None):
                                C.c_int),
         "rg_plan_stage_times": ([vp, C.POINTER(C.c_double), C.POINTER(i64)], C.c_int),
         "rg_plan_stage_times_gauss": ([vp, C.POINTER(C.c_double)], C.c_int),
+        "rg_plan_test_scatter_stall": ([vp, C.c_int32, i64], C.c_int),
         "rg_debug_ldm": ([vp, C.POINTER(Conditions), vp, i64, C.POINTER(SpectrumInfo)], C.c_int),
         "rg_server_create": ([vp, C.c_int, i64, C.POINTER(vp)], C.c_int),
         "rg_server_submit": ([vp, C.POINTER(Request), C.POINTER(i64)], C.c_int),
@@ -142,6 +145,8 @@ def load(path: str | None = None):
         "rg_jvp": ([vp, C.POINTER(Conditions), vp, vp, vp, C.POINTER(SpectrumInfo)], C.c_int),
         "rg_synthesize_quantities": ([vp, C.POINTER(Conditions), C.c_double, vp, vp, C.POINTER(SpectrumInfo)],
                                      C.c_int),
+        "rg_synthesize_quantities_host": ([vp, C.POINTER(Conditions), C.c_double, vp, vp, C.c_int,
+                                           C.POINTER(SpectrumInfo)], C.c_int),
         "rg_slit_convolve": ([vp, vp, i64, vp, C.c_int32, C.c_double, C.c_int32, vp, vp], C.c_int),
         "rg_lines_set_partition": ([vp, C.c_int32, i64, vp, vp, C.c_int32], C.c_int),
         "rg_partition_eval": ([i64, vp, vp, C.c_int32, C.c_double, C.POINTER(C.c_double),
@@ -327,13 +332,17 @@ class Plan:
     """Spectral grid + workspace over one line list (rg_plan)."""
 
     def __init__(self, lines: Lines, vmin: float, dv: float, n_v: int, dxG=None, dxL=None,
-                 n_G=None, n_L=None, folding_thresh: float = 1e-6, n_ft: int = 0, accumulator: int = 0):
+                 n_G=None, n_L=None, folding_thresh: float = 1e-6, n_ft: int = 0, accumulator: int = 0,
+                 axes_window: bool = False):
         """``accumulator``: fixed-point width of the scatter (0: from the
-        densest grid column, 32 or 64: forced)."""
+        densest grid column, 32 or 64: forced).  ``axes_window``: the Gaussian
+        node axis spans only the lines that can reach the window (instead of
+        the whole list)."""
         lib = load()
         self.lines = lines
         d = PlanDesc(float(vmin), float(dv), int(n_v), float(dxG or 0.0), float(dxL or 0.0),
-                     int(n_G or 0), int(n_L or 0), float(folding_thresh), int(n_ft), int(accumulator))
+                     int(n_G or 0), int(n_L or 0), float(folding_thresh), int(n_ft), int(accumulator),
+                     1 if axes_window else 0)
         h = C.c_void_p()
         check(lib.rg_plan_create(lines.handle, C.byref(d), C.byref(h)))
         self._h = h
@@ -422,6 +431,27 @@ class Plan:
                                               C.c_void_p(stream_ptr) if stream_ptr else None, C.byref(info)))
         return info
 
+    QUANTITIES = ("abscoeff", "absorbance", "emissivity_noslit", "transmittance_noslit", "radiance_noslit")
+
+    def synthesize_quantities_host(self, T, p_bar, x, path_length, q_ratio=None, timing=False):
+        """Blocking: ({quantity: float32 array n_v}, SpectrumInfo) with the
+        post-processing fused into the spectrum's last kernel.  abscoeff and
+        absorbance are in units of exp(info.log_scale); emissivity,
+        transmittance and radiance (mW/cm2/sr/nm) in physical units."""
+        c, _q = self._cond(T, p_bar, x, q_ratio)
+        out = np.empty(5 * self.n_v, dtype=np.float32)
+        info = SpectrumInfo()
+        check(load().rg_synthesize_quantities_host(self.handle, C.byref(c), float(path_length), ptr(out), None,
+                                                   1 if timing else 0, C.byref(info)))
+        rows = out.reshape(5, self.n_v)
+        return {k: rows[i] for i, k in enumerate(self.QUANTITIES)}, info
+
+    def test_scatter_stall(self, withhold: bool, wait_cycles: int = 0):
+        """Test hook (rg_plan_test_scatter_stall): with ``withhold`` the next
+        spectra's scatter receives no line copies and its bounded waits run
+        out (RG_ERR_TIMEOUT); ``wait_cycles`` bounds those waits (0: default)."""
+        check(load().rg_plan_test_scatter_stall(self.handle, 1 if withhold else 0, int(wait_cycles)))
+
     def gauss_time(self):
         """Gaussian-stage part (ms, summed) of the fft-col sum that the last
         ``stage_times`` call returned (merged layout; 0 otherwise)."""
@@ -487,7 +517,7 @@ def _line_arrays(lines: dict):
 
 
 def grid_estimate(lines: dict, molar_mass, vmin, dv, n_v, T, p_bar, x, dxG=None, dxL=None,
-                  n_G=None, n_L=None, t_ref=296.0, q_ratio=None, n_ft=0) -> Grid:
+                  n_G=None, n_L=None, t_ref=296.0, q_ratio=None, n_ft=0, axes_window=False) -> Grid:
     """Host-only (no GPU): the LDM grid a plan would use (rg_grid_estimate)."""
     la, keep = _line_arrays(lines)
     mm = np.atleast_1d(np.asarray(molar_mass, dtype=np.float64))
@@ -497,7 +527,7 @@ def grid_estimate(lines: dict, molar_mass, vmin, dv, n_v, T, p_bar, x, dxG=None,
         iso_s.molar_mass[i] = float(m)
     iso_s.t_ref = float(t_ref)
     d = PlanDesc(float(vmin), float(dv), int(n_v), float(dxG or 0.0), float(dxL or 0.0),
-                 int(n_G or 0), int(n_L or 0), 1e-6, int(n_ft), 0)
+                 int(n_G or 0), int(n_L or 0), 1e-6, int(n_ft), 0, 1 if axes_window else 0)
     q = None if q_ratio is None else np.ascontiguousarray(
         np.broadcast_to(np.asarray(q_ratio, np.float64), (len(mm),)))
     c = Conditions(float(T), float(p_bar), float(x), ptr(q))
@@ -527,14 +557,15 @@ class Server:
         return self._h
 
     def submit(self, lines: Lines, vmin, dv, n_v, T, p_bar, x, dxG=None, dxL=None, n_G=None,
-               n_L=None, q_ratio=None, out=None, folding_thresh=1e-6, accumulator=0) -> int:
+               n_L=None, q_ratio=None, out=None, folding_thresh=1e-6, accumulator=0, axes_window=False) -> int:
         if out is None:
             out = np.empty(int(n_v), dtype=np.float32)
         q = None if q_ratio is None else np.ascontiguousarray(
             np.broadcast_to(np.asarray(q_ratio, np.float64), (lines.n_iso,)))
         req = Request(lines.handle.value,
                       PlanDesc(float(vmin), float(dv), int(n_v), float(dxG or 0.0), float(dxL or 0.0),
-                               int(n_G or 0), int(n_L or 0), float(folding_thresh), 0, int(accumulator)),
+                               int(n_G or 0), int(n_L or 0), float(folding_thresh), 0, int(accumulator),
+                               1 if axes_window else 0),
                       Conditions(float(T), float(p_bar), float(x), ptr(q)), out.ctypes.data)
         t = C.c_int64()
         check(load().rg_server_submit(self.handle, C.byref(req), C.byref(t)))
@@ -572,13 +603,14 @@ class Server:
 
 def synthesize_static(lines: Lines, vmin, dv, n_v, T, p_bar, x, out_dev_ptr: int, dxG=None, dxL=None,
                       n_G=None, n_L=None, q_ratio=None, stream_ptr: int | None = None,
-                      folding_thresh=1e-6, accumulator=0) -> SpectrumInfo:
+                      folding_thresh=1e-6, accumulator=0, axes_window=False) -> SpectrumInfo:
     """Allocation-free spectrum (rg_synthesize_static): every scratch buffer
     comes from the library's static 64 MiB device array, so nothing is
     allocated on the device during the call.  ``out_dev_ptr``: caller-owned
     device buffer of n_v floats.  Blocking."""
     d = PlanDesc(float(vmin), float(dv), int(n_v), float(dxG or 0.0), float(dxL or 0.0),
-                 int(n_G or 0), int(n_L or 0), float(folding_thresh), 0, int(accumulator))
+                 int(n_G or 0), int(n_L or 0), float(folding_thresh), 0, int(accumulator),
+                 1 if axes_window else 0)
     q = None if q_ratio is None else np.ascontiguousarray(
         np.broadcast_to(np.asarray(q_ratio, np.float64), (lines.n_iso,)))
     c = Conditions(float(T), float(p_bar), float(x), ptr(q))

@@ -174,6 +174,14 @@ struct Work {
     unsigned* err_host = nullptr;     // pinned copy of err, refreshed after every spectrum
     unsigned* err_pub = nullptr;      // device view of err_host when it is mapped (the last kernel writes it)
     bool count_lines = false;         // count the lines in the window (timing = 1 reports it)
+    // post-processing rows written by the last kernel (rg_synthesize_quantities):
+    // 4 rows of n_v floats, or null; path length (cm) and gas temperature (K)
+    float* quant_out = nullptr;
+    double quant_path = 0.0, quant_T = 0.0;
+    // bound of the scatter's handshake waits (cycles) and the test hook that
+    // withholds its line copies (rg_plan_test_scatter_stall)
+    long long scat_wait = kScatWaitCycles;
+    int scat_withhold = 0;
 };
 
 struct rg_plan {
@@ -183,6 +191,7 @@ struct rg_plan {
     float2* tw_hi_own = nullptr;
     float2* tw_lo_own = nullptr;
     float* out_d = nullptr;
+    float* quant_d = nullptr;           // 5 rows of n_v (rg_synthesize_quantities_host), on first use
     double* grad_d = nullptr;           // 3 sums of the adjoint gather, allocated on first use
     // stage events: start, after scatter, fft-col, fft-row, ifft-row, ifft-col,
     // and [6] after the Gaussian stage inside fft-col (at [1] without it)
@@ -280,7 +289,10 @@ bool radices(int L, int* rad, int* np) {
 
 constexpr int kN2Max = 256 * 32;   // row FFT limit (threads x register accumulators)
 
-// choose n = n1 * n2 >= n_min, n1 a power of two <= 512, n2 = 32 * (5-smooth)
+// choose n = n1 * n2 >= n_min, n1 a power of two <= 512, n2 = 32 * (5-smooth).
+// The row kernel runs n1 x (pair groups) CTAs, so n1 = 8 (a handful of long
+// rows) is taken only when its length is at least a quarter shorter than the
+// best with n1 = 512 or 64, or when neither fits.
 bool choose_fft(int64_t n_min, int64_t forced, int* n1o, int* n2o) {
     int64_t best = std::numeric_limits<int64_t>::max();
     int b1 = 0, b2 = 0;
@@ -302,6 +314,7 @@ bool choose_fft(int64_t n_min, int64_t forced, int* n1o, int* n2o) {
         int64_t n = (int64_t)n1 * n2;
         if (n < n_min) continue;
         // prefer the shorter transform, then the larger n1 (fewer row FFT launches)
+        if (n1 == 8 && !forced && b1 && 4 * n > 3 * best) continue;
         if (n < best) {
             best = n;
             b1 = n1;
@@ -366,12 +379,24 @@ int compute_grid_env(const Envelope& E, const rg_lines* lines, const rg_plan_des
     const double eps = 1e-4;   // params.py:89,107
     const double T = c->T;
     s->p_atm = c->p_bar / kAtm;
-    // Gaussian axis: min/max of log v0 + log_c2Mm + 0.5 log T  (params.py:70-81,107-117)
+    // Gaussian axis: min/max of log v0 + log_c2Mm + 0.5 log T  (params.py:70-81,107-117),
+    // over the list, or (axes_window) over the lines whose shifted centre can
+    // fall inside the window: v0 in [vmin - s, vmax + s], s = max |shift| + dv
     double lg_lo = std::numeric_limits<double>::infinity(), lg_hi = -lg_lo;
-    for (int i = 0; i < L->n_iso; ++i) {
-        if (!(L->lv_min[i] <= L->lv_max[i])) continue;
-        lg_lo = std::min(lg_lo, L->lv_min[i] + L->log_c2Mm[i]);
-        lg_hi = std::max(lg_hi, L->lv_max[i] + L->log_c2Mm[i]);
+    for (int pass = d.axes_window ? 0 : 1; pass < 2 && !(lg_lo <= lg_hi); ++pass) {
+        double wlo = -std::numeric_limits<double>::infinity(), whi = -wlo;
+        if (pass == 0) {   // the window's reach; an empty reach falls back to the list
+            const double sh = L->max_abs_delta * s->p_atm + d.dv;
+            const double vlo = d.vmin - sh, vhi = d.vmin + (double)(d.n_v - 1) * d.dv + sh;
+            if (vlo > 0) wlo = std::log(vlo);
+            whi = vhi > 0 ? std::log(vhi) : -std::numeric_limits<double>::infinity();
+        }
+        for (int i = 0; i < L->n_iso; ++i) {
+            const double lo = std::max(L->lv_min[i], wlo), hi = std::min(L->lv_max[i], whi);
+            if (!(lo <= hi)) continue;
+            lg_lo = std::min(lg_lo, lo + L->log_c2Mm[i]);
+            lg_hi = std::max(lg_hi, hi + L->log_c2Mm[i]);
+        }
     }
     lg_lo += 0.5 * std::log(T);
     lg_hi += 0.5 * std::log(T) + eps;
@@ -660,6 +685,8 @@ int build_scatter_args(const rg_lines* L, const Work& W, const rg_conditions* c,
     }
     a->stim_c = (float)(kC2 / T * kLog2e);
     a->in_window = W.count_lines ? W.counter : nullptr;
+    a->wait_limit = W.scat_wait;
+    a->withhold = W.scat_withhold;
     return RG_OK;
 }
 
@@ -852,20 +879,17 @@ int take_err(Work& W) {
 // Enqueue one spectrum on `st` into W's buffers: scatter, the four FFT/Voigt
 // stages (unless ldm_only), and the publication of the device error flag.
 // ev: 6 events recorded between stages (nullable).
-// Launch the scatter with the 32- or 64-bit accumulator; check = 1: the
-// kernel compares the device-side column bound with the limit itself.
-int launch_scatter_acc(const rg_lines* L, const Work& W, const rg_conditions* c, const SpecHost& s, bool wide,
-                       int check, cudaStream_t st) {
-    ScatterArgs sa;
-    RG(build_scatter_args(L, W, c, s, wide, &sa));
-    sa.acc_check = check;
+// Shape of the scatter with the 32- or 64-bit accumulator: arguments, grid
+// (one persistent CTA per SM, more only past kScatMaxTilesPerCta tiles each)
+// and dynamic shared memory.
+int scatter_launch_shape(const rg_lines* L, const Work& W, const rg_conditions* c, const SpecHost& s, bool wide,
+                         ScatterArgs* sa, int* grid, size_t* smem) {
+    RG(build_scatter_args(L, W, c, s, wide, sa));
     int ch_unused, tk_unused, st_unused;
-    size_t smem;
-    RG(scatter_shape(s.n_nodes, wide, &ch_unused, &tk_unused, &st_unused, &smem));
+    RG(scatter_shape(s.n_nodes, wide, &ch_unused, &tk_unused, &st_unused, smem));
     const int sms = L->ctx->sms;
-    const int grid = std::max(std::min(sa.n_tiles, sms),
-                              (sa.n_tiles + kScatMaxTilesPerCta - 1) / kScatMaxTilesPerCta);
-    return launch_scatter(sa, grid, kScatThreads, smem, wide, st);
+    *grid = std::max(std::min(sa->n_tiles, sms), (sa->n_tiles + kScatMaxTilesPerCta - 1) / kScatMaxTilesPerCta);
+    return RG_OK;
 }
 
 int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const SpecHost& s, float* out,
@@ -878,11 +902,19 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
     // it (plans); otherwise both variants are launched and the device decides
     if (W.desc.accumulator || W.cmax_host >= 0) {
         const bool wide = W.desc.accumulator ? W.desc.accumulator == 64 : fx_wide((int)W.cmax_host);
-        RG(launch_scatter_acc(L, W, c, s, wide, 0, st));
+        ScatterArgs sa;
+        int grid;
+        size_t smem;
+        RG(scatter_launch_shape(L, W, c, s, wide, &sa, &grid, &smem));
+        RG(launch_scatter(sa, grid, kScatThreads, smem, wide, st));
         W.last_accum = wide ? 64 : 32;
     } else {
-        RG(launch_scatter_acc(L, W, c, s, false, 1, st));
-        RG(launch_scatter_acc(L, W, c, s, true, 1, st));
+        ScatterArgs a32, a64;
+        int g32, g64;
+        size_t m32, m64;
+        RG(scatter_launch_shape(L, W, c, s, false, &a32, &g32, &m32));
+        RG(scatter_launch_shape(L, W, c, s, true, &a64, &g64, &m64));
+        RG(launch_scatter_auto(a32, a64, std::max(g32, g64), kScatThreads, std::max(m32, m64), st));
         W.last_accum = 0;
     }
     if (ev) CU(cudaEventRecord(ev[1], st));
@@ -968,6 +1000,14 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
         ca.out_scale = (float)(std::exp(s.log_scale_int - s.log_scale_out) / ((double)W.n * W.desc.dv));
         ca.err = W.err;
         ca.err_pub = W.err_pub;   // mapped: the kernel publishes and clears the flag
+        if (W.quant_out) {        // fused post-processing of eq_spectrum_gpu
+            ca.q_out = W.quant_out;
+            ca.q_scale = (float)std::exp(s.log_scale_out);
+            ca.q_path = (float)W.quant_path;
+            ca.q_c2_T = (float)(kC2 / W.quant_T);
+            ca.q_vmin = W.desc.vmin;
+            ca.q_dv = W.desc.dv;
+        }
         RG(launch_col_ifft(ca, st));
         if (ev) CU(cudaEventRecord(ev[5], st));
         if (W.err_pub) return RG_OK;
@@ -1406,6 +1446,8 @@ int rg_plan_create(rg_lines* L, const rg_plan_desc* d, rg_plan** out) {
         return fail(RG_ERR_ARG, "give dxG/dxL > 0 or node counts n_G/n_L > 1");
     if (d->accumulator != 0 && d->accumulator != 32 && d->accumulator != 64)
         return fail(RG_ERR_ARG, "accumulator must be 0, 32 or 64 (got %d)", (int)d->accumulator);
+    if (d->axes_window != 0 && d->axes_window != 1)
+        return fail(RG_ERR_ARG, "axes_window must be 0 or 1 (got %d)", (int)d->axes_window);
     DeviceGuard dev_guard_;
     CU(dev_guard_.use(L->ctx->device));
     auto* P = new (std::nothrow) rg_plan();
@@ -1486,6 +1528,7 @@ int rg_plan_free(rg_plan* P) {
         dfree(P->tw_lo_own);
         free_work(P->w);
         dfree(P->out_d);
+        dfree(P->quant_d);
         dfree(P->grad_d);
         for (auto& e : P->ev)
             if (e) cudaEventDestroy(e);
@@ -1537,6 +1580,22 @@ int rg_synthesize(rg_plan* P, const rg_conditions* c, float* out_dev, void* stre
     return run_spectrum(P, c, out_dev, st, timing, false, info);
 }
 
+namespace {
+// One spectrum with the post-processing rows written by its last kernel into
+// out_dev + n_v (4 rows); the epilogue request is cleared on every return.
+int run_quantities(rg_plan* P, const rg_conditions* c, double path_length, float* out_dev, cudaStream_t st,
+                   int timing, rg_spectrum_info* info) {
+    struct Clear {
+        Work& w;
+        ~Clear() { w.quant_out = nullptr; }
+    } clear_{P->w};
+    P->w.quant_out = out_dev + P->w.desc.n_v;
+    P->w.quant_path = path_length;
+    P->w.quant_T = c->T;
+    return run_spectrum(P, c, out_dev, st, timing, false, info);
+}
+}  // namespace
+
 int rg_synthesize_quantities(rg_plan* P, const rg_conditions* c, double path_length, float* out_dev, void* stream,
                              rg_spectrum_info* info) {
     g_err.clear();
@@ -1547,21 +1606,26 @@ int rg_synthesize_quantities(rg_plan* P, const rg_conditions* c, double path_len
     CU(dev_guard_.use(P->lines->ctx->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
     rg_spectrum_info inf;
-    RG(run_spectrum(P, c, out_dev, st, 0, false, &inf));
-    QuantArgs q;
-    q.abscoeff = out_dev;
-    q.out = out_dev + P->w.desc.n_v;
-    q.n_v = (int)P->w.desc.n_v;
-    q.vmin = P->w.desc.vmin;
-    q.dv = P->w.desc.dv;
-    q.scale = (float)std::exp(inf.log_scale);
-    q.path_length = (float)path_length;
-    q.c2_T = (float)(kC2 / c->T);
-    RG(plan_stream_begin(P, st));
-    RG(launch_quantities(q, st));
-    RG(plan_stream_end(P, st));
+    RG(run_quantities(P, c, path_length, out_dev, st, 0, &inf));
     if (info) *info = inf;
     return RG_OK;
+}
+
+int rg_synthesize_quantities_host(rg_plan* P, const rg_conditions* c, double path_length, float* out_host,
+                                  void* stream, int timing, rg_spectrum_info* info) {
+    g_err.clear();
+    if (!valid(P) || !c || !out_host) return fail(RG_ERR_ARG, "invalid argument");
+    if (!(path_length > 0)) return fail(RG_ERR_ARG, "path_length must be positive");
+    std::lock_guard<std::mutex> lk(P->mu);
+    DeviceGuard dev_guard_;
+    CU(dev_guard_.use(P->lines->ctx->device));
+    cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
+    const size_t n5 = 5 * (size_t)P->w.desc.n_v;
+    if (!P->quant_d) CU(cudaMalloc((void**)&P->quant_d, sizeof(float) * n5));
+    RG(run_quantities(P, c, path_length, P->quant_d, st, (timing && info) ? 1 : 0, info));
+    CU(cudaMemcpyAsync(out_host, P->quant_d, sizeof(float) * n5, cudaMemcpyDeviceToHost, st));
+    CU(cudaStreamSynchronize(st));
+    return take_err(P->w);
 }
 
 int rg_lines_set_partition(rg_lines* L, int32_t iso, int64_t n, const double* T, const double* Q, int32_t interp) {
@@ -1625,6 +1689,17 @@ int rg_slit_convolve(rg_ctx* ctx, const float* in_dev, int64_t n, const float* s
     a.scale = (float)wstep;
     a.valid = mode == RG_SLIT_VALID;
     RG(launch_slit_conv(a, st));
+    return RG_OK;
+}
+
+int rg_plan_test_scatter_stall(rg_plan* P, int32_t withhold, int64_t wait_cycles) {
+    g_err.clear();
+    if (!valid(P)) return fail(RG_ERR_ARG, "invalid plan");
+    if (wait_cycles < 0 || wait_cycles > kScatWaitCycles)
+        return fail(RG_ERR_ARG, "wait_cycles must be in [0, %lld]", (long long)kScatWaitCycles);
+    std::lock_guard<std::mutex> lk(P->mu);
+    P->w.scat_withhold = withhold ? 1 : 0;
+    P->w.scat_wait = wait_cycles ? wait_cycles : kScatWaitCycles;
     return RG_OK;
 }
 
@@ -2153,6 +2228,8 @@ int rg_server_submit(rg_server* S, const rg_request* req, int64_t* ticket) {
         return fail(RG_ERR_ARG, "give dxG/dxL > 0 or node counts n_G/n_L > 1");
     if (d.accumulator != 0 && d.accumulator != 32 && d.accumulator != 64)
         return fail(RG_ERR_ARG, "accumulator must be 0, 32 or 64 (got %d)", (int)d.accumulator);
+    if (d.axes_window != 0 && d.axes_window != 1)
+        return fail(RG_ERR_ARG, "axes_window must be 0 or 1 (got %d)", (int)d.axes_window);
     auto r = std::make_shared<ServerReq>();
     r->lines = req->lines;
     r->desc = d;
@@ -2308,6 +2385,8 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
         return fail(RG_ERR_ARG, "give dxG/dxL > 0 or node counts n_G/n_L > 1");
     if (d->accumulator != 0 && d->accumulator != 32 && d->accumulator != 64)
         return fail(RG_ERR_ARG, "accumulator must be 0, 32 or 64 (got %d)", (int)d->accumulator);
+    if (d->axes_window != 0 && d->axes_window != 1)
+        return fail(RG_ERR_ARG, "axes_window must be 0 or 1 (got %d)", (int)d->axes_window);
     const int dev = L->ctx->device;
     if (dev < 0 || dev >= 64) return fail(RG_ERR_ARG, "device ordinal %d not supported", dev);
     std::lock_guard<std::mutex> lk(g_static_mu);

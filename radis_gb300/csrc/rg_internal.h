@@ -138,9 +138,11 @@ struct ScatterArgs {
     int chunk;                // lines per staged chunk (multiple of 16)
     int stages;               // chunk buffers in the TMA ring (2..kScatMaxStages)
     unsigned* err;            // set to 1 when a bounded wait gives up
-    int acc_check;            // 1: the accumulator is chosen on the device from *cmax (both
-                              // variants are launched; the one not chosen returns at once)
+    long long wait_limit;     // SM clock cycles a producer/consumer handshake wait may take
+    int withhold;             // test hook: the producer issues no line copies, so the
+                              // consumers' waits run out (the error path, exercised safely)
 };
+constexpr long long kScatWaitCycles = 1LL << 31;   // about one second of SM clocks
 
 // Lines are staged per chunk as [v0 8B][ls2][el][ga][gs][na][dl 4B each][iso 1B]
 // x chunk; line arrays are allocated with room for a multiple of 16 lines.
@@ -188,6 +190,15 @@ struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
     unsigned char map_l[kMaxAxis];
     unsigned* err;        // K4: non-null with err_pub: publish the device error flag
     unsigned* err_pub;    //   into host-mapped memory and clear it (one thread)
+    // K4 epilogue (q_out non-null): the post-processing of eq_spectrum_gpu
+    // (radis/lbl/factory.py:1284-1297) on each abscoeff value as it is written:
+    // q_out rows of n_v floats = absorbance (x exp(-log_scale), like out),
+    // emissivity, transmittance, radiance (mW/cm2/sr/nm at Planck(1e7/v nm, T))
+    float* q_out;
+    float q_scale;        // exp(log_scale): out x q_scale = abscoeff in cm-1 (may be inf)
+    float q_path;         // path length (cm)
+    float q_c2_T;         // hc / (k T) in cm
+    double q_vmin, q_dv;  // v_k = q_vmin + k q_dv (cm-1)
 };
 
 struct VoigtArgs {        // K3 (row FFT + Voigt weights + pair reduction)
@@ -276,16 +287,6 @@ struct SlitArgs {
     int valid;            // 1: NaN on the boundary points (remove_boundary 'valid')
 };
 
-struct QuantArgs {         // post-processing epilogue (radis/lbl/factory.py:1284-1297)
-    const float* abscoeff;    // n_v, in units of exp(log_scale)
-    float* out;               // 4 rows of n_v: absorbance (same units), emissivity, transmittance, radiance
-    int n_v;
-    double vmin, dv;
-    float scale;              // exp(log_scale) (may be inf when the spectrum exceeds FP32)
-    float path_length;        // cm
-    float c2_T;               // hc / (k T) in cm (x nu in cm-1)
-};
-
 struct AdjRowArgs {       // adjoint row stage: per pair, IFFT_row(Ghat (V_a + i V_b)) x twiddle
     VoigtArgs v;          // v.g holds Ghat [n1][n2] (FFT of the upstream gradient)
     float2* y;            // output [pair][n1][n2]
@@ -339,6 +340,9 @@ int launch_col_cmax(const int64_t* col_start, int col_off, int col_count, int n_
                     cudaStream_t st);
 // wide: the 64-bit accumulator variant
 int launch_scatter(const ScatterArgs& a, int grid, int threads, size_t smem, bool wide, cudaStream_t st);
+// one launch, the accumulator chosen on the device from *cmax (a32 / a64: the two shapes)
+int launch_scatter_auto(const ScatterArgs& a32, const ScatterArgs& a64, int grid, int threads, size_t smem,
+                        cudaStream_t st);
 int scatter_smem_optin(size_t* avail, bool wide);
 int launch_col_fft_fwd(const ColFftArgs& a, cudaStream_t st);
 int launch_row_fft_voigt(const VoigtArgs& a, cudaStream_t st);
@@ -351,7 +355,6 @@ int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st);
 int launch_gather_grad(const GradArgs& a, int grid, cudaStream_t st);
 int launch_gauss_merge(const GaussArgs& a, int out_rows, cudaStream_t st);
 int launch_slit_conv(const SlitArgs& a, cudaStream_t st);
-int launch_quantities(const QuantArgs& a, cudaStream_t st);
 int launch_scatter_tangent(const GradArgs& a, int grid, cudaStream_t st);
 int col_block(int n1);               // columns per CTA of the column FFTs
 int row_threads(const FftLen& f);    // block size of the forward row kernel

@@ -372,11 +372,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
-// Bounded wait (about one second of SM clocks); false when it gives up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Bounded wait (`limit` SM clock cycles); false when it gives up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit = kScatWaitCycles) {
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > (1LL << 31)) return false;
+        if (clock64() - t0 > limit) return false;
     return true;
 }
 
@@ -542,11 +542,9 @@ __device__ __forceinline__ unsigned scatter_chunk(const ScatterArgs& a, const St
 // warps) to flush the finished tile to HBM with plain stores.  Every wait is
 // bounded; a wait that gives up sets the error flag and the CTA stops after
 // the copies it issued have landed (bounded).  Acc: the 32- or 64-bit
-// fixed-point word of the tile; with a.acc_check both variants are launched
-// and the one whose width *cmax does not call for returns before any work.
+// fixed-point word of the tile.
 template <typename Acc>
-__global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a) {
-    if (a.acc_check && fx_wide(*a.cmax) != (sizeof(Acc) == 8)) return;
+__device__ __forceinline__ void scatter_body(const ScatterArgs& a) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int ch = a.chunk;
     const int S = a.stages;
@@ -586,9 +584,9 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
         int buf = 0;          // ring slot of chunk c (c mod S, kept incrementally)
         uint32_t round = 0;   // c / S: slot reuse number
         bool bad = false;
-        for (int q = 0; q < nq && !bad; ++q)
+        for (int q = 0; q < nq && !bad && !a.withhold; ++q)
             for (int cs = rng[q].x; cs < rng[q].y; cs += ch) {
-                if (round > 0 && !mbar_wait(&empty[buf], (round - 1) & 1)) {
+                if (round > 0 && !mbar_wait(&empty[buf], (round - 1) & 1, a.wait_limit)) {
                     bad = true;
                     break;
                 }
@@ -600,7 +598,8 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
                 }
             }
         if (bad) atomicExch(a.err, 1u);
-        // the last copies must land before the CTA may end (normally already consumed)
+        // the last copies must land before the CTA may end (normally already
+        // consumed); this drain keeps the full bound whatever a.wait_limit is
         for (uint32_t k = c > (uint32_t)S ? c - S : 0; k < c; ++k)
             mbar_wait(&full[k % (uint32_t)S], (k / (uint32_t)S) & 1);
         return;
@@ -622,7 +621,7 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
         const int b = rng[q].y;
         for (int cs = rng[q].x; cs < b && !bad; cs += ch) {
             // every lane acquires the TMA data through the mbarrier itself
-            const bool ok = mbar_wait(&full[buf], par);
+            const bool ok = mbar_wait(&full[buf], par, a.wait_limit);
             if (!__all_sync(0xffffffffu, ok)) {
                 bad = true;
                 break;
@@ -655,7 +654,8 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
             Acc* row = tile + node * pitch;
             float* dst = a.ldm + node * a.row_stride + k_start;
             for (int c = lane; c < tk; c += 32) {   // one 128-byte store per warp step
-                dst[c] = Fx<Acc>::to_float(row[c]) * inv_fx;
+                // streaming store: the LDM is read once by the next stage, long after
+                __stcs(&dst[c], Fx<Acc>::to_float(row[c]) * inv_fx);
                 row[c] = 0;
             }
         }
@@ -665,6 +665,23 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
         const unsigned tot = __reduce_add_sync(0xffffffffu, counted);
         if (lane == 0 && tot) atomicAdd(a.in_window, (unsigned long long)tot);
     }
+}
+
+template <typename Acc>
+__global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a) {
+    scatter_body<Acc>(a);
+}
+
+// The accumulator chosen on the device from the column bound *cmax (served and
+// allocation-free spectra, whose bound is never read back): a32 / a64 are the
+// shapes of the two variants; the launch covers the larger grid and shared
+// memory (tiles are dealt out by gridDim.x, so the extra CTAs of the smaller
+// variant only take fewer tiles each).
+__global__ void __launch_bounds__(kScatThreads, 1) k_scatter_auto(const ScatterArgs a32, const ScatterArgs a64) {
+    if (fx_wide(*a32.cmax))
+        scatter_body<unsigned long long>(a64);
+    else
+        scatter_body<unsigned>(a32);
 }
 
 // ---------------------------------------------------------------------------
@@ -1140,6 +1157,25 @@ __global__ void __launch_bounds__(kRowThreads) k_row_ifft(const RowIfftArgs a) {
 // ---------------------------------------------------------------------------
 // K4: inverse column FFT (length n1), real part, scaled, first n_v samples
 // ---------------------------------------------------------------------------
+// Post-processing epilogue (radis/lbl/factory.py:1284-1297 and
+// radis/spectrum/equations.py:21-44): absorbance A L, emissivity
+// -expm1(-A L), transmittance 1 - emissivity, radiance emissivity x Planck
+// (radis/phys/blackbody.py:35-74, mW / cm2 / sr / nm at lambda = 1e7/nu nm).
+__device__ __forceinline__ void quantities_at(const ColFftArgs& a, int64_t k, float A) {
+    const float tau = A * a.q_scale * a.q_path;      // absorbance in physical units
+    const float eps = -expm1f(-tau);
+    const float nu = (float)(a.q_vmin + a.q_dv * (double)k);
+    const float lam = 0.01f / nu;                    // m
+    // 2 h c^2 / lambda^5 / expm1(h c / (lambda k T)) W m-3 sr-1 -> mW cm-2 sr-1 nm-1 (x 1e-10)
+    const float l2 = lam * lam;
+    const float planck = 1.19104297e-16f / (l2 * l2 * lam) / expm1f(a.q_c2_T * nu) * 1e-10f;
+    const int64_t n = a.n_v;
+    a.q_out[k] = A * a.q_path;
+    a.q_out[n + k] = eps;
+    a.q_out[2 * n + k] = 1.f - eps;
+    a.q_out[3 * n + k] = eps * planck;
+}
+
 template <int N1>
 __global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_ifft(const ColFftArgs a) {
     constexpr int TPC = ColShape<N1>::TPC;
@@ -1155,7 +1191,11 @@ __global__ void __launch_bounds__(ColShape<N1>::THREADS) k_col_ifft(const ColFft
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
         const int64_t nidx = (int64_t)(j + r * TPC) * a.n2 + n2i;
-        if (nidx < a.n_v) a.out[nidx] = v[r].x * a.out_scale;   // Re(conj(z)) = Re(z)
+        if (nidx < a.n_v) {
+            const float A = v[r].x * a.out_scale;   // Re(conj(z)) = Re(z)
+            a.out[nidx] = A;
+            if (a.q_out) quantities_at(a, nidx, A);
+        }
     }
     // last kernel of the spectrum: hand the error flag to the host (mapped
     // memory, read after the stream synchronises) and clear it
@@ -1608,29 +1648,6 @@ __global__ void __launch_bounds__(256) k_scatter_tangent(const GradArgs g) {
 }
 
 // ---------------------------------------------------------------------------
-// Post-processing epilogue (radis/lbl/factory.py:1284-1297 and
-// radis/spectrum/equations.py:21-44): absorbance A L, emissivity
-// -expm1(-A L), transmittance 1 - emissivity, radiance emissivity x Planck
-// (radis/phys/blackbody.py:35-74, mW / cm2 / sr / nm at lambda = 1e7/nu nm).
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_quantities(const QuantArgs a) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.n_v) return;
-    const float A = a.abscoeff[k];
-    const float tau = A * a.scale * a.path_length;   // absorbance in physical units
-    const float eps = -expm1f(-tau);
-    const float nu = (float)(a.vmin + a.dv * (double)k);
-    const float lam = 0.01f / nu;                     // m
-    // 2 h c^2 / lambda^5 / expm1(h c / (lambda k T)) W m-3 sr-1 -> mW cm-2 sr-1 nm-1 (x 1e-10)
-    const float l2 = lam * lam;
-    const float planck = 1.19104297e-16f / (l2 * l2 * lam) / expm1f(a.c2_T * nu) * 1e-10f;
-    a.out[k] = A * a.path_length;
-    a.out[a.n_v + k] = eps;
-    a.out[2 * (int64_t)a.n_v + k] = 1.f - eps;
-    a.out[3 * (int64_t)a.n_v + k] = eps * planck;
-}
-
-// ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
 static int check_launch() {
@@ -1709,6 +1726,13 @@ int launch_scatter(const ScatterArgs& a, int grid, int threads, size_t smem, boo
     return check_launch();
 }
 
+int launch_scatter_auto(const ScatterArgs& a32, const ScatterArgs& a64, int grid, int threads, size_t smem,
+                        cudaStream_t st) {
+    ALLOW_SMEM(k_scatter_auto, smem);
+    k_scatter_auto<<<grid, threads, smem, st>>>(a32, a64);
+    return check_launch();
+}
+
 // Dynamic shared memory a scatter variant may have (one CTA per SM).
 template <typename Acc>
 static int scatter_optin(size_t* avail) {
@@ -1728,6 +1752,8 @@ static int scatter_optin(size_t* avail) {
     return RG_OK;
 }
 int scatter_smem_optin(size_t* avail, bool wide) {
+    // every variant (and k_scatter_auto) has the same static shared memory
+    // (none); the opt-in limit of one serves for all
     return wide ? scatter_optin<unsigned long long>(avail) : scatter_optin<unsigned>(avail);
 }
 
@@ -1877,12 +1903,6 @@ int launch_slit_conv(const SlitArgs& a, cudaStream_t st) {
     const int64_t blocks = (a.n + kGaussTile - 1) / kGaussTile;
     if (blocks > 0x7fffffff) return RG_ERR_RANGE;
     k_slit_conv<<<(unsigned)blocks, 256, smem, st>>>(a);
-    return check_launch();
-}
-
-int launch_quantities(const QuantArgs& a, cudaStream_t st) {
-    if (a.n_v <= 0) return RG_OK;
-    k_quantities<<<(a.n_v + 255) / 256, 256, 0, st>>>(a);
     return check_launch();
 }
 

@@ -17,7 +17,7 @@ import numpy as np
 
 from . import __version__
 from .gpu import gpuApp
-from .spectrum import DEFAULT_UNITS, Spectrum, derived_quantities
+from .spectrum import DEFAULT_UNITS, Spectrum
 from .units import get_wavenumber_range
 
 # default LDM steps (radis/lbl/loader.py:452-460, 538-543)
@@ -162,12 +162,13 @@ class SpectrumFactory:
                      verbose=verbose, device_id=device_id, S_ref=d["S_ref"],
                      n_G=self.params.n_G, n_L=self.params.n_L,
                      folding_thresh=self.params.folding_thresh)
-        abscoeff_calc, times = app.iterate(self.input.pressure, Tgas, self.input.mole_fraction,
-                                           verbose=verbose)
+        # abscoeff and the post-processing of factory.py:1284-1297 from the device
+        # (fused into the last kernel), cropped to the output range
+        quant, times = app.iterate_quantities(self.input.pressure, Tgas, self.input.mole_fraction,
+                                              self.input.path_length, verbose=verbose)
         n_L, n_G = app.get_griddims()
         w0, w1 = self.woutrange
-        abscoeff = abscoeff_calc[w0:w1]
-        a, e, t, r = derived_quantities(self.wavenumber, abscoeff, self.input.path_length, Tgas)
+        abscoeff, a, e, t, r = (quant[k][w0:w1] for k in gpuApp.QUANTITIES)
         conditions = dict(
             Tgas=Tgas, Trot=Tgas, Tvib=Tgas, pressure=self.input.pressure,
             pressure_mbar=self.input.pressure * 1e3, mole_fraction=self.input.mole_fraction,

@@ -26,6 +26,7 @@ from . import _lib as L
 C2 = 6.62607015e-34 * 2.99792458e8 / 1.3806490e-23 * 100.0   # hc/k, cm K
 TREF = 296.0
 STAGES = ("scatter", "fft_col", "fft_row+voigt", "ifft_row", "ifft_col")
+QUANTITIES = ("abscoeff", "absorbance", "emissivity_noslit", "transmittance_noslit", "radiance_noslit")
 
 
 class gpuApp:
@@ -90,6 +91,8 @@ class gpuApp:
         self._griddims = (0, 0)
         self.last_info = None
 
+    QUANTITIES = QUANTITIES
+
     def q_ratio(self, T):
         return np.array([self._Qref[i] / float(q(T)) for i, q in enumerate(self._Q)])
 
@@ -109,6 +112,29 @@ class gpuApp:
         times["total"] = float(info.stage_ms[5])
         if info.log_scale != 0.0:
             out = out.astype(np.float64) * np.exp(info.log_scale)
+        if verbose >= 1 or self.verbose >= 2:
+            print(f"gpuApp: N_G={g.n_G} N_L={g.n_L} n_ft={g.n_ft} total {times['total']:.3f} ms")
+        return out, times
+
+    def iterate_quantities(self, p, T, mole_fraction, path_length, verbose=0):
+        """The spectral quantities of eq_spectrum_gpu on the plan's grid, with
+        the post-processing of radis/lbl/factory.py:1284-1297 fused into the
+        last kernel: ({abscoeff, absorbance, emissivity_noslit,
+        transmittance_noslit, radiance_noslit}, stage times).  float32 arrays
+        (float64 for abscoeff/absorbance when the spectrum exceeds FP32)."""
+        if self._freed:
+            raise RuntimeError("gpuApp was freed (exit_gpu)")
+        q = None if self._q_in_lib else self.q_ratio(T)
+        out, info = self.plan.synthesize_quantities_host(T, p, mole_fraction, path_length, q_ratio=q,
+                                                         timing=True)
+        g = info.grid
+        self._griddims = (g.n_L, g.n_G)
+        self.last_info = info
+        times = {n: float(info.stage_ms[i]) for i, n in enumerate(STAGES)}
+        times["total"] = float(info.stage_ms[5])
+        if info.log_scale != 0.0:
+            for k in ("abscoeff", "absorbance"):
+                out[k] = out[k].astype(np.float64) * np.exp(info.log_scale)
         if verbose >= 1 or self.verbose >= 2:
             print(f"gpuApp: N_G={g.n_G} N_L={g.n_L} n_ft={g.n_ft} total {times['total']:.3f} ms")
         return out, times

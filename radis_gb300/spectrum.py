@@ -167,10 +167,12 @@ class Spectrum:
     def recalc_gpu(self, var="abscoeff", wunit="default", Iunit="default", pressure=None, Tgas=None,
                    mole_fraction=None, path_length=None, slit_function=None, verbose=False):
         """Re-run the resident GPU application at new conditions and return
-        ``var`` (spectrum.py:6438-6572).  Only abscoeff comes from the GPU; the
-        other quantities are re-derived on request.  With ``slit_function``
-        the slit is applied on the GPU (``apply_slit``) and a convolved
-        quantity (transmittance, radiance, emissivity) is returned."""
+        ``var`` (spectrum.py:6438-6572).  abscoeff and the quantities derived
+        from it (absorbance, emissivity, transmittance, radiance) all come from
+        the GPU, the post-processing fused into the spectrum's last kernel.
+        With ``slit_function`` the slit is applied on the GPU (``apply_slit``)
+        and a convolved quantity (transmittance, radiance, emissivity) is
+        returned."""
         if self.gpu_app is None:
             warnings.warn("no GPU application attached to this Spectrum (exit_gpu was "
                           "called or exit_gpu=True was used)", GPUInitWarning)
@@ -184,14 +186,14 @@ class Spectrum:
             c["mole_fraction"] = mole_fraction
         if path_length is not None:
             c["path_length"] = path_length
-        abscoeff, times = self.gpu_app.iterate(c["pressure"], c["Tgas"], c["mole_fraction"],
-                                               verbose=verbose)
-        w0, w1 = self._woutrange or (0, len(abscoeff))
-        abscoeff = abscoeff[w0:w1]
+        quant, times = self.gpu_app.iterate_quantities(c["pressure"], c["Tgas"], c["mole_fraction"],
+                                                       c["path_length"], verbose=verbose)
+        w0, w1 = self._woutrange or (0, len(quant["abscoeff"]))
         for k in list(self._q):
             if k != "wavenumber":
                 del self._q[k]
-        self._q["abscoeff"] = abscoeff
+        for k, v in quant.items():
+            self._q[k] = v[w0:w1]
         n_L, n_G = self.gpu_app.get_griddims()
         c.update(NwL=n_L, NwG=n_G, gpu_times=times)
         if slit_function is not None:

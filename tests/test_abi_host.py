@@ -145,3 +145,28 @@ def test_grid_independent_of_line_order(native_lib):
     bad["v0"][[555_555, 555_556]] = -1.0
     with pytest.raises(L.RgError, match=r"v0\[555555\]"):
         L.grid_estimate(bad, 44.0, 2000.0, 0.001, 400001, 296.0, 1.0, 0.1, n_G=8, n_L=16)
+
+
+def test_window_axes_cover_window_lines(native_lib):
+    """axes_window: the Gaussian node axis of a narrow window of a wide list
+    spans the lines that can reach the window -- every such line's log wG lies
+    on the axis -- with far fewer nodes than the whole-list axis; the
+    Lorentzian axis is unchanged.  A window with no line falls back to the
+    whole list."""
+    import numpy as np
+
+    from oracle import ldm_oracle as O
+    lines = S.h2o_like(400_000, seed=4)
+    T, p, x, dv = 2000.0, 1.0, 0.2, 0.005
+    kw = dict(dxG=S.DXG_DEFAULT, dxL=S.DXL_DEFAULT)
+    full = L.grid_estimate(lines, 18.0, 3700.0, dv, 10001, T, p, x, **kw)
+    win = L.grid_estimate(lines, 18.0, 3700.0, dv, 10001, T, p, x, axes_window=True, **kw)
+    assert win.n_G < full.n_G / 4
+    assert (win.n_L, win.log_wL_min, win.dxL) == (full.n_L, full.log_wL_min, full.dxL)
+    v0 = np.asarray(lines["v0"])
+    sel = (v0 >= 3700.0 - dv) & (v0 <= 3700.0 + 10000 * dv + dv)
+    lgG = np.log(2.0 * O.doppler_hwhm(v0[sel], 18.0, T))
+    top = win.log_wG_min + (win.n_G - 1) * win.dxG
+    assert lgG.min() >= win.log_wG_min - 1e-12 and lgG.max() <= top + 1e-12
+    empty = L.grid_estimate(lines, 18.0, 9000.0, dv, 1001, T, p, x, axes_window=True, **kw)
+    assert (empty.n_G, empty.log_wG_min) == (full.n_G, full.log_wG_min)

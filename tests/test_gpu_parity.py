@@ -136,6 +136,51 @@ def test_device_quantities(ctx):
         assert np.max(np.abs(gq - wq)) <= 1e-5 * np.max(np.abs(wq))
 
 
+def test_fused_quantities_host_vs_oracle(ctx):
+    """rg_synthesize_quantities_host (the post-processing fused into the last
+    kernel, host output) against the oracle's quantities of the FP64
+    reference abscoeff, per output, on a path length that makes the gas
+    optically thick somewhere (transmittance spans (0, 1])."""
+    lines = S.uniform_lines(30_000, 2000.0, 2030.0, seed=52)
+    M, vmin, dv, n_v, T, p, x = 28.0, 2000.0, 0.001, 30001, 1100.0, 1.0, 0.1
+    ln = L.Lines(ctx, lines, M)
+    plan = L.Plan(ln, vmin, dv, n_v, dxG=S.DXG_DEFAULT, dxL=S.DXL_DEFAULT)
+    _, info = plan.synthesize_host(T, p, x)
+    a_ref = oracle(lines, M, vmin, dv, n_v, T, p, x, info)
+    Lp = 5.0 / a_ref.max()           # peak absorbance 5
+    got, info = plan.synthesize_quantities_host(T, p, x, Lp)
+    plan.close()
+    ln.close()
+    ref = O.quantities(a_ref, vmin, dv, T, Lp)
+    assert ref["transmittance_noslit"].min() < 0.01 and ref["transmittance_noslit"].max() > 0.5
+    sc = np.exp(info.log_scale)
+    for k in ref:
+        g = got[k].astype(np.float64) * (sc if k in ("abscoeff", "absorbance") else 1.0)
+        assert rel_err(g, ref[k]) <= TOL, k
+
+
+def test_scatter_wait_timeout_then_recovers(ctx):
+    """The failure path of the scatter's bounded waits: with the test hook the
+    producer withholds its line copies, every consumer's wait for its first
+    chunk runs out after ~2M SM cycles, the kernels finish and the call
+    reports RG_ERR_TIMEOUT; the next spectrum on the same plan matches the
+    oracle (the flag was cleared, the LDM is rewritten)."""
+    lines = S.uniform_lines(100_000, 2000.0, 2020.0, seed=81)
+    args = (28.0, 2000.0, 0.001, 20001, 900.0, 1.0, 0.1)
+    ln = L.Lines(ctx, lines, 28.0)
+    plan = L.Plan(ln, 2000.0, 0.001, 20001, dxG=S.DXG_DEFAULT, dxL=S.DXL_DEFAULT)
+    plan.test_scatter_stall(True, wait_cycles=2_000_000)
+    with pytest.raises(L.RgError) as e:
+        plan.synthesize_host(900.0, 1.0, 0.1)
+    assert e.value.code == 6
+    plan.test_scatter_stall(False)
+    out, info = plan.synthesize_host(900.0, 1.0, 0.1)
+    gpu = out.astype(np.float64) * np.exp(info.log_scale)
+    plan.close()
+    ln.close()
+    assert rel_err(gpu, oracle(lines, *args, info)) <= TOL
+
+
 def test_odd_node_count_padding(ctx):
     lines = S.uniform_lines(20_000, 2000.0, 2020.0, seed=24)
     args = (28.0, 2000.0, 0.001, 20001, 400.0, 0.5, 0.05)
@@ -360,5 +405,32 @@ def test_sparse_list_keeps_32_bit_accumulator(ctx):
     plan = L.Plan(ln, 1900.0, 0.002, 200001, dxG=S.DXG_DEFAULT, dxL=S.DXL_DEFAULT)
     _, info = plan.synthesize_host(700.0, 1.01325, 0.1)
     assert info.accum_bits == 32
+    plan.close()
+    ln.close()
+
+
+def test_window_axes_narrow_window_of_wide_list(ctx):
+    """A 40 cm-1 window of an H2O-like list spanning 500-8000 cm-1 with the
+    Gaussian axis from the lines that can reach the window (axes_window): far
+    fewer LDM rows, the same oracle parity, through a plan and a served
+    request."""
+    lines = S.h2o_like(3_000_000, seed=6)
+    M, vmin, dv, n_v, T, p, x = 18.0, 3680.0, 0.005, 8001, 1800.0, 0.8, 0.2
+    grid = dict(dxG=S.DXG_DEFAULT, dxL=S.DXL_DEFAULT)
+    ln = L.Lines(ctx, lines, M)
+    full = L.Plan(ln, vmin, dv, n_v, **grid).grid(T, p, x)
+    plan = L.Plan(ln, vmin, dv, n_v, axes_window=True, **grid)
+    out, info = plan.synthesize_host(T, p, x)
+    assert info.grid.n_G < full.n_G / 3
+    gpu = out.astype(np.float64) * np.exp(info.log_scale)
+    ref = O.synthesize(lines, T, p, x, vmin, dv, n_v, info.grid.axes(), info.grid.n_ft, molar_mass=M,
+                       fft_workers=WORKERS)
+    assert rel_err(gpu, ref) <= TOL
+    srv = L.Server(ctx, slots=2, mem_budget=4 << 30)
+    t = srv.submit(ln, vmin, dv, n_v, T, p, x, axes_window=True, **grid)
+    o_s, i_s, _ = srv.wait(t)
+    srv.close()
+    assert (i_s.grid.n_G, i_s.grid.log_wG_min) == (info.grid.n_G, info.grid.log_wG_min)
+    assert rel_err(o_s.astype(np.float64) * np.exp(i_s.log_scale), ref) <= TOL
     plan.close()
     ln.close()
