@@ -257,6 +257,7 @@ struct GaussArgs {
     int wide_l[kMaxAxis], K[kMaxAxis];       // wide nodes and kernel half-widths
     float c[kMaxAxis], a2[kMaxAxis];         // taps c ex2(-a2 j^2), |j| <= K
     int narrow_l[kMaxAxis];
+    int slot_taps, slot_len;                 // set by the launcher: floats per ring slot (taps, taps + window)
     // The wide Gaussians are split as g_l = d_l conv g_b (sigma_l^2 = sigma_d^2 +
     // sigma_b^2, one base g_b shared by all wide l): c/a2/K above describe the
     // residual d_l, and the base is applied to the merged rows in Fourier space

@@ -1282,8 +1282,6 @@ __device__ __forceinline__ void load8(float (&d)[8], const float* s) {
     d[4] = b.x; d[5] = b.y; d[6] = b.z; d[7] = b.w;
 }
 
-constexpr int kGaussXs = kGaussTile + 2 * kGaussMaxK + 24;   // window buffer floats
-
 // acc[i] += sum_jj taps[jj] xs[t0 + i + jj], jj < KP (a multiple of 4; xs
 // readable up to t0 + KP + 7): three 8-value register blocks rotate through
 // the window (no moves): taps jj..jj+7 use A ++ B, jj+8.. use B ++ C, jj+16..
@@ -1338,15 +1336,27 @@ __device__ __forceinline__ void conv_window(float (&acc)[8], const float* xs, co
     }
 }
 
+// Nodes are streamed through a ring of kGaussStages shared-memory slots, each
+// holding one node's taps and window, filled with cp.async (zero-filled
+// outside the row) kGaussStages - 1 nodes ahead of the convolution: one
+// barrier per node and no staging through registers.
+constexpr int kGaussStages = 4;
+
+__device__ __forceinline__ void cp_async16(float* dst, const float* src, int bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
 __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
     extern __shared__ __align__(16) float gsm[];
     constexpr int TW = kGaussTile;
     constexpr int P = kGaussPer;                     // outputs per thread (8)
-    float* taps = gsm;                               // KP <= 2 kGaussMaxK + 4 (K <= kGaussMaxK, shift <= 3)
-    float* xs = gsm + (2 * kGaussMaxK + 16);         // 4 n4 <= TW + KP + 11 <= kGaussXs
+    constexpr int S = kGaussStages;
     const int r = blockIdx.y;
     const int p0 = blockIdx.x * TW;                  // first output (buffer position)
-    const int q0 = p0;                               // first position of the per-thread accumulators
     const int Lr = a.n_v + 2 * a.ext;
     float* orow = a.out + (int64_t)r * a.out_stride;
     const int m = r;   // merged row of wL node m
@@ -1354,55 +1364,43 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
 #pragma unroll
     for (int i = 0; i < P; ++i) acc[i] = 0.f;
     const int t0 = threadIdx.x * P;
-    // Node w's window starts at LDM index base = q0 - ext - K_w; it is staged
+    // Node w's window starts at LDM index base = p0 - ext - K_w; it is staged
     // from the 16-byte aligned index base & ~3, and the offset s = base & 3 is
-    // absorbed by s leading zero taps.  The next node's window is fetched into
-    // registers (NPRE float4 per thread) while the current one is convolved.
-    constexpr int NPRE = ((TW + 2 * kGaussMaxK + 24) / 4 + 255) / 256;
-    float4 pre[NPRE];
-    auto shift_of = [&](int w) { return (q0 - a.ext - a.K[w]) & 3; };
+    // absorbed by s leading zero taps.
+    auto shift_of = [&](int w) { return (p0 - a.ext - a.K[w]) & 3; };
     auto taps_of = [&](int w) { return (2 * a.K[w] + 1 + shift_of(w) + 3) & ~3; };   // multiple of 4
-    auto fetch = [&](int w) {
-        const int k0 = (q0 - a.ext - a.K[w]) & ~3;   // LDM index of xs[0]
-        const int n4 = (TW + taps_of(w) + 8 + 3) / 4;
-        const float* src = a.ldm + (int64_t)(a.wide_l[w] * a.NL + m) * a.row_stride;
-#pragma unroll
-        for (int u = 0; u < NPRE; ++u) {
-            const int q = threadIdx.x + u * 256;
-            const int k = k0 + 4 * q;
-            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (q < n4) {
-                if (k >= 0 && k + 3 < a.n_v) {
-                    v = __ldg(reinterpret_cast<const float4*>(src + k));   // rows start 128-byte aligned
-                } else {   // row ends: zeros outside [0, n_v)
-                    if (k >= 0 && k < a.n_v) v.x = __ldg(&src[k]);
-                    if (k + 1 >= 0 && k + 1 < a.n_v) v.y = __ldg(&src[k + 1]);
-                    if (k + 2 >= 0 && k + 2 < a.n_v) v.z = __ldg(&src[k + 2]);
-                    if (k + 3 >= 0 && k + 3 < a.n_v) v.w = __ldg(&src[k + 3]);
-                }
-            }
-            pre[u] = v;
-        }
-    };
-    fetch(0);
-    for (int w = 0; w < a.n_wide; ++w) {
+    auto slot_taps = [&](int w) { return gsm + (w % S) * a.slot_len; };
+    auto issue = [&](int w) {   // taps (plain stores) and window (cp.async) of node w into its slot
+        float* taps = slot_taps(w);
+        float* xs = taps + a.slot_taps;
         const int K = a.K[w];
         const int sh = shift_of(w);
         const int KP = taps_of(w);
-        const int n4 = (TW + KP + 8 + 3) / 4;
-        __syncthreads();   // previous node's taps and tile consumed
         for (int jj = threadIdx.x; jj < KP; jj += blockDim.x) {
             const float j = (float)(jj - sh - K);
             taps[jj] = jj >= sh && jj <= sh + 2 * K ? a.c[w] * ex2(-a.a2[w] * j * j) : 0.f;
         }
-#pragma unroll
-        for (int u = 0; u < NPRE; ++u) {
-            const int q = threadIdx.x + u * 256;
-            if (q < n4) reinterpret_cast<float4*>(xs)[q] = pre[u];
+        const int k0 = (p0 - a.ext - K) & ~3;        // LDM index of xs[0]
+        const int n4 = (TW + KP + 8 + 3) / 4;        // 4 n4 <= slot_len - slot_taps
+        const float* src = a.ldm + (int64_t)(a.wide_l[w] * a.NL + m) * a.row_stride;
+        for (int q = threadIdx.x; q < n4; q += blockDim.x) {
+            const int k = k0 + 4 * q;                // rows start 128-byte aligned; k is a multiple of 4
+            const int bytes = (k >= 0 && k < a.n_v) ? 4 * min(4, a.n_v - k) : 0;   // zeros outside [0, n_v)
+            cp_async16(xs + 4 * q, bytes ? src + k : src, bytes);
         }
-        if (w + 1 < a.n_wide) fetch(w + 1);
-        __syncthreads();
-        conv_window(acc, xs, taps, t0, KP);
+    };
+#pragma unroll
+    for (int w = 0; w < S - 1; ++w) {
+        if (w < a.n_wide) issue(w);
+        cp_async_commit();
+    }
+    for (int w = 0; w < a.n_wide; ++w) {
+        cp_async_wait<S - 2>();   // this thread's copies of node w have landed
+        __syncthreads();          // everyone's have, and everyone is done with node w - 1
+        if (w + S - 1 < a.n_wide) issue(w + S - 1);   // into node w - 1's slot
+        cp_async_commit();
+        const float* taps = slot_taps(w);
+        conv_window(acc, taps + a.slot_taps, taps, t0, taps_of(w));
     }
     const int p = p0 + t0;
 #pragma unroll
@@ -1885,12 +1883,19 @@ int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st) {
     }
 }
 
-int launch_gauss_merge(const GaussArgs& a, int out_rows, cudaStream_t st) {
-    const size_t smem = sizeof(float) * ((2 * kGaussMaxK + 16) + kGaussXs);
+int launch_gauss_merge(const GaussArgs& a0, int out_rows, cudaStream_t st) {
+    GaussArgs a = a0;
     const int Lr = a.n_v + 2 * a.ext;
     if (a.n_wide < 0 || a.n_wide > kMaxAxis || a.row_stride % 4) return RG_ERR_RANGE;
-    for (int w = 0; w < a.n_wide; ++w)
+    int kp_max = 4;   // taps of the widest node: 2 K + 1 + shift (<= 3), rounded up to 4
+    for (int w = 0; w < a.n_wide; ++w) {
         if (a.K[w] < 0 || a.K[w] > kGaussMaxK) return RG_ERR_RANGE;
+        kp_max = std::max(kp_max, (2 * a.K[w] + 1 + 3 + 3) & ~3);
+    }
+    a.slot_taps = kp_max;
+    a.slot_len = kp_max + ((kGaussTile + kp_max + 8 + 3) / 4) * 4;   // taps + staged window, 16-byte multiple
+    const size_t smem = sizeof(float) * (size_t)kGaussStages * a.slot_len;
+    ALLOW_SMEM(k_gauss_merge, smem);
     dim3 grid((Lr + kGaussTile - 1) / kGaussTile, out_rows);
     k_gauss_merge<<<grid, 256, smem, st>>>(a);
     return check_launch();
