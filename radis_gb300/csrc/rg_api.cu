@@ -224,9 +224,10 @@ int64_t next_smooth(int64_t x) {
     }
 }
 
-// Radix plan of a length L = 2^a 3^b 5^c: the leftover 2 or 4 first, then the
-// 3s and 5s, then radix 8 -- the last pass is radix 8 whenever 8 divides L,
-// which the row kernel relies on (n2 is a multiple of 32).
+// Radix plan of a length L = 2^a 3^b 5^c: the leftover 2 or 4, the 3s and 5s
+// (merged into composite radices: up to 12 first, 6 later), then radix 8
+// -- the last pass is radix 8 whenever 8 divides L, which the row kernel
+// relies on (n2 is a multiple of 32).
 // Partition-function ratio Q(Tref)/Q(T) of isotopologue i: the caller's,
 // else the list's tables when every isotopologue has one, else 1.
 bool have_qtables(const rg_lines* L) {
@@ -278,13 +279,35 @@ bool radices(int L, int* rad, int* np) {
         r /= 5;
         ++c;
     }
-    if (a % 3 == 2) rad[k++] = 4;
-    if (a % 3 == 1) rad[k++] = 2;
-    for (int i = 0; i < b; ++i) rad[k++] = 3;
-    for (int i = 0; i < c; ++i) rad[k++] = 5;
-    for (int i = 0; i < a / 3; ++i) rad[k++] = 8;
+    // the small factors (the leftover 2 or 4, the 3s and 5s), merged in order
+    // into composite radices (6, 9, 10, 12) within the bounds the row kernels
+    // transform in registers without spilling
+    int small[64], ns = 0;
+    if (a % 3 == 2) small[ns++] = 4;
+    if (a % 3 == 1) small[ns++] = 2;
+    for (int i = 0; i < b && ns < 64; ++i) small[ns++] = 3;
+    for (int i = 0; i < c && ns < 64; ++i) small[ns++] = 5;
+    int cur = 1;
+    for (int i = 0; i < ns; ++i) {
+        const int cap = k == 0 ? kFirstRadixMax : kMidRadixMax;
+        if (cur * small[i] <= cap) {
+            cur *= small[i];
+        } else {
+            if (k >= kMaxPasses) return false;
+            rad[k++] = cur;
+            cur = small[i];
+        }
+    }
+    if (cur > 1) {
+        if (k >= kMaxPasses) return false;
+        rad[k++] = cur;
+    }
+    for (int i = 0; i < a / 3; ++i) {
+        if (k >= kMaxPasses) return false;
+        rad[k++] = 8;
+    }
     *np = k;
-    return r == 1 && k <= kMaxPasses;
+    return r == 1;
 }
 
 constexpr int kN2Max = 256 * 32;   // row FFT limit (threads x register accumulators)

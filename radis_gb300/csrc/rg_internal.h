@@ -39,6 +39,12 @@ constexpr int kMaxAxis = 64;        // max nodes along one LDM axis
 constexpr int kMaxNodes = 1024;     // max N_G * N_L (padded to even)
 constexpr int kPairGroup = 16;      // node pairs per Voigt-reduce work item
 constexpr int kMaxPasses = 16;
+// FFT radix plans merge the small factors into composite radices of at most
+// kFirstRadixMax in the first pass (no pass twiddles) and kMidRadixMax later:
+// the bounds under which the row kernels keep two pairs' butterflies in
+// registers without spilling
+constexpr int kFirstRadixMax = 12;
+constexpr int kMidRadixMax = 6;
 
 // --- host work over line arrays ------------------------------------------------
 // [0, n) in T contiguous chunks, chunk t = [n t / T, n (t + 1) / T): one per

@@ -120,13 +120,114 @@ __device__ __forceinline__ void dft8(float2* v) {
     v[7] = csub(e[3], o3);
 }
 
+// exp(-2 pi i M / N) at compile time: octant-free quadrant reduction of the
+// exact fraction M / N, then Taylor series on [0, pi/2) (double, ~1e-16)
+constexpr double kPiC = 3.14159265358979323846;
+__host__ __device__ constexpr double csin_q(double y) {
+    double t = y, s = y;
+    for (int k = 1; k < 14; ++k) {
+        t *= -y * y / ((2.0 * k) * (2.0 * k + 1.0));
+        s += t;
+    }
+    return s;
+}
+__host__ __device__ constexpr double ccos_q(double y) {
+    double t = 1.0, s = 1.0;
+    for (int k = 1; k < 14; ++k) {
+        t *= -y * y / ((2.0 * k - 1.0) * (2.0 * k));
+        s += t;
+    }
+    return s;
+}
+__host__ __device__ constexpr double ctw(int m, int n, bool sine) {
+    const int mm = ((m % n) + n) % n;
+    const int q = 4 * mm / n;                                  // quadrant
+    const double y = 2.0 * kPiC * (double)(4 * mm - q * n) / (4.0 * n);   // in [0, pi/2)
+    const double c = ccos_q(y), sn = csin_q(y);
+    if (!sine) return q == 0 ? c : q == 1 ? -sn : q == 2 ? -c : sn;
+    return q == 0 ? sn : q == 1 ? c : q == 2 ? -sn : -c;
+}
+template <int M, int N>
+struct TwConst {   // exp(-2 pi i M / N)
+    static constexpr float re = (float)ctw(M, N, false);
+    static constexpr float im = (float)-ctw(M, N, true);
+};
+template <int R>
+__device__ __forceinline__ void dftR(float2* v);
+
+// Stage 1 of a length-A B DFT, in place: for column n2 (N2), the A-point DFT
+// of v[B n1 + n2] over n1, each output k1 times exp(-2 pi i n2 k1 / (A B))
+// (compile-time constants), written back to v[B k1 + n2].
+template <int A, int B, int N2, int K1>
+__device__ __forceinline__ void twiddle_col(float2* v, const float2* t) {
+    if constexpr (K1 < A) {
+        constexpr int e = N2 * K1 % (A * B);
+        if constexpr (e == 0)
+            v[B * K1 + N2] = t[K1];
+        else
+            v[B * K1 + N2] = cmul(t[K1], make_float2(TwConst<e, A * B>::re, TwConst<e, A * B>::im));
+        twiddle_col<A, B, N2, K1 + 1>(v, t);
+    }
+}
+template <int A, int B, int N2>
+__device__ __forceinline__ void dft_stage1(float2* v) {
+    if constexpr (N2 < B) {
+        float2 t[A];
+#pragma unroll
+        for (int n1 = 0; n1 < A; ++n1) t[n1] = v[B * n1 + N2];
+        dftR<A>(t);
+        twiddle_col<A, B, N2, 0>(v, t);
+        dft_stage1<A, B, N2 + 1>(v);
+    }
+}
+
+// DFT of length A B in registers, natural order in and out (Cooley-Tukey,
+// n = B n1 + n2, k = k1 + A k2), in place: stage 1 above, then the B-point
+// DFTs of v[B k1 + n2] over n2 back into the same slots, which leaves
+// X[k1 + A k2] in v[B k1 + k2]; a compile-time register permutation restores
+// natural order.
+template <int A, int B>
+__device__ __forceinline__ void dftAB(float2* v) {
+    constexpr int N = A * B;
+    dft_stage1<A, B, 0>(v);
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) dftR<B>(v + B * k1);
+    float2 t[N];
+#pragma unroll
+    for (int r = 0; r < N; ++r) t[r] = v[B * (r % A) + r / A];
+#pragma unroll
+    for (int r = 0; r < N; ++r) v[r] = t[r];
+}
+
+// radices of the FFT plans: 2, 3, 4, 5, 8 and the composites 6, 9, 10, 12 of
+// the small factors
 template <int R>
 __device__ __forceinline__ void dftR(float2* v) {
-    if (R == 2) dft2(v);
-    if (R == 3) dft3(v);
-    if (R == 4) dft4(v);
-    if (R == 5) dft5(v);
-    if (R == 8) dft8(v);
+    if constexpr (R == 2) dft2(v);
+    else if constexpr (R == 3) dft3(v);
+    else if constexpr (R == 4) dft4(v);
+    else if constexpr (R == 5) dft5(v);
+    else if constexpr (R == 8) dft8(v);
+    else if constexpr (R == 6) dftAB<2, 3>(v);
+    else if constexpr (R == 9) dftAB<3, 3>(v);
+    else if constexpr (R == 10) dftAB<2, 5>(v);
+    else if constexpr (R == 12) dftAB<4, 3>(v);
+}
+// dispatch of a run-time radix to f(integral_constant<R>), instantiating only
+// the radices up to MAXR (other radices never reach the call)
+template <int MAXR = 12, class F>
+__device__ __forceinline__ void with_radix(int R, F&& f) {
+    switch (R) {
+        case 2: f(std::integral_constant<int, 2>()); break;
+        case 3: f(std::integral_constant<int, 3>()); break;
+        case 4: f(std::integral_constant<int, 4>()); break;
+        case 5: f(std::integral_constant<int, 5>()); break;
+        case 6: f(std::integral_constant<int, 6>()); break;
+        case 9: if constexpr (MAXR >= 9) f(std::integral_constant<int, 9>()); break;
+        case 10: if constexpr (MAXR >= 10) f(std::integral_constant<int, 10>()); break;
+        case 12: if constexpr (MAXR >= 12) f(std::integral_constant<int, 12>()); break;
+        default: f(std::integral_constant<int, 8>()); break;
+    }
 }
 
 // Multiply v[1..R-1] by w^r, w = tw[s] (tw[t] = exp(-2 pi i t / L)); three
@@ -150,7 +251,7 @@ __device__ __forceinline__ void twiddle(float2* v, const float2* __restrict__ tw
         v[2] = cmul(v[2], w2);
         v[3] = cmul(v[3], cmul(w1, w2));
         v[4] = cmul(v[4], cmul(w2, w2));
-    } else {
+    } else if (R == 8) {
         const float2 w2 = __ldg(&tw[2 * s]);
         const float2 w4 = __ldg(&tw[4 * s]);
         const float2 w3 = cmul(w1, w2);
@@ -161,6 +262,13 @@ __device__ __forceinline__ void twiddle(float2* v, const float2* __restrict__ tw
         v[5] = cmul(v[5], cmul(w1, w4));
         v[6] = cmul(v[6], cmul(w2, w4));
         v[7] = cmul(v[7], cmul(w3, w4));
+    } else {   // composite radix: w^r by products, from the table at every 4th power
+        float2 w = w1;
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+            if (r > 1) w = (r % 4 == 0) ? __ldg(&tw[r * s]) : cmul(w, w1);
+            v[r] = cmul(v[r], w);
+        }
     }
 }
 
@@ -196,13 +304,7 @@ __device__ __forceinline__ void row_pass(const float2* __restrict__ in, float2* 
 template <bool PIN, bool POUT>
 __device__ __forceinline__ void row_pass_r(int R, const float2* in, float2* out, int L, int Ns, unsigned mag,
                                            const float2* tw) {
-    switch (R) {
-        case 2: row_pass<2, PIN, POUT>(in, out, L, Ns, mag, tw); break;
-        case 3: row_pass<3, PIN, POUT>(in, out, L, Ns, mag, tw); break;
-        case 4: row_pass<4, PIN, POUT>(in, out, L, Ns, mag, tw); break;
-        case 5: row_pass<5, PIN, POUT>(in, out, L, Ns, mag, tw); break;
-        default: row_pass<8, PIN, POUT>(in, out, L, Ns, mag, tw); break;
-    }
+    with_radix(R, [&](auto rc) { row_pass<decltype(rc)::value, PIN, POUT>(in, out, L, Ns, mag, tw); });
 }
 
 // Forward DFT of one row in shared memory; buf0 holds the input (plain
@@ -838,48 +940,33 @@ struct TwShared {
 
 template <int R, int PAIRS, class TW>
 __device__ __forceinline__ void twiddleP(float2* A, float2* B, const TW& tw, int s) {
-    float2 w[R];
-    w[0] = make_float2(1.f, 0.f);
-    w[1] = tw(s);
-    if (R >= 3) w[2] = tw(2 * s);
-    if (R >= 4) w[3] = cmul(w[1], w[2]);
-    if (R == 5) w[4] = cmul(w[2], w[2]);
-    if (R == 8) {
-        w[4] = tw(4 * s);
-        w[5] = cmul(w[1], w[4]);
-        w[6] = cmul(w[2], w[4]);
-        w[7] = cmul(w[3], w[4]);
-    }
-#pragma unroll
-    for (int r = 1; r < R; ++r) {
-        A[r] = cmul(A[r], w[r]);
-        if (PAIRS == 2) B[r] = cmul(B[r], w[r]);
-    }
-}
-
-// first pass (sub-transform length 1): global rows -> (x four-step twiddle
-// from the per-row table twr, when TWR; otherwise the column stage applied
-// it) -> registers -> smem
-template <int R, int PAIRS, bool TWR>
-__device__ __forceinline__ void row_first(const float2* __restrict__ ya, const float2* __restrict__ yb,
-                                          const float2* twr, typename RowT<PAIRS>::E* out, int L) {
-    const int M = L / R;
-    for (int j = threadIdx.x; j < M; j += blockDim.x) {
-        float2 A[R], B[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            A[r] = __ldg(&ya[j + r * M]);
-            if (PAIRS == 2) B[r] = yb ? __ldg(&yb[j + r * M]) : make_float2(0.f, 0.f);
-            if (TWR) {
-                const float2 w = twr[j + r * M];
-                A[r] = cmul(A[r], w);
-                if (PAIRS == 2) B[r] = cmul(B[r], w);
-            }
+    if constexpr (R == 2 || R == 3 || R == 4 || R == 5 || R == 8) {
+        float2 w[R];
+        w[0] = make_float2(1.f, 0.f);
+        w[1] = tw(s);
+        if (R >= 3) w[2] = tw(2 * s);
+        if (R >= 4) w[3] = cmul(w[1], w[2]);
+        if (R == 5) w[4] = cmul(w[2], w[2]);
+        if (R == 8) {
+            w[4] = tw(4 * s);
+            w[5] = cmul(w[1], w[4]);
+            w[6] = cmul(w[2], w[4]);
+            w[7] = cmul(w[3], w[4]);
         }
-        dftR<R>(A);
-        if (PAIRS == 2) dftR<R>(B);
 #pragma unroll
-        for (int r = 0; r < R; ++r) out[RowT<PAIRS>::pad(j * R + r)] = RowT<PAIRS>::join(A[r], B[r]);
+        for (int r = 1; r < R; ++r) {
+            A[r] = cmul(A[r], w[r]);
+            if (PAIRS == 2) B[r] = cmul(B[r], w[r]);
+        }
+    } else {   // composite radix: w^r by products, from the table at every 4th power
+        const float2 w1 = tw(s);
+        float2 w = w1;
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+            if (r > 1) w = (r % 4 == 0) ? tw(r * s) : cmul(w, w1);
+            A[r] = cmul(A[r], w);
+            if (PAIRS == 2) B[r] = cmul(B[r], w);
+        }
     }
 }
 
@@ -937,6 +1024,9 @@ __device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_group
 
 // first pass from the staged rows (stage = [row a | row b], n2 each; row a
 // only for PAIRS = 1)
+// first pass (sub-transform length 1) from the staged rows: (x four-step
+// twiddle from the per-row table twr, when TWR; otherwise the column stage
+// applied it) -> registers -> smem
 template <int R, int PAIRS, bool TWR>
 __device__ __forceinline__ void row_first_staged(const float2* stage, bool two, const float2* twr,
                                                  typename RowT<PAIRS>::E* out, int L) {
@@ -965,6 +1055,7 @@ __device__ __forceinline__ void row_first_staged(const float2* stage, bool two, 
 // the first pass reads them from there (the buffers swap roles).
 template <int PAIRS, int MAXT, bool TWR, bool STAGE, bool TWS, bool SF>
 __global__ void __launch_bounds__(MAXT, MAXT <= 384 ? 2 : 1) k_row_fft_voigt(const VoigtArgs a) {
+    static_assert(STAGE || SF, "the forward row kernel stages its rows");
     using E = typename RowT<PAIRS>::E;
     extern __shared__ float4 sm4[];
     const int n2 = a.n2;
@@ -1012,40 +1103,20 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 384 ? 2 : 1) k_row_fft_voigt(con
             const float2* src = STAGE ? stage : reinterpret_cast<const float2*>(fbuf);
             stage_wait();
             __syncthreads();   // staged rows (and the twiddle tables) visible to all threads
-            switch (P.radix[0]) {
-                case 2: row_first_staged<2, PAIRS, TWR>(src, two, twr, wbuf, n2); break;
-                case 3: row_first_staged<3, PAIRS, TWR>(src, two, twr, wbuf, n2); break;
-                case 4: row_first_staged<4, PAIRS, TWR>(src, two, twr, wbuf, n2); break;
-                case 5: row_first_staged<5, PAIRS, TWR>(src, two, twr, wbuf, n2); break;
-                default: row_first_staged<8, PAIRS, TWR>(src, two, twr, wbuf, n2); break;
-            }
+            with_radix(P.radix[0], [&](auto rc) {
+                row_first_staged<decltype(rc)::value, PAIRS, TWR>(src, two, twr, wbuf, n2);
+            });
             __syncthreads();   // stage consumed: prefetch the next two rows under the remaining passes
             if (STAGE && j + 2 < j1) stage_group(stage, j + 2);
-        } else {
-            const float2* ya = row_ptr(j);
-            const float2* yb = two ? row_ptr(j + 1) : nullptr;
-            if (TWR && j == j0) __syncthreads();   // twr complete
-            switch (P.radix[0]) {
-                case 2: row_first<2, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
-                case 3: row_first<3, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
-                case 4: row_first<4, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
-                case 5: row_first<5, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
-                default: row_first<8, PAIRS, TWR>(ya, yb, twr, buf0, n2); break;
-            }
-            __syncthreads();
         }
         E* in = wbuf;
         E* out = fbuf;
         for (int p = 1; p < P.npass - 1; ++p) {
             const int Ns = P.ns[p];
             const unsigned mag = P.mag[p];
-            switch (P.radix[p]) {
-                case 2: row_mid<2, PAIRS, TwT>(in, out, n2, Ns, mag, twp); break;
-                case 3: row_mid<3, PAIRS, TwT>(in, out, n2, Ns, mag, twp); break;
-                case 4: row_mid<4, PAIRS, TwT>(in, out, n2, Ns, mag, twp); break;
-                case 5: row_mid<5, PAIRS, TwT>(in, out, n2, Ns, mag, twp); break;
-                default: row_mid<8, PAIRS, TwT>(in, out, n2, Ns, mag, twp); break;
-            }
+            with_radix<kMidRadixMax>(P.radix[p], [&](auto rc) {
+                row_mid<decltype(rc)::value, PAIRS, TwT>(in, out, n2, Ns, mag, twp);
+            });
             __syncthreads();
             E* t = in;
             in = out;
