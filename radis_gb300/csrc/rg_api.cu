@@ -827,7 +827,10 @@ bool plan_merge(const Work& W, const SpecHost& s, const VoigtArgs& va, GaussArgs
     // CO2 5M grid, <= ~8e-9 for the narrowest wide node (variance 4.2).
     double alpha_b = 0.0;
     {
-        const double kSigMin = 1.2, kTail = std::sqrt(2.0 * std::log(1e8));   // taps to 1e-8 of the peak
+        // residual taps out to 1e-6 of the kernel's peak (+-5.26 sigma): the mass
+        // beyond, erfc(5.26 / sqrt 2) = 1.4e-7 of the kernel, is below the FP32
+        // error of the synthesis (~1e-6 of the peak)
+        const double kSigMin = 1.2, kTail = std::sqrt(2.0 * std::log(1e6));
         auto sig = [&](int w) { return std::exp(g.log_wG_min + ga->wide_l[w] * g.dxG) / dv / (2.0 * std::sqrt(2.0 * kLn2)); };
         double smin = 1e300;
         for (int w = 0; w < ga->n_wide; ++w) smin = std::min(smin, sig(w));
