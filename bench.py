@@ -50,9 +50,12 @@ KERNELS_PER_STEP = 5   # plain layout: scatter, column FFT, row FFT + Voigt, inv
 
 
 def kernels_per_step(info):
-    """Kernels one spectrum launches: the plain five, or with the merged layout
-    the Gaussian stage and the merged-row column FFT instead of the column
-    FFT, plus a column FFT of the narrow-node rows when there are any."""
+    """Kernels one spectrum launches: the plain five; with the skeleton layout
+    the projection in addition; with the merged layout the Gaussian stage and
+    the merged-row column FFT instead of the column FFT, plus a column FFT of
+    the narrow-node rows when there are any."""
+    if int(info.layout) == 3:
+        return KERNELS_PER_STEP + 1
     if not info.merged_rows:
         return KERNELS_PER_STEP
     nlv = info.merged_rows + (info.merged_rows & 1)
@@ -174,7 +177,8 @@ def algorithmic_bytes(n_lines_read, line_bytes, n_nodes, n_v, n_ft, info):
     inverse stages read/write G and the output.  With the merged layout the
     Gaussian stage reads the wide-node LDM rows and writes the n_L merged rows
     (n_v + 2 ext points), and the column FFT reads those and the narrow-node
-    rows."""
+    rows.  With the skeleton layout the projection reads the node rows and
+    writes the skeleton rows, which the column FFT reads."""
     pairs = int(info.fft_rows or n_nodes) // 2
     out = {
         "k_scatter": n_lines_read * line_bytes + n_nodes * n_v * 4,
@@ -191,6 +195,11 @@ def algorithmic_bytes(n_lines_read, line_bytes, n_nodes, n_v, n_ft, info):
         merged = NL * (n_v + 2 * int(info.merged_ext)) * 4
         out["k_gauss_merge"] = wide_rows * n_v * 4 + merged
         out["k_col_fft_fwd"] = merged + n_narrow * NL * n_v * 4 + pairs * n_ft * 8
+    if int(info.layout) == 3:
+        rows = int(info.fft_rows)
+        real_nodes = int(info.grid.n_G) * int(info.grid.n_L)
+        out["k_node_project"] = real_nodes * n_v * 4 + rows * n_v * 4
+        out["k_col_fft_fwd"] = rows * n_v * 4 + pairs * n_ft * 8
     return out
 
 
@@ -651,9 +660,13 @@ def time_plan(plan, T, p, x, n_v, K, stream, warm=3):
 
 def kernel_times(stage_avg, gauss, info):
     """Per-kernel ms from the stage events: with the merged layout the column
-    stage is the Gaussian stage (its own event) followed by the column FFT."""
+    stage is the Gaussian stage (its own event) followed by the column FFT,
+    with the skeleton layout the projection followed by the column FFT."""
     kt = {STAGES[i]: stage_avg[i] for i in range(5)}
-    if info.merged_rows:
+    if int(info.layout) == 3:
+        kt["k_node_project"] = gauss
+        kt["k_col_fft_fwd"] = stage_avg[1] - gauss
+    elif info.merged_rows:
         kt["k_gauss_merge"] = gauss
         kt["k_col_fft_fwd"] = stage_avg[1] - gauss
     return kt
@@ -686,8 +699,9 @@ def run_c3(ctx, L, h2o_host, h2o, K, peak, peak_kind, workers, check=True):
         "scatter_roofline": {"achieved": sc_gbs, "peak": peak, "unit": "GB/s", "frac": sc_gbs / peak,
                              "peak_kind": peak_kind, "bytes_per_line": lb,
                              "lines_read": int(info.lines_in_window)},
-        "fft_layout": {"fft_rows": int(info.fft_rows), "merged_rows": int(info.merged_rows),
-                       "n_ft": int(g.n_ft)},
+        "fft_layout": {"layout": {1: "node rows", 2: "merged rows", 3: "skeleton rows"}.get(int(info.layout)),
+                       "fft_rows": int(info.fft_rows), "merged_rows": int(info.merged_rows),
+                       "n_ft": int(g.n_ft), "skeleton_sampled_err": float(info.layout_err)},
         "scatter_accumulator_bits": int(info.accum_bits),
     }
     if check:
@@ -829,15 +843,15 @@ def run_ours(args):
                          "avg_launch_ms": kt[name]},
             "stages": stages,
             "scatter_accumulator_bits": int(info.accum_bits),
-            "fft_layout": {"fft_rows": int(info.fft_rows), "merged_rows": int(info.merged_rows),
+            "fft_layout": {"layout": {1: "node rows", 2: "merged rows", 3: "skeleton rows"}.get(int(info.layout)),
+                           "fft_rows": int(info.fft_rows), "merged_rows": int(info.merged_rows),
                            "gauss_halfwidth": int(info.merged_ext), "n_ft": int(g.n_ft),
-                           "note": ("k_col_fft_fwd covers the real-space Gaussian stage of the merged "
-                                    "layout and the column FFTs")},
+                           "skeleton_sampled_err": float(info.layout_err)},
             "setup_s": setup_s,
         }
         if name == "k_gauss_merge":
             res["roofline"]["note"] = ("the real-space Gaussian stage is FP32-FMA-bound (a banded convolution of "
-                                       "each wide-node row with its residual Gaussian, ~220 FMA per merged "
+                                       "each wide-node row with its residual Gaussian, ~200 FMA per merged "
                                        "output point on the 8 wide nodes of this grid): frac is the HBM fraction "
                                        "of the bytes it must move")
         workers = os.cpu_count() or 1

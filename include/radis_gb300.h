@@ -52,7 +52,7 @@
 extern "C" {
 #endif
 
-#define RG_ABI_VERSION 2
+#define RG_ABI_VERSION 3
 
 enum rg_status {
     RG_OK = 0,
@@ -116,6 +116,16 @@ typedef struct {
      * loads only the window's lines, and far fewer nodes for a narrow window
      * of a wide list */
     int32_t axes_window;
+    /* FFT-stage layout (none changes what is computed, only how): 0 = the
+     * one that transforms the fewest rows; 1 = every node row; 2 = merged
+     * rows where the grid allows it (wide Gaussian nodes convolved in real
+     * space and summed per wL node), else 1; 3 = skeleton rows where the
+     * grid allows it (the node rows projected onto the few nodes whose
+     * lineshape transforms span all the others within layout_tol), else 0 */
+    int32_t layout;
+    /* skeleton layout: largest error allowed in any node's normalised
+     * lineshape transform (peak 1); <= 0 -> 1e-8 */
+    double layout_tol;
 } rg_plan_desc;
 
 /* Gas conditions of one spectrum.  Pressure in bar (as the reference API);
@@ -142,15 +152,22 @@ typedef struct {
     float stage_ms[6];         /* scatter, fft-col, fft-row+voigt, ifft-row,
                                   ifft-col, total (filled when timing != 0)    */
     int64_t lines_in_window;   /* lines whose k0 >= 0 and k0+1 < n_v          */
-    /* layout of the FFT stage: rows transformed (node rows, or with the merged
-     * layout n_L merged rows + the narrow-Gaussian node rows), how many of them
-     * are merged rows and the half-width (points) of their widest Gaussian */
+    /* layout of the FFT stage: rows transformed (node rows; with the merged
+     * layout n_L merged rows + the narrow-Gaussian node rows; with the
+     * skeleton layout the skeleton rows), how many of them are merged rows
+     * and the half-width (points) of their widest Gaussian */
     int32_t fft_rows, merged_rows, merged_ext;
-    float gauss_ms;            /* merged layout: the real-space Gaussian stage's
-                                  part of stage_ms[1] (timing = 1), else 0     */
+    float gauss_ms;            /* the real-space stage before the column FFT
+                                  (merged layout: the Gaussian stage; skeleton
+                                  layout: the projection), part of
+                                  stage_ms[1] (timing = 1), else 0             */
     int32_t accum_bits;        /* the scatter's accumulator: 32 or 64 bits, or
                                   0 when it was chosen on the device (served
                                   and allocation-free spectra in auto mode)    */
+    int32_t layout;            /* FFT-stage layout used: 1 node rows, 2 merged
+                                  rows, 3 skeleton rows (fft_rows of them)     */
+    float layout_err;          /* skeleton layout: the largest error of the
+                                  decomposition over its frequency samples     */
 } rg_spectrum_info;
 
 int rg_abi_version(void);
@@ -176,6 +193,17 @@ int rg_plan_grid(rg_plan* plan, const rg_conditions* cond, rg_grid* out);
  * request before any device memory is touched. */
 int rg_grid_estimate(const rg_line_arrays* lines, const rg_isotopes* iso, const rg_plan_desc* desc,
                      const rg_conditions* cond, rg_grid* out);
+
+/* Host-only, no device needed: the skeleton layout (rg_plan_desc.layout 3)
+ * of a node grid at spacing dv: the n = n_G n_L nodes' folded, normalised
+ * lineshape transforms (folding_thresh <= 0 -> 1e-6) written as combinations
+ * of at most r_max of them within tol (<= 0 -> 1e-8) at every frequency
+ * sample.  nodes[r], r < *n_rows: node index l n_L + m of skeleton row r;
+ * coef[r n + node] (capacity r_max n): its coefficient for every node;
+ * *err: the largest sampled error.  RG_ERR_RANGE when r_max rows fall short
+ * of tol.  The same decomposition a plan makes for each spectrum. */
+int rg_grid_skeleton(const rg_grid* grid, double dv, double folding_thresh, double tol, int32_t r_max,
+                     int32_t* n_rows, int32_t* nodes, double* coef, double* err);
 
 /* Host-only, no device needed: HITRAN-2004 160-character records -> columns.
  * `text`: the file's bytes (ASCII).  A record ends at "\n", "\r\n" or "\r";

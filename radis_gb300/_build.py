@@ -17,7 +17,7 @@ CSRC = os.path.join(PKG, "csrc")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 BUILD = os.path.join(os.path.dirname(PKG), "_build")
 LIB = os.path.join(PKG, "libradisgb.so")
-SOURCES = ["rg_kernels.cu", "rg_api.cu", "rg_hull.cpp", "rg_partition.cpp", "rg_hitran.cpp"]
+SOURCES = ["rg_kernels.cu", "rg_api.cu", "rg_hull.cpp", "rg_skeleton.cpp", "rg_partition.cpp", "rg_hitran.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -22,6 +22,7 @@ STATUS = {1: "RG_ERR_ARG", 2: "RG_ERR_CUDA", 3: "RG_ERR_OOM", 4: "RG_ERR_UNSORTE
 EXPORTS = [
     "rg_abi_version", "rg_last_error", "rg_ctx_create", "rg_ctx_destroy", "rg_lines_upload",
     "rg_lines_free", "rg_lines_count", "rg_plan_create", "rg_plan_free", "rg_plan_grid", "rg_grid_estimate",
+    "rg_grid_skeleton",
     "rg_synthesize", "rg_synthesize_host", "rg_debug_ldm", "rg_plan_stage_times",
     "rg_server_create", "rg_server_submit", "rg_server_wait", "rg_server_stats_get", "rg_server_destroy",
     "rg_synthesize_static", "rg_backward", "rg_jvp", "rg_synthesize_quantities",
@@ -60,7 +61,7 @@ class PlanDesc(C.Structure):
     _fields_ = [("vmin", C.c_double), ("dv", C.c_double), ("n_v", C.c_int64),
                 ("dxG", C.c_double), ("dxL", C.c_double), ("n_G", C.c_int), ("n_L", C.c_int),
                 ("folding_thresh", C.c_double), ("n_ft", C.c_int64), ("accumulator", C.c_int32),
-                ("axes_window", C.c_int32)]
+                ("axes_window", C.c_int32), ("layout", C.c_int32), ("layout_tol", C.c_double)]
 
 
 class Conditions(C.Structure):
@@ -81,7 +82,8 @@ class Grid(C.Structure):
 class SpectrumInfo(C.Structure):
     _fields_ = [("grid", Grid), ("log_scale", C.c_double), ("stage_ms", C.c_float * 6),
                 ("lines_in_window", C.c_int64), ("fft_rows", C.c_int32), ("merged_rows", C.c_int32),
-                ("merged_ext", C.c_int32), ("gauss_ms", C.c_float), ("accum_bits", C.c_int32)]
+                ("merged_ext", C.c_int32), ("gauss_ms", C.c_float), ("accum_bits", C.c_int32),
+                ("layout", C.c_int32), ("layout_err", C.c_float)]
 
 
 class Request(C.Structure):
@@ -125,6 +127,8 @@ def load(path: str | None = None):
         "rg_plan_grid": ([vp, C.POINTER(Conditions), C.POINTER(Grid)], C.c_int),
         "rg_grid_estimate": ([C.POINTER(LineArrays), C.POINTER(Isotopes), C.POINTER(PlanDesc),
                               C.POINTER(Conditions), C.POINTER(Grid)], C.c_int),
+        "rg_grid_skeleton": ([C.POINTER(Grid), C.c_double, C.c_double, C.c_double, C.c_int32,
+                              C.POINTER(C.c_int32), vp, vp, C.POINTER(C.c_double)], C.c_int),
         "rg_synthesize": ([vp, C.POINTER(Conditions), vp, vp, C.c_int, C.POINTER(SpectrumInfo)], C.c_int),
         "rg_synthesize_host": ([vp, C.POINTER(Conditions), vp, vp, C.c_int, C.POINTER(SpectrumInfo)],
                                C.c_int),
@@ -333,16 +337,19 @@ class Plan:
 
     def __init__(self, lines: Lines, vmin: float, dv: float, n_v: int, dxG=None, dxL=None,
                  n_G=None, n_L=None, folding_thresh: float = 1e-6, n_ft: int = 0, accumulator: int = 0,
-                 axes_window: bool = False):
+                 axes_window: bool = False, layout: int = 0, layout_tol: float = 0.0):
         """``accumulator``: fixed-point width of the scatter (0: from the
         densest grid column, 32 or 64: forced).  ``axes_window``: the Gaussian
         node axis spans only the lines that can reach the window (instead of
-        the whole list)."""
+        the whole list).  ``layout``: rows of the FFT stage (0: the fewest,
+        1: node rows, 2: merged rows where possible, 3: skeleton rows where
+        possible); ``layout_tol``: the skeleton decomposition's error bound
+        (0: 1e-8)."""
         lib = load()
         self.lines = lines
         d = PlanDesc(float(vmin), float(dv), int(n_v), float(dxG or 0.0), float(dxL or 0.0),
                      int(n_G or 0), int(n_L or 0), float(folding_thresh), int(n_ft), int(accumulator),
-                     1 if axes_window else 0)
+                     1 if axes_window else 0, int(layout), float(layout_tol))
         h = C.c_void_p()
         check(lib.rg_plan_create(lines.handle, C.byref(d), C.byref(h)))
         self._h = h
@@ -536,6 +543,20 @@ def grid_estimate(lines: dict, molar_mass, vmin, dv, n_v, T, p_bar, x, dxG=None,
     return g
 
 
+def grid_skeleton(grid: Grid, dv: float, folding_thresh: float = 1e-6, tol: float = 0.0, r_max: int = 64):
+    """Host-only (no GPU): the skeleton layout of a node grid
+    (rg_grid_skeleton).  Returns (nodes int32[R], coef float64[R, n_G n_L],
+    largest sampled error)."""
+    n = int(grid.n_G) * int(grid.n_L)
+    r_max = max(1, min(int(r_max), n))
+    nodes = np.zeros(r_max, np.int32)
+    coef = np.zeros((r_max, n), np.float64)
+    R, err = C.c_int32(), C.c_double()
+    check(load().rg_grid_skeleton(C.byref(grid), float(dv), float(folding_thresh), float(tol), r_max,
+                                  C.byref(R), nodes.ctypes.data, coef.ctypes.data, C.byref(err)))
+    return nodes[:R.value].copy(), coef[:R.value].copy(), err.value
+
+
 class Server:
     """Continuous-batching spectrum server over resident line lists
     (rg_server_*): ``submit`` queues a request and returns a ticket at once;
@@ -557,7 +578,8 @@ class Server:
         return self._h
 
     def submit(self, lines: Lines, vmin, dv, n_v, T, p_bar, x, dxG=None, dxL=None, n_G=None,
-               n_L=None, q_ratio=None, out=None, folding_thresh=1e-6, accumulator=0, axes_window=False) -> int:
+               n_L=None, q_ratio=None, out=None, folding_thresh=1e-6, accumulator=0, axes_window=False,
+               layout=0, layout_tol=0.0) -> int:
         if out is None:
             out = np.empty(int(n_v), dtype=np.float32)
         q = None if q_ratio is None else np.ascontiguousarray(
@@ -565,7 +587,7 @@ class Server:
         req = Request(lines.handle.value,
                       PlanDesc(float(vmin), float(dv), int(n_v), float(dxG or 0.0), float(dxL or 0.0),
                                int(n_G or 0), int(n_L or 0), float(folding_thresh), 0, int(accumulator),
-                               1 if axes_window else 0),
+                               1 if axes_window else 0, int(layout), float(layout_tol)),
                       Conditions(float(T), float(p_bar), float(x), ptr(q)), out.ctypes.data)
         t = C.c_int64()
         check(load().rg_server_submit(self.handle, C.byref(req), C.byref(t)))

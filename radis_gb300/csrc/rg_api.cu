@@ -164,6 +164,15 @@ struct Work {
     float* mrow = nullptr;
     size_t mrow_bytes = 0;
     int last_fft_rows = 0, last_merged_rows = 0, last_ext = 0;   // layout of the last spectrum
+    int last_layout = 0;              // 1 node rows, 2 merged rows, 3 skeleton rows
+    double last_layout_err = 0.0;     // skeleton layout: the decomposition's sampled error
+    // skeleton layout: projection coefficients [n_nodes][rows_pad] (device,
+    // grow-only) and their host staging (copied from pageable memory: the
+    // copy has left this buffer when cudaMemcpyAsync returns)
+    bool allow_skeleton = true;
+    float* proj_coef = nullptr;
+    size_t proj_bytes = 0;
+    std::vector<float> proj_host;
     int last_accum = 0;               // accumulator bits of the last scatter (0: chosen on the device)
     int64_t row_stride = 0;
     float* ldm = nullptr;             // LDM [node][row_stride] (the scatter's float values)
@@ -387,6 +396,17 @@ void dfree(T*& p) {
 
 // Per-spectrum host parameters (the reference's set_pTQ / set_G_params /
 // set_L_params, radis/gpu/params.py:89-155).
+// The plan options that select how, not what, is computed.
+int check_desc_options(const rg_plan_desc& d) {
+    if (d.accumulator != 0 && d.accumulator != 32 && d.accumulator != 64)
+        return fail(RG_ERR_ARG, "accumulator must be 0, 32 or 64 (got %d)", (int)d.accumulator);
+    if (d.axes_window != 0 && d.axes_window != 1)
+        return fail(RG_ERR_ARG, "axes_window must be 0 or 1 (got %d)", (int)d.axes_window);
+    if (d.layout < 0 || d.layout > 3) return fail(RG_ERR_ARG, "layout must be 0..3 (got %d)", (int)d.layout);
+    if (!(d.layout_tol < 1e-2)) return fail(RG_ERR_ARG, "layout_tol must be < 1e-2 (got %g)", d.layout_tol);
+    return RG_OK;
+}
+
 struct SpecHost {
     rg_grid grid;
     double p_atm, log_scale_int, log_scale_out;
@@ -893,6 +913,119 @@ bool plan_merge(const Work& W, const SpecHost& s, const VoigtArgs& va, GaussArgs
 // n_L; the narrow rows are read from the LDM by the column FFT directly)
 int NL_merged(const GaussArgs& ga) { return ga.NLv; }
 
+// Skeleton layout of one spectrum (interp_decomp, rg_skeleton.cpp): the
+// folded, normalised Voigt transform of every node, sampled at S frequencies
+// f_j = (j / (S - 1))^2 / (2 dv) (dense where the wide nodes' transforms
+// live; the largest error over the whole DFT grid stays within a few percent
+// of the sampled one on the grids tried), is decomposed on the host in FP64.
+// Succeeds when at most r_max skeleton rows (rounded up to even) reproduce
+// every node's transform within tol; fills the row kernel's arguments (row r
+// = skeleton node sk[r], with its own transform) and the projection
+// coefficients [n_nodes][rows_pad] in W.proj_host.
+constexpr int kSkelSamples = 48;
+constexpr double kSkelTol = 1e-8;
+
+// The decomposition itself (host only): skeleton nodes sk[0, R) and
+// coefficients C[r * n + node] for the n = n_G n_L nodes of grid g.
+int skeleton_decomp(const rg_grid& g, double dv, double thresh, double tol, int r_max, std::vector<int>* sk,
+                    std::vector<double>* C, int* R, double* err) {
+    const int n = g.n_G * g.n_L;
+    const double h = 0.5 / dv;
+    constexpr int S = kSkelSamples;
+    double f[S];
+    for (int j = 0; j < S; ++j) f[j] = h * std::pow((double)j / (S - 1), 2);
+    std::vector<int> nf(n);
+    std::vector<double> nrm(n);
+    int qmax = 0;
+    for (int node = 0; node < n; ++node) {
+        const int l = node / g.n_L, m = node % g.n_L;
+        node_fold(dv, std::exp(g.log_wG_min + l * g.dxG), std::exp(g.log_wL_min + m * g.dxL), thresh, &nf[node],
+                  &nrm[node]);
+        qmax = std::max(qmax, nf[node]);
+    }
+    // separable factors per folded copy q, at the copy's frequency
+    // q h + (q odd ? h - f : f) (broadening.py:1914-1926)
+    std::vector<double> Gt((size_t)(qmax + 1) * g.n_G * S), Lt((size_t)(qmax + 1) * g.n_L * S);
+    for (int q = 0; q <= qmax; ++q)
+        for (int j = 0; j < S; ++j) {
+            const double fq = q == 0 ? f[j] : q * h + ((q & 1) ? h - f[j] : f[j]);
+            for (int l = 0; l < g.n_G; ++l) {
+                const double wG = std::exp(g.log_wG_min + l * g.dxG);
+                Gt[((size_t)q * g.n_G + l) * S + j] = std::exp(-std::pow(kPi * fq * wG, 2) / (4.0 * kLn2));
+            }
+            for (int m = 0; m < g.n_L; ++m) {
+                const double wL = std::exp(g.log_wL_min + m * g.dxL);
+                Lt[((size_t)q * g.n_L + m) * S + j] = std::exp(-kPi * fq * wL);
+            }
+        }
+    std::vector<double> A((size_t)n * S);
+    for (int node = 0; node < n; ++node) {
+        const int l = node / g.n_L, m = node % g.n_L;
+        double* a = &A[(size_t)node * S];
+        for (int j = 0; j < S; ++j) {
+            double v = 0.0;
+            for (int q = 0; q <= nf[node]; ++q)
+                v += Gt[((size_t)q * g.n_G + l) * S + j] * Lt[((size_t)q * g.n_L + m) * S + j];
+            a[j] = v * nrm[node];
+        }
+    }
+    sk->assign(r_max, 0);
+    C->assign((size_t)r_max * n, 0.0);
+    return interp_decomp(A.data(), S, n, tol, r_max, sk->data(), C->data(), R, err);
+}
+
+bool plan_skeleton(Work& W, const SpecHost& s, const VoigtArgs& va, int r_max, VoigtArgs* vk, ProjArgs* pa,
+                   double* err_out) {
+    const rg_grid& g = s.grid;
+    const int n = g.n_G * g.n_L;
+    r_max = std::min(r_max, kProjMaxRows);
+    if (!W.allow_skeleton || n < 4 || r_max < 2) return false;
+    const double thresh = W.desc.folding_thresh > 0 ? W.desc.folding_thresh : 1e-6;
+    const double tol = W.desc.layout_tol > 0 ? W.desc.layout_tol : kSkelTol;
+    std::vector<int> sk;
+    std::vector<double> C;
+    int R = 0;
+    double err = 0.0;
+    if (skeleton_decomp(g, W.desc.dv, thresh, tol, r_max, &sk, &C, &R, &err) != RG_OK) return false;
+    const int rows = R + (R & 1);
+    if (R < 1 || rows > r_max) return false;
+    const int rp = proj_rows_pad(rows);
+    if ((size_t)n * rp * sizeof(float) > 96 * 1024) return false;   // coefficients in shared memory
+    W.proj_host.assign((size_t)n * rp, 0.f);
+    for (int r = 0; r < R; ++r)
+        for (int node = 0; node < n; ++node) W.proj_host[(size_t)node * rp + r] = (float)C[(size_t)r * n + node];
+    *vk = va;
+    vk->rowwise = 1;
+    vk->n_nodes = rows;
+    vk->n_pairs = rows / 2;
+    vk->any_fold = 0;
+    for (int r = 0; r < rows; ++r) {
+        if (r < R) {
+            const int node = sk[r];
+            vk->alpha[r] = va.alpha[node / g.n_L];
+            vk->beta[r] = va.beta[node % g.n_L];
+            vk->norm[r] = va.norm[node];
+            vk->lnorm[r] = va.lnorm[node];
+            vk->nfold[r] = va.nfold[node];
+            if (va.nfold[node]) vk->any_fold = 1;
+        } else {   // zero pad row
+            vk->alpha[r] = vk->beta[r] = 0.f;
+            vk->norm[r] = 0.f;
+            vk->lnorm[r] = -std::numeric_limits<float>::infinity();
+            vk->nfold[r] = 0;
+        }
+    }
+    std::memset(pa, 0, sizeof *pa);
+    pa->ldm = W.ldm;
+    pa->row_stride = W.row_stride;
+    pa->n_v = (int)W.desc.n_v;
+    pa->n_nodes = n;   // the pad node row of an odd grid is not read
+    pa->rows = rows;
+    pa->rows_pad = rp;
+    *err_out = err;
+    return true;
+}
+
 // After a synchronisation: report (once) a bounded device wait that gave up.
 int take_err(Work& W) {
     if (*W.err_host) {
@@ -965,12 +1098,43 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
         auto vm = std::make_unique<VoigtArgs>();
         auto ga = std::make_unique<GaussArgs>();
         fill_voigt_args(W, s, va.get());
+        // layout: node rows, merged rows or skeleton rows (rg_plan_desc.layout)
+        const int lay = W.desc.layout;
         int m_rows = 0;
-        const bool merged = plan_merge(W, s, *va, ga.get(), vm.get(), &m_rows);
-        W.last_fft_rows = merged ? m_rows : s.n_nodes;
+        bool merged = lay != 1 && lay != 3 && plan_merge(W, s, *va, ga.get(), vm.get(), &m_rows);
+        auto vk = std::make_unique<VoigtArgs>();
+        ProjArgs pa;
+        double sk_err = 0.0;
+        const int alt_rows = merged ? m_rows : s.n_nodes;
+        const bool skel = (lay == 0 || lay == 3) &&
+                          plan_skeleton(W, s, *va, lay == 3 ? kProjMaxRows : merged ? alt_rows : 3 * alt_rows / 4,
+                                        vk.get(), &pa, &sk_err);
+        if (skel) merged = false;
+        else if (lay == 3) merged = plan_merge(W, s, *va, ga.get(), vm.get(), &m_rows);
+        W.last_layout = skel ? 3 : merged ? 2 : 1;
+        W.last_layout_err = skel ? sk_err : 0.0;
+        W.last_fft_rows = skel ? pa.rows : merged ? m_rows : s.n_nodes;
         W.last_merged_rows = merged ? ga->NL : 0;
         W.last_ext = merged ? ga->ext : 0;
-        if (merged) {
+        if (skel) {
+            const size_t need = sizeof(float) * W.proj_host.size();
+            if (need > W.proj_bytes) {
+                if (W.proj_coef) CU(cudaFreeAsync(W.proj_coef, st));
+                W.proj_coef = nullptr;
+                W.proj_bytes = 0;
+                const size_t want = std::max<size_t>(need, 64 * 1024);
+                CU(cudaMallocAsync((void**)&W.proj_coef, want, st));
+                W.proj_bytes = want;
+            }
+            // pageable source: staged before the call returns, so the host
+            // vector may be refilled by the next spectrum at once
+            CU(cudaMemcpyAsync(W.proj_coef, W.proj_host.data(), need, cudaMemcpyHostToDevice, st));
+            pa.coef = W.proj_coef;
+            RG(launch_node_project(pa, st));
+            if (ev) CU(cudaEventRecord(ev[6], st));
+            ca.n_pairs = pa.rows / 2;
+            RG(launch_col_fft_fwd(ca, st));
+        } else if (merged) {
             const size_t need = sizeof(float) * (size_t)NL_merged(*ga) * (size_t)ga->out_stride;
             if (need > W.mrow_bytes) {
                 const size_t want = std::max(need, (size_t)(W.mrow_bytes * 1.25));
@@ -1006,7 +1170,7 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
             RG(launch_col_fft_fwd(ca, st));
         }
         if (ev) CU(cudaEventRecord(ev[2], st));
-        VoigtArgs& vr = merged ? *vm : *va;
+        VoigtArgs& vr = skel ? *vk : merged ? *vm : *va;
         vr.store_g = vr.n_pairs <= kPairGroup;   // one pair group per row: it stores G itself
         if (!vr.store_g) CU(cudaMemsetAsync(W.g, 0, sizeof(float2) * (size_t)W.n, st));
         RG(launch_row_fft_voigt(vr, st));
@@ -1227,6 +1391,8 @@ int run_spectrum(rg_plan* P, const rg_conditions* c, float* out, cudaStream_t st
         info->merged_rows = ldm_only ? 0 : P->w.last_merged_rows;
         info->merged_ext = ldm_only ? 0 : P->w.last_ext;
         info->accum_bits = P->w.last_accum;
+        info->layout = ldm_only ? 0 : P->w.last_layout;
+        info->layout_err = ldm_only ? 0.f : (float)P->w.last_layout_err;
     }
     if (timing == 1 && info) {
         CU(cudaStreamSynchronize(st));
@@ -1470,10 +1636,7 @@ int rg_plan_create(rg_lines* L, const rg_plan_desc* d, rg_plan** out) {
     if (d->n_v > (int64_t)1 << 30) return fail(RG_ERR_RANGE, "n_v too large");
     if (!((d->n_G > 1) || d->dxG > 0) || !((d->n_L > 1) || d->dxL > 0))
         return fail(RG_ERR_ARG, "give dxG/dxL > 0 or node counts n_G/n_L > 1");
-    if (d->accumulator != 0 && d->accumulator != 32 && d->accumulator != 64)
-        return fail(RG_ERR_ARG, "accumulator must be 0, 32 or 64 (got %d)", (int)d->accumulator);
-    if (d->axes_window != 0 && d->axes_window != 1)
-        return fail(RG_ERR_ARG, "axes_window must be 0 or 1 (got %d)", (int)d->axes_window);
+    RG(check_desc_options(*d));
     DeviceGuard dev_guard_;
     CU(dev_guard_.use(L->ctx->device));
     auto* P = new (std::nothrow) rg_plan();
@@ -1536,6 +1699,8 @@ void free_work(Work& W) {
     W.ldm_bytes = W.y_bytes = 0;
     dfree(W.mrow);
     W.mrow_bytes = 0;
+    dfree(W.proj_coef);
+    W.proj_bytes = 0;
 }
 
 int rg_plan_free(rg_plan* P) {
@@ -1592,6 +1757,32 @@ int rg_grid_estimate(const rg_line_arrays* lines, const rg_isotopes* iso, const 
     SpecHost s;
     RG(compute_grid_env(*env, nullptr, *d, (int64_t)n1 * n2, n1, n2, c, &s));
     *out = s.grid;
+    return RG_OK;
+}
+
+int rg_grid_skeleton(const rg_grid* grid, double dv, double folding_thresh, double tol, int32_t r_max,
+                     int32_t* n_rows, int32_t* nodes, double* coef, double* err) {
+    g_err.clear();
+    if (!grid || !n_rows || !nodes || !coef || !err) return fail(RG_ERR_ARG, "NULL argument");
+    if (!(dv > 0)) return fail(RG_ERR_ARG, "dv must be > 0");
+    if (grid->n_G < 1 || grid->n_L < 1 || grid->n_G * grid->n_L > kMaxNodes)
+        return fail(RG_ERR_RANGE, "grid %d x %d outside 1..%d nodes", grid->n_G, grid->n_L, kMaxNodes);
+    if (r_max < 1 || r_max > grid->n_G * grid->n_L)
+        return fail(RG_ERR_ARG, "r_max must be in 1..n_G n_L (got %d)", (int)r_max);
+    if (!(tol < 1e-2)) return fail(RG_ERR_ARG, "tol must be < 1e-2 (got %g)", tol);
+    const int n = grid->n_G * grid->n_L;
+    std::vector<int> sk;
+    std::vector<double> C;
+    int R = 0;
+    double e = 0.0;
+    const int rc = skeleton_decomp(*grid, dv, folding_thresh > 0 ? folding_thresh : 1e-6, tol > 0 ? tol : kSkelTol,
+                                   r_max, &sk, &C, &R, &e);
+    *n_rows = R;
+    *err = e;
+    if (rc == RG_ERR_RANGE) return fail(RG_ERR_RANGE, "%d skeleton rows leave a sampled error of %g > %g", R, e, tol);
+    RG(rc);
+    for (int r = 0; r < R; ++r) nodes[r] = sk[r];
+    std::copy(C.begin(), C.begin() + (size_t)R * n, coef);
     return RG_OK;
 }
 
@@ -2020,6 +2211,9 @@ void release_slot_buffers(Slot& sl) {
     if (sl.w.mrow) cudaFreeAsync(sl.w.mrow, sl.st);
     sl.w.mrow = nullptr;
     sl.w.mrow_bytes = 0;
+    if (sl.w.proj_coef) cudaFreeAsync(sl.w.proj_coef, sl.st);
+    sl.w.proj_coef = nullptr;
+    sl.w.proj_bytes = 0;
     sl.w.nodes_cap = 0;
     sl.w.ldm_bytes = sl.w.y_bytes = 0;
     sl.out_cap = sl.col_cap = sl.g_cap = 0;
@@ -2064,6 +2258,8 @@ int start_on_slot(rg_server* S, int si, const std::shared_ptr<ServerReq>& r, con
     r->info.merged_rows = W.last_merged_rows;
     r->info.merged_ext = W.last_ext;
     r->info.accum_bits = W.last_accum;
+    r->info.layout = W.last_layout;
+    r->info.layout_err = (float)W.last_layout_err;
     sl.notified.store(false);
     auto* hn = new HostNote{S, si};
     CU(cudaLaunchHostFunc(sl.st, slot_done_cb, hn));
@@ -2252,10 +2448,7 @@ int rg_server_submit(rg_server* S, const rg_request* req, int64_t* ticket) {
     if (!(d.dv > 0) || d.n_v < 2 || d.n_v > ((int64_t)1 << 30)) return fail(RG_ERR_ARG, "bad grid");
     if (!((d.n_G > 1) || d.dxG > 0) || !((d.n_L > 1) || d.dxL > 0))
         return fail(RG_ERR_ARG, "give dxG/dxL > 0 or node counts n_G/n_L > 1");
-    if (d.accumulator != 0 && d.accumulator != 32 && d.accumulator != 64)
-        return fail(RG_ERR_ARG, "accumulator must be 0, 32 or 64 (got %d)", (int)d.accumulator);
-    if (d.axes_window != 0 && d.axes_window != 1)
-        return fail(RG_ERR_ARG, "axes_window must be 0 or 1 (got %d)", (int)d.axes_window);
+    RG(check_desc_options(d));
     auto r = std::make_shared<ServerReq>();
     r->lines = req->lines;
     r->desc = d;
@@ -2409,10 +2602,7 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
     if (!(d->dv > 0) || d->n_v < 2 || d->n_v > ((int64_t)1 << 30)) return fail(RG_ERR_ARG, "bad grid");
     if (!((d->n_G > 1) || d->dxG > 0) || !((d->n_L > 1) || d->dxL > 0))
         return fail(RG_ERR_ARG, "give dxG/dxL > 0 or node counts n_G/n_L > 1");
-    if (d->accumulator != 0 && d->accumulator != 32 && d->accumulator != 64)
-        return fail(RG_ERR_ARG, "accumulator must be 0, 32 or 64 (got %d)", (int)d->accumulator);
-    if (d->axes_window != 0 && d->axes_window != 1)
-        return fail(RG_ERR_ARG, "axes_window must be 0 or 1 (got %d)", (int)d->axes_window);
+    RG(check_desc_options(*d));
     const int dev = L->ctx->device;
     if (dev < 0 || dev >= 64) return fail(RG_ERR_ARG, "device ordinal %d not supported", dev);
     std::lock_guard<std::mutex> lk(g_static_mu);
@@ -2467,8 +2657,10 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
     W.tw_hi = twh;
     W.tw_lo = twl;
     // sized here: the workspace step finds them large enough and allocates nothing;
-    // the merged layout (its own row buffer) is not used on this path
+    // the merged and skeleton layouts (their own device buffers) are not used
+    // on this path
     W.allow_merge = false;
+    W.allow_skeleton = false;
     W.ldm_bytes = sizeof(float) * (size_t)s.n_nodes * (size_t)W.row_stride;
     W.y_bytes = sizeof(float2) * (size_t)(s.n_nodes / 2) * (size_t)W.n;
     W.ldm = static_cast<float*>(take(W.ldm_bytes));
@@ -2514,6 +2706,7 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
         info->lines_in_window = -1;
         info->fft_rows = W.last_fft_rows;
         info->accum_bits = W.last_accum;
+        info->layout = W.last_layout;
     }
     return RG_OK;
 }

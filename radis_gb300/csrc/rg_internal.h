@@ -231,6 +231,7 @@ struct VoigtArgs {        // K3 (row FFT + Voigt weights + pair reduction)
     float lnorm[kMaxNodes];   // log2(norm) (-inf for padding node)
     unsigned char nfold[kMaxNodes];
     int any_fold;
+    int rowwise;          // 1: row r's transform uses alpha[r], beta[r] (skeleton rows, r < kMaxAxis)
 };
 
 struct RowIfftArgs {      // K3b (inverse row FFT + twiddle, in place)
@@ -247,6 +248,21 @@ struct RowIfftArgs {      // K3b (inverse row FFT + twiddle, in place)
 // their Gaussian kernel and summed into one row per wL node (the other,
 // narrow-Gaussian node rows stay in the LDM).  Output rows [m][out_stride]
 // hold k in [-ext, n_v + ext) at offset k + ext.
+// Skeleton layout: the LDM rows projected, in place, onto the rows of a few
+// skeleton nodes whose transforms span every node's (interp_decomp):
+// row r (r < rows) <- sum_n coef[n * rows_pad + r] x row n, column by column;
+// rows [R, rows) of an odd R are the zero pad row.
+constexpr int kProjMaxRows = 64;
+struct ProjArgs {
+    float* ldm;           // LDM [node][row_stride], rows [0, rows) overwritten
+    int64_t row_stride;
+    int n_v;
+    int n_nodes;          // rows read
+    int rows;             // rows written (R rounded up to even)
+    int rows_pad;         // coefficient row pitch (the kernel's row block)
+    const float* coef;    // [n_nodes][rows_pad]
+};
+
 constexpr int kGaussPer = 8;          // outputs per thread
 constexpr int kGaussTile = 256 * kGaussPer;   // outputs per CTA (256 threads)
 constexpr int kGaussMaxK = 256;       // widest kernel half-width (points)
@@ -361,6 +377,14 @@ int launch_row_ifft_adj(const AdjRowArgs& a, cudaStream_t st);
 int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st);
 int launch_gather_grad(const GradArgs& a, int grid, cudaStream_t st);
 int launch_gauss_merge(const GaussArgs& a, int out_rows, cudaStream_t st);
+int proj_rows_pad(int rows);         // coefficient pitch of launch_node_project for `rows` rows
+int launch_node_project(const ProjArgs& a, cudaStream_t st);
+// interpolative decomposition of the n columns of A (S samples each, column
+// major): skeleton columns sk[0, R) and coefficients C[r * n + j] with
+// |A_j - sum_r C[r][j] A_sk[r]| <= tol at every sample; RG_ERR_RANGE when R
+// would exceed r_max (rg_skeleton.cpp)
+int interp_decomp(const double* A, int S, int n, double tol, int r_max, int* sk, double* C, int* R_out,
+                  double* err_out);
 int launch_slit_conv(const SlitArgs& a, cudaStream_t st);
 int launch_scatter_tangent(const GradArgs& a, int grid, cudaStream_t st);
 int col_block(int n1);               // columns per CTA of the column FFTs

@@ -850,8 +850,8 @@ struct NodeV {
 };
 
 __device__ __forceinline__ NodeV node_params(const VoigtArgs& a, int node) {
-    const int l = node / a.NL;
-    const int m = node - l * a.NL;
+    const int l = a.rowwise ? node : node / a.NL;
+    const int m = a.rowwise ? node : node - l * a.NL;
     NodeV n;
     n.al = a.alpha[l];
     n.bm = a.beta[m];
@@ -883,10 +883,10 @@ struct NodeF {
     float nal, nbm, lnrm;
 };
 __device__ __forceinline__ NodeF node_fast(const VoigtArgs& a, int node) {
-    const int l = node / a.NL;
+    const int l = a.rowwise ? node : node / a.NL;
     NodeF n;
     n.nal = -a.alpha[l];
-    n.nbm = -a.beta[node - l * a.NL];
+    n.nbm = -a.beta[a.rowwise ? node : node - l * a.NL];
     n.lnrm = a.lnorm[node];
     return n;
 }
@@ -1486,6 +1486,81 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
     }
 }
 
+// Skeleton layout: rows [0, rows) of the LDM <- the projection of all node
+// rows onto the skeleton rows, in place.  Each thread owns CPT consecutive
+// columns: it reads every node row's values there (one streaming vector load
+// per row), accumulates RB x CPT sums with the coefficients broadcast from
+// shared memory (one 16-byte load per 4 x CPT FMAs), and only then writes
+// its columns of the first rows: no other thread touches those columns.
+// HBM-bound: n_nodes x 4 B read and rows x 4 B written per column.
+template <int CPT>
+__device__ __forceinline__ void load_cols(float (&x)[CPT], const float* p) {
+    if constexpr (CPT == 4) {
+        const float4 v = __ldcs(reinterpret_cast<const float4*>(p));
+        x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
+    } else if constexpr (CPT == 2) {
+        const float2 v = __ldcs(reinterpret_cast<const float2*>(p));
+        x[0] = v.x; x[1] = v.y;
+    } else {
+        x[0] = __ldcs(p);
+    }
+}
+
+template <int RB, int CPT>
+__global__ void __launch_bounds__(256) k_node_project(const ProjArgs a) {
+    extern __shared__ __align__(16) float pcs[];   // coefficients [n_nodes][RB]
+    {
+        const float4* src = reinterpret_cast<const float4*>(a.coef);
+        float4* dst = reinterpret_cast<float4*>(pcs);
+        for (int i = threadIdx.x; i < a.n_nodes * (RB / 4); i += blockDim.x) dst[i] = __ldg(&src[i]);
+    }
+    __syncthreads();
+    const int64_t k0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * CPT;
+    if (k0 >= a.n_v) return;
+    float acc[RB][CPT];
+#pragma unroll
+    for (int r = 0; r < RB; ++r)
+#pragma unroll
+        for (int j = 0; j < CPT; ++j) acc[r][j] = 0.f;
+    const float* src = a.ldm + k0;   // rows are 128-byte aligned and k0 % CPT == 0: aligned vector loads
+#pragma unroll 4
+    for (int nd = 0; nd < a.n_nodes; ++nd) {
+        float x[CPT];
+        load_cols<CPT>(x, src + (int64_t)nd * a.row_stride);   // in the row's padding past n_v: unused
+        const float4* c4 = reinterpret_cast<const float4*>(pcs + nd * RB);
+#pragma unroll
+        for (int r = 0; r < RB; r += 4) {
+            const float4 c = c4[r / 4];
+#pragma unroll
+            for (int j = 0; j < CPT; ++j) {
+                acc[r][j] = fmaf(c.x, x[j], acc[r][j]);
+                acc[r + 1][j] = fmaf(c.y, x[j], acc[r + 1][j]);
+                acc[r + 2][j] = fmaf(c.z, x[j], acc[r + 2][j]);
+                acc[r + 3][j] = fmaf(c.w, x[j], acc[r + 3][j]);
+            }
+        }
+    }
+    const int nk = a.n_v - k0 < CPT ? (int)(a.n_v - k0) : CPT;
+#pragma unroll
+    for (int r = 0; r < RB; ++r) {
+        if (r >= a.rows) break;
+        float* dst = a.ldm + (int64_t)r * a.row_stride + k0;
+        if (nk == CPT) {
+            if constexpr (CPT == 4) {
+                *reinterpret_cast<float4*>(dst) = make_float4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
+            } else if constexpr (CPT == 2) {
+                *reinterpret_cast<float2*>(dst) = make_float2(acc[r][0], acc[r][1]);
+            } else {
+                dst[0] = acc[r][0];
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < CPT; ++j)
+                if (j < nk) dst[j] = acc[r][j];
+        }
+    }
+}
+
 // Instrument slit (radis/tools/slit.py:737 and remove_boundary, :1063-1072):
 // out[i] = scale sum_j slit[j] in[i + (m-1)/2 - j], the 'same' part of the
 // full convolution, zero outside [0, n); written as a correlation with the
@@ -1952,6 +2027,38 @@ int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st) {
         case 512: return col_inv_adj<512>(a, st);
         default: return RG_ERR_RANGE;
     }
+}
+
+// Row block of the projection: the rows rounded up to a multiple of 4;
+// columns per thread such that RB x CPT <= 64 accumulators (4 up to 16 rows,
+// 2 up to 32, else 1).
+int proj_rows_pad(int rows) { return (rows + 3) & ~3; }
+
+template <int RB>
+int launch_proj_rb(const ProjArgs& a, size_t smem, cudaStream_t st) {
+    constexpr int CPT = RB <= 16 ? 4 : RB <= 32 ? 2 : 1;
+    ALLOW_SMEM((k_node_project<RB, CPT>), smem);
+    const int64_t threads = (a.n_v + CPT - 1) / CPT;
+    k_node_project<RB, CPT><<<(unsigned)((threads + 255) / 256), 256, smem, st>>>(a);
+    return check_launch();
+}
+
+template <int RB>
+int launch_proj_dispatch(const ProjArgs& a, size_t smem, cudaStream_t st) {
+    if constexpr (RB > kProjMaxRows) {
+        return RG_ERR_ARG;
+    } else {
+        if (a.rows_pad == RB) return launch_proj_rb<RB>(a, smem, st);
+        return launch_proj_dispatch<RB + 4>(a, smem, st);
+    }
+}
+
+int launch_node_project(const ProjArgs& a, cudaStream_t st) {
+    if (a.rows <= 0 || a.rows > kProjMaxRows || a.rows_pad != proj_rows_pad(a.rows) || a.n_nodes <= 0 ||
+        a.n_v <= 0 || a.row_stride % 4 != 0)
+        return RG_ERR_ARG;
+    const size_t smem = sizeof(float) * (size_t)a.n_nodes * a.rows_pad;
+    return launch_proj_dispatch<4>(a, smem, st);
 }
 
 int launch_gauss_merge(const GaussArgs& a0, int out_rows, cudaStream_t st) {

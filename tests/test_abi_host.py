@@ -32,7 +32,7 @@ def test_exports_match_header(native_lib):
 
 
 def test_abi_version(native_lib):
-    assert native_lib.rg_abi_version() == 2
+    assert native_lib.rg_abi_version() == 3
 
 
 def test_grid_matches_reference_params(native_lib, golden):

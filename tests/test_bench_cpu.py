@@ -5,7 +5,7 @@
   the host cores and prints one JSON line carrying impl, cpu_baseline and an
   e2e object with zero copy bytes; the other rank exits 0 without work.
 * The kernel-launch claim (gpu_launches = kernels per spectrum x steps) for
-  the plain, merged and merged-with-narrow-rows FFT layouts.
+  the plain, merged, merged-with-narrow-rows and skeleton FFT layouts.
 * The multi-rank timing reduction of the GPU arm (max over ranks) on two
   gloo ranks.
 * The host-only ingestion mode (--ingest-only) on a small file.
@@ -87,10 +87,12 @@ def test_kernels_per_step():
     import bench
 
     class Info:
-        def __init__(self, merged_rows, fft_rows):
+        def __init__(self, merged_rows, fft_rows, layout=None):
             self.merged_rows, self.fft_rows = merged_rows, fft_rows
+            self.layout = layout if layout is not None else (2 if merged_rows else 1)
 
     assert bench.kernels_per_step(Info(0, 128)) == 5     # plain layout
+    assert bench.kernels_per_step(Info(0, 12, 3)) == 6   # skeleton rows: the projection in addition
     assert bench.kernels_per_step(Info(16, 16)) == 6     # CO2 5M: all Gaussian nodes wide
     assert bench.kernels_per_step(Info(24, 216)) == 7    # H2O 100M: merged + narrow-node rows
     assert bench.kernels_per_step(Info(7, 8)) == 6       # odd n_L padded with a zero row
