@@ -56,11 +56,14 @@ def kernels_per_step(info):
     the narrow-node rows when there are any."""
     if int(info.layout) == 3:
         return KERNELS_PER_STEP + 1
+    if int(info.layout) == 4:
+        return KERNELS_PER_STEP
     if not info.merged_rows:
         return KERNELS_PER_STEP
     nlv = info.merged_rows + (info.merged_rows & 1)
     return KERNELS_PER_STEP + 1 + (1 if info.fft_rows > nlv else 0)
 STAGES = ["k_scatter", "k_col_fft_fwd", "k_row_fft_voigt", "k_row_ifft", "k_col_ifft"]
+LAYOUT_NAMES = {1: "node rows", 2: "merged rows", 3: "skeleton rows", 4: "skeleton rows, projected in the scatter"}
 
 
 # name: (label, lines factory, molar mass, vmin, vmax, wstep, T, p_bar, x, n_G, n_L)
@@ -178,7 +181,8 @@ def algorithmic_bytes(n_lines_read, line_bytes, n_nodes, n_v, n_ft, info):
     Gaussian stage reads the wide-node LDM rows and writes the n_L merged rows
     (n_v + 2 ext points), and the column FFT reads those and the narrow-node
     rows.  With the skeleton layout the projection reads the node rows and
-    writes the skeleton rows, which the column FFT reads."""
+    writes the skeleton rows, which the column FFT reads; projected in the
+    scatter's flush, the scatter writes only the skeleton rows."""
     pairs = int(info.fft_rows or n_nodes) // 2
     out = {
         "k_scatter": n_lines_read * line_bytes + n_nodes * n_v * 4,
@@ -195,11 +199,14 @@ def algorithmic_bytes(n_lines_read, line_bytes, n_nodes, n_v, n_ft, info):
         merged = NL * (n_v + 2 * int(info.merged_ext)) * 4
         out["k_gauss_merge"] = wide_rows * n_v * 4 + merged
         out["k_col_fft_fwd"] = merged + n_narrow * NL * n_v * 4 + pairs * n_ft * 8
-    if int(info.layout) == 3:
+    if int(info.layout) in (3, 4):
         rows = int(info.fft_rows)
         real_nodes = int(info.grid.n_G) * int(info.grid.n_L)
-        out["k_node_project"] = real_nodes * n_v * 4 + rows * n_v * 4
         out["k_col_fft_fwd"] = rows * n_v * 4 + pairs * n_ft * 8
+        if int(info.layout) == 3:
+            out["k_node_project"] = real_nodes * n_v * 4 + rows * n_v * 4
+        else:   # projected by the scatter's flush: only the skeleton rows are written
+            out["k_scatter"] = n_lines_read * line_bytes + rows * n_v * 4
     return out
 
 
@@ -699,7 +706,7 @@ def run_c3(ctx, L, h2o_host, h2o, K, peak, peak_kind, workers, check=True):
         "scatter_roofline": {"achieved": sc_gbs, "peak": peak, "unit": "GB/s", "frac": sc_gbs / peak,
                              "peak_kind": peak_kind, "bytes_per_line": lb,
                              "lines_read": int(info.lines_in_window)},
-        "fft_layout": {"layout": {1: "node rows", 2: "merged rows", 3: "skeleton rows"}.get(int(info.layout)),
+        "fft_layout": {"layout": LAYOUT_NAMES.get(int(info.layout)),
                        "fft_rows": int(info.fft_rows), "merged_rows": int(info.merged_rows),
                        "n_ft": int(g.n_ft), "skeleton_sampled_err": float(info.layout_err)},
         "scatter_accumulator_bits": int(info.accum_bits),
@@ -799,6 +806,15 @@ def run_ours(args):
     p50 = lat_ms[len(lat_ms) // 2]
     p99 = lat_ms[min(len(lat_ms) - 1, int(math.ceil(0.99 * len(lat_ms))) - 1)]
     e2e_ms = max_over_ranks(e2e_ms, ws, "cuda")
+    # the same with T stepped by 0.1 K per spectrum: new node axes every step,
+    # so every per-grid host step (envelopes, skeleton decomposition) reruns
+    lat_v = []
+    for i in range(W + K):
+        t0 = time.perf_counter()
+        plan.synthesize_host(T + 0.1 * (i + 1), p, x, out=host)
+        if i >= W:
+            lat_v.append(time.perf_counter() - t0)
+    e2e_var_ms = max_over_ranks(statistics.mean(lat_v) * 1e3, ws, "cuda")
     # cold path: upload from host arrays + plan + one spectrum (eq_spectrum_gpu with exit_gpu)
     cold = []
     for _ in range(2 if n_lines <= 10_000_000 else 1):
@@ -833,6 +849,11 @@ def run_ours(args):
                     "note": ("resident line list (as the reference's gpuApp.iterate); per step the conditions "
                              "travel as kernel parameters and the float32 spectrum is copied to pinned host "
                              "memory")},
+            "e2e_varied_T": {"value": ws * 1000.0 / e2e_var_ms, "unit": "spectra/s",
+                             "h2d_bytes_per_step": 0, "d2h_bytes_per_step": n_v * 4,
+                             "note": ("as e2e with T raised by 0.1 K every step: new node axes each step, so the "
+                                      "host recomputes the grid and the skeleton decomposition every step (a fit "
+                                      "over temperature)")},
             "e2e_cold": {"value": 1.0 / statistics.mean(cold), "unit": "spectra/s",
                          "h2d_bytes_per_step": n_lines * (8 + 8 + 4 * 4), "d2h_bytes_per_step": n_v * 4,
                          "note": "line upload from host arrays + envelopes + plan + one spectrum"},
@@ -843,7 +864,7 @@ def run_ours(args):
                          "avg_launch_ms": kt[name]},
             "stages": stages,
             "scatter_accumulator_bits": int(info.accum_bits),
-            "fft_layout": {"layout": {1: "node rows", 2: "merged rows", 3: "skeleton rows"}.get(int(info.layout)),
+            "fft_layout": {"layout": LAYOUT_NAMES.get(int(info.layout)),
                            "fft_rows": int(info.fft_rows), "merged_rows": int(info.merged_rows),
                            "gauss_halfwidth": int(info.merged_ext), "n_ft": int(g.n_ft),
                            "skeleton_sampled_err": float(info.layout_err)},

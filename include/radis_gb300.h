@@ -165,7 +165,10 @@ typedef struct {
                                   0 when it was chosen on the device (served
                                   and allocation-free spectra in auto mode)    */
     int32_t layout;            /* FFT-stage layout used: 1 node rows, 2 merged
-                                  rows, 3 skeleton rows (fft_rows of them)     */
+                                  rows, 3 skeleton rows (fft_rows of them)
+                                  projected in a pass of their own, 4 skeleton
+                                  rows projected by the scatter as it writes
+                                  each finished tile                           */
     float layout_err;          /* skeleton layout: the largest error of the
                                   decomposition over its frequency samples     */
 } rg_spectrum_info;

@@ -91,7 +91,10 @@ static int fail(int code, const char* fmt, ...) {
     do {                                                           \
         int r_ = (call);                                           \
         if (r_ != RG_OK) {                                         \
-            if (g_err.empty()) fail(r_, "%s failed", #call);       \
+            if (g_err.empty())                                     \
+                fail(r_, "%s failed%s%s", #call,                   \
+                     r_ == RG_ERR_CUDA && last_launch_error() ? ": " : "", \
+                     r_ == RG_ERR_CUDA && last_launch_error() ? last_launch_error() : ""); \
             return r_;                                             \
         }                                                          \
     } while (0)
@@ -173,6 +176,14 @@ struct Work {
     float* proj_coef = nullptr;
     size_t proj_bytes = 0;
     std::vector<float> proj_host;
+    // the last decomposition, reused while the node grid is the same (a pure
+    // function of the axes, spacing, folding threshold and tolerance); the
+    // device copy of its coefficients is current while skel_dev is set
+    double skel_key[10] = {0};
+    bool skel_valid = false, skel_dev = false;
+    int skel_R = 0;
+    double skel_err = 0.0;
+    std::vector<int> skel_nodes;
     int last_accum = 0;               // accumulator bits of the last scatter (0: chosen on the device)
     int64_t row_stride = 0;
     float* ldm = nullptr;             // LDM [node][row_stride] (the scatter's float values)
@@ -642,12 +653,13 @@ int ensure_workspace(Work& W, int n_nodes, cudaStream_t st) {
 // columns); with wide node grids the tile narrows and two 2048-line chunks
 // per stage ring win (H2O 100M, 12x24 nodes: 1.35 ms vs 1.45 ms); smaller
 // chunks only when even those do not fit.
-int scatter_shape(int n_nodes, bool wide, int* chunk, int* TK, int* stages, size_t* smem) {
+// coef_bytes: the skeleton layout's flush coefficients (0 without).
+int scatter_shape(int n_nodes, bool wide, size_t coef_bytes, int* chunk, int* TK, int* stages, size_t* smem) {
     size_t avail = 0;
     RG(scatter_smem_optin(&avail, wide));
     const size_t word = wide ? 8 : 4;   // bytes per tile cell
     auto tile_cols = [&](int S, int ch) {   // widest tile next to the ring (rows of tk + 1 words)
-        const size_t fixed = scatter_fixed_smem(ch, S);
+        const size_t fixed = scatter_fixed_smem(ch, S) + coef_bytes + 16;
         if (fixed >= avail) return 0;
         return std::min(1024, ((int)((avail - fixed) / (word * (size_t)n_nodes)) - 1) / 32 * 32);
     };
@@ -655,7 +667,7 @@ int scatter_shape(int n_nodes, bool wide, int* chunk, int* TK, int* stages, size
         *chunk = ch;
         *TK = tk;
         *stages = S;
-        *smem = scatter_fixed_smem(ch, S) + word * n_nodes * (tk + 1);
+        *smem = scatter_fixed_smem(ch, S) + scatter_coef_offset((size_t)n_nodes * (tk + 1), word) + coef_bytes;
         return RG_OK;
     };
     // GB300 sweeps (CO2 5M / 128 nodes, H2O 100M / 288 nodes): one line per
@@ -669,8 +681,9 @@ int scatter_shape(int n_nodes, bool wide, int* chunk, int* TK, int* stages, size
     return fail(RG_ERR_RANGE, "LDM grid of %d nodes does not fit a shared-memory tile", n_nodes);
 }
 
+// fuse: the skeleton projection done by the scatter's flush (nullable).
 int build_scatter_args(const rg_lines* L, const Work& W, const rg_conditions* c, const SpecHost& s, bool wide,
-                       ScatterArgs* a) {
+                       const ProjArgs* fuse, ScatterArgs* a) {
     const rg_grid& g = s.grid;
     std::memset(a, 0, sizeof *a);
     a->v0 = L->v0;
@@ -690,8 +703,16 @@ int build_scatter_args(const rg_lines* L, const Work& W, const rg_conditions* c,
     a->NL = g.n_L;
     a->row_stride = W.row_stride;
     a->ldm = W.ldm;
+    size_t coef_bytes = 0;
+    if (fuse) {
+        a->proj_coef = fuse->coef;
+        a->proj_rows = fuse->rows;
+        a->proj_rp = fuse->rows_pad;
+        a->n_real = fuse->n_nodes;
+        coef_bytes = sizeof(float) * (size_t)fuse->n_nodes * fuse->rows_pad;
+    }
     size_t smem_unused;
-    RG(scatter_shape(s.n_nodes, wide, &a->chunk, &a->TK, &a->stages, &smem_unused));
+    RG(scatter_shape(s.n_nodes, wide, coef_bytes, &a->chunk, &a->TK, &a->stages, &smem_unused));
     a->n_tiles = (int)((W.desc.n_v + a->TK - 1) / a->TK);
     a->cmax = W.cmax_dev;
     a->err = W.err;
@@ -922,7 +943,7 @@ int NL_merged(const GaussArgs& ga) { return ga.NLv; }
 // every node's transform within tol; fills the row kernel's arguments (row r
 // = skeleton node sk[r], with its own transform) and the projection
 // coefficients [n_nodes][rows_pad] in W.proj_host.
-constexpr int kSkelSamples = 48;
+constexpr int kSkelSamples = 32;
 constexpr double kSkelTol = 1e-8;
 
 // The decomposition itself (host only): skeleton nodes sk[0, R) and
@@ -934,11 +955,17 @@ int skeleton_decomp(const rg_grid& g, double dv, double thresh, double tol, int 
     constexpr int S = kSkelSamples;
     double f[S];
     for (int j = 0; j < S; ++j) f[j] = h * std::pow((double)j / (S - 1), 2);
-    std::vector<int> nf(n);
-    std::vector<double> nrm(n);
+    std::vector<int> nf(n, 0);
+    std::vector<double> nrm(n, 1.0);
     int qmax = 0;
+    // folded copies only where the transform at the Nyquist frequency reaches
+    // the threshold (node_fold's first test, here from the separable factors)
+    std::vector<double> gh(g.n_G), lh(g.n_L);
+    for (int l = 0; l < g.n_G; ++l) gh[l] = std::exp(-std::pow(kPi * h * std::exp(g.log_wG_min + l * g.dxG), 2) / (4.0 * kLn2));
+    for (int m = 0; m < g.n_L; ++m) lh[m] = std::exp(-kPi * h * std::exp(g.log_wL_min + m * g.dxL));
     for (int node = 0; node < n; ++node) {
         const int l = node / g.n_L, m = node % g.n_L;
+        if (!(gh[l] * lh[m] >= thresh)) continue;   // no folded copy: norm 1 / V(0) = 1
         node_fold(dv, std::exp(g.log_wG_min + l * g.dxG), std::exp(g.log_wL_min + m * g.dxL), thresh, &nf[node],
                   &nrm[node]);
         qmax = std::max(qmax, nf[node]);
@@ -958,6 +985,8 @@ int skeleton_decomp(const rg_grid& g, double dv, double thresh, double tol, int 
                 Lt[((size_t)q * g.n_L + m) * S + j] = std::exp(-kPi * fq * wL);
             }
         }
+    // samples below 1e-30 (far below any tolerance) are flushed to zero:
+    // their products would otherwise reach the subnormal range
     std::vector<double> A((size_t)n * S);
     for (int node = 0; node < n; ++node) {
         const int l = node / g.n_L, m = node % g.n_L;
@@ -966,7 +995,8 @@ int skeleton_decomp(const rg_grid& g, double dv, double thresh, double tol, int 
             double v = 0.0;
             for (int q = 0; q <= nf[node]; ++q)
                 v += Gt[((size_t)q * g.n_G + l) * S + j] * Lt[((size_t)q * g.n_L + m) * S + j];
-            a[j] = v * nrm[node];
+            v *= nrm[node];
+            a[j] = v < 1e-30 ? 0.0 : v;
         }
     }
     sk->assign(r_max, 0);
@@ -982,18 +1012,36 @@ bool plan_skeleton(Work& W, const SpecHost& s, const VoigtArgs& va, int r_max, V
     if (!W.allow_skeleton || n < 4 || r_max < 2) return false;
     const double thresh = W.desc.folding_thresh > 0 ? W.desc.folding_thresh : 1e-6;
     const double tol = W.desc.layout_tol > 0 ? W.desc.layout_tol : kSkelTol;
-    std::vector<int> sk;
-    std::vector<double> C;
-    int R = 0;
-    double err = 0.0;
-    if (skeleton_decomp(g, W.desc.dv, thresh, tol, r_max, &sk, &C, &R, &err) != RG_OK) return false;
+    const double key[10] = {g.log_wG_min, g.dxG, (double)g.n_G, g.log_wL_min, g.dxL, (double)g.n_L,
+                            W.desc.dv, thresh, tol, (double)r_max};
+    const bool hit = W.skel_valid && std::equal(key, key + 10, W.skel_key);
+    if (!hit) {
+        W.skel_dev = false;
+        std::copy(key, key + 10, W.skel_key);
+        W.skel_valid = true;
+        W.skel_R = 0;   // no skeleton layout for this grid (cached as well)
+        std::vector<int> sk;
+        std::vector<double> C;
+        int R = 0;
+        double err = 0.0;
+        if (skeleton_decomp(g, W.desc.dv, thresh, tol, r_max, &sk, &C, &R, &err) != RG_OK) return false;
+        const int rows = R + (R & 1);
+        if (R < 1 || rows > r_max) return false;
+        const int rp = proj_rows_pad(rows);
+        if ((size_t)n * rp * sizeof(float) > 96 * 1024) return false;   // coefficients in shared memory
+        W.proj_host.assign((size_t)n * rp, 0.f);
+        for (int r = 0; r < R; ++r)
+            for (int node = 0; node < n; ++node) W.proj_host[(size_t)node * rp + r] = (float)C[(size_t)r * n + node];
+        W.skel_nodes.assign(sk.begin(), sk.begin() + R);
+        W.skel_R = R;
+        W.skel_err = err;
+    }
+    if (W.skel_R == 0) return false;
+    const int R = W.skel_R;
     const int rows = R + (R & 1);
-    if (R < 1 || rows > r_max) return false;
     const int rp = proj_rows_pad(rows);
-    if ((size_t)n * rp * sizeof(float) > 96 * 1024) return false;   // coefficients in shared memory
-    W.proj_host.assign((size_t)n * rp, 0.f);
-    for (int r = 0; r < R; ++r)
-        for (int node = 0; node < n; ++node) W.proj_host[(size_t)node * rp + r] = (float)C[(size_t)r * n + node];
+    const double err = W.skel_err;
+    const std::vector<int>& sk = W.skel_nodes;
     *vk = va;
     vk->rowwise = 1;
     vk->n_nodes = rows;
@@ -1042,19 +1090,93 @@ int take_err(Work& W) {
 // (one persistent CTA per SM, more only past kScatMaxTilesPerCta tiles each)
 // and dynamic shared memory.
 int scatter_launch_shape(const rg_lines* L, const Work& W, const rg_conditions* c, const SpecHost& s, bool wide,
-                         ScatterArgs* sa, int* grid, size_t* smem) {
-    RG(build_scatter_args(L, W, c, s, wide, sa));
+                         const ProjArgs* fuse, ScatterArgs* sa, int* grid, size_t* smem) {
+    RG(build_scatter_args(L, W, c, s, wide, fuse, sa));
     int ch_unused, tk_unused, st_unused;
-    RG(scatter_shape(s.n_nodes, wide, &ch_unused, &tk_unused, &st_unused, smem));
+    const size_t coef_bytes = fuse ? sizeof(float) * (size_t)fuse->n_nodes * fuse->rows_pad : 0;
+    RG(scatter_shape(s.n_nodes, wide, coef_bytes, &ch_unused, &tk_unused, &st_unused, smem));
     const int sms = L->ctx->sms;
     *grid = std::max(std::min(sa->n_tiles, sms), (sa->n_tiles + kScatMaxTilesPerCta - 1) / kScatMaxTilesPerCta);
     return RG_OK;
 }
 
+// The FFT-stage layout of one spectrum (rg_plan_desc.layout) and its
+// arguments; for the skeleton layout the projection coefficients are
+// uploaded (stream ordered) into W.proj_coef.
+struct LayoutPlan {
+    std::unique_ptr<VoigtArgs> va, vm, vk;
+    std::unique_ptr<GaussArgs> ga;
+    ProjArgs pa{};
+    bool merged = false, skel = false;
+    int m_rows = 0;
+};
+
+int plan_layout(Work& W, const SpecHost& s, cudaStream_t st, LayoutPlan* lp) {
+    lp->va = std::make_unique<VoigtArgs>();
+    lp->vm = std::make_unique<VoigtArgs>();
+    lp->vk = std::make_unique<VoigtArgs>();
+    lp->ga = std::make_unique<GaussArgs>();
+    fill_voigt_args(W, s, lp->va.get());
+    const int lay = W.desc.layout;
+    int& m_rows = lp->m_rows;
+    bool merged = lay != 1 && lay != 3 && plan_merge(W, s, *lp->va, lp->ga.get(), lp->vm.get(), &m_rows);
+    double sk_err = 0.0;
+    const int alt_rows = merged ? m_rows : s.n_nodes;
+    // auto: skeleton rows when no more than the merged rows (whose Gaussian
+    // stage costs more than the projection), or 3/4 of the node rows
+    const bool skel = (lay == 0 || lay == 3) &&
+                      plan_skeleton(W, s, *lp->va, lay == 3 ? kProjMaxRows : merged ? alt_rows : 3 * alt_rows / 4,
+                                    lp->vk.get(), &lp->pa, &sk_err);
+    if (skel) merged = false;
+    else if (lay == 3) merged = plan_merge(W, s, *lp->va, lp->ga.get(), lp->vm.get(), &m_rows);
+    lp->merged = merged;
+    lp->skel = skel;
+    W.last_layout = skel ? 3 : merged ? 2 : 1;
+    W.last_layout_err = skel ? sk_err : 0.0;
+    W.last_fft_rows = skel ? lp->pa.rows : merged ? m_rows : s.n_nodes;
+    W.last_merged_rows = merged ? lp->ga->NL : 0;
+    W.last_ext = merged ? lp->ga->ext : 0;
+    if (skel) {
+        const size_t need = sizeof(float) * W.proj_host.size();
+        if (need > W.proj_bytes) {
+            if (W.proj_coef) CU(cudaFreeAsync(W.proj_coef, st));
+            W.proj_coef = nullptr;
+            W.proj_bytes = 0;
+            W.skel_dev = false;
+            const size_t want = std::max<size_t>(need, 64 * 1024);
+            CU(cudaMallocAsync((void**)&W.proj_coef, want, st));
+            W.proj_bytes = want;
+        }
+        if (!W.skel_dev) {
+            // pageable source: staged before the call returns, so the host
+            // vector may be refilled by the next spectrum at once
+            CU(cudaMemcpyAsync(W.proj_coef, W.proj_host.data(), need, cudaMemcpyHostToDevice, st));
+            W.skel_dev = true;
+        }
+        lp->pa.coef = W.proj_coef;
+    }
+    return RG_OK;
+}
+
+// Skeleton projection in the scatter's flush (no LDM round trip through HBM)
+// for grids of at most this many nodes; larger grids project in a separate
+// pass (the flush's FMAs would stall the scatter longer than the round trip
+// costs), with the decomposition computed on the host while the scatter runs.
+constexpr int kFuseMaxNodes = 160;
+
 int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const SpecHost& s, float* out,
                      cudaStream_t st, cudaEvent_t* ev, bool ldm_only) {
     RG(ensure_workspace(W, s.n_nodes, st));
     const int n_v = (int)W.desc.n_v;
+    const int n_real = s.grid.n_G * s.grid.n_L;
+    LayoutPlan lp;
+    bool planned = false;
+    if (!ldm_only && W.allow_skeleton && (W.desc.layout == 0 || W.desc.layout == 3) && n_real <= kFuseMaxNodes) {
+        RG(plan_layout(W, s, st, &lp));
+        planned = true;
+    }
+    lp.pa.sms = L->ctx->sms;
+    const ProjArgs* fuse = planned && lp.skel ? &lp.pa : nullptr;
     if (ev) CU(cudaEventRecord(ev[0], st));
     if (W.count_lines) CU(cudaMemsetAsync(W.counter, 0, sizeof(unsigned long long), st));
     // accumulator width: forced, or from the densest column when the host knows
@@ -1064,18 +1186,19 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
         ScatterArgs sa;
         int grid;
         size_t smem;
-        RG(scatter_launch_shape(L, W, c, s, wide, &sa, &grid, &smem));
+        RG(scatter_launch_shape(L, W, c, s, wide, fuse, &sa, &grid, &smem));
         RG(launch_scatter(sa, grid, kScatThreads, smem, wide, st));
         W.last_accum = wide ? 64 : 32;
     } else {
         ScatterArgs a32, a64;
         int g32, g64;
         size_t m32, m64;
-        RG(scatter_launch_shape(L, W, c, s, false, &a32, &g32, &m32));
-        RG(scatter_launch_shape(L, W, c, s, true, &a64, &g64, &m64));
+        RG(scatter_launch_shape(L, W, c, s, false, fuse, &a32, &g32, &m32));
+        RG(scatter_launch_shape(L, W, c, s, true, fuse, &a64, &g64, &m64));
         RG(launch_scatter_auto(a32, a64, std::max(g32, g64), kScatThreads, std::max(m32, m64), st));
         W.last_accum = 0;
     }
+    if (fuse) W.last_layout = 4;
     if (ev) CU(cudaEventRecord(ev[1], st));
     if (!ldm_only) {
         ColFftArgs ca;
@@ -1094,43 +1217,15 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
         ca.y = W.y;
         ca.tw_hi = W.tw_hi;
         ca.tw_lo = W.tw_lo;
-        auto va = std::make_unique<VoigtArgs>();
-        auto vm = std::make_unique<VoigtArgs>();
-        auto ga = std::make_unique<GaussArgs>();
-        fill_voigt_args(W, s, va.get());
-        // layout: node rows, merged rows or skeleton rows (rg_plan_desc.layout)
-        const int lay = W.desc.layout;
-        int m_rows = 0;
-        bool merged = lay != 1 && lay != 3 && plan_merge(W, s, *va, ga.get(), vm.get(), &m_rows);
-        auto vk = std::make_unique<VoigtArgs>();
-        ProjArgs pa;
-        double sk_err = 0.0;
-        const int alt_rows = merged ? m_rows : s.n_nodes;
-        const bool skel = (lay == 0 || lay == 3) &&
-                          plan_skeleton(W, s, *va, lay == 3 ? kProjMaxRows : merged ? alt_rows : 3 * alt_rows / 4,
-                                        vk.get(), &pa, &sk_err);
-        if (skel) merged = false;
-        else if (lay == 3) merged = plan_merge(W, s, *va, ga.get(), vm.get(), &m_rows);
-        W.last_layout = skel ? 3 : merged ? 2 : 1;
-        W.last_layout_err = skel ? sk_err : 0.0;
-        W.last_fft_rows = skel ? pa.rows : merged ? m_rows : s.n_nodes;
-        W.last_merged_rows = merged ? ga->NL : 0;
-        W.last_ext = merged ? ga->ext : 0;
+        if (!planned) {
+            RG(plan_layout(W, s, st, &lp));
+            lp.pa.sms = L->ctx->sms;
+        }
+        const bool skel = lp.skel, merged = lp.merged;
+        GaussArgs* ga = lp.ga.get();
+        ProjArgs& pa = lp.pa;
         if (skel) {
-            const size_t need = sizeof(float) * W.proj_host.size();
-            if (need > W.proj_bytes) {
-                if (W.proj_coef) CU(cudaFreeAsync(W.proj_coef, st));
-                W.proj_coef = nullptr;
-                W.proj_bytes = 0;
-                const size_t want = std::max<size_t>(need, 64 * 1024);
-                CU(cudaMallocAsync((void**)&W.proj_coef, want, st));
-                W.proj_bytes = want;
-            }
-            // pageable source: staged before the call returns, so the host
-            // vector may be refilled by the next spectrum at once
-            CU(cudaMemcpyAsync(W.proj_coef, W.proj_host.data(), need, cudaMemcpyHostToDevice, st));
-            pa.coef = W.proj_coef;
-            RG(launch_node_project(pa, st));
+            if (!fuse) RG(launch_node_project(pa, st));
             if (ev) CU(cudaEventRecord(ev[6], st));
             ca.n_pairs = pa.rows / 2;
             RG(launch_col_fft_fwd(ca, st));
@@ -1170,7 +1265,7 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
             RG(launch_col_fft_fwd(ca, st));
         }
         if (ev) CU(cudaEventRecord(ev[2], st));
-        VoigtArgs& vr = skel ? *vk : merged ? *vm : *va;
+        VoigtArgs& vr = skel ? *lp.vk : merged ? *lp.vm : *lp.va;
         vr.store_g = vr.n_pairs <= kPairGroup;   // one pair group per row: it stores G itself
         if (!vr.store_g) CU(cudaMemsetAsync(W.g, 0, sizeof(float2) * (size_t)W.n, st));
         RG(launch_row_fft_voigt(vr, st));
@@ -1213,7 +1308,7 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
 int fill_grad_args(const rg_lines* L, const Work& W, const rg_conditions* c, const SpecHost& s,
                    const double* dlnq_dT, GradArgs* g) {
     std::memset(g, 0, sizeof *g);
-    RG(build_scatter_args(L, W, c, s, false, &g->s));
+    RG(build_scatter_args(L, W, c, s, false, nullptr, &g->s));
     if (!(c->x > 0)) return fail(RG_ERR_ARG, "derivatives need a mole fraction x > 0");
     const double T = c->T, p = c->p_bar;
     g->n_lines = L->n;
@@ -1701,6 +1796,7 @@ void free_work(Work& W) {
     W.mrow_bytes = 0;
     dfree(W.proj_coef);
     W.proj_bytes = 0;
+    W.skel_dev = false;
 }
 
 int rg_plan_free(rg_plan* P) {
@@ -2214,6 +2310,7 @@ void release_slot_buffers(Slot& sl) {
     if (sl.w.proj_coef) cudaFreeAsync(sl.w.proj_coef, sl.st);
     sl.w.proj_coef = nullptr;
     sl.w.proj_bytes = 0;
+    sl.w.skel_dev = false;
     sl.w.nodes_cap = 0;
     sl.w.ldm_bytes = sl.w.y_bytes = 0;
     sl.out_cap = sl.col_cap = sl.g_cap = 0;

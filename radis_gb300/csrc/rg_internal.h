@@ -147,6 +147,13 @@ struct ScatterArgs {
     long long wait_limit;     // SM clock cycles a producer/consumer handshake wait may take
     int withhold;             // test hook: the producer issues no line copies, so the
                               // consumers' waits run out (the error path, exercised safely)
+    // skeleton layout fused into the flush (proj_coef non-null): each finished
+    // tile is written as proj_rows skeleton rows (ldm rows [0, proj_rows)),
+    // row r = sum over the n_real node rows of proj_coef[node * proj_rp + r] x row
+    const float* proj_coef;   // [n_real][proj_rp], staged into shared memory after the tile
+    int proj_rows;            // even; rows >= the skeleton's are zero rows
+    int proj_rp;              // coefficient pitch, a multiple of 4
+    int n_real;               // NG x NL (the pad node of an odd grid is not read)
 };
 constexpr long long kScatWaitCycles = 1LL << 31;   // about one second of SM clocks
 
@@ -167,6 +174,9 @@ RG_HD inline size_t scatter_stage_bytes(int chunk) { return (size_t)33 * chunk; 
 RG_HD inline size_t scatter_fixed_smem(int chunk, int stages) {
     return stages * scatter_stage_bytes(chunk) + 16 * kScatMaxStages + 8 * kScatMaxTilesPerCta;
 }
+// byte offset of the flush coefficients (skeleton layout) after a tile of
+// `words` accumulator words of `word` bytes
+RG_HD inline size_t scatter_coef_offset(size_t words, size_t word) { return (words * word + 15) / 16 * 16; }
 
 struct ColFftArgs {       // K2 (forward column FFT) and K4 (inverse column FFT)
     FftLen f1;
@@ -261,6 +271,7 @@ struct ProjArgs {
     int rows;             // rows written (R rounded up to even)
     int rows_pad;         // coefficient row pitch (the kernel's row block)
     const float* coef;    // [n_nodes][rows_pad]
+    int sms;              // SMs of the device (persistent grid)
 };
 
 constexpr int kGaussPer = 8;          // outputs per thread
@@ -377,6 +388,7 @@ int launch_row_ifft_adj(const AdjRowArgs& a, cudaStream_t st);
 int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st);
 int launch_gather_grad(const GradArgs& a, int grid, cudaStream_t st);
 int launch_gauss_merge(const GaussArgs& a, int out_rows, cudaStream_t st);
+const char* last_launch_error();     // the CUDA error of this thread's last failed launch, or null
 int proj_rows_pad(int rows);         // coefficient pitch of launch_node_project for `rows` rows
 int launch_node_project(const ProjArgs& a, cudaStream_t st);
 // interpolative decomposition of the n columns of A (S samples each, column

@@ -671,6 +671,12 @@ __device__ __forceinline__ void scatter_body(const ScatterArgs& a) {
         rng[q] = make_int2(lo / kLinePad * kLinePad, hi);   // 16-line aligned start
     }
     for (int i = threadIdx.x; i < n_words; i += blockDim.x) tile[i] = 0;
+    // skeleton layout: the projection coefficients after the tile
+    float* coef = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(tile) +
+                                           scatter_coef_offset(n_words, sizeof(Acc)));
+    const bool proj = a.proj_coef != nullptr;
+    if (proj)
+        for (int i = threadIdx.x; i < a.n_real * a.proj_rp; i += blockDim.x) coef[i] = __ldg(&a.proj_coef[i]);
     if (threadIdx.x == 0) {
         for (int b = 0; b < S; ++b) {
             mbar_init(&full[b], 1);
@@ -749,16 +755,49 @@ __device__ __forceinline__ void scatter_body(const ScatterArgs& a) {
             if (threadIdx.x == 32) atomicExch(a.err, 1u);
             return;
         }
-        // flush the finished tile as floats, word / fx_scale (a power of two:
-        // exact scaling of the rounded word), with plain stores (this CTA owns
-        // its columns), and re-zero it
-        for (int node = cw; node < a.n_nodes; node += n_cons_warps) {
-            Acc* row = tile + node * pitch;
-            float* dst = a.ldm + node * a.row_stride + k_start;
-            for (int c = lane; c < tk; c += 32) {   // one 128-byte store per warp step
-                // streaming store: the LDM is read once by the next stage, long after
-                __stcs(&dst[c], Fx<Acc>::to_float(row[c]) * inv_fx);
-                row[c] = 0;
+        if (proj) {
+            // skeleton rows of the finished tile: warp task (32-column group,
+            // block of 4 rows); lane c sums its column over the node rows with
+            // the block's 4 coefficients (one 16-byte broadcast load per node)
+            const int ncg = (tk + 31) >> 5, nrb = a.proj_rp >> 2;
+            for (int t = cw; t < ncg * nrb; t += n_cons_warps) {
+                const int cg = t % ncg, rb = t / ncg;
+                const int c = (cg << 5) + lane;
+                if (c >= tk) continue;
+                const Acc* col = tile + c;
+                const float4* cf = reinterpret_cast<const float4*>(coef) + rb;
+                const int cstep = a.proj_rp >> 2;
+                float y0 = 0.f, y1 = 0.f, y2 = 0.f, y3 = 0.f;
+#pragma unroll 4
+                for (int nd = 0; nd < a.n_real; ++nd) {
+                    const float v = Fx<Acc>::to_float(col[nd * pitch]);
+                    const float4 w = cf[nd * cstep];
+                    y0 = fmaf(w.x, v, y0);
+                    y1 = fmaf(w.y, v, y1);
+                    y2 = fmaf(w.z, v, y2);
+                    y3 = fmaf(w.w, v, y3);
+                }
+                const int r = rb << 2;
+                float* dst = a.ldm + (int64_t)r * a.row_stride + k_start + c;
+                if (r < a.proj_rows) __stcs(dst, y0 * inv_fx);
+                if (r + 1 < a.proj_rows) __stcs(dst + a.row_stride, y1 * inv_fx);
+                if (r + 2 < a.proj_rows) __stcs(dst + 2 * a.row_stride, y2 * inv_fx);
+                if (r + 3 < a.proj_rows) __stcs(dst + 3 * a.row_stride, y3 * inv_fx);
+            }
+            asm volatile("bar.sync 1, %0;" ::"r"(nct) : "memory");   // every read of the tile done
+            for (int i = ct; i < n_words; i += nct) tile[i] = 0;
+        } else {
+            // flush the finished tile as floats, word / fx_scale (a power of
+            // two: exact scaling of the rounded word), with plain stores (this
+            // CTA owns its columns), and re-zero it
+            for (int node = cw; node < a.n_nodes; node += n_cons_warps) {
+                Acc* row = tile + node * pitch;
+                float* dst = a.ldm + node * a.row_stride + k_start;
+                for (int c = lane; c < tk; c += 32) {   // one 128-byte store per warp step
+                    // streaming store: the LDM is read once by the next stage, long after
+                    __stcs(&dst[c], Fx<Acc>::to_float(row[c]) * inv_fx);
+                    row[c] = 0;
+                }
             }
         }
         asm volatile("bar.sync 1, %0;" ::"r"(nct) : "memory");
@@ -1487,77 +1526,109 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
 }
 
 // Skeleton layout: rows [0, rows) of the LDM <- the projection of all node
-// rows onto the skeleton rows, in place.  Each thread owns CPT consecutive
-// columns: it reads every node row's values there (one streaming vector load
-// per row), accumulates RB x CPT sums with the coefficients broadcast from
-// shared memory (one 16-byte load per 4 x CPT FMAs), and only then writes
-// its columns of the first rows: no other thread touches those columns.
-// HBM-bound: n_nodes x 4 B read and rows x 4 B written per column.
+// rows onto the skeleton rows, in place.  Persistent CTAs walk column tiles
+// of TC = 256 CPT columns; the tile's node rows stream through a ring of
+// kProjStages shared-memory stages of NC = 16 / CPT rows (16 KB, cp.async,
+// zero-filled past n_v), kProjStages - 1 stages ahead, across tile
+// boundaries.  Thread t owns columns CPT t .. CPT t + CPT - 1 of the tile and
+// accumulates RB x CPT sums: per node one CPT-wide shared load and RB / 4
+// 16-byte broadcast loads of the coefficients for RB x CPT FMAs.  After a
+// tile's last node row it writes its columns of rows [0, rows): every node
+// row of those columns has landed in shared memory by then, and no other CTA
+// touches them.
+constexpr int kProjStages = 4;
+
 template <int CPT>
-__device__ __forceinline__ void load_cols(float (&x)[CPT], const float* p) {
-    if constexpr (CPT == 4) {
-        const float4 v = __ldcs(reinterpret_cast<const float4*>(p));
-        x[0] = v.x; x[1] = v.y; x[2] = v.z; x[3] = v.w;
-    } else if constexpr (CPT == 2) {
-        const float2 v = __ldcs(reinterpret_cast<const float2*>(p));
-        x[0] = v.x; x[1] = v.y;
+__device__ __forceinline__ void load_cols_smem(float (&x)[CPT], const float* p) {
+    if constexpr (CPT == 2) {
+        const float2 v = *reinterpret_cast<const float2*>(p);
+        x[0] = v.x;
+        x[1] = v.y;
     } else {
-        x[0] = __ldcs(p);
+        x[0] = *p;
     }
 }
 
 template <int RB, int CPT>
 __global__ void __launch_bounds__(256) k_node_project(const ProjArgs a) {
-    extern __shared__ __align__(16) float pcs[];   // coefficients [n_nodes][RB]
+    constexpr int TC = 256 * CPT;   // columns per tile
+    constexpr int NC = 16 / CPT;    // node rows per stage (16 KB)
+    constexpr int S = kProjStages;
+    extern __shared__ __align__(16) float psm[];
+    const int n_chunks = (a.n_nodes + NC - 1) / NC;       // node chunks per tile
+    float* cs = psm;                                      // coefficients [n_chunks NC][RB], zero rows past n_nodes
+    float* xs = psm + n_chunks * NC * RB;                 // stages [S][NC][TC]
+    const int n_tiles = (int)((a.n_v + TC - 1) / TC);
+    const int my_tiles = (n_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int total = my_tiles * n_chunks;                // chunks this CTA consumes
+    auto tile_k0 = [&](int t) { return (int64_t)((int)blockIdx.x + t * (int)gridDim.x) * TC; };
+    // this thread's 16-byte pieces of a stage: row r_i, column 4 c4_i (the
+    // same in every chunk); only the chunk's origin changes
+    constexpr int PIECES = NC * TC / 4 / 256;
+    constexpr int ROW_STEP = 256 / (TC / 4);   // rows between a thread's pieces
+    const int r_0 = threadIdx.x / (TC / 4), c4_t = threadIdx.x % (TC / 4);
+    auto issue = [&](int g) {   // chunk g of this CTA into stage g % S
+        const int64_t k = tile_k0(g / n_chunks) + 4 * c4_t;
+        const int nd0 = (g % n_chunks) * NC + r_0;
+        float* dst = xs + (g % S) * NC * TC + r_0 * TC + 4 * c4_t;
+        const float* src = a.ldm + (int64_t)nd0 * a.row_stride + k;
+        const bool col_ok = k < a.n_v;   // a piece past n_v stays in the row's padding
+#pragma unroll
+        for (int i = 0; i < PIECES; ++i) {
+            const bool ok = col_ok && nd0 + i * ROW_STEP < a.n_nodes;
+            cp_async16(dst + i * ROW_STEP * TC, ok ? src + (int64_t)i * ROW_STEP * a.row_stride : a.ldm, ok ? 16 : 0);
+        }
+    };
+#pragma unroll
+    for (int g = 0; g < S - 1; ++g) {
+        if (g < total) issue(g);
+        cp_async_commit();
+    }
     {
         const float4* src = reinterpret_cast<const float4*>(a.coef);
-        float4* dst = reinterpret_cast<float4*>(pcs);
-        for (int i = threadIdx.x; i < a.n_nodes * (RB / 4); i += blockDim.x) dst[i] = __ldg(&src[i]);
+        float4* dst = reinterpret_cast<float4*>(cs);
+        const int nc4 = a.n_nodes * (RB / 4);
+        for (int i = threadIdx.x; i < n_chunks * NC * (RB / 4); i += blockDim.x)
+            dst[i] = i < nc4 ? __ldg(&src[i]) : make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    __syncthreads();
-    const int64_t k0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * CPT;
-    if (k0 >= a.n_v) return;
-    float acc[RB][CPT];
+    for (int t = 0; t < my_tiles; ++t) {
+        float acc[RB][CPT];
 #pragma unroll
-    for (int r = 0; r < RB; ++r)
+        for (int r = 0; r < RB; ++r)
 #pragma unroll
-        for (int j = 0; j < CPT; ++j) acc[r][j] = 0.f;
-    const float* src = a.ldm + k0;   // rows are 128-byte aligned and k0 % CPT == 0: aligned vector loads
-#pragma unroll 4
-    for (int nd = 0; nd < a.n_nodes; ++nd) {
-        float x[CPT];
-        load_cols<CPT>(x, src + (int64_t)nd * a.row_stride);   // in the row's padding past n_v: unused
-        const float4* c4 = reinterpret_cast<const float4*>(pcs + nd * RB);
+            for (int j = 0; j < CPT; ++j) acc[r][j] = 0.f;
+        for (int ch = 0; ch < n_chunks; ++ch) {
+            const int g = t * n_chunks + ch;
+            cp_async_wait<S - 2>();   // this thread's pieces of chunk g have landed
+            __syncthreads();          // everyone's have, and everyone is done with chunk g - 1
+            if (g + S - 1 < total) issue(g + S - 1);   // into chunk g - 1's stage
+            cp_async_commit();
+            const float* xb = xs + (g % S) * NC * TC + threadIdx.x * CPT;
+            const float4* c4 = reinterpret_cast<const float4*>(cs + ch * NC * RB);
 #pragma unroll
-        for (int r = 0; r < RB; r += 4) {
-            const float4 c = c4[r / 4];
+            for (int r = 0; r < NC; ++r) {   // rows past n_nodes: zero data, zero coefficients
+                float x[CPT];
+                load_cols_smem<CPT>(x, xb + r * TC);
 #pragma unroll
-            for (int j = 0; j < CPT; ++j) {
-                acc[r][j] = fmaf(c.x, x[j], acc[r][j]);
-                acc[r + 1][j] = fmaf(c.y, x[j], acc[r + 1][j]);
-                acc[r + 2][j] = fmaf(c.z, x[j], acc[r + 2][j]);
-                acc[r + 3][j] = fmaf(c.w, x[j], acc[r + 3][j]);
+                for (int q = 0; q < RB / 4; ++q) {
+                    const float4 c = c4[r * (RB / 4) + q];
+#pragma unroll
+                    for (int j = 0; j < CPT; ++j) {
+                        acc[4 * q][j] = fmaf(c.x, x[j], acc[4 * q][j]);
+                        acc[4 * q + 1][j] = fmaf(c.y, x[j], acc[4 * q + 1][j]);
+                        acc[4 * q + 2][j] = fmaf(c.z, x[j], acc[4 * q + 2][j]);
+                        acc[4 * q + 3][j] = fmaf(c.w, x[j], acc[4 * q + 3][j]);
+                    }
+                }
             }
         }
-    }
-    const int nk = a.n_v - k0 < CPT ? (int)(a.n_v - k0) : CPT;
+        // the tile is complete: its skeleton rows
+        const int64_t k = tile_k0(t) + threadIdx.x * CPT;
 #pragma unroll
-    for (int r = 0; r < RB; ++r) {
-        if (r >= a.rows) break;
-        float* dst = a.ldm + (int64_t)r * a.row_stride + k0;
-        if (nk == CPT) {
-            if constexpr (CPT == 4) {
-                *reinterpret_cast<float4*>(dst) = make_float4(acc[r][0], acc[r][1], acc[r][2], acc[r][3]);
-            } else if constexpr (CPT == 2) {
-                *reinterpret_cast<float2*>(dst) = make_float2(acc[r][0], acc[r][1]);
-            } else {
-                dst[0] = acc[r][0];
-            }
-        } else {
+        for (int r = 0; r < RB; ++r)
 #pragma unroll
             for (int j = 0; j < CPT; ++j)
-                if (j < nk) dst[j] = acc[r][j];
-        }
+                if (r < a.rows && k + j < a.n_v) a.ldm[(int64_t)r * a.row_stride + k + j] = acc[r][j];
     }
 }
 
@@ -1794,8 +1865,12 @@ __global__ void __launch_bounds__(256) k_scatter_tangent(const GradArgs g) {
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
+static thread_local const char* g_launch_err = nullptr;
+const char* last_launch_error() { return g_launch_err; }
+
 static int check_launch() {
     cudaError_t e = cudaGetLastError();
+    g_launch_err = e == cudaSuccess ? nullptr : cudaGetErrorString(e);
     return e == cudaSuccess ? RG_OK : RG_ERR_CUDA;
 }
 
@@ -2029,27 +2104,39 @@ int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st) {
     }
 }
 
-// Row block of the projection: the rows rounded up to a multiple of 4;
-// columns per thread such that RB x CPT <= 64 accumulators (4 up to 16 rows,
-// 2 up to 32, else 1).
+// Row block of the projection: the rows rounded up to a multiple of 4.
 int proj_rows_pad(int rows) { return (rows + 3) & ~3; }
 
-template <int RB>
-int launch_proj_rb(const ProjArgs& a, size_t smem, cudaStream_t st) {
-    constexpr int CPT = RB <= 16 ? 4 : RB <= 32 ? 2 : 1;
+// one launcher per instantiation: its shared-memory opt-in is its own
+template <int RB, int CPT>
+int launch_proj_kernel(const ProjArgs& a, int slots, cudaStream_t st) {
+    constexpr int NC = 16 / CPT;
+    const size_t smem = sizeof(float) * ((size_t)((a.n_nodes + NC - 1) / NC) * NC * RB + (size_t)kProjStages * 4096);
     ALLOW_SMEM((k_node_project<RB, CPT>), smem);
-    const int64_t threads = (a.n_v + CPT - 1) / CPT;
-    k_node_project<RB, CPT><<<(unsigned)((threads + 255) / 256), 256, smem, st>>>(a);
+    const int64_t tiles = (a.n_v + 256 * CPT - 1) / (256 * CPT);
+    const int grid = (int)std::min<int64_t>(tiles, slots);
+    k_node_project<RB, CPT><<<grid, 256, smem, st>>>(a);
     return check_launch();
 }
 
 template <int RB>
-int launch_proj_dispatch(const ProjArgs& a, size_t smem, cudaStream_t st) {
+int launch_proj_rb(const ProjArgs& a, cudaStream_t st) {
+    // two columns per thread where the FMAs dominate (up to 32 rows) and the
+    // grid still has >= 4 tiles per CTA slot; else one
+    const int slots = 2 * std::max(a.sms, 1);
+    if constexpr (RB <= 32) {
+        if ((a.n_v + 511) / 512 >= 4 * (int64_t)slots) return launch_proj_kernel<RB, 2>(a, slots, st);
+    }
+    return launch_proj_kernel<RB, 1>(a, slots, st);
+}
+
+template <int RB>
+int launch_proj_dispatch(const ProjArgs& a, cudaStream_t st) {
     if constexpr (RB > kProjMaxRows) {
         return RG_ERR_ARG;
     } else {
-        if (a.rows_pad == RB) return launch_proj_rb<RB>(a, smem, st);
-        return launch_proj_dispatch<RB + 4>(a, smem, st);
+        if (a.rows_pad == RB) return launch_proj_rb<RB>(a, st);
+        return launch_proj_dispatch<RB + 4>(a, st);
     }
 }
 
@@ -2057,8 +2144,7 @@ int launch_node_project(const ProjArgs& a, cudaStream_t st) {
     if (a.rows <= 0 || a.rows > kProjMaxRows || a.rows_pad != proj_rows_pad(a.rows) || a.n_nodes <= 0 ||
         a.n_v <= 0 || a.row_stride % 4 != 0)
         return RG_ERR_ARG;
-    const size_t smem = sizeof(float) * (size_t)a.n_nodes * a.rows_pad;
-    return launch_proj_dispatch<4>(a, smem, st);
+    return launch_proj_dispatch<4>(a, st);
 }
 
 int launch_gauss_merge(const GaussArgs& a0, int out_rows, cudaStream_t st) {

@@ -25,7 +25,7 @@ namespace rg {
 namespace {
 
 // dot product in four partial sums (vectorisable without reassociation flags)
-inline double dot(const double* a, const double* b, int S) {
+inline double dot(const double* __restrict a, const double* __restrict b, int S) {
     double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
     int i = 0;
     for (; i + 4 <= S; i += 4) {
@@ -112,30 +112,40 @@ int interp_decomp(const double* A, int S, int n, double tol, int r_max, int* sk,
         if (!(nq > 0.0)) break;   // exactly dependent: the rest is within tol already
         for (int i = 0; i < S; ++i) q[i] /= nq;
         Rm[(size_t)R * n + R] = nq;
+        // the remaining columns: all projections first (independent dot
+        // products), then the updates
+        double* rrow = &Rm[(size_t)R * n];
+        for (int j = R + 1; j < n; ++j) rrow[j] = dot(q, col(j), S);
         for (int j = R + 1; j < n; ++j) {
-            double* w = col(j);
-            const double d = dot(q, w, S);
+            double* __restrict w = col(j);
+            const double d = rrow[j];
             for (int i = 0; i < S; ++i) w[i] -= d * q[i];
-            Rm[(size_t)R * n + j] = d;
             // downdated norm, recomputed once it has lost most of its digits
             nrm2[j] -= d * d;
             if (nrm2[j] < 1e-6 * nrm2_ref[j]) nrm2[j] = nrm2_ref[j] = dot(w, w, S);
         }
     }
-    // coefficients: skeleton column r -> unit vector; others R11^-1 Rm[:, j]
+    // coefficients: skeleton column r -> unit vector; the others solve
+    // R11 T = R12, row by row from the last (each row a contiguous sweep over
+    // the columns)
     std::fill(C, C + (size_t)R * n, 0.0);
-    std::vector<double> t(R);
-    for (int j = 0; j < n; ++j) {
-        if (j < R) {
-            C[(size_t)j * n + perm[j]] = 1.0;
-            continue;
+    const int m = n - R;
+    std::vector<double> T((size_t)R * m);
+    for (int r = R - 1; r >= 0; --r) {
+        double* __restrict tr = &T[(size_t)r * m];
+        const double* rr = &Rm[(size_t)r * n];
+        for (int j = 0; j < m; ++j) tr[j] = rr[R + j];
+        for (int k = r + 1; k < R; ++k) {
+            const double f = rr[k];
+            const double* __restrict tk = &T[(size_t)k * m];
+            for (int j = 0; j < m; ++j) tr[j] -= f * tk[j];
         }
-        for (int r = R - 1; r >= 0; --r) {
-            double v = Rm[(size_t)r * n + j];
-            for (int k = r + 1; k < R; ++k) v -= Rm[(size_t)r * n + k] * t[k];
-            t[r] = v / Rm[(size_t)r * n + r];
-        }
-        for (int r = 0; r < R; ++r) C[(size_t)r * n + perm[j]] = t[r];
+        const double inv = 1.0 / rr[r];
+        for (int j = 0; j < m; ++j) tr[j] *= inv;
+    }
+    for (int r = 0; r < R; ++r) {
+        C[(size_t)r * n + perm[r]] = 1.0;
+        for (int j = 0; j < m; ++j) C[(size_t)r * n + perm[R + j]] = T[(size_t)r * m + j];
     }
     for (int r = 0; r < R; ++r) sk[r] = perm[r];
     *R_out = R;

@@ -93,6 +93,7 @@ def test_kernels_per_step():
 
     assert bench.kernels_per_step(Info(0, 128)) == 5     # plain layout
     assert bench.kernels_per_step(Info(0, 12, 3)) == 6   # skeleton rows: the projection in addition
+    assert bench.kernels_per_step(Info(0, 12, 4)) == 5   # projected in the scatter's flush
     assert bench.kernels_per_step(Info(16, 16)) == 6     # CO2 5M: all Gaussian nodes wide
     assert bench.kernels_per_step(Info(24, 216)) == 7    # H2O 100M: merged + narrow-node rows
     assert bench.kernels_per_step(Info(7, 8)) == 6       # odd n_L padded with a zero row

@@ -126,6 +126,14 @@ LAYOUT_CASES = {
     # odd node count (5 x 3 = 15 nodes, a pad node) and pressure shifts
     "odd_shift": (lambda: S.uniform_lines(20_000, 2000.0, 2020.0, seed=34, delta=(-0.01, 0.008)),
                   (28.0, 2000.0, 0.002, 10001, 900.0, 3.0, 0.4), dict(n_G=5, n_L=3)),
+    # 12 x 16 = 192 nodes: more than the scatter's flush projects itself, so
+    # the skeleton rows come from the separate projection pass
+    "wide_12x16": (lambda: S.uniform_lines(100_000, 1000.0, 1600.0, seed=35),
+                   (18.0, 1000.0, 0.005, 120001, 2000.0, 1.0, 0.2), dict(n_G=12, n_L=16)),
+    # the same node grid over 700 001 points: the projection pass takes two
+    # columns per thread
+    "long_12x16": (lambda: S.uniform_lines(200_000, 1000.0, 4500.0, seed=36),
+                   (18.0, 1000.0, 0.005, 700001, 2000.0, 1.0, 0.2), dict(n_G=12, n_L=16)),
 }
 
 
@@ -142,12 +150,26 @@ def test_layouts_same_spectrum(ctx, case, layout):
     gpu, info = run_gpu(ctx, lines, *args, layout=layout, **grid)
     n_nodes = info.grid.n_G * info.grid.n_L
     if layout == 3:
-        assert info.layout == 3, case
+        assert info.layout in (3, 4), case
         assert 0 < info.fft_rows < n_nodes and 0 <= info.layout_err <= 1e-8
     elif layout == 1:
         assert info.layout == 1 and info.fft_rows >= n_nodes
     else:
         assert info.layout in (1, 2)
+    assert rel_err(gpu, oracle(lines, *args, info)) <= TOL
+
+
+@pytest.mark.parametrize("case,accumulator,fused", [("co2_8x16", 32, True), ("co2_8x16", 64, True),
+                                                     ("wide_12x16", 0, False), ("long_12x16", 0, False)])
+def test_skeleton_projection_paths(ctx, case, accumulator, fused):
+    """The skeleton projection in the scatter's flush (32- and 64-bit tile
+    words) and in its own pass (grids of more nodes) against the oracle."""
+    make, args, grid = LAYOUT_CASES[case]
+    lines = make()
+    gpu, info = run_gpu(ctx, lines, *args, layout=3, accumulator=accumulator, **grid)
+    assert info.layout == (4 if fused else 3)
+    if accumulator:
+        assert info.accum_bits == accumulator
     assert rel_err(gpu, oracle(lines, *args, info)) <= TOL
 
 
@@ -159,7 +181,7 @@ def test_skeleton_layout_close_to_node_rows(ctx):
     lines = make()
     a, ia = run_gpu(ctx, lines, *args, layout=1, **grid)
     b, ib = run_gpu(ctx, lines, *args, layout=3, **grid)
-    assert ia.layout == 1 and ib.layout == 3
+    assert ia.layout == 1 and ib.layout in (3, 4)
     assert rel_err(b, a) <= 2e-5
 
 
