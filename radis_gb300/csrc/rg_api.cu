@@ -1267,18 +1267,21 @@ int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const S
         if (ev) CU(cudaEventRecord(ev[2], st));
         VoigtArgs& vr = skel ? *lp.vk : merged ? *lp.vm : *lp.va;
         vr.store_g = vr.n_pairs <= kPairGroup;   // one pair group per row: it stores G itself
+        vr.inv_fused = vr.store_g;                // ... after its inverse row DFT
         if (!vr.store_g) CU(cudaMemsetAsync(W.g, 0, sizeof(float2) * (size_t)W.n, st));
         RG(launch_row_fft_voigt(vr, st));
         if (ev) CU(cudaEventRecord(ev[3], st));
-        RowIfftArgs ra;
-        ra.f2 = W.f2;
-        ra.n1 = W.n1;
-        ra.n2 = W.n2;
-        ra.n = W.n;
-        ra.g = W.g;
-        ra.tw_hi = W.tw_hi;
-        ra.tw_lo = W.tw_lo;
-        RG(launch_row_ifft(ra, st));
+        if (!vr.inv_fused) {
+            RowIfftArgs ra;
+            ra.f2 = W.f2;
+            ra.n1 = W.n1;
+            ra.n2 = W.n2;
+            ra.n = W.n;
+            ra.g = W.g;
+            ra.tw_hi = W.tw_hi;
+            ra.tw_lo = W.tw_lo;
+            RG(launch_row_ifft(ra, st));
+        }
         if (ev) CU(cudaEventRecord(ev[4], st));
         ca.h = W.g;
         ca.out = out;

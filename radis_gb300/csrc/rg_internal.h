@@ -242,6 +242,8 @@ struct VoigtArgs {        // K3 (row FFT + Voigt weights + pair reduction)
     unsigned char nfold[kMaxNodes];
     int any_fold;
     int rowwise;          // 1: row r's transform uses alpha[r], beta[r] (skeleton rows, r < kMaxAxis)
+    int inv_fused;        // 1 (with store_g, one pair group): the CTA also applies the inverse
+                          // row DFT and inverse twiddle (K3b) to its row of sums before storing it
 };
 
 struct RowIfftArgs {      // K3b (inverse row FFT + twiddle, in place)

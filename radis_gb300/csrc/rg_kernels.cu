@@ -1230,6 +1230,27 @@ __global__ void __launch_bounds__(MAXT, MAXT <= 384 ? 2 : 1) k_row_fft_voigt(con
             fbuf = out;
         }
     }
+    if (a.inv_fused) {
+        // K3b on the CTA's own sums: inverse DFT = conj(forward DFT(conj(G))),
+        // through the work buffers (free after the last pair group), then the
+        // inverse four-step twiddle w_N^{-t k1}; the row is stored once
+        float2* f0 = reinterpret_cast<float2*>(sm4);
+        float2* f1 = f0 + row_buf_len(n2);
+        if (jl < ML) {
+#pragma unroll
+            for (int r = 0; r < 8; ++r) f0[jl + r * ML] = conjf2(acc[r]);
+        }
+        __syncthreads();
+        bool padded;
+        const float2* res = fft_row(f0, f1, a.f2, &padded);
+        float2* g = a.g + (int64_t)k1 * n2;
+        for (int t = threadIdx.x; t < n2; t += blockDim.x) {
+            float2 z = conjf2(res[padded ? rp(t) : t]);
+            if (k1 && t) z = cmul(z, conjf2(twiddle_n(a.tw_hi, a.tw_lo, t * k1)));
+            g[t] = z;
+        }
+        return;
+    }
     if (jl < ML) {
         float2* g = a.g + (int64_t)k1 * n2;
         if (a.store_g && gridDim.y == 1) {   // the only pair group of this row: plain stores
