@@ -49,19 +49,26 @@ WORKLOAD = "co2_5M"
 KERNELS_PER_STEP = 5   # plain layout: scatter, column FFT, row FFT + Voigt, inverse row, inverse column
 
 
+def inverse_fused(info):
+    """The inverse row DFT runs inside the forward row kernel when one CTA
+    holds a row's whole pair sum (at most 16 pairs, i.e. 32 FFT rows)."""
+    return int(info.fft_rows) // 2 <= 16
+
+
 def kernels_per_step(info):
-    """Kernels one spectrum launches: the plain five; with the skeleton layout
-    the projection in addition; with the merged layout the Gaussian stage and
-    the merged-row column FFT instead of the column FFT, plus a column FFT of
-    the narrow-node rows when there are any."""
+    """Kernels one spectrum launches: scatter, column FFT, row FFT + Voigt,
+    inverse row FFT (unless fused into the row kernel) and inverse column
+    FFT; with the skeleton layout the projection in addition (none when the
+    scatter projects); with the merged layout the Gaussian stage and the
+    merged-row column FFT instead of the column FFT, plus a column FFT of the
+    narrow-node rows when there are any."""
+    base = KERNELS_PER_STEP - (1 if inverse_fused(info) else 0)
     if int(info.layout) == 3:
-        return KERNELS_PER_STEP + 1
-    if int(info.layout) == 4:
-        return KERNELS_PER_STEP
-    if not info.merged_rows:
-        return KERNELS_PER_STEP
+        return base + 1
+    if int(info.layout) == 4 or not info.merged_rows:
+        return base
     nlv = info.merged_rows + (info.merged_rows & 1)
-    return KERNELS_PER_STEP + 1 + (1 if info.fft_rows > nlv else 0)
+    return base + 1 + (1 if info.fft_rows > nlv else 0)
 STAGES = ["k_scatter", "k_col_fft_fwd", "k_row_fft_voigt", "k_row_ifft", "k_col_ifft"]
 LAYOUT_NAMES = {1: "node rows", 2: "merged rows", 3: "skeleton rows", 4: "skeleton rows, projected in the scatter"}
 
@@ -191,6 +198,8 @@ def algorithmic_bytes(n_lines_read, line_bytes, n_nodes, n_v, n_ft, info):
         "k_row_ifft": 2 * n_ft * 8,
         "k_col_ifft": n_ft * 8 + n_v * 4,
     }
+    if inverse_fused(info):   # G written once, after the inverse part
+        out.pop("k_row_ifft")
     NL = int(info.merged_rows)
     if NL:
         nlv = NL + (NL & 1)
@@ -243,10 +252,13 @@ def _synthetic():
     return mod
 
 
-def load_workload(wl):
+def load_workload(wl, n_lines=None):
+    """The workload's seeded line list (its own size, or the first draw of
+    ``n_lines`` lines of the same generator: same geometry, fewer lines, for
+    small profiling cases) and its grid."""
     S = _synthetic()
     _, fac, M, vmin, vmax, ws, T, p, x, nG, nL = WORKLOADS[wl]
-    lines = getattr(S, fac)()
+    lines = getattr(S, fac)() if not n_lines else getattr(S, fac)(n=int(n_lines))
     return lines, M, vmin, ws, S.grid_points(vmin, vmax, ws), T, p, x, nG, nL
 
 
@@ -670,6 +682,8 @@ def kernel_times(stage_avg, gauss, info):
     stage is the Gaussian stage (its own event) followed by the column FFT,
     with the skeleton layout the projection followed by the column FFT."""
     kt = {STAGES[i]: stage_avg[i] for i in range(5)}
+    if inverse_fused(info):   # one kernel: its stage ends after its inverse part
+        kt["k_row_fft_voigt"] += kt.pop("k_row_ifft")
     if int(info.layout) == 3:
         kt["k_node_project"] = gauss
         kt["k_col_fft_fwd"] = stage_avg[1] - gauss
@@ -744,13 +758,13 @@ def run_ours(args):
     from radis_gb300 import _lib as L, synthetic as S
 
     wl = args.workload
-    lines, M, vmin, dv, n_v, T, p, x, nG, nL = load_workload(wl)
+    lines, M, vmin, dv, n_v, T, p, x, nG, nL = load_workload(wl, args.lines)
     n_lines = len(lines["v0"])
     lb = line_record_bytes(lines)
     ctx = L.Context(local)
     t0 = time.perf_counter()
     ln = L.Lines(ctx, lines, M)
-    plan = L.Plan(ln, vmin, dv, n_v, n_G=nG, n_L=nL)
+    plan = L.Plan(ln, vmin, dv, n_v, n_G=nG, n_L=nL, layout=args.layout)
     setup_s = time.perf_counter() - t0
     g = plan.grid(T, p, x)
     n_nodes = g.n_G * g.n_L + (g.n_G * g.n_L) % 2
@@ -820,7 +834,7 @@ def run_ours(args):
     for _ in range(2 if n_lines <= 10_000_000 else 1):
         t0 = time.perf_counter()
         ln2 = L.Lines(ctx, lines, M)
-        pl2 = L.Plan(ln2, vmin, dv, n_v, n_G=nG, n_L=nL)
+        pl2 = L.Plan(ln2, vmin, dv, n_v, n_G=nG, n_L=nL, layout=args.layout)
         pl2.synthesize_host(T, p, x, out=host)
         cold.append(time.perf_counter() - t0)
         pl2.close()
@@ -870,6 +884,13 @@ def run_ours(args):
                            "skeleton_sampled_err": float(info.layout_err)},
             "setup_s": setup_s,
         }
+        if name == "k_scatter" and int(info.layout) == 4:
+            res["roofline"]["note"] = (
+                "the scatter writes only the skeleton rows: each finished tile is projected onto them in shared "
+                f"memory ({g.n_G * g.n_L} x {int(info.fft_rows)} FMA per grid column), so the kernel moves "
+                f"{ab[name] / 1e6:.0f} MB instead of {(lines_in_window * lb + n_nodes * n_v * 4) / 1e6:.0f} MB "
+                "and is bound by its instruction issue, not HBM; frac is the HBM fraction of the bytes it must "
+                "move")
         if name == "k_gauss_merge":
             res["roofline"]["note"] = ("the real-space Gaussian stage is FP32-FMA-bound (a banded convolution of "
                                        "each wide-node row with its residual Gaussian, ~200 FMA per merged "
@@ -1016,6 +1037,10 @@ def main():
     ap.add_argument("--no-c3", action="store_true", help="skip the 100M-line H2O-like section")
     ap.add_argument("--no-c3-check", action="store_true", help="skip its full-size oracle comparison")
     ap.add_argument("--no-fft-compare", action="store_true", help="skip the cuFFT comparison")
+    ap.add_argument("--layout", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="FFT-stage layout of the timed plan (0: the fewest rows; 1 node, 2 merged, 3 skeleton)")
+    ap.add_argument("--lines", type=int, default=0,
+                    help="profiling cases: the workload's geometry with this many lines of its generator")
     ap.add_argument("--serve-requests", type=int, default=120)
     ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--serve-h2o-lines", type=int, default=100_000_000)

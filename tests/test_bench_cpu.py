@@ -91,13 +91,15 @@ def test_kernels_per_step():
             self.merged_rows, self.fft_rows = merged_rows, fft_rows
             self.layout = layout if layout is not None else (2 if merged_rows else 1)
 
+    # up to 32 FFT rows the inverse row DFT runs inside the row kernel
     assert bench.kernels_per_step(Info(0, 128)) == 5     # plain layout
-    assert bench.kernels_per_step(Info(0, 12, 3)) == 6   # skeleton rows: the projection in addition
-    assert bench.kernels_per_step(Info(0, 12, 4)) == 5   # projected in the scatter's flush
-    assert bench.kernels_per_step(Info(16, 16)) == 6     # CO2 5M: all Gaussian nodes wide
+    assert bench.kernels_per_step(Info(0, 12, 3)) == 5   # skeleton rows: the projection in addition
+    assert bench.kernels_per_step(Info(0, 12, 4)) == 4   # projected in the scatter's flush
+    assert bench.kernels_per_step(Info(0, 40, 3)) == 6   # more rows: separate inverse row DFT
+    assert bench.kernels_per_step(Info(16, 16)) == 5     # CO2 5M: all Gaussian nodes wide
     assert bench.kernels_per_step(Info(24, 216)) == 7    # H2O 100M: merged + narrow-node rows
-    assert bench.kernels_per_step(Info(7, 8)) == 6       # odd n_L padded with a zero row
-    assert bench.kernels_per_step(Info(7, 16)) == 7
+    assert bench.kernels_per_step(Info(7, 8)) == 5       # odd n_L padded with a zero row
+    assert bench.kernels_per_step(Info(7, 16)) == 6
 
 
 def _max_worker(rank, port, q):
