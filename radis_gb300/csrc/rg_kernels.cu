@@ -756,33 +756,43 @@ __device__ __forceinline__ void scatter_body(const ScatterArgs& a) {
             return;
         }
         if (proj) {
-            // skeleton rows of the finished tile: warp task (32-column group,
-            // block of 4 rows); lane c sums its column over the node rows with
-            // the block's 4 coefficients (one 16-byte broadcast load per node)
-            const int ncg = (tk + 31) >> 5, nrb = a.proj_rp >> 2;
+            // skeleton rows of the finished tile: warp task (64-column group,
+            // block of 4 rows); lane l sums columns l and l + 32 of its group
+            // (each load conflict-free across the warp) over the node rows, one
+            // 16-byte broadcast coefficient load per node for 8 FMAs
+            const int ncg = (tk + 63) >> 6, nrb = a.proj_rp >> 2;
             for (int t = cw; t < ncg * nrb; t += n_cons_warps) {
                 const int cg = t % ncg, rb = t / ncg;
-                const int c = (cg << 5) + lane;
+                const int c = (cg << 6) + lane;
                 if (c >= tk) continue;
                 const Acc* col = tile + c;
                 const float4* cf = reinterpret_cast<const float4*>(coef) + rb;
                 const int cstep = a.proj_rp >> 2;
-                float y0 = 0.f, y1 = 0.f, y2 = 0.f, y3 = 0.f;
+                const bool two = c + 32 < tk;
+                float y0 = 0.f, y1 = 0.f, y2 = 0.f, y3 = 0.f, z0 = 0.f, z1 = 0.f, z2 = 0.f, z3 = 0.f;
 #pragma unroll 4
                 for (int nd = 0; nd < a.n_real; ++nd) {
                     const float v = Fx<Acc>::to_float(col[nd * pitch]);
+                    const float u = two ? Fx<Acc>::to_float(col[nd * pitch + 32]) : 0.f;
                     const float4 w = cf[nd * cstep];
                     y0 = fmaf(w.x, v, y0);
                     y1 = fmaf(w.y, v, y1);
                     y2 = fmaf(w.z, v, y2);
                     y3 = fmaf(w.w, v, y3);
+                    z0 = fmaf(w.x, u, z0);
+                    z1 = fmaf(w.y, u, z1);
+                    z2 = fmaf(w.z, u, z2);
+                    z3 = fmaf(w.w, u, z3);
                 }
                 const int r = rb << 2;
                 float* dst = a.ldm + (int64_t)r * a.row_stride + k_start + c;
-                if (r < a.proj_rows) __stcs(dst, y0 * inv_fx);
-                if (r + 1 < a.proj_rows) __stcs(dst + a.row_stride, y1 * inv_fx);
-                if (r + 2 < a.proj_rows) __stcs(dst + 2 * a.row_stride, y2 * inv_fx);
-                if (r + 3 < a.proj_rows) __stcs(dst + 3 * a.row_stride, y3 * inv_fx);
+                const float ys[4] = {y0, y1, y2, y3}, zs[4] = {z0, z1, z2, z3};
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    if (r + i >= a.proj_rows) break;
+                    __stcs(dst + i * a.row_stride, ys[i] * inv_fx);
+                    if (two) __stcs(dst + i * a.row_stride + 32, zs[i] * inv_fx);
+                }
             }
             asm volatile("bar.sync 1, %0;" ::"r"(nct) : "memory");   // every read of the tile done
             for (int i = ct; i < n_words; i += nct) tile[i] = 0;
