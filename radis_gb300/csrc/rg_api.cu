@@ -1029,9 +1029,27 @@ bool plan_skeleton(Work& W, const SpecHost& s, const VoigtArgs& va, int r_max, V
         if (R < 1 || rows > r_max) return false;
         const int rp = proj_rows_pad(rows);
         if ((size_t)n * rp * sizeof(float) > 96 * 1024) return false;   // coefficients in shared memory
-        W.proj_host.assign((size_t)n * rp, 0.f);
+        // [n][rp] coefficients (the FP32 forms), then the tensor-core pass's B
+        // fragments: TF32 hi / lo parts, [nr][ks][part][lane][2] with
+        // b0, b1 = C[8 nr + g][8 ks + t], C[8 nr + g][8 ks + t + 4], g = lane / 4,
+        // t = lane % 4
+        const int NR = (rows + 7) / 8, KSP = 2 * ((n + 15) / 16);
+        W.proj_host.assign((size_t)n * rp + (size_t)NR * KSP * 128, 0.f);
         for (int r = 0; r < R; ++r)
             for (int node = 0; node < n; ++node) W.proj_host[(size_t)node * rp + r] = (float)C[(size_t)r * n + node];
+        float* fr = W.proj_host.data() + (size_t)n * rp;
+        auto cf = [&](int r, int k) { return r < R && k < n ? (float)C[(size_t)r * n + k] : 0.f; };
+        for (int nr = 0; nr < NR; ++nr)
+            for (int ks = 0; ks < KSP; ++ks)
+                for (int lane = 0; lane < 32; ++lane) {
+                    const int g = lane >> 2, t = lane & 3;
+                    const float v[2] = {cf(8 * nr + g, 8 * ks + t), cf(8 * nr + g, 8 * ks + t + 4)};
+                    for (int i = 0; i < 2; ++i) {
+                        const float hi = tf32_round_host(v[i]);
+                        fr[((size_t)(nr * KSP + ks) * 2 + 0) * 64 + lane * 2 + i] = hi;
+                        fr[((size_t)(nr * KSP + ks) * 2 + 1) * 64 + lane * 2 + i] = tf32_round_host(v[i] - hi);
+                    }
+                }
         W.skel_nodes.assign(sk.begin(), sk.begin() + R);
         W.skel_R = R;
         W.skel_err = err;
@@ -1070,6 +1088,8 @@ bool plan_skeleton(Work& W, const SpecHost& s, const VoigtArgs& va, int r_max, V
     pa->n_nodes = n;   // the pad node row of an odd grid is not read
     pa->rows = rows;
     pa->rows_pad = rp;
+    pa->mtiles = (rows + 7) / 8;   // the tensor-core pass's 8-row n-tiles
+    pa->ksteps = 2 * ((n + 15) / 16);
     *err_out = err;
     return true;
 }
@@ -1154,6 +1174,8 @@ int plan_layout(Work& W, const SpecHost& s, cudaStream_t st, LayoutPlan* lp) {
             W.skel_dev = true;
         }
         lp->pa.coef = W.proj_coef;
+        // the tensor-core fragments follow the [n][rp] coefficients
+        lp->pa.frag = W.proj_coef + (size_t)lp->pa.n_nodes * lp->pa.rows_pad;
     }
     return RG_OK;
 }

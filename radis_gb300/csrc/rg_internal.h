@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -274,7 +275,24 @@ struct ProjArgs {
     int rows_pad;         // coefficient row pitch (the kernel's row block)
     const float* coef;    // [n_nodes][rows_pad]
     int sms;              // SMs of the device (persistent grid)
+    // tensor-core form: the coefficients as TF32 hi / lo parts in the B
+    // fragments of mma.m16n8k8 (rows in blocks of 8, nodes in steps of 8):
+    // frag[((nr * ksteps + ks) * 2 + part) * 64 + lane * 2 + i]
+    const float* frag;    // null: FP32 pass
+    int mtiles;           // row blocks of 8 (<= 8)
+    int ksteps;           // node steps of 8 in frag (a multiple of 2)
 };
+// TF32 (10-bit mantissa) rounding to nearest even, as the host prepares the
+// tensor-core operands; x - tf32(x) is exact in FP32
+inline float tf32_round_host(float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    u += 0x0FFFu + ((u >> 13) & 1u);
+    u &= 0xFFFFE000u;
+    float r;
+    std::memcpy(&r, &u, 4);
+    return r;
+}
 
 constexpr int kGaussPer = 8;          // outputs per thread
 constexpr int kGaussTile = 256 * kGaussPer;   // outputs per CTA (256 threads)

@@ -2138,6 +2138,158 @@ int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st) {
 // Row block of the projection: the rows rounded up to a multiple of 4.
 int proj_rows_pad(int rows) { return (rows + 3) & ~3; }
 
+// Tensor-core form of the projection pass: Y^T[columns x rows] = X^T[columns
+// x nodes] C^T[nodes x rows] with mma.sync m16n8k8 TF32 (columns as M, rows
+// as N in steps of 8, nodes as K), each product split into three TF32
+// products (hi hi + lo hi + hi lo; x = hi + lo with hi = tf32(x), lo =
+// tf32(x - hi)): ~22 significant bits per operand, FP32-level sums.  CTA = 8
+// warps over a 256-column tile; warp w owns columns 32 w .. 32 w + 31 as two
+// 16-column m-tiles, for every 8-row n-tile (NR of them), accumulators in
+// registers; the three products of a k-step are issued part by part over all
+// 2 NR accumulators (independent MMAs between dependent ones).  Node rows
+// stream through kTcStages shared-memory stages of 16 rows (cp.async,
+// zero-filled past n_v and past the last node), row pitch 264 floats: the A
+// fragment loads (node t / t + 4, column g / g + 8 of each m-tile) are
+// conflict-free.  The B fragments (coefficients, hi and lo parts, prepared on
+// the host in fragment order) sit in shared memory, 8 bytes per lane per part.
+constexpr int kTcTC = 256;                // columns per CTA tile (8 warps x 32)
+constexpr int kTcKC = 16;                 // node rows per stage (two k-steps)
+constexpr int kTcPitch = kTcTC + 8;       // staged row pitch (floats)
+constexpr int kTcStages = 3;
+
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+template <int NR>
+__global__ void __launch_bounds__(256, 2) k_node_project_tc(const ProjArgs a) {
+    constexpr int S = kTcStages;
+    extern __shared__ __align__(16) float tsm[];
+    const int KSP = a.ksteps;                             // node steps of 8 (even, covers n_nodes)
+    const int n_chunks = KSP / 2;                         // 16-node chunks per tile
+    float* fr = tsm;                                      // fragments [NR][KSP][2][32][2]
+    float* xs = tsm + NR * KSP * 128;                     // stages [S][kTcKC][kTcPitch]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = lane >> 2, t = lane & 3;
+    const int n_tiles = (int)((a.n_v + kTcTC - 1) / kTcTC);
+    const int my_tiles = (n_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
+    const int total = my_tiles * n_chunks;
+    auto tile_k0 = [&](int tt) { return (int64_t)((int)blockIdx.x + tt * (int)gridDim.x) * kTcTC; };
+    // this thread's 16-byte pieces of a stage: rows r_0 + 4 i, columns 4 c4_t
+    const int r_0 = threadIdx.x / (kTcTC / 4), c4_t = threadIdx.x % (kTcTC / 4);
+    auto issue = [&](int gq) {
+        const int64_t k = tile_k0(gq / n_chunks) + 4 * c4_t;
+        const int nd0 = (gq % n_chunks) * kTcKC + r_0;
+        float* dst = xs + (gq % S) * kTcKC * kTcPitch + r_0 * kTcPitch + 4 * c4_t;
+        const float* src = a.ldm + (int64_t)nd0 * a.row_stride + k;
+        const bool col_ok = k < a.n_v;   // a piece past n_v stays in the row's padding
+#pragma unroll
+        for (int i = 0; i < kTcKC * kTcTC / 4 / 256; ++i) {
+            const bool ok = col_ok && nd0 + 4 * i < a.n_nodes;
+            cp_async16(dst + 4 * i * kTcPitch, ok ? src + (int64_t)4 * i * a.row_stride : a.ldm, ok ? 16 : 0);
+        }
+    };
+#pragma unroll
+    for (int q = 0; q < S - 1; ++q) {
+        if (q < total) issue(q);
+        cp_async_commit();
+    }
+    {
+        const float4* src = reinterpret_cast<const float4*>(a.frag);
+        float4* dst = reinterpret_cast<float4*>(fr);
+        for (int i = threadIdx.x; i < NR * KSP * 32; i += blockDim.x) dst[i] = __ldg(&src[i]);
+    }
+    for (int tt = 0; tt < my_tiles; ++tt) {
+        float d[2][NR][4];
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+#pragma unroll
+            for (int nr = 0; nr < NR; ++nr)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) d[m][nr][i] = 0.f;
+        for (int ch = 0; ch < n_chunks; ++ch) {
+            const int gq = tt * n_chunks + ch;
+            cp_async_wait<S - 2>();
+            __syncthreads();
+            if (gq + S - 1 < total) issue(gq + S - 1);
+            cp_async_commit();
+            const float* xb = xs + (gq % S) * kTcKC * kTcPitch + warp * 32 + g;
+#pragma unroll
+            for (int s2 = 0; s2 < 2; ++s2) {
+                const int ks = 2 * ch + s2;
+                // A fragments (two m-tiles): (col g / g + 8, node t / t + 4), hi and lo
+                uint32_t ah[2][4], al[2][4];
+#pragma unroll
+                for (int m = 0; m < 2; ++m) {
+                    const float* xm = xb + (8 * s2 + t) * kTcPitch + 16 * m;
+                    const float v[4] = {xm[0], xm[8], xm[4 * kTcPitch], xm[4 * kTcPitch + 8]};
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        ah[m][i] = tf32_rna(v[i]);
+                        al[m][i] = tf32_rna(v[i] - __uint_as_float(ah[m][i]));
+                    }
+                }
+                uint32_t bh[NR][2], bl[NR][2];
+#pragma unroll
+                for (int nr = 0; nr < NR; ++nr) {
+                    const float* f = fr + ((nr * KSP + ks) * 2) * 64 + lane * 2;
+                    const float2 h = *reinterpret_cast<const float2*>(f);
+                    const float2 l = *reinterpret_cast<const float2*>(f + 64);
+                    bh[nr][0] = __float_as_uint(h.x);
+                    bh[nr][1] = __float_as_uint(h.y);
+                    bl[nr][0] = __float_as_uint(l.x);
+                    bl[nr][1] = __float_as_uint(l.y);
+                }
+#pragma unroll
+                for (int m = 0; m < 2; ++m)
+#pragma unroll
+                    for (int nr = 0; nr < NR; ++nr) mma_tf32(d[m][nr], ah[m], bh[nr][0], bh[nr][1]);
+#pragma unroll
+                for (int m = 0; m < 2; ++m)
+#pragma unroll
+                    for (int nr = 0; nr < NR; ++nr) mma_tf32(d[m][nr], al[m], bh[nr][0], bh[nr][1]);
+#pragma unroll
+                for (int m = 0; m < 2; ++m)
+#pragma unroll
+                    for (int nr = 0; nr < NR; ++nr) mma_tf32(d[m][nr], ah[m], bl[nr][0], bl[nr][1]);
+            }
+        }
+        // the tile is complete: d[m][nr] = (column g / g + 8 of m-tile m, row 8 nr + 2 t / + 1)
+        const int64_t kc = tile_k0(tt) + warp * 32 + g;
+#pragma unroll
+        for (int m = 0; m < 2; ++m)
+#pragma unroll
+            for (int nr = 0; nr < NR; ++nr)
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int r = 8 * nr + 2 * t + (i & 1);
+                    const int64_t k = kc + 16 * m + 8 * (i >> 1);
+                    if (r < a.rows && k < a.n_v) a.ldm[(int64_t)r * a.row_stride + k] = d[m][nr][i];
+                }
+    }
+}
+
+template <int NR>
+int launch_proj_tc(const ProjArgs& a, cudaStream_t st) {
+    const size_t smem = sizeof(float) * ((size_t)NR * a.ksteps * 128 + (size_t)kTcStages * kTcKC * kTcPitch);
+    ALLOW_SMEM((k_node_project_tc<NR>), smem);
+    const int64_t tiles = (a.n_v + kTcTC - 1) / kTcTC;
+    // two CTAs per SM where their shared memory fits (fragments of up to ~4 row
+    // blocks of a 288-node grid), else one
+    const int per_sm = smem <= 110 * 1024 ? 2 : 1;
+    const int grid = (int)std::min<int64_t>(tiles, (int64_t)per_sm * std::max(a.sms, 1));
+    k_node_project_tc<NR><<<grid, 256, smem, st>>>(a);
+    return check_launch();
+}
+
 // one launcher per instantiation: its shared-memory opt-in is its own
 template <int RB, int CPT>
 int launch_proj_kernel(const ProjArgs& a, int slots, cudaStream_t st) {
@@ -2175,6 +2327,22 @@ int launch_node_project(const ProjArgs& a, cudaStream_t st) {
     if (a.rows <= 0 || a.rows > kProjMaxRows || a.rows_pad != proj_rows_pad(a.rows) || a.n_nodes <= 0 ||
         a.n_v <= 0 || a.row_stride % 4 != 0)
         return RG_ERR_ARG;
+    // the tensor-core pass while its fragments and stages fit 200 KB of shared memory
+    const size_t tc_smem = sizeof(float) * ((size_t)a.mtiles * a.ksteps * 128 + (size_t)kTcStages * kTcKC * kTcPitch);
+    if (a.frag && tc_smem <= 200 * 1024) {
+        if (a.mtiles != (a.rows + 7) / 8 || a.ksteps < (a.n_nodes + 7) / 8 || a.ksteps % 2) return RG_ERR_ARG;
+        switch (a.mtiles) {
+        case 1: return launch_proj_tc<1>(a, st);
+        case 2: return launch_proj_tc<2>(a, st);
+        case 3: return launch_proj_tc<3>(a, st);
+        case 4: return launch_proj_tc<4>(a, st);
+        case 5: return launch_proj_tc<5>(a, st);
+        case 6: return launch_proj_tc<6>(a, st);
+        case 7: return launch_proj_tc<7>(a, st);
+        case 8: return launch_proj_tc<8>(a, st);
+        default: return RG_ERR_ARG;
+        }
+    }
     return launch_proj_dispatch<4>(a, st);
 }
 
