@@ -861,8 +861,8 @@ def run_ours(args):
             "e2e": {"value": ws * 1000.0 / e2e_ms, "unit": "spectra/s",
                     "h2d_bytes_per_step": 0, "d2h_bytes_per_step": n_v * 4,
                     "note": ("resident line list (as the reference's gpuApp.iterate); per step the conditions "
-                             "travel as kernel parameters and the float32 spectrum is copied to pinned host "
-                             "memory")},
+                             "travel as kernel parameters and the spectrum's last kernel writes the float32 "
+                             "spectrum into the caller's pinned host buffer (over NVLink-C2C)")},
             "e2e_varied_T": {"value": ws * 1000.0 / e2e_var_ms, "unit": "spectra/s",
                              "h2d_bytes_per_step": 0, "d2h_bytes_per_step": n_v * 4,
                              "note": ("as e2e with T raised by 0.1 K every step: new node axes each step, so the "

@@ -250,9 +250,10 @@ int rg_synthesize(rg_plan* plan, const rg_conditions* cond, float* out_dev, void
  * Planck at cond->T) in physical units.  Asynchronous on `stream`. */
 int rg_synthesize_quantities(rg_plan* plan, const rg_conditions* cond, double path_length, float* out_dev,
                              void* stream, rg_spectrum_info* info);
-/* The same into host memory (5 n_v floats, pinned or pageable), blocking:
- * the drop-in form of gpuApp.iterate + the host post-processing of
- * eq_spectrum_gpu (factory.py:1247-1297).  timing = 1 fills info->stage_ms. */
+/* The same into host memory (5 n_v floats; page-locked memory is written by
+ * the last kernel itself, pageable memory gets a copy), blocking: the drop-in
+ * form of gpuApp.iterate + the host post-processing of eq_spectrum_gpu
+ * (factory.py:1247-1297).  timing = 1 fills info->stage_ms. */
 int rg_synthesize_quantities_host(rg_plan* plan, const rg_conditions* cond, double path_length,
                                   float* out_host, void* stream, int timing, rg_spectrum_info* info);
 
@@ -312,9 +313,11 @@ int rg_plan_stage_times(rg_plan* plan, double* sum_ms, int64_t* count);
  * rg_plan_stage_times call returned, in ms (0 without the merged layout). */
 int rg_plan_stage_times_gauss(rg_plan* plan, double* gauss_sum_ms);
 
-/* As rg_synthesize, then copies the n_v floats to `out_host` (pinned or
- * pageable) and waits for the copy: the drop-in `iterate()` form.  timing = 1
- * fills info->stage_ms (0 or 2 leave it empty). */
+/* As rg_synthesize into `out_host` (n_v floats), and waits: the drop-in
+ * `iterate()` form.  Page-locked host memory (cudaHostAlloc'd or registered)
+ * is written by the spectrum's last kernel itself; pageable memory gets a copy
+ * from device memory after it.  timing = 1 fills info->stage_ms (0 or 2 leave
+ * it empty). */
 int rg_synthesize_host(rg_plan* plan, const rg_conditions* cond, float* out_host,
                        void* stream, int timing, rg_spectrum_info* info);
 

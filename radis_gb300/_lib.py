@@ -440,13 +440,16 @@ class Plan:
 
     QUANTITIES = ("abscoeff", "absorbance", "emissivity_noslit", "transmittance_noslit", "radiance_noslit")
 
-    def synthesize_quantities_host(self, T, p_bar, x, path_length, q_ratio=None, timing=False):
+    def synthesize_quantities_host(self, T, p_bar, x, path_length, q_ratio=None, timing=False, out=None):
         """Blocking: ({quantity: float32 array n_v}, SpectrumInfo) with the
         post-processing fused into the spectrum's last kernel.  abscoeff and
         absorbance are in units of exp(info.log_scale); emissivity,
-        transmittance and radiance (mW/cm2/sr/nm) in physical units."""
+        transmittance and radiance (mW/cm2/sr/nm) in physical units.  ``out``:
+        optional float32 buffer of 5 n_v (page-locked memory is written by the
+        kernel itself)."""
         c, _q = self._cond(T, p_bar, x, q_ratio)
-        out = np.empty(5 * self.n_v, dtype=np.float32)
+        if out is None:
+            out = np.empty(5 * self.n_v, dtype=np.float32)
         info = SpectrumInfo()
         check(load().rg_synthesize_quantities_host(self.handle, C.byref(c), float(path_length), ptr(out), None,
                                                    1 if timing else 0, C.byref(info)))

@@ -1921,6 +1921,20 @@ int rg_synthesize(rg_plan* P, const rg_conditions* c, float* out_dev, void* stre
 namespace {
 // One spectrum with the post-processing rows written by its last kernel into
 // out_dev + n_v (4 rows); the epilogue request is cleared on every return.
+// Device address of page-locked host memory (cudaHostAlloc'd or registered:
+// mapped into the device's address space under unified addressing), or null.
+// The spectrum's last kernel then stores into the caller's buffer itself
+// (over NVLink-C2C on a Grace host) instead of a copy after it.
+float* mapped_host(void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    return static_cast<float*>(a.devicePointer);
+}
+
 int run_quantities(rg_plan* P, const rg_conditions* c, double path_length, float* out_dev, cudaStream_t st,
                    int timing, rg_spectrum_info* info) {
     struct Clear {
@@ -1959,9 +1973,10 @@ int rg_synthesize_quantities_host(rg_plan* P, const rg_conditions* c, double pat
     CU(dev_guard_.use(P->lines->ctx->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
     const size_t n5 = 5 * (size_t)P->w.desc.n_v;
-    if (!P->quant_d) CU(cudaMalloc((void**)&P->quant_d, sizeof(float) * n5));
-    RG(run_quantities(P, c, path_length, P->quant_d, st, (timing && info) ? 1 : 0, info));
-    CU(cudaMemcpyAsync(out_host, P->quant_d, sizeof(float) * n5, cudaMemcpyDeviceToHost, st));
+    float* direct = mapped_host(out_host);   // page-locked: written by the last kernel
+    if (!direct && !P->quant_d) CU(cudaMalloc((void**)&P->quant_d, sizeof(float) * n5));
+    RG(run_quantities(P, c, path_length, direct ? direct : P->quant_d, st, (timing && info) ? 1 : 0, info));
+    if (!direct) CU(cudaMemcpyAsync(out_host, P->quant_d, sizeof(float) * n5, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
     return take_err(P->w);
 }
@@ -2085,8 +2100,10 @@ int rg_synthesize_host(rg_plan* P, const rg_conditions* c, float* out_host, void
     DeviceGuard dev_guard_;
     CU(dev_guard_.use(P->lines->ctx->device));
     cudaStream_t st = stream ? (cudaStream_t)stream : P->lines->ctx->stream;
-    RG(run_spectrum(P, c, P->out_d, st, (timing && info) ? 1 : 0, false, info));
-    CU(cudaMemcpyAsync(out_host, P->out_d, sizeof(float) * (size_t)P->w.desc.n_v, cudaMemcpyDeviceToHost, st));
+    float* direct = mapped_host(out_host);   // page-locked: written by the last kernel
+    RG(run_spectrum(P, c, direct ? direct : P->out_d, st, (timing && info) ? 1 : 0, false, info));
+    if (!direct)
+        CU(cudaMemcpyAsync(out_host, P->out_d, sizeof(float) * (size_t)P->w.desc.n_v, cudaMemcpyDeviceToHost, st));
     CU(cudaStreamSynchronize(st));
     return take_err(P->w);
 }

@@ -173,6 +173,29 @@ def test_skeleton_projection_paths(ctx, case, accumulator, fused):
     assert rel_err(gpu, oracle(lines, *args, info)) <= TOL
 
 
+def test_host_output_page_locked_and_pageable(ctx):
+    """The host entry points into page-locked memory (written by the last
+    kernel itself) and into pageable memory (copied after it) give the same
+    bytes, for the spectrum and for the fused quantities."""
+    import torch
+    make, args, grid = LAYOUT_CASES["co2_8x16"]
+    lines = make()
+    M, vmin, dv, n_v, T, p, x = args
+    ln = L.Lines(ctx, lines, M)
+    plan = L.Plan(ln, vmin, dv, n_v, **grid)
+    pinned = torch.empty(n_v, dtype=torch.float32, pin_memory=True).numpy()
+    a, _ = plan.synthesize_host(T, p, x, out=pinned)
+    b, _ = plan.synthesize_host(T, p, x, out=np.empty(n_v, np.float32))
+    assert a is pinned and np.array_equal(a, b) and np.max(a) > 0
+    pq = torch.empty(5 * n_v, dtype=torch.float32, pin_memory=True).numpy()
+    qa, _ = plan.synthesize_quantities_host(T, p, x, 1.0, out=pq)
+    qb, _ = plan.synthesize_quantities_host(T, p, x, 1.0)
+    for k in qa:
+        assert np.array_equal(qa[k], qb[k]), k
+    plan.close()
+    ln.close()
+
+
 def test_skeleton_layout_close_to_node_rows(ctx):
     """Skeleton rows and node rows on the same inputs agree far below the
     parity bar (the decomposition's error is 1e-8 of each transform's peak;
