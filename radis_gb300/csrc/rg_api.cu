@@ -180,6 +180,13 @@ struct Work {
     // function of the axes, spacing, folding threshold and tolerance); the
     // device copy of its coefficients is current while skel_dev is set
     double skel_key[10] = {0};
+    // the per-node folded-Voigt parameters of the last grid (fill_voigt_args),
+    // reused while the axes, spacing and folding threshold repeat
+    double va_key[8] = {0};
+    bool va_valid = false;
+    std::vector<float> va_norm, va_lnorm, va_alpha, va_beta;
+    std::vector<unsigned char> va_nfold;
+    int va_any_fold = 0;
     bool skel_valid = false, skel_dev = false;
     int skel_R = 0;
     double skel_err = 0.0;
@@ -774,7 +781,7 @@ void node_fold(double dv, double wG, double wL, double thresh, int* nfold, doubl
 
 // Row-kernel arguments of one spectrum: FFT geometry and the folded,
 // normalised Voigt FT parameters of every node of the grid.
-void fill_voigt_args(const Work& W, const SpecHost& s, VoigtArgs* va) {
+void fill_voigt_args(Work& W, const SpecHost& s, VoigtArgs* va) {
     const rg_grid& g = s.grid;
     va->f2 = W.f2;
     va->threads = row_threads(W.f2);
@@ -794,6 +801,16 @@ void fill_voigt_args(const Work& W, const SpecHost& s, VoigtArgs* va) {
     va->inv_ndv = (float)(1.0 / ((double)W.n * W.desc.dv));
     va->half_fs = (float)(0.5 / W.desc.dv);
     const double thresh = W.desc.folding_thresh > 0 ? W.desc.folding_thresh : 1e-6;
+    const double key[8] = {g.log_wG_min, g.dxG, (double)g.n_G, g.log_wL_min, g.dxL, (double)g.n_L, W.desc.dv, thresh};
+    if (W.va_valid && std::equal(key, key + 8, W.va_key) && (int)W.va_norm.size() == s.n_nodes) {
+        std::copy(W.va_alpha.begin(), W.va_alpha.end(), va->alpha);
+        std::copy(W.va_beta.begin(), W.va_beta.end(), va->beta);
+        std::copy(W.va_norm.begin(), W.va_norm.end(), va->norm);
+        std::copy(W.va_lnorm.begin(), W.va_lnorm.end(), va->lnorm);
+        std::copy(W.va_nfold.begin(), W.va_nfold.end(), va->nfold);
+        va->any_fold = W.va_any_fold;
+        return;
+    }
     for (int l = 0; l < g.n_G; ++l) {
         double wG = std::exp(g.log_wG_min + l * g.dxG);
         va->alpha[l] = (float)(std::pow(kPi * wG, 2) / (4.0 * kLn2) * kLog2e);
@@ -820,6 +837,14 @@ void fill_voigt_args(const Work& W, const SpecHost& s, VoigtArgs* va) {
         va->nfold[node] = (unsigned char)nf;
         if (nf) va->any_fold = 1;
     }
+    std::copy(key, key + 8, W.va_key);
+    W.va_alpha.assign(va->alpha, va->alpha + g.n_G);
+    W.va_beta.assign(va->beta, va->beta + g.n_L);
+    W.va_norm.assign(va->norm, va->norm + s.n_nodes);
+    W.va_lnorm.assign(va->lnorm, va->lnorm + s.n_nodes);
+    W.va_nfold.assign(va->nfold, va->nfold + s.n_nodes);
+    W.va_any_fold = va->any_fold;
+    W.va_valid = true;
 }
 
 // Merged layout of one spectrum.  Without folding, the Voigt FT of node
