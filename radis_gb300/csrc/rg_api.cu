@@ -679,8 +679,10 @@ int scatter_shape(int n_nodes, bool wide, size_t coef_bytes, int* chunk, int* TK
     };
     // GB300 sweeps (CO2 5M / 128 nodes, H2O 100M / 288 nodes): one line per
     // consumer thread per chunk (992 = 31 warps) in three stages while the tile
-    // keeps >= 256 columns; else two 1536-line stages (wider tiles than 2048)
-    if (tile_cols(3, 992) >= 256) return take(3, 992, tile_cols(3, 992));
+    // keeps >= 192 columns (CO2 5M: 256 columns, or 224 beside the skeleton
+    // coefficients, where three stages beat two 1536-line ones by 2%); else two
+    // 1536-line stages (wider tiles than 2048)
+    if (tile_cols(3, 992) >= 192) return take(3, 992, tile_cols(3, 992));
     if (tile_cols(2, 1536) >= 64) return take(2, 1536, tile_cols(2, 1536));
     for (int min_tk : {64, 32})
         for (int ch : {1024, 512, 256})
@@ -968,6 +970,12 @@ int NL_merged(const GaussArgs& ga) { return ga.NLv; }
 // every node's transform within tol; fills the row kernel's arguments (row r
 // = skeleton node sk[r], with its own transform) and the projection
 // coefficients [n_nodes][rows_pad] in W.proj_host.
+// Skeleton projection in the scatter's flush (no LDM round trip through HBM)
+// for grids of at most this many nodes; larger grids project in a separate
+// pass (the flush's FMAs would stall the scatter longer than the round trip
+// costs), with the decomposition computed on the host while the scatter runs.
+constexpr int kFuseMaxNodes = 160;
+
 constexpr int kSkelSamples = 32;
 constexpr double kSkelTol = 1e-8;
 
@@ -1053,7 +1061,10 @@ bool plan_skeleton(Work& W, const SpecHost& s, const VoigtArgs& va, int r_max, V
         const int rows = R + (R & 1);
         if (R < 1 || rows > r_max) return false;
         const int rp = proj_rows_pad(rows);
-        if ((size_t)n * rp * sizeof(float) > 96 * 1024) return false;   // coefficients in shared memory
+        // coefficients in shared memory: beside the scatter's tile (grids of up
+        // to kFuseMaxNodes nodes) or as the projection pass's fragments
+        if ((size_t)n * rp * sizeof(float) > 96 * 1024) return false;
+        if (n > kFuseMaxNodes && proj_tc_smem((rows + 7) / 8, 2 * ((n + 15) / 16)) > kProjTcSmemMax) return false;
         // [n][rp] coefficients (the FP32 forms), then the tensor-core pass's B
         // fragments: TF32 hi / lo parts, [nr][ks][part][lane][2] with
         // b0, b1 = C[8 nr + g][8 ks + t], C[8 nr + g][8 ks + t + 4], g = lane / 4,
@@ -1205,11 +1216,6 @@ int plan_layout(Work& W, const SpecHost& s, cudaStream_t st, LayoutPlan* lp) {
     return RG_OK;
 }
 
-// Skeleton projection in the scatter's flush (no LDM round trip through HBM)
-// for grids of at most this many nodes; larger grids project in a separate
-// pass (the flush's FMAs would stall the scatter longer than the round trip
-// costs), with the decomposition computed on the host while the scatter runs.
-constexpr int kFuseMaxNodes = 160;
 
 int enqueue_spectrum(const rg_lines* L, Work& W, const rg_conditions* c, const SpecHost& s, float* out,
                      cudaStream_t st, cudaEvent_t* ev, bool ldm_only) {

@@ -409,7 +409,11 @@ int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st);
 int launch_gather_grad(const GradArgs& a, int grid, cudaStream_t st);
 int launch_gauss_merge(const GaussArgs& a, int out_rows, cudaStream_t st);
 const char* last_launch_error();     // the CUDA error of this thread's last failed launch, or null
-int proj_rows_pad(int rows);         // coefficient pitch of launch_node_project for `rows` rows
+int proj_rows_pad(int rows);         // pitch of the [node][pitch] projection coefficients for `rows` rows
+// shared memory of the tensor-core projection pass (launch_node_project) for
+// `row_blocks` blocks of 8 rows and `ksteps` node steps of 8; at most kProjTcSmemMax
+size_t proj_tc_smem(int row_blocks, int ksteps);
+constexpr size_t kProjTcSmemMax = 200 * 1024;
 int launch_node_project(const ProjArgs& a, cudaStream_t st);
 // interpolative decomposition of the n columns of A (S samples each, column
 // major): skeleton columns sk[0, R) and coefficients C[r * n + j] with

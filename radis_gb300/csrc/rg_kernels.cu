@@ -1556,113 +1556,6 @@ __global__ void __launch_bounds__(256) k_gauss_merge(const GaussArgs a) {
     }
 }
 
-// Skeleton layout: rows [0, rows) of the LDM <- the projection of all node
-// rows onto the skeleton rows, in place.  Persistent CTAs walk column tiles
-// of TC = 256 CPT columns; the tile's node rows stream through a ring of
-// kProjStages shared-memory stages of NC = 16 / CPT rows (16 KB, cp.async,
-// zero-filled past n_v), kProjStages - 1 stages ahead, across tile
-// boundaries.  Thread t owns columns CPT t .. CPT t + CPT - 1 of the tile and
-// accumulates RB x CPT sums: per node one CPT-wide shared load and RB / 4
-// 16-byte broadcast loads of the coefficients for RB x CPT FMAs.  After a
-// tile's last node row it writes its columns of rows [0, rows): every node
-// row of those columns has landed in shared memory by then, and no other CTA
-// touches them.
-constexpr int kProjStages = 4;
-
-template <int CPT>
-__device__ __forceinline__ void load_cols_smem(float (&x)[CPT], const float* p) {
-    if constexpr (CPT == 2) {
-        const float2 v = *reinterpret_cast<const float2*>(p);
-        x[0] = v.x;
-        x[1] = v.y;
-    } else {
-        x[0] = *p;
-    }
-}
-
-template <int RB, int CPT>
-__global__ void __launch_bounds__(256) k_node_project(const ProjArgs a) {
-    constexpr int TC = 256 * CPT;   // columns per tile
-    constexpr int NC = 16 / CPT;    // node rows per stage (16 KB)
-    constexpr int S = kProjStages;
-    extern __shared__ __align__(16) float psm[];
-    const int n_chunks = (a.n_nodes + NC - 1) / NC;       // node chunks per tile
-    float* cs = psm;                                      // coefficients [n_chunks NC][RB], zero rows past n_nodes
-    float* xs = psm + n_chunks * NC * RB;                 // stages [S][NC][TC]
-    const int n_tiles = (int)((a.n_v + TC - 1) / TC);
-    const int my_tiles = (n_tiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x;
-    const int total = my_tiles * n_chunks;                // chunks this CTA consumes
-    auto tile_k0 = [&](int t) { return (int64_t)((int)blockIdx.x + t * (int)gridDim.x) * TC; };
-    // this thread's 16-byte pieces of a stage: row r_i, column 4 c4_i (the
-    // same in every chunk); only the chunk's origin changes
-    constexpr int PIECES = NC * TC / 4 / 256;
-    constexpr int ROW_STEP = 256 / (TC / 4);   // rows between a thread's pieces
-    const int r_0 = threadIdx.x / (TC / 4), c4_t = threadIdx.x % (TC / 4);
-    auto issue = [&](int g) {   // chunk g of this CTA into stage g % S
-        const int64_t k = tile_k0(g / n_chunks) + 4 * c4_t;
-        const int nd0 = (g % n_chunks) * NC + r_0;
-        float* dst = xs + (g % S) * NC * TC + r_0 * TC + 4 * c4_t;
-        const float* src = a.ldm + (int64_t)nd0 * a.row_stride + k;
-        const bool col_ok = k < a.n_v;   // a piece past n_v stays in the row's padding
-#pragma unroll
-        for (int i = 0; i < PIECES; ++i) {
-            const bool ok = col_ok && nd0 + i * ROW_STEP < a.n_nodes;
-            cp_async16(dst + i * ROW_STEP * TC, ok ? src + (int64_t)i * ROW_STEP * a.row_stride : a.ldm, ok ? 16 : 0);
-        }
-    };
-#pragma unroll
-    for (int g = 0; g < S - 1; ++g) {
-        if (g < total) issue(g);
-        cp_async_commit();
-    }
-    {
-        const float4* src = reinterpret_cast<const float4*>(a.coef);
-        float4* dst = reinterpret_cast<float4*>(cs);
-        const int nc4 = a.n_nodes * (RB / 4);
-        for (int i = threadIdx.x; i < n_chunks * NC * (RB / 4); i += blockDim.x)
-            dst[i] = i < nc4 ? __ldg(&src[i]) : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    for (int t = 0; t < my_tiles; ++t) {
-        float acc[RB][CPT];
-#pragma unroll
-        for (int r = 0; r < RB; ++r)
-#pragma unroll
-            for (int j = 0; j < CPT; ++j) acc[r][j] = 0.f;
-        for (int ch = 0; ch < n_chunks; ++ch) {
-            const int g = t * n_chunks + ch;
-            cp_async_wait<S - 2>();   // this thread's pieces of chunk g have landed
-            __syncthreads();          // everyone's have, and everyone is done with chunk g - 1
-            if (g + S - 1 < total) issue(g + S - 1);   // into chunk g - 1's stage
-            cp_async_commit();
-            const float* xb = xs + (g % S) * NC * TC + threadIdx.x * CPT;
-            const float4* c4 = reinterpret_cast<const float4*>(cs + ch * NC * RB);
-#pragma unroll
-            for (int r = 0; r < NC; ++r) {   // rows past n_nodes: zero data, zero coefficients
-                float x[CPT];
-                load_cols_smem<CPT>(x, xb + r * TC);
-#pragma unroll
-                for (int q = 0; q < RB / 4; ++q) {
-                    const float4 c = c4[r * (RB / 4) + q];
-#pragma unroll
-                    for (int j = 0; j < CPT; ++j) {
-                        acc[4 * q][j] = fmaf(c.x, x[j], acc[4 * q][j]);
-                        acc[4 * q + 1][j] = fmaf(c.y, x[j], acc[4 * q + 1][j]);
-                        acc[4 * q + 2][j] = fmaf(c.z, x[j], acc[4 * q + 2][j]);
-                        acc[4 * q + 3][j] = fmaf(c.w, x[j], acc[4 * q + 3][j]);
-                    }
-                }
-            }
-        }
-        // the tile is complete: its skeleton rows
-        const int64_t k = tile_k0(t) + threadIdx.x * CPT;
-#pragma unroll
-        for (int r = 0; r < RB; ++r)
-#pragma unroll
-            for (int j = 0; j < CPT; ++j)
-                if (r < a.rows && k + j < a.n_v) a.ldm[(int64_t)r * a.row_stride + k + j] = acc[r][j];
-    }
-}
-
 // Instrument slit (radis/tools/slit.py:737 and remove_boundary, :1063-1072):
 // out[i] = scale sum_j slit[j] in[i + (m-1)/2 - j], the 'same' part of the
 // full convolution, zero outside [0, n); written as a correlation with the
@@ -2135,7 +2028,7 @@ int launch_col_ifft_adj(const ColFftArgs& a, cudaStream_t st) {
     }
 }
 
-// Row block of the projection: the rows rounded up to a multiple of 4.
+// Row pitch of the projection coefficients: the rows rounded up to a multiple of 4.
 int proj_rows_pad(int rows) { return (rows + 3) & ~3; }
 
 // Tensor-core form of the projection pass: Y^T[columns x rows] = X^T[columns
@@ -2156,6 +2049,10 @@ constexpr int kTcTC = 256;                // columns per CTA tile (8 warps x 32)
 constexpr int kTcKC = 16;                 // node rows per stage (two k-steps)
 constexpr int kTcPitch = kTcTC + 8;       // staged row pitch (floats)
 constexpr int kTcStages = 3;
+
+size_t proj_tc_smem(int row_blocks, int ksteps) {
+    return sizeof(float) * ((size_t)row_blocks * ksteps * 128 + (size_t)kTcStages * kTcKC * kTcPitch);
+}
 
 __device__ __forceinline__ uint32_t tf32_rna(float x) {
     uint32_t r;
@@ -2279,7 +2176,7 @@ __global__ void __launch_bounds__(256, 2) k_node_project_tc(const ProjArgs a) {
 
 template <int NR>
 int launch_proj_tc(const ProjArgs& a, cudaStream_t st) {
-    const size_t smem = sizeof(float) * ((size_t)NR * a.ksteps * 128 + (size_t)kTcStages * kTcKC * kTcPitch);
+    const size_t smem = proj_tc_smem(NR, a.ksteps);
     ALLOW_SMEM((k_node_project_tc<NR>), smem);
     const int64_t tiles = (a.n_v + kTcTC - 1) / kTcTC;
     // two CTAs per SM where their shared memory fits (fragments of up to ~4 row
@@ -2290,60 +2187,23 @@ int launch_proj_tc(const ProjArgs& a, cudaStream_t st) {
     return check_launch();
 }
 
-// one launcher per instantiation: its shared-memory opt-in is its own
-template <int RB, int CPT>
-int launch_proj_kernel(const ProjArgs& a, int slots, cudaStream_t st) {
-    constexpr int NC = 16 / CPT;
-    const size_t smem = sizeof(float) * ((size_t)((a.n_nodes + NC - 1) / NC) * NC * RB + (size_t)kProjStages * 4096);
-    ALLOW_SMEM((k_node_project<RB, CPT>), smem);
-    const int64_t tiles = (a.n_v + 256 * CPT - 1) / (256 * CPT);
-    const int grid = (int)std::min<int64_t>(tiles, slots);
-    k_node_project<RB, CPT><<<grid, 256, smem, st>>>(a);
-    return check_launch();
-}
-
-template <int RB>
-int launch_proj_rb(const ProjArgs& a, cudaStream_t st) {
-    // two columns per thread where the FMAs dominate (up to 32 rows) and the
-    // grid still has >= 4 tiles per CTA slot; else one
-    const int slots = 2 * std::max(a.sms, 1);
-    if constexpr (RB <= 32) {
-        if ((a.n_v + 511) / 512 >= 4 * (int64_t)slots) return launch_proj_kernel<RB, 2>(a, slots, st);
-    }
-    return launch_proj_kernel<RB, 1>(a, slots, st);
-}
-
-template <int RB>
-int launch_proj_dispatch(const ProjArgs& a, cudaStream_t st) {
-    if constexpr (RB > kProjMaxRows) {
-        return RG_ERR_ARG;
-    } else {
-        if (a.rows_pad == RB) return launch_proj_rb<RB>(a, st);
-        return launch_proj_dispatch<RB + 4>(a, st);
-    }
-}
-
 int launch_node_project(const ProjArgs& a, cudaStream_t st) {
     if (a.rows <= 0 || a.rows > kProjMaxRows || a.rows_pad != proj_rows_pad(a.rows) || a.n_nodes <= 0 ||
-        a.n_v <= 0 || a.row_stride % 4 != 0)
+        a.n_v <= 0 || a.row_stride % 4 != 0 || !a.frag)
         return RG_ERR_ARG;
-    // the tensor-core pass while its fragments and stages fit 200 KB of shared memory
-    const size_t tc_smem = sizeof(float) * ((size_t)a.mtiles * a.ksteps * 128 + (size_t)kTcStages * kTcKC * kTcPitch);
-    if (a.frag && tc_smem <= 200 * 1024) {
-        if (a.mtiles != (a.rows + 7) / 8 || a.ksteps < (a.n_nodes + 7) / 8 || a.ksteps % 2) return RG_ERR_ARG;
-        switch (a.mtiles) {
-        case 1: return launch_proj_tc<1>(a, st);
-        case 2: return launch_proj_tc<2>(a, st);
-        case 3: return launch_proj_tc<3>(a, st);
-        case 4: return launch_proj_tc<4>(a, st);
-        case 5: return launch_proj_tc<5>(a, st);
-        case 6: return launch_proj_tc<6>(a, st);
-        case 7: return launch_proj_tc<7>(a, st);
-        case 8: return launch_proj_tc<8>(a, st);
-        default: return RG_ERR_ARG;
-        }
+    if (a.mtiles != (a.rows + 7) / 8 || a.ksteps < (a.n_nodes + 7) / 8 || a.ksteps % 2) return RG_ERR_ARG;
+    if (proj_tc_smem(a.mtiles, a.ksteps) > kProjTcSmemMax) return RG_ERR_RANGE;
+    switch (a.mtiles) {
+    case 1: return launch_proj_tc<1>(a, st);
+    case 2: return launch_proj_tc<2>(a, st);
+    case 3: return launch_proj_tc<3>(a, st);
+    case 4: return launch_proj_tc<4>(a, st);
+    case 5: return launch_proj_tc<5>(a, st);
+    case 6: return launch_proj_tc<6>(a, st);
+    case 7: return launch_proj_tc<7>(a, st);
+    case 8: return launch_proj_tc<8>(a, st);
+    default: return RG_ERR_ARG;
     }
-    return launch_proj_dispatch<4>(a, st);
 }
 
 int launch_gauss_merge(const GaussArgs& a0, int out_rows, cudaStream_t st) {
