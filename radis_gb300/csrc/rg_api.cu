@@ -1438,15 +1438,32 @@ int enqueue_backward(const rg_lines* L, Work& W, const rg_conditions* c, const S
     unit->any_fold = 0;
     CU(cudaMemsetAsync(W.g, 0, sizeof(float2) * (size_t)W.n, st));
     RG(launch_row_fft_voigt(*unit, st));
-    // adjoint LDM rows: Re / Im of IFFT(Ghat (V_a + i V_b)) / (N dv), per pair
+    // adjoint LDM rows: Re / Im of IFFT(Ghat (V_a + i V_b)) / (N dv), per pair;
+    // with the skeleton layout only the skeleton rows (the gather expands them
+    // into node rows with the projection coefficients: C restricted to node n
+    // is sum_r C[r][n] times skeleton node s_r's convolution)
+    LayoutPlan lp;
+    const bool skel = W.desc.layout != 1 && W.desc.layout != 2 && plan_layout(W, s, st, &lp) == RG_OK && lp.skel;
+    if (skel) {
+        const VoigtArgs ghat = ar->v;   // keeps g = Ghat
+        ar->v = *lp.vk;
+        ar->v.g = ghat.g;
+    }
     ar->y = W.y;
     RG(launch_row_ifft_adj(*ar, st));
     ColFftArgs cb = col_args(W, s);
+    if (skel) cb.n_pairs = lp.pa.rows / 2;
     cb.h = W.y;
     cb.out = W.ldm;
     cb.out_scale = (float)(1.0 / ((double)W.n * W.desc.dv));
     RG(launch_col_ifft_adj(cb, st));
     // per-line chain rule gathered at the lines' cells
+    if (skel) {
+        ga->proj_coef = lp.pa.coef;
+        ga->proj_rows = lp.pa.rows;
+        ga->proj_rp = lp.pa.rows_pad;
+        ga->proj_n = lp.pa.n_nodes;
+    }
     ga->adj = W.ldm;
     ga->out = grad_d;
     CU(cudaMemsetAsync(grad_d, 0, 3 * sizeof(double), st));
@@ -1464,6 +1481,13 @@ int enqueue_tangent(const rg_lines* L, Work& W, const rg_conditions* c, const Sp
     RG(fill_grad_args(L, W, c, s, dlnq_dT, ga.get()));
     auto va = std::make_unique<VoigtArgs>();
     fill_voigt_args(W, s, va.get());
+    // skeleton layout: each tangent LDM is projected onto the skeleton rows
+    // (in place, tensor cores) before its FFT, as the spectrum's LDM is
+    LayoutPlan lp;
+    const bool skel = W.desc.layout != 1 && W.desc.layout != 2 && plan_layout(W, s, st, &lp) == RG_OK && lp.skel;
+    VoigtArgs& vr = skel ? *lp.vk : *va;
+    vr.store_g = vr.n_pairs <= kPairGroup;
+    vr.inv_fused = vr.store_g;
     float* tan = W.ldm;
     ga->tan = tan;
     const int n_v = (int)W.desc.n_v;
@@ -1472,11 +1496,18 @@ int enqueue_tangent(const rg_lines* L, Work& W, const rg_conditions* c, const Sp
         CU(cudaMemsetAsync(tan, 0, sizeof(float) * (size_t)s.n_nodes * W.row_stride, st));
         RG(launch_scatter_tangent(*ga, L->ctx->sms * 8, st));
         ColFftArgs ca = col_args(W, s);
+        if (skel) {
+            ProjArgs pa = lp.pa;
+            pa.ldm = tan;
+            pa.sms = L->ctx->sms;
+            RG(launch_node_project(pa, st));
+            ca.n_pairs = pa.rows / 2;
+        }
         ca.src = tan;
         ca.y = W.y;
         RG(launch_col_fft_fwd_f(ca, st));
-        CU(cudaMemsetAsync(W.g, 0, sizeof(float2) * (size_t)W.n, st));
-        RG(launch_row_fft_voigt(*va, st));
+        if (!vr.store_g) CU(cudaMemsetAsync(W.g, 0, sizeof(float2) * (size_t)W.n, st));
+        RG(launch_row_fft_voigt(vr, st));
         RowIfftArgs ra;
         ra.f2 = W.f2;
         ra.n1 = W.n1;
@@ -1485,7 +1516,7 @@ int enqueue_tangent(const rg_lines* L, Work& W, const rg_conditions* c, const Sp
         ra.g = W.g;
         ra.tw_hi = W.tw_hi;
         ra.tw_lo = W.tw_lo;
-        RG(launch_row_ifft(ra, st));
+        if (!vr.inv_fused) RG(launch_row_ifft(ra, st));
         ca.h = W.g;
         ca.out = out + (size_t)q * n_v;
         ca.out_scale = (float)(std::exp(s.log_scale_int - s.log_scale_out) / ((double)W.n * W.desc.dv));

@@ -360,6 +360,11 @@ struct GradArgs {         // adjoint gather (reverse mode) and tangent scatter (
     float kP;             // d(grid position)/d(p_bar) per unit shift = 1 / (1.01325 dv)
     float iP, iX;         // 1/p_bar, 1/x
     double* out;          // gather output: d/dT, d/dp_bar, d/dx sums, zeroed
+    // skeleton layout: adj holds the skeleton rows Z_r (r < proj_rows) and a
+    // node's adjoint row is sum_r proj_coef[node * proj_rp + r] Z_r (gather);
+    // null: adj holds every node row
+    const float* proj_coef;
+    int proj_rows, proj_rp, proj_n;
 };
 
 // Fixed-point scale of the scatter accumulator: 2^e with (cmax + 1) 2^e <= 2^31

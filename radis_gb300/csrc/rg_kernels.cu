@@ -1694,7 +1694,12 @@ __device__ __forceinline__ LineRates line_rates(const GradArgs& g, float v0, flo
 // dtL SL), with S0 the adjoint LDM interpolated at the line and Sk, SG, SL its
 // differences along the three cell axes.  One FP64 atomic per block and theta.
 __global__ void __launch_bounds__(256) k_gather_grad(const GradArgs g) {
+    extern __shared__ float gcs[];   // skeleton layout: the coefficients [proj_n][proj_rp]
     const ScatterArgs& a = g.s;
+    if (g.proj_coef) {
+        for (int i = threadIdx.x; i < g.proj_n * g.proj_rp; i += blockDim.x) gcs[i] = __ldg(&g.proj_coef[i]);
+        __syncthreads();
+    }
     float acc[3] = {0.f, 0.f, 0.f};
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < g.n_lines; i += stride) {
@@ -1711,14 +1716,37 @@ __global__ void __launch_bounds__(256) k_gather_grad(const GradArgs g) {
         line_nodes(a, v.x, ga, gs, na, is, l0, m0, tG, tL);
         const float I = line_intensity(a, v.x, el, a.ls2[i], is);
         if (!(I > 0.f)) continue;
-        const float* r00 = g.adj + (int64_t)(l0 * a.NL + m0) * g.row_stride + k0;
-        const float* r01 = r00 + g.row_stride;
-        const float* r10 = r00 + (int64_t)a.NL * g.row_stride;
-        const float* r11 = r10 + g.row_stride;
-        const float d00 = r00[1] - r00[0], d01 = r01[1] - r01[0];
-        const float d10 = r10[1] - r10[0], d11 = r11[1] - r11[0];
-        const float e00 = fmaf(tv, d00, r00[0]), e01 = fmaf(tv, d01, r01[0]);
-        const float e10 = fmaf(tv, d10, r10[0]), e11 = fmaf(tv, d11, r11[0]);
+        // the adjoint at the line's 4 nodes, columns k0 and k0 + 1
+        float u0[4], u1[4];   // node order (l0, m0), (l0, m0 + 1), (l0 + 1, m0), (l0 + 1, m0 + 1)
+        const int n00 = l0 * a.NL + m0;
+        if (g.proj_coef) {   // from the skeleton rows
+            const int nd[4] = {n00, n00 + 1, n00 + a.NL, n00 + a.NL + 1};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) u0[j] = u1[j] = 0.f;
+            const float* z = g.adj + k0;
+            for (int r = 0; r < g.proj_rows; ++r, z += g.row_stride) {
+                const float z0 = z[0], z1 = z[1];
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    const float c = gcs[nd[j] * g.proj_rp + r];
+                    u0[j] = fmaf(c, z0, u0[j]);
+                    u1[j] = fmaf(c, z1, u1[j]);
+                }
+            }
+        } else {
+            const float* r00 = g.adj + (int64_t)n00 * g.row_stride + k0;
+            const float* rr[4] = {r00, r00 + g.row_stride, r00 + (int64_t)a.NL * g.row_stride,
+                                  r00 + (int64_t)(a.NL + 1) * g.row_stride};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                u0[j] = rr[j][0];
+                u1[j] = rr[j][1];
+            }
+        }
+        const float d00 = u1[0] - u0[0], d01 = u1[1] - u0[1];
+        const float d10 = u1[2] - u0[2], d11 = u1[3] - u0[3];
+        const float e00 = fmaf(tv, d00, u0[0]), e01 = fmaf(tv, d01, u0[1]);
+        const float e10 = fmaf(tv, d10, u0[2]), e11 = fmaf(tv, d11, u0[3]);
         const float uG = 1.f - tG, uL = 1.f - tL;
         const float S0 = uG * (uL * e00 + tL * e01) + tG * (uL * e10 + tL * e11);
         const float Sk = uG * (uL * d00 + tL * d01) + tG * (uL * d10 + tL * d11);
@@ -2236,7 +2264,9 @@ int launch_slit_conv(const SlitArgs& a, cudaStream_t st) {
 
 int launch_gather_grad(const GradArgs& a, int grid, cudaStream_t st) {
     if (a.n_lines <= 0) return RG_OK;
-    k_gather_grad<<<grid, 256, 0, st>>>(a);
+    const size_t smem = a.proj_coef ? sizeof(float) * (size_t)a.proj_n * a.proj_rp : 0;
+    ALLOW_SMEM(k_gather_grad, smem);
+    k_gather_grad<<<grid, 256, smem, st>>>(a);
     return check_launch();
 }
 

@@ -80,20 +80,45 @@ def fd_columns(case, lines, axes, n_ft):
     return cols
 
 
-@pytest.fixture(scope="module", params=sorted(CASES))
+_FD = {}
+
+
+# every case with the FFT-stage layout the planner picks (skeleton rows where
+# the grid allows: the adjoint then expands skeleton rows in the gather, the
+# tangent projects its LDM) and with node rows (layout 1)
+@pytest.fixture(scope="module", params=[(name, lay) for name in sorted(CASES) for lay in (0, 1)],
+                ids=lambda p: f"{p[0]}-layout{p[1]}")
 def setup(request, ctx):
-    case = CASES[request.param]
+    name, layout = request.param
+    case = CASES[name]
     lines = case["lines"]()
     vmin, dv, n_v = case["grid"]
     ln = L.Lines(ctx, lines, case["M"])
-    plan = L.Plan(ln, vmin, dv, n_v, dxG=S.DXG_DEFAULT, dxL=S.DXL_DEFAULT)
+    plan = L.Plan(ln, vmin, dv, n_v, dxG=S.DXG_DEFAULT, dxL=S.DXL_DEFAULT, layout=layout)
     T, p, x = case["cond"]
     g = plan.grid(T, p, x)
-    fd = fd_columns(case, lines, g.axes(), g.n_ft)
-    ref = oracle_A(case, lines, T, p, x, g.axes(), g.n_ft)
-    yield request.param, case, plan, fd, ref
+    if name not in _FD:   # the oracle's columns do not depend on the layout
+        _FD[name] = (fd_columns(case, lines, g.axes(), g.n_ft), oracle_A(case, lines, T, p, x, g.axes(), g.n_ft))
+    fd, ref = _FD[name]
+    yield name, case, plan, fd, ref
     plan.close()
     ln.close()
+
+
+def test_skeleton_rows_in_some_case(ctx):
+    """At least one case's grid takes the skeleton layout under the planner's
+    choice, so the skeleton adjoint and tangent paths run in the tests above."""
+    used = []
+    for name, case in CASES.items():
+        lines = case["lines"]()
+        vmin, dv, n_v = case["grid"]
+        ln = L.Lines(ctx, lines, case["M"])
+        plan = L.Plan(ln, vmin, dv, n_v, dxG=S.DXG_DEFAULT, dxL=S.DXL_DEFAULT)
+        _, info = plan.synthesize_host(*case["cond"], q_ratio=q_of(case["Q"], case["cond"][0], 0))
+        used.append(int(info.layout))
+        plan.close()
+        ln.close()
+    assert any(u in (3, 4) for u in used), used
 
 
 def test_jvp_matches_fd(setup):
