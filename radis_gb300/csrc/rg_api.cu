@@ -173,6 +173,7 @@ struct Work {
     // grow-only) and their host staging (copied from pageable memory: the
     // copy has left this buffer when cudaMemcpyAsync returns)
     bool allow_skeleton = true;
+    bool proj_fixed = false;          // proj_coef is a fixed piece of scratch (never reallocated)
     float* proj_coef = nullptr;
     size_t proj_bytes = 0;
     std::vector<float> proj_host;
@@ -1091,6 +1092,7 @@ bool plan_skeleton(Work& W, const SpecHost& s, const VoigtArgs& va, int r_max, V
         W.skel_err = err;
     }
     if (W.skel_R == 0) return false;
+    if (W.proj_fixed && sizeof(float) * W.proj_host.size() > W.proj_bytes) return false;
     const int R = W.skel_R;
     const int rows = R + (R & 1);
     const int rp = proj_rows_pad(rows);
@@ -2759,6 +2761,7 @@ int rg_server_destroy(rg_server* S) {
 // every GPU that loads this library holds it until the process exits.
 constexpr size_t kStaticScratchBytes = (size_t)64 << 20;   // 64 MiB
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+constexpr size_t kStaticProjBytes = 256 * 1024;
 
 namespace {
 
@@ -2858,10 +2861,14 @@ extern "C" int rg_synthesize_static(rg_lines* L, const rg_plan_desc* d, const rg
     W.tw_hi = twh;
     W.tw_lo = twl;
     // sized here: the workspace step finds them large enough and allocates nothing;
-    // the merged and skeleton layouts (their own device buffers) are not used
-    // on this path
+    // the merged layout (its own row buffer) is not used on this path; the
+    // skeleton layout's coefficients get a fixed piece (the largest a grid can
+    // need: [n][rp] <= 96 KB plus tensor-core fragments < 150 KB)
     W.allow_merge = false;
-    W.allow_skeleton = false;
+    W.allow_skeleton = true;
+    W.proj_fixed = true;
+    W.proj_bytes = kStaticProjBytes;
+    W.proj_coef = static_cast<float*>(take(kStaticProjBytes));
     W.ldm_bytes = sizeof(float) * (size_t)s.n_nodes * (size_t)W.row_stride;
     W.y_bytes = sizeof(float2) * (size_t)(s.n_nodes / 2) * (size_t)W.n;
     W.ldm = static_cast<float*>(take(W.ldm_bytes));

@@ -61,3 +61,33 @@ def test_static_scratch_matches_plan(native_lib):
     plan.close()
     lines.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("nodes,layout", [((8, 16), 4), ((12, 16), 3)])
+def test_static_skeleton_layouts(native_lib, nodes, layout):
+    """The allocation-free path on grids that take the skeleton layout: 8 x 16
+    nodes (projection in the scatter's flush) and 12 x 16 (the tensor-core
+    projection pass), both from the static array's coefficient piece; same
+    spectrum as a plan, no device allocation."""
+    torch = pytest.importorskip("torch")
+    ctx = L.Context(0)
+    lines = L.Lines(ctx, S.uniform_lines(100_000, 1000.0, 1100.0, seed=62), 18.0)
+    vmin, dv, n_v = 1000.0, 0.005, 20001
+    grid = dict(n_G=nodes[0], n_L=nodes[1])
+    plan = L.Plan(lines, vmin, dv, n_v, **grid)
+    T, p, x = 2000.0, 1.0, 0.2
+    ref, ref_info = plan.synthesize_host(T, p, x)
+    out = torch.empty(n_v, dtype=torch.float32, device="cuda")
+    L.synthesize_static(lines, vmin, dv, n_v, T, p, x, out.data_ptr(), **grid)   # warm-up
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    out.fill_(-1.0)
+    info = L.synthesize_static(lines, vmin, dv, n_v, T, p, x, out.data_ptr(), **grid)
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
+    assert info.layout == layout and ref_info.layout == layout
+    g = out.cpu().numpy()
+    assert np.max(np.abs(g - ref)) <= TOL * np.max(np.abs(ref))
+    plan.close()
+    lines.close()
+    ctx.close()
