@@ -607,7 +607,7 @@ def quantity_errors(plan, T, p, x, vmin, dv, n_v, ref_abscoeff, path_length=1.0)
     return {k: rel_err(got[k], ref[k]) for k in got}
 
 
-def run_fft_compare(n_ft, rows, our_fwd_ms, our_inv_ms, reps=10):
+def run_fft_compare(n_ft, rows, our_fwd_ms, our_inv_ms, reps=10, inverse_row_in_forward=False):
     """cuFFT, through torch.fft, on the batched rows this library's FFT stages
     transform: R2C of ``rows`` real rows of length n_ft (the reference's
     per-node rfft, radis/lbl/broadening.py:2521-2530), C2C of the rows packed
@@ -644,7 +644,9 @@ def run_fft_compare(n_ft, rows, our_fwd_ms, our_inv_ms, reps=10):
         "ours_forward_fft_voigt_ms": our_fwd_ms,
         "ours_inverse_ms": our_inv_ms,
         "note": ("ours = column FFT (+ twiddle) + row FFT fused with the Voigt multiply and the sum over "
-                 "nodes, on the same packed rows; cuFFT's figures exclude the Voigt multiply and node sum"),
+                 "nodes, on the same packed rows; cuFFT's figures exclude the Voigt multiply and node sum"
+                 + ("; the inverse row DFT runs inside our row kernel, so ours_forward includes it and "
+                    "ours_inverse is the inverse column DFT alone" if inverse_row_in_forward else "")),
     }
     del x, z, h
     torch.cuda.empty_cache()
@@ -921,7 +923,8 @@ def run_ours(args):
         if ws == 1 and not args.no_fft_compare:
             fwd = kt["k_col_fft_fwd"] + kt["k_row_fft_voigt"]
             res["fft_vs_cufft"] = {wl: run_fft_compare(int(g.n_ft), int(info.fft_rows or n_nodes), fwd,
-                                                       kt["k_row_ifft"] + kt["k_col_ifft"])}
+                                                       kt.get("k_row_ifft", 0.0) + kt["k_col_ifft"],
+                                                       inverse_row_in_forward="k_row_ifft" not in kt)}
         if ws == 1 and not args.no_slit:
             plan.synthesize_device(T, p, x, out.data_ptr(), torch.cuda.current_stream().cuda_stream or 1)
             res["slit"] = run_slit(ctx, out, vmin, dv)
@@ -938,7 +941,8 @@ def run_ours(args):
                 c3_rows = c3["fft_layout"]["fft_rows"]
                 res.setdefault("fft_vs_cufft", {})["h2o_100M"] = run_fft_compare(
                     c3["fft_layout"]["n_ft"], c3_rows, kt3["k_col_fft_fwd"] + kt3["k_row_fft_voigt"],
-                    kt3["k_row_ifft"] + kt3["k_col_ifft"], reps=5)
+                    kt3.get("k_row_ifft", 0.0) + kt3["k_col_ifft"], reps=5,
+                    inverse_row_in_forward="k_row_ifft" not in kt3)
             res["c3"] = c3
         if h2o_host is not None:
             h2o_host = None
