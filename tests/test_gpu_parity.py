@@ -173,6 +173,23 @@ def test_skeleton_projection_paths(ctx, case, accumulator, fused):
     assert rel_err(gpu, oracle(lines, *args, info)) <= TOL
 
 
+def test_skeleton_tolerance_trades_rows_for_error(ctx):
+    """A looser decomposition bound (layout_tol) transforms fewer skeleton
+    rows; the spectrum moves by about the bound and stays within the parity
+    bar of the reference."""
+    make, args, grid = LAYOUT_CASES["long_12x16"]
+    lines = make()
+    exact, ie = run_gpu(ctx, lines, *args, layout=1, **grid)
+    tight, it = run_gpu(ctx, lines, *args, layout=3, **grid)
+    loose, il = run_gpu(ctx, lines, *args, layout=3, layout_tol=1e-5, **grid)
+    assert it.layout in (3, 4) and il.layout in (3, 4)
+    assert il.fft_rows < it.fft_rows < ie.fft_rows
+    assert il.layout_err <= 1e-5 and it.layout_err <= 1e-8
+    assert rel_err(tight, exact) <= 2e-5
+    assert rel_err(loose, exact) <= 1e-4
+    assert rel_err(loose, oracle(lines, *args, il)) <= TOL
+
+
 def test_host_output_page_locked_and_pageable(ctx):
     """The host entry points into page-locked memory (written by the last
     kernel itself) and into pageable memory (copied after it) give the same
