@@ -517,7 +517,8 @@ def run_autodiff(ctx, L, n_cond=64, seed=12):
     """Derivative configuration: 64 seeded conditions on the CO-like 10k list
     at 0.001 cm-1 (1900-2300, 400 001 points), T log-U[300, 3000] K, p
     log-U[0.1, 10] bar, x log-U[0.01, 1].  Times, per condition, the FP32
-    forward, forward + adjoint (gradient of a scalar loss), forward + the
+    forward, forward + adjoint (gradient of a scalar loss, through the
+    library's API and through the torch.autograd wrapper), forward + the
     three tangent spectra, and finite differences by forward runs (a central
     difference per parameter: 6 extra spectra)."""
     import numpy as np
@@ -538,7 +539,13 @@ def run_autodiff(ctx, L, n_cond=64, seed=12):
     def fwd(c):
         plan.synthesize_device(*c, out.data_ptr(), torch.cuda.current_stream().cuda_stream or 1)
 
-    def fwd_bwd(c):
+    st = torch.cuda.current_stream().cuda_stream or 1
+
+    def fwd_bwd(c):   # the library's adjoint: spectrum, then the gradient of sum(w A) by rg_backward
+        plan.synthesize_device(*c, out.data_ptr(), st)
+        plan.backward(*c, w.data_ptr(), stream_ptr=st)
+
+    def fwd_bwd_autograd(c):   # the same through the torch.autograd.Function wrapper
         T, p, x = (torch.tensor(v, dtype=torch.float64, requires_grad=True) for v in c)
         (absorbance(plan, T, p, x) * w).sum().backward()
 
@@ -556,8 +563,8 @@ def run_autodiff(ctx, L, n_cond=64, seed=12):
     res = {"workload": ("CO-like synthetic list, 10000 lines, 1900-2300 cm-1 at 0.001 cm-1 (400001 points), "
                         f"{n_cond} conditions T log-U[300,3000] K, p log-U[0.1,10] bar, x log-U[0.01,1]"),
            "conditions": n_cond}
-    for name, f in (("forward", fwd), ("forward_adjoint", fwd_bwd), ("forward_tangent3", fwd_jvp),
-                    ("fd_by_forward", fd)):
+    for name, f in (("forward", fwd), ("forward_adjoint", fwd_bwd), ("forward_adjoint_autograd", fwd_bwd_autograd),
+                    ("forward_tangent3", fwd_jvp), ("fd_by_forward", fd)):
         for c in conds[:3]:
             f(c)
         torch.cuda.synchronize()
@@ -568,9 +575,12 @@ def run_autodiff(ctx, L, n_cond=64, seed=12):
         res[name + "_ms"] = (time.perf_counter() - t0) * 1e3 / n_cond
     res["adjoint_speedup_vs_fd"] = res["fd_by_forward_ms"] / res["forward_adjoint_ms"]
     res["tangent_speedup_vs_fd"] = res["fd_by_forward_ms"] / res["forward_tangent3_ms"]
-    res["note"] = ("per-condition wall time (host API calls, device work synchronised per batch); node axes "
-                   "follow each condition; accuracy vs central FD of the FP64 oracle is checked in "
-                   "tests/test_gpu_autodiff.py")
+    res["note"] = ("per-condition wall time through the library's API (forward: rg_synthesize; adjoint: "
+                   "rg_synthesize + rg_backward of sum(w A), which returns the three sums to the host; tangents: "
+                   "rg_synthesize + rg_jvp; FD: 7 forwards), device work synchronised per batch; "
+                   "forward_adjoint_autograd is the same gradient through the torch.autograd.Function wrapper "
+                   "(its graph, small torch kernels and engine hand-off included); node axes follow each "
+                   "condition; accuracy vs central FD of the FP64 oracle is checked in tests/test_gpu_autodiff.py")
     plan.close()
     ln.close()
     return res
