@@ -366,8 +366,12 @@ def run_serving(ctx, L, lists, n_req, slots, seed=11):
     import threading
 
     import numpy as np
+    import torch
     from radis_gb300 import synthetic as S
     reqs = serving_requests(lists, n_req, seed)
+    # one page-locked output buffer per request, the same in both forms: the
+    # spectrum's last kernel writes it directly (no staging copy)
+    bufs = [torch.empty(r[4], dtype=torch.float32, pin_memory=True).numpy() for r in reqs]
     # node spacing of the reference's defaults; the Gaussian axis spans the
     # lines that can reach each request's window (as the reference's factory
     # loads only those), in both forms
@@ -376,12 +380,12 @@ def run_serving(ctx, L, lists, n_req, slots, seed=11):
     def plain(arrivals):
         outs, lat = [], []
         t0 = time.perf_counter()
-        for (name, lines, vmin, dv, n_v, T, p, x), ta in zip(reqs, arrivals):
+        for i, ((name, lines, vmin, dv, n_v, T, p, x), ta) in enumerate(zip(reqs, arrivals)):
             now = time.perf_counter() - t0
             if ta > now:
                 time.sleep(ta - now)
             plan = L.Plan(lines, vmin, dv, n_v, **dx)
-            o, info = plan.synthesize_host(T, p, x)
+            o, info = plan.synthesize_host(T, p, x, out=bufs[i])
             plan.close()
             outs.append((o, info.log_scale))
             lat.append(time.perf_counter() - t0 - ta)
@@ -401,7 +405,7 @@ def run_serving(ctx, L, lists, n_req, slots, seed=11):
                 now = time.perf_counter() - t0
                 if ta > now:
                     time.sleep(ta - now)
-                tickets[i] = srv.submit(lines, vmin, dv, n_v, T, p, x, **dx)
+                tickets[i] = srv.submit(lines, vmin, dv, n_v, T, p, x, out=bufs[i], **dx)
         th = threading.Thread(target=submitter)
         th.start()
         outs, lat = [], []

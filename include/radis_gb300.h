@@ -377,9 +377,12 @@ int rg_synthesize_static(rg_lines* lines, const rg_plan_desc* grid, const rg_con
  * SpectrumFactory.eq_spectrum_gpu + Spectrum.recalc_gpu for many clients.
  * A worker thread admits queued requests (FIFO) into `slots` CUDA streams as
  * slots and device memory (LDM + FFT workspace, within `mem_budget` bytes)
- * free up; admitted requests run concurrently on the device.  Each result is
- * copied device -> pinned staging buffer of its slot (asynchronous) and, once
- * the request is complete, to the request's host buffer (any host memory).
+ * free up; admitted requests run concurrently on the device.  A request
+ * buffer that is page-locked (cudaHostAlloc / cudaHostRegister, or a pinned
+ * torch tensor) is written by the spectrum's last kernel directly; any other
+ * host buffer gets the result through its slot's pinned staging buffer (an
+ * asynchronous device -> staging copy, then a host copy once the request is
+ * complete).
  * ------------------------------------------------------------------------- */
 typedef struct rg_server rg_server;
 
@@ -387,7 +390,8 @@ typedef struct {
     rg_lines* lines;           /* resident line list                            */
     rg_plan_desc grid;         /* spectral grid + LDM node policy               */
     rg_conditions cond;        /* q_ratio is copied at submission               */
-    float* out_host;           /* n_v floats: abscoeff x exp(-info.log_scale)    */
+    float* out_host;           /* n_v floats: abscoeff x exp(-info.log_scale);
+                                * page-locked memory is written directly       */
 } rg_request;
 
 typedef struct {

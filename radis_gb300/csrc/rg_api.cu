@@ -2279,6 +2279,7 @@ struct Slot {
     // worker until the request finished); copied to the caller at harvest
     float* pin = nullptr;
     int64_t pin_cap = 0;
+    bool direct = false;                  // the request's page-locked buffer is written by the last kernel
     std::shared_ptr<ServerReq> req;       // owned by the worker thread
     std::atomic<bool> notified{false};    // set by the stream's host callback
     size_t bytes() const {
@@ -2440,8 +2441,12 @@ int start_on_slot(rg_server* S, int si, const std::shared_ptr<ServerReq>& r, con
     W.row_stride = (d.n_v + 31) / 32 * 32;
     RG(grow(&W.col_start, &sl.col_cap, W.col_count, sl.st));
     RG(grow(&W.g, &sl.g_cap, W.n, sl.st));
-    RG(grow(&sl.out_d, &sl.out_cap, d.n_v, sl.st));
-    if (d.n_v > sl.pin_cap) {   // grow-only, at least 2M points (8 MB)
+    // a page-locked output buffer is written by the spectrum's last kernel
+    // itself: no staging copy, nothing for the worker to copy at harvest
+    float* direct = mapped_host(r->out_host);
+    sl.direct = direct != nullptr;
+    if (!direct) RG(grow(&sl.out_d, &sl.out_cap, d.n_v, sl.st));
+    if (!direct && d.n_v > sl.pin_cap) {   // grow-only, at least 2M points (8 MB)
         const int64_t cap = std::max<int64_t>({d.n_v, sl.pin_cap * 3 / 2, (int64_t)1 << 21});
         if (sl.pin) CU(cudaFreeHost(sl.pin));
         sl.pin = nullptr;
@@ -2452,8 +2457,9 @@ int start_on_slot(rg_server* S, int si, const std::shared_ptr<ServerReq>& r, con
     const rg_lines* L = r->lines;
     RG(launch_col_index(L->v0, L->n, d.vmin, d.dv, -W.E, W.col_count, W.col_start, sl.st));
     RG(launch_col_cmax(W.col_start, W.col_off, W.col_count, (int)d.n_v, W.E - 1, W.cmax_dev, sl.st));
-    RG(enqueue_spectrum(L, W, &r->cond, sh, sl.out_d, sl.st, nullptr, false));
-    CU(cudaMemcpyAsync(sl.pin, sl.out_d, sizeof(float) * (size_t)d.n_v, cudaMemcpyDeviceToHost, sl.st));
+    RG(enqueue_spectrum(L, W, &r->cond, sh, direct ? direct : sl.out_d, sl.st, nullptr, false));
+    if (!direct)
+        CU(cudaMemcpyAsync(sl.pin, sl.out_d, sizeof(float) * (size_t)d.n_v, cudaMemcpyDeviceToHost, sl.st));
     r->info.grid = sh.grid;
     r->info.log_scale = sh.log_scale_out;
     r->info.lines_in_window = -1;
@@ -2494,7 +2500,7 @@ void worker_loop(rg_server* S) {
             if (sl.notified.load()) {
                 const bool bad = *sl.w.err_host != 0;
                 *sl.w.err_host = 0;
-                if (!bad) {
+                if (!bad && !sl.direct) {
                     const double tc = S->now();
                     std::memcpy(sl.req->out_host, sl.pin, sizeof(float) * (size_t)sl.req->desc.n_v);
                     S->t_copy.store(S->t_copy.load() + (S->now() - tc));

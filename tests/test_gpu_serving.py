@@ -60,6 +60,37 @@ def test_same_alone_and_in_the_mix(env):
     srv.close()
 
 
+def test_page_locked_request_buffers(env):
+    """Page-locked request buffers are written by the last kernel directly;
+    pageable ones through the slot's staging buffer: the same spectra, and the
+    worker copies only the pageable ones."""
+    import torch
+    ctx, co, co2 = env
+    reqs = mix(co, co2, n=12, seed=11)
+    srv = L.Server(ctx, slots=4, mem_budget=8 << 30)
+    pinned = [torch.full((r[3],), np.nan, dtype=torch.float32, pin_memory=True).numpy() for r in reqs]
+    tickets = [srv.submit(*r, out=(pinned[i] if i % 2 else None), dxG=S.DXG_DEFAULT, dxL=S.DXL_DEFAULT)
+               for i, r in enumerate(reqs)]
+    for i, (r, t) in enumerate(zip(reqs, tickets)):
+        out, info, _ = srv.wait(t, timeout_ms=60000)
+        if i % 2:
+            assert out is pinned[i]
+        got = out.astype(np.float64) * np.exp(info.log_scale)
+        ref = alone(r)
+        assert np.all(np.isfinite(got))
+        assert np.max(np.abs(got - ref)) <= TOL * max(np.max(np.abs(ref)), 1e-300)
+    st = srv.stats()
+    assert st.completed == len(reqs) and st.failed == 0
+    srv.close()
+    # all page-locked: the worker copies nothing
+    srv = L.Server(ctx, slots=4, mem_budget=8 << 30)
+    tickets = [srv.submit(*r, out=pinned[i], dxG=S.DXG_DEFAULT, dxL=S.DXL_DEFAULT) for i, r in enumerate(reqs)]
+    for t in tickets:
+        srv.wait(t, timeout_ms=60000)
+    assert srv.stats().host_copy_ms == 0.0
+    srv.close()
+
+
 def test_budget_admission_and_errors(env):
     ctx, co, co2 = env
     # a budget that fits one mid-size request at a time: the queue drains in order
