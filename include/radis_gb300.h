@@ -359,7 +359,11 @@ int rg_jvp(rg_plan* plan, const rg_conditions* cond, const double* dlnq_dT, floa
  * static device array of 64 MiB that every GPU loading this library keeps
  * until the process exits; a spectrum that needs more returns RG_ERR_RANGE.
  * Calls no cudaMalloc or cudaFree.  The first call on a device resolves the
- * array's device address, so make it before any stream capture.  The array
+ * array's device address, so make it before any stream capture.  The first
+ * launch of a kernel variant in a process can make the CUDA driver reserve
+ * device memory of its own (lazy module loading; local memory of a kernel
+ * that spills): to keep that off a request path too, make one call per
+ * spectrum shape at setup.  The array
  * belongs to this process and device (each process that loads the library
  * has its own); all calls in the process share it and a lock serialises
  * them.  Blocking: a call returns only after all the work it enqueued on

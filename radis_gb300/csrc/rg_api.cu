@@ -192,6 +192,7 @@ struct Work {
     int skel_R = 0;
     double skel_err = 0.0;
     std::vector<int> skel_nodes;
+    int skel_flush_ks = 0;   // the scatter flush's tensor-core section: node steps (0: none)
     int last_accum = 0;               // accumulator bits of the last scatter (0: chosen on the device)
     int64_t row_stride = 0;
     float* ldm = nullptr;             // LDM [node][row_stride] (the scatter's float values)
@@ -691,6 +692,15 @@ int scatter_shape(int n_nodes, bool wide, size_t coef_bytes, int* chunk, int* TK
     return fail(RG_ERR_RANGE, "LDM grid of %d nodes does not fit a shared-memory tile", n_nodes);
 }
 
+// Shared-memory bytes of the skeleton projection beside the scatter's tile:
+// the tensor-core flush's section (32-bit tiles, where the grid has one) or
+// the FP32 coefficients.
+size_t fuse_smem_bytes(const ProjArgs* fuse, bool wide) {
+    if (!fuse) return 0;
+    if (!wide && fuse->flush) return flush_tc_bytes(fuse->flush_ks, fuse->flush_nr);
+    return sizeof(float) * (size_t)fuse->n_nodes * fuse->rows_pad;
+}
+
 // fuse: the skeleton projection done by the scatter's flush (nullable).
 int build_scatter_args(const rg_lines* L, const Work& W, const rg_conditions* c, const SpecHost& s, bool wide,
                        const ProjArgs* fuse, ScatterArgs* a) {
@@ -713,13 +723,17 @@ int build_scatter_args(const rg_lines* L, const Work& W, const rg_conditions* c,
     a->NL = g.n_L;
     a->row_stride = W.row_stride;
     a->ldm = W.ldm;
-    size_t coef_bytes = 0;
+    const size_t coef_bytes = fuse_smem_bytes(fuse, wide);
     if (fuse) {
         a->proj_coef = fuse->coef;
         a->proj_rows = fuse->rows;
         a->proj_rp = fuse->rows_pad;
         a->n_real = fuse->n_nodes;
-        coef_bytes = sizeof(float) * (size_t)fuse->n_nodes * fuse->rows_pad;
+        if (!wide && fuse->flush) {
+            a->proj_frag = fuse->flush;
+            a->proj_ks = fuse->flush_ks;
+            a->proj_nr = fuse->flush_nr;
+        }
     }
     size_t smem_unused;
     RG(scatter_shape(s.n_nodes, wide, coef_bytes, &a->chunk, &a->TK, &a->stages, &smem_unused));
@@ -1038,6 +1052,52 @@ int skeleton_decomp(const rg_grid& g, double dv, double thresh, double tol, int 
     return interp_decomp(A.data(), S, n, tol, r_max, sk->data(), C->data(), R, err);
 }
 
+// Node order of the scatter flush's tensor-core form (steps of 8 nodes, see
+// flush_tc): tile rows have a pitch of 1 (mod 32) words, so node m sits in the
+// bank class m mod 32 = 8 ((m / 8) mod 4) + m mod 8, and the four nodes that
+// one A-fragment load reads (t = 0..3) must come from the classes v, v + 8,
+// v + 16, v + 24.  Nodes are grouped by (m mod 8, (m / 8) mod 4) into such
+// quadruples; a class short of nodes repeats one of its nodes (real = 0: a
+// zero coefficient), two quadruples make a step.  Below 32 nodes some classes
+// are empty and no order is conflict-free: the natural one, padded.
+void flush_node_order(int n, std::vector<int>* nodes, std::vector<char>* real) {
+    nodes->clear();
+    real->clear();
+    if (n < 32) {
+        for (int j = 0; j < (n + 7) / 8 * 8; ++j) {
+            nodes->push_back(j < n ? j : 0);
+            real->push_back(j < n ? 1 : 0);
+        }
+        return;
+    }
+    std::vector<int> quad_nodes;
+    std::vector<char> quad_real;
+    for (int v = 0; v < 8 && v < n; ++v) {
+        std::vector<int> cls[4];
+        for (int m = v; m < n; m += 8) cls[(m / 8) % 4].push_back(m);
+        size_t cnt = 0;
+        int any = -1;
+        for (auto& c : cls) {
+            cnt = std::max(cnt, c.size());
+            if (any < 0 && !c.empty()) any = c[0];
+        }
+        for (size_t i = 0; i < cnt; ++i)
+            for (int w = 0; w < 4; ++w) {
+                const bool have = i < cls[w].size();
+                quad_nodes.push_back(have ? cls[w][i] : !cls[w].empty() ? cls[w][0] : any);
+                quad_real.push_back(have ? 1 : 0);
+            }
+    }
+    if (quad_nodes.size() % 8) {   // odd number of quadruples: a zero one
+        for (int j = 0; j < 4; ++j) {
+            quad_nodes.push_back(quad_nodes[quad_nodes.size() - 4]);
+            quad_real.push_back(0);
+        }
+    }
+    *nodes = std::move(quad_nodes);
+    *real = std::move(quad_real);
+}
+
 bool plan_skeleton(Work& W, const SpecHost& s, const VoigtArgs& va, int r_max, VoigtArgs* vk, ProjArgs* pa,
                    double* err_out) {
     const rg_grid& g = s.grid;
@@ -1054,6 +1114,7 @@ bool plan_skeleton(Work& W, const SpecHost& s, const VoigtArgs& va, int r_max, V
         std::copy(key, key + 10, W.skel_key);
         W.skel_valid = true;
         W.skel_R = 0;   // no skeleton layout for this grid (cached as well)
+        W.skel_flush_ks = 0;
         std::vector<int> sk;
         std::vector<double> C;
         int R = 0;
@@ -1071,7 +1132,14 @@ bool plan_skeleton(Work& W, const SpecHost& s, const VoigtArgs& va, int r_max, V
         // b0, b1 = C[8 nr + g][8 ks + t], C[8 nr + g][8 ks + t + 4], g = lane / 4,
         // t = lane % 4
         const int NR = (rows + 7) / 8, KSP = 2 * ((n + 15) / 16);
-        W.proj_host.assign((size_t)n * rp + (size_t)NR * KSP * 128, 0.f);
+        // the scatter flush's tensor-core section (fused grids of up to two
+        // row blocks): B fragments [ks][nr][lane] (b0, b1 hi, b0, b1 lo) in
+        // the flush's node order, then that order as a table [ks][t][2]
+        std::vector<int> fl_nodes;
+        std::vector<char> fl_real;
+        if (n <= kFuseMaxNodes && NR <= 2) flush_node_order(n, &fl_nodes, &fl_real);
+        const int KSF = (int)fl_nodes.size() / 8;
+        W.proj_host.assign((size_t)n * rp + (size_t)NR * KSP * 128 + flush_tc_bytes(KSF, NR) / sizeof(float), 0.f);
         for (int r = 0; r < R; ++r)
             for (int node = 0; node < n; ++node) W.proj_host[(size_t)node * rp + r] = (float)C[(size_t)r * n + node];
         float* fr = W.proj_host.data() + (size_t)n * rp;
@@ -1087,6 +1155,26 @@ bool plan_skeleton(Work& W, const SpecHost& s, const VoigtArgs& va, int r_max, V
                         fr[((size_t)(nr * KSP + ks) * 2 + 1) * 64 + lane * 2 + i] = tf32_round_host(v[i] - hi);
                     }
                 }
+        float* ff = fr + (size_t)NR * KSP * 128;
+        for (int ks = 0; ks < KSF; ++ks)
+            for (int nr = 0; nr < NR; ++nr)
+                for (int lane = 0; lane < 32; ++lane) {
+                    const int g = lane >> 2, t = lane & 3;
+                    float* o = ff + ((size_t)(ks * NR + nr) * 32 + lane) * 4;
+                    for (int i = 0; i < 2; ++i) {
+                        const int j = 8 * ks + t + 4 * i;
+                        const float v = fl_real[j] ? cf(8 * nr + g, fl_nodes[j]) : 0.f;
+                        o[i] = tf32_round_host(v);
+                        o[2 + i] = tf32_round_host(v - o[i]);
+                    }
+                }
+        int32_t* tbl = reinterpret_cast<int32_t*>(ff + (size_t)KSF * NR * 128);
+        for (int ks = 0; ks < KSF; ++ks)
+            for (int t = 0; t < 4; ++t) {
+                tbl[ks * 8 + 2 * t] = fl_nodes[8 * ks + t];
+                tbl[ks * 8 + 2 * t + 1] = fl_nodes[8 * ks + t + 4];
+            }
+        W.skel_flush_ks = KSF;
         W.skel_nodes.assign(sk.begin(), sk.begin() + R);
         W.skel_R = R;
         W.skel_err = err;
@@ -1128,6 +1216,8 @@ bool plan_skeleton(Work& W, const SpecHost& s, const VoigtArgs& va, int r_max, V
     pa->rows_pad = rp;
     pa->mtiles = (rows + 7) / 8;   // the tensor-core pass's 8-row n-tiles
     pa->ksteps = 2 * ((n + 15) / 16);
+    pa->flush_ks = W.skel_flush_ks;
+    pa->flush_nr = W.skel_flush_ks ? pa->mtiles : 0;
     *err_out = err;
     return true;
 }
@@ -1151,8 +1241,7 @@ int scatter_launch_shape(const rg_lines* L, const Work& W, const rg_conditions* 
                          const ProjArgs* fuse, ScatterArgs* sa, int* grid, size_t* smem) {
     RG(build_scatter_args(L, W, c, s, wide, fuse, sa));
     int ch_unused, tk_unused, st_unused;
-    const size_t coef_bytes = fuse ? sizeof(float) * (size_t)fuse->n_nodes * fuse->rows_pad : 0;
-    RG(scatter_shape(s.n_nodes, wide, coef_bytes, &ch_unused, &tk_unused, &st_unused, smem));
+    RG(scatter_shape(s.n_nodes, wide, fuse_smem_bytes(fuse, wide), &ch_unused, &tk_unused, &st_unused, smem));
     const int sms = L->ctx->sms;
     *grid = std::max(std::min(sa->n_tiles, sms), (sa->n_tiles + kScatMaxTilesPerCta - 1) / kScatMaxTilesPerCta);
     return RG_OK;
@@ -1212,8 +1301,10 @@ int plan_layout(Work& W, const SpecHost& s, cudaStream_t st, LayoutPlan* lp) {
             W.skel_dev = true;
         }
         lp->pa.coef = W.proj_coef;
-        // the tensor-core fragments follow the [n][rp] coefficients
+        // the tensor-core fragments follow the [n][rp] coefficients, then the
+        // scatter flush's section
         lp->pa.frag = W.proj_coef + (size_t)lp->pa.n_nodes * lp->pa.rows_pad;
+        lp->pa.flush = lp->pa.flush_ks ? lp->pa.frag + (size_t)lp->pa.mtiles * lp->pa.ksteps * 128 : nullptr;
     }
     return RG_OK;
 }

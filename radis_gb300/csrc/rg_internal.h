@@ -155,6 +155,13 @@ struct ScatterArgs {
     int proj_rows;            // even; rows >= the skeleton's are zero rows
     int proj_rp;              // coefficient pitch, a multiple of 4
     int n_real;               // NG x NL (the pad node of an odd grid is not read)
+    // tensor-core form of that flush (32-bit tiles; nullable): B fragments
+    // [proj_ks][proj_nr][32] x 4 floats (b0, b1 TF32 hi, then lo), then the
+    // node table [proj_ks][8] ints (step s: node(s, t), node(s, t + 4) for
+    // t = 0..3)
+    const float* proj_frag;
+    int proj_ks;              // node steps of 8
+    int proj_nr;              // row blocks of 8 (1 or 2)
 };
 constexpr long long kScatWaitCycles = 1LL << 31;   // about one second of SM clocks
 
@@ -170,6 +177,8 @@ constexpr int kScatMaxTilesPerCta = 512;
 #endif
 constexpr int kScatMaxStages = 4;
 RG_HD inline size_t scatter_stage_bytes(int chunk) { return (size_t)33 * chunk; }
+// bytes of the tensor-core flush's fragments and node table in shared memory
+RG_HD inline size_t flush_tc_bytes(int ks, int nr) { return (size_t)ks * nr * 512 + (size_t)ks * 32; }
 // stage ring, its full and empty mbarriers (one 64-byte block) and the
 // per-tile line ranges
 RG_HD inline size_t scatter_fixed_smem(int chunk, int stages) {
@@ -281,6 +290,10 @@ struct ProjArgs {
     const float* frag;    // null: FP32 pass
     int mtiles;           // row blocks of 8 (<= 8)
     int ksteps;           // node steps of 8 in frag (a multiple of 2)
+    // the scatter flush's tensor-core section (ScatterArgs::proj_frag; null
+    // where the grid has none)
+    const float* flush;
+    int flush_ks, flush_nr;
 };
 // TF32 (10-bit mantissa) rounding to nearest even, as the host prepares the
 // tensor-core operands; x - tf32(x) is exact in FP32

@@ -528,6 +528,22 @@ __device__ __forceinline__ void issue_chunk(const ScatterArgs& a, unsigned char*
     if (a.iso) tma_load_1d(base + 32 * ch, a.iso + start, cp, bar);
 }
 
+// TF32 operands (round to nearest, ties away) and mma.sync m16n8k8 with FP32
+// accumulators: a[0..3] = A (row g, col t), (g + 8, t), (g, t + 4),
+// (g + 8, t + 4); b0, b1 = B (row t, col g), (t + 4, g); d = (g, 2t), (g, 2t
+// + 1), (g + 8, 2t), (g + 8, 2t + 1), with g = lane / 4, t = lane % 4.
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};"
+                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
 // --- per-line quantities at the conditions of a ScatterArgs -----------------
 // (shared by the scatter, the tangent scatter and the adjoint gather)
 
@@ -633,6 +649,73 @@ __device__ __forceinline__ unsigned scatter_chunk(const ScatterArgs& a, const St
     return counted;
 }
 
+// Zero `words` accumulator words from thread `i0` in steps of `step` threads,
+// 16 bytes per store (the tile starts on a 16-byte boundary).
+template <typename Acc>
+__device__ __forceinline__ void zero_tile(Acc* tile, int words, int i0, int step) {
+    const int n16 = (int)(((size_t)words * sizeof(Acc)) >> 4);
+    uint4* z = reinterpret_cast<uint4*>(tile);
+    for (int i = i0; i < n16; i += step) z[i] = make_uint4(0u, 0u, 0u, 0u);
+    for (int i = (int)(((size_t)n16 << 4) / sizeof(Acc)) + i0; i < words; i += step) tile[i] = 0;
+}
+
+// Skeleton rows of a finished 32-bit tile on the tensor cores: Y^T[columns x
+// rows] = T^T[columns x nodes] C^T[nodes x rows] with mma.sync m16n8k8 TF32,
+// each product split into three (hi hi + lo hi + hi lo; x = hi + lo, hi =
+// tf32(x), lo = tf32(x - hi)).  Warp task: 16 columns (M) x the NR row blocks
+// of 8 (N); nodes (K) eight per step in the order of the staged node table
+// offs[s][t] = (node(s, t), node(s, t + 4)) x pitch.  Tile rows have a pitch
+// of 1 (mod 32) words and the table puts the nodes of t = 0..3 in the bank
+// classes v, v + 8, v + 16, v + 24, so the A loads (column g / g + 8, node t /
+// t + 4) are conflict-free; frag[s][nr][lane] = the coefficients' B fragments
+// (b0, b1 hi, then lo), zero where the table repeats a node.
+template <int NR>
+__device__ __forceinline__ void flush_tc(const ScatterArgs& a, const unsigned* tile, const float4* frag,
+                                         const int2* offs, int k_start, int tk, float inv_fx, int cw, int ncw,
+                                         int lane) {
+    const int g = lane >> 2, t = lane & 3;
+    const int n_mt = (tk + 15) >> 4;
+    for (int mt = cw; mt < n_mt; mt += ncw) {
+        const unsigned* col = tile + (mt << 4) + g;
+        float d[NR][4];
+#pragma unroll
+        for (int nr = 0; nr < NR; ++nr)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) d[nr][i] = 0.f;
+#pragma unroll 2
+        for (int s = 0; s < a.proj_ks; ++s) {
+            const int2 o = offs[s * 4 + t];
+            const float v[4] = {__uint2float_rn(col[o.x]), __uint2float_rn(col[o.x + 8]),
+                                __uint2float_rn(col[o.y]), __uint2float_rn(col[o.y + 8])};
+            uint32_t ah[4], al[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                ah[i] = tf32_rna(v[i]);
+                al[i] = tf32_rna(v[i] - __uint_as_float(ah[i]));
+            }
+            float4 f[NR];
+#pragma unroll
+            for (int nr = 0; nr < NR; ++nr) f[nr] = frag[(s * NR + nr) * 32 + lane];
+#pragma unroll
+            for (int nr = 0; nr < NR; ++nr) mma_tf32(d[nr], ah, __float_as_uint(f[nr].x), __float_as_uint(f[nr].y));
+#pragma unroll
+            for (int nr = 0; nr < NR; ++nr) mma_tf32(d[nr], al, __float_as_uint(f[nr].x), __float_as_uint(f[nr].y));
+#pragma unroll
+            for (int nr = 0; nr < NR; ++nr) mma_tf32(d[nr], ah, __float_as_uint(f[nr].z), __float_as_uint(f[nr].w));
+        }
+        // d[nr][i]: column 16 mt + g + 8 (i / 2), row 8 nr + 2 t + i % 2
+        const int c = (mt << 4) + g;
+#pragma unroll
+        for (int nr = 0; nr < NR; ++nr)
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = 8 * nr + 2 * t + (i & 1);
+                const int cc = c + 8 * (i >> 1);
+                if (r < a.proj_rows && cc < tk) __stcs(a.ldm + (int64_t)r * a.row_stride + k_start + cc, d[nr][i] * inv_fx);
+            }
+    }
+}
+
 // Persistent, warp-specialised scatter: CTA b owns tiles b, b + G, b + 2G,
 // ...  Warp 0 (one thread) is the producer: it streams the tiles' line
 // records chunk by chunk into a ring of `stages` buffers with TMA bulk copies,
@@ -670,13 +753,26 @@ __device__ __forceinline__ void scatter_body(const ScatterArgs& a) {
         const int hi = (int)a.col_start[col_idx(k_start + tk + a.margin_cols)];
         rng[q] = make_int2(lo / kLinePad * kLinePad, hi);   // 16-line aligned start
     }
-    for (int i = threadIdx.x; i < n_words; i += blockDim.x) tile[i] = 0;
-    // skeleton layout: the projection coefficients after the tile
+    zero_tile(tile, n_words, (int)threadIdx.x, (int)blockDim.x);
+    // skeleton layout: the projection coefficients after the tile, as FP32
+    // [node][row] or (32-bit tiles) the tensor-core flush's B fragments and
+    // node table
     float* coef = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(tile) +
                                            scatter_coef_offset(n_words, sizeof(Acc)));
     const bool proj = a.proj_coef != nullptr;
-    if (proj)
+    const bool proj_tc = sizeof(Acc) == 4 && proj && a.proj_frag != nullptr;
+    const int n_frag = proj_tc ? a.proj_ks * a.proj_nr * 32 : 0;
+    const float4* frag_s = reinterpret_cast<const float4*>(coef);
+    const int2* offs_s = reinterpret_cast<const int2*>(frag_s + n_frag);
+    if (proj_tc) {
+        const float4* src = reinterpret_cast<const float4*>(a.proj_frag);
+        for (int i = threadIdx.x; i < n_frag; i += blockDim.x) reinterpret_cast<float4*>(coef)[i] = __ldg(&src[i]);
+        const int* tbl = reinterpret_cast<const int*>(src + n_frag);
+        int* offs = reinterpret_cast<int*>(reinterpret_cast<float4*>(coef) + n_frag);
+        for (int i = threadIdx.x; i < a.proj_ks * 8; i += blockDim.x) offs[i] = __ldg(&tbl[i]) * pitch;
+    } else if (proj) {
         for (int i = threadIdx.x; i < a.n_real * a.proj_rp; i += blockDim.x) coef[i] = __ldg(&a.proj_coef[i]);
+    }
     if (threadIdx.x == 0) {
         for (int b = 0; b < S; ++b) {
             mbar_init(&full[b], 1);
@@ -755,7 +851,16 @@ __device__ __forceinline__ void scatter_body(const ScatterArgs& a) {
             if (threadIdx.x == 32) atomicExch(a.err, 1u);
             return;
         }
-        if (proj) {
+        if (proj_tc) {
+            if constexpr (sizeof(Acc) == 4) {
+                if (a.proj_nr == 2)
+                    flush_tc<2>(a, tile, frag_s, offs_s, k_start, tk, inv_fx, cw, n_cons_warps, lane);
+                else
+                    flush_tc<1>(a, tile, frag_s, offs_s, k_start, tk, inv_fx, cw, n_cons_warps, lane);
+            }
+            asm volatile("bar.sync 1, %0;" ::"r"(nct) : "memory");   // every read of the tile done
+            zero_tile(tile, n_words, ct, nct);
+        } else if (proj) {
             // skeleton rows of the finished tile: warp task (64-column group,
             // block of 4 rows); lane l sums columns l and l + 32 of its group
             // (each load conflict-free across the warp) over the node rows, one
@@ -795,7 +900,7 @@ __device__ __forceinline__ void scatter_body(const ScatterArgs& a) {
                 }
             }
             asm volatile("bar.sync 1, %0;" ::"r"(nct) : "memory");   // every read of the tile done
-            for (int i = ct; i < n_words; i += nct) tile[i] = 0;
+            zero_tile(tile, n_words, ct, nct);
         } else {
             // flush the finished tile as floats, word / fx_scale (a power of
             // two: exact scaling of the rounded word), with plain stores (this
@@ -2082,17 +2187,6 @@ size_t proj_tc_smem(int row_blocks, int ksteps) {
     return sizeof(float) * ((size_t)row_blocks * ksteps * 128 + (size_t)kTcStages * kTcKC * kTcPitch);
 }
 
-__device__ __forceinline__ uint32_t tf32_rna(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return r;
-}
-__device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
-    asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-                 "{%0,%1,%2,%3};"
-                 : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
 
 template <int NR>
 __global__ void __launch_bounds__(256, 2) k_node_project_tc(const ProjArgs a) {

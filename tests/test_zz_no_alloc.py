@@ -10,8 +10,8 @@ fooled by what the first left in the shared array) and checks both spectra
 against the plan-based entry point within the parity tolerance, 1e-4 of the
 peak absorption coefficient.  One more call runs on a stream the caller
 created, and the device's free memory must be the same before and after the
-calls (after one warm-up call has resolved the array's address), which is the
-entry point's whole contract.  A spectrum too large for the array must be
+calls (after a warm-up pass has resolved the array's address and launched
+every kernel variant once), which is the entry point's whole contract.  A spectrum too large for the array must be
 refused with RG_ERR_RANGE.
 """
 import numpy as np
@@ -35,18 +35,24 @@ def test_static_scratch_matches_plan(native_lib):
     caller_stream = torch.cuda.Stream()
     conds = ((700.0, 1.0, 0.1), (1800.0, 3.0, 0.5), (1200.0, 0.5, 0.3))
     refs = [plan.synthesize_host(T, p, x) for T, p, x in conds]
-    # warm-up: resolves the array's device address and loads the kernels
-    L.synthesize_static(lines, vmin, dv, n_v, *conds[0], out.data_ptr(), **grid)
-    torch.cuda.synchronize()
-    free_before = torch.cuda.mem_get_info()[0]
-    got = []
-    for i, (T, p, x) in enumerate(conds):
-        out.fill_(-1.0)
+    def run_all():
+        got = []
+        for i, (T, p, x) in enumerate(conds):
+            out.fill_(-1.0)
+            torch.cuda.synchronize()
+            sptr = caller_stream.cuda_stream if i == 2 else None
+            info = L.synthesize_static(lines, vmin, dv, n_v, T, p, x, out.data_ptr(), stream_ptr=sptr, **grid)
+            got.append((out.cpu().numpy(), info))
         torch.cuda.synchronize()
-        sptr = caller_stream.cuda_stream if i == 2 else None
-        info = L.synthesize_static(lines, vmin, dv, n_v, T, p, x, out.data_ptr(), stream_ptr=sptr, **grid)
-        got.append((out.cpu().numpy(), info))
-    torch.cuda.synchronize()
+        return got
+
+    # warm-up: the same calls once, which resolves the array's device address
+    # and launches every kernel variant (this library's and torch's fill) a
+    # first time: the driver's first launch of a variant may reserve memory of
+    # its own (lazy module loading, spill space)
+    run_all()
+    free_before = torch.cuda.mem_get_info()[0]
+    got = run_all()
     assert torch.cuda.mem_get_info()[0] == free_before
     for (g, info), (ref, ref_info) in zip(got, refs):
         assert (info.grid.n_G, info.grid.n_L, info.grid.n_ft) == \
@@ -78,7 +84,8 @@ def test_static_skeleton_layouts(native_lib, nodes, layout):
     T, p, x = 2000.0, 1.0, 0.2
     ref, ref_info = plan.synthesize_host(T, p, x)
     out = torch.empty(n_v, dtype=torch.float32, device="cuda")
-    L.synthesize_static(lines, vmin, dv, n_v, T, p, x, out.data_ptr(), **grid)   # warm-up
+    out.fill_(-1.0)   # warm-up: torch's fill and this call's kernels launched once
+    L.synthesize_static(lines, vmin, dv, n_v, T, p, x, out.data_ptr(), **grid)
     torch.cuda.synchronize()
     free_before = torch.cuda.mem_get_info()[0]
     out.fill_(-1.0)
