@@ -532,11 +532,12 @@ __device__ __forceinline__ void issue_chunk(const ScatterArgs& a, unsigned char*
 // accumulators: a[0..3] = A (row g, col t), (g + 8, t), (g, t + 4),
 // (g + 8, t + 4); b0, b1 = B (row t, col g), (t + 4, g); d = (g, 2t), (g, 2t
 // + 1), (g + 8, 2t), (g + 8, 2t + 1), with g = lane / 4, t = lane % 4.
-__device__ __forceinline__ uint32_t tf32_rna(float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return r;
-}
+// TF32 rounding to nearest, ties away from zero (the rna mode) on the bit
+// pattern: half a TF32 unit (bit 12) added to the magnitude bits, the 13 low
+// mantissa bits cleared; a carry out of the mantissa bumps the exponent, as
+// rounding up must.  Two integer instructions; finite inputs only (the
+// operands here are sums of finite line contributions).
+__device__ __forceinline__ uint32_t tf32_rna(float x) { return (__float_as_uint(x) + 0x1000u) & 0xFFFFE000u; }
 __device__ __forceinline__ void mma_tf32(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
     asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
                  "{%0,%1,%2,%3};"
@@ -669,7 +670,7 @@ __device__ __forceinline__ void zero_tile(Acc* tile, int words, int i0, int step
 // classes v, v + 8, v + 16, v + 24, so the A loads (column g / g + 8, node t /
 // t + 4) are conflict-free; frag[s][nr][lane] = the coefficients' B fragments
 // (b0, b1 hi, then lo), zero where the table repeats a node.
-template <int NR>
+template <int NR, int U>
 __device__ __forceinline__ void flush_tc(const ScatterArgs& a, const unsigned* tile, const float4* frag,
                                          const int2* offs, int k_start, int tk, float inv_fx, int cw, int ncw,
                                          int lane) {
@@ -682,7 +683,7 @@ __device__ __forceinline__ void flush_tc(const ScatterArgs& a, const unsigned* t
         for (int nr = 0; nr < NR; ++nr)
 #pragma unroll
             for (int i = 0; i < 4; ++i) d[nr][i] = 0.f;
-#pragma unroll 2
+#pragma unroll U
         for (int s = 0; s < a.proj_ks; ++s) {
             const int2 o = offs[s * 4 + t];
             const float v[4] = {__uint2float_rn(col[o.x]), __uint2float_rn(col[o.x + 8]),
@@ -727,8 +728,9 @@ __device__ __forceinline__ void flush_tc(const ScatterArgs& a, const unsigned* t
 // warps) to flush the finished tile to HBM with plain stores.  Every wait is
 // bounded; a wait that gives up sets the error flag and the CTA stops after
 // the copies it issued have landed (bounded).  Acc: the 32- or 64-bit
-// fixed-point word of the tile.
-template <typename Acc>
+// fixed-point word of the tile.  U: unrolling of the tensor-core flush's node
+// steps (4 where registers allow, 1 in the kernel that holds both variants).
+template <typename Acc, int U = 4>
 __device__ __forceinline__ void scatter_body(const ScatterArgs& a) {
     extern __shared__ __align__(128) unsigned char smem[];
     const int ch = a.chunk;
@@ -854,9 +856,9 @@ __device__ __forceinline__ void scatter_body(const ScatterArgs& a) {
         if (proj_tc) {
             if constexpr (sizeof(Acc) == 4) {
                 if (a.proj_nr == 2)
-                    flush_tc<2>(a, tile, frag_s, offs_s, k_start, tk, inv_fx, cw, n_cons_warps, lane);
+                    flush_tc<2, U>(a, tile, frag_s, offs_s, k_start, tk, inv_fx, cw, n_cons_warps, lane);
                 else
-                    flush_tc<1>(a, tile, frag_s, offs_s, k_start, tk, inv_fx, cw, n_cons_warps, lane);
+                    flush_tc<1, U>(a, tile, frag_s, offs_s, k_start, tk, inv_fx, cw, n_cons_warps, lane);
             }
             asm volatile("bar.sync 1, %0;" ::"r"(nct) : "memory");   // every read of the tile done
             zero_tile(tile, n_words, ct, nct);
@@ -935,9 +937,9 @@ __global__ void __launch_bounds__(kScatThreads, 1) k_scatter(const ScatterArgs a
 // variant only take fewer tiles each).
 __global__ void __launch_bounds__(kScatThreads, 1) k_scatter_auto(const ScatterArgs a32, const ScatterArgs a64) {
     if (fx_wide(*a32.cmax))
-        scatter_body<unsigned long long>(a64);
+        scatter_body<unsigned long long, 1>(a64);
     else
-        scatter_body<unsigned>(a32);
+        scatter_body<unsigned, 1>(a32);
 }
 
 // ---------------------------------------------------------------------------
