@@ -663,12 +663,23 @@ int ensure_workspace(Work& W, int n_nodes, cudaStream_t st) {
 // per stage ring win (H2O 100M, 12x24 nodes: 1.35 ms vs 1.45 ms); smaller
 // chunks only when even those do not fit.
 // coef_bytes: the skeleton layout's flush coefficients (0 without).
-int scatter_shape(int n_nodes, bool wide, size_t coef_bytes, int* chunk, int* TK, int* stages, size_t* smem) {
+// Entries of the scatter's per-tile line-range table: at least the tiles of
+// any CTA, whatever tile width the shape takes (>= 32 columns), so at most
+// ceil(ceil(n_v / 32) / sms) while the grid is one CTA per SM, and never more
+// than kScatMaxTilesPerCta (more CTAs are launched past that); even.
+int scatter_rng_cap(int64_t n_v, int sms) {
+    const int64_t per = ((n_v + 31) / 32 + std::max(sms, 1) - 1) / std::max(sms, 1);
+    const int cap = (int)std::min<int64_t>(kScatMaxTilesPerCta, std::max<int64_t>(per, 1));
+    return (cap + 1) & ~1;
+}
+
+int scatter_shape(int n_nodes, bool wide, size_t coef_bytes, int rng_cap, int* chunk, int* TK, int* stages,
+                  size_t* smem) {
     size_t avail = 0;
     RG(scatter_smem_optin(&avail, wide));
     const size_t word = wide ? 8 : 4;   // bytes per tile cell
     auto tile_cols = [&](int S, int ch) {   // widest tile next to the ring (rows of tk + 1 words)
-        const size_t fixed = scatter_fixed_smem(ch, S) + coef_bytes + 16;
+        const size_t fixed = scatter_fixed_smem(ch, S, rng_cap) + coef_bytes + 16;
         if (fixed >= avail) return 0;
         return std::min(1024, ((int)((avail - fixed) / (word * (size_t)n_nodes)) - 1) / 32 * 32);
     };
@@ -676,14 +687,15 @@ int scatter_shape(int n_nodes, bool wide, size_t coef_bytes, int* chunk, int* TK
         *chunk = ch;
         *TK = tk;
         *stages = S;
-        *smem = scatter_fixed_smem(ch, S) + scatter_coef_offset((size_t)n_nodes * (tk + 1), word) + coef_bytes;
+        *smem = scatter_fixed_smem(ch, S, rng_cap) + scatter_coef_offset((size_t)n_nodes * (tk + 1), word) +
+                coef_bytes;
         return RG_OK;
     };
     // GB300 sweeps (CO2 5M / 128 nodes, H2O 100M / 288 nodes): one line per
     // consumer thread per chunk (992 = 31 warps) in three stages while the tile
     // keeps >= 192 columns (CO2 5M: 256 columns, or 224 beside the skeleton
-    // coefficients, where three stages beat two 1536-line ones by 2%); else two
-    // 1536-line stages (wider tiles than 2048)
+    // projection's 17 KB of tensor-core fragments, where three stages beat two
+    // 1536-line ones by 2%); else two 1536-line stages (wider tiles than 2048)
     if (tile_cols(3, 992) >= 192) return take(3, 992, tile_cols(3, 992));
     if (tile_cols(2, 1536) >= 64) return take(2, 1536, tile_cols(2, 1536));
     for (int min_tk : {64, 32})
@@ -736,7 +748,8 @@ int build_scatter_args(const rg_lines* L, const Work& W, const rg_conditions* c,
         }
     }
     size_t smem_unused;
-    RG(scatter_shape(s.n_nodes, wide, coef_bytes, &a->chunk, &a->TK, &a->stages, &smem_unused));
+    a->rng_cap = scatter_rng_cap(W.desc.n_v, L->ctx->sms);
+    RG(scatter_shape(s.n_nodes, wide, coef_bytes, a->rng_cap, &a->chunk, &a->TK, &a->stages, &smem_unused));
     a->n_tiles = (int)((W.desc.n_v + a->TK - 1) / a->TK);
     a->cmax = W.cmax_dev;
     a->err = W.err;
@@ -1241,9 +1254,12 @@ int scatter_launch_shape(const rg_lines* L, const Work& W, const rg_conditions* 
                          const ProjArgs* fuse, ScatterArgs* sa, int* grid, size_t* smem) {
     RG(build_scatter_args(L, W, c, s, wide, fuse, sa));
     int ch_unused, tk_unused, st_unused;
-    RG(scatter_shape(s.n_nodes, wide, fuse_smem_bytes(fuse, wide), &ch_unused, &tk_unused, &st_unused, smem));
+    RG(scatter_shape(s.n_nodes, wide, fuse_smem_bytes(fuse, wide), sa->rng_cap, &ch_unused, &tk_unused, &st_unused,
+                     smem));
     const int sms = L->ctx->sms;
     *grid = std::max(std::min(sa->n_tiles, sms), (sa->n_tiles + kScatMaxTilesPerCta - 1) / kScatMaxTilesPerCta);
+    if ((sa->n_tiles + *grid - 1) / *grid > sa->rng_cap)
+        return fail(RG_ERR_RANGE, "scatter tiles per CTA above the line-range table");
     return RG_OK;
 }
 

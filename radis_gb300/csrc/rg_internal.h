@@ -162,6 +162,7 @@ struct ScatterArgs {
     const float* proj_frag;
     int proj_ks;              // node steps of 8
     int proj_nr;              // row blocks of 8 (1 or 2)
+    int rng_cap;              // entries of the per-tile line-range table (>= tiles per CTA, even)
 };
 constexpr long long kScatWaitCycles = 1LL << 31;   // about one second of SM clocks
 
@@ -180,9 +181,10 @@ RG_HD inline size_t scatter_stage_bytes(int chunk) { return (size_t)33 * chunk; 
 // bytes of the tensor-core flush's fragments and node table in shared memory
 RG_HD inline size_t flush_tc_bytes(int ks, int nr) { return (size_t)ks * nr * 512 + (size_t)ks * 32; }
 // stage ring, its full and empty mbarriers (one 64-byte block) and the
-// per-tile line ranges
-RG_HD inline size_t scatter_fixed_smem(int chunk, int stages) {
-    return stages * scatter_stage_bytes(chunk) + 16 * kScatMaxStages + 8 * kScatMaxTilesPerCta;
+// per-tile line ranges (rng_cap entries of 8 bytes, rng_cap even: the tile
+// after them starts on a 16-byte boundary)
+RG_HD inline size_t scatter_fixed_smem(int chunk, int stages, int rng_cap) {
+    return stages * scatter_stage_bytes(chunk) + 16 * kScatMaxStages + 8 * (size_t)rng_cap;
 }
 // byte offset of the flush coefficients (skeleton layout) after a tile of
 // `words` accumulator words of `word` bytes

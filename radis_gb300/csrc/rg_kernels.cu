@@ -739,14 +739,18 @@ __device__ __forceinline__ void scatter_body(const ScatterArgs& a) {
     uint64_t* full = reinterpret_cast<uint64_t*>(smem + S * sb);
     uint64_t* empty = full + kScatMaxStages;
     int2* rng = reinterpret_cast<int2*>(smem + S * sb + 16 * kScatMaxStages);
-    Acc* tile = reinterpret_cast<Acc*>(smem + scatter_fixed_smem(ch, S));
+    Acc* tile = reinterpret_cast<Acc*>(smem + scatter_fixed_smem(ch, S, a.rng_cap));
     const int pitch = a.TK + 1;
     const int G = gridDim.x;
-    const int nq = (a.n_tiles - (int)blockIdx.x + G - 1) / G;   // tiles of this CTA (<= kScatMaxTilesPerCta)
+    const int nq = (a.n_tiles - (int)blockIdx.x + G - 1) / G;   // tiles of this CTA (<= a.rng_cap)
     const int n_words = a.n_nodes * pitch;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n_cons_warps = (blockDim.x >> 5) - 1;
 
+    if (nq > a.rng_cap) {   // the host sizes the table for every CTA: never taken
+        if (threadIdx.x == 0) atomicExch(a.err, 1u);
+        return;
+    }
     auto col_idx = [&](int c) { return max(0, min(c + a.col_off, a.col_count - 1)); };
     for (int q = threadIdx.x; q < nq; q += blockDim.x) {
         const int k_start = ((int)blockIdx.x + q * G) * a.TK;
