@@ -173,6 +173,33 @@ def test_skeleton_projection_paths(ctx, case, accumulator, fused):
     assert rel_err(gpu, oracle(lines, *args, info)) <= TOL
 
 
+@pytest.mark.parametrize("nodes,tol,form", [((8, 16), 1e-5, "tensor cores, one row block"),
+                                             ((8, 16), 1e-8, "tensor cores, two row blocks"),
+                                             ((4, 6), 1e-8, "tensor cores, natural node order"),
+                                             ((8, 16), 1e-13, "FP32")])
+def test_flush_projection_forms(ctx, nodes, tol, form):
+    """The scatter's flush projects a 32-bit tile on the tensor cores for up
+    to 16 skeleton rows (one or two row blocks of 8; from 32 nodes up in the
+    bank-conflict-free node order, which repeats nodes with zero
+    coefficients where a bank class runs short, below 32 in the natural
+    order) and on FP32 FMAs for more rows: each form against the oracle."""
+    make, args, _ = LAYOUT_CASES["co2_8x16"]
+    lines = make()
+    grid = dict(n_G=nodes[0], n_L=nodes[1])
+    gpu, info = run_gpu(ctx, lines, *args, layout=3, layout_tol=tol, accumulator=32, **grid)
+    assert info.layout == 4 and info.accum_bits == 32 and info.layout_err <= tol
+    n = info.grid.n_G * info.grid.n_L
+    if form == "FP32":
+        assert info.fft_rows > 16
+    elif "one row block" in form:
+        assert info.fft_rows <= 8 and n >= 32
+    elif "two row blocks" in form:
+        assert 8 < info.fft_rows <= 16 and n >= 32
+    else:
+        assert info.fft_rows <= 16 and n < 32
+    assert rel_err(gpu, oracle(lines, *args, info)) <= TOL
+
+
 def test_skeleton_tolerance_trades_rows_for_error(ctx):
     """A looser decomposition bound (layout_tol) transforms fewer skeleton
     rows; the spectrum moves by about the bound and stays within the parity
