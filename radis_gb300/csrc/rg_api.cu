@@ -654,15 +654,6 @@ int ensure_workspace(Work& W, int n_nodes, cudaStream_t st) {
     return RG_OK;
 }
 
-// Shape of the persistent scatter (one 1024-thread CTA per SM): TMA ring
-// stages, chunk (lines) and tile width (columns, a multiple of 32 for the bank
-// swizzle).  Measured on GB300 (warp-specialised kernel): a three-stage ring
-// of 512-line chunks wins while it leaves tiles of >= 256 columns (few nodes:
-// CO2 5M, 8x16 nodes: 0.14 ms vs 0.19 ms with 2 x 2048 lines and 160
-// columns); with wide node grids the tile narrows and two 2048-line chunks
-// per stage ring win (H2O 100M, 12x24 nodes: 1.35 ms vs 1.45 ms); smaller
-// chunks only when even those do not fit.
-// coef_bytes: the skeleton layout's flush coefficients (0 without).
 // Entries of the scatter's per-tile line-range table: at least the tiles of
 // any CTA, whatever tile width the shape takes (>= 32 columns), so at most
 // ceil(ceil(n_v / 32) / sms) while the grid is one CTA per SM, and never more
@@ -673,6 +664,10 @@ int scatter_rng_cap(int64_t n_v, int sms) {
     return (cap + 1) & ~1;
 }
 
+// Shape of the persistent scatter (one 1024-thread CTA per SM): TMA ring
+// stages, chunk (lines) and tile width (columns, a multiple of 32 for the bank
+// swizzle), the widest tile that fits beside the ring, the line-range table
+// (rng_cap entries) and coef_bytes of skeleton projection data (0 without).
 int scatter_shape(int n_nodes, bool wide, size_t coef_bytes, int rng_cap, int* chunk, int* TK, int* stages,
                   size_t* smem) {
     size_t avail = 0;
