@@ -303,6 +303,13 @@ int rg_slit_convolve(rg_ctx* ctx, const float* in_dev, int64_t n, const float* s
  * wait for copies already in flight always keeps the default bound. */
 int rg_plan_test_scatter_stall(rg_plan* plan, int32_t withhold, int64_t wait_cycles);
 
+/* Test hook, host-only, no counterpart in the reference: the node order in
+ * which the scatter's flush projects a tile of n_nodes node rows on the tensor
+ * cores (steps of 8 nodes: nodes[8 s + j]; real[8 s + j] = 0 where a node is
+ * repeated with a zero coefficient).  *count = 8 x steps; RG_ERR_RANGE when
+ * capacity is smaller. */
+int rg_test_flush_order(int32_t n_nodes, int32_t* nodes, uint8_t* real, int32_t capacity, int32_t* count);
+
 /* Sums (ms) of the stage times recorded with timing = 2 since the last call:
  * scatter, fft-col, fft-row+voigt, ifft-row, ifft-col, total; *count =
  * spectra recorded.  Synchronises the recording stream and empties the ring.

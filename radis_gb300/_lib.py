@@ -28,6 +28,7 @@ EXPORTS = [
     "rg_synthesize_static", "rg_backward", "rg_jvp", "rg_synthesize_quantities",
     "rg_synthesize_quantities_host", "rg_slit_convolve",
     "rg_lines_set_partition", "rg_partition_eval", "rg_plan_stage_times_gauss", "rg_plan_test_scatter_stall",
+    "rg_test_flush_order",
     "rg_hitran_count", "rg_hitran_parse",
 ]
 
@@ -135,6 +136,7 @@ def load(path: str | None = None):
         "rg_plan_stage_times": ([vp, C.POINTER(C.c_double), C.POINTER(i64)], C.c_int),
         "rg_plan_stage_times_gauss": ([vp, C.POINTER(C.c_double)], C.c_int),
         "rg_plan_test_scatter_stall": ([vp, C.c_int32, i64], C.c_int),
+        "rg_test_flush_order": ([C.c_int32, vp, vp, C.c_int32, C.POINTER(C.c_int32)], C.c_int),
         "rg_debug_ldm": ([vp, C.POINTER(Conditions), vp, i64, C.POINTER(SpectrumInfo)], C.c_int),
         "rg_server_create": ([vp, C.c_int, i64, C.POINTER(vp)], C.c_int),
         "rg_server_submit": ([vp, C.POINTER(Request), C.POINTER(i64)], C.c_int),
@@ -558,6 +560,18 @@ def grid_skeleton(grid: Grid, dv: float, folding_thresh: float = 1e-6, tol: floa
     check(load().rg_grid_skeleton(C.byref(grid), float(dv), float(folding_thresh), float(tol), r_max,
                                   C.byref(R), nodes.ctypes.data, coef.ctypes.data, C.byref(err)))
     return nodes[:R.value].copy(), coef[:R.value].copy(), err.value
+
+
+def flush_order(n_nodes: int):
+    """Host-only test hook (rg_test_flush_order): the node order in which the
+    scatter's flush projects a tile on the tensor cores, as (nodes int32[8 S],
+    real bool[8 S]) for S steps of 8 nodes."""
+    cap = 8 * ((int(n_nodes) + 7) // 8 + 64)
+    nodes = np.zeros(cap, np.int32)
+    real = np.zeros(cap, np.uint8)
+    cnt = C.c_int32()
+    check(load().rg_test_flush_order(int(n_nodes), nodes.ctypes.data, real.ctypes.data, cap, C.byref(cnt)))
+    return nodes[:cnt.value].copy(), real[:cnt.value].astype(bool)
 
 
 class Server:

@@ -2222,6 +2222,22 @@ int rg_plan_test_scatter_stall(rg_plan* P, int32_t withhold, int64_t wait_cycles
     return RG_OK;
 }
 
+int rg_test_flush_order(int32_t n_nodes, int32_t* nodes, uint8_t* real, int32_t capacity, int32_t* count) {
+    g_err.clear();
+    if (!nodes || !real || !count) return fail(RG_ERR_ARG, "NULL argument");
+    if (n_nodes < 1 || n_nodes > kMaxNodes) return fail(RG_ERR_RANGE, "n_nodes %d outside 1..%d", n_nodes, kMaxNodes);
+    std::vector<int> nd;
+    std::vector<char> re;
+    flush_node_order(n_nodes, &nd, &re);
+    *count = (int32_t)nd.size();
+    if ((int64_t)nd.size() > capacity) return fail(RG_ERR_RANGE, "capacity %d < %d", capacity, (int)nd.size());
+    for (size_t i = 0; i < nd.size(); ++i) {
+        nodes[i] = nd[i];
+        real[i] = re[i] ? 1 : 0;
+    }
+    return RG_OK;
+}
+
 int rg_plan_stage_times(rg_plan* P, double* sum_ms, int64_t* count) {
     g_err.clear();
     if (!valid(P) || !sum_ms || !count) return fail(RG_ERR_ARG, "invalid argument");

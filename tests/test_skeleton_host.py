@@ -92,3 +92,29 @@ def test_projected_rows_give_the_reference_spectrum(native_lib):
     Y[:, :n_v] = coef @ rows
     out = sfft.irfft((sfft.rfft(Y, axis=1) * V[nodes]).sum(0), n=n_ft)[:n_v] / dv
     assert np.max(np.abs(out - ref)) <= 1e-7 * np.max(np.abs(ref))
+
+
+def test_flush_node_order_covers_and_spreads_banks(native_lib):
+    """The scatter's tensor-core flush reads a tile's node rows in the order
+    of rg_test_flush_order, eight nodes per step: every node appears once
+    with its coefficient (repeats carry zero coefficients), and from 32 nodes
+    up each A-fragment load (nodes of t = 0..3, or t + 4, at columns g = 0..7
+    of a row pitch of 1 mod 32 words) touches 32 distinct banks.  Below 32
+    nodes the natural order, padded to a step."""
+    for n in range(1, 161):
+        nodes, real = L.flush_order(n)
+        assert len(nodes) % 8 == 0 and np.all((nodes >= 0) & (nodes < n)), n
+        assert sorted(nodes[real].tolist()) == list(range(n)), n
+        steps = len(nodes) // 8
+        if n < 32:
+            assert steps == (n + 7) // 8 and np.array_equal(nodes[real], np.arange(n)), n
+            continue
+        assert steps <= (n + 7) // 8 + 4, n
+        if n % 32 == 0:
+            assert steps == n // 8 and real.all(), n
+        for pitch in (33, 225, 257, 1025):   # TK + 1, TK a multiple of 32
+            for s in range(steps):
+                for half in (0, 1):
+                    banks = {(int(nodes[8 * s + t + 4 * half]) * pitch + g) % 32 for t in range(4) for g in range(8)}
+                    assert len(banks) == 32, (n, pitch, s, half)
+
