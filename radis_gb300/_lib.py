@@ -365,6 +365,8 @@ class Plan:
         return self._h
 
     def _cond(self, T, p_bar, x, q_ratio):
+        if q_ratio is None:
+            return Conditions(float(T), float(p_bar), float(x), None), None
         q = None
         if q_ratio is not None:
             q = np.ascontiguousarray(np.broadcast_to(np.asarray(q_ratio, np.float64),
@@ -383,9 +385,13 @@ class Plan:
         c, _q = self._cond(T, p_bar, x, q_ratio)
         if out is None:
             out = np.empty(self.n_v, dtype=np.float32)
+        elif out.dtype != np.float32 or not out.flags.c_contiguous or out.size < self.n_v:
+            raise ValueError(f"out must be a C-contiguous float32 array of >= {self.n_v} values")
         info = SpectrumInfo()
-        check(load().rg_synthesize_host(self.handle, C.byref(c), ptr(out), None, 1 if timing else 0,
-                                        C.byref(info)))
+        rc = load().rg_synthesize_host(self.handle, C.byref(c), out.ctypes.data, None, 1 if timing else 0,
+                                       C.byref(info))
+        if rc != RG_OK:
+            check(rc)
         return out, info
 
     def synthesize_device(self, T, p_bar, x, out_dev_ptr: int, stream_ptr: int | None = None,
