@@ -995,8 +995,11 @@ int NL_merged(const GaussArgs& ga) { return ga.NLv; }
 // coefficients [n_nodes][rows_pad] in W.proj_host.
 // Skeleton projection in the scatter's flush (no LDM round trip through HBM)
 // for grids of at most this many nodes; larger grids project in a separate
-// pass (the flush's FMAs would stall the scatter longer than the round trip
-// costs), with the decomposition computed on the host while the scatter runs.
+// pass, with the decomposition computed on the host while the scatter runs.
+// Measured on the 288-node H2O 100M grid, also with a tensor-core flush of
+// three row blocks: its fragments leave 64-column tiles (4 flush tasks for 31
+// warps) and the fused scatter took 1.91 ms against 1.13 + 0.41 ms for the
+// scatter and the pass.
 constexpr int kFuseMaxNodes = 160;
 
 constexpr int kSkelSamples = 32;
