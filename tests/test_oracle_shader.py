@@ -10,8 +10,8 @@ cmdApplyLineshapes.comp, FP32 as the shaders run and FP64), CPU only.
   CO-like case (200 001 points at 0.002 cm-1): the reference GPU design does
   not meet 1e-4 there.  The error shrinks as the lines move to lower
   wavenumbers (FP32 v0 rounding) down to a floor set by the FP32 grid index
-  (ulp 1/64 of a step at index 2e5); this build computes both in
-  double-float.
+  (ulp 1/64 of a step at index 2e5); this library's scatter computes both
+  in double-float.
 """
 import numpy as np
 import pytest
